@@ -1,0 +1,213 @@
+/*
+ * epspectral_gb300.h -- C ABI of the GB300 scGD0 / ladder library (libepspectral_gb300.so).
+ *
+ * The library replaces the bodies of the two iteration loops of EPSpectral.jl:
+ *   _loop_scgd0(setup, occ; eta_min, eta_init, maxiter, tol, backend, gpu_tile, Sigma_init,
+ *               fix_mu, omega_acoustic, verbosity)                 src/scgd0.jl:189-346
+ *   _loop_ladder(ladder, Sigma, mu, Tlist, Omegas; solver, rtol, maxiter, store_vertex,
+ *                backend, gpu_tile, omega_acoustic, verbosity)     src/ladder.jl:303-379
+ * and the single operator application apply_ladder_kernel! (src/ladder.jl:245-296) that the
+ * reference's tests drive on its own.
+ *
+ * Conventions (every entry point):
+ *  - Arrays are column-major in the reference's index order (the first index varies fastest), so a
+ *    Julia caller passes pointer(A) with no copy. Complex arrays are interleaved (re, im) doubles,
+ *    the memory layout of Julia's ComplexF64.
+ *  - Index arrays (iq_kk, iks_i, iks_f, f_to_i, multiplet lists) are int32 and 0-based.
+ *  - Inputs are caller-owned and read only during the call; outputs are caller-allocated. A plan
+ *    owns all device memory it uses. No C++ exception crosses the ABI.
+ *  - A context is bound to one CUDA device and one stream; it is not thread-safe. Every call is
+ *    synchronous on return.
+ *  - Every call returns an epsp_status; on failure epsp_last_error(ctx) holds a message.
+ */
+#ifndef EPSPECTRAL_GB300_H
+#define EPSPECTRAL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EPSP_ABI_VERSION 1
+
+/* Status codes. The Julia shim maps EINVAL and ENOROOT_MU to ArgumentError, as the reference
+ * throws (src/scgd0.jl:81-113, src/scgd0.jl:316-322, src/ladder.jl:71-80). */
+typedef enum epsp_status {
+  EPSP_OK = 0,
+  EPSP_EINVAL = 1,            /* an argument is out of range */
+  EPSP_ENOMEM = 2,            /* a device or host allocation failed */
+  EPSP_ENOROOT_MU = 3,        /* no chemical potential in the bracket (src/scgd0.jl:316-322) */
+  EPSP_ENOTCONV = 4,          /* reserved: non-convergence is reported through flags, not status */
+  EPSP_EDEVICE_TIMEOUT = 5,   /* a bounded device-side wait ran out */
+  EPSP_ECUDA = 6,             /* a CUDA runtime call failed */
+  EPSP_EUNSUPPORTED = 7       /* the requested path does not apply to these inputs */
+} epsp_status;
+
+/* Storage type of g2 (the reference's g2 is Array{FT,3}; the benchmark configurations store it as
+ * FP32 or BF16). */
+enum { EPSP_F64 = 0, EPSP_F32 = 1, EPSP_BF16 = 2 };
+
+/* occ.type of ElectronOccupationParams (src/scgd0.jl:85-86, 312). */
+enum { EPSP_METAL = 0, EPSP_SEMICONDUCTOR = 1 };
+
+/* Computation path of a plan.
+ *  DIRECT_FP64 : the reference's element sum, term by term in FP64 (src/scgd0_kernel.jl:27-86) and
+ *                the shift-grid coupling of the ladder (src/ladder_kernel.jl:195-288); any phonon
+ *                dispersion. This is the parity path.
+ *  GEMM_FP64   : dispersionless modes only: the Fan-Migdal sum recast as a kernel tensor times a
+ *                coupling matrix, the ladder's shift sums regrouped per mode; FP64 arithmetic.
+ *  GEMM_BF16X3 : as GEMM_FP64, with the contractions on the tcgen05 tensor cores in BF16 hi/lo
+ *                split precision (three products, FP32 accumulation); the chemical-potential
+ *                bisection, the carrier integral and the GMRES orthogonalisation stay FP64. */
+enum { EPSP_PATH_DIRECT_FP64 = 0, EPSP_PATH_GEMM_FP64 = 1, EPSP_PATH_GEMM_BF16X3 = 2 };
+
+/* Ladder solver (src/ladder.jl:340-369). */
+enum { EPSP_SOLVER_GMRES = 0, EPSP_SOLVER_FIXED_POINT = 1 };
+
+/* A FrequencyGrid (src/frequency_grids.jl:119-133): nodes origin + offsets[j] * unit, offsets
+ * strictly increasing, n >= 2. */
+typedef struct epsp_grid {
+  double origin;
+  double unit;
+  const int64_t* offsets;  /* [n] */
+  int64_t n;
+} epsp_grid;
+
+/* The iteration-invariant inputs: the fields of the reference's `setup` NamedTuple
+ * (src/scgd0.jl:173-183) plus the ladder's additions (src/ladder.jl:153-157). */
+typedef struct epsp_model {
+  int64_t nm, ni, nf;        /* modes, outer (irreducible) states, inner (full-BZ) states */
+  int32_t g2_dtype;          /* EPSP_F64 / EPSP_F32 / EPSP_BF16 */
+  int32_t reserved0;
+  const void* g2;            /* [nm, ni, nf] */
+  int64_t nq;
+  const double* omega_ph;    /* [nm, nq] phonon frequencies */
+  int64_t nk_i, nk_f;
+  const int32_t* iq_kk;      /* [nk_i, nk_f] q index of a (k_i, k_f) pair */
+  const int32_t* iks_i;      /* [ni] k index of each outer state */
+  const int32_t* iks_f;      /* [nf] k index of each inner state */
+  const double* eps_i;       /* [ni] */
+  const double* w_i;         /* [ni] state weights */
+  const double* eps_f;       /* [nf] */
+  const double* w_f;         /* [nf] */
+  const int32_t* f_to_i;     /* [nf] IBZ representative of each inner state */
+  int64_t nmult;             /* degenerate multiplets, CSR: members of multiplet m are */
+  const int32_t* mult_ptr;   /*   mult_idx[mult_ptr[m] .. mult_ptr[m+1]-1]   ([nmult+1]) */
+  const int32_t* mult_idx;
+  epsp_grid omegas;          /* output grid ωs */
+  epsp_grid omegas_spectral; /* spectral grid ωs_spectral */
+  double W;                  /* sum(w_i) */
+  double nstates_base;
+  const double* R;           /* [3, 3, nf] vertex rotation of each inner state (ladder only) */
+  const double* v;           /* [3, ni] band velocities (ladder only) */
+} epsp_model;
+
+/* Plan options: the keywords of the reference loops that shape the setup. */
+typedef struct epsp_options {
+  int32_t path;              /* EPSP_PATH_* */
+  int32_t verbosity;
+  int64_t gpu_tile;          /* 0 = `nothing`; > 0 = inner states per chunk, g2 streamed */
+  double omega_acoustic;     /* modes below it are skipped */
+} epsp_options;
+
+/* ElectronOccupationParams fields the loop reads. */
+typedef struct epsp_occ {
+  int64_t nT;
+  const double* Tlist;       /* [nT] */
+  const double* nlist;       /* [nT] doping */
+  double nelec;
+  double spin_degeneracy;
+  int32_t type;              /* EPSP_METAL / EPSP_SEMICONDUCTOR */
+  int32_t reserved0;
+} epsp_occ;
+
+/* `history` of SCGD0Result (src/scgd0.jl:21-23): arrays [nT, maxiter] column-major; entries of
+ * iterations a temperature did not run are NaN. niter is the number of iterations run. */
+typedef struct epsp_scgd0_history {
+  double* err;
+  double* mu;
+  double* min_spectral_weight;
+  double* wall;              /* [maxiter] seconds */
+  int32_t* iter_frozen;      /* [nT] iteration at which T converged, 0 if it did not */
+  int32_t niter;
+  int32_t reserved0;
+} epsp_scgd0_history;
+
+/* Ladder history (src/ladder.jl:20-23): GMRES residual norms per (Ω, T), at most maxiter + 1 each,
+ * in norms[(maxiter+1) * (iΩ + nΩ iT) + k], their counts in nnorms; fixed-point σ after each
+ * iteration in sigma_iter[9 * (maxiter * (iΩ + nΩ iT) + k) + (a + 3b)], their counts in nsigma. */
+typedef struct epsp_ladder_history {
+  double* norms;
+  int32_t* nnorms;
+  double* sigma_iter;
+  int32_t* nsigma;
+} epsp_ladder_history;
+
+typedef struct epsp_ctx epsp_ctx;
+typedef struct epsp_scgd0_plan epsp_scgd0_plan;
+typedef struct epsp_ladder_plan epsp_ladder_plan;
+
+/* ---- context ---- */
+
+/* Binds a context to CUDA device `device`, with its own stream. Replaces the reference's backend
+ * object (ElectronPhonon gpu_backend(), used at src/scgd0.jl:189 and src/ladder.jl:303). */
+epsp_status epsp_create(epsp_ctx** ctx, int32_t device);
+void epsp_destroy(epsp_ctx* ctx);
+/* The message of the last failed call on ctx ("" if none). Valid until the next call. */
+const char* epsp_last_error(const epsp_ctx* ctx);
+/* Number of kernels this context launched since creation (for launch accounting). */
+int64_t epsp_kernel_launches(const epsp_ctx* ctx);
+
+/* ---- scGD0 ---- */
+
+/* Uploads the iteration-invariant tables of `model` (the `setup` of src/scgd0.jl:127-184 and the
+ * buffers of src/scgd0.jl:199-245). Replaces the setup half of _loop_scgd0. */
+epsp_status epsp_scgd0_setup(epsp_ctx* ctx, const epsp_model* model, const epsp_options* opts,
+                             epsp_scgd0_plan** plan);
+void epsp_scgd0_plan_destroy(epsp_scgd0_plan* plan);
+
+/* The scGD0 iteration: the body of _loop_scgd0 (src/scgd0.jl:246-346). sigma_init is NULL for
+ * the start -i*eta_init, else [nω, ni, nT] complex. mu_start [nT] is the starting μ (occ.μlist or
+ * the bare-band μ). Outputs: sigma_out [nω, ni, nT] complex, mu_out [nT], converged [nT], hist. */
+epsp_status epsp_scgd0_run(epsp_scgd0_plan* plan, const epsp_occ* occ, const double* eta_min,
+                           double eta_init, int32_t maxiter, double tol, int32_t fix_mu,
+                           const double* mu_start, const double* sigma_init, double* sigma_out,
+                           double* mu_out, uint8_t* converged, epsp_scgd0_history* hist);
+
+/* One Fan-Migdal sum at one temperature: imsigma [nω, ni] += Σ_{νf} term, with sigma_in [nω, ni]
+ * complex the clamped input self-energy. add_fan_migdal_imsigma! (src/scgd0_kernel.jl:59-72). */
+epsp_status epsp_scgd0_imsigma(epsp_scgd0_plan* plan, const double* sigma_in, double mu, double T,
+                               double* imsigma);
+
+/* ---- ladder ---- */
+
+/* Uploads the ladder tables: the scGD0 tables plus R, v, the stars of f_to_i, the hat-basis shift
+ * tables and the trapezoid weights of ωs (_setup_ladder, src/ladder.jl:112-158, and
+ * _ladder_workspace, src/ladder.jl:174-233). */
+epsp_status epsp_ladder_setup(epsp_ctx* ctx, const epsp_model* model, const epsp_options* opts,
+                              epsp_ladder_plan** plan);
+void epsp_ladder_plan_destroy(epsp_ladder_plan* plan);
+
+/* The (T, Ω) loops of _loop_ladder (src/ladder.jl:327-375). sigma [nω, ni, nT] complex, mu [nT],
+ * Tlist [nT], Omegas [nΩ]. Outputs (unsymmetrized, without spin_degeneracy / volume):
+ * sigma_bubble, sigma_ladder [3, 3, nΩ, nT]; converged [nΩ, nT]; niter [nΩ, nT]; hist (may be
+ * NULL); J_out [nω, 4, 3, 2, ni, nΩ, nT] complex or NULL (store_vertex = false). */
+epsp_status epsp_ladder_run(epsp_ladder_plan* plan, const double* sigma, const double* mu,
+                            const double* Tlist, int64_t nT, const double* Omegas, int64_t nOmega,
+                            int32_t solver, double rtol, int32_t maxiter, double* sigma_bubble,
+                            double* sigma_ladder, uint8_t* converged, int32_t* niter,
+                            epsp_ladder_history* hist, double* J_out);
+
+/* One application LJ = L(J) of the ladder kernel at temperature T, chemical potential mu and
+ * probe frequency Omega, with sigma_T [nω, ni] complex the self-energy of that temperature:
+ * apply_ladder_kernel! (src/ladder.jl:245-296) with the propagators of contour_greens!
+ * (src/ladder_kernel.jl:51-57). J, LJ: [nω, 4, 3, 2, ni] complex. */
+epsp_status epsp_ladder_apply(epsp_ladder_plan* plan, const double* sigma_T, double mu, double T,
+                              double Omega, const double* J, double* LJ);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EPSPECTRAL_GB300_H */
