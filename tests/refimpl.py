@@ -150,9 +150,26 @@ def propagators(ws, sigma_T, eps_i, mu, T, Omega):
     return Gm, Gp
 
 
+def hat_matrix(ws, q):
+    """S with (S y)[j] = hat_value(y, ws, ws[j] + q): linear interpolation at ωs[j] + q, zero
+    outside the grid (test/test_ladder_kernel.jl:68-73)."""
+    nw = len(ws)
+    S = np.zeros((nw, nw))
+    for j in range(nw):
+        x = ws[j] + q
+        if x < ws[0] or x > ws[-1]:
+            continue
+        k = min(int(np.searchsorted(ws, x, side="right")) - 1, nw - 2)
+        t = (x - ws[k]) / (ws[k + 1] - ws[k])
+        S[j, k] += 1 - t
+        S[j, k + 1] += t
+    return S
+
+
 def naive_apply_ladder(setup, J, Gm, Gp, T, w_ac):
-    """L(J) = -Gm (s ⊙ K[J]) Gp by loops (test/test_ladder_kernel.jl:76-116), exact hat-basis
-    shifts at ωs[j] ± ωq, no shift grid."""
+    """L(J) = -Gm (s ⊙ K[J]) Gp by loops over (i, f, ν) (test/test_ladder_kernel.jl:76-116), with the
+    vertex shifted by exact hat-basis interpolation at ωs[j] ± ωq and no shift grid. Terms with the
+    same ωq share one interpolation matrix (a regrouping of the same sum)."""
     g2 = np.asarray(setup["g2"], dtype=np.float64)
     nm, ni, nf = g2.shape
     ws = setup["omegas"].nodes()
@@ -162,8 +179,12 @@ def naive_apply_ladder(setup, J, Gm, Gp, T, w_ac):
     F = np.zeros((nw, 4, 3, 2, nf), dtype=complex)
     for f in range(nf):
         F[:, :, :, :, f] = np.einsum("ab,wcbd->wcad", R[:, :, f], J[:, :, :, :, f_to_i[f]])
-    Up, Um, Vp, Vm = (np.zeros((nw, 4, 3, 2, ni), dtype=complex) for _ in range(4))
+    Ff = F.reshape(nw, 24, nf, order="F")
+    U = {s: np.zeros((nw, 24, ni), dtype=complex) for s in (1, -1)}
+    V = {s: np.zeros((nw, 24, ni), dtype=complex) for s in (1, -1)}
+    cache = {}
     for i in range(ni):
+        groups = {}
         for f in range(nf):
             for nu in range(nm):
                 q = oph[nu, iq[iks_i[i], iks_f[f]]]
@@ -171,29 +192,34 @@ def naive_apply_ladder(setup, J, Gm, Gp, T, w_ac):
                     continue
                 w = w_f[f] * g2[nu, i, f]
                 n = 1.0 / math.expm1(q / T)
-                Fy = F[:, :, :, :, f].reshape(nw, -1, order="F")
-                up = np.array([hat_value(Fy, ws, ws[j] + q) for j in range(nw)]) * w
-                um = np.array([hat_value(Fy, ws, ws[j] - q) for j in range(nw)]) * w
-                Up[:, :, :, :, i] += up.reshape(nw, 4, 3, 2, order="F")
-                Um[:, :, :, :, i] += um.reshape(nw, 4, 3, 2, order="F")
-                Vp[:, :, :, :, i] += n * up.reshape(nw, 4, 3, 2, order="F")
-                Vm[:, :, :, :, i] += n * um.reshape(nw, 4, 3, 2, order="F")
+                acc = groups.setdefault(q, [np.zeros((nw, 24), dtype=complex), np.zeros((nw, 24), dtype=complex)])
+                acc[0] += w * Ff[:, :, f]
+                acc[1] += (n * w) * Ff[:, :, f]
+        for q, (a, b) in groups.items():
+            for s in (1, -1):
+                key = s * q
+                if key not in cache:
+                    cache[key] = hat_matrix(ws, key)
+                U[s][:, :, i] += cache[key] @ a
+                V[s][:, :, i] += cache[key] @ b
+    Up, Um, Vp, Vm = (X.reshape(nw, 4, 3, 2, ni, order="F") for X in (U[1], U[-1], V[1], V[-1]))
     K = kk_matrix(ws)
     KY = (K @ ((Up - Um) / 2).reshape(nw, -1, order="F")).reshape(Up.shape, order="F")
+    k11 = -1j * KY[:, 0] - (Up[:, 0] + Um[:, 0]) / 2 - (Vp[:, 0] + Vm[:, 0])
+    k22 = 1j * KY[:, 3] - (Up[:, 3] + Um[:, 3]) / 2 - (Vp[:, 3] + Vm[:, 3])
+    k21 = -(Vp[:, 1] + Um[:, 1] + Vm[:, 1])
+    k12 = -(Up[:, 2] + Vp[:, 2] + Vm[:, 2])
+    # s ⊙ K with s = [1 -1; -1 1]; the contour matrix of pair index c12 = c1 + 2 c2.
+    Kab = np.stack([k11, -k21, -k12, k22], axis=1)  # [nω, c12, cart, c0, i]
     LJ = np.zeros((nw, 4, 3, 2, ni), dtype=complex)
-    s = np.array([[1, -1], [-1, 1]])
-    for i in range(ni):
-        for c0 in range(2):
-            for a in range(3):
-                k11 = -1j * KY[:, 0, a, c0, i] - (Up[:, 0, a, c0, i] + Um[:, 0, a, c0, i]) / 2 - (Vp[:, 0, a, c0, i] + Vm[:, 0, a, c0, i])
-                k22 = 1j * KY[:, 3, a, c0, i] - (Up[:, 3, a, c0, i] + Um[:, 3, a, c0, i]) / 2 - (Vp[:, 3, a, c0, i] + Vm[:, 3, a, c0, i])
-                k21 = -(Vp[:, 1, a, c0, i] + Um[:, 1, a, c0, i] + Vm[:, 1, a, c0, i])
-                k12 = -(Up[:, 2, a, c0, i] + Vp[:, 2, a, c0, i] + Vm[:, 2, a, c0, i])
-                for j in range(nw):
-                    Kab = s * np.array([[k11[j], k12[j]], [k21[j], k22[j]]])
-                    gm = Gm[j, :, i].reshape(2, 2, order="F")
-                    gp = Gp[j, :, i].reshape(2, 2, order="F")
-                    LJ[j, :, a, c0, i] = -(gm @ Kab @ gp).reshape(4, order="F")
+    for c1 in range(2):
+        for c2 in range(2):
+            acc = 0
+            for a in range(2):
+                for b in range(2):
+                    acc = acc + (Gm[:, c1 + 2 * a, None, None, :] * Kab[:, a + 2 * b]
+                                 * Gp[:, b + 2 * c2, None, None, :])
+            LJ[:, c1 + 2 * c2] = -acc
     return LJ
 
 
