@@ -1,0 +1,202 @@
+// common.cuh -- shared host and device pieces of libepspectral_gb300: errors, device buffers, the
+// context, and the scalar element functions of the reference (occupations, grid interpolation)
+// as device code.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <cmath>
+
+#include "../../include/epspectral_gb300.h"
+
+namespace epsp {
+
+// ---- errors ----
+
+struct Error {
+  int code;
+  std::string msg;
+};
+
+[[noreturn]] inline void fail(int code, const std::string& msg) { throw Error{code, msg}; }
+
+inline void cuda_check(cudaError_t e, const char* what, const char* file, int line) {
+  if (e != cudaSuccess) {
+    char buf[512];
+    std::snprintf(buf, sizeof buf, "%s failed at %s:%d: %s", what, file, line, cudaGetErrorString(e));
+    fail(e == cudaErrorMemoryAllocation ? EPSP_ENOMEM : EPSP_ECUDA, buf);
+  }
+}
+#define EPSP_CUDA(call) ::epsp::cuda_check((call), #call, __FILE__, __LINE__)
+
+// ---- context ----
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  int64_t launches = 0;
+  int sm_count = 0;
+  // Device-side timing of one named kernel family (enabled by epsp_profile_kernel).
+  std::string prof_name;
+  std::vector<cudaEvent_t> prof_events;  // pairs (start, stop)
+  size_t prof_used = 0;
+  // Host-side test hook: the next allocation of at least `fail_alloc_bytes` fails (0 = off).
+  size_t fail_alloc_bytes = 0;
+};
+
+// Records the start event of a profiled launch; returns the pair index or -1.
+inline long prof_begin(Ctx* c, const char* name) {
+  if (c->prof_name.empty() || c->prof_name != name) return -1;
+  if (c->prof_used + 2 > c->prof_events.size()) {
+    for (int k = 0; k < 64; ++k) {
+      cudaEvent_t e;
+      EPSP_CUDA(cudaEventCreate(&e));
+      c->prof_events.push_back(e);
+    }
+  }
+  long idx = long(c->prof_used);
+  EPSP_CUDA(cudaEventRecord(c->prof_events[idx], c->stream));
+  c->prof_used += 2;
+  return idx;
+}
+inline void prof_end(Ctx* c, long idx) {
+  if (idx >= 0) EPSP_CUDA(cudaEventRecord(c->prof_events[size_t(idx) + 1], c->stream));
+}
+
+#define EPSP_LAUNCHED(ctx) do { (ctx)->launches++; EPSP_CUDA(cudaGetLastError()); } while (0)
+
+// ---- device buffers ----
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  Ctx* ctx = nullptr;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept { *this = std::move(o); }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p; n = o.n; ctx = o.ctx;
+      o.p = nullptr; o.n = 0;
+    }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(Ctx* c, size_t count) {
+    release();
+    ctx = c;
+    n = count;
+    if (count == 0) return;
+    size_t bytes = count * sizeof(T);
+    if (c && c->fail_alloc_bytes && bytes >= c->fail_alloc_bytes) {
+      c->fail_alloc_bytes = 0;
+      fail(EPSP_ENOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed (test hook)");
+    }
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      (void)cudaGetLastError();
+      fail(EPSP_ENOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
+    }
+  }
+  void upload(const T* h, size_t count, cudaStream_t s) {
+    EPSP_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void download(T* h, size_t count, cudaStream_t s) const {
+    EPSP_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+  }
+  void zero(cudaStream_t s) {
+    if (n) EPSP_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+  }
+};
+
+template <class T>
+DBuf<T> to_device(Ctx* c, const T* h, size_t count) {
+  DBuf<T> b;
+  b.alloc(c, count);
+  if (count) b.upload(h, count, c->stream);
+  return b;
+}
+template <class T>
+DBuf<T> to_device(Ctx* c, const std::vector<T>& h) {
+  return to_device(c, h.data(), h.size());
+}
+
+inline unsigned div_up(size_t a, size_t b) { return unsigned((a + b - 1) / b); }
+
+// ---- grids (host) ----
+
+struct GridHost {
+  std::vector<double> nodes;  // origin + offsets[j] * unit (src/frequency_grids.jl:140-141)
+  std::vector<int64_t> offsets;
+  double origin = 0, unit = 0, dw_min = 0;
+  int64_t n = 0;
+};
+
+GridHost make_grid(const epsp_grid& g, const char* name);
+
+// cell_search_table (src/frequency_grids.jl:184-196)
+struct CellTableHost {
+  std::vector<int32_t> jtab;
+  double x0 = 0, inv_h = 0;
+};
+CellTableHost make_cell_table(const GridHost& g);
+
+// linear_interpolation_table (src/frequency_grids.jl:65-84), 0-based cells.
+void interp_table(const std::vector<double>& ws, const std::vector<double>& xs, std::vector<int32_t>& j,
+                  std::vector<double>& t);
+
+std::vector<double> trapezoid_weights(const std::vector<double>& ws);
+
+// ---- device element functions ----
+
+struct CellTableDev {
+  const int32_t* jtab;
+  const double* ws;
+  double x0, inv_h;
+  int n;
+};
+
+// occ_fermion, src/utils.jl:14-22 (negative T is rejected on the host before any launch).
+__device__ __forceinline__ double occ_fermion_d(double e, double T) {
+  if (T > 1.4901161193847656e-08) return 1.0 / (exp(e / T) + 1.0);
+  return e > 0 ? 0.0 : (e < 0 ? 1.0 : 0.5);
+}
+
+// occ_boson, src/utils.jl:24-38.
+__device__ __forceinline__ double occ_boson_d(double e, double T) {
+  if (T > 1.4901161193847656e-08) return e == 0 ? -0.5 : 1.0 / expm1(e / T);
+  return e > 0 ? 0.0 : (e == 0 ? -0.5 : -1.0);
+}
+
+// _interp_linear_grid (src/frequency_grids.jl:207-219) of a complex column (interleaved) at x.
+__device__ __forceinline__ double2 interp_grid_d(const double2* __restrict__ col, const CellTableDev& ct, double x) {
+  if (!(x > ct.ws[0])) return col[0];
+  if (x >= ct.ws[ct.n - 1]) return col[ct.n - 1];
+  int c = __ldg(ct.jtab + (long long)((x - ct.x0) * ct.inv_h));
+  int j = c - 1 + (__ldg(ct.ws + c) <= x ? 1 : 0);
+  double wl = __ldg(ct.ws + j), wh = __ldg(ct.ws + j + 1);
+  double t = (x - wl) / (wh - wl);
+  double2 lo = col[j], hi = col[j + 1];
+  return make_double2((1 - t) * lo.x + t * hi.x, (1 - t) * lo.y + t * hi.y);
+}
+
+}  // namespace epsp
+
+// The opaque handle types of the ABI.
+struct epsp_ctx {
+  epsp::Ctx c;
+};

@@ -1,0 +1,151 @@
+// context.cu -- the context entry points of the ABI and the host-side grid tables shared by the
+// scGD0 and ladder plans.
+#include "common.cuh"
+
+#include <algorithm>
+#include <limits>
+
+namespace epsp {
+
+GridHost make_grid(const epsp_grid& g, const char* name) {
+  // FrequencyGrid's constructor checks, src/frequency_grids.jl:124-132.
+  if (!(std::isfinite(g.origin) && std::isfinite(g.unit) && g.unit > 0))
+    fail(EPSP_EINVAL, std::string(name) + ": origin must be finite and unit finite and positive");
+  if (g.n < 2 || g.offsets == nullptr) fail(EPSP_EINVAL, std::string(name) + ": a FrequencyGrid needs at least two nodes");
+  GridHost h;
+  h.origin = g.origin;
+  h.unit = g.unit;
+  h.n = g.n;
+  h.offsets.assign(g.offsets, g.offsets + g.n);
+  int64_t mg = std::numeric_limits<int64_t>::max();
+  for (int64_t j = 0; j + 1 < g.n; ++j) {
+    int64_t d = g.offsets[j + 1] - g.offsets[j];
+    if (d <= 0) fail(EPSP_EINVAL, std::string(name) + ": offsets must be strictly increasing");
+    mg = std::min(mg, d);
+  }
+  h.dw_min = g.unit * double(mg);
+  h.nodes.resize(size_t(g.n));
+  for (int64_t j = 0; j < g.n; ++j) h.nodes[size_t(j)] = g.origin + double(g.offsets[j]) * g.unit;
+  return h;
+}
+
+CellTableHost make_cell_table(const GridHost& g) {
+  CellTableHost ct;
+  ct.x0 = g.nodes[0];
+  ct.inv_h = 1.0 / ((1.0 - 1e-6) * g.dw_min);
+  double span_b = std::min((g.nodes.back() - ct.x0) * ct.inv_h, std::ldexp(1.0, 40));
+  if (int64_t(span_b) + 1 > (int64_t(1) << 24))
+    fail(EPSP_EINVAL, "cell search table of more than 2^24 entries: use a grid without a near-coincident pair of nodes");
+  std::vector<int64_t> b(g.nodes.size());
+  for (size_t j = 0; j < g.nodes.size(); ++j) b[j] = int64_t((g.nodes[j] - ct.x0) * ct.inv_h);
+  for (size_t j = 0; j + 1 < b.size(); ++j)
+    if (b[j + 1] == b[j]) fail(EPSP_EINVAL, "two grid nodes fall in one bucket");
+  ct.jtab.resize(size_t(b.back() + 1));
+  size_t c = 0;
+  for (int64_t k = 0; k <= b.back(); ++k) {
+    while (c < b.size() && b[c] < k) ++c;
+    ct.jtab[size_t(k)] = int32_t(c);
+  }
+  return ct;
+}
+
+void interp_table(const std::vector<double>& ws, const std::vector<double>& xs, std::vector<int32_t>& j,
+                  std::vector<double>& t) {
+  const size_t n = ws.size();
+  j.resize(xs.size());
+  t.resize(xs.size());
+  for (size_t r = 0; r < xs.size(); ++r) {
+    double x = xs[r];
+    if (x <= ws[0]) {
+      j[r] = 0;
+      t[r] = 0;
+    } else if (x >= ws[n - 1]) {
+      j[r] = int32_t(n - 2);
+      t[r] = 1;
+    } else {
+      size_t jr = size_t(std::upper_bound(ws.begin(), ws.end(), x) - ws.begin()) - 1;
+      j[r] = int32_t(jr);
+      t[r] = (x - ws[jr]) / (ws[jr + 1] - ws[jr]);
+    }
+  }
+}
+
+std::vector<double> trapezoid_weights(const std::vector<double>& ws) {  // src/frequency_grids.jl:53-54
+  const size_t n = ws.size();
+  std::vector<double> W(n);
+  for (size_t j = 0; j < n; ++j) W[j] = (ws[std::min(j + 1, n - 1)] - ws[j == 0 ? 0 : j - 1]) / 2;
+  return W;
+}
+
+}  // namespace epsp
+
+using namespace epsp;
+
+extern "C" {
+
+epsp_status epsp_create(epsp_ctx** out, int32_t device) {
+  if (!out) return EPSP_EINVAL;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return EPSP_ECUDA;
+  if (device < 0 || device >= n) return EPSP_EINVAL;
+  auto* c = new (std::nothrow) epsp_ctx;
+  if (!c) return EPSP_ENOMEM;
+  c->c.device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return EPSP_ECUDA;
+  }
+  cudaDeviceGetAttribute(&c->c.sm_count, cudaDevAttrMultiProcessorCount, device);
+  *out = c;
+  return EPSP_OK;
+}
+
+void epsp_destroy(epsp_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->c.device);
+  for (auto e : c->c.prof_events) cudaEventDestroy(e);
+  if (c->c.stream) cudaStreamDestroy(c->c.stream);
+  delete c;
+}
+
+const char* epsp_last_error(const epsp_ctx* c) { return c ? c->c.last_error.c_str() : "null context"; }
+
+int64_t epsp_kernel_launches(const epsp_ctx* c) { return c ? c->c.launches : 0; }
+
+/* Kernel timing for the roofline report (not in the reference): every launch of the kernel family
+ * `name` is bracketed by CUDA events on the context's stream until the next call. name = NULL or ""
+ * switches it off. epsp_profile_read returns the summed milliseconds and the number of launches. */
+epsp_status epsp_profile_kernel(epsp_ctx* c, const char* name) {
+  if (!c) return EPSP_EINVAL;
+  c->c.prof_name = name ? name : "";
+  c->c.prof_used = 0;
+  return EPSP_OK;
+}
+
+epsp_status epsp_profile_read(epsp_ctx* c, double* total_ms, int64_t* count) {
+  if (!c) return EPSP_EINVAL;
+  if (cudaStreamSynchronize(c->c.stream) != cudaSuccess) return EPSP_ECUDA;
+  double tot = 0;
+  size_t n = c->c.prof_used / 2;
+  for (size_t k = 0; k < n; ++k) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, c->c.prof_events[2 * k], c->c.prof_events[2 * k + 1]) != cudaSuccess) return EPSP_ECUDA;
+    tot += ms;
+  }
+  if (total_ms) *total_ms = tot;
+  if (count) *count = int64_t(n);
+  c->c.prof_used = 0;
+  return EPSP_OK;
+}
+
+/* Test hook (not in the reference): the next device allocation of at least `bytes` bytes made
+ * through this context fails with EPSP_ENOMEM, as a device without room would. 0 switches it off. */
+epsp_status epsp_test_fail_alloc(epsp_ctx* c, uint64_t bytes) {
+  if (!c) return EPSP_EINVAL;
+  c->c.fail_alloc_bytes = size_t(bytes);
+  return EPSP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,896 @@
+// scgd0.cu -- the scGD0 plan: setup (src/scgd0.jl:127-245) and the iteration (src/scgd0.jl:246-346)
+// on one GPU.
+//
+// HBM layout of a plan (column-major, reference index order):
+//   Σ, Σ_new       [nω, ni, nT] double2        Σ_in [nω, ni] double2 (clamped, one T at a time)
+//   ImΣ, ReΣ       [nω, ni] double             KK [nω, nω] double
+//   DIRECT_FP64 :  g2_t, ωq_t [nm·nf, ni] double (the (ν f, i) layout of src/scgd0.jl:275-278)
+//   GEMM paths  :  G [nc·nm, ni] coupling summed over each column set (a star, or one inner state)
+//                  K_t [nω, nc·nm] the kernel tensor of one iteration and temperature
+//   spectral    :  A [nωa, ni] double, D [nωa], column sums [ni]
+#include "common.cuh"
+#include "gemm_f64.cuh"
+#include "scgd0.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <limits>
+
+namespace epsp {
+
+// ---------------------------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------------------------
+
+// kramers_kronig_matrix (src/frequency_grids.jl:5-44) on the padded nodes xs[0..n+1].
+__device__ __forceinline__ double xlogx_d(double x) { return x == 0 ? 0.0 : x * log(fabs(x)); }
+
+__global__ void kk_build_kernel(const double* __restrict__ xs, int n, double* __restrict__ K) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= long(n) * n) return;
+  int i = int(idx % n), j = int(idx / n);
+  double x = xs[i + 1], x1 = xs[j], x2 = xs[j + 1], x3 = xs[j + 2];
+  double v = xlogx_d(x1 - x) / (x2 - x1) - xlogx_d(x2 - x) * (x3 - x1) / (x2 - x1) / (x3 - x2) + xlogx_d(x3 - x) / (x3 - x2);
+  K[idx] = v / 3.14159265358979323846;
+}
+
+// g2 [nm, ni, nf] (any storage type) -> g2_t [nm, nf, ni] double (src/scgd0.jl:275-278), and
+// ωq_t[ν, f, i] = ωph[ν, iq_kk[iks_i[i], iks_f[f]]] (gather_pair_table!, src/scgd0.jl:270).
+template <class T>
+__device__ __forceinline__ double load_g2(const T* p, long k);
+template <>
+__device__ __forceinline__ double load_g2<double>(const double* p, long k) { return p[k]; }
+template <>
+__device__ __forceinline__ double load_g2<float>(const float* p, long k) { return double(p[k]); }
+template <>
+__device__ __forceinline__ double load_g2<uint16_t>(const uint16_t* p, long k) {
+  return double(__uint_as_float(uint32_t(p[k]) << 16));
+}
+
+template <class T>
+__global__ void permute_g2_kernel(const T* __restrict__ g2, int nm, int ni, long nf, long f0, long nfc,
+                                  double* __restrict__ g2t) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  long total = long(nm) * nfc * ni;
+  if (idx >= total) return;
+  int nu = int(idx % nm);
+  long f = (idx / nm) % nfc;
+  int i = int(idx / (long(nm) * nfc));
+  g2t[nu + nm * (f + nf * long(i))] = load_g2(g2, nu + nm * (long(i) + ni * (f0 + f)));
+  (void)f0;
+}
+
+__global__ void gather_wq_kernel(const double* __restrict__ wph, const int32_t* __restrict__ iq_kk,
+                                 const int32_t* __restrict__ iks_i, const int32_t* __restrict__ iks_f, int nm, int ni,
+                                 long nf, long nk_i, double* __restrict__ wqt) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  long total = long(nm) * nf * ni;
+  if (idx >= total) return;
+  int nu = int(idx % nm);
+  long f = (idx / nm) % nf;
+  int i = int(idx / (long(nm) * nf));
+  long q = iq_kk[iks_i[i] + nk_i * long(iks_f[f])];
+  wqt[idx] = wph[nu + long(nm) * q];
+}
+
+// Σ_in = Re Σ + i min(Im Σ, -η_min) (src/scgd0.jl:256-260).
+__global__ void clamp_kernel(const double2* __restrict__ S, double2* __restrict__ Sin, long n, double eta_min) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double2 z = S[k];
+  Sin[k] = make_double2(z.x, fmin(z.y, -eta_min));
+}
+
+// The reference's Fan-Migdal sum, term by term in FP64: for each (ω, i), the sum over νf of
+// _fan_migdal_imsigma_term (src/scgd0_kernel.jl:27-39) in ascending νf, added to ImΣ
+// (src/scgd0_kernel.jl:74-86). One thread per (ω, i); the block's νf tile (g2, ωq, n_B(ωq) and the
+// per-state ε, w, i_f) is staged in shared memory. n_B is evaluated once per (νf, i), the same
+// function on the same argument as the reference's per-term call.
+constexpr int kFmTile = 128;
+
+__global__ void __launch_bounds__(kFmTile) fm_direct_kernel(
+    const double* __restrict__ ws, int nw, CellTableDev ct, const double2* __restrict__ Sin,
+    const double* __restrict__ g2t, const double* __restrict__ wqt, long nvf, const double* __restrict__ eps_f,
+    const double* __restrict__ w_f, const int32_t* __restrict__ f_to_i, int nm, long vf0, long vf1, double mu,
+    double T, double w_ac, double* __restrict__ imsigma) {
+  __shared__ double s_g2[kFmTile], s_wq[kFmTile], s_nq[kFmTile], s_eps[kFmTile], s_wf[kFmTile];
+  __shared__ int s_col[kFmTile];
+  const int i = blockIdx.y;
+  const int iw = blockIdx.x * kFmTile + threadIdx.x;
+  const double w = iw < nw ? ws[iw] : 0.0;
+  double acc = 0.0;
+  for (long t0 = vf0; t0 < vf1; t0 += kFmTile) {
+    long vf = t0 + threadIdx.x;
+    if (vf < vf1) {
+      double wq = wqt[vf + nvf * i];
+      long f = vf / nm;
+      s_g2[threadIdx.x] = g2t[vf + nvf * i];
+      s_wq[threadIdx.x] = wq;
+      s_nq[threadIdx.x] = wq < w_ac ? 0.0 : occ_boson_d(wq, T);
+      s_eps[threadIdx.x] = eps_f[f];
+      s_wf[threadIdx.x] = w_f[f];
+      s_col[threadIdx.x] = f_to_i[f];
+    }
+    __syncthreads();
+    int nt = int(min(long(kFmTile), vf1 - t0));
+    if (iw < nw) {
+      for (int k = 0; k < nt; ++k) {
+        double wq = s_wq[k];
+        if (wq < w_ac) continue;
+        const double2* col = Sin + long(nw) * s_col[k];
+        double xa = w + wq, xe = w - wq;
+        double2 sa = interp_grid_d(col, ct, xa);
+        double2 se = interp_grid_d(col, ct, xe);
+        double zar = xa - s_eps[k] - sa.x, zai = -sa.y;
+        double zer = xe - s_eps[k] - se.x, zei = -se.y;
+        double ga = -zai / (zar * zar + zai * zai);
+        double ge = -zei / (zer * zer + zei * zei);
+        double nq = s_nq[k];
+        acc += s_wf[k] * s_g2[k] * (ga * (nq + occ_fermion_d(xa - mu, T)) + ge * (nq + 1 - occ_fermion_d(xe - mu, T)));
+      }
+    }
+    __syncthreads();
+  }
+  if (iw < nw) imsigma[iw + long(nw) * i] += acc;
+}
+
+// The occupation factors of the recast sum, per (ω, ν): F_abs = n_ν + f(ω + ω_ν - μ) and
+// F_emi = n_ν + 1 - f(ω - ω_ν - μ) (the two brackets of src/scgd0_kernel.jl:37-38); 0 for a mode
+// below ω_acoustic.
+__global__ void occ_table_kernel(const double* __restrict__ ws, int nw, const double* __restrict__ wnu, int nm,
+                                 double mu, double T, double w_ac, double* __restrict__ Fa, double* __restrict__ Fe) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nw * nm) return;
+  int iw = k % nw, nu = k / nw;
+  double q = wnu[nu], w = ws[iw];
+  if (q < w_ac) {
+    Fa[k] = 0;
+    Fe[k] = 0;
+    return;
+  }
+  double nq = occ_boson_d(q, T);
+  Fa[k] = nq + occ_fermion_d(w + q - mu, T);
+  Fe[k] = nq + 1 - occ_fermion_d(w - q - mu, T);
+}
+
+// The kernel tensor of the recast sum (dispersionless modes): K_t[ω, (ν, c)] =
+// Im G_c(ω + ω_ν) F_abs[ω, ν] + Im G_c(ω - ω_ν) F_emi[ω, ν], with Im G_c(x) = Im 1/(x - ε_c -
+// Σ_in,col(c)(x)), for the column set c (a star of inner states sharing ε and the representative's
+// Σ, or one inner state).
+__global__ void kbuild_f64_kernel(const double* __restrict__ ws, int nw, CellTableDev ct, const double2* __restrict__ Sin,
+                                  const double* __restrict__ wnu, int nm, const double* __restrict__ eps_c,
+                                  const int32_t* __restrict__ col_c, long nc, const double* __restrict__ Fa,
+                                  const double* __restrict__ Fe, double w_ac, double* __restrict__ Kt) {
+  const int iw = blockIdx.x * blockDim.x + threadIdx.x;
+  const long kc = blockIdx.y;  // (ν, c) with ν fastest
+  if (iw >= nw) return;
+  const int nu = int(kc % nm);
+  const long c = kc / nm;
+  double q = wnu[nu];
+  double out = 0.0;
+  if (!(q < w_ac)) {
+    const double2* col = Sin + long(nw) * col_c[c];
+    double w = ws[iw], e = eps_c[c];
+    double xa = w + q, xe = w - q;
+    double2 sa = interp_grid_d(col, ct, xa);
+    double2 se = interp_grid_d(col, ct, xe);
+    double zar = xa - e - sa.x, zai = -sa.y;
+    double zer = xe - e - se.x, zei = -se.y;
+    double ga = -zai / (zar * zar + zai * zai);
+    double ge = -zei / (zer * zer + zei * zei);
+    out = ga * Fa[iw + long(nw) * nu] + ge * Fe[iw + long(nw) * nu];
+  }
+  Kt[iw + long(nw) * kc] = out;
+}
+
+// G[(ν, c), i] = Σ_{f in c} w_f g2[ν, i, f] over the inner states of column set c in star order;
+// rows of modes below ω_acoustic are 0 (they are skipped before g2 is read in the reference).
+template <class T>
+__global__ void coupling_sum_kernel(const T* __restrict__ g2, int nm, int ni, const int32_t* __restrict__ cptr,
+                                    const int32_t* __restrict__ members, long nc, const double* __restrict__ w_f,
+                                    const double* __restrict__ wnu, double w_ac, double* __restrict__ G) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= long(nm) * ni) return;
+  int nu = int(idx % nm), i = int(idx / nm);
+  bool skip = wnu[nu] < w_ac;
+  for (long c = 0; c < nc; ++c) {
+    double s = 0.0;
+    if (!skip)
+      for (int p = cptr[c]; p < cptr[c + 1]; ++p) {
+        long f = members[p];
+        s += w_f[f] * load_g2(g2, nu + long(nm) * (i + long(ni) * f));
+      }
+    G[(nu + nm * c) + long(nm) * nc * i] = s;
+  }
+}
+
+// Σ_new = ReΣ + i ImΣ (src/scgd0.jl:290-291).
+__global__ void assemble_kernel(const double* __restrict__ re, const double* __restrict__ im, double2* __restrict__ out,
+                                long n) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = make_double2(re[k], im[k]);
+}
+
+__global__ void assemble_f32_kernel(const float* __restrict__ re, const float* __restrict__ im, double2* __restrict__ out,
+                                    long n) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = make_double2(double(re[k]), double(im[k]));
+}
+
+// Average over degenerate multiplets (src/scgd0.jl:293-301): thread per (ω, multiplet), the sum
+// over members in order divided by the count.
+__global__ void multiplet_kernel(double2* __restrict__ S, int nw, const int32_t* __restrict__ mptr,
+                                 const int32_t* __restrict__ midx, long nmult) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= long(nw) * nmult) return;
+  int iw = int(k % nw);
+  long g = k / nw;
+  int p0 = mptr[g], p1 = mptr[g + 1];
+  double sr = 0, si = 0;
+  for (int p = p0; p < p1; ++p) {
+    double2 z = S[iw + long(nw) * midx[p]];
+    sr += z.x;
+    si += z.y;
+  }
+  double len = double(p1 - p0);
+  for (int p = p0; p < p1; ++p) S[iw + long(nw) * midx[p]] = make_double2(sr / len, si / len);
+}
+
+// Imaginary part of Julia's inv(z) (Smith's algorithm), as in `inv.(…)` of src/scgd0.jl:305.
+__device__ __forceinline__ double imag_inv_d(double c, double d) {
+  if (fabs(d) <= fabs(c)) {
+    double r = d / c;
+    double t = 1.0 / (c + d * r);
+    return -r * t;
+  }
+  double r = c / d;
+  double t = 1.0 / (d + c * r);
+  return -t;
+}
+
+// Spectral functions on ωs_spectral (src/scgd0.jl:303-305): A[a, i] = -Im(1/(ωa - ε_i -
+// Σ(ωa)))/π with Σ read by the table (j_sp, t_sp) (apply_interpolation_table!).
+__global__ void spectral_A_kernel(const double2* __restrict__ S, int nw, const double* __restrict__ wsa, int nwa,
+                                  const int32_t* __restrict__ jsp, const double* __restrict__ tsp,
+                                  const double* __restrict__ eps_i, double* __restrict__ A) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y;
+  if (a >= nwa) return;
+  int j = jsp[a];
+  double t = tsp[a];
+  const double2* col = S + long(nw) * i;
+  double2 lo = col[j], hi = col[j + 1];
+  double sr = (1 - t) * lo.x + t * hi.x;
+  double si = (1 - t) * lo.y + t * hi.y;
+  A[a + long(nwa) * i] = -imag_inv_d(wsa[a] - eps_i[i] - sr, -si) / 3.14159265358979323846;
+}
+
+// Fixed-order block reduction helpers (deterministic for a fixed block size).
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+#pragma unroll
+  for (int s = NT / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// colsum[i] = Σ_a A[a, i] Wa[a] (the ∫A_i of min_spectral_weight, src/scgd0.jl:308).
+__global__ void __launch_bounds__(256) spectral_colsum_kernel(const double* __restrict__ A, int nwa,
+                                                              const double* __restrict__ Wa, double* __restrict__ colsum) {
+  __shared__ double sh[256];
+  int i = blockIdx.x;
+  double s = 0;
+  for (int a = threadIdx.x; a < nwa; a += 256) s += A[a + long(nwa) * i] * Wa[a];
+  double r = block_sum<256>(s, sh);
+  if (threadIdx.x == 0) colsum[i] = r;
+}
+
+// D[a] = (Σ_i A[a, i] w_i) Wa[a] (src/scgd0.jl:306-307).
+__global__ void spectral_D_kernel(const double* __restrict__ A, int nwa, int ni, const double* __restrict__ w_i,
+                                  const double* __restrict__ Wa, double* __restrict__ D) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nwa) return;
+  double s = 0;
+  for (int i = 0; i < ni; ++i) s += A[a + long(nwa) * i] * w_i[i];
+  D[a] = s * Wa[a];
+}
+
+__global__ void __launch_bounds__(256) min_kernel(const double* __restrict__ x, int n, double* __restrict__ out) {
+  __shared__ double sh[256];
+  double m = INFINITY;
+  for (int k = threadIdx.x; k < n; k += 256) m = fmin(m, x[k]);
+  sh[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = fmin(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+// Roots.jl's Bisection midpoint over floating-point values (Roots._middle).
+__device__ __forceinline__ double float_middle_d(double x, double y) {
+  if (!isfinite(x) || !isfinite(y)) return x + y;
+  if (x != 0 && y != 0 && (signbit(x) != signbit(y))) return 0.0;
+  bool negate = (x < 0) || (y < 0);
+  unsigned long long ux = __double_as_longlong(fabs(x)), uy = __double_as_longlong(fabs(y));
+  double m = __longlong_as_double((long long)((ux + uy) >> 1));
+  return negate ? -m : m;
+}
+
+// The μ solve of one temperature (src/scgd0.jl:309-324): the root of n(μ) - n_target with
+// n(μ) = compute_ncarrier_spectral (src/scgd0.jl:361-366) by bisection over floating-point values
+// on the bracket, FP64 throughout; each evaluation is a fixed-order block sum over ωs_spectral.
+// status: 0 ok, 1 no sign change on the bracket.
+constexpr int kMuThreads = 1024;
+__global__ void __launch_bounds__(kMuThreads) mu_bisect_kernel(const double* __restrict__ D, const double* __restrict__ wsa,
+                                                               int nwa, double T, double W, double base, double gs,
+                                                               double n_target, int holes, double br0, double br1,
+                                                               double* __restrict__ mu_out, int* __restrict__ status) {
+  __shared__ double sh[kMuThreads];
+  __shared__ double s_m;
+  __shared__ int s_done;
+  auto excess = [&](double mu) {
+    double s = 0;
+    if (holes)
+      for (int a = threadIdx.x; a < nwa; a += kMuThreads) s += D[a] * occ_fermion_d(mu - wsa[a], T);
+    else
+      for (int a = threadIdx.x; a < nwa; a += kMuThreads) s += D[a] * occ_fermion_d(wsa[a] - mu, T);
+    double tot = block_sum<kMuThreads>(s, sh);
+    return (holes ? (W - tot + base) * gs : (tot + base) * gs) - n_target;
+  };
+  double a = br0, b = br1;
+  double fa = excess(a), fb = excess(b);
+  if (fa * fb > 0) {
+    if (threadIdx.x == 0) *status = 1;
+    return;
+  }
+  double result;
+  if (fa == 0) {
+    result = a;
+  } else if (fb == 0) {
+    result = b;
+  } else {
+    result = NAN;
+    for (int it = 0; it < 2100; ++it) {
+      if (threadIdx.x == 0) {
+        double m = float_middle_d(a, b);
+        s_m = m;
+        s_done = (m == a || m == b);
+      }
+      __syncthreads();
+      double m = s_m;
+      int done = s_done;
+      __syncthreads();
+      if (done) break;
+      double fm = excess(m);
+      if (fm == 0) {
+        result = m;
+        break;
+      }
+      if (signbit(fm) == signbit(fa)) {
+        a = m;
+        fa = fm;
+      } else {
+        b = m;
+        fb = fm;
+      }
+    }
+    if (isnan(result)) result = fabs(fa) <= fabs(fb) ? a : b;
+  }
+  if (threadIdx.x == 0) {
+    *mu_out = result;
+    *status = 0;
+  }
+}
+
+// err = max |Σ_new - Σ| over one temperature, and Σ ← Σ_new (src/scgd0.jl:326-328). The maximum of
+// non-negative doubles is taken on their bit patterns, which order the same way; NaN wins, as in
+// Julia's maximum.
+__global__ void err_copy_kernel(const double2* __restrict__ Snew, double2* __restrict__ S, long n,
+                                unsigned long long* __restrict__ errbits) {
+  __shared__ unsigned long long sh[256];
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  unsigned long long e = 0;
+  if (k < n) {
+    double2 a = Snew[k], b = S[k];
+    double d = hypot(a.x - b.x, a.y - b.y);
+    e = (unsigned long long)__double_as_longlong(d);
+    S[k] = a;
+  }
+  sh[threadIdx.x] = e;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = max(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicMax(errbits, sh[0]);
+}
+
+// ---------------------------------------------------------------------------------------------
+// setup
+// ---------------------------------------------------------------------------------------------
+
+static void check_model_common(const epsp_model* m) {
+  if (!m) fail(EPSP_EINVAL, "model is NULL");
+  if (m->nm < 1 || m->ni < 1 || m->nf < 1) fail(EPSP_EINVAL, "nm, ni and nf must be positive");
+  if (!m->g2 || !m->omega_ph || !m->iq_kk || !m->iks_i || !m->iks_f || !m->eps_i || !m->w_i || !m->eps_f ||
+      !m->w_f || !m->f_to_i)
+    fail(EPSP_EINVAL, "a required model array is NULL");
+  if (m->g2_dtype != EPSP_F64 && m->g2_dtype != EPSP_F32 && m->g2_dtype != EPSP_BF16)
+    fail(EPSP_EINVAL, "g2_dtype must be EPSP_F64, EPSP_F32 or EPSP_BF16");
+  if (m->nm > 1024) fail(EPSP_EINVAL, "at most 1024 modes");
+  for (int64_t f = 0; f < m->nf; ++f) {
+    if (m->f_to_i[f] < 0 || m->f_to_i[f] >= m->ni) fail(EPSP_EINVAL, "f_to_i out of range");
+    if (m->iks_f[f] < 0 || m->iks_f[f] >= m->nk_f) fail(EPSP_EINVAL, "iks_f out of range");
+  }
+  for (int64_t i = 0; i < m->ni; ++i)
+    if (m->iks_i[i] < 0 || m->iks_i[i] >= m->nk_i) fail(EPSP_EINVAL, "iks_i out of range");
+  for (int64_t k = 0; k < m->nk_i * m->nk_f; ++k)
+    if (m->iq_kk[k] < 0 || m->iq_kk[k] >= m->nq) fail(EPSP_EINVAL, "iq_kk out of range");
+  if (m->nmult < 0 || (m->nmult > 0 && (!m->mult_ptr || !m->mult_idx))) fail(EPSP_EINVAL, "bad multiplet lists");
+  for (int64_t g = 0; g < m->nmult; ++g) {
+    if (m->mult_ptr[g + 1] < m->mult_ptr[g]) fail(EPSP_EINVAL, "multiplet pointers must not decrease");
+    for (int32_t p = m->mult_ptr[g]; p < m->mult_ptr[g + 1]; ++p)
+      if (m->mult_idx[p] < 0 || m->mult_idx[p] >= m->ni) fail(EPSP_EINVAL, "multiplet member out of range");
+  }
+}
+
+// Modes are dispersionless when every row of ωph is constant; then ωq[ν, f, i] = ω_ν for every pair.
+static bool dispersionless(const epsp_model* m, std::vector<double>& wnu) {
+  wnu.assign(size_t(m->nm), 0.0);
+  for (int64_t nu = 0; nu < m->nm; ++nu) {
+    double w0 = m->omega_ph[nu];
+    for (int64_t q = 1; q < m->nq; ++q)
+      if (!(m->omega_ph[nu + m->nm * q] == w0)) return false;
+    wnu[size_t(nu)] = w0;
+  }
+  return true;
+}
+
+void upload_g2_permuted(Ctx* ctx, const epsp_model* m, DBuf<double>& g2t) {
+  const size_t elem = m->g2_dtype == EPSP_F64 ? 8 : (m->g2_dtype == EPSP_F32 ? 4 : 2);
+  const long nm = m->nm, ni = m->ni, nf = m->nf;
+  g2t.alloc(ctx, size_t(nm * nf * ni));
+  // Stage by slabs of inner states so the raw staging buffer stays bounded (~256 MB).
+  long per_f = nm * ni;
+  long fchunk = std::max<long>(1, long((size_t(256) << 20) / (elem * size_t(per_f))));
+  DBuf<uint8_t> stage;
+  stage.alloc(ctx, size_t(std::min(fchunk, nf) * per_f) * elem);
+  for (long f0 = 0; f0 < nf; f0 += fchunk) {
+    long nfc = std::min(fchunk, nf - f0);
+    const uint8_t* src = static_cast<const uint8_t*>(m->g2) + size_t(f0 * per_f) * elem;
+    EPSP_CUDA(cudaMemcpyAsync(stage.p, src, size_t(nfc * per_f) * elem, cudaMemcpyHostToDevice, ctx->stream));
+    long total = nm * nfc * ni;
+    unsigned grid = div_up(size_t(total), 256);
+    // permute_g2_kernel reads slab-relative inner states and writes at absolute f0 + f.
+    double* dst = g2t.p + nm * f0;
+    if (m->g2_dtype == EPSP_F64)
+      permute_g2_kernel<double><<<grid, 256, 0, ctx->stream>>>(reinterpret_cast<const double*>(stage.p), int(nm), int(ni), nf, 0, nfc, dst);
+    else if (m->g2_dtype == EPSP_F32)
+      permute_g2_kernel<float><<<grid, 256, 0, ctx->stream>>>(reinterpret_cast<const float*>(stage.p), int(nm), int(ni), nf, 0, nfc, dst);
+    else
+      permute_g2_kernel<uint16_t><<<grid, 256, 0, ctx->stream>>>(reinterpret_cast<const uint16_t*>(stage.p), int(nm), int(ni), nf, 0, nfc, dst);
+    EPSP_LAUNCHED(ctx);
+  }
+  EPSP_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) {
+  check_model_common(m);
+  if (!opts) fail(EPSP_EINVAL, "options are NULL");
+  if (opts->gpu_tile < 0) fail(EPSP_EINVAL, "gpu_tile must be nothing or a positive number of inner states");
+  auto* P = new Scgd0Plan;
+  std::unique_ptr<Scgd0Plan> guard(P);
+  P->ctx = ctx;
+  P->path = opts->path;
+  P->w_ac = opts->omega_acoustic;
+  P->verbosity = opts->verbosity;
+  P->nm = m->nm;
+  P->ni = m->ni;
+  P->nf = m->nf;
+  P->ws = make_grid(m->omegas, "omegas");
+  P->wsa = make_grid(m->omegas_spectral, "omegas_spectral");
+  P->nw = P->ws.n;
+  P->nwa = P->wsa.n;
+  P->W = m->W;
+  P->nstates_base = m->nstates_base;
+  P->gpu_tile = opts->gpu_tile;
+  cudaStream_t s = ctx->stream;
+  // grid tables
+  CellTableHost ct = make_cell_table(P->ws);
+  P->d_jtab = to_device(ctx, ct.jtab);
+  P->d_ws = to_device(ctx, P->ws.nodes);
+  P->ct = CellTableDev{P->d_jtab.p, P->d_ws.p, ct.x0, ct.inv_h, int(P->nw)};
+  P->d_wsa = to_device(ctx, P->wsa.nodes);
+  std::vector<int32_t> jsp;
+  std::vector<double> tsp;
+  interp_table(P->ws.nodes, P->wsa.nodes, jsp, tsp);  // src/scgd0.jl:163
+  P->d_jsp = to_device(ctx, jsp);
+  P->d_tsp = to_device(ctx, tsp);
+  P->d_Wa = to_device(ctx, trapezoid_weights(P->wsa.nodes));
+  P->d_eps_i = to_device(ctx, m->eps_i, size_t(m->ni));
+  P->d_w_i = to_device(ctx, m->w_i, size_t(m->ni));
+  if (m->nmult > 0) {
+    P->nmult = m->nmult;
+    P->d_mptr = to_device(ctx, m->mult_ptr, size_t(m->nmult + 1));
+    P->d_midx = to_device(ctx, m->mult_idx, size_t(m->mult_ptr[m->nmult]));
+  }
+  // Kramers-Kronig matrix on the device from the padded nodes (src/frequency_grids.jl:30-44).
+  {
+    const auto& w = P->ws.nodes;
+    std::vector<double> xs(size_t(P->nw + 2));
+    xs[0] = w[0] - (w[1] - w[0]);
+    for (int64_t j = 0; j < P->nw; ++j) xs[size_t(j + 1)] = w[size_t(j)];
+    xs[size_t(P->nw + 1)] = w[size_t(P->nw - 1)] + (w[size_t(P->nw - 1)] - w[size_t(P->nw - 2)]);
+    auto d_xs = to_device(ctx, xs);
+    P->d_KK.alloc(ctx, size_t(P->nw * P->nw));
+    kk_build_kernel<<<div_up(size_t(P->nw * P->nw), 256), 256, 0, s>>>(d_xs.p, int(P->nw), P->d_KK.p);
+    EPSP_LAUNCHED(ctx);
+    EPSP_CUDA(cudaStreamSynchronize(s));
+  }
+  const long nm = m->nm, ni = m->ni, nf = m->nf;
+  if (P->path == EPSP_PATH_DIRECT_FP64) {
+    // nf_chunk of src/scgd0.jl:201-202; the chunks fix the order of the f sum.
+    const int64_t chunk_bytes = int64_t(1) << 30;
+    P->nf_chunk = opts->gpu_tile <= 0 ? std::clamp<int64_t>(chunk_bytes / (8 * nm * ni), 1, nf) : std::min<int64_t>(opts->gpu_tile, nf);
+    upload_g2_permuted(ctx, m, P->d_g2t);
+    auto d_wph = to_device(ctx, m->omega_ph, size_t(nm * m->nq));
+    auto d_iq = to_device(ctx, m->iq_kk, size_t(m->nk_i * m->nk_f));
+    auto d_iksi = to_device(ctx, m->iks_i, size_t(ni));
+    auto d_iksf = to_device(ctx, m->iks_f, size_t(nf));
+    P->d_wqt.alloc(ctx, size_t(nm * nf * ni));
+    gather_wq_kernel<<<div_up(size_t(nm * nf * ni), 256), 256, 0, s>>>(d_wph.p, d_iq.p, d_iksi.p, d_iksf.p, int(nm), int(ni), nf,
+                                                                      m->nk_i, P->d_wqt.p);
+    EPSP_LAUNCHED(ctx);
+    P->d_eps_f = to_device(ctx, m->eps_f, size_t(nf));
+    P->d_w_f = to_device(ctx, m->w_f, size_t(nf));
+    P->d_f_to_i = to_device(ctx, m->f_to_i, size_t(nf));
+    EPSP_CUDA(cudaStreamSynchronize(s));
+  } else if (P->path == EPSP_PATH_GEMM_FP64 || P->path == EPSP_PATH_GEMM_BF16X3) {
+    std::vector<double> wnu;
+    if (!dispersionless(m, wnu))
+      fail(EPSP_EUNSUPPORTED, "the GEMM paths need dispersionless modes (every row of omega_ph constant); use EPSP_PATH_DIRECT_FP64");
+    // Column sets: the stars of the representatives when every inner state of a star has the same
+    // energy (then the f sum of one star is one column); one inner state per column otherwise.
+    std::vector<int32_t> order(static_cast<size_t>(nf));
+    for (long f = 0; f < nf; ++f) order[size_t(f)] = int32_t(f);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return m->f_to_i[a] < m->f_to_i[b]; });
+    std::vector<int32_t> sptr(size_t(ni + 1), 0);
+    for (long f = 0; f < nf; ++f) sptr[size_t(m->f_to_i[f] + 1)]++;
+    for (long i = 0; i < ni; ++i) sptr[size_t(i + 1)] += sptr[size_t(i)];
+    bool uniform = true;
+    std::vector<double> eps_star(static_cast<size_t>(ni), 0.0);
+    for (long i = 0; i < ni && uniform; ++i) {
+      if (sptr[size_t(i + 1)] == sptr[size_t(i)]) continue;
+      double e0 = m->eps_f[order[size_t(sptr[size_t(i)])]];
+      eps_star[size_t(i)] = e0;
+      for (int32_t p = sptr[size_t(i)]; p < sptr[size_t(i + 1)]; ++p)
+        if (!(m->eps_f[order[size_t(p)]] == e0)) uniform = false;
+    }
+    std::vector<int32_t> cptr, members, colc;
+    std::vector<double> epsc;
+    if (uniform) {
+      for (long i = 0; i < ni; ++i)
+        if (sptr[size_t(i + 1)] > sptr[size_t(i)]) {
+          cptr.push_back(sptr[size_t(i)]);
+          colc.push_back(int32_t(i));
+          epsc.push_back(eps_star[size_t(i)]);
+        }
+      cptr.push_back(int32_t(nf));
+      members = order;
+    } else {
+      for (long f = 0; f < nf; ++f) {
+        cptr.push_back(int32_t(f));
+        members.push_back(int32_t(f));
+        colc.push_back(m->f_to_i[f]);
+        epsc.push_back(m->eps_f[f]);
+      }
+      cptr.push_back(int32_t(nf));
+    }
+    P->star_reduced = uniform;
+    P->nc = long(colc.size());
+    P->d_wnu = to_device(ctx, wnu);
+    P->d_colc = to_device(ctx, colc);
+    P->d_epsc = to_device(ctx, epsc);
+    auto d_cptr = to_device(ctx, cptr);
+    auto d_mem = to_device(ctx, members);
+    auto d_wf = to_device(ctx, m->w_f, size_t(nf));
+    // raw g2 on the device for the coupling sums
+    const size_t elem = m->g2_dtype == EPSP_F64 ? 8 : (m->g2_dtype == EPSP_F32 ? 4 : 2);
+    DBuf<uint8_t> g2raw;
+    g2raw.alloc(ctx, size_t(nm * ni * nf) * elem);
+    g2raw.upload(static_cast<const uint8_t*>(m->g2), size_t(nm * ni * nf) * elem, s);
+    P->d_G.alloc(ctx, size_t(nm * P->nc * ni));
+    unsigned grid = div_up(size_t(nm * ni), 128);
+    if (m->g2_dtype == EPSP_F64)
+      coupling_sum_kernel<double><<<grid, 128, 0, s>>>(reinterpret_cast<const double*>(g2raw.p), int(nm), int(ni), d_cptr.p, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac, P->d_G.p);
+    else if (m->g2_dtype == EPSP_F32)
+      coupling_sum_kernel<float><<<grid, 128, 0, s>>>(reinterpret_cast<const float*>(g2raw.p), int(nm), int(ni), d_cptr.p, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac, P->d_G.p);
+    else
+      coupling_sum_kernel<uint16_t><<<grid, 128, 0, s>>>(reinterpret_cast<const uint16_t*>(g2raw.p), int(nm), int(ni), d_cptr.p, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac, P->d_G.p);
+    EPSP_LAUNCHED(ctx);
+    P->d_Fa.alloc(ctx, size_t(P->nw * nm));
+    P->d_Fe.alloc(ctx, size_t(P->nw * nm));
+    if (P->path == EPSP_PATH_GEMM_FP64) {
+      P->d_Kt.alloc(ctx, size_t(P->nw * nm * P->nc));
+    } else {
+      tc_setup(P);
+    }
+    EPSP_CUDA(cudaStreamSynchronize(s));
+  } else {
+    fail(EPSP_EINVAL, "unknown path");
+  }
+  // iteration buffers
+  P->d_Sin.alloc(ctx, size_t(P->nw * ni));
+  P->d_ImS.alloc(ctx, size_t(P->nw * ni));
+  P->d_ReS.alloc(ctx, size_t(P->nw * ni));
+  P->d_A.alloc(ctx, size_t(P->nwa * ni));
+  P->d_colsum.alloc(ctx, size_t(ni));
+  P->d_D.alloc(ctx, size_t(P->nwa));
+  return guard.release();
+}
+
+// ---------------------------------------------------------------------------------------------
+// one Fan-Migdal sum at one temperature: ImΣ += Σ (src/scgd0_kernel.jl:59-86)
+// ---------------------------------------------------------------------------------------------
+
+void scgd0_imsigma(Scgd0Plan* P, const double2* d_Sin, double mu, double T, double* d_ImS) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  const long nm = P->nm, ni = P->ni, nf = P->nf, nw = P->nw;
+  if (P->path == EPSP_PATH_DIRECT_FP64) {
+    const long nvf = nm * nf;
+    dim3 grid(div_up(size_t(nw), kFmTile), unsigned(ni));
+    for (long f0 = 0; f0 < nf; f0 += P->nf_chunk) {
+      long f1 = std::min(nf, f0 + P->nf_chunk);
+      long pi = prof_begin(ctx, "fan_migdal");
+      fm_direct_kernel<<<grid, kFmTile, 0, s>>>(P->d_ws.p, int(nw), P->ct, d_Sin, P->d_g2t.p, P->d_wqt.p, nvf,
+                                                P->d_eps_f.p, P->d_w_f.p, P->d_f_to_i.p, int(nm), nm * f0, nm * f1, mu, T,
+                                                P->w_ac, d_ImS);
+      EPSP_LAUNCHED(ctx);
+      prof_end(ctx, pi);
+    }
+    return;
+  }
+  occ_table_kernel<<<div_up(size_t(nw * nm), 256), 256, 0, s>>>(P->d_ws.p, int(nw), P->d_wnu.p, int(nm), mu, T, P->w_ac,
+                                                                 P->d_Fa.p, P->d_Fe.p);
+  EPSP_LAUNCHED(ctx);
+  const long nk = nm * P->nc;
+  if (P->path == EPSP_PATH_GEMM_FP64) {
+    long pk = prof_begin(ctx, "kbuild");
+    kbuild_f64_kernel<<<dim3(div_up(size_t(nw), 128), unsigned(nk)), 128, 0, s>>>(
+        P->d_ws.p, int(nw), P->ct, d_Sin, P->d_wnu.p, int(nm), P->d_epsc.p, P->d_colc.p, P->nc, P->d_Fa.p, P->d_Fe.p,
+        P->w_ac, P->d_Kt.p);
+    EPSP_LAUNCHED(ctx);
+    prof_end(ctx, pk);
+    long pg = prof_begin(ctx, "fm_gemm");
+    // ImΣ[ω, i] += Σ_k K_t[ω, k] G[k, i]
+    gemm_f64(ctx, false, int(nw), int(ni), int(nk), 1.0, P->d_Kt.p, nw, P->d_G.p, nk, 1.0, d_ImS, nw);
+    prof_end(ctx, pg);
+    return;
+  }
+  tc_imsigma(P, d_Sin, d_ImS);
+}
+
+// ---------------------------------------------------------------------------------------------
+// the iteration (src/scgd0.jl:246-346)
+// ---------------------------------------------------------------------------------------------
+
+void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double eta_init, int32_t maxiter, double tol,
+               int32_t fix_mu, const double* mu_start, const double* sigma_init, double* sigma_out, double* mu_out,
+               uint8_t* converged, epsp_scgd0_history* hist) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  if (!occ || !occ->Tlist || (!occ->nlist && !fix_mu)) fail(EPSP_EINVAL, "occ is incomplete");
+  if (maxiter < 1) fail(EPSP_EINVAL, "maxiter must be at least 1, got " + std::to_string(maxiter));
+  const int64_t nT = occ->nT;
+  if (nT < 1) fail(EPSP_EINVAL, "at least one temperature");
+  if (!eta_min || !mu_start || !sigma_out || !mu_out || !converged || !hist || !hist->err || !hist->mu ||
+      !hist->min_spectral_weight || !hist->wall || !hist->iter_frozen)
+    fail(EPSP_EINVAL, "an output or input array is NULL");
+  for (int64_t iT = 0; iT < nT; ++iT)
+    if (!(occ->Tlist[iT] >= 0)) fail(EPSP_EINVAL, "Temperature must be positive");
+  const long nw = P->nw, ni = P->ni, nwa = P->nwa;
+  const long slab = nw * ni;
+  DBuf<double2> S, Snew;
+  S.alloc(ctx, size_t(slab * nT));
+  Snew.alloc(ctx, size_t(slab * nT));
+  if (sigma_init) {
+    for (long k = 0; k < 2 * slab * nT; ++k)
+      if (!std::isfinite(sigma_init[k])) fail(EPSP_EINVAL, "Sigma_init must be finite");
+    S.upload(reinterpret_cast<const double2*>(sigma_init), size_t(slab * nT), s);
+  } else {
+    std::vector<double2> init(size_t(slab * nT), make_double2(0.0, -eta_init));
+    S.upload(init.data(), init.size(), s);
+    EPSP_CUDA(cudaStreamSynchronize(s));
+  }
+  EPSP_CUDA(cudaMemcpyAsync(Snew.p, S.p, size_t(slab * nT) * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  std::vector<double> mu(mu_start, mu_start + nT);
+  std::vector<char> active(static_cast<size_t>(nT), 1);
+  const double nan = std::numeric_limits<double>::quiet_NaN();
+  for (int64_t k = 0; k < nT * maxiter; ++k) hist->err[k] = hist->mu[k] = hist->min_spectral_weight[k] = nan;
+  for (int32_t k = 0; k < maxiter; ++k) hist->wall[k] = 0;
+  for (int64_t k = 0; k < nT; ++k) hist->iter_frozen[k] = 0;
+  const double br0 = P->wsa.nodes.front() - 0.1, br1 = P->wsa.nodes.back() + 0.1;  // src/scgd0.jl:197
+  DBuf<unsigned long long> d_err;
+  DBuf<double> d_mu, d_minA;
+  DBuf<int> d_status;
+  d_err.alloc(ctx, size_t(nT));
+  d_mu.alloc(ctx, size_t(nT));
+  d_minA.alloc(ctx, size_t(nT));
+  d_status.alloc(ctx, size_t(nT));
+  std::vector<unsigned long long> h_err(static_cast<size_t>(nT));
+  std::vector<double> h_mu(static_cast<size_t>(nT)), h_minA(static_cast<size_t>(nT));
+  std::vector<int> h_status(static_cast<size_t>(nT));
+  int32_t niter = 0;
+  const unsigned eb = div_up(size_t(slab), 256);
+  for (int32_t iter = 1; iter <= maxiter; ++iter) {
+    auto t0 = std::chrono::steady_clock::now();
+    d_err.zero(s);
+    d_status.zero(s);
+    for (int64_t iT = 0; iT < nT; ++iT) {
+      if (!active[size_t(iT)]) continue;
+      const double T = occ->Tlist[iT];
+      double2* ST = S.p + slab * iT;
+      double2* SnT = Snew.p + slab * iT;
+      clamp_kernel<<<eb, 256, 0, s>>>(ST, P->d_Sin.p, slab, eta_min[iT]);
+      EPSP_LAUNCHED(ctx);
+      P->d_ImS.zero(s);
+      scgd0_imsigma(P, P->d_Sin.p, mu[size_t(iT)], T, P->d_ImS.p);
+      long pk = prof_begin(ctx, "kk");
+      if (P->path == EPSP_PATH_GEMM_BF16X3) {
+        tc_kk_assemble(P, SnT);
+      } else {
+        gemm_f64(ctx, false, int(nw), int(ni), int(nw), 1.0, P->d_KK.p, nw, P->d_ImS.p, nw, 0.0, P->d_ReS.p, nw);
+        assemble_kernel<<<eb, 256, 0, s>>>(P->d_ReS.p, P->d_ImS.p, SnT, slab);
+        EPSP_LAUNCHED(ctx);
+      }
+      prof_end(ctx, pk);
+    }
+    if (P->nmult > 0)
+      for (int64_t iT = 0; iT < nT; ++iT) {
+        if (!active[size_t(iT)]) continue;
+        multiplet_kernel<<<div_up(size_t(nw * P->nmult), 256), 256, 0, s>>>(Snew.p + slab * iT, int(nw), P->d_mptr.p,
+                                                                            P->d_midx.p, P->nmult);
+        EPSP_LAUNCHED(ctx);
+      }
+    for (int64_t iT = 0; iT < nT; ++iT) {
+      if (!active[size_t(iT)]) continue;
+      const double T = occ->Tlist[iT];
+      double2* ST = S.p + slab * iT;
+      double2* SnT = Snew.p + slab * iT;
+      spectral_A_kernel<<<dim3(div_up(size_t(nwa), 256), unsigned(ni)), 256, 0, s>>>(SnT, int(nw), P->d_wsa.p, int(nwa), P->d_jsp.p,
+                                                                                    P->d_tsp.p, P->d_eps_i.p, P->d_A.p);
+      EPSP_LAUNCHED(ctx);
+      spectral_colsum_kernel<<<unsigned(ni), 256, 0, s>>>(P->d_A.p, int(nwa), P->d_Wa.p, P->d_colsum.p);
+      EPSP_LAUNCHED(ctx);
+      min_kernel<<<1, 256, 0, s>>>(P->d_colsum.p, int(ni), d_minA.p + iT);
+      EPSP_LAUNCHED(ctx);
+      if (!fix_mu) {
+        spectral_D_kernel<<<div_up(size_t(nwa), 256), 256, 0, s>>>(P->d_A.p, int(nwa), int(ni), P->d_w_i.p, P->d_Wa.p, P->d_D.p);
+        EPSP_LAUNCHED(ctx);
+        bool holes = occ->type == EPSP_SEMICONDUCTOR && occ->nlist[iT] < 0;
+        double n_target = occ->nlist[iT] + occ->nelec;
+        long pm = prof_begin(ctx, "mu");
+        mu_bisect_kernel<<<1, kMuThreads, 0, s>>>(P->d_D.p, P->d_wsa.p, int(nwa), T, P->W, P->nstates_base,
+                                                  occ->spin_degeneracy, n_target, holes ? 1 : 0, br0, br1, d_mu.p + iT,
+                                                  d_status.p + iT);
+        EPSP_LAUNCHED(ctx);
+        prof_end(ctx, pm);
+      }
+      err_copy_kernel<<<eb, 256, 0, s>>>(SnT, ST, slab, d_err.p + iT);
+      EPSP_LAUNCHED(ctx);
+    }
+    d_err.download(h_err.data(), size_t(nT), s);
+    d_mu.download(h_mu.data(), size_t(nT), s);
+    d_minA.download(h_minA.data(), size_t(nT), s);
+    d_status.download(h_status.data(), size_t(nT), s);
+    EPSP_CUDA(cudaStreamSynchronize(s));
+    for (int64_t iT = 0; iT < nT; ++iT) {
+      if (!active[size_t(iT)]) continue;
+      hist->min_spectral_weight[iT + nT * (iter - 1)] = h_minA[size_t(iT)];
+      if (!fix_mu) {
+        if (h_status[size_t(iT)] != 0) {
+          char buf[400];
+          std::snprintf(buf, sizeof buf,
+                        "no chemical potential in (%g, %g) gives %g electrons per cell at T = %g: the window holds too "
+                        "few states on one side of the gap, or the spectral weight it loses outside omegas_spectral "
+                        "moves the count past the target. Pass mu_start with fix_mu, or widen the window or omegas.",
+                        br0, br1, occ->nlist[iT] + occ->nelec, occ->Tlist[iT]);
+          fail(EPSP_ENOROOT_MU, buf);
+        }
+        mu[size_t(iT)] = h_mu[size_t(iT)];
+      }
+      double err;
+      std::memcpy(&err, &h_err[size_t(iT)], 8);
+      hist->err[iT + nT * (iter - 1)] = err;
+      hist->mu[iT + nT * (iter - 1)] = mu[size_t(iT)];
+      if (err < tol) {
+        active[size_t(iT)] = 0;
+        hist->iter_frozen[iT] = iter;
+      }
+    }
+    hist->wall[iter - 1] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    niter = iter;
+    if (std::none_of(active.begin(), active.end(), [](char a) { return a != 0; })) break;
+  }
+  hist->niter = niter;
+  S.download(reinterpret_cast<double2*>(sigma_out), size_t(slab * nT), s);
+  EPSP_CUDA(cudaStreamSynchronize(s));
+  for (int64_t iT = 0; iT < nT; ++iT) {
+    mu_out[iT] = mu[size_t(iT)];
+    converged[iT] = active[size_t(iT)] ? 0 : 1;
+  }
+}
+
+}  // namespace epsp
+
+using namespace epsp;
+
+template <class F>
+static epsp_status guarded(Ctx* c, F&& f) {
+  try {
+    EPSP_CUDA(cudaSetDevice(c->device));
+    f();
+    c->last_error.clear();
+    return EPSP_OK;
+  } catch (const Error& e) {
+    c->last_error = e.msg;
+    return epsp_status(e.code);
+  } catch (const std::bad_alloc&) {
+    c->last_error = "host allocation failed";
+    return EPSP_ENOMEM;
+  } catch (const std::exception& e) {
+    c->last_error = e.what();
+    return EPSP_EINVAL;
+  }
+}
+
+extern "C" {
+
+epsp_status epsp_scgd0_setup(epsp_ctx* ctx, const epsp_model* model, const epsp_options* opts, epsp_scgd0_plan** plan) {
+  if (!ctx || !plan) return EPSP_EINVAL;
+  *plan = nullptr;
+  return guarded(&ctx->c, [&] { *plan = reinterpret_cast<epsp_scgd0_plan*>(scgd0_setup(&ctx->c, model, opts)); });
+}
+
+void epsp_scgd0_plan_destroy(epsp_scgd0_plan* plan) {
+  if (!plan) return;
+  auto* P = reinterpret_cast<Scgd0Plan*>(plan);
+  cudaSetDevice(P->ctx->device);
+  delete P;
+}
+
+epsp_status epsp_scgd0_run(epsp_scgd0_plan* plan, const epsp_occ* occ, const double* eta_min, double eta_init,
+                           int32_t maxiter, double tol, int32_t fix_mu, const double* mu_start, const double* sigma_init,
+                           double* sigma_out, double* mu_out, uint8_t* converged, epsp_scgd0_history* hist) {
+  if (!plan) return EPSP_EINVAL;
+  auto* P = reinterpret_cast<Scgd0Plan*>(plan);
+  return guarded(P->ctx, [&] {
+    scgd0_run(P, occ, eta_min, eta_init, maxiter, tol, fix_mu, mu_start, sigma_init, sigma_out, mu_out, converged, hist);
+  });
+}
+
+epsp_status epsp_scgd0_imsigma(epsp_scgd0_plan* plan, const double* sigma_in, double mu, double T, double* imsigma) {
+  if (!plan || !sigma_in || !imsigma) return EPSP_EINVAL;
+  auto* P = reinterpret_cast<Scgd0Plan*>(plan);
+  return guarded(P->ctx, [&] {
+    if (!(T >= 0)) fail(EPSP_EINVAL, "Temperature must be positive");
+    cudaStream_t s = P->ctx->stream;
+    const size_t n = size_t(P->nw * P->ni);
+    P->d_Sin.upload(reinterpret_cast<const double2*>(sigma_in), n, s);
+    P->d_ImS.upload(imsigma, n, s);
+    scgd0_imsigma(P, P->d_Sin.p, mu, T, P->d_ImS.p);
+    P->d_ImS.download(imsigma, n, s);
+    EPSP_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+}  // extern "C"

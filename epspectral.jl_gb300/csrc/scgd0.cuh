@@ -1,0 +1,47 @@
+// scgd0.cuh -- the scGD0 plan object shared by scgd0.cu and the tensor-core path (scgd0_tc.cu).
+#pragma once
+
+#include "common.cuh"
+
+#include <memory>
+
+namespace epsp {
+
+struct Scgd0Plan {
+  Ctx* ctx = nullptr;
+  int path = EPSP_PATH_DIRECT_FP64;
+  int verbosity = 0;
+  double w_ac = 0;
+  int64_t gpu_tile = 0;
+  long nm = 0, ni = 0, nf = 0, nw = 0, nwa = 0;
+  double W = 0, nstates_base = 0;
+  GridHost ws, wsa;
+  // grid tables
+  DBuf<int32_t> d_jtab, d_jsp;
+  DBuf<double> d_ws, d_wsa, d_tsp, d_Wa, d_eps_i, d_w_i, d_KK;
+  CellTableDev ct{};
+  long nmult = 0;
+  DBuf<int32_t> d_mptr, d_midx;
+  // DIRECT_FP64
+  int64_t nf_chunk = 1;
+  DBuf<double> d_g2t, d_wqt, d_eps_f, d_w_f;
+  DBuf<int32_t> d_f_to_i;
+  // GEMM paths
+  bool star_reduced = false;
+  long nc = 0;
+  DBuf<double> d_wnu, d_epsc, d_G, d_Fa, d_Fe, d_Kt;
+  DBuf<int32_t> d_colc;
+  // tensor-core path state (scgd0_tc.cu)
+  struct Tc;
+  std::unique_ptr<Tc, void (*)(Tc*)> tc{nullptr, [](Tc*) {}};
+  // iteration buffers
+  DBuf<double2> d_Sin;
+  DBuf<double> d_ImS, d_ReS, d_A, d_colsum, d_D;
+};
+
+// Tensor-core (BF16x3) pieces of the GEMM_BF16X3 path, in scgd0_tc.cu.
+void tc_setup(Scgd0Plan* P);
+void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS);
+void tc_kk_assemble(Scgd0Plan* P, double2* d_Snew);
+
+}  // namespace epsp

@@ -1,0 +1,196 @@
+// scgd0_tc.cu -- the GEMM_BF16X3 path of the scGD0 iteration: the kernel tensor written directly as
+// BF16 hi/lo operands, the Fan-Migdal contraction and the Kramers-Kronig map on the tcgen05 tensor
+// cores (tc_gemm.cuh), split-K partials summed in fixed order.
+//
+//   ImΣ[ω, i] = Σ_k K_t[ω, k] G[k, i]      A = K_t  [nω][Kp]  (K-major),  B = G^T [ni][Kp]
+//   ReΣ[ω, i] = Σ_ω' KK[ω, ω'] ImΣ[ω', i]   A = KK   [nω][Kp2],           B = ImΣ^T [ni][Kp2]
+#include "scgd0.cuh"
+#include "tc_gemm.cuh"
+
+#include <algorithm>
+
+namespace epsp {
+
+struct Scgd0Plan::Tc {
+  long Kp = 0, Kp2 = 0;
+  int splits1 = 1, splits2 = 1, bn1 = 128, bn2 = 128;
+  DBuf<__nv_bfloat16> Kt_h, Kt_l, G_h, G_l, KK_h, KK_l, Im_h, Im_l;
+  DBuf<float> part;
+  DBuf<int> err;
+  TcOperand opK, opG, opKK, opIm;
+};
+
+// x = hi + lo + O(2^-16 |x|) with hi, lo BF16.
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(x);
+  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+
+// Kernel tensor of the recast Fan-Migdal sum (see kbuild_f64_kernel in scgd0.cu), written as BF16
+// hi/lo rows K_t[ω][k] through a shared-memory transpose. The differences x - ε - Re Σ stay FP64
+// (they cancel near the quasiparticle pole); the reciprocal and the occupation products are FP32,
+// below the BF16x3 rounding of the contraction.
+__global__ void __launch_bounds__(256) kbuild_bf16_kernel(const double* __restrict__ ws, int nw, CellTableDev ct,
+                                                          const double2* __restrict__ Sin, const double* __restrict__ wnu,
+                                                          int nm, const double* __restrict__ eps_c,
+                                                          const int32_t* __restrict__ col_c, long nk,
+                                                          const double* __restrict__ Fa, const double* __restrict__ Fe,
+                                                          double w_ac, __nv_bfloat16* __restrict__ Kh,
+                                                          __nv_bfloat16* __restrict__ Kl, long Kp) {
+  __shared__ float tile[64][33];
+  const int w0 = blockIdx.x * 32;
+  const long k0 = long(blockIdx.y) * 64;
+  const int tw = threadIdx.x % 32, tk = threadIdx.x / 32;
+  const int iw = w0 + tw;
+  const double w = iw < nw ? ws[iw] : 0.0;
+#pragma unroll 1
+  for (int r = 0; r < 8; ++r) {
+    const int kl = tk + 8 * r;
+    const long k = k0 + kl;
+    float v = 0.f;
+    if (iw < nw && k < nk) {
+      const int nu = int(k % nm);
+      const long c = k / nm;
+      const double q = wnu[nu];
+      if (!(q < w_ac)) {
+        const double2* col = Sin + long(nw) * col_c[c];
+        const double e = eps_c[c];
+        const double xa = w + q, xe = w - q;
+        const double2 sa = interp_grid_d(col, ct, xa);
+        const double2 se = interp_grid_d(col, ct, xe);
+        const float zar = float(xa - e - sa.x), zai = float(-sa.y);
+        const float zer = float(xe - e - se.x), zei = float(-se.y);
+        const float ga = -zai / (zar * zar + zai * zai);
+        const float ge = -zei / (zer * zer + zei * zei);
+        v = ga * float(Fa[iw + long(nw) * nu]) + ge * float(Fe[iw + long(nw) * nu]);
+      }
+    }
+    tile[kl][tw] = v;
+  }
+  __syncthreads();
+  const int wr = threadIdx.x / 8, kc = (threadIdx.x % 8) * 8;
+  const int ow = w0 + wr;
+  if (ow < nw) {
+    __align__(16) __nv_bfloat16 h[8], l[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) split_bf16(tile[kc + j][wr], h[j], l[j]);
+    const long off = long(ow) * Kp + k0 + kc;
+    *reinterpret_cast<uint4*>(Kh + off) = *reinterpret_cast<const uint4*>(h);
+    *reinterpret_cast<uint4*>(Kl + off) = *reinterpret_cast<const uint4*>(l);
+  }
+}
+
+// out[r * ld + c] = split(src(r, c)) for c < cols, 0 for cols <= c < ld; src(r, c) = S[c + ldc * r]
+// (a column-major matrix read transposed: rows of the output are columns of S).
+__global__ void split_rows_kernel(const double* __restrict__ S, long ldc, long rows, long cols, long ld,
+                                  __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= rows * ld) return;
+  long r = idx / ld, c = idx % ld;
+  float x = c < cols ? float(S[c + ldc * r]) : 0.f;
+  split_bf16(x, oh[idx], ol[idx]);
+}
+
+// Transposed split: out[r * ld + c] = split(S[r + ldr * c]) (rows of the output are rows of S).
+__global__ void split_rows_t_kernel(const double* __restrict__ S, long ldr, long rows, long cols, long ld,
+                                    __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= rows * ld) return;
+  long r = idx / ld, c = idx % ld;
+  float x = c < cols ? float(S[r + ldr * c]) : 0.f;
+  split_bf16(x, oh[idx], ol[idx]);
+}
+
+// ImΣ (FP64) += Σ_s part[s] in ascending s.
+__global__ void finalize_add_kernel(const float* __restrict__ part, long n, int splits, long stride, double* __restrict__ out) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  float s = 0.f;
+  for (int p = 0; p < splits; ++p) s += part[k + stride * p];
+  out[k] += double(s);
+}
+
+// Σ_new = Σ_s part[s] + i ImΣ.
+__global__ void finalize_assemble_kernel(const float* __restrict__ part, long n, int splits, long stride,
+                                         const double* __restrict__ im, double2* __restrict__ out) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  float s = 0.f;
+  for (int p = 0; p < splits; ++p) s += part[k + stride * p];
+  out[k] = make_double2(double(s), im[k]);
+}
+
+static long pad64(long x) { return (x + 63) / 64 * 64; }
+
+void tc_setup(Scgd0Plan* P) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  auto* T = new Scgd0Plan::Tc;
+  P->tc = std::unique_ptr<Scgd0Plan::Tc, void (*)(Scgd0Plan::Tc*)>(T, [](Scgd0Plan::Tc* t) { delete t; });
+  const long nw = P->nw, ni = P->ni, nk = P->nm * P->nc;
+  T->Kp = pad64(nk);
+  T->Kp2 = pad64(nw);
+  if (nw > (1l << 30) || ni > (1l << 30) || nk > (1l << 30)) fail(EPSP_EINVAL, "sizes beyond the 32-bit tile grid");
+  T->Kt_h.alloc(ctx, size_t(nw * T->Kp));
+  T->Kt_l.alloc(ctx, size_t(nw * T->Kp));
+  T->G_h.alloc(ctx, size_t(ni * T->Kp));
+  T->G_l.alloc(ctx, size_t(ni * T->Kp));
+  T->KK_h.alloc(ctx, size_t(nw * T->Kp2));
+  T->KK_l.alloc(ctx, size_t(nw * T->Kp2));
+  T->Im_h.alloc(ctx, size_t(ni * T->Kp2));
+  T->Im_l.alloc(ctx, size_t(ni * T->Kp2));
+  T->err.alloc(ctx, 1);
+  T->err.zero(s);
+  // B of the contraction: G [nk, ni] column-major is G^T row-major [ni][nk].
+  split_rows_kernel<<<div_up(size_t(ni * T->Kp), 256), 256, 0, s>>>(P->d_G.p, nk, ni, nk, T->Kp, T->G_h.p, T->G_l.p);
+  EPSP_LAUNCHED(ctx);
+  // A of the Kramers-Kronig map: A[ω][ω'] = KK[ω + nω ω'].
+  split_rows_t_kernel<<<div_up(size_t(nw * T->Kp2), 256), 256, 0, s>>>(P->d_KK.p, nw, nw, nw, T->Kp2, T->KK_h.p, T->KK_l.p);
+  EPSP_LAUNCHED(ctx);
+  tc_gemm_shape(ctx, int(nw), int(ni), int(nk), 16, &T->bn1, &T->splits1);
+  tc_gemm_shape(ctx, int(nw), int(ni), int(nw), 16, &T->bn2, &T->splits2);
+  T->part.alloc(ctx, size_t(std::max(T->splits1, T->splits2)) * size_t(nw * ni));
+  T->opK = {make_tmap_bf16(T->Kt_h.p, nw, nk, T->Kp, kTcBM), make_tmap_bf16(T->Kt_l.p, nw, nk, T->Kp, kTcBM)};
+  T->opG = {make_tmap_bf16(T->G_h.p, ni, nk, T->Kp, T->bn1), make_tmap_bf16(T->G_l.p, ni, nk, T->Kp, T->bn1)};
+  T->opKK = {make_tmap_bf16(T->KK_h.p, nw, nw, T->Kp2, kTcBM), make_tmap_bf16(T->KK_l.p, nw, nw, T->Kp2, kTcBM)};
+  T->opIm = {make_tmap_bf16(T->Im_h.p, ni, nw, T->Kp2, T->bn2), make_tmap_bf16(T->Im_l.p, ni, nw, T->Kp2, T->bn2)};
+}
+
+static void check_err(Scgd0Plan* P) {
+  int e = 0;
+  P->tc->err.download(&e, 1, P->ctx->stream);
+  EPSP_CUDA(cudaStreamSynchronize(P->ctx->stream));
+  if (e) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+}
+
+void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  auto* T = P->tc.get();
+  const long nw = P->nw, ni = P->ni, nk = P->nm * P->nc;
+  long pk = prof_begin(ctx, "kbuild");
+  kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), 32), unsigned(T->Kp / 64)), 256, 0, s>>>(
+      P->d_ws.p, int(nw), P->ct, d_Sin, P->d_wnu.p, int(P->nm), P->d_epsc.p, P->d_colc.p, nk, P->d_Fa.p, P->d_Fe.p,
+      P->w_ac, T->Kt_h.p, T->Kt_l.p, T->Kp);
+  EPSP_LAUNCHED(ctx);
+  prof_end(ctx, pk);
+  const long slab = nw * ni;
+  int sp = tc_gemm_launch(ctx, T->opK, T->opG, int(nw), int(ni), int(nk), T->part.p, nw, slab, 16, T->err.p);
+  finalize_add_kernel<<<div_up(size_t(slab), 256), 256, 0, s>>>(T->part.p, slab, sp, slab, d_ImS);
+  EPSP_LAUNCHED(ctx);
+  check_err(P);
+}
+
+void tc_kk_assemble(Scgd0Plan* P, double2* d_Snew) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  auto* T = P->tc.get();
+  const long nw = P->nw, ni = P->ni, slab = nw * ni;
+  split_rows_kernel<<<div_up(size_t(ni * T->Kp2), 256), 256, 0, s>>>(P->d_ImS.p, nw, ni, nw, T->Kp2, T->Im_h.p, T->Im_l.p);
+  EPSP_LAUNCHED(ctx);
+  int sp = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(ni), int(nw), T->part.p, nw, slab, 16, T->err.p);
+  finalize_assemble_kernel<<<div_up(size_t(slab), 256), 256, 0, s>>>(T->part.p, slab, sp, slab, P->d_ImS.p, d_Snew);
+  EPSP_LAUNCHED(ctx);
+}
+
+}  // namespace epsp

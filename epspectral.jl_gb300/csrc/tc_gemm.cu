@@ -1,0 +1,80 @@
+// tc_gemm.cu -- host side of the tcgen05 BF16x3 GEMM: tensor maps, tile shape and split-K choice.
+#include "tc_gemm.cuh"
+
+#include <algorithm>
+#include <mutex>
+
+namespace epsp {
+
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  if (!fn) fail(EPSP_ECUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  return fn;
+}
+
+CUtensorMap make_tmap_bf16(const void* base, long rows, long cols, long ld, int box_rows) {
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || (ld * 2) % 16 != 0)
+    fail(EPSP_EINVAL, "tensor map base and row stride must be 16-byte aligned");
+  CUtensorMap m;
+  cuuint64_t dims[2] = {cuuint64_t(cols), cuuint64_t(rows)};
+  cuuint64_t strides[1] = {cuuint64_t(ld * 2)};
+  cuuint32_t box[2] = {cuuint32_t(kTcBK), cuuint32_t(box_rows)};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) fail(EPSP_ECUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string(int(r)));
+  return m;
+}
+
+void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int* bn, int* splits) {
+  const int BN = N > 128 ? 256 : 128;
+  const int tiles = ((M + kTcBM - 1) / kTcBM) * ((N + BN - 1) / BN);
+  const int kblocks = (K + kTcBK - 1) / kTcBK;
+  int sp = std::max(1, (ctx->sm_count + tiles - 1) / tiles);
+  sp = std::min({sp, std::max(1, max_splits), std::max(1, kblocks)});
+  const int per = (kblocks + sp - 1) / sp;
+  sp = std::max(1, (kblocks + per - 1) / per);
+  *bn = BN;
+  *splits = sp;
+}
+
+template <int BN, int STAGES>
+static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int kblocks, int per, int splits,
+                   float* out, long ld_out, long split_stride, int* d_err) {
+  using L = TcSmem<BN, STAGES>;
+  static bool configured = false;  // one process, one attribute setting per instantiation
+  if (!configured) {
+    EPSP_CUDA(cudaFuncSetAttribute(tc_gemm_bf16x3_kernel<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::kBytes));
+    configured = true;
+  }
+  dim3 grid((M + kTcBM - 1) / kTcBM, (N + BN - 1) / BN, splits);
+  tc_gemm_bf16x3_kernel<BN, STAGES><<<grid, 128, L::kBytes, ctx->stream>>>(A.hi, A.lo, B.hi, B.lo, M, N, kblocks, per, out,
+                                                                           ld_out, split_stride, d_err);
+  EPSP_LAUNCHED(ctx);
+}
+
+int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int K, float* out, long ld_out,
+                   long split_stride, int max_splits, int* d_err) {
+  int BN, splits;
+  tc_gemm_shape(ctx, M, N, K, max_splits, &BN, &splits);
+  const int kblocks = (K + kTcBK - 1) / kTcBK;
+  const int per = (kblocks + splits - 1) / splits;
+  long pi = prof_begin(ctx, "tc_gemm");
+  if (BN == 256)
+    launch<256, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+  else
+    launch<128, 3>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+  prof_end(ctx, pi);
+  return splits;
+}
+
+}  // namespace epsp

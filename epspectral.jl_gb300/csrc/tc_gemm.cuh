@@ -1,0 +1,249 @@
+// tc_gemm.cuh -- BF16x3 split-precision GEMM on the sm_103a tensor cores (tcgen05 + TMA + TMEM).
+//
+//   D[m, n] (FP32) = Σ_k A[m, k] B[n, k]   with   A ≈ A_hi + A_lo,  B ≈ B_hi + B_lo  (BF16 each)
+//   evaluated as A_hi·B_hi + A_hi·B_lo + A_lo·B_hi, all three products accumulated in one TMEM
+//   accumulator (FP32). A [M][K] and B [N][K] are row-major with K contiguous ("K-major"), row
+//   stride `ldk` elements (a multiple of 8, so rows start on 16-byte boundaries).
+//
+// One CTA of 128 threads computes a 128 x BN tile of D over a range of 64-wide K blocks (split-K
+// over blockIdx.z; each split writes its own FP32 slab, summed afterwards in fixed order):
+//   warp 0, lane 0 : TMA producer, a ring of STAGES stages [A_hi | A_lo | B_hi | B_lo] with
+//                    128-byte swizzle, completion through mbarriers (expect_tx);
+//   warp 1, lane 0 : issues tcgen05.mma (M = 128, N = BN, K = 16 per instruction, three per K step)
+//                    and tcgen05.commit to release a stage and, at the end, to signal the epilogue;
+//   warps 0-3      : epilogue, tcgen05.ld of TMEM lanes 32w..32w+31 into registers, masked stores.
+// Every mbarrier wait is bounded; on timeout the kernel records the error in *err and winds down
+// (waits, again bounded, for its own copies and MMAs, frees TMEM and returns).
+#pragma once
+
+#include "common.cuh"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+namespace epsp {
+
+constexpr int kTcBM = 128, kTcBK = 64;
+constexpr unsigned kWaitLimit = 1u << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred P1;\nmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\nselp.b32 %0, 1, 0, P1;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for the phase of parity `parity` to complete; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (unsigned it = 0; it < kWaitLimit; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (it > 64) __nanosleep(64);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(map), "r"(c0), "r"(c1), "r"(bar)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major operand tile with 128-byte swizzle: rows of 128 B
+// (64 BF16), 8-row groups 1024 B apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  return uint64_t((addr >> 4) & 0x3FFF) | (uint64_t(1024 >> 4) << 32) | (uint64_t(1) << 46) | (uint64_t(2) << 61);
+}
+
+// Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 lanes x 32 columns of 32-bit values from TMEM: thread `lane` gets row (lane base + lane),
+// columns col..col+31.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,"
+      "%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+template <int BN, int STAGES>
+struct TcSmem {
+  static constexpr int kA = kTcBM * kTcBK * 2;   // bytes of one A tile
+  static constexpr int kB = BN * kTcBK * 2;      // bytes of one B tile
+  static constexpr int kStage = 2 * kA + 2 * kB;
+  static constexpr int kBars = 2 * STAGES + 1;
+  static constexpr int kBytes = STAGES * kStage + 8 * kBars + 16 + 1024;  // + alignment slack
+};
+
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(128, 1)
+    tc_gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+                          const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, int M, int N,
+                          int kblocks, int kb_per_split, float* __restrict__ out, long ld_out, long split_stride,
+                          int* __restrict__ err) {
+  using L = TcSmem<BN, STAGES>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * L::kStage);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + L::kBars);
+  __shared__ int s_abort;
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES), done_bar = smem_u32(bars + 2 * STAGES);
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * BN;
+  const int kb0 = blockIdx.z * kb_per_split;
+  const int nkb = max(0, min(kblocks, kb0 + kb_per_split) - kb0);
+
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int s = 0; s < 2 * STAGES + 1; ++s) mbar_init(smem_u32(bars + s), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)), "r"(BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // producer
+    int issued = 0;
+    for (int kb = 0; kb < nkb; ++kb) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (kb / STAGES) & 1;
+      if (kb >= STAGES && !mbar_wait(empty0 + 8 * s, ph ^ 1)) {
+        atomicExch(&s_abort, 1);
+        break;
+      }
+      if (*(volatile int*)&s_abort) break;
+      uint8_t* st = smem + s * L::kStage;
+      const uint32_t fb = full0 + 8 * s;
+      mbar_expect_tx(fb, L::kStage);
+      const int kc = (kb0 + kb) * kTcBK;
+      tma_load_2d(smem_u32(st), &mAh, kc, m0, fb);
+      tma_load_2d(smem_u32(st + L::kA), &mAl, kc, m0, fb);
+      tma_load_2d(smem_u32(st + 2 * L::kA), &mBh, kc, n0, fb);
+      tma_load_2d(smem_u32(st + 2 * L::kA + L::kB), &mBl, kc, n0, fb);
+      issued = kb + 1;
+    }
+    if (*(volatile int*)&s_abort) {
+      // wind down: wait (bounded) for the copies this thread issued into stages not yet consumed
+      for (int kb = max(0, issued - STAGES); kb < issued; ++kb) mbar_wait(full0 + 8 * (kb % STAGES), (kb / STAGES) & 1);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    constexpr uint32_t idesc = idesc_bf16_f32(BN);
+    for (int kb = 0; kb < nkb; ++kb) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (kb / STAGES) & 1;
+      if (!mbar_wait(full0 + 8 * s, ph)) {
+        atomicExch(&s_abort, 1);
+        break;
+      }
+      if (*(volatile int*)&s_abort) break;
+      tc_fence_after();
+      const uint32_t a_h = smem_u32(smem + s * L::kStage);
+      const uint32_t a_l = a_h + L::kA, b_h = a_h + 2 * L::kA, b_l = b_h + L::kB;
+#pragma unroll
+      for (int ks = 0; ks < kTcBK / 16; ++ks) {
+        const uint32_t off = ks * 32;  // 16 BF16 along K inside the 128-byte swizzle row
+        const uint64_t dah = sw128_desc(a_h + off), dal = sw128_desc(a_l + off);
+        const uint64_t dbh = sw128_desc(b_h + off), dbl = sw128_desc(b_l + off);
+        umma_bf16(tmem, dah, dbh, idesc, (kb | ks) != 0);
+        umma_bf16(tmem, dah, dbl, idesc, 1);
+        umma_bf16(tmem, dal, dbh, idesc, 1);
+      }
+      umma_commit(empty0 + 8 * s);
+    }
+    umma_commit(done_bar);  // completes when every MMA issued above has
+  }
+  __syncwarp();
+  // epilogue
+  bool ok = true;
+  if (!mbar_wait(done_bar, 0)) {
+    ok = false;
+    atomicExch(&s_abort, 1);
+  }
+  tc_fence_after();
+  __syncthreads();
+  const bool aborted = *(volatile int*)&s_abort != 0;
+  if (aborted && threadIdx.x == 0) atomicExch(err, 1);
+  if (!aborted && ok) {
+    const int row = m0 + warp * 32 + lane;
+    float* o = out + long(blockIdx.z) * split_stride;
+#pragma unroll 1
+    for (int c = 0; c < BN; c += 32) {
+      float v[32];
+      tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
+      if (nkb == 0) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = 0.f;
+      }
+      if (row < M) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int n = n0 + c + j;
+          if (n < N) o[row + ld_out * long(n)] = v[j];
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+}
+
+// ---- host side ----
+
+// A 2-D BF16 tensor map over a row-major [rows][ld] array (K contiguous, rows of `cols` valid
+// elements), box = 64 x box_rows, 128-byte swizzle; out-of-range elements read as zero.
+CUtensorMap make_tmap_bf16(const void* base, long rows, long cols, long ld, int box_rows);
+
+struct TcOperand {
+  CUtensorMap hi, lo;
+};
+
+// Launches D = A_hi B_hi + A_hi B_lo + A_lo B_hi for A [M][K], B [N][K] (K-major) into the
+// FP32 slabs out[split][m + ld_out n]; returns the number of splits used.
+int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int K, float* out, long ld_out,
+                   long split_stride, int max_splits, int* d_err);
+
+// The BN and split count tc_gemm_launch picks for (M, N, K) with at most max_splits splits.
+void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int* bn, int* splits);
+
+}  // namespace epsp

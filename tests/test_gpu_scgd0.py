@@ -1,0 +1,133 @@
+"""GPU parity of the scGD0 path: the CUDA library through its C ABI against the oracle.
+
+Tolerances: the plain FP64 paths (DIRECT_FP64, GEMM_FP64) match the oracle to 1e-10 relative in Σ
+and μ (the reference's own GPU-vs-host gate, test/test_scgd0_gpu.jl:36-37) and are bitwise
+reproducible run to run (test/test_scgd0_gpu.jl:38-40). The BF16x3 tensor-core path matches to
+|ΔΣ| <= 1e-5 eV and |Δμ| <= 1e-5 eV.
+"""
+import numpy as np
+import pytest
+
+import refimpl as R
+from epspectral_gb300 import ArgumentError, FrequencyGrid, graded_frequency_grid, synthetic
+
+pytestmark = pytest.mark.gpu
+
+W_AC = 1e-6
+
+
+@pytest.fixture(scope="module")
+def api():
+    from epspectral_gb300 import api as A
+    A.lib()
+    return A
+
+
+def occ(nlist=0.0, Tlist=(0.1,), typ="metal", nelec=1.0):
+    return dict(Tlist=list(Tlist), nlist=[nlist] * len(Tlist), nelec=nelec, spin_degeneracy=2.0, type=typ)
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
+
+
+def test_fan_migdal_sum_matches_oracle(api, oracle):
+    # the case of test/test_scgd0_kernel.jl: per-pair ωq, an Inf coupling below ω_acoustic, a
+    # random f -> i map, accumulation into a nonzero Im Σ, a graded grid.
+    from test_oracle_scgd0 import per_pair_setup
+    nm, ni, nf = 3, 13, 17
+    g = FrequencyGrid.from_nodes(np.concatenate([np.arange(-1.0, -0.5999, 0.02), np.arange(-0.5, 0.5001, 0.1),
+                                                 np.arange(0.6, 1.0001, 0.02)]))
+    nw = len(g)
+    Sin = 0.1 * R.pseudorandom(nw, ni, seed=7) + 1j * (-0.05 - 0.05 * np.abs(R.pseudorandom(nw, ni, seed=8)))
+    g2 = np.abs(R.pseudorandom(nm, ni, nf, seed=9))
+    wq = 0.05 + 0.2 * np.abs(R.pseudorandom(nm, ni, nf, seed=10))
+    wq[1, 2, :] = 0.0
+    g2[1, 2, :] = np.inf
+    s = per_pair_setup(g, g2, wq, 0.8 * R.pseudorandom(nf, seed=11),
+                       np.array([(5 * (f + 1)) % ni for f in range(nf)], dtype=np.int32), np.full(nf, 1.0 / nf))
+    for tile in (None, 5):
+        ref = oracle.imsigma(s, Sin, 0.07, 0.03, np.full((nw, ni), 0.5), omega_acoustic=1e-3, gpu_tile=tile)
+        plan = api.Scgd0Plan(s, path="direct_fp64", gpu_tile=tile, omega_acoustic=1e-3)
+        got = plan.imsigma(Sin, 0.07, 0.03, np.full((nw, ni), 0.5))
+        assert np.all(np.isfinite(got))
+        assert rel(got, ref) <= 1e-13
+
+
+@pytest.fixture(scope="module")
+def holstein_gpu():
+    ws = FrequencyGrid.from_nodes(np.arange(-200, 201) * 0.02)
+    return synthetic.holstein_1d_setup(64, 1.0, 0.2, 0.2, ws)
+
+
+@pytest.mark.parametrize("nlist", [0.0, -0.3])
+def test_holstein_loop_matches_oracle(api, oracle, holstein_gpu, nlist):
+    s = holstein_gpu
+    kw = dict(eta_init=0.05, tol=1e-6, maxiter=30, mu_start=[0.0], omega_acoustic=W_AC)
+    ref = oracle.loop_scgd0(s, occ(nlist), **kw)
+    for path in ("direct_fp64", "gemm_fp64"):
+        got = api.loop_scgd0(s, occ(nlist), path=path, **kw)
+        assert got["niter"] == ref["niter"] and list(got["converged"]) == list(ref["converged"])
+        assert rel(got["sigma"], ref["sigma"]) <= 1e-10
+        assert abs(got["mu"][0] - ref["mu"][0]) <= 1e-10 * max(1.0, abs(ref["mu"][0]))
+        again = api.loop_scgd0(s, occ(nlist), path=path, **kw)
+        assert np.array_equal(again["sigma"], got["sigma"]) and np.array_equal(again["mu"], got["mu"])
+    tiled = api.loop_scgd0(s, occ(nlist), path="direct_fp64", gpu_tile=7, **kw)
+    assert rel(tiled["sigma"], ref["sigma"]) <= 1e-10
+    bf = api.loop_scgd0(s, occ(nlist), path="gemm_bf16x3", **kw)
+    assert np.max(np.abs(bf["sigma"] - ref["sigma"])) <= 1e-5
+    assert abs(bf["mu"][0] - ref["mu"][0]) <= 1e-5
+
+
+@pytest.fixture(scope="module")
+def cubic_small():
+    ws = graded_frequency_grid([(-0.3, 0.3, 0.01), (-1.5, 1.5, 0.05)])
+    return synthetic.cubic_t2g_setup(N=4, ws=ws, g2_dtype=np.float32, seed=5)
+
+
+def test_cubic_loop_matches_oracle(api, oracle, cubic_small):
+    # two temperatures with their own η_min, multiplets, several modes, stars: three iterations
+    # with the μ update, never converged (tol = 0), as test/test_scgd0_gpu.jl:9-11.
+    s = cubic_small
+    assert len(s["multiplets"]) > 0
+    o = occ(0.0, Tlist=(300 * synthetic.KELVIN, 600 * synthetic.KELVIN))
+    kw = dict(eta_init=0.05, eta_min=[0.0, 0.03], tol=0.0, maxiter=3, mu_start=[-0.5, -0.5], omega_acoustic=W_AC)
+    ref = oracle.loop_scgd0(s, o, **kw)
+    for path in ("direct_fp64", "gemm_fp64"):
+        got = api.loop_scgd0(s, o, path=path, **kw)
+        assert rel(got["sigma"], ref["sigma"]) <= 1e-10
+        assert np.allclose(got["mu"], ref["mu"], rtol=1e-10, atol=1e-12)
+        assert np.allclose(got["history"]["err"], ref["history"]["err"], rtol=1e-8)
+        assert np.allclose(got["history"]["min_spectral_weight"], ref["history"]["min_spectral_weight"], rtol=1e-10)
+    bf = api.loop_scgd0(s, o, path="gemm_bf16x3", **kw)
+    assert np.max(np.abs(bf["sigma"] - ref["sigma"])) <= 1e-5
+    assert np.max(np.abs(bf["mu"] - ref["mu"])) <= 1e-5
+    gt = api.loop_scgd0(s, o, path="direct_fp64", gpu_tile=37, **kw)
+    assert rel(gt["sigma"], ref["sigma"]) <= 1e-10
+
+
+def test_errors_come_back_as_status(api, holstein_gpu, cubic_small):
+    s = holstein_gpu
+    with pytest.raises(ArgumentError, match="no chemical potential"):
+        api.loop_scgd0(s, occ(1.5), eta_init=0.05, tol=1e-6, maxiter=5, mu_start=[0.0], omega_acoustic=W_AC)
+    with pytest.raises(ArgumentError):
+        api.loop_scgd0(s, occ(0.0), eta_init=0.05, tol=1e-6, maxiter=0, mu_start=[0.0], omega_acoustic=W_AC)
+    with pytest.raises(ArgumentError):
+        api.loop_scgd0(s, occ(0.0), eta_init=0.05, tol=1e-6, maxiter=2, mu_start=[0.0], eta_min=[0.0, 0.0],
+                       omega_acoustic=W_AC)
+    with pytest.raises(ArgumentError):
+        api.loop_scgd0(s, occ(0.0), eta_init=0.05, tol=1e-6, maxiter=2, mu_start=[0.0],
+                       sigma_init=np.zeros((401, 33, 2), complex), omega_acoustic=W_AC)
+    # dispersive modes are refused by the recast paths, accepted by the direct one
+    disp = dict(s, omega_ph=np.asfortranarray(0.2 + 0.01 * np.arange(64.0)[None, :]))
+    with pytest.raises(api.EpspError, match="dispersionless"):
+        api.Scgd0Plan(disp, path="gemm_bf16x3", omega_acoustic=W_AC)
+    api.Scgd0Plan(disp, path="direct_fp64", omega_acoustic=W_AC).close()
+    # a device allocation failure is reported, and the context stays usable
+    ctx = api.Context(0)
+    ctx.fail_next_alloc(1)
+    with pytest.raises(api.EpspError, match="ENOMEM"):
+        api.Scgd0Plan(s, path="direct_fp64", omega_acoustic=W_AC, ctx=ctx)
+    r = api.loop_scgd0(s, occ(0.0), eta_init=0.05, tol=1e-6, maxiter=2, mu_start=[0.0], omega_acoustic=W_AC, ctx=ctx)
+    assert r["niter"] == 2
+    assert ctx.kernel_launches > 0
