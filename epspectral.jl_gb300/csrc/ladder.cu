@@ -1,0 +1,1242 @@
+// ladder.cu -- the ladder plan: setup (_setup_ladder + _ladder_workspace, src/ladder.jl:112-233),
+// one application of the ladder kernel (apply_ladder_kernel!, src/ladder.jl:245-296) and the (T, Ω)
+// solves (_loop_ladder, src/ladder.jl:303-379) on one GPU.
+//
+// Index legend and layouts as in the reference (src/ladder_kernel.jl:1-13), column-major:
+//   J, LJ, J0   [nω, 4, 3, 2, ni] double2   (ω, c12, cart, c0, i)
+//   Gm, Gp      [nω, 4, ni] double2
+// DIRECT_FP64 follows the reference's shift grid:
+//   B̃ [nshift·3·ni, 6 ni] per temperature (the star-summed coupling of every chunk, kept for all
+//   the solves at that temperature: it depends on T only), X [16 nω, nshift·3·nip] per chunk and
+//   sign, C± [16 nω, 6 ni] += X B̃, the four channels with the Kramers-Kronig image, then
+//   LJ = -Gm K Gp.
+// GEMM_FP64 / GEMM_BF16X3 (dispersionless modes) regroup the shift sums per mode: a mode of
+// frequency ω_ν = (m_ν + r_ν) h contributes (1 - r_ν) S_{m_ν} + r_ν S_{m_ν+1}, the same two shift
+// tables and weights the shift grid gives it, so
+//   U±, V± [row, (a, i)] = Σ_{ν, b, i'} X±_ν[row, (ν, b, i')] (1 or n_ν) G̃[(ν, b, i'), (a, i)],
+//   G̃[(ν, b, i'), (a, i)] = Σ_{f in star(i')} R_f[a, b] w_f g2[ν, i, f]   (T-independent, setup),
+// and the channel combinations are folded into the A operand rows: 6 combinations q per
+// (c0, re/im) instead of the 16 of (c12, type) x sign, and K = nm·3·ni instead of nshift·3·ni.
+#include "common.cuh"
+#include "gemm_f64.cuh"
+#include "tc_gemm.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <complex>
+#include <limits>
+#include <memory>
+
+namespace epsp {
+
+using cplx = std::complex<double>;
+
+// ---------------------------------------------------------------------------------------------
+// plan
+// ---------------------------------------------------------------------------------------------
+
+struct LadderChunk {
+  long i0 = 0, i1 = 0;     // outer states [i0, i1)
+  long f0 = 0, f1 = 0;     // positions [f0, f1) in star order
+  long k_off = 0;          // row offset of the chunk in B̃
+};
+
+struct LadderPlan {
+  Ctx* ctx = nullptr;
+  int path = EPSP_PATH_DIRECT_FP64;
+  double w_ac = 0, h = 0;
+  long nm = 0, ni = 0, nf = 0, nw = 0, nshift = 0;
+  GridHost ws;
+  std::vector<double> Ww_h, v_h, w_i_h, wnu;
+  std::vector<int32_t> m_nu;
+  std::vector<double> r_nu;
+  DBuf<double> d_ws, d_Ww, d_KK, d_eps_i, d_v;
+  // DIRECT_FP64
+  std::vector<LadderChunk> chunks;
+  DBuf<int32_t> d_by_star, d_star_ptr, d_klo;
+  DBuf<double> d_wlo, d_whi, d_g2, d_wq, d_wf, d_R, d_B, d_Bt, d_X, d_Cp, d_Cm;
+  long Ktot = 0;
+  double Bt_T = std::numeric_limits<double>::quiet_NaN();  // temperature B̃ was built for
+  // GEMM paths
+  long Kx = 0, Kp = 0;
+  DBuf<double> d_Gt, d_Af, d_D;   // G̃ [Kx, 3ni]; A (FP64) [24nω, Kx]; D [24nω, 3ni]
+  DBuf<int32_t> d_mnu;
+  DBuf<double> d_rnu, d_nnu;
+  DBuf<__nv_bfloat16> d_Ah, d_Al, d_Gh, d_Gl;
+  DBuf<float> d_part;
+  DBuf<int> d_err;
+  TcOperand opA{}, opG{};
+  int bn = 128, splits = 1;
+  // exchange (both paths)
+  DBuf<double> d_Y, d_KY;
+  // per (T, Ω)
+  DBuf<double2> d_Gm, d_Gp, d_Sm, d_Sp, d_ST;
+  DBuf<int32_t> d_jm, d_jp;
+  DBuf<double> d_tm, d_tp;
+  double cur_T = 0, cur_mu = 0, cur_Om = 0;
+};
+
+// ---------------------------------------------------------------------------------------------
+// element kernels
+// ---------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ long jidx(long nw, long w, int c12, int cart, int c0, long i) {
+  return w + nw * (c12 + 4 * (cart + 3 * (c0 + 2 * i)));
+}
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+
+// Julia's inv(::ComplexF64) (Smith's algorithm).
+__device__ __forceinline__ double2 cinv_d(double c, double d) {
+  if (fabs(d) <= fabs(c)) {
+    double r = d / c, t = 1.0 / (c + d * r);
+    return make_double2(t, -r * t);
+  }
+  double r = c / d, t = 1.0 / (d + c * r);
+  return make_double2(r * t, -t);
+}
+
+// contour_greens! (src/ladder_kernel.jl:27-57) of the self-energy read at ωs ∓ Ω/2 by the
+// interpolation tables (jm, tm), (jp, tp) (src/ladder.jl:321-334).
+__global__ void propagators_kernel(const double2* __restrict__ ST, const double* __restrict__ ws, int nw,
+                                   const int32_t* __restrict__ jm, const double* __restrict__ tm,
+                                   const int32_t* __restrict__ jp, const double* __restrict__ tp,
+                                   const double* __restrict__ eps_i, double mu, double T, double Om,
+                                   double2* __restrict__ Gm, double2* __restrict__ Gp, int ni) {
+  int w = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y;
+  if (w >= nw) return;
+  const double2* col = ST + long(nw) * i;
+  for (int side = 0; side < 2; ++side) {
+    int j = side == 0 ? jm[w] : jp[w];
+    double t = side == 0 ? tm[w] : tp[w];
+    double2 lo = col[j], hi = col[j + 1];
+    double sr = (1 - t) * lo.x + t * hi.x, si = (1 - t) * lo.y + t * hi.y;
+    double x = side == 0 ? ws[w] - Om / 2 : ws[w] + Om / 2;
+    double2 GR = cinv_d(x - eps_i[i] - sr, -si);
+    double2 GA = make_double2(GR.x, -GR.y);
+    double fac = 1 - 2 * occ_fermion_d(x - mu, T);
+    double2 GK = cscale(csub(GR, GA), fac);
+    double2 g[4] = {cscale(cadd(cadd(GR, GA), GK), 0.5), cscale(cadd(csub(GR, GA), GK), 0.5),
+                    cscale(cadd(csub(GA, GR), GK), 0.5), cscale(csub(csub(GK, GR), GA), 0.5)};
+    double2* G = side == 0 ? Gm : Gp;
+    for (int c = 0; c < 4; ++c) G[w + long(nw) * (c + 4 * i)] = g[c];
+  }
+}
+
+// attach_greens_to_bare_vertex! (src/ladder_kernel.jl:70-73, 97-99): J0^{c1c2,c0} = Gm^{c1c0} v Gp^{c0c2}.
+__global__ void attach_bare_kernel(const double2* __restrict__ Gm, const double2* __restrict__ Gp,
+                                   const double* __restrict__ v, int nw, int ni, double2* __restrict__ J0) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= long(nw) * 24 * ni) return;
+  long w = idx % nw;
+  long r = idx / nw;
+  int c12 = int(r % 4), cart = int((r / 4) % 3), c0 = int((r / 12) % 2);
+  long i = r / 24;
+  int c1 = c12 % 2, c2 = c12 / 2;
+  double2 a = Gm[w + long(nw) * (c1 + 2 * c0 + 4 * i)];
+  double2 b = Gp[w + long(nw) * (c0 + 2 * c2 + 4 * i)];
+  J0[idx] = cmul(cscale(a, v[cart + 3 * i]), b);
+}
+
+// Y[b, i] = Σ_ω Wω[ω] (J[ω, 22, b, c0=1, i] + J[ω, 11, b, c0=2, i]), the inner sum of
+// conductivity_from_vertex (src/ladder_kernel.jl:116-122); fixed-order block sum.
+__global__ void __launch_bounds__(256) cond_sum_kernel(const double2* __restrict__ J, const double* __restrict__ Ww, int nw,
+                                                       int ni, double2* __restrict__ Y) {
+  __shared__ double sr[256], si[256];
+  int b = blockIdx.x % 3;
+  long i = blockIdx.x / 3;
+  double ar = 0, ai = 0;
+  for (int w = threadIdx.x; w < nw; w += 256) {
+    double2 x = J[jidx(nw, w, 3, b, 0, i)], y = J[jidx(nw, w, 0, b, 1, i)];
+    ar += Ww[w] * (x.x + y.x);
+    ai += Ww[w] * (x.y + y.y);
+  }
+  sr[threadIdx.x] = ar;
+  si[threadIdx.x] = ai;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sr[threadIdx.x] += sr[threadIdx.x + s];
+      si[threadIdx.x] += si[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) Y[b + 3 * i] = make_double2(sr[0], si[0]);
+}
+
+// ---- DIRECT_FP64: the reference's shift grid ----
+
+// ωq of every (ν, inner state in star order, outer state) (gather_pair_table!, src/ladder.jl:259).
+__global__ void gather_wq_star_kernel(const double* __restrict__ wph, const int32_t* __restrict__ iq_kk,
+                                      const int32_t* __restrict__ iks_i, const int32_t* __restrict__ iks_f,
+                                      const int32_t* __restrict__ by_star, int nm, long nf, int ni, long nk_i,
+                                      double* __restrict__ wq) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= long(nm) * nf * ni) return;
+  int nu = int(idx % nm);
+  long fc = (idx / nm) % nf;
+  int i = int(idx / (long(nm) * nf));
+  long q = iq_kk[iks_i[i] + nk_i * long(iks_f[by_star[fc]])];
+  wq[idx] = wph[nu + long(nm) * q];
+}
+
+// bin_coupling_on_shift_grid! (src/ladder_kernel.jl:195-236) for the inner states [f0, f1) in star
+// order: B[m, fc, i, type] with each mode added to its two shifts in ascending ν, then times w_f.
+// One thread per (fc, i, type) column, which it owns.
+__global__ void bin_coupling_kernel(const double* __restrict__ g2, const double* __restrict__ wq, const int32_t* __restrict__ by_star,
+                                    const double* __restrict__ w_f, int nm, int ni, long nf, long f0, long nfc, int ns, double h,
+                                    double w_ac, double T, double* __restrict__ B) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= nfc * ni * 2) return;
+  long fc = idx % nfc;
+  int i = int((idx / nfc) % ni), type = int(idx / (nfc * ni));
+  double* col = B + long(ns) * idx;
+  for (int m = 0; m < ns; ++m) col[m] = 0.0;
+  long f = by_star[f0 + fc];
+  for (int nu = 0; nu < nm; ++nu) {
+    double w = wq[nu + long(nm) * ((f0 + fc) + nf * i)];
+    if (w < w_ac) continue;
+    double x = w / h;
+    long lo = long(floor(x));
+    double g = g2[nu + long(nm) * (i + long(ni) * f)];
+    for (long m = lo; m <= lo + 1; ++m) {
+      double c = g * fmax(0.0, 1 - fabs(x - double(m)));
+      if (m >= 0 && m < ns) col[m] += type == 0 ? c : c * occ_boson_d(w, T);
+    }
+  }
+  double wf = w_f[f];
+  for (int m = 0; m < ns; ++m) col[m] *= wf;
+}
+
+// star_sum_coupling! (src/ladder_kernel.jl:240-264) into the rows [k_off, k_off + ns·3·nip) of B̃:
+// B̃[(m, b, ip), (a, i, type)] = Σ_{fc in star(ip)} R[a, b, f] B[m, fc, i, type].
+__global__ void star_sum_kernel(const double* __restrict__ B, const double* __restrict__ R, const int32_t* __restrict__ by_star,
+                                const int32_t* __restrict__ star_ptr, long i0, long nip, long f0, long nfc, int ns, int ni,
+                                long Ktot, long k_off, double* __restrict__ Bt) {
+  long kc = long(ns) * 3 * nip;
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= kc * 6 * ni) return;
+  long k = idx % kc, col = idx / kc;
+  int m = int(k % ns), b = int((k / ns) % 3);
+  long ip = k / (3 * ns);
+  int a = int(col % 3), i = int((col / 3) % ni), type = int(col / (3 * ni));
+  long p0 = star_ptr[i0 + ip] - f0, p1 = star_ptr[i0 + ip + 1] - f0;
+  double acc = 0.0;
+  for (long fc = p0; fc < p1; ++fc) {
+    long f = by_star[f0 + fc];
+    acc += R[a + 3 * (b + 3 * f)] * B[m + long(ns) * (fc + nfc * (i + long(ni) * type))];
+  }
+  Bt[(k_off + k) + Ktot * col] = acc;
+}
+
+// gather_shifted_vertex! (src/ladder_kernel.jl:268-288) for one sign:
+// X[(j, c12, c0, ri), (m, b, ip)] = re/im of wlo J[klo] + whi J[klo + 1] of outer state i0 + ip.
+__global__ void shifted_vertex_kernel(const double2* __restrict__ J, const int32_t* __restrict__ klo,
+                                      const double* __restrict__ wlo, const double* __restrict__ whi, int nw, int ns,
+                                      long i0, long nip, double* __restrict__ X) {
+  const long nrow = 16l * nw;
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= nrow * ns * 3 * nip) return;
+  long row = idx % nrow, k = idx / nrow;
+  int j = int(row % nw);
+  int c12 = int((row / nw) % 4), c0 = int((row / (4l * nw)) % 2), ri = int(row / (8l * nw));
+  int m = int(k % ns), b = int((k / ns) % 3);
+  long i = i0 + k / (3 * ns);
+  int kl = klo[j + long(nw) * m];
+  double wl = wlo[j + long(nw) * m], wh = whi[j + long(nw) * m];
+  double2 z0 = J[jidx(nw, kl, c12, b, c0, i)], z1 = J[jidx(nw, kl + 1, c12, b, c0, i)];
+  X[idx] = ri == 0 ? wl * z0.x + wh * z1.x : wl * z0.y + wh * z1.y;
+}
+
+// Y = (C+ - C-)/2 of type 1 (src/ladder_kernel.jl:319): [nω, (c12, c0, ri, a, i)].
+__global__ void y_direct_kernel(const double* __restrict__ Cp, const double* __restrict__ Cm, long n, double* __restrict__ Y) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) Y[k] = (Cp[k] - Cm[k]) / 2;
+}
+
+// The four channels (src/ladder_kernel.jl:296-307) from C± [nω, 4, 2, 2, 3, ni, 2] and KY, then
+// LJ = -(Gm K Gp) as 2x2 contour matrices (src/ladder.jl:294-295). One thread per (ω, a, c0, i).
+__global__ void finish_direct_kernel(const double* __restrict__ Cp, const double* __restrict__ Cm, const double* __restrict__ KY,
+                                     const double2* __restrict__ Gm, const double2* __restrict__ Gp, int nw, int ni,
+                                     double2* __restrict__ LJ) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= long(nw) * 6 * ni) return;
+  long w = idx % nw;
+  long r = idx / nw;
+  int a = int(r % 3), c0 = int((r / 3) % 2);
+  long i = r / 6;
+  auto cidx = [&](int c12, int ri, int type) {
+    return w + nw * (c12 + 4 * (c0 + 2 * (ri + 2 * (a + 3 * (i + long(ni) * type)))));
+  };
+  double2 K[4];
+  for (int c12 = 0; c12 < 4; ++c12) {
+    double2 Up = make_double2(Cp[cidx(c12, 0, 0)], Cp[cidx(c12, 1, 0)]);
+    double2 Um = make_double2(Cm[cidx(c12, 0, 0)], Cm[cidx(c12, 1, 0)]);
+    double2 Vp = make_double2(Cp[cidx(c12, 0, 1)], Cp[cidx(c12, 1, 1)]);
+    double2 Vm = make_double2(Cm[cidx(c12, 0, 1)], Cm[cidx(c12, 1, 1)]);
+    if (c12 == 0 || c12 == 3) {
+      double2 ky = make_double2(KY[cidx(c12, 0, 0)], KY[cidx(c12, 1, 0)]);
+      double2 iky = c12 == 0 ? make_double2(ky.y, -ky.x) : make_double2(-ky.y, ky.x);
+      K[c12] = csub(csub(iky, cscale(cadd(Up, Um), 0.5)), cadd(Vp, Vm));
+    } else if (c12 == 1) {
+      K[c12] = cadd(cadd(Vp, Um), Vm);
+    } else {
+      K[c12] = cadd(cadd(Up, Vp), Vm);
+    }
+  }
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2) {
+      auto gm = [&](int c) { return Gm[w + long(nw) * (c + 4 * i)]; };
+      auto gp = [&](int c) { return Gp[w + long(nw) * (c + 4 * i)]; };
+      double2 z = cmul(cmul(gm(c1), K[0]), gp(0 + 2 * c2));
+      z = cadd(z, cmul(cmul(gm(c1 + 2), K[1]), gp(0 + 2 * c2)));
+      z = cadd(z, cmul(cmul(gm(c1), K[2]), gp(1 + 2 * c2)));
+      z = cadd(z, cmul(cmul(gm(c1 + 2), K[3]), gp(1 + 2 * c2)));
+      LJ[jidx(nw, w, c1 + 2 * c2, a, c0, i)] = make_double2(-z.x, -z.y);
+    }
+}
+
+// ---- GEMM paths: per-mode regrouped shift sums ----
+
+// G̃[(ν, b, i'), (a, i)] = Σ_{f in star(i')} R_f[a, b] w_f g2[ν, i, f], zero for ν below ω_acoustic.
+// One thread per (ν, i), looping over the stars in order.
+__global__ void coupling_rot_kernel(const double* __restrict__ g2, const double* __restrict__ R, const double* __restrict__ w_f,
+                                    const int32_t* __restrict__ by_star, const int32_t* __restrict__ star_ptr,
+                                    const double* __restrict__ wnu, double w_ac, int nm, int ni, long Kx,
+                                    double* __restrict__ Gt) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= long(nm) * ni) return;
+  int nu = int(idx % nm), i = int(idx / nm);
+  bool skip = wnu[nu] < w_ac;
+  for (int ip = 0; ip < ni; ++ip) {
+    double acc[3][3] = {};
+    if (!skip)
+      for (int p = star_ptr[ip]; p < star_ptr[ip + 1]; ++p) {
+        long f = by_star[p];
+        double g = w_f[f] * g2[nu + long(nm) * (i + long(ni) * f)];
+        for (int b = 0; b < 3; ++b)
+          for (int a = 0; a < 3; ++a) acc[a][b] += R[a + 3 * (b + 3 * f)] * g;
+      }
+    for (int b = 0; b < 3; ++b)
+      for (int a = 0; a < 3; ++a) Gt[(nu + long(nm) * (b + 3l * ip)) + Kx * (a + 3l * i)] = acc[a][b];
+  }
+}
+
+// One element of the A operand: row (j, q, c0, ri), column k = (ν, b, i'). The shifted vertex of
+// sign s at shift m, node j: wlo J[klo] + whi J[klo + 1]; the mode value
+// X±_ν = (1 - r_ν) S_{m_ν} + r_ν S_{m_ν + 1}; the combination q folds the channel algebra:
+//   q = 0, 2 : (X+ - X-)/2 of c12 = 11, 22        (the Kramers-Kronig argument)
+//   q = 1, 3 : -(1/2 + n_ν)(X+ + X-) of c12 = 11, 22
+//   q = 4    : n_ν X+ + (1 + n_ν) X- of c12 = 21
+//   q = 5    : (1 + n_ν) X+ + n_ν X- of c12 = 12
+__device__ __forceinline__ double xgen_value(const double2* __restrict__ J, const int32_t* __restrict__ klo,
+                                             const double* __restrict__ wlo, const double* __restrict__ whi, int nw,
+                                             int ns, int j, int q, int c0, int ri, int m, double r, double n, int b,
+                                             long ip) {
+  const int c12 = (q < 2) ? 0 : (q < 4 ? 3 : (q == 4 ? 1 : 2));
+  double xs[2];
+  for (int s = 0; s < 2; ++s) {
+    double acc = 0;
+    for (int dm = 0; dm < 2; ++dm) {
+      const int mm = m + dm;
+      const double wgt = dm == 0 ? 1 - r : r;
+      if (wgt == 0.0 || mm >= ns) continue;
+      const long t = j + long(nw) * (mm + long(ns) * s);
+      const int kl = klo[t];
+      const double2 z0 = J[jidx(nw, kl, c12, b, c0, ip)], z1 = J[jidx(nw, kl + 1, c12, b, c0, ip)];
+      const double zz = ri == 0 ? wlo[t] * z0.x + whi[t] * z1.x : wlo[t] * z0.y + whi[t] * z1.y;
+      acc += wgt * zz;
+    }
+    xs[s] = acc;
+  }
+  switch (q) {
+    case 0:
+    case 2: return (xs[0] - xs[1]) / 2;
+    case 1:
+    case 3: return -(0.5 + n) * (xs[0] + xs[1]);
+    case 4: return n * xs[0] + (1 + n) * xs[1];
+    default: return (1 + n) * xs[0] + n * xs[1];
+  }
+}
+
+// FP64 A operand, column-major [24 nω, Kx].
+__global__ void xgen_f64_kernel(const double2* __restrict__ J, const int32_t* __restrict__ klo, const double* __restrict__ wlo,
+                                const double* __restrict__ whi, const int32_t* __restrict__ mnu, const double* __restrict__ rnu,
+                                const double* __restrict__ nnu, int nw, int ns, int nm, int ni, double* __restrict__ A) {
+  const long nrow = 24l * nw;
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= nrow * nm * 3 * ni) return;
+  long row = idx % nrow, k = idx / nrow;
+  int j = int(row % nw);
+  int rr = int(row / nw);
+  int q = rr % 6, c0 = (rr / 6) % 2, ri = rr / 12;
+  int nu = int(k % nm), b = int((k / nm) % 3);
+  long ip = k / (3l * nm);
+  A[idx] = xgen_value(J, klo, wlo, whi, nw, ns, j, q, c0, ri, mnu[nu], rnu[nu], nnu[nu], b, ip);
+}
+
+// BF16 hi/lo A operand, row-major [24 nω][Kp], through a shared-memory transpose (32 rows x 64 k).
+__global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restrict__ J, const int32_t* __restrict__ klo,
+                                                        const double* __restrict__ wlo, const double* __restrict__ whi,
+                                                        const int32_t* __restrict__ mnu, const double* __restrict__ rnu,
+                                                        const double* __restrict__ nnu, int nw, int ns, int nm, int ni,
+                                                        long Kx, long Kp, __nv_bfloat16* __restrict__ Ah,
+                                                        __nv_bfloat16* __restrict__ Al) {
+  __shared__ float tile[64][33];
+  const long nrow = 24l * nw;
+  const long r0 = long(blockIdx.x) * 32;
+  const long k0 = long(blockIdx.y) * 64;
+  const int tr = threadIdx.x % 32, tk = threadIdx.x / 32;
+  const long row = r0 + tr;
+  const int j = int(row % nw);
+  const int rr = int(row / nw);
+  const int q = rr % 6, c0 = (rr / 6) % 2, ri = (rr / 12) % 2;
+#pragma unroll 1
+  for (int p = 0; p < 8; ++p) {
+    const int kl = tk + 8 * p;
+    const long k = k0 + kl;
+    float v = 0.f;
+    if (row < nrow && k < Kx) {
+      const int nu = int(k % nm), b = int((k / nm) % 3);
+      const long ip = k / (3l * nm);
+      v = float(xgen_value(J, klo, wlo, whi, nw, ns, j, q, c0, ri, mnu[nu], rnu[nu], nnu[nu], b, ip));
+    }
+    tile[kl][tr] = v;
+  }
+  __syncthreads();
+  const int wr = threadIdx.x / 8, kc = (threadIdx.x % 8) * 8;
+  const long orow = r0 + wr;
+  if (orow < nrow) {
+    __align__(16) __nv_bfloat16 hh[8], ll[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const float x = tile[kc + t][wr];
+      hh[t] = __float2bfloat16_rn(x);
+      ll[t] = __float2bfloat16_rn(x - __bfloat162float(hh[t]));
+    }
+    const long off = orow * Kp + k0 + kc;
+    *reinterpret_cast<uint4*>(Ah + off) = *reinterpret_cast<const uint4*>(hh);
+    *reinterpret_cast<uint4*>(Al + off) = *reinterpret_cast<const uint4*>(ll);
+  }
+}
+
+__global__ void split_rows_plain_kernel(const double* __restrict__ S, long rows, long cols, long ld, long Kp,
+                                        __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol) {
+  // out[r * Kp + c] = split(S[c + ld r]) (a column-major [cols, rows] matrix read row by row).
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= rows * Kp) return;
+  long r = idx / Kp, c = idx % Kp;
+  float x = c < cols ? float(S[c + ld * r]) : 0.f;
+  __nv_bfloat16 h = __float2bfloat16_rn(x);
+  oh[idx] = h;
+  ol[idx] = __float2bfloat16_rn(x - __bfloat162float(h));
+}
+
+// Sum of split-K partials into D (FP64).
+__global__ void sum_parts_kernel(const float* __restrict__ part, long n, int splits, long stride, double* __restrict__ D) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  float s = 0.f;
+  for (int p = 0; p < splits; ++p) s += part[k + stride * p];
+  D[k] = double(s);
+}
+
+// Y of the regrouped path: the rows q = 0 (c12 = 11) and q = 2 (c12 = 22) of D, as [nω, (qq, c0, ri, n)].
+__global__ void y_gemm_kernel(const double* __restrict__ D, int nw, long ncol, double* __restrict__ Y) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  long total = long(nw) * 8 * ncol;
+  if (idx >= total) return;
+  long w = idx % nw, r = idx / nw;
+  int qq = int(r % 2), c0 = int((r / 2) % 2), ri = int((r / 4) % 2);
+  long n = r / 8;
+  int q = qq == 0 ? 0 : 2;
+  Y[idx] = D[w + nw * (q + 6 * (c0 + 2 * ri)) + 24l * nw * n];
+}
+
+__global__ void finish_gemm_kernel(const double* __restrict__ D, const double* __restrict__ KY, const double2* __restrict__ Gm,
+                                   const double2* __restrict__ Gp, int nw, int ni, double2* __restrict__ LJ) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= long(nw) * 6 * ni) return;
+  long w = idx % nw;
+  long r = idx / nw;
+  int a = int(r % 3), c0 = int((r / 3) % 2);
+  long i = r / 6;
+  const long n = a + 3 * i;
+  auto d = [&](int q, int ri) { return D[w + nw * (q + 6 * (c0 + 2 * ri)) + 24l * nw * n]; };
+  auto ky = [&](int qq, int ri) { return KY[w + nw * (qq + 2 * (c0 + 2 * (ri + 2 * n)))]; };
+  double2 K[4];
+  {
+    double2 y0 = make_double2(ky(0, 0), ky(0, 1));
+    K[0] = make_double2(y0.y + d(1, 0), -y0.x + d(1, 1));      // -i KY + rest
+    double2 y3 = make_double2(ky(1, 0), ky(1, 1));
+    K[3] = make_double2(-y3.y + d(3, 0), y3.x + d(3, 1));      // +i KY + rest
+    K[1] = make_double2(d(4, 0), d(4, 1));
+    K[2] = make_double2(d(5, 0), d(5, 1));
+  }
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2) {
+      auto gm = [&](int c) { return Gm[w + long(nw) * (c + 4 * i)]; };
+      auto gp = [&](int c) { return Gp[w + long(nw) * (c + 4 * i)]; };
+      double2 z = cmul(cmul(gm(c1), K[0]), gp(0 + 2 * c2));
+      z = cadd(z, cmul(cmul(gm(c1 + 2), K[1]), gp(0 + 2 * c2)));
+      z = cadd(z, cmul(cmul(gm(c1), K[2]), gp(1 + 2 * c2)));
+      z = cadd(z, cmul(cmul(gm(c1 + 2), K[3]), gp(1 + 2 * c2)));
+      LJ[jidx(nw, w, c1 + 2 * c2, a, c0, i)] = make_double2(-z.x, -z.y);
+    }
+}
+
+// ---- GMRES BLAS-1 (FP64, fixed-order reductions) ----
+
+constexpr int kDotBlocks = 1024;
+
+__global__ void __launch_bounds__(256) dot_partial_kernel(const double2* __restrict__ u, const double2* __restrict__ v, long n,
+                                                          double2* __restrict__ part) {
+  __shared__ double sr[256], si[256];
+  double ar = 0, ai = 0;
+  for (long k = long(blockIdx.x) * 256 + threadIdx.x; k < n; k += long(gridDim.x) * 256) {
+    double2 a = u[k], b = v[k];
+    ar += a.x * b.x + a.y * b.y;  // conj(a) b
+    ai += a.x * b.y - a.y * b.x;
+  }
+  sr[threadIdx.x] = ar;
+  si[threadIdx.x] = ai;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sr[threadIdx.x] += sr[threadIdx.x + s];
+      si[threadIdx.x] += si[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = make_double2(sr[0], si[0]);
+}
+
+__global__ void __launch_bounds__(256) dot_final_kernel(const double2* __restrict__ part, int np, double2* __restrict__ out) {
+  __shared__ double sr[256], si[256];
+  double ar = 0, ai = 0;
+  for (int k = threadIdx.x; k < np; k += 256) {
+    ar += part[k].x;
+    ai += part[k].y;
+  }
+  sr[threadIdx.x] = ar;
+  si[threadIdx.x] = ai;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      sr[threadIdx.x] += sr[threadIdx.x + s];
+      si[threadIdx.x] += si[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = make_double2(sr[0], si[0]);
+}
+
+// q -= h v with h read from device memory.
+__global__ void axpy_dev_kernel(double2* __restrict__ q, const double2* __restrict__ v, const double2* __restrict__ h, long n) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double2 hh = *h, x = v[k];
+  q[k] = make_double2(q[k].x - (hh.x * x.x - hh.y * x.y), q[k].y - (hh.x * x.y + hh.y * x.x));
+}
+
+// y = a x + b y (complex a, b from the host).
+__global__ void axpby_kernel(double2 a, const double2* __restrict__ x, double2 b, double2* __restrict__ y, long n) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double2 xv = x[k], yv = y[k];
+  y[k] = make_double2(a.x * xv.x - a.y * xv.y + b.x * yv.x - b.y * yv.y, a.x * xv.y + a.y * xv.x + b.x * yv.y + b.y * yv.x);
+}
+
+__global__ void sub_kernel(const double2* __restrict__ x, const double2* __restrict__ y, double2* __restrict__ out, long n) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = make_double2(x[k].x - y[k].x, x[k].y - y[k].y);
+}
+
+__global__ void add_kernel(const double2* __restrict__ x, const double2* __restrict__ y, double2* __restrict__ out, long n) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = make_double2(x[k].x + y[k].x, x[k].y + y[k].y);
+}
+
+// ---------------------------------------------------------------------------------------------
+// setup
+// ---------------------------------------------------------------------------------------------
+
+static void check_ladder_model(const epsp_model* m) {
+  if (!m) fail(EPSP_EINVAL, "model is NULL");
+  if (m->nm < 1 || m->ni < 1 || m->nf < 1) fail(EPSP_EINVAL, "nm, ni and nf must be positive");
+  if (!m->g2 || !m->omega_ph || !m->iq_kk || !m->iks_i || !m->iks_f || !m->eps_i || !m->w_i || !m->w_f ||
+      !m->f_to_i || !m->R || !m->v)
+    fail(EPSP_EINVAL, "a required model array is NULL (the ladder needs R and v)");
+  for (int64_t f = 0; f < m->nf; ++f) {
+    if (m->f_to_i[f] < 0 || m->f_to_i[f] >= m->ni) fail(EPSP_EINVAL, "f_to_i out of range");
+    if (m->iks_f[f] < 0 || m->iks_f[f] >= m->nk_f) fail(EPSP_EINVAL, "iks_f out of range");
+  }
+  for (int64_t i = 0; i < m->ni; ++i)
+    if (m->iks_i[i] < 0 || m->iks_i[i] >= m->nk_i) fail(EPSP_EINVAL, "iks_i out of range");
+  for (int64_t k = 0; k < m->nk_i * m->nk_f; ++k)
+    if (m->iq_kk[k] < 0 || m->iq_kk[k] >= m->nq) fail(EPSP_EINVAL, "iq_kk out of range");
+}
+
+static std::vector<double> g2_as_double(const epsp_model* m) {
+  const size_t n = size_t(m->nm * m->ni * m->nf);
+  std::vector<double> out(n);
+  if (m->g2_dtype == EPSP_F64) {
+    std::memcpy(out.data(), m->g2, n * 8);
+  } else if (m->g2_dtype == EPSP_F32) {
+    const float* p = static_cast<const float*>(m->g2);
+    for (size_t k = 0; k < n; ++k) out[k] = double(p[k]);
+  } else {
+    const uint16_t* p = static_cast<const uint16_t*>(m->g2);
+    for (size_t k = 0; k < n; ++k) {
+      uint32_t u = uint32_t(p[k]) << 16;
+      float x;
+      std::memcpy(&x, &u, 4);
+      out[k] = double(x);
+    }
+  }
+  return out;
+}
+
+LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) {
+  check_ladder_model(m);
+  if (!opts) fail(EPSP_EINVAL, "options are NULL");
+  if (opts->gpu_tile < 0) fail(EPSP_EINVAL, "gpu_tile must be nothing or a positive number of inner states");
+  if (!(opts->omega_acoustic > 0))
+    fail(EPSP_EINVAL, "omega_acoustic must be positive: the shift-grid coupling build has no row for a negative phonon frequency");
+  auto* P = new LadderPlan;
+  std::unique_ptr<LadderPlan> guard(P);
+  cudaStream_t s = ctx->stream;
+  P->ctx = ctx;
+  P->path = opts->path;
+  P->w_ac = opts->omega_acoustic;
+  P->nm = m->nm;
+  P->ni = m->ni;
+  P->nf = m->nf;
+  P->ws = make_grid(m->omegas, "omegas");
+  P->nw = P->ws.n;
+  P->h = P->ws.unit;
+  const long nm = P->nm, ni = P->ni, nf = P->nf, nw = P->nw;
+  // nshift = ceil(max ωph / dω_unit) + 2 (src/ladder.jl:151)
+  double mx = -std::numeric_limits<double>::infinity();
+  for (int64_t k = 0; k < m->nm * m->nq; ++k) mx = std::max(mx, m->omega_ph[k]);
+  if (!std::isfinite(mx)) fail(EPSP_EINVAL, "omega_ph must be finite");
+  P->nshift = long(std::ceil(mx / P->h)) + 2;
+  if (P->nshift < 2) P->nshift = 2;
+  const long ns = P->nshift;
+  P->Ww_h = trapezoid_weights(P->ws.nodes);
+  P->v_h.assign(m->v, m->v + 3 * ni);
+  P->w_i_h.assign(m->w_i, m->w_i + ni);
+  P->d_ws = to_device(ctx, P->ws.nodes);
+  P->d_Ww = to_device(ctx, P->Ww_h);
+  P->d_eps_i = to_device(ctx, m->eps_i, size_t(ni));
+  P->d_v = to_device(ctx, m->v, size_t(3 * ni));
+  // KK (src/frequency_grids.jl:30-44), through the same device builder as the scGD0 plan
+  {
+    const auto& w = P->ws.nodes;
+    std::vector<double> xs(size_t(nw + 2));
+    xs[0] = w[0] - (w[1] - w[0]);
+    for (long j = 0; j < nw; ++j) xs[size_t(j + 1)] = w[size_t(j)];
+    xs[size_t(nw + 1)] = w[size_t(nw - 1)] + (w[size_t(nw - 1)] - w[size_t(nw - 2)]);
+    // K[i, j] = lskk(xs[i+1], xs[j], xs[j+1], xs[j+2]) / π on the host (setup, O(nω²))
+    std::vector<double> K(size_t(nw * nw));
+    auto xlogx = [](double x) { return x == 0 ? 0.0 : x * std::log(std::fabs(x)); };
+    for (long j = 0; j < nw; ++j)
+      for (long i = 0; i < nw; ++i) {
+        double x = xs[size_t(i + 1)], x1 = xs[size_t(j)], x2 = xs[size_t(j + 1)], x3 = xs[size_t(j + 2)];
+        K[size_t(i + nw * j)] = (xlogx(x1 - x) / (x2 - x1) - xlogx(x2 - x) * (x3 - x1) / (x2 - x1) / (x3 - x2) +
+                                 xlogx(x3 - x) / (x3 - x2)) /
+                                3.14159265358979323846;
+      }
+    P->d_KK = to_device(ctx, K);
+  }
+  // stars: sortperm(f_to_i) (stable) and the cumulative star sizes (src/ladder.jl:144-149)
+  std::vector<int32_t> by_star(static_cast<size_t>(nf));
+  for (long f = 0; f < nf; ++f) by_star[size_t(f)] = int32_t(f);
+  std::stable_sort(by_star.begin(), by_star.end(), [&](int32_t a, int32_t b) { return m->f_to_i[a] < m->f_to_i[b]; });
+  std::vector<int32_t> sp(size_t(ni + 1), 0);
+  for (long f = 0; f < nf; ++f) sp[size_t(m->f_to_i[f] + 1)]++;
+  for (long i = 0; i < ni; ++i) sp[size_t(i + 1)] += sp[size_t(i)];
+  P->d_by_star = to_device(ctx, by_star);
+  P->d_star_ptr = to_device(ctx, sp);
+  // shift tables (src/ladder_kernel.jl:158-176): [nω, nshift, 2]
+  {
+    std::vector<int32_t> klo(size_t(nw * ns * 2));
+    std::vector<double> wlo(klo.size()), whi(klo.size());
+    const auto& off = P->ws.offsets;
+    for (int sg = 0; sg < 2; ++sg)
+      for (long mm = 0; mm < ns; ++mm)
+        for (long j = 0; j < nw; ++j) {
+          int64_t p = off[size_t(j)] + (sg == 0 ? mm : -mm);
+          long ssl = long(std::upper_bound(off.begin(), off.end(), p) - off.begin());
+          long k = std::clamp<long>(ssl, 1, nw - 1) - 1;
+          double t = double(p - off[size_t(k)]) / double(off[size_t(k + 1)] - off[size_t(k)]);
+          bool inside = off[0] <= p && p <= off[size_t(nw - 1)];
+          size_t idx = size_t(j + nw * (mm + ns * sg));
+          klo[idx] = int32_t(k);
+          wlo[idx] = inside ? 1 - t : 0.0;
+          whi[idx] = inside ? t : 0.0;
+        }
+    P->d_klo = to_device(ctx, klo);
+    P->d_wlo = to_device(ctx, wlo);
+    P->d_whi = to_device(ctx, whi);
+  }
+  auto g2d = g2_as_double(m);
+  P->d_g2 = to_device(ctx, g2d);
+  P->d_wf = to_device(ctx, m->w_f, size_t(nf));
+  P->d_R = to_device(ctx, m->R, size_t(9 * nf));
+  if (P->path == EPSP_PATH_DIRECT_FP64) {
+    // chunks by whole stars (src/ladder.jl:180-202)
+    const int64_t CB = int64_t(1) << 30;
+    int64_t bytes_per_f = 8 * std::max(ns * ni * 2, nm * ni);
+    int64_t bytes_per_i = 8 * std::max(ns * 9 * ni * 2, nw * 16 * ns * 3);
+    int64_t max_f = opts->gpu_tile <= 0 ? std::max<int64_t>(CB / bytes_per_f, 1) : opts->gpu_tile;
+    int64_t max_i = std::max<int64_t>(CB / bytes_per_i, 1);
+    long i1 = 0, koff = 0, maxnf = 0, maxnip = 0;
+    while (i1 < ni) {
+      long i2 = i1;
+      while (i2 < ni - 1 && i2 - i1 + 2 <= max_i && sp[size_t(i2 + 2)] - sp[size_t(i1)] <= max_f) ++i2;
+      LadderChunk c;
+      c.i0 = i1;
+      c.i1 = i2 + 1;
+      c.f0 = sp[size_t(i1)];
+      c.f1 = sp[size_t(i2 + 1)];
+      c.k_off = koff;
+      koff += ns * 3 * (c.i1 - c.i0);
+      maxnf = std::max(maxnf, c.f1 - c.f0);
+      maxnip = std::max(maxnip, c.i1 - c.i0);
+      P->chunks.push_back(c);
+      i1 = i2 + 1;
+    }
+    P->Ktot = koff;
+    auto d_wph = to_device(ctx, m->omega_ph, size_t(nm * m->nq));
+    auto d_iq = to_device(ctx, m->iq_kk, size_t(m->nk_i * m->nk_f));
+    auto d_iksi = to_device(ctx, m->iks_i, size_t(ni));
+    auto d_iksf = to_device(ctx, m->iks_f, size_t(nf));
+    P->d_wq.alloc(ctx, size_t(nm * nf * ni));
+    gather_wq_star_kernel<<<div_up(size_t(nm * nf * ni), 256), 256, 0, s>>>(d_wph.p, d_iq.p, d_iksi.p, d_iksf.p, P->d_by_star.p,
+                                                                           int(nm), nf, int(ni), m->nk_i, P->d_wq.p);
+    EPSP_LAUNCHED(ctx);
+    P->d_B.alloc(ctx, size_t(ns * maxnf * ni * 2));
+    P->d_Bt.alloc(ctx, size_t(P->Ktot * 6 * ni));
+    P->d_X.alloc(ctx, size_t(16 * nw * ns * 3 * maxnip));
+    P->d_Cp.alloc(ctx, size_t(16 * nw * 6 * ni));
+    P->d_Cm.alloc(ctx, size_t(16 * nw * 6 * ni));
+    EPSP_CUDA(cudaStreamSynchronize(s));
+  } else if (P->path == EPSP_PATH_GEMM_FP64 || P->path == EPSP_PATH_GEMM_BF16X3) {
+    P->wnu.assign(size_t(nm), 0.0);
+    for (long nu = 0; nu < nm; ++nu) {
+      double w0 = m->omega_ph[nu];
+      for (int64_t q = 1; q < m->nq; ++q)
+        if (!(m->omega_ph[nu + nm * q] == w0))
+          fail(EPSP_EUNSUPPORTED, "the GEMM paths need dispersionless modes (every row of omega_ph constant); use EPSP_PATH_DIRECT_FP64");
+      P->wnu[size_t(nu)] = w0;
+    }
+    P->m_nu.resize(size_t(nm));
+    P->r_nu.resize(size_t(nm));
+    for (long nu = 0; nu < nm; ++nu) {
+      double x = P->wnu[size_t(nu)] / P->h;  // the tent split of src/ladder_kernel.jl:199-206
+      long lo = long(std::floor(x));
+      P->m_nu[size_t(nu)] = int32_t(std::max<long>(lo, 0));
+      P->r_nu[size_t(nu)] = x - double(lo);
+      if (P->wnu[size_t(nu)] < P->w_ac) {
+        P->m_nu[size_t(nu)] = 0;
+        P->r_nu[size_t(nu)] = 0;
+      }
+    }
+    P->d_mnu = to_device(ctx, P->m_nu);
+    P->d_rnu = to_device(ctx, P->r_nu);
+    P->d_nnu.alloc(ctx, size_t(nm));
+    auto d_wnu = to_device(ctx, P->wnu);
+    P->Kx = nm * 3 * ni;
+    P->d_Gt.alloc(ctx, size_t(P->Kx * 3 * ni));
+    coupling_rot_kernel<<<div_up(size_t(nm * ni), 128), 128, 0, s>>>(P->d_g2.p, P->d_R.p, P->d_wf.p, P->d_by_star.p,
+                                                                     P->d_star_ptr.p, d_wnu.p, P->w_ac, int(nm), int(ni),
+                                                                     P->Kx, P->d_Gt.p);
+    EPSP_LAUNCHED(ctx);
+    P->d_D.alloc(ctx, size_t(24 * nw * 3 * ni));
+    if (P->path == EPSP_PATH_GEMM_FP64) {
+      P->d_Af.alloc(ctx, size_t(24 * nw * P->Kx));
+    } else {
+      P->Kp = (P->Kx + 63) / 64 * 64;
+      const long M = 24 * nw, N = 3 * ni;
+      P->d_Ah.alloc(ctx, size_t(M * P->Kp));
+      P->d_Al.alloc(ctx, size_t(M * P->Kp));
+      P->d_Gh.alloc(ctx, size_t(N * P->Kp));
+      P->d_Gl.alloc(ctx, size_t(N * P->Kp));
+      split_rows_plain_kernel<<<div_up(size_t(N * P->Kp), 256), 256, 0, s>>>(P->d_Gt.p, N, P->Kx, P->Kx, P->Kp, P->d_Gh.p,
+                                                                              P->d_Gl.p);
+      EPSP_LAUNCHED(ctx);
+      tc_gemm_shape(ctx, int(M), int(N), int(P->Kx), 16, &P->bn, &P->splits);
+      P->d_part.alloc(ctx, size_t(P->splits) * size_t(M * N));
+      P->d_err.alloc(ctx, 1);
+      P->d_err.zero(s);
+      P->opA = {make_tmap_bf16(P->d_Ah.p, M, P->Kx, P->Kp, kTcBM), make_tmap_bf16(P->d_Al.p, M, P->Kx, P->Kp, kTcBM)};
+      P->opG = {make_tmap_bf16(P->d_Gh.p, N, P->Kx, P->Kp, P->bn), make_tmap_bf16(P->d_Gl.p, N, P->Kx, P->Kp, P->bn)};
+    }
+    EPSP_CUDA(cudaStreamSynchronize(s));
+  } else {
+    fail(EPSP_EINVAL, "unknown path");
+  }
+  P->d_Y.alloc(ctx, size_t(nw * 48 * ni));
+  P->d_KY.alloc(ctx, size_t(nw * 48 * ni));
+  P->d_Gm.alloc(ctx, size_t(nw * 4 * ni));
+  P->d_Gp.alloc(ctx, size_t(nw * 4 * ni));
+  P->d_ST.alloc(ctx, size_t(nw * ni));
+  P->d_jm.alloc(ctx, size_t(nw));
+  P->d_jp.alloc(ctx, size_t(nw));
+  P->d_tm.alloc(ctx, size_t(nw));
+  P->d_tp.alloc(ctx, size_t(nw));
+  return guard.release();
+}
+
+// ---------------------------------------------------------------------------------------------
+// operator
+// ---------------------------------------------------------------------------------------------
+
+// Propagators of (T, μ, Ω) from Σ_T on the device (d_ST).
+static void set_propagators(LadderPlan* P, double mu, double T, double Om) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  const long nw = P->nw, ni = P->ni;
+  std::vector<double> xm(static_cast<size_t>(nw)), xp(static_cast<size_t>(nw)), tm, tp;
+  std::vector<int32_t> jm, jp;
+  for (long k = 0; k < nw; ++k) {
+    xm[size_t(k)] = P->ws.nodes[size_t(k)] - Om / 2;
+    xp[size_t(k)] = P->ws.nodes[size_t(k)] + Om / 2;
+  }
+  interp_table(P->ws.nodes, xm, jm, tm);
+  interp_table(P->ws.nodes, xp, jp, tp);
+  P->d_jm.upload(jm.data(), size_t(nw), s);
+  P->d_jp.upload(jp.data(), size_t(nw), s);
+  P->d_tm.upload(tm.data(), size_t(nw), s);
+  P->d_tp.upload(tp.data(), size_t(nw), s);
+  propagators_kernel<<<dim3(div_up(size_t(nw), 128), unsigned(ni)), 128, 0, s>>>(P->d_ST.p, P->d_ws.p, int(nw), P->d_jm.p,
+                                                                                P->d_tm.p, P->d_jp.p, P->d_tp.p, P->d_eps_i.p,
+                                                                                mu, T, Om, P->d_Gm.p, P->d_Gp.p, int(ni));
+  EPSP_LAUNCHED(ctx);
+  EPSP_CUDA(cudaStreamSynchronize(s));  // the host tables above are freed on return
+  P->cur_T = T;
+  P->cur_mu = mu;
+  P->cur_Om = Om;
+}
+
+// B̃ of temperature T for every chunk (the B build and star sum of src/ladder.jl:257-281).
+static void build_Bt(LadderPlan* P, double T) {
+  if (P->Bt_T == T) return;
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  const long ni = P->ni, ns = P->nshift;
+  for (const auto& c : P->chunks) {
+    const long nfc = c.f1 - c.f0, nip = c.i1 - c.i0;
+    bin_coupling_kernel<<<div_up(size_t(nfc * ni * 2), 128), 128, 0, s>>>(P->d_g2.p, P->d_wq.p, P->d_by_star.p, P->d_wf.p,
+                                                                         int(P->nm), int(ni), P->nf, c.f0, nfc, int(ns), P->h,
+                                                                         P->w_ac, T, P->d_B.p);
+    EPSP_LAUNCHED(ctx);
+    const long total = ns * 3 * nip * 6 * ni;
+    star_sum_kernel<<<div_up(size_t(total), 256), 256, 0, s>>>(P->d_B.p, P->d_R.p, P->d_by_star.p, P->d_star_ptr.p, c.i0, nip,
+                                                               c.f0, nfc, int(ns), int(ni), P->Ktot, c.k_off, P->d_Bt.p);
+    EPSP_LAUNCHED(ctx);
+  }
+  P->Bt_T = T;
+}
+
+// LJ = L(J) with the current propagators (apply_ladder_kernel!, src/ladder.jl:245-296).
+static void apply_L(LadderPlan* P, const double2* J, double2* LJ) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  const long nw = P->nw, ni = P->ni, ns = P->nshift;
+  const double T = P->cur_T;
+  if (P->path == EPSP_PATH_DIRECT_FP64) {
+    build_Bt(P, T);
+    const long nrow = 16 * nw, ncol = 6 * ni;
+    P->d_Cp.zero(s);
+    P->d_Cm.zero(s);
+    for (const auto& c : P->chunks) {
+      const long nip = c.i1 - c.i0, kc = ns * 3 * nip;
+      for (int sg = 0; sg < 2; ++sg) {
+        shifted_vertex_kernel<<<div_up(size_t(nrow * kc), 256), 256, 0, s>>>(J, P->d_klo.p + nw * ns * sg, P->d_wlo.p + nw * ns * sg,
+                                                                            P->d_whi.p + nw * ns * sg, int(nw), int(ns), c.i0, nip,
+                                                                            P->d_X.p);
+        EPSP_LAUNCHED(ctx);
+        long pg = prof_begin(ctx, "ladder_gemm");
+        gemm_f64(ctx, false, int(nrow), int(ncol), int(kc), 1.0, P->d_X.p, nrow, P->d_Bt.p + c.k_off, P->Ktot, 1.0,
+                 sg == 0 ? P->d_Cp.p : P->d_Cm.p, nrow);
+        prof_end(ctx, pg);
+      }
+    }
+    const long ny = nw * 48 * ni;
+    y_direct_kernel<<<div_up(size_t(ny), 256), 256, 0, s>>>(P->d_Cp.p, P->d_Cm.p, ny, P->d_Y.p);
+    EPSP_LAUNCHED(ctx);
+    gemm_f64(ctx, false, int(nw), int(48 * ni), int(nw), 1.0, P->d_KK.p, nw, P->d_Y.p, nw, 0.0, P->d_KY.p, nw);
+    finish_direct_kernel<<<div_up(size_t(nw * 6 * ni), 256), 256, 0, s>>>(P->d_Cp.p, P->d_Cm.p, P->d_KY.p, P->d_Gm.p, P->d_Gp.p,
+                                                                          int(nw), int(ni), LJ);
+    EPSP_LAUNCHED(ctx);
+    return;
+  }
+  // regrouped GEMM paths
+  if (P->Bt_T != T) {
+    std::vector<double> nnu(size_t(P->nm));
+    for (long nu = 0; nu < P->nm; ++nu) {
+      double w = P->wnu[size_t(nu)];
+      nnu[size_t(nu)] = w < P->w_ac ? 0.0 : (T > 1.4901161193847656e-08 ? (w == 0 ? -0.5 : 1.0 / std::expm1(w / T)) : (w > 0 ? 0.0 : -1.0));
+    }
+    P->d_nnu.upload(nnu.data(), size_t(P->nm), s);
+    EPSP_CUDA(cudaStreamSynchronize(s));
+    P->Bt_T = T;
+  }
+  const long M = 24 * nw, N = 3 * ni;
+  if (P->path == EPSP_PATH_GEMM_FP64) {
+    long px = prof_begin(ctx, "xgen");
+    xgen_f64_kernel<<<div_up(size_t(M * P->Kx), 256), 256, 0, s>>>(J, P->d_klo.p, P->d_wlo.p, P->d_whi.p, P->d_mnu.p, P->d_rnu.p,
+                                                                   P->d_nnu.p, int(nw), int(ns), int(P->nm), int(ni), P->d_Af.p);
+    EPSP_LAUNCHED(ctx);
+    prof_end(ctx, px);
+    long pg = prof_begin(ctx, "ladder_gemm");
+    gemm_f64(ctx, false, int(M), int(N), int(P->Kx), 1.0, P->d_Af.p, M, P->d_Gt.p, P->Kx, 0.0, P->d_D.p, M);
+    prof_end(ctx, pg);
+  } else {
+    long px = prof_begin(ctx, "xgen");
+    xgen_bf16_kernel<<<dim3(div_up(size_t(M), 32), unsigned(P->Kp / 64)), 256, 0, s>>>(
+        J, P->d_klo.p, P->d_wlo.p, P->d_whi.p, P->d_mnu.p, P->d_rnu.p, P->d_nnu.p, int(nw), int(ns), int(P->nm), int(ni), P->Kx,
+        P->Kp, P->d_Ah.p, P->d_Al.p);
+    EPSP_LAUNCHED(ctx);
+    prof_end(ctx, px);
+    int sp = tc_gemm_launch(ctx, P->opA, P->opG, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N, 16, P->d_err.p);
+    sum_parts_kernel<<<div_up(size_t(M * N), 256), 256, 0, s>>>(P->d_part.p, M * N, sp, M * N, P->d_D.p);
+    EPSP_LAUNCHED(ctx);
+  }
+  const long ny = nw * 8 * N;
+  y_gemm_kernel<<<div_up(size_t(ny), 256), 256, 0, s>>>(P->d_D.p, int(nw), N, P->d_Y.p);
+  EPSP_LAUNCHED(ctx);
+  gemm_f64(ctx, false, int(nw), int(8 * N), int(nw), 1.0, P->d_KK.p, nw, P->d_Y.p, nw, 0.0, P->d_KY.p, nw);
+  finish_gemm_kernel<<<div_up(size_t(nw * 6 * ni), 256), 256, 0, s>>>(P->d_D.p, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, int(nw), int(ni), LJ);
+  EPSP_LAUNCHED(ctx);
+}
+
+static void check_tc_err(LadderPlan* P) {
+  if (P->path != EPSP_PATH_GEMM_BF16X3) return;
+  int e = 0;
+  P->d_err.download(&e, 1, P->ctx->stream);
+  EPSP_CUDA(cudaStreamSynchronize(P->ctx->stream));
+  if (e) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+}
+
+// ---------------------------------------------------------------------------------------------
+// solves (src/ladder.jl:327-375)
+// ---------------------------------------------------------------------------------------------
+
+static cplx dot_dev(LadderPlan* P, const double2* u, const double2* v, long n, DBuf<double2>& part, double2* out_dev) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  dot_partial_kernel<<<kDotBlocks, 256, 0, s>>>(u, v, n, part.p);
+  EPSP_LAUNCHED(ctx);
+  dot_final_kernel<<<1, 256, 0, s>>>(part.p, kDotBlocks, out_dev);
+  EPSP_LAUNCHED(ctx);
+  return cplx();
+}
+
+static double nrm_host(LadderPlan* P, const double2* u, long n, DBuf<double2>& part, DBuf<double2>& scal) {
+  dot_dev(P, u, u, n, part, scal.p);
+  double2 r;
+  scal.download(&r, 1, P->ctx->stream);
+  EPSP_CUDA(cudaStreamSynchronize(P->ctx->stream));
+  return std::sqrt(r.x);
+}
+
+// conductivity_from_vertex (src/ladder_kernel.jl:116-122) of the device vertex J.
+static void conductivity_dev(LadderPlan* P, const double2* J, double Om, double T, DBuf<double2>& Ybuf, double* sigma) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  const long nw = P->nw, ni = P->ni;
+  cond_sum_kernel<<<unsigned(3 * ni), 256, 0, s>>>(J, P->d_Ww.p, int(nw), int(ni), Ybuf.p);
+  EPSP_LAUNCHED(ctx);
+  std::vector<double2> Y(size_t(3 * ni));
+  Ybuf.download(Y.data(), size_t(3 * ni), s);
+  EPSP_CUDA(cudaStreamSynchronize(s));
+  cplx F = Om == 0 ? cplx(0, 1) / (4 * T)
+                   : -1.0 / (cplx(0, 2) * Om * (1 + 2 * (T > 1.4901161193847656e-08 ? 1.0 / std::expm1(Om / T) : 0.0)));
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      cplx S = 0;
+      for (long i = 0; i < ni; ++i) S += (P->v_h[size_t(a + 3 * i)] * P->w_i_h[size_t(i)]) * cplx(Y[size_t(b + 3 * i)].x, Y[size_t(b + 3 * i)].y);
+      sigma[a + 3 * b] = (F / (2 * 3.14159265358979323846 * cplx(0, 1)) * S).real();
+    }
+}
+
+static double mat3_norm(const double* a) {
+  double s = 0;
+  for (int k = 0; k < 9; ++k) s += a[k] * a[k];
+  return std::sqrt(s);
+}
+
+void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const double* Tlist, int64_t nT, const double* Omegas,
+                int64_t nO, int32_t solver, double rtol, int32_t maxiter, double* sb, double* sl, uint8_t* conv, int32_t* niter,
+                epsp_ladder_history* hist, double* J_out) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  if (solver != EPSP_SOLVER_GMRES && solver != EPSP_SOLVER_FIXED_POINT) fail(EPSP_EINVAL, "solver must be :gmres or :fixed_point");
+  if (maxiter < 1) fail(EPSP_EINVAL, "maxiter must be at least 1, got " + std::to_string(maxiter));
+  if (nO < 1) fail(EPSP_EINVAL, "Omegas must hold at least one probe frequency");
+  if (nT < 1 || !sigma || !mu || !Tlist || !Omegas || !sb || !sl || !conv || !niter) fail(EPSP_EINVAL, "an input or output array is NULL");
+  for (int64_t iT = 0; iT < nT; ++iT)
+    if (!(Tlist[iT] >= 0)) fail(EPSP_EINVAL, "Temperature must be positive");
+  const long nw = P->nw, ni = P->ni;
+  const long n = nw * 24 * ni;
+  const unsigned eb = div_up(size_t(n), 256);
+  DBuf<double2> J0, J, LJ, W, part, scal, Hdev, Ybuf;
+  J0.alloc(ctx, size_t(n));
+  J.alloc(ctx, size_t(n));
+  LJ.alloc(ctx, size_t(n));
+  W.alloc(ctx, size_t(n));
+  part.alloc(ctx, kDotBlocks);
+  scal.alloc(ctx, 1);
+  Hdev.alloc(ctx, size_t(maxiter + 2));
+  Ybuf.alloc(ctx, size_t(3 * ni));
+  std::vector<DBuf<double2>> V;
+  const double btol = std::pow(std::numeric_limits<double>::epsilon(), 0.75);
+  for (int64_t iT = 0; iT < nT; ++iT) {
+    const double T = Tlist[iT];
+    P->d_ST.upload(reinterpret_cast<const double2*>(sigma) + size_t(nw * ni * iT), size_t(nw * ni), s);
+    for (int64_t iO = 0; iO < nO; ++iO) {
+      const double Om = Omegas[iO];
+      const int64_t idx = iO + nO * iT;
+      set_propagators(P, mu[iT], T, Om);
+      attach_bare_kernel<<<eb, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
+      EPSP_LAUNCHED(ctx);
+      conductivity_dev(P, J0.p, Om, T, Ybuf, sb + 9 * idx);
+      auto op = [&](const double2* x, double2* y) {  // y = x - L(x)
+        apply_L(P, x, LJ.p);
+        sub_kernel<<<eb, 256, 0, s>>>(x, LJ.p, y, n);
+        EPSP_LAUNCHED(ctx);
+      };
+      if (solver == EPSP_SOLVER_GMRES) {
+        // Krylov.gmres(A, b[, x0]; atol = rtol ‖J0‖, rtol = 0, itmax = maxiter), restart = false,
+        // MGS, Givens (src/ladder.jl:340-353).
+        const bool warm = iO > 0;
+        const double atol = rtol * nrm_host(P, J0.p, n, part, scal);
+        std::vector<double> res;
+        // r0 = b - A x0 (warm) or b
+        if (warm) {
+          op(J.p, W.p);
+          axpby_kernel<<<eb, 256, 0, s>>>(make_double2(1, 0), J0.p, make_double2(-1, 0), W.p, n);
+          EPSP_LAUNCHED(ctx);
+        } else {
+          EPSP_CUDA(cudaMemcpyAsync(W.p, J0.p, size_t(n) * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        }
+        const double beta = nrm_host(P, W.p, n, part, scal);
+        double rNorm = beta;
+        res.push_back(beta);
+        bool solved = rNorm <= atol, breakdown = false;
+        int inner = 0;
+        std::vector<cplx> R, sv, z;
+        std::vector<double> cv;
+        if (beta == 0) solved = true;
+        if (!solved) {
+          if (V.empty()) V.emplace_back();
+          if (V[0].n != size_t(n)) V[0].alloc(ctx, size_t(n));
+          axpby_kernel<<<eb, 256, 0, s>>>(make_double2(1.0 / rNorm, 0), W.p, make_double2(0, 0), V[0].p, n);
+          EPSP_LAUNCHED(ctx);
+          z.push_back(beta);
+          int nr = 0;
+          bool tired = false;
+          while (!(solved || tired || breakdown)) {
+            ++inner;
+            op(V[size_t(inner - 1)].p, W.p);  // q = A v_k
+            for (int i = 0; i < inner; ++i) {
+              dot_dev(P, V[size_t(i)].p, W.p, n, part, Hdev.p + i);
+              axpy_dev_kernel<<<eb, 256, 0, s>>>(W.p, V[size_t(i)].p, Hdev.p + i, n);
+              EPSP_LAUNCHED(ctx);
+            }
+            dot_dev(P, W.p, W.p, n, part, Hdev.p + inner);
+            std::vector<double2> hcol(size_t(inner + 1));
+            Hdev.download(hcol.data(), size_t(inner + 1), s);
+            EPSP_CUDA(cudaStreamSynchronize(s));
+            check_tc_err(P);
+            for (int i = 0; i < inner; ++i) R.push_back(cplx(hcol[size_t(i)].x, hcol[size_t(i)].y));
+            const double Hbis = std::sqrt(hcol[size_t(inner)].x);
+            for (int i = 0; i < inner - 1; ++i) {
+              cplx Rt = cv[size_t(i)] * R[size_t(nr + i)] + sv[size_t(i)] * R[size_t(nr + i + 1)];
+              R[size_t(nr + i + 1)] = std::conj(sv[size_t(i)]) * R[size_t(nr + i)] - cv[size_t(i)] * R[size_t(nr + i + 1)];
+              R[size_t(nr + i)] = Rt;
+            }
+            cplx a = R[size_t(nr + inner - 1)];
+            double abs_a = std::abs(a), cc;
+            cplx ss, rho;
+            if (Hbis == 0) {
+              cc = 1;
+              ss = 0;
+              rho = a;
+            } else if (abs_a == 0) {
+              cc = 0;
+              ss = 1;
+              rho = Hbis;
+            } else {
+              double rr = std::hypot(abs_a, Hbis);
+              cplx psi = a / abs_a;
+              cc = abs_a / rr;
+              ss = psi * (Hbis / rr);
+              rho = psi * rr;
+            }
+            cv.push_back(cc);
+            sv.push_back(ss);
+            R[size_t(nr + inner - 1)] = rho;
+            cplx zeta = std::conj(ss) * z[size_t(inner - 1)];
+            z[size_t(inner - 1)] = cc * z[size_t(inner - 1)];
+            rNorm = std::abs(zeta);
+            res.push_back(rNorm);
+            nr += inner;
+            solved = rNorm <= atol || rNorm + 1.0 <= 1.0;
+            breakdown = Hbis <= btol;
+            tired = inner >= maxiter;
+            if (!(solved || tired || breakdown)) {
+              if (V.size() < size_t(inner + 1)) V.emplace_back();
+              if (V[size_t(inner)].n != size_t(n)) V[size_t(inner)].alloc(ctx, size_t(n));
+              axpby_kernel<<<eb, 256, 0, s>>>(make_double2(1.0 / Hbis, 0), W.p, make_double2(0, 0), V[size_t(inner)].p, n);
+              EPSP_LAUNCHED(ctx);
+              z.push_back(zeta);
+            }
+          }
+          std::vector<cplx> y = z;
+          for (int i = inner - 1; i >= 0; --i) {
+            int pos = nr + i - inner;
+            for (int jj = inner - 1; jj >= i + 1; --jj) {
+              y[size_t(i)] -= R[size_t(pos)] * y[size_t(jj)];
+              pos -= jj;
+            }
+            if (std::abs(R[size_t(pos)]) <= btol)
+              y[size_t(i)] = 0;
+            else
+              y[size_t(i)] /= R[size_t(pos)];
+          }
+          // x = x0 + V y (x0 = J for a warm start, else 0)
+          if (!warm) J.zero(s);
+          for (int i = 0; i < inner; ++i) {
+            axpby_kernel<<<eb, 256, 0, s>>>(make_double2(y[size_t(i)].real(), y[size_t(i)].imag()), V[size_t(i)].p,
+                                            make_double2(1, 0), J.p, n);
+            EPSP_LAUNCHED(ctx);
+          }
+        } else if (!warm) {
+          J.zero(s);
+        }
+        conv[idx] = solved ? 1 : 0;
+        niter[idx] = inner;
+        if (hist && hist->norms && hist->nnorms) {
+          int32_t nn = int32_t(std::min<size_t>(res.size(), size_t(maxiter + 1)));
+          for (int32_t k = 0; k < nn; ++k) hist->norms[size_t(maxiter + 1) * size_t(idx) + size_t(k)] = res[size_t(k)];
+          hist->nnorms[idx] = nn;
+        }
+        if (hist && hist->nsigma) hist->nsigma[idx] = 0;
+      } else {
+        // J ← J0 + L(J) from J0 until the relative change of σ is below rtol (src/ladder.jl:354-369)
+        EPSP_CUDA(cudaMemcpyAsync(J.p, J0.p, size_t(n) * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        double sprev[9] = {}, scur[9];
+        conv[idx] = 0;
+        int32_t ns_ = 0;
+        for (int32_t it = 1; it <= maxiter; ++it) {
+          apply_L(P, J.p, LJ.p);
+          add_kernel<<<eb, 256, 0, s>>>(J0.p, LJ.p, J.p, n);
+          EPSP_LAUNCHED(ctx);
+          check_tc_err(P);
+          conductivity_dev(P, J.p, Om, T, Ybuf, scur);
+          if (hist && hist->sigma_iter)
+            for (int k = 0; k < 9; ++k) hist->sigma_iter[9 * (size_t(maxiter) * size_t(idx) + size_t(it - 1)) + size_t(k)] = scur[k];
+          ns_ = it;
+          niter[idx] = it;
+          if (it > 1) {
+            double d[9];
+            for (int k = 0; k < 9; ++k) d[k] = scur[k] - sprev[k];
+            if (mat3_norm(d) < rtol * mat3_norm(scur)) {
+              conv[idx] = 1;
+              break;
+            }
+          }
+          std::copy(scur, scur + 9, sprev);
+        }
+        if (hist && hist->nsigma) hist->nsigma[idx] = ns_;
+        if (hist && hist->nnorms) hist->nnorms[idx] = 0;
+      }
+      conductivity_dev(P, J.p, Om, T, Ybuf, sl + 9 * idx);
+      if (J_out) {
+        J.download(reinterpret_cast<double2*>(J_out) + size_t(n) * size_t(idx), size_t(n), s);
+        EPSP_CUDA(cudaStreamSynchronize(s));
+      }
+    }
+  }
+}
+
+}  // namespace epsp
+
+using namespace epsp;
+
+template <class F>
+static epsp_status lguard(Ctx* c, F&& f) {
+  try {
+    EPSP_CUDA(cudaSetDevice(c->device));
+    f();
+    c->last_error.clear();
+    return EPSP_OK;
+  } catch (const Error& e) {
+    c->last_error = e.msg;
+    return epsp_status(e.code);
+  } catch (const std::bad_alloc&) {
+    c->last_error = "host allocation failed";
+    return EPSP_ENOMEM;
+  } catch (const std::exception& e) {
+    c->last_error = e.what();
+    return EPSP_EINVAL;
+  }
+}
+
+extern "C" {
+
+epsp_status epsp_ladder_setup(epsp_ctx* ctx, const epsp_model* model, const epsp_options* opts, epsp_ladder_plan** plan) {
+  if (!ctx || !plan) return EPSP_EINVAL;
+  *plan = nullptr;
+  return lguard(&ctx->c, [&] { *plan = reinterpret_cast<epsp_ladder_plan*>(ladder_setup(&ctx->c, model, opts)); });
+}
+
+void epsp_ladder_plan_destroy(epsp_ladder_plan* plan) {
+  if (!plan) return;
+  auto* P = reinterpret_cast<LadderPlan*>(plan);
+  cudaSetDevice(P->ctx->device);
+  delete P;
+}
+
+epsp_status epsp_ladder_run(epsp_ladder_plan* plan, const double* sigma, const double* mu, const double* Tlist, int64_t nT,
+                            const double* Omegas, int64_t nOmega, int32_t solver, double rtol, int32_t maxiter,
+                            double* sigma_bubble, double* sigma_ladder, uint8_t* converged, int32_t* niter,
+                            epsp_ladder_history* hist, double* J_out) {
+  if (!plan) return EPSP_EINVAL;
+  auto* P = reinterpret_cast<LadderPlan*>(plan);
+  return lguard(P->ctx, [&] {
+    ladder_run(P, sigma, mu, Tlist, nT, Omegas, nOmega, solver, rtol, maxiter, sigma_bubble, sigma_ladder, converged, niter,
+               hist, J_out);
+  });
+}
+
+epsp_status epsp_ladder_apply(epsp_ladder_plan* plan, const double* sigma_T, double mu, double T, double Omega, const double* J,
+                              double* LJ) {
+  if (!plan || !sigma_T || !J || !LJ) return EPSP_EINVAL;
+  auto* P = reinterpret_cast<LadderPlan*>(plan);
+  return lguard(P->ctx, [&] {
+    if (!(T >= 0)) fail(EPSP_EINVAL, "Temperature must be positive");
+    cudaStream_t s = P->ctx->stream;
+    const long n = P->nw * 24 * P->ni;
+    P->d_ST.upload(reinterpret_cast<const double2*>(sigma_T), size_t(P->nw * P->ni), s);
+    set_propagators(P, mu, T, Omega);
+    DBuf<double2> dJ, dLJ;
+    dJ.alloc(P->ctx, size_t(n));
+    dLJ.alloc(P->ctx, size_t(n));
+    dJ.upload(reinterpret_cast<const double2*>(J), size_t(n), s);
+    apply_L(P, dJ.p, dLJ.p);
+    dLJ.download(reinterpret_cast<double2*>(LJ), size_t(n), s);
+    EPSP_CUDA(cudaStreamSynchronize(s));
+    check_tc_err(P);
+  });
+}
+
+}  // extern "C"
