@@ -47,6 +47,7 @@ struct Ctx {
   size_t prof_used = 0;
   // Host-side test hook: the next allocation of at least `fail_alloc_bytes` fails (0 = off).
   size_t fail_alloc_bytes = 0;
+  cudaEvent_t timer[2] = {nullptr, nullptr};
 };
 
 // Records the start event of a profiled launch; returns the pair index or -1.

@@ -106,6 +106,8 @@ void epsp_destroy(epsp_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->c.device);
   for (auto e : c->c.prof_events) cudaEventDestroy(e);
+  for (auto e : c->c.timer)
+    if (e) cudaEventDestroy(e);
   if (c->c.stream) cudaStreamDestroy(c->c.stream);
   delete c;
 }
@@ -137,6 +139,26 @@ epsp_status epsp_profile_read(epsp_ctx* c, double* total_ms, int64_t* count) {
   if (total_ms) *total_ms = tot;
   if (count) *count = int64_t(n);
   c->c.prof_used = 0;
+  return EPSP_OK;
+}
+
+/* Device-side stopwatch on the context's stream (for benchmarks): epsp_timer_begin records a start
+ * event, epsp_timer_end a stop event, waits for it and returns the elapsed milliseconds. */
+epsp_status epsp_timer_begin(epsp_ctx* c) {
+  if (!c) return EPSP_EINVAL;
+  if (!c->c.timer[0]) {
+    if (cudaEventCreate(&c->c.timer[0]) != cudaSuccess || cudaEventCreate(&c->c.timer[1]) != cudaSuccess) return EPSP_ECUDA;
+  }
+  return cudaEventRecord(c->c.timer[0], c->c.stream) == cudaSuccess ? EPSP_OK : EPSP_ECUDA;
+}
+
+epsp_status epsp_timer_end(epsp_ctx* c, double* ms) {
+  if (!c || !c->c.timer[0]) return EPSP_EINVAL;
+  if (cudaEventRecord(c->c.timer[1], c->c.stream) != cudaSuccess || cudaEventSynchronize(c->c.timer[1]) != cudaSuccess)
+    return EPSP_ECUDA;
+  float f = 0;
+  if (cudaEventElapsedTime(&f, c->c.timer[0], c->c.timer[1]) != cudaSuccess) return EPSP_ECUDA;
+  if (ms) *ms = double(f);
   return EPSP_OK;
 }
 

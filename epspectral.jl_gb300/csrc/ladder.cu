@@ -57,8 +57,17 @@ struct LadderPlan {
   DBuf<double> d_wlo, d_whi, d_g2, d_wq, d_wf, d_R, d_B, d_Bt, d_X, d_Cp, d_Cm;
   long Ktot = 0;
   double Bt_T = std::numeric_limits<double>::quiet_NaN();  // temperature B̃ was built for
-  // GEMM paths
-  long Kx = 0, Kp = 0;
+  // GEMM paths: rows (j, q, c0, ri) with j padded to nwp (a multiple of 32), K = (ν, b, i') with ν
+  // padded to nmp (a multiple of 16)
+  long nwp = 0, nmp = 0;
+  long Kx = 0, Kp = 0, Kp2 = 0;
+  DBuf<int32_t> d_mt_k;          // [nwp, nmp, 2][2] first nodes of the two shift tables of a mode
+  DBuf<float> d_mt_w;            // [nwp, nmp, 2][4] their weights (1 - r) wlo, (1 - r) whi, r wlo, r whi
+  DBuf<float> d_nnu_f;
+  DBuf<__nv_bfloat16> d_KKh, d_KKl, d_Yh, d_Yl;
+  DBuf<float> d_part2;
+  TcOperand opKK{}, opY{};
+  int bn2 = 128, splits2 = 1;
   DBuf<double> d_Gt, d_Af, d_D;   // G̃ [Kx, 3ni]; A (FP64) [24nω, Kx]; D [24nω, 3ni]
   DBuf<int32_t> d_mnu;
   DBuf<double> d_rnu, d_nnu;
@@ -306,7 +315,7 @@ __global__ void finish_direct_kernel(const double* __restrict__ Cp, const double
 // One thread per (ν, i), looping over the stars in order.
 __global__ void coupling_rot_kernel(const double* __restrict__ g2, const double* __restrict__ R, const double* __restrict__ w_f,
                                     const int32_t* __restrict__ by_star, const int32_t* __restrict__ star_ptr,
-                                    const double* __restrict__ wnu, double w_ac, int nm, int ni, long Kx,
+                                    const double* __restrict__ wnu, double w_ac, int nm, int nmp, int ni, long Kx,
                                     double* __restrict__ Gt) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= long(nm) * ni) return;
@@ -322,7 +331,7 @@ __global__ void coupling_rot_kernel(const double* __restrict__ g2, const double*
           for (int a = 0; a < 3; ++a) acc[a][b] += R[a + 3 * (b + 3 * f)] * g;
       }
     for (int b = 0; b < 3; ++b)
-      for (int a = 0; a < 3; ++a) Gt[(nu + long(nm) * (b + 3l * ip)) + Kx * (a + 3l * i)] = acc[a][b];
+      for (int a = 0; a < 3; ++a) Gt[(nu + long(nmp) * (b + 3l * ip)) + Kx * (a + 3l * i)] = acc[a][b];
   }
 }
 
@@ -363,54 +372,105 @@ __device__ __forceinline__ double xgen_value(const double2* __restrict__ J, cons
   }
 }
 
-// FP64 A operand, column-major [24 nω, Kx].
+// FP64 A operand, column-major [24 nwp, Kx] (rows j >= nω and modes ν >= nm are zero).
 __global__ void xgen_f64_kernel(const double2* __restrict__ J, const int32_t* __restrict__ klo, const double* __restrict__ wlo,
                                 const double* __restrict__ whi, const int32_t* __restrict__ mnu, const double* __restrict__ rnu,
-                                const double* __restrict__ nnu, int nw, int ns, int nm, int ni, double* __restrict__ A) {
-  const long nrow = 24l * nw;
+                                const double* __restrict__ nnu, int nw, int nwp, int ns, int nm, int nmp, int ni,
+                                double* __restrict__ A) {
+  const long nrow = 24l * nwp;
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= nrow * nm * 3 * ni) return;
+  if (idx >= nrow * nmp * 3 * ni) return;
   long row = idx % nrow, k = idx / nrow;
-  int j = int(row % nw);
-  int rr = int(row / nw);
+  int j = int(row % nwp);
+  int rr = int(row / nwp);
   int q = rr % 6, c0 = (rr / 6) % 2, ri = rr / 12;
-  int nu = int(k % nm), b = int((k / nm) % 3);
-  long ip = k / (3l * nm);
-  A[idx] = xgen_value(J, klo, wlo, whi, nw, ns, j, q, c0, ri, mnu[nu], rnu[nu], nnu[nu], b, ip);
+  int nu = int(k % nmp), b = int((k / nmp) % 3);
+  long ip = k / (3l * nmp);
+  A[idx] = (j < nw && nu < nm) ? xgen_value(J, klo, wlo, whi, nw, ns, j, q, c0, ri, mnu[nu], rnu[nu], nnu[nu], b, ip) : 0.0;
 }
 
-// BF16 hi/lo A operand, row-major [24 nω][Kp], through a shared-memory transpose (32 rows x 64 k).
-__global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restrict__ J, const int32_t* __restrict__ klo,
-                                                        const double* __restrict__ wlo, const double* __restrict__ whi,
-                                                        const int32_t* __restrict__ mnu, const double* __restrict__ rnu,
-                                                        const double* __restrict__ nnu, int nw, int ns, int nm, int ni,
-                                                        long Kx, long Kp, __nv_bfloat16* __restrict__ Ah,
-                                                        __nv_bfloat16* __restrict__ Al) {
-  __shared__ float tile[64][33];
-  const long nrow = 24l * nw;
+// BF16 hi/lo A operand, row-major [24 nwp][Kp], FP32 arithmetic. A block owns 32 rows (32 nodes j
+// of one row group (q, c0, re/im), nwp being a multiple of 32) and kXgTiles K-tiles of 64 columns
+// (4 pairs (b, i') x 16 modes). Per K-tile it stages the window of the vertex the shift tables of
+// its nodes can reach (nodes j0 - W .. j0 + 32 + W, W = nshift + 2, zero outside the grid) in
+// shared memory; the mode tables mt (two shift tables per mode and sign, with the tent weights
+// folded in) are staged once per block. The tile is transposed through shared memory so that the
+// BF16 rows are written 16 bytes at a time.
+constexpr int kXgTiles = 8;
+
+__global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restrict__ J, const int32_t* __restrict__ mt_k,
+                                                        const float* __restrict__ mt_w, const float* __restrict__ nnu,
+                                                        int nw, int nwp, int ns, int nmp, int ni, long Kx, long Kp,
+                                                        __nv_bfloat16* __restrict__ Ah, __nv_bfloat16* __restrict__ Al) {
+  extern __shared__ float xg_smem[];
+  const int W = ns + 2, win = 32 + 2 * W;
+  float* s_w = xg_smem;                                   // [32][16][2][4]
+  int* s_k = reinterpret_cast<int*>(s_w + 32 * 16 * 2 * 4); // [32][16][2][2]
+  float* s_j = reinterpret_cast<float*>(s_k + 32 * 16 * 2 * 2);  // [4][win]
+  float (*tile)[33] = reinterpret_cast<float (*)[33]>(s_j + 4 * win);  // [64][33]
   const long r0 = long(blockIdx.x) * 32;
-  const long k0 = long(blockIdx.y) * 64;
-  const int tr = threadIdx.x % 32, tk = threadIdx.x / 32;
-  const long row = r0 + tr;
-  const int j = int(row % nw);
-  const int rr = int(row / nw);
-  const int q = rr % 6, c0 = (rr / 6) % 2, ri = (rr / 12) % 2;
-#pragma unroll 1
-  for (int p = 0; p < 8; ++p) {
-    const int kl = tk + 8 * p;
-    const long k = k0 + kl;
-    float v = 0.f;
-    if (row < nrow && k < Kx) {
-      const int nu = int(k % nm), b = int((k / nm) % 3);
-      const long ip = k / (3l * nm);
-      v = float(xgen_value(J, klo, wlo, whi, nw, ns, j, q, c0, ri, mnu[nu], rnu[nu], nnu[nu], b, ip));
-    }
-    tile[kl][tr] = v;
+  const int rr = int(r0 / nwp), j0 = int(r0 % nwp);
+  const int q = rr % 6, c0 = (rr / 6) % 2, ri = rr / 12;
+  const int c12 = (q < 2) ? 0 : (q < 4 ? 3 : (q == 4 ? 1 : 2));
+  // mode tables of the block's nodes
+  for (int e = threadIdx.x; e < 32 * 16 * 2; e += 256) {
+    const int jj = e / 32, rest = e % 32;  // rest = (nu, s)
+    const long g = (long(j0 + jj) * nmp) * 2 + rest;  // [j][nu][s] with nmp == 16 per K-group
+    const bool ok = j0 + jj < nwp;
+    for (int t = 0; t < 4; ++t) s_w[e * 4 + t] = ok ? mt_w[g * 4 + t] : 0.f;
+    for (int t = 0; t < 2; ++t) s_k[e * 2 + t] = ok ? mt_k[g * 2 + t] : 0;
   }
-  __syncthreads();
-  const int wr = threadIdx.x / 8, kc = (threadIdx.x % 8) * 8;
-  const long orow = r0 + wr;
-  if (orow < nrow) {
+  const int tr = threadIdx.x % 32, tk = threadIdx.x / 32;
+  const int j = j0 + tr;
+  const long kt0 = long(blockIdx.y) * kXgTiles;
+  for (int kt = 0; kt < kXgTiles; ++kt) {
+    const long k0 = (kt0 + kt) * 64;
+    if (k0 >= Kp) break;
+    __syncthreads();
+    // vertex window of the 4 pairs (b, i') of this K-tile
+    for (int e = threadIdx.x; e < 4 * win; e += 256) {
+      const int g = e / win, node = j0 - W + e % win;
+      const long pair = (k0 / 16) + g;  // (b, i') index = k / 16
+      float v = 0.f;
+      if (node >= 0 && node < nw && pair < 3l * ni) {
+        const int b = int(pair % 3);
+        const long ip = pair / 3;
+        const double2 z = J[jidx(nw, node, c12, b, c0, ip)];
+        v = float(ri == 0 ? z.x : z.y);
+      }
+      s_j[e] = v;
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int p = 0; p < 8; ++p) {
+      const int kl = tk + 8 * p;           // 0..63
+      const int g = kl / 16, nu = kl % 16;
+      const long k = k0 + kl;
+      float v = 0.f;
+      if (j < nw && k < Kx) {
+        const float* jw = s_j + g * win - (j0 - W);
+        float xs[2];
+#pragma unroll
+        for (int sg = 0; sg < 2; ++sg) {
+          const int e = (tr * 16 + nu) * 2 + sg;
+          const int ka = s_k[e * 2], kb = s_k[e * 2 + 1];
+          const float* w4 = s_w + e * 4;
+          xs[sg] = w4[0] * jw[ka] + w4[1] * jw[ka + 1] + w4[2] * jw[kb] + w4[3] * jw[kb + 1];
+        }
+        const float n = nnu[nu];
+        switch (q) {
+          case 0:
+          case 2: v = 0.5f * (xs[0] - xs[1]); break;
+          case 1:
+          case 3: v = -(0.5f + n) * (xs[0] + xs[1]); break;
+          case 4: v = n * xs[0] + (1.f + n) * xs[1]; break;
+          default: v = (1.f + n) * xs[0] + n * xs[1]; break;
+        }
+      }
+      tile[kl][tr] = v;
+    }
+    __syncthreads();
+    const int wr = threadIdx.x / 8, kc = (threadIdx.x % 8) * 8;
     __align__(16) __nv_bfloat16 hh[8], ll[8];
 #pragma unroll
     for (int t = 0; t < 8; ++t) {
@@ -418,10 +478,31 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
       hh[t] = __float2bfloat16_rn(x);
       ll[t] = __float2bfloat16_rn(x - __bfloat162float(hh[t]));
     }
-    const long off = orow * Kp + k0 + kc;
+    const long off = (r0 + wr) * Kp + k0 + kc;
     *reinterpret_cast<uint4*>(Ah + off) = *reinterpret_cast<const uint4*>(hh);
     *reinterpret_cast<uint4*>(Al + off) = *reinterpret_cast<const uint4*>(ll);
   }
+}
+
+static size_t xgen_smem_bytes(int ns) {
+  const int W = ns + 2, win = 32 + 2 * W;
+  return size_t(32 * 16 * 2 * 4) * 4 + size_t(32 * 16 * 2 * 2) * 4 + size_t(4 * win) * 4 + size_t(64 * 33) * 4;
+}
+
+// Y (rows q = 0, 2 of D) as the BF16 hi/lo B operand of the Kramers-Kronig GEMM: row (qq, c0, ri, n),
+// K = ω' contiguous, stride Kp2.
+__global__ void y_split_kernel(const double* __restrict__ D, int nw, int nwp, long N, long Kp2, __nv_bfloat16* __restrict__ Yh,
+                               __nv_bfloat16* __restrict__ Yl) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= 8 * N * Kp2) return;
+  long w = idx % Kp2, r = idx / Kp2;
+  int qq = int(r % 2), c0 = int((r / 2) % 2), ri = int((r / 4) % 2);
+  long n = r / 8;
+  float x = 0.f;
+  if (w < nw) x = float(D[w + long(nwp) * ((qq == 0 ? 0 : 2) + 6 * (c0 + 2 * ri)) + 24l * nwp * n]);
+  __nv_bfloat16 h = __float2bfloat16_rn(x);
+  Yh[idx] = h;
+  Yl[idx] = __float2bfloat16_rn(x - __bfloat162float(h));
 }
 
 __global__ void split_rows_plain_kernel(const double* __restrict__ S, long rows, long cols, long ld, long Kp,
@@ -431,6 +512,18 @@ __global__ void split_rows_plain_kernel(const double* __restrict__ S, long rows,
   if (idx >= rows * Kp) return;
   long r = idx / Kp, c = idx % Kp;
   float x = c < cols ? float(S[c + ld * r]) : 0.f;
+  __nv_bfloat16 h = __float2bfloat16_rn(x);
+  oh[idx] = h;
+  ol[idx] = __float2bfloat16_rn(x - __bfloat162float(h));
+}
+
+// out[r * Kp + c] = split(S[r + ldr c]) for c < cols (a column-major matrix read by rows).
+__global__ void split_rows_t2_kernel(const double* __restrict__ S, long ldr, long rows, long cols, long Kp,
+                                     __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= rows * Kp) return;
+  long r = idx / Kp, c = idx % Kp;
+  float x = c < cols ? float(S[r + ldr * c]) : 0.f;
   __nv_bfloat16 h = __float2bfloat16_rn(x);
   oh[idx] = h;
   ol[idx] = __float2bfloat16_rn(x - __bfloat162float(h));
@@ -446,7 +539,7 @@ __global__ void sum_parts_kernel(const float* __restrict__ part, long n, int spl
 }
 
 // Y of the regrouped path: the rows q = 0 (c12 = 11) and q = 2 (c12 = 22) of D, as [nω, (qq, c0, ri, n)].
-__global__ void y_gemm_kernel(const double* __restrict__ D, int nw, long ncol, double* __restrict__ Y) {
+__global__ void y_gemm_kernel(const double* __restrict__ D, int nw, int nwp, long ncol, double* __restrict__ Y) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
   long total = long(nw) * 8 * ncol;
   if (idx >= total) return;
@@ -454,11 +547,11 @@ __global__ void y_gemm_kernel(const double* __restrict__ D, int nw, long ncol, d
   int qq = int(r % 2), c0 = int((r / 2) % 2), ri = int((r / 4) % 2);
   long n = r / 8;
   int q = qq == 0 ? 0 : 2;
-  Y[idx] = D[w + nw * (q + 6 * (c0 + 2 * ri)) + 24l * nw * n];
+  Y[idx] = D[w + long(nwp) * (q + 6 * (c0 + 2 * ri)) + 24l * nwp * n];
 }
 
 __global__ void finish_gemm_kernel(const double* __restrict__ D, const double* __restrict__ KY, const double2* __restrict__ Gm,
-                                   const double2* __restrict__ Gp, int nw, int ni, double2* __restrict__ LJ) {
+                                   const double2* __restrict__ Gp, int nw, int nwp, int ni, double2* __restrict__ LJ) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= long(nw) * 6 * ni) return;
   long w = idx % nw;
@@ -466,7 +559,7 @@ __global__ void finish_gemm_kernel(const double* __restrict__ D, const double* _
   int a = int(r % 3), c0 = int((r / 3) % 2);
   long i = r / 6;
   const long n = a + 3 * i;
-  auto d = [&](int q, int ri) { return D[w + nw * (q + 6 * (c0 + 2 * ri)) + 24l * nw * n]; };
+  auto d = [&](int q, int ri) { return D[w + long(nwp) * (q + 6 * (c0 + 2 * ri)) + 24l * nwp * n]; };
   auto ky = [&](int qq, int ri) { return KY[w + nw * (qq + 2 * (c0 + 2 * (ri + 2 * n)))]; };
   double2 K[4];
   {
@@ -750,19 +843,61 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
     P->d_mnu = to_device(ctx, P->m_nu);
     P->d_rnu = to_device(ctx, P->r_nu);
     P->d_nnu.alloc(ctx, size_t(nm));
+    P->d_nnu_f.alloc(ctx, 16);
     auto d_wnu = to_device(ctx, P->wnu);
-    P->Kx = nm * 3 * ni;
+    P->nwp = (nw + 31) / 32 * 32;
+    P->nmp = (nm + 15) / 16 * 16;
+    if (P->path == EPSP_PATH_GEMM_BF16X3 && P->nmp != 16)
+      fail(EPSP_EUNSUPPORTED, "the BF16x3 ladder path takes at most 16 modes; use EPSP_PATH_GEMM_FP64");
+    P->Kx = P->nmp * 3 * ni;
     P->d_Gt.alloc(ctx, size_t(P->Kx * 3 * ni));
+    P->d_Gt.zero(s);
     coupling_rot_kernel<<<div_up(size_t(nm * ni), 128), 128, 0, s>>>(P->d_g2.p, P->d_R.p, P->d_wf.p, P->d_by_star.p,
-                                                                     P->d_star_ptr.p, d_wnu.p, P->w_ac, int(nm), int(ni),
-                                                                     P->Kx, P->d_Gt.p);
+                                                                     P->d_star_ptr.p, d_wnu.p, P->w_ac, int(nm), int(P->nmp),
+                                                                     int(ni), P->Kx, P->d_Gt.p);
     EPSP_LAUNCHED(ctx);
-    P->d_D.alloc(ctx, size_t(24 * nw * 3 * ni));
+    const long M = 24 * P->nwp, N = 3 * ni;
+    P->d_D.alloc(ctx, size_t(M * N));
     if (P->path == EPSP_PATH_GEMM_FP64) {
-      P->d_Af.alloc(ctx, size_t(24 * nw * P->Kx));
+      P->d_Af.alloc(ctx, size_t(M * P->Kx));
     } else {
+      // mode tables: for node j, mode ν and sign s, the two shift tables (m_ν, m_ν + 1) with the
+      // tent weights (1 - r_ν, r_ν) folded into their interpolation weights (FP32).
+      {
+        const long nwp = P->nwp;
+        std::vector<int32_t> hk(size_t(nwp * 16 * 2 * 2));
+        std::vector<float> hw(size_t(nwp * 16 * 2 * 4), 0.f);
+        std::vector<int32_t> klo(size_t(nw * ns * 2));
+        std::vector<double> wlo(klo.size()), whi(klo.size());
+        P->d_klo.download(klo.data(), klo.size(), s);
+        P->d_wlo.download(wlo.data(), wlo.size(), s);
+        P->d_whi.download(whi.data(), whi.size(), s);
+        EPSP_CUDA(cudaStreamSynchronize(s));
+        for (long j = 0; j < nwp; ++j)
+          for (long nu = 0; nu < 16; ++nu)
+            for (long sg = 0; sg < 2; ++sg) {
+              const size_t e = size_t((j * 16 + nu) * 2 + sg);
+              hk[2 * e] = hk[2 * e + 1] = int32_t(j);
+              if (j >= nw || nu >= nm || P->wnu[size_t(nu)] < P->w_ac) continue;
+              const long mm = P->m_nu[size_t(nu)];
+              const double r = P->r_nu[size_t(nu)];
+              const size_t t0 = size_t(j + nw * (mm + ns * sg));
+              hk[2 * e] = klo[t0];
+              hw[4 * e] = float((1 - r) * wlo[t0]);
+              hw[4 * e + 1] = float((1 - r) * whi[t0]);
+              hk[2 * e + 1] = hk[2 * e];
+              if (mm + 1 < ns && r != 0.0) {
+                const size_t t1 = size_t(j + nw * (mm + 1 + ns * sg));
+                hk[2 * e + 1] = klo[t1];
+                hw[4 * e + 2] = float(r * wlo[t1]);
+                hw[4 * e + 3] = float(r * whi[t1]);
+              }
+            }
+        P->d_mt_k = to_device(ctx, hk);
+        P->d_mt_w = to_device(ctx, hw);
+      }
       P->Kp = (P->Kx + 63) / 64 * 64;
-      const long M = 24 * nw, N = 3 * ni;
+      P->Kp2 = (nw + 63) / 64 * 64;
       P->d_Ah.alloc(ctx, size_t(M * P->Kp));
       P->d_Al.alloc(ctx, size_t(M * P->Kp));
       P->d_Gh.alloc(ctx, size_t(N * P->Kp));
@@ -776,6 +911,19 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       P->d_err.zero(s);
       P->opA = {make_tmap_bf16(P->d_Ah.p, M, P->Kx, P->Kp, kTcBM), make_tmap_bf16(P->d_Al.p, M, P->Kx, P->Kp, kTcBM)};
       P->opG = {make_tmap_bf16(P->d_Gh.p, N, P->Kx, P->Kp, P->bn), make_tmap_bf16(P->d_Gl.p, N, P->Kx, P->Kp, P->bn)};
+      // the Kramers-Kronig image on the tensor cores: A = KK [nω][nω'], B = Y [8N][nω']
+      P->d_KKh.alloc(ctx, size_t(nw * P->Kp2));
+      P->d_KKl.alloc(ctx, size_t(nw * P->Kp2));
+      split_rows_t2_kernel<<<div_up(size_t(nw * P->Kp2), 256), 256, 0, s>>>(P->d_KK.p, nw, nw, nw, P->Kp2, P->d_KKh.p,
+                                                                            P->d_KKl.p);
+      EPSP_LAUNCHED(ctx);
+      P->d_Yh.alloc(ctx, size_t(8 * N * P->Kp2));
+      P->d_Yl.alloc(ctx, size_t(8 * N * P->Kp2));
+      tc_gemm_shape(ctx, int(nw), int(8 * N), int(nw), 16, &P->bn2, &P->splits2);
+      P->d_part2.alloc(ctx, size_t(P->splits2) * size_t(nw * 8 * N));
+      P->opKK = {make_tmap_bf16(P->d_KKh.p, nw, nw, P->Kp2, kTcBM), make_tmap_bf16(P->d_KKl.p, nw, nw, P->Kp2, kTcBM)};
+      P->opY = {make_tmap_bf16(P->d_Yh.p, 8 * N, nw, P->Kp2, P->bn2), make_tmap_bf16(P->d_Yl.p, 8 * N, nw, P->Kp2, P->bn2)};
+      EPSP_CUDA(cudaFuncSetAttribute(xgen_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(xgen_smem_bytes(int(ns)))));
     }
     EPSP_CUDA(cudaStreamSynchronize(s));
   } else {
@@ -880,40 +1028,52 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ) {
   // regrouped GEMM paths
   if (P->Bt_T != T) {
     std::vector<double> nnu(size_t(P->nm));
+    std::vector<float> nf16(16, 0.f);
     for (long nu = 0; nu < P->nm; ++nu) {
       double w = P->wnu[size_t(nu)];
       nnu[size_t(nu)] = w < P->w_ac ? 0.0 : (T > 1.4901161193847656e-08 ? (w == 0 ? -0.5 : 1.0 / std::expm1(w / T)) : (w > 0 ? 0.0 : -1.0));
+      if (nu < 16) nf16[size_t(nu)] = float(nnu[size_t(nu)]);
     }
     P->d_nnu.upload(nnu.data(), size_t(P->nm), s);
+    P->d_nnu_f.upload(nf16.data(), 16, s);
     EPSP_CUDA(cudaStreamSynchronize(s));
     P->Bt_T = T;
   }
-  const long M = 24 * nw, N = 3 * ni;
+  const long nwp = P->nwp, M = 24 * nwp, N = 3 * ni;
   if (P->path == EPSP_PATH_GEMM_FP64) {
     long px = prof_begin(ctx, "xgen");
     xgen_f64_kernel<<<div_up(size_t(M * P->Kx), 256), 256, 0, s>>>(J, P->d_klo.p, P->d_wlo.p, P->d_whi.p, P->d_mnu.p, P->d_rnu.p,
-                                                                   P->d_nnu.p, int(nw), int(ns), int(P->nm), int(ni), P->d_Af.p);
+                                                                   P->d_nnu.p, int(nw), int(nwp), int(ns), int(P->nm),
+                                                                   int(P->nmp), int(ni), P->d_Af.p);
     EPSP_LAUNCHED(ctx);
     prof_end(ctx, px);
     long pg = prof_begin(ctx, "ladder_gemm");
     gemm_f64(ctx, false, int(M), int(N), int(P->Kx), 1.0, P->d_Af.p, M, P->d_Gt.p, P->Kx, 0.0, P->d_D.p, M);
     prof_end(ctx, pg);
+    const long ny = nw * 8 * N;
+    y_gemm_kernel<<<div_up(size_t(ny), 256), 256, 0, s>>>(P->d_D.p, int(nw), int(nwp), N, P->d_Y.p);
+    EPSP_LAUNCHED(ctx);
+    gemm_f64(ctx, false, int(nw), int(8 * N), int(nw), 1.0, P->d_KK.p, nw, P->d_Y.p, nw, 0.0, P->d_KY.p, nw);
   } else {
     long px = prof_begin(ctx, "xgen");
-    xgen_bf16_kernel<<<dim3(div_up(size_t(M), 32), unsigned(P->Kp / 64)), 256, 0, s>>>(
-        J, P->d_klo.p, P->d_wlo.p, P->d_whi.p, P->d_mnu.p, P->d_rnu.p, P->d_nnu.p, int(nw), int(ns), int(P->nm), int(ni), P->Kx,
-        P->Kp, P->d_Ah.p, P->d_Al.p);
+    const unsigned ktiles = unsigned((P->Kp / 64 + kXgTiles - 1) / kXgTiles);
+    xgen_bf16_kernel<<<dim3(unsigned(M / 32), ktiles), 256, xgen_smem_bytes(int(ns)), s>>>(
+        J, P->d_mt_k.p, P->d_mt_w.p, P->d_nnu_f.p, int(nw), int(nwp), int(ns), int(P->nmp), int(ni), P->Kx, P->Kp, P->d_Ah.p,
+        P->d_Al.p);
     EPSP_LAUNCHED(ctx);
     prof_end(ctx, px);
-    int sp = tc_gemm_launch(ctx, P->opA, P->opG, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N, 16, P->d_err.p);
+    int sp = tc_gemm_launch(ctx, P->opA, P->opG, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N, 16, P->d_err.p, "tc_ladder");
     sum_parts_kernel<<<div_up(size_t(M * N), 256), 256, 0, s>>>(P->d_part.p, M * N, sp, M * N, P->d_D.p);
     EPSP_LAUNCHED(ctx);
+    y_split_kernel<<<div_up(size_t(8 * N * P->Kp2), 256), 256, 0, s>>>(P->d_D.p, int(nw), int(nwp), N, P->Kp2, P->d_Yh.p, P->d_Yl.p);
+    EPSP_LAUNCHED(ctx);
+    int sp2 = tc_gemm_launch(ctx, P->opKK, P->opY, int(nw), int(8 * N), int(nw), P->d_part2.p, nw, nw * 8 * N, 16, P->d_err.p,
+                             "tc_ladder_kk");
+    sum_parts_kernel<<<div_up(size_t(nw * 8 * N), 256), 256, 0, s>>>(P->d_part2.p, nw * 8 * N, sp2, nw * 8 * N, P->d_KY.p);
+    EPSP_LAUNCHED(ctx);
   }
-  const long ny = nw * 8 * N;
-  y_gemm_kernel<<<div_up(size_t(ny), 256), 256, 0, s>>>(P->d_D.p, int(nw), N, P->d_Y.p);
-  EPSP_LAUNCHED(ctx);
-  gemm_f64(ctx, false, int(nw), int(8 * N), int(nw), 1.0, P->d_KK.p, nw, P->d_Y.p, nw, 0.0, P->d_KY.p, nw);
-  finish_gemm_kernel<<<div_up(size_t(nw * 6 * ni), 256), 256, 0, s>>>(P->d_D.p, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, int(nw), int(ni), LJ);
+  finish_gemm_kernel<<<div_up(size_t(nw * 6 * ni), 256), 256, 0, s>>>(P->d_D.p, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, int(nw), int(nwp),
+                                                                     int(ni), LJ);
   EPSP_LAUNCHED(ctx);
 }
 

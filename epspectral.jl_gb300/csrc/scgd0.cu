@@ -12,6 +12,8 @@
 #include "gemm_f64.cuh"
 #include "scgd0.cuh"
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <chrono>
 #include <limits>
@@ -324,31 +326,67 @@ __device__ __forceinline__ double float_middle_d(double x, double y) {
   return negate ? -m : m;
 }
 
-// The μ solve of one temperature (src/scgd0.jl:309-324): the root of n(μ) - n_target with
-// n(μ) = compute_ncarrier_spectral (src/scgd0.jl:361-366) by bisection over floating-point values
-// on the bracket, FP64 throughout; each evaluation is a fixed-order block sum over ωs_spectral.
+// The μ solve of one temperature (src/scgd0.jl:309-324): the root of n(μ) - n_target on the bracket,
+// n(μ) = compute_ncarrier_spectral (src/scgd0.jl:361-366), FP64 throughout. The reference
+// bisects to adjacent floats (Roots.find_zero on a bracket, ~64 evaluations); here a safeguarded
+// Newton iteration on the same bracket finds the same root (n is increasing in μ, with
+// dn/dμ = g Σ_a D_a f(1 - f)/T), falling back to Roots' floating-point midpoint whenever the
+// Newton step leaves the bracket, and stops at a step below 2^-50 max(|μ|, 1) or at adjacent floats.
+// One cluster of kMuCluster CTAs per temperature: each CTA sums a slice of ωs_spectral in fixed
+// order, the partials are combined through distributed shared memory in rank order, so every
+// thread of the cluster holds the same totals and takes the same branches.
 // status: 0 ok, 1 no sign change on the bracket.
-constexpr int kMuThreads = 1024;
-__global__ void __launch_bounds__(kMuThreads) mu_bisect_kernel(const double* __restrict__ D, const double* __restrict__ wsa,
-                                                               int nwa, double T, double W, double base, double gs,
-                                                               double n_target, int holes, double br0, double br1,
-                                                               double* __restrict__ mu_out, int* __restrict__ status) {
-  __shared__ double sh[kMuThreads];
-  __shared__ double s_m;
-  __shared__ int s_done;
-  auto excess = [&](double mu) {
-    double s = 0;
-    if (holes)
-      for (int a = threadIdx.x; a < nwa; a += kMuThreads) s += D[a] * occ_fermion_d(mu - wsa[a], T);
-    else
-      for (int a = threadIdx.x; a < nwa; a += kMuThreads) s += D[a] * occ_fermion_d(wsa[a] - mu, T);
-    double tot = block_sum<kMuThreads>(s, sh);
-    return (holes ? (W - tot + base) * gs : (tot + base) * gs) - n_target;
+constexpr int kMuCluster = 8;
+constexpr int kMuThreads = 512;
+
+__global__ void __cluster_dims__(kMuCluster, 1, 1) __launch_bounds__(kMuThreads)
+    mu_solve_kernel(const double* __restrict__ D, const double* __restrict__ wsa, int nwa, double T, double W,
+                    double base, double gs, double n_target, int holes, double br0, double br1, double guess,
+                    double* __restrict__ mu_out, int* __restrict__ status) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const unsigned rank = cluster.block_rank();
+  __shared__ double sh[kMuThreads], sh2[kMuThreads];
+  __shared__ double part[2];
+  const int chunk = (nwa + kMuCluster - 1) / kMuCluster;
+  const int a0 = int(rank) * chunk, a1 = min(nwa, a0 + chunk);
+  auto evaluate = [&](double mu, double& F, double& dF) {
+    double s1 = 0, s2 = 0;
+    for (int a = a0 + int(threadIdx.x); a < a1; a += kMuThreads) {
+      const double f = occ_fermion_d(holes ? mu - wsa[a] : wsa[a] - mu, T);
+      s1 += D[a] * f;
+      s2 += D[a] * (f * (1 - f));
+    }
+    sh[threadIdx.x] = s1;
+    sh2[threadIdx.x] = s2;
+    __syncthreads();
+    for (int st = kMuThreads / 2; st > 0; st >>= 1) {
+      if (int(threadIdx.x) < st) {
+        sh[threadIdx.x] += sh[threadIdx.x + st];
+        sh2[threadIdx.x] += sh2[threadIdx.x + st];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      part[0] = sh[0];
+      part[1] = sh2[0];
+    }
+    cluster.sync();
+    double t1 = 0, t2 = 0;
+    for (unsigned r = 0; r < kMuCluster; ++r) {
+      const double* p = cluster.map_shared_rank(part, r);
+      t1 += p[0];
+      t2 += p[1];
+    }
+    cluster.sync();
+    F = (holes ? (W - t1 + base) * gs : (t1 + base) * gs) - n_target;
+    dF = T > 1.4901161193847656e-08 ? gs * t2 / T : 0.0;
   };
-  double a = br0, b = br1;
-  double fa = excess(a), fb = excess(b);
+  double a = br0, b = br1, fa, fb, dd;
+  evaluate(a, fa, dd);
+  evaluate(b, fb, dd);
   if (fa * fb > 0) {
-    if (threadIdx.x == 0) *status = 1;
+    if (rank == 0 && threadIdx.x == 0) *status = 1;
     return;
   }
   double result;
@@ -357,34 +395,34 @@ __global__ void __launch_bounds__(kMuThreads) mu_bisect_kernel(const double* __r
   } else if (fb == 0) {
     result = b;
   } else {
-    result = NAN;
-    for (int it = 0; it < 2100; ++it) {
-      if (threadIdx.x == 0) {
-        double m = float_middle_d(a, b);
-        s_m = m;
-        s_done = (m == a || m == b);
+    double x = (guess > a && guess < b) ? guess : float_middle_d(a, b);
+    result = x;
+    for (int it = 0; it < 400; ++it) {
+      double F, dF;
+      evaluate(x, F, dF);
+      result = x;
+      if (F == 0) break;
+      if (signbit(F) == signbit(fa)) {
+        a = x;
+        fa = F;
+      } else {
+        b = x;
+        fb = F;
       }
-      __syncthreads();
-      double m = s_m;
-      int done = s_done;
-      __syncthreads();
-      if (done) break;
-      double fm = excess(m);
-      if (fm == 0) {
-        result = m;
+      double xn = x - F / dF;
+      if (!(dF > 0) || !(xn > a && xn < b)) xn = float_middle_d(a, b);
+      if (xn == a || xn == b) {
+        result = fabs(fa) <= fabs(fb) ? a : b;
         break;
       }
-      if (signbit(fm) == signbit(fa)) {
-        a = m;
-        fa = fm;
-      } else {
-        b = m;
-        fb = fm;
+      if (fabs(xn - x) <= 0x1p-50 * fmax(fabs(x), 1.0)) {
+        result = xn;
+        break;
       }
+      x = xn;
     }
-    if (isnan(result)) result = fabs(fa) <= fabs(fb) ? a : b;
   }
-  if (threadIdx.x == 0) {
+  if (rank == 0 && threadIdx.x == 0) {
     *mu_out = result;
     *status = 0;
   }
@@ -616,6 +654,37 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
     else
       coupling_sum_kernel<uint16_t><<<grid, 128, 0, s>>>(reinterpret_cast<const uint16_t*>(g2raw.p), int(nm), int(ni), d_cptr.p, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac, P->d_G.p);
     EPSP_LAUNCHED(ctx);
+    // The cells of ω ± ω_ν, by the lookup of _interp_linear_grid (src/frequency_grids.jl:207-219):
+    // the value there is (1 - t) Σ[j] + t Σ[j + 1], which is Σ[0] below the grid (t = 0) and Σ[end]
+    // above it (t = 1).
+    {
+      const auto& w = P->ws.nodes;
+      const long n = P->nw;
+      std::vector<int32_t> cj(size_t(2 * n * nm));
+      std::vector<double> ctt(cj.size()), cx(cj.size());
+      for (long side = 0; side < 2; ++side)
+        for (long nu = 0; nu < nm; ++nu)
+          for (long iw = 0; iw < n; ++iw) {
+            const double x = side == 0 ? w[size_t(iw)] + wnu[size_t(nu)] : w[size_t(iw)] - wnu[size_t(nu)];
+            const size_t k = size_t(iw + n * (nu + nm * side));
+            cx[k] = x;
+            if (!(x > w[0])) {
+              cj[k] = 0;
+              ctt[k] = 0.0;
+            } else if (x >= w[size_t(n - 1)]) {
+              cj[k] = int32_t(n - 2);
+              ctt[k] = 1.0;
+            } else {
+              const int32_t c = ct.jtab[size_t(int64_t((x - ct.x0) * ct.inv_h))];
+              const int32_t j = c - 1 + (w[size_t(c)] <= x ? 1 : 0);
+              cj[k] = j;
+              ctt[k] = (x - w[size_t(j)]) / (w[size_t(j + 1)] - w[size_t(j)]);
+            }
+          }
+      P->d_cell_j = to_device(ctx, cj);
+      P->d_cell_t = to_device(ctx, ctt);
+      P->d_cell_x = to_device(ctx, cx);
+    }
     P->d_Fa.alloc(ctx, size_t(P->nw * nm));
     P->d_Fe.alloc(ctx, size_t(P->nw * nm));
     if (P->path == EPSP_PATH_GEMM_FP64) {
@@ -779,9 +848,9 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
         bool holes = occ->type == EPSP_SEMICONDUCTOR && occ->nlist[iT] < 0;
         double n_target = occ->nlist[iT] + occ->nelec;
         long pm = prof_begin(ctx, "mu");
-        mu_bisect_kernel<<<1, kMuThreads, 0, s>>>(P->d_D.p, P->d_wsa.p, int(nwa), T, P->W, P->nstates_base,
-                                                  occ->spin_degeneracy, n_target, holes ? 1 : 0, br0, br1, d_mu.p + iT,
-                                                  d_status.p + iT);
+        mu_solve_kernel<<<kMuCluster, kMuThreads, 0, s>>>(P->d_D.p, P->d_wsa.p, int(nwa), T, P->W, P->nstates_base,
+                                                          occ->spin_degeneracy, n_target, holes ? 1 : 0, br0, br1,
+                                                          mu[size_t(iT)], d_mu.p + iT, d_status.p + iT);
         EPSP_LAUNCHED(ctx);
         prof_end(ctx, pm);
       }

@@ -31,6 +31,9 @@ struct Scgd0Plan {
   long nc = 0;
   DBuf<double> d_wnu, d_epsc, d_G, d_Fa, d_Fe, d_Kt;
   DBuf<int32_t> d_colc;
+  // cells of ω ± ω_ν for every (ω, ν): [2][nω·nm] lower node, weight and point (absorption, emission)
+  DBuf<int32_t> d_cell_j;
+  DBuf<double> d_cell_t, d_cell_x;
   // tensor-core path state (scgd0_tc.cu)
   struct Tc;
   std::unique_ptr<Tc, void (*)(Tc*)> tc{nullptr, [](Tc*) {}};

@@ -27,12 +27,15 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bflo
 }
 
 // Kernel tensor of the recast Fan-Migdal sum (see kbuild_f64_kernel in scgd0.cu), written as BF16
-// hi/lo rows K_t[ω][k] through a shared-memory transpose. The differences x - ε - Re Σ stay FP64
-// (they cancel near the quasiparticle pole); the reciprocal and the occupation products are FP32,
-// below the BF16x3 rounding of the contraction.
-__global__ void __launch_bounds__(256) kbuild_bf16_kernel(const double* __restrict__ ws, int nw, CellTableDev ct,
-                                                          const double2* __restrict__ Sin, const double* __restrict__ wnu,
-                                                          int nm, const double* __restrict__ eps_c,
+// hi/lo rows K_t[ω][k] through a shared-memory transpose. The cells of ω ± ω_ν come from the setup
+// table; Re z = (x - ε) - Re Σ(x) stays FP64 (it cancels near the quasiparticle pole), Im Σ(x), the
+// reciprocal and the occupation products are FP32, below the BF16x3 rounding of the contraction.
+__global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, const double2* __restrict__ Sin,
+                                                          const int32_t* __restrict__ cell_j,
+                                                          const double* __restrict__ cell_t,
+                                                          const double* __restrict__ cell_x,
+                                                          const double* __restrict__ wnu, int nm,
+                                                          const double* __restrict__ eps_c,
                                                           const int32_t* __restrict__ col_c, long nk,
                                                           const double* __restrict__ Fa, const double* __restrict__ Fe,
                                                           double w_ac, __nv_bfloat16* __restrict__ Kh,
@@ -42,7 +45,7 @@ __global__ void __launch_bounds__(256) kbuild_bf16_kernel(const double* __restri
   const long k0 = long(blockIdx.y) * 64;
   const int tw = threadIdx.x % 32, tk = threadIdx.x / 32;
   const int iw = w0 + tw;
-  const double w = iw < nw ? ws[iw] : 0.0;
+  const long nwm = long(nw) * nm;
 #pragma unroll 1
   for (int r = 0; r < 8; ++r) {
     const int kl = tk + 8 * r;
@@ -51,18 +54,21 @@ __global__ void __launch_bounds__(256) kbuild_bf16_kernel(const double* __restri
     if (iw < nw && k < nk) {
       const int nu = int(k % nm);
       const long c = k / nm;
-      const double q = wnu[nu];
-      if (!(q < w_ac)) {
+      if (!(wnu[nu] < w_ac)) {
         const double2* col = Sin + long(nw) * col_c[c];
         const double e = eps_c[c];
-        const double xa = w + q, xe = w - q;
-        const double2 sa = interp_grid_d(col, ct, xa);
-        const double2 se = interp_grid_d(col, ct, xe);
-        const float zar = float(xa - e - sa.x), zai = float(-sa.y);
-        const float zer = float(xe - e - se.x), zei = float(-se.y);
-        const float ga = -zai / (zar * zar + zai * zai);
-        const float ge = -zei / (zer * zer + zei * zei);
-        v = ga * float(Fa[iw + long(nw) * nu]) + ge * float(Fe[iw + long(nw) * nu]);
+        const long ia = iw + long(nw) * nu, ie = ia + nwm;
+        const int ja = cell_j[ia], je = cell_j[ie];
+        const double ta = cell_t[ia], te = cell_t[ie];
+        const double2 la = col[ja], ha = col[ja + 1], le = col[je], he = col[je + 1];
+        const float zar = float((cell_x[ia] - e) - ((1 - ta) * la.x + ta * ha.x));
+        const float zer = float((cell_x[ie] - e) - ((1 - te) * le.x + te * he.x));
+        const float tfa = float(ta), tfe = float(te);
+        const float sia = (1.f - tfa) * float(la.y) + tfa * float(ha.y);
+        const float sie = (1.f - tfe) * float(le.y) + tfe * float(he.y);
+        const float ga = sia / (zar * zar + sia * sia);   // Im 1/z with Im z = -Im Σ
+        const float ge = sie / (zer * zer + sie * sie);
+        v = ga * float(Fa[ia]) + ge * float(Fe[ia]);
       }
     }
     tile[kl][tw] = v;
@@ -170,12 +176,12 @@ void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS) {
   const long nw = P->nw, ni = P->ni, nk = P->nm * P->nc;
   long pk = prof_begin(ctx, "kbuild");
   kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), 32), unsigned(T->Kp / 64)), 256, 0, s>>>(
-      P->d_ws.p, int(nw), P->ct, d_Sin, P->d_wnu.p, int(P->nm), P->d_epsc.p, P->d_colc.p, nk, P->d_Fa.p, P->d_Fe.p,
-      P->w_ac, T->Kt_h.p, T->Kt_l.p, T->Kp);
+      int(nw), d_Sin, P->d_cell_j.p, P->d_cell_t.p, P->d_cell_x.p, P->d_wnu.p, int(P->nm), P->d_epsc.p, P->d_colc.p, nk,
+      P->d_Fa.p, P->d_Fe.p, P->w_ac, T->Kt_h.p, T->Kt_l.p, T->Kp);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pk);
   const long slab = nw * ni;
-  int sp = tc_gemm_launch(ctx, T->opK, T->opG, int(nw), int(ni), int(nk), T->part.p, nw, slab, 16, T->err.p);
+  int sp = tc_gemm_launch(ctx, T->opK, T->opG, int(nw), int(ni), int(nk), T->part.p, nw, slab, 16, T->err.p, "tc_fm");
   finalize_add_kernel<<<div_up(size_t(slab), 256), 256, 0, s>>>(T->part.p, slab, sp, slab, d_ImS);
   EPSP_LAUNCHED(ctx);
   check_err(P);
@@ -188,7 +194,7 @@ void tc_kk_assemble(Scgd0Plan* P, double2* d_Snew) {
   const long nw = P->nw, ni = P->ni, slab = nw * ni;
   split_rows_kernel<<<div_up(size_t(ni * T->Kp2), 256), 256, 0, s>>>(P->d_ImS.p, nw, ni, nw, T->Kp2, T->Im_h.p, T->Im_l.p);
   EPSP_LAUNCHED(ctx);
-  int sp = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(ni), int(nw), T->part.p, nw, slab, 16, T->err.p);
+  int sp = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(ni), int(nw), T->part.p, nw, slab, 16, T->err.p, "tc_kk");
   finalize_assemble_kernel<<<div_up(size_t(slab), 256), 256, 0, s>>>(T->part.p, slab, sp, slab, P->d_ImS.p, d_Snew);
   EPSP_LAUNCHED(ctx);
 }

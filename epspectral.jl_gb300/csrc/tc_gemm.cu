@@ -63,12 +63,12 @@ static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int 
 }
 
 int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int K, float* out, long ld_out,
-                   long split_stride, int max_splits, int* d_err) {
+                   long split_stride, int max_splits, int* d_err, const char* prof_name) {
   int BN, splits;
   tc_gemm_shape(ctx, M, N, K, max_splits, &BN, &splits);
   const int kblocks = (K + kTcBK - 1) / kTcBK;
   const int per = (kblocks + splits - 1) / splits;
-  long pi = prof_begin(ctx, "tc_gemm");
+  long pi = prof_begin(ctx, prof_name);
   if (BN == 256)
     launch<256, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   else

@@ -241,7 +241,7 @@ struct TcOperand {
 // Launches D = A_hi B_hi + A_hi B_lo + A_lo B_hi for A [M][K], B [N][K] (K-major) into the
 // FP32 slabs out[split][m + ld_out n]; returns the number of splits used.
 int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int K, float* out, long ld_out,
-                   long split_stride, int max_splits, int* d_err);
+                   long split_stride, int max_splits, int* d_err, const char* prof_name = "tc_gemm");
 
 // The BN and split count tc_gemm_launch picks for (M, N, K) with at most max_splits splits.
 void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int* bn, int* splits);

@@ -60,6 +60,8 @@ def lib():
         "epsp_profile_kernel": (C.c_int, [vp, C.c_char_p]),
         "epsp_profile_read": (C.c_int, [vp, P(d), P(i64)]),
         "epsp_test_fail_alloc": (C.c_int, [vp, C.c_uint64]),
+        "epsp_timer_begin": (C.c_int, [vp]),
+        "epsp_timer_end": (C.c_int, [vp, P(d)]),
         "epsp_scgd0_setup": (C.c_int, [vp, P(epsp_model), P(epsp_options), P(vp)]),
         "epsp_scgd0_plan_destroy": (None, [vp]),
         "epsp_scgd0_run": (C.c_int, [vp, P(epsp_occ), c_double_p, d, i32, d, i32, c_double_p, c_double_p,
@@ -110,6 +112,15 @@ class Context:
         ms, n = C.c_double(), C.c_int64()
         self.check(lib().epsp_profile_read(self.handle, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def timer_begin(self):
+        self.check(lib().epsp_timer_begin(self.handle))
+
+    def timer_end(self) -> float:
+        """Milliseconds on the context's stream since timer_begin (waits for the stream)."""
+        ms = C.c_double()
+        self.check(lib().epsp_timer_end(self.handle, C.byref(ms)))
+        return ms.value
 
     def fail_next_alloc(self, nbytes: int):
         """Test hook: the next device allocation of at least nbytes fails with ENOMEM."""

@@ -211,3 +211,24 @@ def float32_to_bf16_bits(x: np.ndarray) -> np.ndarray:
 
 def bf16_bits_to_float32(b: np.ndarray) -> np.ndarray:
     return (np.asarray(b, dtype=np.uint32) << 16).view(np.float32)
+
+
+def bare_mu(setup: dict, T: float, n_target: float, spin_degeneracy: float = 2.0) -> float:
+    """The chemical potential of the bare window bands (the starting μ of src/scgd0.jl:165-170,
+    ElectronPhonon's bte_compute_μ!): n(μ) = g Σ_i w_i f(ε_i - μ) + nstates_base = n_target, by
+    bisection on the band range ± 1."""
+    eps, w = np.asarray(setup["eps_i"]), np.asarray(setup["w_i"])
+    base = float(setup.get("nstates_base", 0.0))
+
+    def n(mu):
+        x = np.clip((eps - mu) / T, -700, 700)
+        return spin_degeneracy * (np.sum(w / (np.exp(x) + 1.0)) + base)
+
+    a, b = eps.min() - 1.0, eps.max() + 1.0
+    for _ in range(200):
+        m = 0.5 * (a + b)
+        if n(m) < n_target:
+            a = m
+        else:
+            b = m
+    return 0.5 * (a + b)

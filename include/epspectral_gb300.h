@@ -159,6 +159,19 @@ const char* epsp_last_error(const epsp_ctx* ctx);
 /* Number of kernels this context launched since creation (for launch accounting). */
 int64_t epsp_kernel_launches(const epsp_ctx* ctx);
 
+/* Library utilities with no counterpart in the reference (benchmarks and tests):
+ *  - epsp_profile_kernel brackets every launch of the kernel family `name` ("tc_ladder",
+ *    "tc_fm", "kbuild", "xgen", "mu", ...) with CUDA events on the context's stream until the next
+ *    call (NULL or "" switches it off); epsp_profile_read returns their summed milliseconds and count;
+ *  - epsp_timer_begin / epsp_timer_end time the context's stream between two calls;
+ *  - epsp_test_fail_alloc makes the next device allocation of at least `bytes` bytes fail with
+ *    EPSP_ENOMEM (0 switches it off), to test the error path without exhausting a device. */
+epsp_status epsp_profile_kernel(epsp_ctx* ctx, const char* name);
+epsp_status epsp_profile_read(epsp_ctx* ctx, double* total_ms, int64_t* count);
+epsp_status epsp_timer_begin(epsp_ctx* ctx);
+epsp_status epsp_timer_end(epsp_ctx* ctx, double* ms);
+epsp_status epsp_test_fail_alloc(epsp_ctx* ctx, uint64_t bytes);
+
 /* ---- scGD0 ---- */
 
 /* Uploads the iteration-invariant tables of `model` (the `setup` of src/scgd0.jl:127-184 and the

@@ -300,11 +300,12 @@ int64_t scgd0_nf_chunk(const Model& M, int64_t gpu_tile) {  // src/scgd0.jl:201-
 // add_fan_migdal_imsigma! over all chunks of inner states (src/scgd0.jl:264-287): per chunk, the
 // sum over νf = (ν, f) in order for each (ω, i), added to imsigma [nω, ni].
 void fan_migdal(const Model& M, const CellTable& ct, int64_t nf_chunk, const double* sin,
-                double mu, double T, double w_ac, double* imsigma) {
+                double mu, double T, double w_ac, double* imsigma, int64_t ia = 0, int64_t ib = -1) {
+  if (ib < 0) ib = M.ni;
   for (int64_t f0 = 0; f0 < M.nf; f0 += nf_chunk) {
     int64_t f1 = std::min(M.nf, f0 + nf_chunk);
 #pragma omp parallel for schedule(dynamic, 1)
-    for (int64_t i = 0; i < M.ni; ++i) {
+    for (int64_t i = ia; i < ib; ++i) {
       for (int64_t iw = 0; iw < M.nw; ++iw) {
         double w = M.ws[iw];
         double acc = 0.0;
@@ -699,6 +700,88 @@ void conductivity(const double* J, const double* v, const double* w_i, const dou
       for (int64_t i = 0; i < ni; ++i) S += (v[a + 3 * i] * w_i[i]) * Y[size_t(b + 3 * i)];
       sigma[a + 3 * b] = (F / (2 * kPi * cplx(0, 1)) * S).real();
     }
+}
+
+// The dominant part of apply_ladder_kernel! for the output columns (a, i, type) of the outer states
+// [ia, ib): B, B̃ and C± += X B̃ over every chunk (src/ladder.jl:254-291), the CPU baseline's
+// bounded sample. Returns nothing; the work is what is timed.
+void ladder_contract_sample(const Ladder& L, double T, double w_ac, const double* J, int64_t ia, int64_t ib) {
+  const Model& M = L.M;
+  const epsp_model* mp = M.m;
+  const int64_t nw = M.nw, ni = M.ni, nm = M.nm, ns = L.nshift;
+  const int64_t nrow = nw * 16, nsel = ib - ia, ncol = 6 * nsel;
+  std::vector<double> Cp(size_t(nrow * ncol), 0.0), Cm(size_t(nrow * ncol), 0.0);
+  for (const auto& ch : L.chunks) {
+    const int64_t nfc = int64_t(ch.fidx.size()), nip = ch.i1 - ch.i0;
+    std::vector<double> B(size_t(ns * nfc * nsel * 2), 0.0);
+#pragma omp parallel for schedule(static)
+    for (int64_t fc = 0; fc < nfc; ++fc) {
+      int64_t f = ch.fidx[size_t(fc)];
+      for (int type = 0; type < 2; ++type)
+        for (int64_t ii = 0; ii < nsel; ++ii) {
+          int64_t i = ia + ii;
+          double* col = B.data() + ns * (fc + nfc * (ii + nsel * type));
+          for (int64_t nu = 0; nu < nm; ++nu) {
+            double w = M.omega_q(nu, f, i);
+            if (w < w_ac) continue;
+            double x = w / L.h;
+            int64_t lo = int64_t(std::floor(x));
+            double g = M.g2(nu, i, f);
+            for (int64_t m = lo; m <= lo + 1; ++m) {
+              double c = g * std::max(0.0, 1 - std::fabs(x - double(m)));
+              col[m] += type == 0 ? c : c * occ_boson(w, T);
+            }
+          }
+          for (int64_t m = 0; m < ns; ++m) col[m] *= mp->w_f[f];
+        }
+    }
+    const int64_t nk = ns * 3 * nip;
+    std::vector<double> Bt(size_t(nk * ncol));
+#pragma omp parallel for schedule(static)
+    for (int64_t col = 0; col < ncol; ++col) {
+      int64_t a = col % 3, ii = (col / 3) % nsel, type = col / (3 * nsel);
+      for (int64_t ip = 0; ip < nip; ++ip)
+        for (int b = 0; b < 3; ++b)
+          for (int64_t m = 0; m < ns; ++m) {
+            double acc = 0.0;
+            for (int32_t fc = ch.sptr[size_t(ip)]; fc < ch.sptr[size_t(ip + 1)]; ++fc)
+              acc += mp->R[a + 3 * (b + 3 * int64_t(ch.fidx[size_t(fc)]))] * B[size_t(m + ns * (fc + nfc * (ii + nsel * type)))];
+            Bt[size_t(m + ns * (b + 3 * ip) + nk * col)] = acc;
+          }
+    }
+    std::vector<double> X(size_t(nrow * nk));
+    for (int s = 0; s < 2; ++s) {
+      const int32_t* klo = L.klo.data() + nw * ns * s;
+      const double* wlo = L.wlo.data() + nw * ns * s;
+      const double* whi = L.whi.data() + nw * ns * s;
+#pragma omp parallel for schedule(static)
+      for (int64_t kk = 0; kk < nk; ++kk) {
+        int64_t m = kk % ns, b = (kk / ns) % 3, ip = kk / (3 * ns);
+        int64_t i = ch.i0 + ip;
+        for (int c0 = 0; c0 < 2; ++c0)
+          for (int c12 = 0; c12 < 4; ++c12)
+            for (int64_t j = 0; j < nw; ++j) {
+              int64_t k = klo[j + nw * m];
+              size_t a0 = jidx(nw, k, c12, b, c0, i), a1 = jidx(nw, k + 1, c12, b, c0, i);
+              double wl = wlo[j + nw * m], wh = whi[j + nw * m];
+              X[size_t(j + nw * (c12 + 4 * c0) + nrow * kk)] = wl * J[2 * a0] + wh * J[2 * a1];
+              X[size_t(j + nw * (c12 + 4 * (c0 + 2)) + nrow * kk)] = wl * J[2 * a0 + 1] + wh * J[2 * a1 + 1];
+            }
+      }
+      double* C = s == 0 ? Cp.data() : Cm.data();
+#pragma omp parallel for schedule(static)
+      for (int64_t col = 0; col < ncol; ++col) {
+        double* Cc = C + nrow * col;
+        const double* Bc = Bt.data() + nk * col;
+        for (int64_t k = 0; k < nk; ++k) {
+          double bv = Bc[k];
+          if (bv == 0.0) continue;
+          const double* Xk = X.data() + nrow * k;
+          for (int64_t r = 0; r < nrow; ++r) Cc[r] += Xk[r] * bv;
+        }
+      }
+    }
+  }
 }
 
 // apply_ladder_kernel!, src/ladder.jl:245-296.
@@ -1194,6 +1277,27 @@ int epsp_oracle_ladder_run(const epsp_model* m, const epsp_options* opts, const 
   return guarded(msg, msglen, [&] {
     ladder_run(m, opts, sigma, mu, Tlist, nT, Omegas, nOmega, solver, rtol, maxiter, sigma_bubble, sigma_ladder,
                converged, niter, hist, J_out);
+  });
+}
+
+int epsp_oracle_imsigma_sample(const epsp_model* m, const epsp_options* opts, const double* sigma_in, double mu,
+                               double T, int64_t i0, int64_t i1, double* imsigma, char* msg, int32_t msglen) {
+  apply_threads();
+  return guarded(msg, msglen, [&] {
+    Model M = make_model(m);
+    if (i0 < 0 || i1 > M.ni || i0 >= i1) throw OracleError(EPSP_EINVAL, "bad outer-state range");
+    CellTable ct = cell_search_table(m->omegas, M.ws);
+    fan_migdal(M, ct, scgd0_nf_chunk(M, opts->gpu_tile), sigma_in, mu, T, opts->omega_acoustic, imsigma, i0, i1);
+  });
+}
+
+int epsp_oracle_ladder_contract_sample(const epsp_model* m, const epsp_options* opts, double T, const double* J,
+                                       int64_t i0, int64_t i1, char* msg, int32_t msglen) {
+  apply_threads();
+  return guarded(msg, msglen, [&] {
+    Ladder L = make_ladder(m, opts->gpu_tile);
+    if (i0 < 0 || i1 > L.M.ni || i0 >= i1) throw OracleError(EPSP_EINVAL, "bad outer-state range");
+    ladder_contract_sample(L, T, opts->omega_acoustic, J, i0, i1);
   });
 }
 

@@ -83,6 +83,15 @@ int epsp_oracle_ladder_run(const epsp_model* m, const epsp_options* opts, const 
                            int32_t* niter, epsp_ladder_history* hist, double* J_out, char* msg,
                            int32_t msglen);
 
+/* Bounded samples of the two dominant CPU costs, for the benchmark's CPU baseline: the Fan-Migdal
+ * sum of the outer states [i0, i1) only (imsigma [nω, ni], those columns accumulated), and the
+ * shift-grid contraction C± += X B̃ of apply_ladder_kernel! for the output columns of the outer
+ * states [i0, i1) (src/ladder.jl:254-291). */
+int epsp_oracle_imsigma_sample(const epsp_model* m, const epsp_options* opts, const double* sigma_in, double mu,
+                               double T, int64_t i0, int64_t i1, double* imsigma, char* msg, int32_t msglen);
+int epsp_oracle_ladder_contract_sample(const epsp_model* m, const epsp_options* opts, double T, const double* J,
+                                       int64_t i0, int64_t i1, char* msg, int32_t msglen);
+
 /* Threads used by the OpenMP loops (0 = the OpenMP default). */
 void epsp_oracle_set_threads(int32_t n);
 int32_t epsp_oracle_get_threads(void);

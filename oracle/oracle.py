@@ -77,6 +77,10 @@ def lib():
             "epsp_oracle_ladder_run": (C.c_int, [P(epsp_model), P(epsp_options), c_double_p, c_double_p, c_double_p,
                                                  i64, c_double_p, i64, i32, d, i32, c_double_p, c_double_p, u8p,
                                                  c_int32_p, P(epsp_ladder_history), c_double_p] + msg),
+            "epsp_oracle_imsigma_sample": (C.c_int, [P(epsp_model), P(epsp_options), c_double_p, d, d, i64, i64,
+                                                     c_double_p] + msg),
+            "epsp_oracle_ladder_contract_sample": (C.c_int, [P(epsp_model), P(epsp_options), d, c_double_p, i64, i64]
+                                                   + msg),
             "epsp_oracle_set_threads": (None, [i32]),
             "epsp_oracle_get_threads": (i32, []),
         }
@@ -271,3 +275,25 @@ def loop_ladder(setup, sigma, mu, Tlist, Omegas, *, solver="gmres", rtol=1e-2, m
                                         out.converged.ctypes.data_as(C.POINTER(C.c_uint8)),
                                         ptr(out.niter, C.c_int32), C.byref(out.hist), out.J_ptr(), buf, n), buf)
     return out.result()
+
+
+def imsigma_sample(setup, sigma_in, mu, T, i0, i1, *, omega_acoustic, gpu_tile=None):
+    """The Fan-Migdal sum of the outer states [i0, i1) only (a bounded CPU-baseline sample)."""
+    M = ModelArrays(setup)
+    sin = as_complex_F(sigma_in, (M.nw, M.ni))
+    out = np.zeros((M.nw, M.ni), order="F")
+    opts = _options(gpu_tile, omega_acoustic)
+    buf, n = _msgbuf()
+    _check(lib().epsp_oracle_imsigma_sample(C.byref(M.struct), C.byref(opts), cptr(sin), float(mu), float(T), int(i0),
+                                            int(i1), ptr(out), buf, n), buf)
+    return out
+
+
+def ladder_contract_sample(setup, J, T, i0, i1, *, omega_acoustic, gpu_tile=None):
+    """The shift-grid contraction of one ladder application for the outer states [i0, i1)."""
+    M = ModelArrays(setup)
+    J = as_complex_F(J, (M.nw, 4, 3, 2, M.ni))
+    opts = _options(gpu_tile, omega_acoustic)
+    buf, n = _msgbuf()
+    _check(lib().epsp_oracle_ladder_contract_sample(C.byref(M.struct), C.byref(opts), float(T), cptr(J), int(i0),
+                                                    int(i1), buf, n), buf)
