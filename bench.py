@@ -165,8 +165,8 @@ def run_ours(args, world, rank, local):
     from epspectral_gb300 import api
     s, T, occ, mu0 = workload()
     ctx = api.Context(local)
-    sp = api.Scgd0Plan(s, path="gemm_bf16x3", omega_acoustic=W_AC, ctx=ctx)
-    lp = api.LadderPlan(s, path="gemm_bf16x3", omega_acoustic=W_AC, ctx=ctx)
+    sp = api.Scgd0Plan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
+    lp = api.LadderPlan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
     nw, ni = len(s["omegas"]), s["eps_i"].size
 
     def step():
@@ -205,7 +205,7 @@ def run_ours(args, world, rank, local):
                data="synthetic (seeded 3-band t2g model, log-normal g2)",
                config=dict(workload="3-band cubic t2g nk=16^3, 495 outer / 12288 inner states, 15 modes, graded "
                                     "1251-node grid, T=300 K; scGD0 to 1e-6 eV + ladder at one Omega=0.1 eV",
-                           ni=ni, nf=int(s["eps_f"].size), nw=nw, nm=15, path="gemm_bf16x3",
+                           ni=ni, nf=int(s["eps_f"].size), nw=nw, nm=15, path="gemm_bf16",
                            warm_start=False, l2="flushed between steps (512 MB write)",
                            parallelism=f"replicas x{world}"))
     if rank != 0:
@@ -222,7 +222,7 @@ def run_ours(args, world, rank, local):
         flops = 2.0 * M * N * K
         burst, sust, hbm, src = peaks()
         achieved = flops / avg_s / 1e12
-        out["roofline"] = dict(kernel="tc_gemm_bf16x3 (ladder contraction)", bound="tensor", achieved=achieved,
+        out["roofline"] = dict(kernel="tc_gemm_bf16 (ladder contraction)", bound="tensor", achieved=achieved,
                                peak=sust, unit="TFLOP/s", frac=achieved / sust, traffic=None,
                                peak_source=f"{src} bf16 sustained", launches=prof_n, avg_ms=1e3 * avg_s,
                                flops_per_launch=flops, tensor_pipe_frac=3 * achieved / sust)
@@ -230,9 +230,9 @@ def run_ours(args, world, rank, local):
     # end to end through the public API from host arrays
     t0 = time.perf_counter()
     r_e = api.loop_scgd0(s, occ, eta_init=ETA_INIT, tol=TOL, maxiter=MAXITER, mu_start=[mu0], omega_acoustic=W_AC,
-                         path="gemm_bf16x3", ctx=ctx)
+                         path="gemm_bf16", ctx=ctx)
     l_e = api.loop_ladder(s, r_e["sigma"], r_e["mu"], [T], [OMEGA], rtol=L_RTOL, maxiter=L_MAXITER,
-                          omega_acoustic=W_AC, path="gemm_bf16x3", ctx=ctx)
+                          omega_acoustic=W_AC, path="gemm_bf16", ctx=ctx)
     e2e = time.perf_counter() - t0
     out["e2e"] = dict(value=e2e, unit="s", h2d_bytes_per_step=2 * setup_bytes(s) + 16 * nw * ni,
                       d2h_bytes_per_step=16 * nw * ni + 8 * 9 * 2)

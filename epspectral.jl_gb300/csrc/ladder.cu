@@ -412,13 +412,14 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
   const int rr = int(r0 / nwp), j0 = int(r0 % nwp);
   const int q = rr % 6, c0 = (rr / 6) % 2, ri = rr / 12;
   const int c12 = (q < 2) ? 0 : (q < 4 ? 3 : (q == 4 ? 1 : 2));
-  // mode tables of the block's nodes
+  // mode tables of the block's nodes, stored node-fastest ([(ν, s, t)][32 nodes]) so that the 32
+  // lanes of a warp, which hold 32 consecutive nodes, read consecutive words
   for (int e = threadIdx.x; e < 32 * 16 * 2; e += 256) {
     const int jj = e / 32, rest = e % 32;  // rest = (nu, s)
     const long g = (long(j0 + jj) * nmp) * 2 + rest;  // [j][nu][s] with nmp == 16 per K-group
     const bool ok = j0 + jj < nwp;
-    for (int t = 0; t < 4; ++t) s_w[e * 4 + t] = ok ? mt_w[g * 4 + t] : 0.f;
-    for (int t = 0; t < 2; ++t) s_k[e * 2 + t] = ok ? mt_k[g * 2 + t] : 0;
+    for (int t = 0; t < 4; ++t) s_w[(rest * 4 + t) * 32 + jj] = ok ? mt_w[g * 4 + t] : 0.f;
+    for (int t = 0; t < 2; ++t) s_k[(rest * 2 + t) * 32 + jj] = ok ? mt_k[g * 2 + t] : 0;
   }
   const int tr = threadIdx.x % 32, tk = threadIdx.x / 32;
   const int j = j0 + tr;
@@ -452,10 +453,10 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
         float xs[2];
 #pragma unroll
         for (int sg = 0; sg < 2; ++sg) {
-          const int e = (tr * 16 + nu) * 2 + sg;
-          const int ka = s_k[e * 2], kb = s_k[e * 2 + 1];
-          const float* w4 = s_w + e * 4;
-          xs[sg] = w4[0] * jw[ka] + w4[1] * jw[ka + 1] + w4[2] * jw[kb] + w4[3] * jw[kb + 1];
+          const int rest = nu * 2 + sg;
+          const int ka = s_k[(rest * 2) * 32 + tr], kb = s_k[(rest * 2 + 1) * 32 + tr];
+          const float* w4 = s_w + (rest * 4) * 32 + tr;
+          xs[sg] = w4[0] * jw[ka] + w4[32] * jw[ka + 1] + w4[64] * jw[kb] + w4[96] * jw[kb + 1];
         }
         const float n = nnu[nu];
         switch (q) {
@@ -674,6 +675,15 @@ static void check_ladder_model(const epsp_model* m) {
     if (m->iq_kk[k] < 0 || m->iq_kk[k] >= m->nq) fail(EPSP_EINVAL, "iq_kk out of range");
 }
 
+static TcOperand two_part(const void* hi, const void* lo, long rows, long cols, long ld, int box_rows) {
+  TcOperand op;
+  op.ns = 2;
+  op.m[0] = make_tmap_bf16(hi, rows, cols, ld, box_rows);
+  op.m[1] = make_tmap_bf16(lo, rows, cols, ld, box_rows);
+  op.m[2] = op.m[0];
+  return op;
+}
+
 static std::vector<double> g2_as_double(const epsp_model* m) {
   const size_t n = size_t(m->nm * m->ni * m->nf);
   std::vector<double> out(n);
@@ -819,7 +829,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
     P->d_Cp.alloc(ctx, size_t(16 * nw * 6 * ni));
     P->d_Cm.alloc(ctx, size_t(16 * nw * 6 * ni));
     EPSP_CUDA(cudaStreamSynchronize(s));
-  } else if (P->path == EPSP_PATH_GEMM_FP64 || P->path == EPSP_PATH_GEMM_BF16X3) {
+  } else if (P->path == EPSP_PATH_GEMM_FP64 || P->path == EPSP_PATH_GEMM_BF16) {
     P->wnu.assign(size_t(nm), 0.0);
     for (long nu = 0; nu < nm; ++nu) {
       double w0 = m->omega_ph[nu];
@@ -847,7 +857,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
     auto d_wnu = to_device(ctx, P->wnu);
     P->nwp = (nw + 31) / 32 * 32;
     P->nmp = (nm + 15) / 16 * 16;
-    if (P->path == EPSP_PATH_GEMM_BF16X3 && P->nmp != 16)
+    if (P->path == EPSP_PATH_GEMM_BF16 && P->nmp != 16)
       fail(EPSP_EUNSUPPORTED, "the BF16x3 ladder path takes at most 16 modes; use EPSP_PATH_GEMM_FP64");
     P->Kx = P->nmp * 3 * ni;
     P->d_Gt.alloc(ctx, size_t(P->Kx * 3 * ni));
@@ -905,12 +915,12 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       split_rows_plain_kernel<<<div_up(size_t(N * P->Kp), 256), 256, 0, s>>>(P->d_Gt.p, N, P->Kx, P->Kx, P->Kp, P->d_Gh.p,
                                                                               P->d_Gl.p);
       EPSP_LAUNCHED(ctx);
-      tc_gemm_shape(ctx, int(M), int(N), int(P->Kx), 16, &P->bn, &P->splits);
+      tc_gemm_shape(ctx, int(M), int(N), int(P->Kx), 16, 2, &P->bn, &P->splits);
       P->d_part.alloc(ctx, size_t(P->splits) * size_t(M * N));
       P->d_err.alloc(ctx, 1);
       P->d_err.zero(s);
-      P->opA = {make_tmap_bf16(P->d_Ah.p, M, P->Kx, P->Kp, kTcBM), make_tmap_bf16(P->d_Al.p, M, P->Kx, P->Kp, kTcBM)};
-      P->opG = {make_tmap_bf16(P->d_Gh.p, N, P->Kx, P->Kp, P->bn), make_tmap_bf16(P->d_Gl.p, N, P->Kx, P->Kp, P->bn)};
+      P->opA = two_part(P->d_Ah.p, P->d_Al.p, M, P->Kx, P->Kp, kTcBM);
+      P->opG = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, P->bn);
       // the Kramers-Kronig image on the tensor cores: A = KK [nω][nω'], B = Y [8N][nω']
       P->d_KKh.alloc(ctx, size_t(nw * P->Kp2));
       P->d_KKl.alloc(ctx, size_t(nw * P->Kp2));
@@ -919,10 +929,10 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       EPSP_LAUNCHED(ctx);
       P->d_Yh.alloc(ctx, size_t(8 * N * P->Kp2));
       P->d_Yl.alloc(ctx, size_t(8 * N * P->Kp2));
-      tc_gemm_shape(ctx, int(nw), int(8 * N), int(nw), 16, &P->bn2, &P->splits2);
+      tc_gemm_shape(ctx, int(nw), int(8 * N), int(nw), 16, 2, &P->bn2, &P->splits2);
       P->d_part2.alloc(ctx, size_t(P->splits2) * size_t(nw * 8 * N));
-      P->opKK = {make_tmap_bf16(P->d_KKh.p, nw, nw, P->Kp2, kTcBM), make_tmap_bf16(P->d_KKl.p, nw, nw, P->Kp2, kTcBM)};
-      P->opY = {make_tmap_bf16(P->d_Yh.p, 8 * N, nw, P->Kp2, P->bn2), make_tmap_bf16(P->d_Yl.p, 8 * N, nw, P->Kp2, P->bn2)};
+      P->opKK = two_part(P->d_KKh.p, P->d_KKl.p, nw, nw, P->Kp2, kTcBM);
+      P->opY = two_part(P->d_Yh.p, P->d_Yl.p, 8 * N, nw, P->Kp2, P->bn2);
       EPSP_CUDA(cudaFuncSetAttribute(xgen_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(xgen_smem_bytes(int(ns)))));
     }
     EPSP_CUDA(cudaStreamSynchronize(s));
@@ -1078,7 +1088,7 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ) {
 }
 
 static void check_tc_err(LadderPlan* P) {
-  if (P->path != EPSP_PATH_GEMM_BF16X3) return;
+  if (P->path != EPSP_PATH_GEMM_BF16) return;
   int e = 0;
   P->d_err.download(&e, 1, P->ctx->stream);
   EPSP_CUDA(cudaStreamSynchronize(P->ctx->stream));

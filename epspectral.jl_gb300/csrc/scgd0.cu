@@ -591,7 +591,7 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
     P->d_w_f = to_device(ctx, m->w_f, size_t(nf));
     P->d_f_to_i = to_device(ctx, m->f_to_i, size_t(nf));
     EPSP_CUDA(cudaStreamSynchronize(s));
-  } else if (P->path == EPSP_PATH_GEMM_FP64 || P->path == EPSP_PATH_GEMM_BF16X3) {
+  } else if (P->path == EPSP_PATH_GEMM_FP64 || P->path == EPSP_PATH_GEMM_BF16) {
     std::vector<double> wnu;
     if (!dispersionless(m, wnu))
       fail(EPSP_EUNSUPPORTED, "the GEMM paths need dispersionless modes (every row of omega_ph constant); use EPSP_PATH_DIRECT_FP64");
@@ -814,7 +814,7 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
       P->d_ImS.zero(s);
       scgd0_imsigma(P, P->d_Sin.p, mu[size_t(iT)], T, P->d_ImS.p);
       long pk = prof_begin(ctx, "kk");
-      if (P->path == EPSP_PATH_GEMM_BF16X3) {
+      if (P->path == EPSP_PATH_GEMM_BF16) {
         tc_kk_assemble(P, SnT);
       } else {
         gemm_f64(ctx, false, int(nw), int(ni), int(nw), 1.0, P->d_KK.p, nw, P->d_ImS.p, nw, 0.0, P->d_ReS.p, nw);

@@ -1,9 +1,13 @@
-// scgd0_tc.cu -- the GEMM_BF16X3 path of the scGD0 iteration: the kernel tensor written directly as
-// BF16 hi/lo operands, the Fan-Migdal contraction and the Kramers-Kronig map on the tcgen05 tensor
+// scgd0_tc.cu -- the GEMM_BF16 path of the scGD0 iteration: the kernel tensor written directly as
+// BF16 split operands, the Fan-Migdal contraction and the Kramers-Kronig map on the tcgen05 tensor
 // cores (tc_gemm.cuh), split-K partials summed in fixed order.
 //
 //   ImΣ[ω, i] = Σ_k K_t[ω, k] G[k, i]      A = K_t  [nω][Kp]  (K-major),  B = G^T [ni][Kp]
 //   ReΣ[ω, i] = Σ_ω' KK[ω, ω'] ImΣ[ω', i]   A = KK   [nω][Kp2],           B = ImΣ^T [ni][Kp2]
+//
+// Both contractions use the three-way split (x = hi + mid + lo, six products, ~2^-23 relative): the
+// iteration's own convergence test compares successive Σ to tol (1e-6 eV for the benchmark), and a
+// two-way split's ~2^-16 rounding of the map (~2e-6 eV here) would stall it above that.
 #include "scgd0.cuh"
 #include "tc_gemm.cuh"
 
@@ -11,25 +15,21 @@
 
 namespace epsp {
 
+constexpr int kNs = 3;
+
 struct Scgd0Plan::Tc {
   long Kp = 0, Kp2 = 0;
   int splits1 = 1, splits2 = 1, bn1 = 128, bn2 = 128;
-  DBuf<__nv_bfloat16> Kt_h, Kt_l, G_h, G_l, KK_h, KK_l, Im_h, Im_l;
+  DBuf<__nv_bfloat16> Kt[kNs], G[kNs], KK[kNs], Im[kNs];
   DBuf<float> part;
   DBuf<int> err;
   TcOperand opK, opG, opKK, opIm;
 };
 
-// x = hi + lo + O(2^-16 |x|) with hi, lo BF16.
-__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
-  hi = __float2bfloat16_rn(x);
-  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
-}
-
 // Kernel tensor of the recast Fan-Migdal sum (see kbuild_f64_kernel in scgd0.cu), written as BF16
-// hi/lo rows K_t[ω][k] through a shared-memory transpose. The cells of ω ± ω_ν come from the setup
+// split rows K_t[ω][k] through a shared-memory transpose. The cells of ω ± ω_ν come from the setup
 // table; Re z = (x - ε) - Re Σ(x) stays FP64 (it cancels near the quasiparticle pole), Im Σ(x), the
-// reciprocal and the occupation products are FP32, below the BF16x3 rounding of the contraction.
+// reciprocal and the occupation products are FP32.
 __global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, const double2* __restrict__ Sin,
                                                           const int32_t* __restrict__ cell_j,
                                                           const double* __restrict__ cell_t,
@@ -38,8 +38,9 @@ __global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, const double2*
                                                           const double* __restrict__ eps_c,
                                                           const int32_t* __restrict__ col_c, long nk,
                                                           const double* __restrict__ Fa, const double* __restrict__ Fe,
-                                                          double w_ac, __nv_bfloat16* __restrict__ Kh,
-                                                          __nv_bfloat16* __restrict__ Kl, long Kp) {
+                                                          double w_ac, __nv_bfloat16* __restrict__ K0,
+                                                          __nv_bfloat16* __restrict__ K1, __nv_bfloat16* __restrict__ K2,
+                                                          long Kp) {
   __shared__ float tile[64][33];
   const int w0 = blockIdx.x * 32;
   const long k0 = long(blockIdx.y) * 64;
@@ -77,34 +78,38 @@ __global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, const double2*
   const int wr = threadIdx.x / 8, kc = (threadIdx.x % 8) * 8;
   const int ow = w0 + wr;
   if (ow < nw) {
-    __align__(16) __nv_bfloat16 h[8], l[8];
+    __align__(16) __nv_bfloat16 p0[8], p1[8], p2[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) split_bf16(tile[kc + j][wr], h[j], l[j]);
+    for (int j = 0; j < 8; ++j) {
+      __nv_bfloat16 q[3];
+      split_bf16_n(tile[kc + j][wr], 3, q);
+      p0[j] = q[0];
+      p1[j] = q[1];
+      p2[j] = q[2];
+    }
     const long off = long(ow) * Kp + k0 + kc;
-    *reinterpret_cast<uint4*>(Kh + off) = *reinterpret_cast<const uint4*>(h);
-    *reinterpret_cast<uint4*>(Kl + off) = *reinterpret_cast<const uint4*>(l);
+    *reinterpret_cast<uint4*>(K0 + off) = *reinterpret_cast<const uint4*>(p0);
+    *reinterpret_cast<uint4*>(K1 + off) = *reinterpret_cast<const uint4*>(p1);
+    *reinterpret_cast<uint4*>(K2 + off) = *reinterpret_cast<const uint4*>(p2);
   }
 }
 
-// out[r * ld + c] = split(src(r, c)) for c < cols, 0 for cols <= c < ld; src(r, c) = S[c + ldc * r]
-// (a column-major matrix read transposed: rows of the output are columns of S).
-__global__ void split_rows_kernel(const double* __restrict__ S, long ldc, long rows, long cols, long ld,
-                                  __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol) {
+// out_p[r * ld + c] = part p of S(r, c) for c < cols, 0 for cols <= c < ld, with S(r, c) =
+// S[c + ldc r] (transposed = false: rows of the output are columns of the column-major S) or
+// S[r + ldc c] (transposed = true).
+__global__ void split3_rows_kernel(const double* __restrict__ S, long ldc, long rows, long cols, long ld, bool transposed,
+                                   __nv_bfloat16* __restrict__ o0, __nv_bfloat16* __restrict__ o1,
+                                   __nv_bfloat16* __restrict__ o2) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= rows * ld) return;
   long r = idx / ld, c = idx % ld;
-  float x = c < cols ? float(S[c + ldc * r]) : 0.f;
-  split_bf16(x, oh[idx], ol[idx]);
-}
-
-// Transposed split: out[r * ld + c] = split(S[r + ldr * c]) (rows of the output are rows of S).
-__global__ void split_rows_t_kernel(const double* __restrict__ S, long ldr, long rows, long cols, long ld,
-                                    __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol) {
-  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= rows * ld) return;
-  long r = idx / ld, c = idx % ld;
-  float x = c < cols ? float(S[r + ldr * c]) : 0.f;
-  split_bf16(x, oh[idx], ol[idx]);
+  float x = 0.f;
+  if (c < cols) x = float(transposed ? S[r + ldc * c] : S[c + ldc * r]);
+  __nv_bfloat16 q[3];
+  split_bf16_n(x, 3, q);
+  o0[idx] = q[0];
+  o1[idx] = q[1];
+  o2[idx] = q[2];
 }
 
 // ImΣ (FP64) += Σ_s part[s] in ascending s.
@@ -128,6 +133,13 @@ __global__ void finalize_assemble_kernel(const float* __restrict__ part, long n,
 
 static long pad64(long x) { return (x + 63) / 64 * 64; }
 
+static TcOperand operand(DBuf<__nv_bfloat16>* parts, long rows, long cols, long ld, int box_rows) {
+  TcOperand op;
+  op.ns = kNs;
+  for (int p = 0; p < kNs; ++p) op.m[p] = make_tmap_bf16(parts[p].p, rows, cols, ld, box_rows);
+  return op;
+}
+
 void tc_setup(Scgd0Plan* P) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
@@ -137,29 +149,29 @@ void tc_setup(Scgd0Plan* P) {
   T->Kp = pad64(nk);
   T->Kp2 = pad64(nw);
   if (nw > (1l << 30) || ni > (1l << 30) || nk > (1l << 30)) fail(EPSP_EINVAL, "sizes beyond the 32-bit tile grid");
-  T->Kt_h.alloc(ctx, size_t(nw * T->Kp));
-  T->Kt_l.alloc(ctx, size_t(nw * T->Kp));
-  T->G_h.alloc(ctx, size_t(ni * T->Kp));
-  T->G_l.alloc(ctx, size_t(ni * T->Kp));
-  T->KK_h.alloc(ctx, size_t(nw * T->Kp2));
-  T->KK_l.alloc(ctx, size_t(nw * T->Kp2));
-  T->Im_h.alloc(ctx, size_t(ni * T->Kp2));
-  T->Im_l.alloc(ctx, size_t(ni * T->Kp2));
+  for (int p = 0; p < kNs; ++p) {
+    T->Kt[p].alloc(ctx, size_t(nw * T->Kp));
+    T->G[p].alloc(ctx, size_t(ni * T->Kp));
+    T->KK[p].alloc(ctx, size_t(nw * T->Kp2));
+    T->Im[p].alloc(ctx, size_t(ni * T->Kp2));
+  }
   T->err.alloc(ctx, 1);
   T->err.zero(s);
   // B of the contraction: G [nk, ni] column-major is G^T row-major [ni][nk].
-  split_rows_kernel<<<div_up(size_t(ni * T->Kp), 256), 256, 0, s>>>(P->d_G.p, nk, ni, nk, T->Kp, T->G_h.p, T->G_l.p);
+  split3_rows_kernel<<<div_up(size_t(ni * T->Kp), 256), 256, 0, s>>>(P->d_G.p, nk, ni, nk, T->Kp, false, T->G[0].p,
+                                                                     T->G[1].p, T->G[2].p);
   EPSP_LAUNCHED(ctx);
   // A of the Kramers-Kronig map: A[ω][ω'] = KK[ω + nω ω'].
-  split_rows_t_kernel<<<div_up(size_t(nw * T->Kp2), 256), 256, 0, s>>>(P->d_KK.p, nw, nw, nw, T->Kp2, T->KK_h.p, T->KK_l.p);
+  split3_rows_kernel<<<div_up(size_t(nw * T->Kp2), 256), 256, 0, s>>>(P->d_KK.p, nw, nw, nw, T->Kp2, true, T->KK[0].p,
+                                                                      T->KK[1].p, T->KK[2].p);
   EPSP_LAUNCHED(ctx);
-  tc_gemm_shape(ctx, int(nw), int(ni), int(nk), 16, &T->bn1, &T->splits1);
-  tc_gemm_shape(ctx, int(nw), int(ni), int(nw), 16, &T->bn2, &T->splits2);
+  tc_gemm_shape(ctx, int(nw), int(ni), int(nk), 16, kNs, &T->bn1, &T->splits1);
+  tc_gemm_shape(ctx, int(nw), int(ni), int(nw), 16, kNs, &T->bn2, &T->splits2);
   T->part.alloc(ctx, size_t(std::max(T->splits1, T->splits2)) * size_t(nw * ni));
-  T->opK = {make_tmap_bf16(T->Kt_h.p, nw, nk, T->Kp, kTcBM), make_tmap_bf16(T->Kt_l.p, nw, nk, T->Kp, kTcBM)};
-  T->opG = {make_tmap_bf16(T->G_h.p, ni, nk, T->Kp, T->bn1), make_tmap_bf16(T->G_l.p, ni, nk, T->Kp, T->bn1)};
-  T->opKK = {make_tmap_bf16(T->KK_h.p, nw, nw, T->Kp2, kTcBM), make_tmap_bf16(T->KK_l.p, nw, nw, T->Kp2, kTcBM)};
-  T->opIm = {make_tmap_bf16(T->Im_h.p, ni, nw, T->Kp2, T->bn2), make_tmap_bf16(T->Im_l.p, ni, nw, T->Kp2, T->bn2)};
+  T->opK = operand(T->Kt, nw, nk, T->Kp, kTcBM);
+  T->opG = operand(T->G, ni, nk, T->Kp, T->bn1);
+  T->opKK = operand(T->KK, nw, nw, T->Kp2, kTcBM);
+  T->opIm = operand(T->Im, ni, nw, T->Kp2, T->bn2);
 }
 
 static void check_err(Scgd0Plan* P) {
@@ -177,7 +189,7 @@ void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS) {
   long pk = prof_begin(ctx, "kbuild");
   kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), 32), unsigned(T->Kp / 64)), 256, 0, s>>>(
       int(nw), d_Sin, P->d_cell_j.p, P->d_cell_t.p, P->d_cell_x.p, P->d_wnu.p, int(P->nm), P->d_epsc.p, P->d_colc.p, nk,
-      P->d_Fa.p, P->d_Fe.p, P->w_ac, T->Kt_h.p, T->Kt_l.p, T->Kp);
+      P->d_Fa.p, P->d_Fe.p, P->w_ac, T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pk);
   const long slab = nw * ni;
@@ -192,7 +204,8 @@ void tc_kk_assemble(Scgd0Plan* P, double2* d_Snew) {
   cudaStream_t s = ctx->stream;
   auto* T = P->tc.get();
   const long nw = P->nw, ni = P->ni, slab = nw * ni;
-  split_rows_kernel<<<div_up(size_t(ni * T->Kp2), 256), 256, 0, s>>>(P->d_ImS.p, nw, ni, nw, T->Kp2, T->Im_h.p, T->Im_l.p);
+  split3_rows_kernel<<<div_up(size_t(ni * T->Kp2), 256), 256, 0, s>>>(P->d_ImS.p, nw, ni, nw, T->Kp2, false, T->Im[0].p,
+                                                                      T->Im[1].p, T->Im[2].p);
   EPSP_LAUNCHED(ctx);
   int sp = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(ni), int(nw), T->part.p, nw, slab, 16, T->err.p, "tc_kk");
   finalize_assemble_kernel<<<div_up(size_t(slab), 256), 256, 0, s>>>(T->part.p, slab, sp, slab, P->d_ImS.p, d_Snew);

@@ -35,8 +35,8 @@ CUtensorMap make_tmap_bf16(const void* base, long rows, long cols, long ld, int 
   return m;
 }
 
-void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int* bn, int* splits) {
-  const int BN = N > 128 ? 256 : 128;
+void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* bn, int* splits) {
+  const int BN = (ns == 2 && N > 128) ? 256 : 128;
   const int tiles = ((M + kTcBM - 1) / kTcBM) * ((N + BN - 1) / BN);
   const int kblocks = (K + kTcBK - 1) / kTcBK;
   int sp = std::max(1, (ctx->sm_count + tiles - 1) / tiles);
@@ -47,32 +47,40 @@ void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int* bn, int* 
   *splits = sp;
 }
 
-template <int BN, int STAGES>
+template <int BN, int STAGES, int NS>
 static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int kblocks, int per, int splits,
                    float* out, long ld_out, long split_stride, int* d_err) {
-  using L = TcSmem<BN, STAGES>;
+  using L = TcSmem<BN, STAGES, NS>;
   static bool configured = false;  // one process, one attribute setting per instantiation
   if (!configured) {
-    EPSP_CUDA(cudaFuncSetAttribute(tc_gemm_bf16x3_kernel<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::kBytes));
+    EPSP_CUDA(cudaFuncSetAttribute(tc_gemm_split_kernel<BN, STAGES, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::kBytes));
     configured = true;
   }
+  TcMaps maps;
+  for (int p = 0; p < 3; ++p) {
+    maps.a[p] = A.m[p < NS ? p : 0];
+    maps.b[p] = B.m[p < NS ? p : 0];
+  }
   dim3 grid((M + kTcBM - 1) / kTcBM, (N + BN - 1) / BN, splits);
-  tc_gemm_bf16x3_kernel<BN, STAGES><<<grid, 128, L::kBytes, ctx->stream>>>(A.hi, A.lo, B.hi, B.lo, M, N, kblocks, per, out,
-                                                                           ld_out, split_stride, d_err);
+  tc_gemm_split_kernel<BN, STAGES, NS><<<grid, 128, L::kBytes, ctx->stream>>>(maps, M, N, kblocks, per, out, ld_out,
+                                                                              split_stride, d_err);
   EPSP_LAUNCHED(ctx);
 }
 
 int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int K, float* out, long ld_out,
                    long split_stride, int max_splits, int* d_err, const char* prof_name) {
+  if (A.ns != B.ns || (A.ns != 2 && A.ns != 3)) fail(EPSP_EINVAL, "operands must be split into 2 or 3 parts alike");
   int BN, splits;
-  tc_gemm_shape(ctx, M, N, K, max_splits, &BN, &splits);
+  tc_gemm_shape(ctx, M, N, K, max_splits, A.ns, &BN, &splits);
   const int kblocks = (K + kTcBK - 1) / kTcBK;
   const int per = (kblocks + splits - 1) / splits;
   long pi = prof_begin(ctx, prof_name);
-  if (BN == 256)
-    launch<256, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+  if (A.ns == 3)
+    launch<128, 2, 3>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+  else if (BN == 256)
+    launch<256, 2, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   else
-    launch<128, 3>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    launch<128, 3, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   prof_end(ctx, pi);
   return splits;
 }

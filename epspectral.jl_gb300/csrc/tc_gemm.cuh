@@ -99,22 +99,26 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-template <int BN, int STAGES>
+// NS = 2: operands split x = x0 + x1 (hi, lo), products 00, 01, 10 (BF16x3, ~2^-16 relative);
+// NS = 3: x = x0 + x1 + x2 (hi, mid, lo), products 00, 01, 10, 02, 11, 20 (six, ~2^-23 relative).
+template <int BN, int STAGES, int NS>
 struct TcSmem {
   static constexpr int kA = kTcBM * kTcBK * 2;   // bytes of one A tile
   static constexpr int kB = BN * kTcBK * 2;      // bytes of one B tile
-  static constexpr int kStage = 2 * kA + 2 * kB;
+  static constexpr int kStage = NS * kA + NS * kB;
   static constexpr int kBars = 2 * STAGES + 1;
   static constexpr int kBytes = STAGES * kStage + 8 * kBars + 16 + 1024;  // + alignment slack
 };
 
-template <int BN, int STAGES>
+struct TcMaps {
+  CUtensorMap a[3], b[3];
+};
+
+template <int BN, int STAGES, int NS>
 __global__ void __launch_bounds__(128, 1)
-    tc_gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
-                          const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, int M, int N,
-                          int kblocks, int kb_per_split, float* __restrict__ out, long ld_out, long split_stride,
-                          int* __restrict__ err) {
-  using L = TcSmem<BN, STAGES>;
+    tc_gemm_split_kernel(const __grid_constant__ TcMaps maps, int M, int N, int kblocks, int kb_per_split,
+                         float* __restrict__ out, long ld_out, long split_stride, int* __restrict__ err) {
+  using L = TcSmem<BN, STAGES, NS>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * L::kStage);
@@ -155,10 +159,11 @@ __global__ void __launch_bounds__(128, 1)
       const uint32_t fb = full0 + 8 * s;
       mbar_expect_tx(fb, L::kStage);
       const int kc = (kb0 + kb) * kTcBK;
-      tma_load_2d(smem_u32(st), &mAh, kc, m0, fb);
-      tma_load_2d(smem_u32(st + L::kA), &mAl, kc, m0, fb);
-      tma_load_2d(smem_u32(st + 2 * L::kA), &mBh, kc, n0, fb);
-      tma_load_2d(smem_u32(st + 2 * L::kA + L::kB), &mBl, kc, n0, fb);
+#pragma unroll
+      for (int p = 0; p < NS; ++p) {
+        tma_load_2d(smem_u32(st + p * L::kA), &maps.a[p], kc, m0, fb);
+        tma_load_2d(smem_u32(st + NS * L::kA + p * L::kB), &maps.b[p], kc, n0, fb);
+      }
       issued = kb + 1;
     }
     if (*(volatile int*)&s_abort) {
@@ -177,16 +182,20 @@ __global__ void __launch_bounds__(128, 1)
       }
       if (*(volatile int*)&s_abort) break;
       tc_fence_after();
-      const uint32_t a_h = smem_u32(smem + s * L::kStage);
-      const uint32_t a_l = a_h + L::kA, b_h = a_h + 2 * L::kA, b_l = b_h + L::kB;
+      const uint32_t a0 = smem_u32(smem + s * L::kStage);
+      const uint32_t b0 = a0 + NS * L::kA;
 #pragma unroll
       for (int ks = 0; ks < kTcBK / 16; ++ks) {
         const uint32_t off = ks * 32;  // 16 BF16 along K inside the 128-byte swizzle row
-        const uint64_t dah = sw128_desc(a_h + off), dal = sw128_desc(a_l + off);
-        const uint64_t dbh = sw128_desc(b_h + off), dbl = sw128_desc(b_l + off);
-        umma_bf16(tmem, dah, dbh, idesc, (kb | ks) != 0);
-        umma_bf16(tmem, dah, dbl, idesc, 1);
-        umma_bf16(tmem, dal, dbh, idesc, 1);
+        // the split products of increasing order: 00; 01, 10; (NS = 3) 02, 11, 20
+        umma_bf16(tmem, sw128_desc(a0 + off), sw128_desc(b0 + off), idesc, (kb | ks) != 0);
+        umma_bf16(tmem, sw128_desc(a0 + off), sw128_desc(b0 + L::kB + off), idesc, 1);
+        umma_bf16(tmem, sw128_desc(a0 + L::kA + off), sw128_desc(b0 + off), idesc, 1);
+        if constexpr (NS == 3) {
+          umma_bf16(tmem, sw128_desc(a0 + off), sw128_desc(b0 + 2 * L::kB + off), idesc, 1);
+          umma_bf16(tmem, sw128_desc(a0 + L::kA + off), sw128_desc(b0 + L::kB + off), idesc, 1);
+          umma_bf16(tmem, sw128_desc(a0 + 2 * L::kA + off), sw128_desc(b0 + off), idesc, 1);
+        }
       }
       umma_commit(empty0 + 8 * s);
     }
@@ -234,16 +243,28 @@ __global__ void __launch_bounds__(128, 1)
 // elements), box = 64 x box_rows, 128-byte swizzle; out-of-range elements read as zero.
 CUtensorMap make_tmap_bf16(const void* base, long rows, long cols, long ld, int box_rows);
 
+// The BF16 parts of one operand: ns = 2 (hi, lo) or 3 (hi, mid, lo) tensor maps.
 struct TcOperand {
-  CUtensorMap hi, lo;
+  CUtensorMap m[3];
+  int ns = 2;
 };
 
-// Launches D = A_hi B_hi + A_hi B_lo + A_lo B_hi for A [M][K], B [N][K] (K-major) into the
-// FP32 slabs out[split][m + ld_out n]; returns the number of splits used.
+// Launches the split-precision product of A [M][K] and B [N][K] (K-major, both split into A.ns
+// parts) into the FP32 slabs out[split][m + ld_out n]; returns the number of splits used.
 int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int K, float* out, long ld_out,
                    long split_stride, int max_splits, int* d_err, const char* prof_name = "tc_gemm");
 
-// The BN and split count tc_gemm_launch picks for (M, N, K) with at most max_splits splits.
-void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int* bn, int* splits);
+// The BN and split count tc_gemm_launch picks for (M, N, K), ns parts, at most max_splits splits.
+void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* bn, int* splits);
+
+// x = Σ_p x_p with x_p BF16, p < ns (round to nearest at every step).
+__device__ __forceinline__ void split_bf16_n(float x, int ns, __nv_bfloat16* out) {
+  float r = x;
+  for (int p = 0; p < ns; ++p) {
+    __nv_bfloat16 h = __float2bfloat16_rn(r);
+    out[p] = h;
+    r -= __bfloat162float(h);
+  }
+}
 
 }  // namespace epsp

@@ -60,7 +60,7 @@ enum { EPSP_METAL = 0, EPSP_SEMICONDUCTOR = 1 };
  *  GEMM_BF16X3 : as GEMM_FP64, with the contractions on the tcgen05 tensor cores in BF16 hi/lo
  *                split precision (three products, FP32 accumulation); the chemical-potential
  *                bisection, the carrier integral and the GMRES orthogonalisation stay FP64. */
-enum { EPSP_PATH_DIRECT_FP64 = 0, EPSP_PATH_GEMM_FP64 = 1, EPSP_PATH_GEMM_BF16X3 = 2 };
+enum { EPSP_PATH_DIRECT_FP64 = 0, EPSP_PATH_GEMM_FP64 = 1, EPSP_PATH_GEMM_BF16 = 2 };
 
 /* Ladder solver (src/ladder.jl:340-369). */
 enum { EPSP_SOLVER_GMRES = 0, EPSP_SOLVER_FIXED_POINT = 1 };

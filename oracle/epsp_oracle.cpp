@@ -768,16 +768,21 @@ void ladder_contract_sample(const Ladder& L, double T, double w_ac, const double
               X[size_t(j + nw * (c12 + 4 * (c0 + 2)) + nrow * kk)] = wl * J[2 * a0 + 1] + wh * J[2 * a1 + 1];
             }
       }
+      // C += X B̃ threaded over row blocks of C, as the reference does (src/ladder.jl:286-289).
       double* C = s == 0 ? Cp.data() : Cm.data();
+      const int64_t rb = 256, nrb = (nrow + rb - 1) / rb;
 #pragma omp parallel for schedule(static)
-      for (int64_t col = 0; col < ncol; ++col) {
-        double* Cc = C + nrow * col;
-        const double* Bc = Bt.data() + nk * col;
-        for (int64_t k = 0; k < nk; ++k) {
-          double bv = Bc[k];
-          if (bv == 0.0) continue;
-          const double* Xk = X.data() + nrow * k;
-          for (int64_t r = 0; r < nrow; ++r) Cc[r] += Xk[r] * bv;
+      for (int64_t blk = 0; blk < nrb; ++blk) {
+        const int64_t r0 = blk * rb, r1 = std::min(nrow, r0 + rb);
+        for (int64_t col = 0; col < ncol; ++col) {
+          double* Cc = C + nrow * col;
+          const double* Bc = Bt.data() + nk * col;
+          for (int64_t k = 0; k < nk; ++k) {
+            double bv = Bc[k];
+            if (bv == 0.0) continue;
+            const double* Xk = X.data() + nrow * k;
+            for (int64_t r = r0; r < r1; ++r) Cc[r] += Xk[r] * bv;
+          }
         }
       }
     }

@@ -59,7 +59,7 @@ def test_apply_matches_oracle(api, oracle, request, case, Omega, k):
     for iT in range(2):
         args = (J, c["sigma"][:, :, iT], c["mu"][iT], c["Tlist"][iT], Omega)
         ref = oracle.apply_ladder_kernel(s, *args, omega_acoustic=W_AC)
-        for path, tol in (("direct_fp64", 1e-10), ("gemm_fp64", 1e-10), ("gemm_bf16x3", 1e-4)):
+        for path, tol in (("direct_fp64", 1e-10), ("gemm_fp64", 1e-10), ("gemm_bf16", 1e-4)):
             for tile in ((None, 7) if path == "direct_fp64" else (None,)):
                 got = api.apply_ladder_kernel(s, *args, omega_acoustic=W_AC, path=path, gpu_tile=tile)
                 assert rel(got, ref) <= tol, (path, tile, rel(got, ref))
@@ -81,7 +81,7 @@ def test_loop_matches_oracle(api, oracle, cc):
         again = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], Omegas, path=path, **kw)
         assert np.array_equal(again["J"], got["J"]) and np.array_equal(again["sigma_ladder"], got["sigma_ladder"])
         assert all(np.array_equal(a["norms"], b["norms"]) for a, b in zip(again["history"].ravel(), got["history"].ravel()))
-    bf = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], Omegas, path="gemm_bf16x3", **kw)
+    bf = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], Omegas, path="gemm_bf16", **kw)
     assert rel(bf["sigma_ladder"], ref["sigma_ladder"]) <= 1e-4
     # fixed point, streamed-size chunks, Ω > 0 (test/test_ladder_gpu.jl:134-139)
     fk = dict(solver="fixed_point", rtol=1e-6, maxiter=200, omega_acoustic=W_AC)
@@ -94,7 +94,7 @@ def test_loop_matches_oracle(api, oracle, cc):
 def test_holstein_current_correction_vanishes(api, hsym):
     # test/test_ladder_holstein.jl:5-26 on the GPU paths
     c = hsym
-    for path in ("direct_fp64", "gemm_fp64", "gemm_bf16x3"):
+    for path in ("direct_fp64", "gemm_fp64", "gemm_bf16"):
         out = api.loop_ladder(c["setup"], c["sigma"], c["mu"], c["Tlist"], [0.0, 0.2], path=path, omega_acoustic=W_AC)
         assert np.linalg.norm(out["sigma_ladder"] - out["sigma_bubble"]) <= 1e-9 * np.linalg.norm(out["sigma_bubble"])
         assert out["converged"].all()

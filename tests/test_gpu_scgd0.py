@@ -74,7 +74,7 @@ def test_holstein_loop_matches_oracle(api, oracle, holstein_gpu, nlist):
         assert np.array_equal(again["sigma"], got["sigma"]) and np.array_equal(again["mu"], got["mu"])
     tiled = api.loop_scgd0(s, occ(nlist), path="direct_fp64", gpu_tile=7, **kw)
     assert rel(tiled["sigma"], ref["sigma"]) <= 1e-10
-    bf = api.loop_scgd0(s, occ(nlist), path="gemm_bf16x3", **kw)
+    bf = api.loop_scgd0(s, occ(nlist), path="gemm_bf16", **kw)
     assert np.max(np.abs(bf["sigma"] - ref["sigma"])) <= 1e-5
     assert abs(bf["mu"][0] - ref["mu"][0]) <= 1e-5
 
@@ -99,7 +99,7 @@ def test_cubic_loop_matches_oracle(api, oracle, cubic_small):
         assert np.allclose(got["mu"], ref["mu"], rtol=1e-10, atol=1e-12)
         assert np.allclose(got["history"]["err"], ref["history"]["err"], rtol=1e-8)
         assert np.allclose(got["history"]["min_spectral_weight"], ref["history"]["min_spectral_weight"], rtol=1e-10)
-    bf = api.loop_scgd0(s, o, path="gemm_bf16x3", **kw)
+    bf = api.loop_scgd0(s, o, path="gemm_bf16", **kw)
     assert np.max(np.abs(bf["sigma"] - ref["sigma"])) <= 1e-5
     assert np.max(np.abs(bf["mu"] - ref["mu"])) <= 1e-5
     gt = api.loop_scgd0(s, o, path="direct_fp64", gpu_tile=37, **kw)
@@ -121,7 +121,7 @@ def test_errors_come_back_as_status(api, holstein_gpu, cubic_small):
     # dispersive modes are refused by the recast paths, accepted by the direct one
     disp = dict(s, omega_ph=np.asfortranarray(0.2 + 0.01 * np.arange(64.0)[None, :]))
     with pytest.raises(api.EpspError, match="dispersionless"):
-        api.Scgd0Plan(disp, path="gemm_bf16x3", omega_acoustic=W_AC)
+        api.Scgd0Plan(disp, path="gemm_bf16", omega_acoustic=W_AC)
     api.Scgd0Plan(disp, path="direct_fp64", omega_acoustic=W_AC).close()
     # a device allocation failure is reported, and the context stays usable
     ctx = api.Context(0)
