@@ -3,12 +3,16 @@ frequency, on the synthetic 3-band cubic t2g model (16^3 k points: 495 outer / 1
 15 dispersionless modes in [10, 80] meV, log-normal FP32 g2 from a seed, graded 1251-node ωs, one
 temperature 300 K).
 
-One step = scGD0 from Σ = -iη_init (η_init = 10 meV) to max|ΔΣ| < 1e-6 eV (maxiter 50), then the
+One step = scGD0 to max|ΔΣ| < 1e-6 eV (maxiter 50) started from the learned warm start (the G0D0
+iteration from Σ = -iη_init, η_init = 10 meV, then the network's Σ_init, on the device), then the
 ladder σ(Ω) at Ω = 0.1 eV by GMRES (rtol 1e-2, maxiter 30), on the fast path (recast Fan-Migdal sum
-and per-mode regrouped ladder on the tcgen05 tensor cores, BF16x3). `value` is the device time of a
-step in seconds (CUDA events on the library's stream), inputs resident in HBM; `e2e` is the same
-step through the public API from host arrays (plan set-up with the g2 upload, results read back).
-The plain FP64 GPU paths are timed once beside it for the speed-up and the accuracy check.
+and per-mode regrouped ladder on the tcgen05 tensor cores, BF16 split operands). `value` is the
+device time of a step in seconds (CUDA events on the library's stream), inputs resident in HBM;
+`e2e` is the same step through the public API from host arrays (plan set-up with the g2 upload,
+results read back). Before the timed steps the warm-start network is trained on the GPU on pairs
+the method generates (256 seeded runs of the same model with T in [100, 800] K, filling in
+[0.5, 1.5] e/site, g2 scale in [0.5, 2]) and checked on 32 held-out runs. The plain FP64 GPU
+paths are timed once beside it for the speed-up and the accuracy check.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -42,8 +46,10 @@ W_AC = 1e-4
 # applications per Ω: GMRES iterations plus none for a cold start), measured on a GB300 by this
 # script's FP64 leg; the reference arm, which cannot run the workload to the end on the CPU, times
 # bounded samples and scales them by these counts.
-FP64_SCGD0_ITERS = None
-FP64_LADDER_APPLIES = None
+FP64_SCGD0_ITERS = 12
+FP64_LADDER_APPLIES = 2
+# learned warm start: training and held-out runs, epochs
+WARM_TRAIN_RUNS, WARM_HELDOUT_RUNS, WARM_EPOCHS = 256, 32, 40
 
 
 def workload():
@@ -161,17 +167,63 @@ def flush_l2(device: int, nbytes=512 << 20):
     del b
 
 
+def train_warm_start(s, ctx):
+    """Trains the warm start on the GPU on pairs from the method itself and measures it on held-out
+    runs (plain iterations from the pair generation, warm-started iterations on the device)."""
+    from epspectral_gb300 import api
+    from epspectral_gb300 import warmstart as W
+    t0 = time.perf_counter()
+    runs_tr = W.sample_runs(WARM_TRAIN_RUNS, 11)
+    runs_te = W.sample_runs(WARM_HELDOUT_RUNS, 12, group=4)
+    Xtr, Ytr, _ = W.generate_pairs(s, runs_tr, ctx=ctx)
+    Xte, Yte, rte = W.generate_pairs(s, runs_te, ctx=ctx)
+    t_gen = time.perf_counter() - t0
+    nw = len(s["omegas"])
+    ws = W.WarmStart(nw, ctx=ctx)
+    t0 = time.perf_counter()
+    hist = ws.fit(np.concatenate(Xtr), np.concatenate(Ytr), epochs=WARM_EPOCHS, batch=256, lr=1e-3)
+    t_fit = time.perf_counter() - t0
+    del Xtr, Ytr
+    plain, warm, dsig, fallbacks = [], [], [], 0
+    plan, plan_scale = None, None
+    for run, rec, X, Y in zip(runs_te, rte, Xte, Yte):
+        if plan is None or run["scale"] != plan_scale:
+            if plan is not None:
+                plan.close()
+            ss = dict(s)
+            ss["g2"] = np.asfortranarray(s["g2"] * np.float32(run["scale"]))
+            plan, plan_scale = api.Scgd0Plan(ss, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx), run["scale"]
+        occ = dict(Tlist=[rec["T"]], nlist=[0.0], nelec=run["filling"], spin_degeneracy=2.0, type="metal")
+        r = plan.run(occ, eta_init=ETA_INIT, tol=TOL, maxiter=MAXITER, mu_start=[rec["mu0"]], warm=ws,
+                     coupling_scale=run["scale"])
+        fallbacks += int(r["fallback"])
+        S_plain = (X[:, :nw] + Y[:, :nw] + 1j * (X[:, nw:2 * nw] + Y[:, nw:])).T
+        dsig.append(float(np.max(np.abs(r["sigma"][:, :, 0] - S_plain))))
+        plain.append(rec["niter"])
+        warm.append(r["iters_total"])
+    plan.close()
+    info = dict(train_runs=WARM_TRAIN_RUNS, heldout_runs=WARM_HELDOUT_RUNS, epochs=WARM_EPOCHS,
+                network=f"MLP {'-'.join(map(str, ws.dims))}, SiLU, BF16 weights / FP32 accumulate, Adam",
+                pair_generation_s=t_gen, train_s=t_fit, final_loss=float(hist[-1]), first_loss=float(hist[0]),
+                heldout_plain_iters_mean=float(np.mean(plain)), heldout_warm_iters_mean=float(np.mean(warm)),
+                heldout_fallbacks=fallbacks, heldout_max_abs_dsigma_vs_plain_eV=float(np.max(dsig)))
+    return ws, info
+
+
 def run_ours(args, world, rank, local):
     from epspectral_gb300 import api
     s, T, occ, mu0 = workload()
     ctx = api.Context(local)
+    ws, warm_info = train_warm_start(s, ctx)
+    if args.save_warm:
+        ws.save(args.save_warm)
     sp = api.Scgd0Plan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
     lp = api.LadderPlan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
     nw, ni = len(s["omegas"]), s["eps_i"].size
 
     def step():
         ctx.timer_begin()
-        r = sp.run(occ, eta_init=ETA_INIT, tol=TOL, maxiter=MAXITER, mu_start=[mu0])
+        r = sp.run(occ, eta_init=ETA_INIT, tol=TOL, maxiter=MAXITER, mu_start=[mu0], warm=ws)
         t_s = ctx.timer_end() / 1e3
         ctx.timer_begin()
         l = lp.run(r["sigma"], r["mu"], [T], [OMEGA], solver="gmres", rtol=L_RTOL, maxiter=L_MAXITER)
@@ -206,12 +258,18 @@ def run_ours(args, world, rank, local):
                config=dict(workload="3-band cubic t2g nk=16^3, 495 outer / 12288 inner states, 15 modes, graded "
                                     "1251-node grid, T=300 K; scGD0 to 1e-6 eV + ladder at one Omega=0.1 eV",
                            ni=ni, nf=int(s["eps_f"].size), nw=nw, nm=15, path="gemm_bf16",
-                           warm_start=False, l2="flushed between steps (512 MB write)",
+                           warm_start=True, l2="flushed between steps (512 MB write)",
                            parallelism=f"replicas x{world}"))
     if rank != 0:
         return
     out["scgd0_s_to_tol"] = float(np.median(ts))
-    out["scgd0_iters"] = int(r["niter"])
+    out["scgd0_iters"] = int(r["iters_total"])
+    out["scgd0_warm_fallback"] = bool(r["fallback"])
+    ctx.timer_begin()
+    r_cold = sp.run(occ, eta_init=ETA_INIT, tol=TOL, maxiter=MAXITER, mu_start=[mu0])
+    out["scgd0_s_to_tol_without_warm_start"] = ctx.timer_end() / 1e3
+    out["scgd0_iters_without_warm_start"] = int(r_cold["niter"])
+    out["warm_start"] = warm_info
     out["ladder_s_per_omega"] = float(np.median(tl))
     out["ladder_gmres_iters"] = int(l["niter"][0, 0])
     out["gpu_launches"] = int(launches)
@@ -229,8 +287,9 @@ def run_ours(args, world, rank, local):
     out["clocks"] = clk.summary()
     # end to end through the public API from host arrays
     t0 = time.perf_counter()
-    r_e = api.loop_scgd0(s, occ, eta_init=ETA_INIT, tol=TOL, maxiter=MAXITER, mu_start=[mu0], omega_acoustic=W_AC,
-                         path="gemm_bf16", ctx=ctx)
+    sp_e = api.Scgd0Plan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
+    r_e = sp_e.run(occ, eta_init=ETA_INIT, tol=TOL, maxiter=MAXITER, mu_start=[mu0], warm=ws)
+    sp_e.close()
     l_e = api.loop_ladder(s, r_e["sigma"], r_e["mu"], [T], [OMEGA], rtol=L_RTOL, maxiter=L_MAXITER,
                           omega_acoustic=W_AC, path="gemm_bf16", ctx=ctx)
     e2e = time.perf_counter() - t0
@@ -264,6 +323,7 @@ def run_ours(args, world, rank, local):
     out["speedup_scgd0_vs_direct_fp64"] = plain["direct_fp64_scgd0_s_to_tol"] / out["scgd0_s_to_tol"]
     out["accuracy_vs_fp64"] = dict(
         max_abs_dsigma_eV=float(np.max(np.abs(r["sigma"] - r64["sigma"]))),
+        max_abs_dsigma_without_warm_start_eV=float(np.max(np.abs(r_cold["sigma"] - r64["sigma"]))),
         abs_dmu_eV=float(abs(r["mu"][0] - r64["mu"][0])),
         rel_sigma_ladder=float(np.linalg.norm(l["sigma_ladder"] - l64["sigma_ladder"]) / np.linalg.norm(l64["sigma_ladder"])))
     out["cpu_baseline"] = cpu_baseline(s, T, r64, plain["fp64_scgd0_iters"], plain["fp64_ladder_gmres_iters"])
@@ -342,6 +402,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--save-warm", default=None, help="write the trained warm-start network to this .npz")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

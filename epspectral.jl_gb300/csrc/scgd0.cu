@@ -11,6 +11,7 @@
 #include "common.cuh"
 #include "gemm_f64.cuh"
 #include "scgd0.cuh"
+#include "warmstart.cuh"
 
 #include <cooperative_groups.h>
 
@@ -752,9 +753,13 @@ void scgd0_imsigma(Scgd0Plan* P, const double2* d_Sin, double mu, double T, doub
 // the iteration (src/scgd0.jl:246-346)
 // ---------------------------------------------------------------------------------------------
 
+// The iteration. With `warm`, the network corrects Σ of every still-active temperature after the
+// first iteration (the G0D0 one), with coupling scale warm_scale[iT]; the iterations that follow
+// compare against the corrected Σ, as a run started from Σ_init = G0D0 + correction would.
 void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double eta_init, int32_t maxiter, double tol,
                int32_t fix_mu, const double* mu_start, const double* sigma_init, double* sigma_out, double* mu_out,
-               uint8_t* converged, epsp_scgd0_history* hist) {
+               uint8_t* converged, epsp_scgd0_history* hist, epsp_warmstart* warm = nullptr,
+               const double* warm_scale = nullptr) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
   if (!occ || !occ->Tlist || (!occ->nlist && !fix_mu)) fail(EPSP_EINVAL, "occ is incomplete");
@@ -886,6 +891,11 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
         hist->iter_frozen[iT] = iter;
       }
     }
+    if (warm && iter == 1 && iter < maxiter)
+      for (int64_t iT = 0; iT < nT; ++iT)
+        if (active[size_t(iT)])
+          warmstart_correct(warm, ctx, S.p + slab * iT, nw, ni, P->d_eps_i.p, occ->Tlist[iT], mu[size_t(iT)],
+                            warm_scale[iT]);
     hist->wall[iter - 1] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     niter = iter;
     if (std::none_of(active.begin(), active.end(), [](char a) { return a != 0; })) break;
@@ -944,6 +954,28 @@ epsp_status epsp_scgd0_run(epsp_scgd0_plan* plan, const epsp_occ* occ, const dou
   auto* P = reinterpret_cast<Scgd0Plan*>(plan);
   return guarded(P->ctx, [&] {
     scgd0_run(P, occ, eta_min, eta_init, maxiter, tol, fix_mu, mu_start, sigma_init, sigma_out, mu_out, converged, hist);
+  });
+}
+
+epsp_status epsp_scgd0_run_warm(epsp_scgd0_plan* plan, epsp_warmstart* net, const double* coupling_scale,
+                                const epsp_occ* occ, const double* eta_min, double eta_init, int32_t maxiter, double tol,
+                                int32_t fix_mu, const double* mu_start, double* sigma_out, double* mu_out,
+                                uint8_t* converged, epsp_scgd0_history* hist, int32_t* iters_total, int32_t* fallback) {
+  if (!plan || !net || !coupling_scale || !iters_total || !fallback) return EPSP_EINVAL;
+  auto* P = reinterpret_cast<Scgd0Plan*>(plan);
+  return guarded(P->ctx, [&] {
+    scgd0_run(P, occ, eta_min, eta_init, maxiter, tol, fix_mu, mu_start, nullptr, sigma_out, mu_out, converged, hist,
+              net, coupling_scale);
+    *iters_total = hist->niter;
+    *fallback = 0;
+    bool all = true;
+    for (int64_t iT = 0; iT < occ->nT; ++iT) all = all && converged[iT];
+    if (!all) {  // the plain start decides
+      const int32_t used = hist->niter;
+      scgd0_run(P, occ, eta_min, eta_init, maxiter, tol, fix_mu, mu_start, nullptr, sigma_out, mu_out, converged, hist);
+      *iters_total = used + hist->niter;
+      *fallback = 1;
+    }
   });
 }
 

@@ -72,6 +72,18 @@ def lib():
         "epsp_ladder_run": (C.c_int, [vp, c_double_p, c_double_p, c_double_p, i64, c_double_p, i64, i32, d, i32,
                                       c_double_p, c_double_p, u8p, c_int32_p, P(epsp_ladder_history), c_double_p]),
         "epsp_ladder_apply": (C.c_int, [vp, c_double_p, d, d, d, c_double_p, c_double_p]),
+        "epsp_warmstart_create": (C.c_int, [vp, i32, P(i32), P(vp)]),
+        "epsp_warmstart_destroy": (None, [vp]),
+        "epsp_warmstart_nparams": (i64, [vp]),
+        "epsp_warmstart_set_params": (C.c_int, [vp, P(C.c_float)]),
+        "epsp_warmstart_get_params": (C.c_int, [vp, P(C.c_float)]),
+        "epsp_warmstart_predict": (C.c_int, [vp, P(C.c_float), i64, P(C.c_float)]),
+        "epsp_warmstart_grad": (C.c_int, [vp, P(C.c_float), P(C.c_float), i64, P(d), P(C.c_float)]),
+        "epsp_warmstart_set_scaling": (C.c_int, [vp, P(C.c_float), P(C.c_float), P(C.c_float), C.c_float]),
+        "epsp_scgd0_run_warm": (C.c_int, [vp, vp, c_double_p, P(epsp_occ), c_double_p, d, i32, d, i32, c_double_p,
+                                          c_double_p, c_double_p, u8p, P(epsp_scgd0_history), P(i32), P(i32)]),
+        "epsp_warmstart_train": (C.c_int, [vp, P(C.c_float), P(C.c_float), i64, i32, i32, C.c_float, P(i64),
+                                           c_double_p]),
     }
     for name, (res, args) in sig.items():
         if not hasattr(L, name):
@@ -167,8 +179,13 @@ class Scgd0Plan:
         self.ctx.check(lib().epsp_scgd0_setup(self.ctx.handle, C.byref(self.M.struct), C.byref(self.opts),
                                               C.byref(self.handle)))
 
-    def run(self, occ, *, eta_init, tol, maxiter=20, eta_min=None, fix_mu=False, mu_start=None, sigma_init=None):
-        """The iteration of _loop_scgd0 (src/scgd0.jl:246-346)."""
+    def run(self, occ, *, eta_init, tol, maxiter=20, eta_min=None, fix_mu=False, mu_start=None, sigma_init=None,
+            warm=None, coupling_scale=1.0):
+        """The iteration of _loop_scgd0 (src/scgd0.jl:246-346).
+
+        With `warm` (a trained warmstart.WarmStart, no Σ_init) the run starts from the network's
+        Σ_init after the G0D0 iteration, with the plain start as fallback (epsp_scgd0_run_warm);
+        the result then also holds `iters_total` and `fallback`."""
         M, O = self.M, OccArrays(occ)
         nT = len(O.Tlist)
         if eta_min is not None and np.ndim(eta_min) > 0 and len(eta_min) != nT:
@@ -182,6 +199,19 @@ class Scgd0Plan:
             raise ArgumentError(f"Σ_init must have size (nω, n_i, nT) = {(M.nw, M.ni, nT)}, got {np.shape(sigma_init)}")
         sinit = None if sigma_init is None else as_complex_F(sigma_init, (M.nw, M.ni, nT))
         out = Scgd0Outputs(M.nw, M.ni, nT, maxiter)
+        if warm is not None:
+            if sinit is not None:
+                raise ArgumentError("Σ_init and a warm start are exclusive")
+            scale = np.ascontiguousarray(np.broadcast_to(coupling_scale, (nT,)), dtype=np.float64)
+            it, fb = C.c_int32(), C.c_int32()
+            self.ctx.check(lib().epsp_scgd0_run_warm(self.handle, warm.handle, ptr(scale), C.byref(O.struct),
+                                                     ptr(eta_min), float(eta_init), int(maxiter), float(tol),
+                                                     int(bool(fix_mu)), ptr(mu0), out.sigma_ptr(), ptr(out.mu),
+                                                     out.converged.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                                     C.byref(out.hist), C.byref(it), C.byref(fb)))
+            r = out.result()
+            r["iters_total"], r["fallback"] = int(it.value), bool(fb.value)
+            return r
         self.ctx.check(lib().epsp_scgd0_run(self.handle, C.byref(O.struct), ptr(eta_min), float(eta_init),
                                             int(maxiter), float(tol), int(bool(fix_mu)), ptr(mu0), cptr(sinit),
                                             out.sigma_ptr(), ptr(out.mu),

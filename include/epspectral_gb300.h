@@ -147,6 +147,7 @@ typedef struct epsp_ladder_history {
 typedef struct epsp_ctx epsp_ctx;
 typedef struct epsp_scgd0_plan epsp_scgd0_plan;
 typedef struct epsp_ladder_plan epsp_ladder_plan;
+typedef struct epsp_warmstart epsp_warmstart;
 
 /* ---- context ---- */
 
@@ -237,6 +238,48 @@ epsp_status epsp_ladder_run(epsp_ladder_plan* plan, const double* sigma, const d
  * (src/ladder_kernel.jl:51-57). J, LJ: [nω, 4, 3, 2, ni] complex. */
 epsp_status epsp_ladder_apply(epsp_ladder_plan* plan, const double* sigma_T, double mu, double T,
                               double Omega, const double* J, double* LJ);
+
+/* ---- learned warm start (no counterpart in the reference) ----
+ *
+ * A multilayer perceptron that proposes Σ_init for epsp_scgd0_run (the `Σ_init` keyword of
+ * run_scgd0, src/scgd0.jl:66 and 204-212); the iteration's own tol check judges the start, so the
+ * converged result does not depend on it. Layers d_0 -> d_1 -> ... -> d_L, fully connected, SiLU
+ * between layers, linear output; weights used in BF16 with FP32 accumulation, FP32 master copy
+ * and Adam moments on the device. Parameters as one flat FP32 vector: per layer W [d_{l+1}][d_l]
+ * row-major, then b [d_{l+1}]. X [n][d_0] and Y [n][d_L] are row-major host arrays. */
+epsp_status epsp_warmstart_create(epsp_ctx* ctx, int32_t nlayers, const int32_t* dims, epsp_warmstart** net);
+void epsp_warmstart_destroy(epsp_warmstart* net);
+int64_t epsp_warmstart_nparams(const epsp_warmstart* net);
+/* Setting the parameters resets the optimiser state. */
+epsp_status epsp_warmstart_set_params(epsp_warmstart* net, const float* params);
+epsp_status epsp_warmstart_get_params(epsp_warmstart* net, float* params);
+epsp_status epsp_warmstart_predict(epsp_warmstart* net, const float* X, int64_t n, float* Y);
+/* Mean squared error over the batch and all outputs, and its gradient (flat, as the parameters). */
+epsp_status epsp_warmstart_grad(epsp_warmstart* net, const float* X, const float* Y, int64_t n, double* loss,
+                                float* grad);
+/* Standardisation for the in-iteration use: network inputs (x - x_mean) / x_std [d_0], outputs
+ * y * y_scale + y_mean [d_L]. */
+epsp_status epsp_warmstart_set_scaling(epsp_warmstart* net, const float* x_mean, const float* x_std,
+                                       const float* y_mean, float y_scale);
+/* `epochs` passes of Adam (lr, beta 0.9 / 0.999, eps 1e-8) over minibatches of `batch` rows taken in
+ * the order perm [epochs][n] (NULL: identity); loss_history [epochs] (may be NULL) gets each
+ * epoch's mean training loss. */
+epsp_status epsp_warmstart_train(epsp_warmstart* net, const float* X, const float* Y, int64_t n, int32_t epochs,
+                                 int32_t batch, float lr, const int64_t* perm, double* loss_history);
+
+/* epsp_scgd0_run started from the network's Σ_init, with the reference's plain start as fallback.
+ * Iteration 1 runs from -i*eta_init (the G0D0 self-energy); the network (widths [2 nω + 4, ...,
+ * 2 nω], standardisation set) then maps, per outer state i and temperature, the features
+ * [Re Σ(ω_j), Im Σ(ω_j) for all ωs; T, μ, coupling_scale[iT], ε_i - μ] to a correction added to Σ
+ * on the device, and the iteration continues from there with the reference's own tol check. If a
+ * temperature has not converged after maxiter iterations in all, the plain run from -i*eta_init
+ * (epsp_scgd0_run without sigma_init) is made and its outputs returned, with *fallback = 1.
+ * *iters_total counts every iteration made. Other arguments and outputs as epsp_scgd0_run. */
+epsp_status epsp_scgd0_run_warm(epsp_scgd0_plan* plan, epsp_warmstart* net, const double* coupling_scale,
+                                const epsp_occ* occ, const double* eta_min, double eta_init, int32_t maxiter,
+                                double tol, int32_t fix_mu, const double* mu_start, double* sigma_out,
+                                double* mu_out, uint8_t* converged, epsp_scgd0_history* hist,
+                                int32_t* iters_total, int32_t* fallback);
 
 #ifdef __cplusplus
 }
