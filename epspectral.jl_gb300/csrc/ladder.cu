@@ -393,9 +393,9 @@ __global__ void xgen_f64_kernel(const double2* __restrict__ J, const int32_t* __
 // of one row group (q, c0, re/im), nwp being a multiple of 32) and kXgTiles K-tiles of 64 columns
 // (4 pairs (b, i') x 16 modes). Per K-tile it stages the window of the vertex the shift tables of
 // its nodes can reach (nodes j0 - W .. j0 + 32 + W, W = nshift + 2, zero outside the grid) in
-// shared memory; the mode tables mt (two shift tables per mode and sign, with the tent weights
-// folded in) are staged once per block. The tile is transposed through shared memory so that the
-// BF16 rows are written 16 bytes at a time.
+// shared memory; each thread holds the mode-table entries it needs (two shift tables per mode and
+// sign, with the tent weights folded in) in registers. The tile is transposed through shared
+// memory so that the BF16 rows are written 16 bytes at a time.
 constexpr int kXgTiles = 8;
 
 __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restrict__ J, const int32_t* __restrict__ mt_k,
@@ -404,25 +404,33 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
                                                         __nv_bfloat16* __restrict__ Ah, __nv_bfloat16* __restrict__ Al) {
   extern __shared__ float xg_smem[];
   const int W = ns + 2, win = 32 + 2 * W;
-  float* s_w = xg_smem;                                   // [32][16][2][4]
-  int* s_k = reinterpret_cast<int*>(s_w + 32 * 16 * 2 * 4); // [32][16][2][2]
-  float* s_j = reinterpret_cast<float*>(s_k + 32 * 16 * 2 * 2);  // [4][win]
+  float* s_j = xg_smem;                                                 // [4][win]
   float (*tile)[33] = reinterpret_cast<float (*)[33]>(s_j + 4 * win);  // [64][33]
   const long r0 = long(blockIdx.x) * 32;
   const int rr = int(r0 / nwp), j0 = int(r0 % nwp);
   const int q = rr % 6, c0 = (rr / 6) % 2, ri = rr / 12;
   const int c12 = (q < 2) ? 0 : (q < 4 ? 3 : (q == 4 ? 1 : 2));
-  // mode tables of the block's nodes, stored node-fastest ([(ν, s, t)][32 nodes]) so that the 32
-  // lanes of a warp, which hold 32 consecutive nodes, read consecutive words
-  for (int e = threadIdx.x; e < 32 * 16 * 2; e += 256) {
-    const int jj = e / 32, rest = e % 32;  // rest = (nu, s)
-    const long g = (long(j0 + jj) * nmp) * 2 + rest;  // [j][nu][s] with nmp == 16 per K-group
-    const bool ok = j0 + jj < nwp;
-    for (int t = 0; t < 4; ++t) s_w[(rest * 4 + t) * 32 + jj] = ok ? mt_w[g * 4 + t] : 0.f;
-    for (int t = 0; t < 2; ++t) s_k[(rest * 2 + t) * 32 + jj] = ok ? mt_k[g * 2 + t] : 0;
-  }
+  // Thread (tr, tk) makes node j = j0 + tr for the K columns tk + 8p (p = 0..7) of each K-tile:
+  // modes ν = tk and tk + 8 only, so their two shift-table entries (first nodes, weights) and n_B
+  // stay in registers for the whole block; per element only the vertex window is read from
+  // shared memory.
   const int tr = threadIdx.x % 32, tk = threadIdx.x / 32;
   const int j = j0 + tr;
+  int ka[2][2], kb[2][2];
+  float w[2][2][4], nB[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int nu = tk + 8 * h;
+    nB[h] = nnu[nu];
+#pragma unroll
+    for (int sg = 0; sg < 2; ++sg) {
+      const long g = (long(j < nwp ? j : 0) * nmp + nu) * 2 + sg;  // [j][nu][s] with nmp == 16 per K-group
+      ka[h][sg] = mt_k[g * 2] - (j0 - W);
+      kb[h][sg] = mt_k[g * 2 + 1] - (j0 - W);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) w[h][sg][t] = j < nwp ? mt_w[g * 4 + t] : 0.f;
+    }
+  }
   const long kt0 = long(blockIdx.y) * kXgTiles;
   for (int kt = 0; kt < kXgTiles; ++kt) {
     const long k0 = (kt0 + kt) * 64;
@@ -442,23 +450,20 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
       s_j[e] = v;
     }
     __syncthreads();
-#pragma unroll 1
+#pragma unroll
     for (int p = 0; p < 8; ++p) {
-      const int kl = tk + 8 * p;           // 0..63
-      const int g = kl / 16, nu = kl % 16;
+      const int h = p & 1, g = p >> 1;
+      const int kl = tk + 8 * p;  // 0..63: pair g, mode tk + 8 h
       const long k = k0 + kl;
       float v = 0.f;
       if (j < nw && k < Kx) {
-        const float* jw = s_j + g * win - (j0 - W);
+        const float* jw = s_j + g * win;
         float xs[2];
 #pragma unroll
-        for (int sg = 0; sg < 2; ++sg) {
-          const int rest = nu * 2 + sg;
-          const int ka = s_k[(rest * 2) * 32 + tr], kb = s_k[(rest * 2 + 1) * 32 + tr];
-          const float* w4 = s_w + (rest * 4) * 32 + tr;
-          xs[sg] = w4[0] * jw[ka] + w4[32] * jw[ka + 1] + w4[64] * jw[kb] + w4[96] * jw[kb + 1];
-        }
-        const float n = nnu[nu];
+        for (int sg = 0; sg < 2; ++sg)
+          xs[sg] = w[h][sg][0] * jw[ka[h][sg]] + w[h][sg][1] * jw[ka[h][sg] + 1] + w[h][sg][2] * jw[kb[h][sg]] +
+                   w[h][sg][3] * jw[kb[h][sg] + 1];
+        const float n = nB[h];
         switch (q) {
           case 0:
           case 2: v = 0.5f * (xs[0] - xs[1]); break;
@@ -487,7 +492,7 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
 
 static size_t xgen_smem_bytes(int ns) {
   const int W = ns + 2, win = 32 + 2 * W;
-  return size_t(32 * 16 * 2 * 4) * 4 + size_t(32 * 16 * 2 * 2) * 4 + size_t(4 * win) * 4 + size_t(64 * 33) * 4;
+  return size_t(4 * win) * 4 + size_t(64 * 33) * 4;
 }
 
 // Y (rows q = 0, 2 of D) as the BF16 hi/lo B operand of the Kramers-Kronig GEMM: row (qq, c0, ri, n),
@@ -551,6 +556,22 @@ __global__ void y_gemm_kernel(const double* __restrict__ D, int nw, int nwp, lon
   Y[idx] = D[w + long(nwp) * (q + 6 * (c0 + 2 * ri)) + 24l * nwp * n];
 }
 
+// Complex arithmetic in R (double for the FP64 path; float for the BF16 path, whose products carry
+// ~1e-5 relative error already and where FP64 would make this kernel compute-bound).
+template <class R>
+struct Cx {
+  R x, y;
+};
+template <class R>
+__device__ __forceinline__ Cx<R> cxmul(Cx<R> a, Cx<R> b) {
+  return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+template <class R>
+__device__ __forceinline__ Cx<R> cxadd(Cx<R> a, Cx<R> b) {
+  return {a.x + b.x, a.y + b.y};
+}
+
+template <class R>
 __global__ void finish_gemm_kernel(const double* __restrict__ D, const double* __restrict__ KY, const double2* __restrict__ Gm,
                                    const double2* __restrict__ Gp, int nw, int nwp, int ni, double2* __restrict__ LJ) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -560,26 +581,33 @@ __global__ void finish_gemm_kernel(const double* __restrict__ D, const double* _
   int a = int(r % 3), c0 = int((r / 3) % 2);
   long i = r / 6;
   const long n = a + 3 * i;
-  auto d = [&](int q, int ri) { return D[w + long(nwp) * (q + 6 * (c0 + 2 * ri)) + 24l * nwp * n]; };
-  auto ky = [&](int qq, int ri) { return KY[w + nw * (qq + 2 * (c0 + 2 * (ri + 2 * n)))]; };
-  double2 K[4];
+  auto d = [&](int q, int ri) { return R(D[w + long(nwp) * (q + 6 * (c0 + 2 * ri)) + 24l * nwp * n]); };
+  auto ky = [&](int qq, int ri) { return R(KY[w + nw * (qq + 2 * (c0 + 2 * (ri + 2 * n)))]); };
+  Cx<R> K[4];
   {
-    double2 y0 = make_double2(ky(0, 0), ky(0, 1));
-    K[0] = make_double2(y0.y + d(1, 0), -y0.x + d(1, 1));      // -i KY + rest
-    double2 y3 = make_double2(ky(1, 0), ky(1, 1));
-    K[3] = make_double2(-y3.y + d(3, 0), y3.x + d(3, 1));      // +i KY + rest
-    K[1] = make_double2(d(4, 0), d(4, 1));
-    K[2] = make_double2(d(5, 0), d(5, 1));
+    const Cx<R> y0{ky(0, 0), ky(0, 1)};
+    K[0] = {y0.y + d(1, 0), -y0.x + d(1, 1)};  // -i KY + rest
+    const Cx<R> y3{ky(1, 0), ky(1, 1)};
+    K[3] = {-y3.y + d(3, 0), y3.x + d(3, 1)};  // +i KY + rest
+    K[1] = {d(4, 0), d(4, 1)};
+    K[2] = {d(5, 0), d(5, 1)};
   }
+  Cx<R> gm[4], gp[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const double2 a = Gm[w + long(nw) * (c + 4 * i)], b = Gp[w + long(nw) * (c + 4 * i)];
+    gm[c] = {R(a.x), R(a.y)};
+    gp[c] = {R(b.x), R(b.y)};
+  }
+#pragma unroll
   for (int c1 = 0; c1 < 2; ++c1)
+#pragma unroll
     for (int c2 = 0; c2 < 2; ++c2) {
-      auto gm = [&](int c) { return Gm[w + long(nw) * (c + 4 * i)]; };
-      auto gp = [&](int c) { return Gp[w + long(nw) * (c + 4 * i)]; };
-      double2 z = cmul(cmul(gm(c1), K[0]), gp(0 + 2 * c2));
-      z = cadd(z, cmul(cmul(gm(c1 + 2), K[1]), gp(0 + 2 * c2)));
-      z = cadd(z, cmul(cmul(gm(c1), K[2]), gp(1 + 2 * c2)));
-      z = cadd(z, cmul(cmul(gm(c1 + 2), K[3]), gp(1 + 2 * c2)));
-      LJ[jidx(nw, w, c1 + 2 * c2, a, c0, i)] = make_double2(-z.x, -z.y);
+      Cx<R> z = cxmul(cxmul(gm[c1], K[0]), gp[0 + 2 * c2]);
+      z = cxadd(z, cxmul(cxmul(gm[c1 + 2], K[1]), gp[0 + 2 * c2]));
+      z = cxadd(z, cxmul(cxmul(gm[c1], K[2]), gp[1 + 2 * c2]));
+      z = cxadd(z, cxmul(cxmul(gm[c1 + 2], K[3]), gp[1 + 2 * c2]));
+      LJ[jidx(nw, w, c1 + 2 * c2, a, c0, i)] = make_double2(-double(z.x), -double(z.y));
     }
 }
 
@@ -1082,8 +1110,12 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ) {
     sum_parts_kernel<<<div_up(size_t(nw * 8 * N), 256), 256, 0, s>>>(P->d_part2.p, nw * 8 * N, sp2, nw * 8 * N, P->d_KY.p);
     EPSP_LAUNCHED(ctx);
   }
-  finish_gemm_kernel<<<div_up(size_t(nw * 6 * ni), 256), 256, 0, s>>>(P->d_D.p, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, int(nw), int(nwp),
-                                                                     int(ni), LJ);
+  if (P->path == EPSP_PATH_GEMM_BF16)
+    finish_gemm_kernel<float><<<div_up(size_t(nw * 6 * ni), 256), 256, 0, s>>>(P->d_D.p, P->d_KY.p, P->d_Gm.p, P->d_Gp.p,
+                                                                              int(nw), int(nwp), int(ni), LJ);
+  else
+    finish_gemm_kernel<double><<<div_up(size_t(nw * 6 * ni), 256), 256, 0, s>>>(P->d_D.p, P->d_KY.p, P->d_Gm.p, P->d_Gp.p,
+                                                                               int(nw), int(nwp), int(ni), LJ);
   EPSP_LAUNCHED(ctx);
 }
 

@@ -253,6 +253,19 @@ __device__ __forceinline__ double imag_inv_d(double c, double d) {
 
 // Spectral functions on ωs_spectral (src/scgd0.jl:303-305): A[a, i] = -Im(1/(ωa - ε_i -
 // Σ(ωa)))/π with Σ read by the table (j_sp, t_sp) (apply_interpolation_table!).
+__device__ __forceinline__ float imag_inv_f(float c, float d) {
+  if (fabsf(d) <= fabsf(c)) {
+    const float r = d / c;
+    return -r * (1.f / (c + d * r));
+  }
+  const float r = c / d;
+  return -(1.f / (d + c * r));
+}
+
+// F32: the interpolation and the cancelling difference ωa - ε_i - Re Σ stay FP64, the reciprocal
+// is FP32 (the tensor-core path, whose Σ carries ~1e-6 eV already; FP64 division would make the
+// kernel compute-bound on the FP64 units).
+template <bool F32>
 __global__ void spectral_A_kernel(const double2* __restrict__ S, int nw, const double* __restrict__ wsa, int nwa,
                                   const int32_t* __restrict__ jsp, const double* __restrict__ tsp,
                                   const double* __restrict__ eps_i, double* __restrict__ A) {
@@ -265,7 +278,11 @@ __global__ void spectral_A_kernel(const double2* __restrict__ S, int nw, const d
   double2 lo = col[j], hi = col[j + 1];
   double sr = (1 - t) * lo.x + t * hi.x;
   double si = (1 - t) * lo.y + t * hi.y;
-  A[a + long(nwa) * i] = -imag_inv_d(wsa[a] - eps_i[i] - sr, -si) / 3.14159265358979323846;
+  const double c = wsa[a] - eps_i[i] - sr;
+  if constexpr (F32)
+    A[a + long(nwa) * i] = double(-imag_inv_f(float(c), float(-si)) * 0.318309886183790671538f);
+  else
+    A[a + long(nwa) * i] = -imag_inv_d(c, -si) / 3.14159265358979323846;
 }
 
 // Fixed-order block reduction helpers (deterministic for a fixed block size).
@@ -294,14 +311,26 @@ __global__ void __launch_bounds__(256) spectral_colsum_kernel(const double* __re
   if (threadIdx.x == 0) colsum[i] = r;
 }
 
-// D[a] = (Σ_i A[a, i] w_i) Wa[a] (src/scgd0.jl:306-307).
-__global__ void spectral_D_kernel(const double* __restrict__ A, int nwa, int ni, const double* __restrict__ w_i,
-                                  const double* __restrict__ Wa, double* __restrict__ D) {
-  int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= nwa) return;
+// D[a] = (Σ_i A[a, i] w_i) Wa[a] (src/scgd0.jl:306-307). A block of 256 threads covers 32 nodes a
+// (the lanes) and splits i over its 8 warps (i ≡ warp mod 8, ascending); the 8 partial sums are
+// added in warp order, so the result is deterministic.
+__global__ void __launch_bounds__(256) spectral_D_kernel(const double* __restrict__ A, int nwa, int ni,
+                                                         const double* __restrict__ w_i, const double* __restrict__ Wa,
+                                                         double* __restrict__ D) {
+  __shared__ double sh[8][32];
+  const int lane = threadIdx.x % 32, g = threadIdx.x / 32;
+  const int a = blockIdx.x * 32 + lane;
   double s = 0;
-  for (int i = 0; i < ni; ++i) s += A[a + long(nwa) * i] * w_i[i];
-  D[a] = s * Wa[a];
+  if (a < nwa)
+    for (int i = g; i < ni; i += 8) s += A[a + long(nwa) * i] * w_i[i];
+  sh[g][lane] = s;
+  __syncthreads();
+  if (g == 0 && a < nwa) {
+    double t = sh[0][lane];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) t += sh[k][lane];
+    D[a] = t * Wa[a];
+  }
 }
 
 __global__ void __launch_bounds__(256) min_kernel(const double* __restrict__ x, int n, double* __restrict__ out) {
@@ -840,7 +869,8 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
       const double T = occ->Tlist[iT];
       double2* ST = S.p + slab * iT;
       double2* SnT = Snew.p + slab * iT;
-      spectral_A_kernel<<<dim3(div_up(size_t(nwa), 256), unsigned(ni)), 256, 0, s>>>(SnT, int(nw), P->d_wsa.p, int(nwa), P->d_jsp.p,
+      auto spectral_A = P->path == EPSP_PATH_GEMM_BF16 ? spectral_A_kernel<true> : spectral_A_kernel<false>;
+      spectral_A<<<dim3(div_up(size_t(nwa), 256), unsigned(ni)), 256, 0, s>>>(SnT, int(nw), P->d_wsa.p, int(nwa), P->d_jsp.p,
                                                                                     P->d_tsp.p, P->d_eps_i.p, P->d_A.p);
       EPSP_LAUNCHED(ctx);
       spectral_colsum_kernel<<<unsigned(ni), 256, 0, s>>>(P->d_A.p, int(nwa), P->d_Wa.p, P->d_colsum.p);
@@ -848,7 +878,7 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
       min_kernel<<<1, 256, 0, s>>>(P->d_colsum.p, int(ni), d_minA.p + iT);
       EPSP_LAUNCHED(ctx);
       if (!fix_mu) {
-        spectral_D_kernel<<<div_up(size_t(nwa), 256), 256, 0, s>>>(P->d_A.p, int(nwa), int(ni), P->d_w_i.p, P->d_Wa.p, P->d_D.p);
+        spectral_D_kernel<<<div_up(size_t(nwa), 32), 256, 0, s>>>(P->d_A.p, int(nwa), int(ni), P->d_w_i.p, P->d_Wa.p, P->d_D.p);
         EPSP_LAUNCHED(ctx);
         bool holes = occ->type == EPSP_SEMICONDUCTOR && occ->nlist[iT] < 0;
         double n_target = occ->nlist[iT] + occ->nelec;

@@ -61,7 +61,7 @@ static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int 
     maps.a[p] = A.m[p < NS ? p : 0];
     maps.b[p] = B.m[p < NS ? p : 0];
   }
-  dim3 grid((M + kTcBM - 1) / kTcBM, (N + BN - 1) / BN, splits);
+  dim3 grid((N + BN - 1) / BN, (M + kTcBM - 1) / kTcBM, splits);
   tc_gemm_split_kernel<BN, STAGES, NS><<<grid, 128, L::kBytes, ctx->stream>>>(maps, M, N, kblocks, per, out, ld_out,
                                                                               split_stride, d_err);
   EPSP_LAUNCHED(ctx);

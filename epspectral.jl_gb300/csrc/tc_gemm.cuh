@@ -126,7 +126,9 @@ __global__ void __launch_bounds__(128, 1)
   __shared__ int s_abort;
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES), done_bar = smem_u32(bars + 2 * STAGES);
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * BN;
+  // N tiles vary fastest over the launch order, so the CTAs resident together share A tiles
+  // (the large operand) through L2 and A streams from DRAM about once
+  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * kTcBM;
   const int kb0 = blockIdx.z * kb_per_split;
   const int nkb = max(0, min(kblocks, kb0 + kb_per_split) - kb0);
 
