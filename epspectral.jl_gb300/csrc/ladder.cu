@@ -389,13 +389,16 @@ __global__ void xgen_f64_kernel(const double2* __restrict__ J, const int32_t* __
   A[idx] = (j < nw && nu < nm) ? xgen_value(J, klo, wlo, whi, nw, ns, j, q, c0, ri, mnu[nu], rnu[nu], nnu[nu], b, ip) : 0.0;
 }
 
-// BF16 hi/lo A operand, row-major [24 nwp][Kp], FP32 arithmetic. A block owns 32 rows (32 nodes j
-// of one row group (q, c0, re/im), nwp being a multiple of 32) and kXgTiles K-tiles of 64 columns
-// (4 pairs (b, i') x 16 modes). Per K-tile it stages the window of the vertex the shift tables of
-// its nodes can reach (nodes j0 - W .. j0 + 32 + W, W = nshift + 2, zero outside the grid) in
-// shared memory; each thread holds the mode-table entries it needs (two shift tables per mode and
-// sign, with the tent weights folded in) in registers. The tile is transposed through shared
-// memory so that the BF16 rows are written 16 bytes at a time.
+// BF16 hi/lo A operand, row-major [24 nwp][Kp], FP32 arithmetic; row (q, c0, re/im) nwp + j. The
+// six row combinations q read four vertex components c12 (q 0, 1: 11; q 2, 3: 22; q 4: 21; q 5:
+// 12), so a block owns 32 nodes j (nwp is a multiple of 32) of one component (c12, c0) and makes
+// every row group that reads it: both q of the component and both re/im parts (4 or 2 row groups)
+// from one staged copy of the vertex and one evaluation of the shifted sums X+, X-. Per K-tile (64
+// columns = 4 pairs (b, i') x 16 modes) it stages the window of the vertex the shift tables of its
+// nodes can reach (nodes j0 - W .. j0 + 32 + W, W = nshift + 2, zero outside the grid) in shared
+// memory; each thread holds the mode-table entries it needs (two shift tables per mode and sign,
+// with the tent weights folded in) in registers. Tiles are transposed through shared memory so
+// that the BF16 rows are written 16 bytes at a time.
 constexpr int kXgTiles = 8;
 
 __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restrict__ J, const int32_t* __restrict__ mt_k,
@@ -404,16 +407,14 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
                                                         __nv_bfloat16* __restrict__ Ah, __nv_bfloat16* __restrict__ Al) {
   extern __shared__ float xg_smem[];
   const int W = ns + 2, win = 32 + 2 * W;
-  float* s_j = xg_smem;                                                 // [4][win]
-  float (*tile)[33] = reinterpret_cast<float (*)[33]>(s_j + 4 * win);  // [64][33]
-  const long r0 = long(blockIdx.x) * 32;
-  const int rr = int(r0 / nwp), j0 = int(r0 % nwp);
-  const int q = rr % 6, c0 = (rr / 6) % 2, ri = rr / 12;
-  const int c12 = (q < 2) ? 0 : (q < 4 ? 3 : (q == 4 ? 1 : 2));
-  // Thread (tr, tk) makes node j = j0 + tr for the K columns tk + 8p (p = 0..7) of each K-tile:
-  // modes ν = tk and tk + 8 only, so their two shift-table entries (first nodes, weights) and n_B
-  // stay in registers for the whole block; per element only the vertex window is read from
-  // shared memory.
+  float2* s_j = reinterpret_cast<float2*>(xg_smem);                               // [4][win] (re, im)
+  float (*tile)[64][33] = reinterpret_cast<float (*)[64][33]>(s_j + 4 * win);    // [4][64][33]
+  const int nblk = nwp / 32;
+  const int j0 = (blockIdx.x % nblk) * 32, comp = blockIdx.x / nblk;
+  const int cc = comp % 4, c0 = comp / 4;
+  const int c12 = cc == 0 ? 0 : (cc == 1 ? 3 : (cc == 2 ? 1 : 2));
+  const int nq = cc < 2 ? 2 : 1;            // row combinations q reading this component
+  const int qbase = cc < 2 ? 2 * cc : cc + 2;  // 0, 2, 4, 5
   const int tr = threadIdx.x % 32, tk = threadIdx.x / 32;
   const int j = j0 + tr;
   int ka[2][2], kb[2][2];
@@ -424,11 +425,11 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
     nB[h] = nnu[nu];
 #pragma unroll
     for (int sg = 0; sg < 2; ++sg) {
-      const long g = (long(j < nwp ? j : 0) * nmp + nu) * 2 + sg;  // [j][nu][s] with nmp == 16 per K-group
+      const long g = (long(j) * nmp + nu) * 2 + sg;  // [j][nu][s] with nmp == 16 per K-group
       ka[h][sg] = mt_k[g * 2] - (j0 - W);
       kb[h][sg] = mt_k[g * 2 + 1] - (j0 - W);
 #pragma unroll
-      for (int t = 0; t < 4; ++t) w[h][sg][t] = j < nwp ? mt_w[g * 4 + t] : 0.f;
+      for (int t = 0; t < 4; ++t) w[h][sg][t] = mt_w[g * 4 + t];
     }
   }
   const long kt0 = long(blockIdx.y) * kXgTiles;
@@ -440,12 +441,12 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
     for (int e = threadIdx.x; e < 4 * win; e += 256) {
       const int g = e / win, node = j0 - W + e % win;
       const long pair = (k0 / 16) + g;  // (b, i') index = k / 16
-      float v = 0.f;
+      float2 v = make_float2(0.f, 0.f);
       if (node >= 0 && node < nw && pair < 3l * ni) {
         const int b = int(pair % 3);
         const long ip = pair / 3;
         const double2 z = J[jidx(nw, node, c12, b, c0, ip)];
-        v = float(ri == 0 ? z.x : z.y);
+        v = make_float2(float(z.x), float(z.y));
       }
       s_j[e] = v;
     }
@@ -455,44 +456,53 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
       const int h = p & 1, g = p >> 1;
       const int kl = tk + 8 * p;  // 0..63: pair g, mode tk + 8 h
       const long k = k0 + kl;
-      float v = 0.f;
+      float2 xs[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
       if (j < nw && k < Kx) {
-        const float* jw = s_j + g * win;
-        float xs[2];
+        const float2* jw = s_j + g * win;
 #pragma unroll
-        for (int sg = 0; sg < 2; ++sg)
-          xs[sg] = w[h][sg][0] * jw[ka[h][sg]] + w[h][sg][1] * jw[ka[h][sg] + 1] + w[h][sg][2] * jw[kb[h][sg]] +
-                   w[h][sg][3] * jw[kb[h][sg] + 1];
-        const float n = nB[h];
-        switch (q) {
-          case 0:
-          case 2: v = 0.5f * (xs[0] - xs[1]); break;
-          case 1:
-          case 3: v = -(0.5f + n) * (xs[0] + xs[1]); break;
-          case 4: v = n * xs[0] + (1.f + n) * xs[1]; break;
-          default: v = (1.f + n) * xs[0] + n * xs[1]; break;
+        for (int sg = 0; sg < 2; ++sg) {
+          const float2 u0 = jw[ka[h][sg]], u1 = jw[ka[h][sg] + 1], u2 = jw[kb[h][sg]], u3 = jw[kb[h][sg] + 1];
+          xs[sg].x = w[h][sg][0] * u0.x + w[h][sg][1] * u1.x + w[h][sg][2] * u2.x + w[h][sg][3] * u3.x;
+          xs[sg].y = w[h][sg][0] * u0.y + w[h][sg][1] * u1.y + w[h][sg][2] * u2.y + w[h][sg][3] * u3.y;
         }
       }
-      tile[kl][tr] = v;
+      const float n = nB[h];
+      if (cc < 2) {
+        // q even: ½(X+ - X-); q odd: -(½ + n)(X+ + X-)
+        tile[0][kl][tr] = 0.5f * (xs[0].x - xs[1].x);
+        tile[1][kl][tr] = 0.5f * (xs[0].y - xs[1].y);
+        tile[2][kl][tr] = -(0.5f + n) * (xs[0].x + xs[1].x);
+        tile[3][kl][tr] = -(0.5f + n) * (xs[0].y + xs[1].y);
+      } else if (cc == 2) {
+        tile[0][kl][tr] = n * xs[0].x + (1.f + n) * xs[1].x;
+        tile[1][kl][tr] = n * xs[0].y + (1.f + n) * xs[1].y;
+      } else {
+        tile[0][kl][tr] = (1.f + n) * xs[0].x + n * xs[1].x;
+        tile[1][kl][tr] = (1.f + n) * xs[0].y + n * xs[1].y;
+      }
     }
     __syncthreads();
     const int wr = threadIdx.x / 8, kc = (threadIdx.x % 8) * 8;
-    __align__(16) __nv_bfloat16 hh[8], ll[8];
+    for (int t4 = 0; t4 < 2 * nq; ++t4) {
+      const int q = qbase + t4 / 2, ri = t4 % 2;
+      __align__(16) __nv_bfloat16 hh[8], ll[8];
 #pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      const float x = tile[kc + t][wr];
-      hh[t] = __float2bfloat16_rn(x);
-      ll[t] = __float2bfloat16_rn(x - __bfloat162float(hh[t]));
+      for (int t = 0; t < 8; ++t) {
+        const float x = tile[t4][kc + t][wr];
+        hh[t] = __float2bfloat16_rn(x);
+        ll[t] = __float2bfloat16_rn(x - __bfloat162float(hh[t]));
+      }
+      const long row = long(q + 6 * (c0 + 2 * ri)) * nwp + j0 + wr;
+      const long off = row * Kp + k0 + kc;
+      *reinterpret_cast<uint4*>(Ah + off) = *reinterpret_cast<const uint4*>(hh);
+      *reinterpret_cast<uint4*>(Al + off) = *reinterpret_cast<const uint4*>(ll);
     }
-    const long off = (r0 + wr) * Kp + k0 + kc;
-    *reinterpret_cast<uint4*>(Ah + off) = *reinterpret_cast<const uint4*>(hh);
-    *reinterpret_cast<uint4*>(Al + off) = *reinterpret_cast<const uint4*>(ll);
   }
 }
 
 static size_t xgen_smem_bytes(int ns) {
   const int W = ns + 2, win = 32 + 2 * W;
-  return size_t(4 * win) * 4 + size_t(64 * 33) * 4;
+  return size_t(4 * win) * sizeof(float2) + size_t(4 * 64 * 33) * 4;
 }
 
 // Y (rows q = 0, 2 of D) as the BF16 hi/lo B operand of the Kramers-Kronig GEMM: row (qq, c0, ri, n),
@@ -1095,7 +1105,7 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ) {
   } else {
     long px = prof_begin(ctx, "xgen");
     const unsigned ktiles = unsigned((P->Kp / 64 + kXgTiles - 1) / kXgTiles);
-    xgen_bf16_kernel<<<dim3(unsigned(M / 32), ktiles), 256, xgen_smem_bytes(int(ns)), s>>>(
+    xgen_bf16_kernel<<<dim3(unsigned(nwp / 32 * 8), ktiles), 256, xgen_smem_bytes(int(ns)), s>>>(
         J, P->d_mt_k.p, P->d_mt_w.p, P->d_nnu_f.p, int(nw), int(nwp), int(ns), int(P->nmp), int(ni), P->Kx, P->Kp, P->d_Ah.p,
         P->d_Al.p);
     EPSP_LAUNCHED(ctx);

@@ -365,9 +365,21 @@ __device__ __forceinline__ double float_middle_d(double x, double y) {
 // One cluster of kMuCluster CTAs per temperature: each CTA sums a slice of ωs_spectral in fixed
 // order, the partials are combined through distributed shared memory in rank order, so every
 // thread of the cluster holds the same totals and takes the same branches.
+// The first round evaluates n at both bracket ends and at the start x0 together. Every CTA keeps
+// E_a = exp((ωa - x0)/T) of its slice in shared memory, so that near x0 the occupations cost one
+// product and one division: exp((ωa - μ)/T) = E_a exp((x0 - μ)/T) (used while |μ - x0| <= 30 T;
+// farther out, and at T ~ 0, exp is evaluated directly).
 // status: 0 ok, 1 no sign change on the bracket.
 constexpr int kMuCluster = 8;
 constexpr int kMuThreads = 512;
+constexpr int kMuWarps = kMuThreads / 32;
+constexpr int kMuTableMax = 16384;  // slice length up to which E is tabulated (128 KiB)
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
 
 __global__ void __cluster_dims__(kMuCluster, 1, 1) __launch_bounds__(kMuThreads)
     mu_solve_kernel(const double* __restrict__ D, const double* __restrict__ wsa, int nwa, double T, double W,
@@ -376,45 +388,67 @@ __global__ void __cluster_dims__(kMuCluster, 1, 1) __launch_bounds__(kMuThreads)
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned rank = cluster.block_rank();
-  __shared__ double sh[kMuThreads], sh2[kMuThreads];
-  __shared__ double part[2];
+  extern __shared__ double s_E[];
+  __shared__ double sh[4][kMuWarps];
+  __shared__ double part[4];
   const int chunk = (nwa + kMuCluster - 1) / kMuCluster;
   const int a0 = int(rank) * chunk, a1 = min(nwa, a0 + chunk);
-  auto evaluate = [&](double mu, double& F, double& dF) {
-    double s1 = 0, s2 = 0;
-    for (int a = a0 + int(threadIdx.x); a < a1; a += kMuThreads) {
-      const double f = occ_fermion_d(holes ? mu - wsa[a] : wsa[a] - mu, T);
-      s1 += D[a] * f;
-      s2 += D[a] * (f * (1 - f));
+  const bool warm = T > 1.4901161193847656e-08;
+  const bool table = warm && chunk <= kMuTableMax;
+  const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
+  // fixed-order totals of up to 4 per-thread sums over the cluster
+  auto reduce = [&](double (&v)[4], int nv) {
+    for (int q = 0; q < nv; ++q) {
+      const double w = warp_sum_d(v[q]);
+      if (lane == 0) sh[q][wid] = w;
     }
-    sh[threadIdx.x] = s1;
-    sh2[threadIdx.x] = s2;
     __syncthreads();
-    for (int st = kMuThreads / 2; st > 0; st >>= 1) {
-      if (int(threadIdx.x) < st) {
-        sh[threadIdx.x] += sh[threadIdx.x + st];
-        sh2[threadIdx.x] += sh2[threadIdx.x + st];
-      }
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      part[0] = sh[0];
-      part[1] = sh2[0];
+    if (threadIdx.x < nv) {
+      double t = 0;
+      for (int k = 0; k < kMuWarps; ++k) t += sh[threadIdx.x][k];
+      part[threadIdx.x] = t;
     }
     cluster.sync();
-    double t1 = 0, t2 = 0;
-    for (unsigned r = 0; r < kMuCluster; ++r) {
-      const double* p = cluster.map_shared_rank(part, r);
-      t1 += p[0];
-      t2 += p[1];
+    for (int q = 0; q < nv; ++q) {
+      double t = 0;
+      for (unsigned r = 0; r < kMuCluster; ++r) t += cluster.map_shared_rank(part, r)[q];
+      v[q] = t;
     }
     cluster.sync();
-    F = (holes ? (W - t1 + base) * gs : (t1 + base) * gs) - n_target;
-    dF = T > 1.4901161193847656e-08 ? gs * t2 / T : 0.0;
   };
-  double a = br0, b = br1, fa, fb, dd;
-  evaluate(a, fa, dd);
-  evaluate(b, fb, dd);
+  auto occ = [&](double wa, double mu) { return occ_fermion_d(holes ? mu - wa : wa - mu, T); };
+  auto from_y = [&](double y) {  // the occupation from y = exp((ωa - μ)/T)
+    if (holes) return isinf(y) ? 1.0 : y / (1.0 + y);
+    return 1.0 / (y + 1.0);
+  };
+  auto total = [&](double t1) { return (holes ? (W - t1 + base) * gs : (t1 + base) * gs) - n_target; };
+  double a = br0, b = br1;
+  const double x0 = (guess > a && guess < b) ? guess : float_middle_d(a, b);
+  // round 1: n(a), n(b), n(x0) and n'(x0)
+  double fa, fb, F, dF;
+  {
+    double v[4] = {0, 0, 0, 0};
+    for (int k = a0 + int(threadIdx.x); k < a1; k += kMuThreads) {
+      const double wa = wsa[k], d = D[k];
+      double f0;
+      if (table) {
+        const double E = exp((wa - x0) / T);
+        s_E[k - a0] = E;
+        f0 = from_y(E);
+      } else {
+        f0 = occ(wa, x0);
+      }
+      v[0] += d * occ(wa, a);
+      v[1] += d * occ(wa, b);
+      v[2] += d * f0;
+      v[3] += d * (f0 * (1 - f0));
+    }
+    reduce(v, 4);
+    fa = total(v[0]);
+    fb = total(v[1]);
+    F = total(v[2]);
+    dF = warm ? gs * v[3] / T : 0.0;
+  }
   if (fa * fb > 0) {
     if (rank == 0 && threadIdx.x == 0) *status = 1;
     return;
@@ -425,11 +459,23 @@ __global__ void __cluster_dims__(kMuCluster, 1, 1) __launch_bounds__(kMuThreads)
   } else if (fb == 0) {
     result = b;
   } else {
-    double x = (guess > a && guess < b) ? guess : float_middle_d(a, b);
+    double x = x0;
     result = x;
     for (int it = 0; it < 400; ++it) {
-      double F, dF;
-      evaluate(x, F, dF);
+      if (it > 0) {
+        const double sx = (x0 - x) / T;
+        const bool fact = table && fabs(sx) <= 30.0;
+        const double scale = fact ? exp(sx) : 0.0;
+        double v[4] = {0, 0, 0, 0};
+        for (int k = a0 + int(threadIdx.x); k < a1; k += kMuThreads) {
+          const double f = fact ? from_y(s_E[k - a0] * scale) : occ(wsa[k], x);
+          v[0] += D[k] * f;
+          v[1] += D[k] * (f * (1 - f));
+        }
+        reduce(v, 2);
+        F = total(v[0]);
+        dF = warm ? gs * v[1] / T : 0.0;
+      }
       result = x;
       if (F == 0) break;
       if (signbit(F) == signbit(fa)) {
@@ -456,6 +502,11 @@ __global__ void __cluster_dims__(kMuCluster, 1, 1) __launch_bounds__(kMuThreads)
     *mu_out = result;
     *status = 0;
   }
+}
+
+static size_t mu_smem_bytes(long nwa) {
+  const long chunk = (nwa + kMuCluster - 1) / kMuCluster;
+  return chunk <= kMuTableMax ? size_t(chunk) * sizeof(double) : 0;
 }
 
 // err = max |Σ_new - Σ| over one temperature, and Σ ← Σ_new (src/scgd0.jl:326-328). The maximum of
@@ -822,6 +873,8 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   for (int32_t k = 0; k < maxiter; ++k) hist->wall[k] = 0;
   for (int64_t k = 0; k < nT; ++k) hist->iter_frozen[k] = 0;
   const double br0 = P->wsa.nodes.front() - 0.1, br1 = P->wsa.nodes.back() + 0.1;  // src/scgd0.jl:197
+  if (mu_smem_bytes(nwa) > 48 * 1024)
+    EPSP_CUDA(cudaFuncSetAttribute(mu_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(mu_smem_bytes(nwa))));
   DBuf<unsigned long long> d_err;
   DBuf<double> d_mu, d_minA;
   DBuf<int> d_status;
@@ -883,7 +936,7 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
         bool holes = occ->type == EPSP_SEMICONDUCTOR && occ->nlist[iT] < 0;
         double n_target = occ->nlist[iT] + occ->nelec;
         long pm = prof_begin(ctx, "mu");
-        mu_solve_kernel<<<kMuCluster, kMuThreads, 0, s>>>(P->d_D.p, P->d_wsa.p, int(nwa), T, P->W, P->nstates_base,
+        mu_solve_kernel<<<kMuCluster, kMuThreads, mu_smem_bytes(nwa), s>>>(P->d_D.p, P->d_wsa.p, int(nwa), T, P->W, P->nstates_base,
                                                           occ->spin_degeneracy, n_target, holes ? 1 : 0, br0, br1,
                                                           mu[size_t(iT)], d_mu.p + iT, d_status.p + iT);
         EPSP_LAUNCHED(ctx);

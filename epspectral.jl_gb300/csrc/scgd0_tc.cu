@@ -24,30 +24,78 @@ struct Scgd0Plan::Tc {
   DBuf<float> part;
   DBuf<int> err;
   TcOperand opK, opG, opKK, opIm;
+  // FP32 forms of the K-tensor inputs: cell points as float pairs (hi, lo), cell weights, the cell
+  // energies as pairs, the occupation tables, and per iteration Σin as {Re hi, Re lo, Im, 0}
+  DBuf<float2> xf, ef;
+  DBuf<float> tf, Ff;
+  DBuf<float4> Sf;
 };
+
+__device__ __forceinline__ float2 split_df(double x) {
+  const float h = float(x);
+  return make_float2(h, float(x - double(h)));
+}
+
+__global__ void split_df_kernel(const double* __restrict__ x, long n, float2* __restrict__ out) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = split_df(x[k]);
+}
+
+__global__ void to_f32_kernel(const double* __restrict__ x, long n, float* __restrict__ out) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = float(x[k]);
+}
+
+__global__ void sigma_f32_kernel(const double2* __restrict__ S, long n, float4* __restrict__ out) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double2 z = S[k];
+  const float2 r = split_df(z.x);
+  out[k] = make_float4(r.x, r.y, float(z.y), 0.f);
+}
+
+// s + e = a + b exactly (Knuth's two-sum; additions only, so no contraction into FMA applies).
+__device__ __forceinline__ float two_sum(float a, float b, float& e) {
+  const float s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+  return s;
+}
+
+// Re z = (x - ε) - Re Σ(x) with Re Σ(x) = lo + t (hi - lo): the cancelling part x - ε - lo is
+// evaluated exactly on the float pairs (two two-sums on the high words, the low words added after),
+// the small interpolation step t (hi - lo) in FP32.
+__device__ __forceinline__ float re_z(float2 x, float2 e, float4 lo, float4 hi, float t) {
+  float e1, e2;
+  const float s1 = two_sum(x.x, -e.x, e1);
+  const float s2 = two_sum(s1, -lo.x, e2);
+  const float r = s2 + (e1 + e2 + ((x.y - e.y) - lo.y));
+  const float d = (hi.x - lo.x) + (hi.y - lo.y);
+  return r - t * d;
+}
 
 // Kernel tensor of the recast Fan-Migdal sum (see kbuild_f64_kernel in scgd0.cu), written as BF16
 // split rows K_t[ω][k] through a shared-memory transpose. The cells of ω ± ω_ν come from the setup
-// table; Re z = (x - ε) - Re Σ(x) stays FP64 (it cancels near the quasiparticle pole), Im Σ(x), the
-// reciprocal and the occupation products are FP32.
-__global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, const double2* __restrict__ Sin,
+// table; Re z = (x - ε) - Re Σ(x), which cancels near the quasiparticle pole, is formed exactly from
+// float pairs (re_z), and Im Σ(x), the reciprocal and the occupation products are FP32: the kernel
+// runs on the FP32 units only.
+__global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, const float4* __restrict__ Sf,
                                                           const int32_t* __restrict__ cell_j,
-                                                          const double* __restrict__ cell_t,
-                                                          const double* __restrict__ cell_x,
+                                                          const float* __restrict__ cell_t,
+                                                          const float2* __restrict__ cell_x,
                                                           const double* __restrict__ wnu, int nm,
-                                                          const double* __restrict__ eps_c,
+                                                          const float2* __restrict__ eps_c,
                                                           const int32_t* __restrict__ col_c, long nk,
-                                                          const double* __restrict__ Fa, const double* __restrict__ Fe,
-                                                          double w_ac, __nv_bfloat16* __restrict__ K0,
-                                                          __nv_bfloat16* __restrict__ K1, __nv_bfloat16* __restrict__ K2,
-                                                          long Kp) {
+                                                          const float* __restrict__ F, double w_ac,
+                                                          __nv_bfloat16* __restrict__ K0, __nv_bfloat16* __restrict__ K1,
+                                                          __nv_bfloat16* __restrict__ K2, long Kp) {
   __shared__ float tile[64][33];
   const int w0 = blockIdx.x * 32;
   const long k0 = long(blockIdx.y) * 64;
   const int tw = threadIdx.x % 32, tk = threadIdx.x / 32;
   const int iw = w0 + tw;
   const long nwm = long(nw) * nm;
-#pragma unroll 1
+#pragma unroll 2
   for (int r = 0; r < 8; ++r) {
     const int kl = tk + 8 * r;
     const long k = k0 + kl;
@@ -56,20 +104,19 @@ __global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, const double2*
       const int nu = int(k % nm);
       const long c = k / nm;
       if (!(wnu[nu] < w_ac)) {
-        const double2* col = Sin + long(nw) * col_c[c];
-        const double e = eps_c[c];
+        const float4* col = Sf + long(nw) * col_c[c];
+        const float2 e = eps_c[c];
         const long ia = iw + long(nw) * nu, ie = ia + nwm;
         const int ja = cell_j[ia], je = cell_j[ie];
-        const double ta = cell_t[ia], te = cell_t[ie];
-        const double2 la = col[ja], ha = col[ja + 1], le = col[je], he = col[je + 1];
-        const float zar = float((cell_x[ia] - e) - ((1 - ta) * la.x + ta * ha.x));
-        const float zer = float((cell_x[ie] - e) - ((1 - te) * le.x + te * he.x));
-        const float tfa = float(ta), tfe = float(te);
-        const float sia = (1.f - tfa) * float(la.y) + tfa * float(ha.y);
-        const float sie = (1.f - tfe) * float(le.y) + tfe * float(he.y);
-        const float ga = sia / (zar * zar + sia * sia);   // Im 1/z with Im z = -Im Σ
+        const float ta = cell_t[ia], te = cell_t[ie];
+        const float4 la = col[ja], ha = col[ja + 1], le = col[je], he = col[je + 1];
+        const float zar = re_z(cell_x[ia], e, la, ha, ta);
+        const float zer = re_z(cell_x[ie], e, le, he, te);
+        const float sia = (1.f - ta) * la.z + ta * ha.z;  // Im Σ(x)
+        const float sie = (1.f - te) * le.z + te * he.z;
+        const float ga = sia / (zar * zar + sia * sia);  // Im 1/z with Im z = -Im Σ
         const float ge = sie / (zer * zer + sie * sie);
-        v = ga * float(Fa[ia]) + ge * float(Fe[ia]);
+        v = ga * F[ia] + ge * F[ie];
       }
     }
     tile[kl][tw] = v;
@@ -168,6 +215,18 @@ void tc_setup(Scgd0Plan* P) {
   tc_gemm_shape(ctx, int(nw), int(ni), int(nk), 16, kNs, &T->bn1, &T->splits1);
   tc_gemm_shape(ctx, int(nw), int(ni), int(nw), 16, kNs, &T->bn2, &T->splits2);
   T->part.alloc(ctx, size_t(std::max(T->splits1, T->splits2)) * size_t(nw * ni));
+  const long nwm = nw * P->nm;
+  T->xf.alloc(ctx, size_t(2 * nwm));
+  T->tf.alloc(ctx, size_t(2 * nwm));
+  T->Ff.alloc(ctx, size_t(2 * nwm));
+  T->ef.alloc(ctx, size_t(P->nc));
+  T->Sf.alloc(ctx, size_t(nw * ni));
+  split_df_kernel<<<div_up(size_t(2 * nwm), 256), 256, 0, s>>>(P->d_cell_x.p, 2 * nwm, T->xf.p);
+  EPSP_LAUNCHED(ctx);
+  to_f32_kernel<<<div_up(size_t(2 * nwm), 256), 256, 0, s>>>(P->d_cell_t.p, 2 * nwm, T->tf.p);
+  EPSP_LAUNCHED(ctx);
+  split_df_kernel<<<div_up(size_t(P->nc), 256), 256, 0, s>>>(P->d_epsc.p, P->nc, T->ef.p);
+  EPSP_LAUNCHED(ctx);
   T->opK = operand(T->Kt, nw, nk, T->Kp, kTcBM);
   T->opG = operand(T->G, ni, nk, T->Kp, T->bn1);
   T->opKK = operand(T->KK, nw, nw, T->Kp2, kTcBM);
@@ -187,9 +246,16 @@ void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS) {
   auto* T = P->tc.get();
   const long nw = P->nw, ni = P->ni, nk = P->nm * P->nc;
   long pk = prof_begin(ctx, "kbuild");
+  const long nwm = nw * P->nm;
+  sigma_f32_kernel<<<div_up(size_t(nw * ni), 256), 256, 0, s>>>(d_Sin, nw * ni, T->Sf.p);
+  EPSP_LAUNCHED(ctx);
+  to_f32_kernel<<<div_up(size_t(nwm), 256), 256, 0, s>>>(P->d_Fa.p, nwm, T->Ff.p);
+  EPSP_LAUNCHED(ctx);
+  to_f32_kernel<<<div_up(size_t(nwm), 256), 256, 0, s>>>(P->d_Fe.p, nwm, T->Ff.p + nwm);
+  EPSP_LAUNCHED(ctx);
   kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), 32), unsigned(T->Kp / 64)), 256, 0, s>>>(
-      int(nw), d_Sin, P->d_cell_j.p, P->d_cell_t.p, P->d_cell_x.p, P->d_wnu.p, int(P->nm), P->d_epsc.p, P->d_colc.p, nk,
-      P->d_Fa.p, P->d_Fe.p, P->w_ac, T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
+      int(nw), T->Sf.p, P->d_cell_j.p, T->tf.p, T->xf.p, P->d_wnu.p, int(P->nm), T->ef.p, P->d_colc.p, nk, T->Ff.p,
+      P->w_ac, T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pk);
   const long slab = nw * ni;
