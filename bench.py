@@ -48,6 +48,9 @@ W_AC = 1e-4
 # bounded samples and scales them by these counts.
 FP64_SCGD0_ITERS = 12
 FP64_LADDER_APPLIES = 2
+# DRAM bytes (read + write) of one ladder-contraction launch of this workload, from one Nsight
+# Compute capture of the same kernel on a GB300 (profiles/tc_ladder_gemm_c2.md)
+TC_LADDER_TRAFFIC_BYTES = 4.414e9 + 0.177e9
 # learned warm start: training and held-out runs, epochs
 WARM_TRAIN_RUNS, WARM_HELDOUT_RUNS, WARM_EPOCHS = 256, 32, 40
 
@@ -59,6 +62,14 @@ def workload():
     occ = dict(Tlist=[T], nlist=[0.0], nelec=1.0, spin_degeneracy=2.0, type="metal")
     mu0 = synthetic.bare_mu(s, T, 1.0)
     return s, T, occ, mu0
+
+
+def bench_config(s, world) -> dict:
+    """The workload, the same on both arms."""
+    return dict(workload="3-band cubic t2g nk=16^3, 495 outer / 12288 inner states, 15 modes, graded "
+                         "1251-node grid, T=300 K; scGD0 to 1e-6 eV + ladder at one Omega=0.1 eV",
+                ni=int(s["eps_i"].size), nf=int(s["eps_f"].size), nw=len(s["omegas"]), nm=15, path="gemm_bf16",
+                warm_start=True, l2="flushed between steps (512 MB write)", parallelism=f"replicas x{world}")
 
 
 def setup_bytes(s) -> int:
@@ -255,11 +266,7 @@ def run_ours(args, world, rank, local):
                ms_per_step=1e3 * total / args.steps, higher_is_better=False,
                scaling="weak", vs_baseline=None, dtype="bf16x3 GEMMs (fp32 accumulate), fp64 reductions",
                data="synthetic (seeded 3-band t2g model, log-normal g2)",
-               config=dict(workload="3-band cubic t2g nk=16^3, 495 outer / 12288 inner states, 15 modes, graded "
-                                    "1251-node grid, T=300 K; scGD0 to 1e-6 eV + ladder at one Omega=0.1 eV",
-                           ni=ni, nf=int(s["eps_f"].size), nw=nw, nm=15, path="gemm_bf16",
-                           warm_start=True, l2="flushed between steps (512 MB write)",
-                           parallelism=f"replicas x{world}"))
+               config=bench_config(s, world))
     if rank != 0:
         return
     out["scgd0_s_to_tol"] = float(np.median(ts))
@@ -281,7 +288,9 @@ def run_ours(args, world, rank, local):
         burst, sust, hbm, src = peaks()
         achieved = flops / avg_s / 1e12
         out["roofline"] = dict(kernel="tc_gemm_bf16 (ladder contraction)", bound="tensor", achieved=achieved,
-                               peak=sust, unit="TFLOP/s", frac=achieved / sust, traffic=None,
+                               peak=sust, unit="TFLOP/s", frac=achieved / sust, traffic=TC_LADDER_TRAFFIC_BYTES,
+                               traffic_source="ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
+                                              "(profiles/tc_ladder_gemm_c2.md)",
                                peak_source=f"{src} bf16 sustained", launches=prof_n, avg_ms=1e3 * avg_s,
                                flops_per_launch=flops, tensor_pipe_frac=3 * achieved / sust)
     out["clocks"] = clk.summary()
@@ -388,8 +397,7 @@ def run_reference(args, world, rank, local):
     out = dict(metric=METRIC, value=v, unit="s", n_gpus=world, steps=args.steps, warmup=args.warmup,
                ms_per_step=1e3 * v, higher_is_better=False, scaling="weak", vs_baseline=None, dtype="fp64",
                data="synthetic (seeded 3-band t2g model, log-normal g2)", impl="reference",
-               config=dict(workload="3-band cubic t2g nk=16^3, scGD0 to 1e-6 eV + ladder at one Omega=0.1 eV",
-                           ni=ni, nw=nw, nm=15),
+               config=bench_config(s, world),
                cpu_baseline=dict(value=v, unit="s", cores=thr, kind="port",
                                  sample=desc + f"; step = {n_it} scGD0 iterations + {n_ap} ladder applications"),
                e2e=dict(value=v, unit="s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
