@@ -76,12 +76,15 @@ __global__ void gather_wq_kernel(const double* __restrict__ wph, const int32_t* 
   wqt[idx] = wph[nu + long(nm) * q];
 }
 
-// Σ_in = Re Σ + i min(Im Σ, -η_min) (src/scgd0.jl:256-260).
-__global__ void clamp_kernel(const double2* __restrict__ S, double2* __restrict__ Sin, long n, double eta_min) {
+// Σ_in = Re Σ + i min(Im Σ, -η_min) (src/scgd0.jl:256-260), for the active temperatures: slot a
+// (blockIdx.y) reads Σ of temperature slots[a] and writes Sin + a n.
+__global__ void clamp_kernel(const double2* __restrict__ S, double2* __restrict__ Sin, long n,
+                             const int* __restrict__ slots, const TParams* __restrict__ tp) {
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  double2 z = S[k];
-  Sin[k] = make_double2(z.x, fmin(z.y, -eta_min));
+  const int a = blockIdx.y, t = slots[a];
+  double2 z = S[long(t) * n + k];
+  Sin[long(a) * n + k] = make_double2(z.x, fmin(z.y, -tp[t].eta_min));
 }
 
 // The reference's Fan-Migdal sum, term by term in FP64: for each (ω, i), the sum over νf of
@@ -222,10 +225,11 @@ __global__ void assemble_f32_kernel(const float* __restrict__ re, const float* _
 
 // Average over degenerate multiplets (src/scgd0.jl:293-301): thread per (ω, multiplet), the sum
 // over members in order divided by the count.
-__global__ void multiplet_kernel(double2* __restrict__ S, int nw, const int32_t* __restrict__ mptr,
-                                 const int32_t* __restrict__ midx, long nmult) {
+__global__ void multiplet_kernel(double2* __restrict__ Sall, int nw, long slab, const int* __restrict__ slots,
+                                 const int32_t* __restrict__ mptr, const int32_t* __restrict__ midx, long nmult) {
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= long(nw) * nmult) return;
+  double2* S = Sall + slab * slots[blockIdx.y];
   int iw = int(k % nw);
   long g = k / nw;
   int p0 = mptr[g], p1 = mptr[g + 1];
@@ -266,12 +270,15 @@ __device__ __forceinline__ float imag_inv_f(float c, float d) {
 // is FP32 (the tensor-core path, whose Σ carries ~1e-6 eV already; FP64 division would make the
 // kernel compute-bound on the FP64 units).
 template <bool F32>
-__global__ void spectral_A_kernel(const double2* __restrict__ S, int nw, const double* __restrict__ wsa, int nwa,
-                                  const int32_t* __restrict__ jsp, const double* __restrict__ tsp,
-                                  const double* __restrict__ eps_i, double* __restrict__ A) {
+__global__ void spectral_A_kernel(const double2* __restrict__ Sall, int nw, long slab, const int* __restrict__ slots,
+                                  const double* __restrict__ wsa, int nwa, const int32_t* __restrict__ jsp,
+                                  const double* __restrict__ tsp, const double* __restrict__ eps_i,
+                                  double* __restrict__ Aall, int ni) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y;
   if (a >= nwa) return;
+  const double2* S = Sall + slab * slots[blockIdx.z];
+  double* A = Aall + long(nwa) * ni * blockIdx.z;
   int j = jsp[a];
   double t = tsp[a];
   const double2* col = S + long(nw) * i;
@@ -301,10 +308,12 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 }
 
 // colsum[i] = Σ_a A[a, i] Wa[a] (the ∫A_i of min_spectral_weight, src/scgd0.jl:308).
-__global__ void __launch_bounds__(256) spectral_colsum_kernel(const double* __restrict__ A, int nwa,
-                                                              const double* __restrict__ Wa, double* __restrict__ colsum) {
+__global__ void __launch_bounds__(256) spectral_colsum_kernel(const double* __restrict__ Aall, int nwa, int ni,
+                                                              const double* __restrict__ Wa, double* __restrict__ colsum_all) {
   __shared__ double sh[256];
   int i = blockIdx.x;
+  const double* A = Aall + long(nwa) * ni * blockIdx.y;
+  double* colsum = colsum_all + long(ni) * blockIdx.y;
   double s = 0;
   for (int a = threadIdx.x; a < nwa; a += 256) s += A[a + long(nwa) * i] * Wa[a];
   double r = block_sum<256>(s, sh);
@@ -314,10 +323,12 @@ __global__ void __launch_bounds__(256) spectral_colsum_kernel(const double* __re
 // D[a] = (Σ_i A[a, i] w_i) Wa[a] (src/scgd0.jl:306-307). A block of 256 threads covers 32 nodes a
 // (the lanes) and splits i over its 8 warps (i ≡ warp mod 8, ascending); the 8 partial sums are
 // added in warp order, so the result is deterministic.
-__global__ void __launch_bounds__(256) spectral_D_kernel(const double* __restrict__ A, int nwa, int ni,
+__global__ void __launch_bounds__(256) spectral_D_kernel(const double* __restrict__ Aall, int nwa, int ni,
                                                          const double* __restrict__ w_i, const double* __restrict__ Wa,
-                                                         double* __restrict__ D) {
+                                                         double* __restrict__ Dall) {
   __shared__ double sh[8][32];
+  const double* A = Aall + long(nwa) * ni * blockIdx.y;
+  double* D = Dall + long(nwa) * blockIdx.y;
   const int lane = threadIdx.x % 32, g = threadIdx.x / 32;
   const int a = blockIdx.x * 32 + lane;
   double s = 0;
@@ -333,8 +344,11 @@ __global__ void __launch_bounds__(256) spectral_D_kernel(const double* __restric
   }
 }
 
-__global__ void __launch_bounds__(256) min_kernel(const double* __restrict__ x, int n, double* __restrict__ out) {
+__global__ void __launch_bounds__(256) min_kernel(const double* __restrict__ xall, int n, const int* __restrict__ slots,
+                                                  double* __restrict__ out_all) {
   __shared__ double sh[256];
+  const double* x = xall + long(n) * blockIdx.x;
+  double* out = out_all + slots[blockIdx.x];
   double m = INFINITY;
   for (int k = threadIdx.x; k < n; k += 256) m = fmin(m, x[k]);
   sh[threadIdx.x] = m;
@@ -382,12 +396,19 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 __global__ void __cluster_dims__(kMuCluster, 1, 1) __launch_bounds__(kMuThreads)
-    mu_solve_kernel(const double* __restrict__ D, const double* __restrict__ wsa, int nwa, double T, double W,
-                    double base, double gs, double n_target, int holes, double br0, double br1, double guess,
-                    double* __restrict__ mu_out, int* __restrict__ status) {
+    mu_solve_kernel(const double* __restrict__ Dall, const double* __restrict__ wsa, int nwa, const int* __restrict__ slots,
+                    const TParams* __restrict__ tp, double W, double base, double gs, double br0, double br1,
+                    double* __restrict__ mu_all, int* __restrict__ status_all) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned rank = cluster.block_rank();
+  // one cluster per active temperature
+  const int slot = blockIdx.x / kMuCluster, t = slots[slot];
+  const double* D = Dall + long(nwa) * slot;
+  const double T = tp[t].T, n_target = tp[t].n_target, guess = tp[t].mu;
+  const int holes = tp[t].holes;
+  double* mu_out = mu_all + t;
+  int* status = status_all + t;
   extern __shared__ double s_E[];
   __shared__ double sh[4][kMuWarps];
   __shared__ double part[4];
@@ -512,9 +533,13 @@ static size_t mu_smem_bytes(long nwa) {
 // err = max |Σ_new - Σ| over one temperature, and Σ ← Σ_new (src/scgd0.jl:326-328). The maximum of
 // non-negative doubles is taken on their bit patterns, which order the same way; NaN wins, as in
 // Julia's maximum.
-__global__ void err_copy_kernel(const double2* __restrict__ Snew, double2* __restrict__ S, long n,
-                                unsigned long long* __restrict__ errbits) {
+__global__ void err_copy_kernel(const double2* __restrict__ Snew_all, double2* __restrict__ S_all, long n,
+                                const int* __restrict__ slots, unsigned long long* __restrict__ errbits_all) {
   __shared__ unsigned long long sh[256];
+  const int t = slots[blockIdx.y];
+  const double2* Snew = Snew_all + long(t) * n;
+  double2* S = S_all + long(t) * n;
+  unsigned long long* errbits = errbits_all + t;
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
   unsigned long long e = 0;
   if (k < n) {
@@ -887,69 +912,89 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   std::vector<int> h_status(static_cast<size_t>(nT));
   int32_t niter = 0;
   const unsigned eb = div_up(size_t(slab), 256);
+  // Every active temperature of an iteration is processed by the same launches (slot a ->
+  // temperature slots[a]); per-temperature T, μ, η_min, target and branch live on the device.
+  DBuf<int> d_slots;
+  DBuf<TParams> d_tp;
+  DBuf<double2> Sin_b;
+  DBuf<double> A_b, colsum_b, D_b;
+  d_slots.alloc(ctx, size_t(nT));
+  d_tp.alloc(ctx, size_t(nT));
+  Sin_b.alloc(ctx, size_t(slab * nT));
+  A_b.alloc(ctx, size_t(nwa * ni * nT));
+  colsum_b.alloc(ctx, size_t(ni * nT));
+  D_b.alloc(ctx, size_t(nwa * nT));
+  if (P->path == EPSP_PATH_GEMM_BF16) tc_reserve(P, nT);
+  std::vector<TParams> h_tp(static_cast<size_t>(nT));
+  std::vector<int> slots;
   for (int32_t iter = 1; iter <= maxiter; ++iter) {
     auto t0 = std::chrono::steady_clock::now();
+    slots.clear();
+    for (int64_t iT = 0; iT < nT; ++iT) {
+      if (!active[size_t(iT)]) continue;
+      slots.push_back(int(iT));
+      TParams& q = h_tp[size_t(iT)];
+      q.T = occ->Tlist[iT];
+      q.mu = mu[size_t(iT)];
+      q.eta_min = eta_min[iT];
+      q.holes = (!fix_mu && occ->type == EPSP_SEMICONDUCTOR && occ->nlist[iT] < 0) ? 1 : 0;
+      q.n_target = fix_mu ? 0.0 : occ->nlist[iT] + occ->nelec;
+      q.pad = 0;
+    }
+    const int nA = int(slots.size());
+    d_slots.upload(slots.data(), slots.size(), s);
+    d_tp.upload(h_tp.data(), h_tp.size(), s);
     d_err.zero(s);
     d_status.zero(s);
-    for (int64_t iT = 0; iT < nT; ++iT) {
-      if (!active[size_t(iT)]) continue;
-      const double T = occ->Tlist[iT];
-      double2* ST = S.p + slab * iT;
-      double2* SnT = Snew.p + slab * iT;
-      clamp_kernel<<<eb, 256, 0, s>>>(ST, P->d_Sin.p, slab, eta_min[iT]);
-      EPSP_LAUNCHED(ctx);
-      P->d_ImS.zero(s);
-      scgd0_imsigma(P, P->d_Sin.p, mu[size_t(iT)], T, P->d_ImS.p);
-      long pk = prof_begin(ctx, "kk");
-      if (P->path == EPSP_PATH_GEMM_BF16) {
-        tc_kk_assemble(P, SnT);
-      } else {
+    clamp_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(S.p, Sin_b.p, slab, d_slots.p, d_tp.p);
+    EPSP_LAUNCHED(ctx);
+    if (P->path == EPSP_PATH_GEMM_BF16) {
+      tc_iterate(P, nA, d_slots.p, slots.data(), d_tp.p, Sin_b.p, Snew.p);
+    } else {
+      for (int a = 0; a < nA; ++a) {
+        const int64_t iT = slots[size_t(a)];
+        P->d_ImS.zero(s);
+        scgd0_imsigma(P, Sin_b.p + slab * a, mu[size_t(iT)], occ->Tlist[iT], P->d_ImS.p);
+        long pk = prof_begin(ctx, "kk");
         gemm_f64(ctx, false, int(nw), int(ni), int(nw), 1.0, P->d_KK.p, nw, P->d_ImS.p, nw, 0.0, P->d_ReS.p, nw);
-        assemble_kernel<<<eb, 256, 0, s>>>(P->d_ReS.p, P->d_ImS.p, SnT, slab);
+        assemble_kernel<<<eb, 256, 0, s>>>(P->d_ReS.p, P->d_ImS.p, Snew.p + slab * iT, slab);
         EPSP_LAUNCHED(ctx);
+        prof_end(ctx, pk);
       }
-      prof_end(ctx, pk);
     }
-    if (P->nmult > 0)
-      for (int64_t iT = 0; iT < nT; ++iT) {
-        if (!active[size_t(iT)]) continue;
-        multiplet_kernel<<<div_up(size_t(nw * P->nmult), 256), 256, 0, s>>>(Snew.p + slab * iT, int(nw), P->d_mptr.p,
-                                                                            P->d_midx.p, P->nmult);
-        EPSP_LAUNCHED(ctx);
-      }
-    for (int64_t iT = 0; iT < nT; ++iT) {
-      if (!active[size_t(iT)]) continue;
-      const double T = occ->Tlist[iT];
-      double2* ST = S.p + slab * iT;
-      double2* SnT = Snew.p + slab * iT;
-      auto spectral_A = P->path == EPSP_PATH_GEMM_BF16 ? spectral_A_kernel<true> : spectral_A_kernel<false>;
-      spectral_A<<<dim3(div_up(size_t(nwa), 256), unsigned(ni)), 256, 0, s>>>(SnT, int(nw), P->d_wsa.p, int(nwa), P->d_jsp.p,
-                                                                                    P->d_tsp.p, P->d_eps_i.p, P->d_A.p);
-      EPSP_LAUNCHED(ctx);
-      spectral_colsum_kernel<<<unsigned(ni), 256, 0, s>>>(P->d_A.p, int(nwa), P->d_Wa.p, P->d_colsum.p);
-      EPSP_LAUNCHED(ctx);
-      min_kernel<<<1, 256, 0, s>>>(P->d_colsum.p, int(ni), d_minA.p + iT);
-      EPSP_LAUNCHED(ctx);
-      if (!fix_mu) {
-        spectral_D_kernel<<<div_up(size_t(nwa), 32), 256, 0, s>>>(P->d_A.p, int(nwa), int(ni), P->d_w_i.p, P->d_Wa.p, P->d_D.p);
-        EPSP_LAUNCHED(ctx);
-        bool holes = occ->type == EPSP_SEMICONDUCTOR && occ->nlist[iT] < 0;
-        double n_target = occ->nlist[iT] + occ->nelec;
-        long pm = prof_begin(ctx, "mu");
-        mu_solve_kernel<<<kMuCluster, kMuThreads, mu_smem_bytes(nwa), s>>>(P->d_D.p, P->d_wsa.p, int(nwa), T, P->W, P->nstates_base,
-                                                          occ->spin_degeneracy, n_target, holes ? 1 : 0, br0, br1,
-                                                          mu[size_t(iT)], d_mu.p + iT, d_status.p + iT);
-        EPSP_LAUNCHED(ctx);
-        prof_end(ctx, pm);
-      }
-      err_copy_kernel<<<eb, 256, 0, s>>>(SnT, ST, slab, d_err.p + iT);
+    if (P->nmult > 0) {
+      multiplet_kernel<<<dim3(div_up(size_t(nw * P->nmult), 256), unsigned(nA)), 256, 0, s>>>(
+          Snew.p, int(nw), slab, d_slots.p, P->d_mptr.p, P->d_midx.p, P->nmult);
       EPSP_LAUNCHED(ctx);
     }
+    auto spectral_A = P->path == EPSP_PATH_GEMM_BF16 ? spectral_A_kernel<true> : spectral_A_kernel<false>;
+    spectral_A<<<dim3(div_up(size_t(nwa), 256), unsigned(ni), unsigned(nA)), 256, 0, s>>>(
+        Snew.p, int(nw), slab, d_slots.p, P->d_wsa.p, int(nwa), P->d_jsp.p, P->d_tsp.p, P->d_eps_i.p, A_b.p, int(ni));
+    EPSP_LAUNCHED(ctx);
+    spectral_colsum_kernel<<<dim3(unsigned(ni), unsigned(nA)), 256, 0, s>>>(A_b.p, int(nwa), int(ni), P->d_Wa.p,
+                                                                          colsum_b.p);
+    EPSP_LAUNCHED(ctx);
+    min_kernel<<<unsigned(nA), 256, 0, s>>>(colsum_b.p, int(ni), d_slots.p, d_minA.p);
+    EPSP_LAUNCHED(ctx);
+    if (!fix_mu) {
+      spectral_D_kernel<<<dim3(div_up(size_t(nwa), 32), unsigned(nA)), 256, 0, s>>>(A_b.p, int(nwa), int(ni), P->d_w_i.p,
+                                                                                   P->d_Wa.p, D_b.p);
+      EPSP_LAUNCHED(ctx);
+      long pm = prof_begin(ctx, "mu");
+      mu_solve_kernel<<<unsigned(kMuCluster * nA), kMuThreads, mu_smem_bytes(nwa), s>>>(
+          D_b.p, P->d_wsa.p, int(nwa), d_slots.p, d_tp.p, P->W, P->nstates_base, occ->spin_degeneracy, br0, br1, d_mu.p,
+          d_status.p);
+      EPSP_LAUNCHED(ctx);
+      prof_end(ctx, pm);
+    }
+    err_copy_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(Snew.p, S.p, slab, d_slots.p, d_err.p);
+    EPSP_LAUNCHED(ctx);
     d_err.download(h_err.data(), size_t(nT), s);
     d_mu.download(h_mu.data(), size_t(nT), s);
     d_minA.download(h_minA.data(), size_t(nT), s);
     d_status.download(h_status.data(), size_t(nT), s);
     EPSP_CUDA(cudaStreamSynchronize(s));
+    if (P->path == EPSP_PATH_GEMM_BF16) tc_check(P);
     for (int64_t iT = 0; iT < nT; ++iT) {
       if (!active[size_t(iT)]) continue;
       hist->min_spectral_weight[iT + nT * (iter - 1)] = h_minA[size_t(iT)];

@@ -7,6 +7,12 @@
 
 namespace epsp {
 
+// Per-temperature parameters of one iteration, on the device (indexed by temperature).
+struct TParams {
+  double T, mu, eta_min, n_target;
+  int holes, pad;
+};
+
 struct Scgd0Plan {
   Ctx* ctx = nullptr;
   int path = EPSP_PATH_DIRECT_FP64;
@@ -42,9 +48,17 @@ struct Scgd0Plan {
   DBuf<double> d_ImS, d_ReS, d_A, d_colsum, d_D;
 };
 
-// Tensor-core (BF16x3) pieces of the GEMM_BF16X3 path, in scgd0_tc.cu.
+// Tensor-core pieces of the GEMM_BF16 path, in scgd0_tc.cu.
 void tc_setup(Scgd0Plan* P);
 void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS);
 void tc_kk_assemble(Scgd0Plan* P, double2* d_Snew);
+// Buffers and tensor maps for up to nT temperatures in one iteration.
+void tc_reserve(Scgd0Plan* P, long nT);
+// Σ_new of nA active temperatures at once: slot a reads the clamped Σ_in + a nω ni and writes
+// Snew_all + slots_h[a] nω ni (temperature index); per-temperature T and μ from tp (device).
+void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, const TParams* d_tp,
+                const double2* d_Sin_b, double2* d_Snew_all);
+// Fails with EPSP_EDEVICE_TIMEOUT if a tensor-core GEMM's bounded wait ran out (synchronises).
+void tc_check(Scgd0Plan* P);
 
 }  // namespace epsp

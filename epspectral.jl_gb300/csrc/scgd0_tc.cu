@@ -16,6 +16,9 @@
 namespace epsp {
 
 constexpr int kNs = 3;
+// K-blocks of 64 summed by one FP32 accumulator at most: the Fan-Migdal sums are long and of one
+// sign, and their FP32 rounding must stay well below the iteration's tol (1e-6 eV)
+constexpr int kKbCap = 16;
 
 struct Scgd0Plan::Tc {
   long Kp = 0, Kp2 = 0;
@@ -29,6 +32,9 @@ struct Scgd0Plan::Tc {
   DBuf<float2> xf, ef;
   DBuf<float> tf, Ff;
   DBuf<float4> Sf;
+  // batched iteration: capacity in temperatures, ImΣ of every slot
+  long capT = 1;
+  DBuf<double> ImS_b;
 };
 
 __device__ __forceinline__ float2 split_df(double x) {
@@ -79,14 +85,14 @@ __device__ __forceinline__ float re_z(float2 x, float2 e, float4 lo, float4 hi, 
 // table; Re z = (x - ε) - Re Σ(x), which cancels near the quasiparticle pole, is formed exactly from
 // float pairs (re_z), and Im Σ(x), the reciprocal and the occupation products are FP32: the kernel
 // runs on the FP32 units only.
-__global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, const float4* __restrict__ Sf,
+__global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, long slab, const float4* __restrict__ Sf_all,
                                                           const int32_t* __restrict__ cell_j,
                                                           const float* __restrict__ cell_t,
                                                           const float2* __restrict__ cell_x,
                                                           const double* __restrict__ wnu, int nm,
                                                           const float2* __restrict__ eps_c,
                                                           const int32_t* __restrict__ col_c, long nk,
-                                                          const float* __restrict__ F, double w_ac,
+                                                          const float* __restrict__ F_all, double w_ac,
                                                           __nv_bfloat16* __restrict__ K0, __nv_bfloat16* __restrict__ K1,
                                                           __nv_bfloat16* __restrict__ K2, long Kp) {
   __shared__ float tile[64][33];
@@ -95,6 +101,10 @@ __global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, const float4* 
   const int tw = threadIdx.x % 32, tk = threadIdx.x / 32;
   const int iw = w0 + tw;
   const long nwm = long(nw) * nm;
+  // slot blockIdx.z: its clamped Σ, its occupation tables, its nω rows of K_t
+  const float4* Sf = Sf_all + slab * blockIdx.z;
+  const float* F = F_all + 2 * nwm * blockIdx.z;
+  const long krow0 = long(nw) * blockIdx.z;
 #pragma unroll 2
   for (int r = 0; r < 8; ++r) {
     const int kl = tk + 8 * r;
@@ -134,7 +144,7 @@ __global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, const float4* 
       p1[j] = q[1];
       p2[j] = q[2];
     }
-    const long off = long(ow) * Kp + k0 + kc;
+    const long off = (krow0 + ow) * Kp + k0 + kc;
     *reinterpret_cast<uint4*>(K0 + off) = *reinterpret_cast<const uint4*>(p0);
     *reinterpret_cast<uint4*>(K1 + off) = *reinterpret_cast<const uint4*>(p1);
     *reinterpret_cast<uint4*>(K2 + off) = *reinterpret_cast<const uint4*>(p2);
@@ -178,6 +188,64 @@ __global__ void finalize_assemble_kernel(const float* __restrict__ part, long n,
   out[k] = make_double2(double(s), im[k]);
 }
 
+// The occupation tables of the active temperatures as FP32 (computed in FP64 as occ_table_kernel):
+// F[a][0 .. nω nm) absorption, F[a][nω nm .. 2 nω nm) emission.
+__global__ void occ_table_f32_kernel(const double* __restrict__ ws, int nw, const double* __restrict__ wnu, int nm,
+                                     const int* __restrict__ slots, const TParams* __restrict__ tp, double w_ac,
+                                     float* __restrict__ F_all) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const long nwm = long(nw) * nm;
+  if (k >= nwm) return;
+  const int a = blockIdx.y;
+  const TParams q = tp[slots[a]];
+  float* F = F_all + 2 * nwm * a;
+  const int iw = k % nw, nu = k / nw;
+  const double wq = wnu[nu], w = ws[iw];
+  if (wq < w_ac) {
+    F[k] = 0.f;
+    F[k + nwm] = 0.f;
+    return;
+  }
+  const double nq = occ_boson_d(wq, q.T);
+  F[k] = float(nq + occ_fermion_d(w + wq - q.mu, q.T));
+  F[k + nwm] = float(nq + 1 - occ_fermion_d(w - wq - q.mu, q.T));
+}
+
+__global__ void sigma_f32_batch_kernel(const double2* __restrict__ S, long n, int nA, float4* __restrict__ out) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n * nA) return;
+  const double2 z = S[k];
+  const float2 r = split_df(z.x);
+  out[k] = make_float4(r.x, r.y, float(z.y), 0.f);
+}
+
+// ImΣ of slot a: ImS[a][ω + nω i] = Σ_s part[s][(a nω + ω) + M i], M = nA nω (the stacked rows).
+__global__ void finalize_fm_batch_kernel(const float* __restrict__ part, int nw, long slab, int nA, int splits,
+                                         long stride, double* __restrict__ ImS) {
+  const long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= slab) return;
+  const int a = blockIdx.y;
+  const long w = k % nw, i = k / nw;
+  const long src = (long(a) * nw + w) + long(nA) * nw * i;
+  float acc = 0.f;
+  for (int p = 0; p < splits; ++p) acc += part[src + stride * p];
+  ImS[slab * a + k] = double(acc);
+}
+
+// Σ_new of temperature slots[a] = Σ_s part[s][a slab + k] + i ImS[a][k] (the KK product's columns
+// are the slots' states in order).
+__global__ void finalize_kk_batch_kernel(const float* __restrict__ part, long slab, int splits, long stride,
+                                         const double* __restrict__ ImS, const int* __restrict__ slots,
+                                         double2* __restrict__ Snew_all) {
+  const long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= slab) return;
+  const int a = blockIdx.y;
+  const long src = slab * a + k;
+  float acc = 0.f;
+  for (int p = 0; p < splits; ++p) acc += part[src + stride * p];
+  Snew_all[slab * slots[a] + k] = make_double2(double(acc), ImS[src]);
+}
+
 static long pad64(long x) { return (x + 63) / 64 * 64; }
 
 static TcOperand operand(DBuf<__nv_bfloat16>* parts, long rows, long cols, long ld, int box_rows) {
@@ -212,8 +280,8 @@ void tc_setup(Scgd0Plan* P) {
   split3_rows_kernel<<<div_up(size_t(nw * T->Kp2), 256), 256, 0, s>>>(P->d_KK.p, nw, nw, nw, T->Kp2, true, T->KK[0].p,
                                                                       T->KK[1].p, T->KK[2].p);
   EPSP_LAUNCHED(ctx);
-  tc_gemm_shape(ctx, int(nw), int(ni), int(nk), 16, kNs, &T->bn1, &T->splits1);
-  tc_gemm_shape(ctx, int(nw), int(ni), int(nw), 16, kNs, &T->bn2, &T->splits2);
+  tc_gemm_shape(ctx, int(nw), int(ni), int(nk), 16, kNs, &T->bn1, &T->splits1, kKbCap);
+  tc_gemm_shape(ctx, int(nw), int(ni), int(nw), 16, kNs, &T->bn2, &T->splits2, kKbCap);
   T->part.alloc(ctx, size_t(std::max(T->splits1, T->splits2)) * size_t(nw * ni));
   const long nwm = nw * P->nm;
   T->xf.alloc(ctx, size_t(2 * nwm));
@@ -253,13 +321,14 @@ void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS) {
   EPSP_LAUNCHED(ctx);
   to_f32_kernel<<<div_up(size_t(nwm), 256), 256, 0, s>>>(P->d_Fe.p, nwm, T->Ff.p + nwm);
   EPSP_LAUNCHED(ctx);
-  kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), 32), unsigned(T->Kp / 64)), 256, 0, s>>>(
-      int(nw), T->Sf.p, P->d_cell_j.p, T->tf.p, T->xf.p, P->d_wnu.p, int(P->nm), T->ef.p, P->d_colc.p, nk, T->Ff.p,
-      P->w_ac, T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
+  kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), 32), unsigned(T->Kp / 64), 1), 256, 0, s>>>(
+      int(nw), nw * ni, T->Sf.p, P->d_cell_j.p, T->tf.p, T->xf.p, P->d_wnu.p, int(P->nm), T->ef.p, P->d_colc.p, nk,
+      T->Ff.p, P->w_ac, T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pk);
   const long slab = nw * ni;
-  int sp = tc_gemm_launch(ctx, T->opK, T->opG, int(nw), int(ni), int(nk), T->part.p, nw, slab, 16, T->err.p, "tc_fm");
+  int sp = tc_gemm_launch(ctx, T->opK, T->opG, int(nw), int(ni), int(nk), T->part.p, nw, slab, 16, T->err.p, "tc_fm",
+                          kKbCap);
   finalize_add_kernel<<<div_up(size_t(slab), 256), 256, 0, s>>>(T->part.p, slab, sp, slab, d_ImS);
   EPSP_LAUNCHED(ctx);
   check_err(P);
@@ -273,8 +342,76 @@ void tc_kk_assemble(Scgd0Plan* P, double2* d_Snew) {
   split3_rows_kernel<<<div_up(size_t(ni * T->Kp2), 256), 256, 0, s>>>(P->d_ImS.p, nw, ni, nw, T->Kp2, false, T->Im[0].p,
                                                                       T->Im[1].p, T->Im[2].p);
   EPSP_LAUNCHED(ctx);
-  int sp = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(ni), int(nw), T->part.p, nw, slab, 16, T->err.p, "tc_kk");
+  int sp = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(ni), int(nw), T->part.p, nw, slab, 16, T->err.p, "tc_kk",
+                          kKbCap);
   finalize_assemble_kernel<<<div_up(size_t(slab), 256), 256, 0, s>>>(T->part.p, slab, sp, slab, P->d_ImS.p, d_Snew);
+  EPSP_LAUNCHED(ctx);
+}
+
+void tc_reserve(Scgd0Plan* P, long nT) {
+  auto* T = P->tc.get();
+  if (nT <= T->capT && T->ImS_b.p) return;
+  Ctx* ctx = P->ctx;
+  const long nw = P->nw, ni = P->ni, nk = P->nm * P->nc, nwm = nw * P->nm, slab = nw * ni;
+  nT = std::max(nT, T->capT);
+  if (nT * nw > (1l << 30) || nT * ni > (1l << 30)) fail(EPSP_EINVAL, "too many temperatures for the 32-bit tile grid");
+  for (int p = 0; p < kNs; ++p) {
+    T->Kt[p].alloc(ctx, size_t(nT * nw * T->Kp));
+    T->Im[p].alloc(ctx, size_t(nT * ni * T->Kp2));
+  }
+  T->Sf.alloc(ctx, size_t(nT * slab));
+  T->Ff.alloc(ctx, size_t(nT * 2 * nwm));
+  T->ImS_b.alloc(ctx, size_t(nT * slab));
+  size_t part = 0;
+  for (long a = 1; a <= nT; ++a) {
+    int bn, sp1, sp2;
+    tc_gemm_shape(ctx, int(a * nw), int(ni), int(nk), 16, kNs, &bn, &sp1, kKbCap);
+    tc_gemm_shape(ctx, int(nw), int(a * ni), int(nw), 16, kNs, &bn, &sp2, kKbCap);
+    part = std::max(part, size_t(std::max(sp1, sp2)) * size_t(a * slab));
+  }
+  T->part.alloc(ctx, part);
+  T->opK = operand(T->Kt, nT * nw, nk, T->Kp, kTcBM);
+  T->opIm = operand(T->Im, nT * ni, nw, T->Kp2, T->bn2);
+  T->capT = nT;
+}
+
+void tc_check(Scgd0Plan* P) { check_err(P); }
+
+void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, const TParams* d_tp,
+                const double2* d_Sin_b, double2* d_Snew_all) {
+  (void)slots_h;
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  auto* T = P->tc.get();
+  if (nA > T->capT) fail(EPSP_EINVAL, "more active temperatures than reserved");
+  const long nw = P->nw, ni = P->ni, nk = P->nm * P->nc, nwm = nw * P->nm, slab = nw * ni;
+  const unsigned eb = div_up(size_t(slab), 256);
+  long pk = prof_begin(ctx, "kbuild");
+  sigma_f32_batch_kernel<<<div_up(size_t(slab * nA), 256), 256, 0, s>>>(d_Sin_b, slab, nA, T->Sf.p);
+  EPSP_LAUNCHED(ctx);
+  occ_table_f32_kernel<<<dim3(div_up(size_t(nwm), 256), unsigned(nA)), 256, 0, s>>>(
+      P->d_ws.p, int(nw), P->d_wnu.p, int(P->nm), d_slots, d_tp, P->w_ac, T->Ff.p);
+  EPSP_LAUNCHED(ctx);
+  kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), 32), unsigned(T->Kp / 64), unsigned(nA)), 256, 0, s>>>(
+      int(nw), slab, T->Sf.p, P->d_cell_j.p, T->tf.p, T->xf.p, P->d_wnu.p, int(P->nm), T->ef.p, P->d_colc.p, nk, T->Ff.p,
+      P->w_ac, T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
+  EPSP_LAUNCHED(ctx);
+  prof_end(ctx, pk);
+  // ImΣ of every slot: the stacked K_t rows times G
+  const long M = long(nA) * nw;
+  int sp = tc_gemm_launch(ctx, T->opK, T->opG, int(M), int(ni), int(nk), T->part.p, M, M * ni, 16, T->err.p, "tc_fm",
+                          kKbCap);
+  finalize_fm_batch_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(T->part.p, int(nw), slab, nA, sp, M * ni, T->ImS_b.p);
+  EPSP_LAUNCHED(ctx);
+  // ReΣ = KK ImΣ for every slot at once (columns: the slots' states in order)
+  split3_rows_kernel<<<div_up(size_t(nA * ni * T->Kp2), 256), 256, 0, s>>>(T->ImS_b.p, nw, nA * ni, nw, T->Kp2, false,
+                                                                            T->Im[0].p, T->Im[1].p, T->Im[2].p);
+  EPSP_LAUNCHED(ctx);
+  const long N2 = long(nA) * ni;
+  int sp2 = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(N2), int(nw), T->part.p, nw, nw * N2, 16, T->err.p,
+                           "tc_kk", kKbCap);
+  finalize_kk_batch_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(T->part.p, slab, sp2, nw * N2, T->ImS_b.p, d_slots,
+                                                                   d_Snew_all);
   EPSP_LAUNCHED(ctx);
 }
 

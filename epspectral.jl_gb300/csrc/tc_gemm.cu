@@ -35,11 +35,12 @@ CUtensorMap make_tmap_bf16(const void* base, long rows, long cols, long ld, int 
   return m;
 }
 
-void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* bn, int* splits) {
+void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* bn, int* splits, int kb_cap) {
   const int BN = (ns == 2 && N > 128) ? 256 : 128;
   const int tiles = ((M + kTcBM - 1) / kTcBM) * ((N + BN - 1) / BN);
   const int kblocks = (K + kTcBK - 1) / kTcBK;
   int sp = std::max(1, (ctx->sm_count + tiles - 1) / tiles);
+  if (kb_cap > 0) sp = std::max(sp, (kblocks + kb_cap - 1) / kb_cap);
   sp = std::min({sp, std::max(1, max_splits), std::max(1, kblocks)});
   const int per = (kblocks + sp - 1) / sp;
   sp = std::max(1, (kblocks + per - 1) / per);
@@ -68,10 +69,10 @@ static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int 
 }
 
 int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int K, float* out, long ld_out,
-                   long split_stride, int max_splits, int* d_err, const char* prof_name) {
+                   long split_stride, int max_splits, int* d_err, const char* prof_name, int kb_cap) {
   if (A.ns != B.ns || (A.ns != 2 && A.ns != 3)) fail(EPSP_EINVAL, "operands must be split into 2 or 3 parts alike");
   int BN, splits;
-  tc_gemm_shape(ctx, M, N, K, max_splits, A.ns, &BN, &splits);
+  tc_gemm_shape(ctx, M, N, K, max_splits, A.ns, &BN, &splits, kb_cap);
   const int kblocks = (K + kTcBK - 1) / kTcBK;
   const int per = (kblocks + splits - 1) / splits;
   long pi = prof_begin(ctx, prof_name);

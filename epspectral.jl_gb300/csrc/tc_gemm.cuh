@@ -252,12 +252,14 @@ struct TcOperand {
 };
 
 // Launches the split-precision product of A [M][K] and B [N][K] (K-major, both split into A.ns
-// parts) into the FP32 slabs out[split][m + ld_out n]; returns the number of splits used.
+// parts) into the FP32 slabs out[split][m + ld_out n]; returns the number of splits used. With
+// kb_cap > 0 no FP32 accumulator sums more than kb_cap K-blocks of 64 (splits are added to bound
+// the accumulation error of long same-sign sums), within max_splits.
 int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int K, float* out, long ld_out,
-                   long split_stride, int max_splits, int* d_err, const char* prof_name = "tc_gemm");
+                   long split_stride, int max_splits, int* d_err, const char* prof_name = "tc_gemm", int kb_cap = 0);
 
 // The BN and split count tc_gemm_launch picks for (M, N, K), ns parts, at most max_splits splits.
-void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* bn, int* splits);
+void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* bn, int* splits, int kb_cap = 0);
 
 // x = Σ_p x_p with x_p BF16, p < ns (round to nearest at every step).
 __device__ __forceinline__ void split_bf16_n(float x, int ns, __nv_bfloat16* out) {

@@ -131,3 +131,30 @@ def test_errors_come_back_as_status(api, holstein_gpu, cubic_small):
     r = api.loop_scgd0(s, occ(0.0), eta_init=0.05, tol=1e-6, maxiter=2, mu_start=[0.0], omega_acoustic=W_AC, ctx=ctx)
     assert r["niter"] == 2
     assert ctx.kernel_launches > 0
+
+
+def test_temperatures_batched_in_one_launch_match_single_runs(api, oracle, cubic_small):
+    # Four temperatures go through each iteration's launches together and freeze at different
+    # iterations; every temperature's result must equal its own single-temperature run (bitwise on
+    # the FP64 paths, whose Fan-Migdal sums still run per temperature; within 1e-6 eV on the
+    # tensor-core path, whose stacked GEMM groups the K sums differently), and the oracle's
+    # iteration history.
+    s = cubic_small
+    Ts = [150 * synthetic.KELVIN, 300 * synthetic.KELVIN, 450 * synthetic.KELVIN, 800 * synthetic.KELVIN]
+    o = occ(0.0, Tlist=Ts)
+    kw = dict(eta_init=0.05, tol=1e-7, maxiter=40, mu_start=[-0.5] * 4, omega_acoustic=W_AC)
+    ref = oracle.loop_scgd0(s, o, **kw)
+    assert len(set(ref["history"]["iter_frozen"])) > 1  # the temperatures freeze at different iterations
+    for path in ("gemm_fp64", "gemm_bf16"):
+        got = api.loop_scgd0(s, o, path=path, **kw)
+        assert list(got["converged"]) == [True] * 4
+        for t in range(4):
+            one = api.loop_scgd0(s, occ(0.0, Tlist=[Ts[t]]), path=path, **dict(kw, mu_start=[-0.5]))
+            if path == "gemm_fp64":
+                assert np.array_equal(got["sigma"][:, :, t], one["sigma"][:, :, 0])
+                assert got["mu"][t] == one["mu"][0]
+                assert got["history"]["iter_frozen"][t] == ref["history"]["iter_frozen"][t]
+                assert rel(got["sigma"][:, :, t], ref["sigma"][:, :, t]) <= 1e-10
+            else:
+                assert np.max(np.abs(got["sigma"][:, :, t] - one["sigma"][:, :, 0])) <= 1e-6
+                assert np.max(np.abs(got["sigma"][:, :, t] - ref["sigma"][:, :, t])) <= 1e-5
