@@ -401,11 +401,18 @@ __global__ void xgen_f64_kernel(const double2* __restrict__ J, const int32_t* __
 // that the BF16 rows are written 16 bytes at a time.
 constexpr int kXgTiles = 8;
 
-__global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restrict__ J, const int32_t* __restrict__ mt_k,
-                                                        const float* __restrict__ mt_w, const float* __restrict__ nnu,
+// Batched over blockIdx.z: slot z makes the rows z 24 nwp.. of A from the vertex J + jstride r and
+// the occupations nnu + 16 r of right-hand side r = rmap[z] (r = z without rmap).
+__global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restrict__ J_all, long jstride,
+                                                        const int* __restrict__ rmap, const int32_t* __restrict__ mt_k,
+                                                        const float* __restrict__ mt_w, const float* __restrict__ nnu_all,
                                                         int nw, int nwp, int ns, int nmp, int ni, long Kx, long Kp,
                                                         __nv_bfloat16* __restrict__ Ah, __nv_bfloat16* __restrict__ Al) {
   extern __shared__ float xg_smem[];
+  const int rhs = rmap ? rmap[blockIdx.z] : int(blockIdx.z);
+  const double2* J = J_all + jstride * rhs;
+  const float* nnu = nnu_all + 16 * rhs;
+  const long row_base = long(blockIdx.z) * 24 * nwp;
   const int W = ns + 2, win = 32 + 2 * W;
   float2* s_j = reinterpret_cast<float2*>(xg_smem);                               // [4][win] (re, im)
   float (*tile)[64][33] = reinterpret_cast<float (*)[64][33]>(s_j + 4 * win);    // [4][64][33]
@@ -492,7 +499,7 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
         hh[t] = __float2bfloat16_rn(x);
         ll[t] = __float2bfloat16_rn(x - __bfloat162float(hh[t]));
       }
-      const long row = long(q + 6 * (c0 + 2 * ri)) * nwp + j0 + wr;
+      const long row = row_base + long(q + 6 * (c0 + 2 * ri)) * nwp + j0 + wr;
       const long off = row * Kp + k0 + kc;
       *reinterpret_cast<uint4*>(Ah + off) = *reinterpret_cast<const uint4*>(hh);
       *reinterpret_cast<uint4*>(Al + off) = *reinterpret_cast<const uint4*>(ll);
@@ -507,18 +514,22 @@ static size_t xgen_smem_bytes(int ns) {
 
 // Y (rows q = 0, 2 of D) as the BF16 hi/lo B operand of the Kramers-Kronig GEMM: row (qq, c0, ri, n),
 // K = ω' contiguous, stride Kp2.
-__global__ void y_split_kernel(const double* __restrict__ D, int nw, int nwp, long N, long Kp2, __nv_bfloat16* __restrict__ Yh,
-                               __nv_bfloat16* __restrict__ Yl) {
+// Batched over blockIdx.y: slot z reads rows z 24 nwp.. of D (column stride ldD) and writes rows
+// z 8N.. of Y.
+__global__ void y_split_kernel(const double* __restrict__ D, long ldD, int nw, int nwp, long N, long Kp2,
+                               __nv_bfloat16* __restrict__ Yh, __nv_bfloat16* __restrict__ Yl) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= 8 * N * Kp2) return;
+  const long z = blockIdx.y;
   long w = idx % Kp2, r = idx / Kp2;
   int qq = int(r % 2), c0 = int((r / 2) % 2), ri = int((r / 4) % 2);
   long n = r / 8;
   float x = 0.f;
-  if (w < nw) x = float(D[w + long(nwp) * ((qq == 0 ? 0 : 2) + 6 * (c0 + 2 * ri)) + 24l * nwp * n]);
+  if (w < nw) x = float(D[z * 24 * nwp + w + long(nwp) * ((qq == 0 ? 0 : 2) + 6 * (c0 + 2 * ri)) + ldD * n]);
   __nv_bfloat16 h = __float2bfloat16_rn(x);
-  Yh[idx] = h;
-  Yl[idx] = __float2bfloat16_rn(x - __bfloat162float(h));
+  const long o = z * 8 * N * Kp2 + idx;
+  Yh[o] = h;
+  Yl[o] = __float2bfloat16_rn(x - __bfloat162float(h));
 }
 
 __global__ void split_rows_plain_kernel(const double* __restrict__ S, long rows, long cols, long ld, long Kp,
@@ -581,17 +592,28 @@ __device__ __forceinline__ Cx<R> cxadd(Cx<R> a, Cx<R> b) {
   return {a.x + b.x, a.y + b.y};
 }
 
+// Batched over blockIdx.y: slot z reads rows z 24 nwp.. of D (column stride ldD) and KY + z nω 24ni,
+// and writes LJ + 24 nω ni r with the propagators Gm, Gp + 4 nω ni r of right-hand side r = rmap[z]
+// (r = z without rmap).
 template <class R>
-__global__ void finish_gemm_kernel(const double* __restrict__ D, const double* __restrict__ KY, const double2* __restrict__ Gm,
-                                   const double2* __restrict__ Gp, int nw, int nwp, int ni, double2* __restrict__ LJ) {
+__global__ void finish_gemm_kernel(const double* __restrict__ D_all, long ldD, const double* __restrict__ KY_all,
+                                   const double2* __restrict__ Gm_all, const double2* __restrict__ Gp_all,
+                                   const int* __restrict__ rmap, int nw, int nwp, int ni, double2* __restrict__ LJ_all) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= long(nw) * 6 * ni) return;
+  const long z = blockIdx.y;
+  const long rhs = rmap ? rmap[z] : z;
+  const double* D = D_all + z * 24 * nwp;
+  const double* KY = KY_all + z * long(nw) * 24 * ni;
+  const double2* Gm = Gm_all + rhs * 4l * nw * ni;
+  const double2* Gp = Gp_all + rhs * 4l * nw * ni;
+  double2* LJ = LJ_all + rhs * 24l * nw * ni;
   long w = idx % nw;
   long r = idx / nw;
   int a = int(r % 3), c0 = int((r / 3) % 2);
   long i = r / 6;
   const long n = a + 3 * i;
-  auto d = [&](int q, int ri) { return R(D[w + long(nwp) * (q + 6 * (c0 + 2 * ri)) + 24l * nwp * n]); };
+  auto d = [&](int q, int ri) { return R(D[w + long(nwp) * (q + 6 * (c0 + 2 * ri)) + ldD * n]); };
   auto ky = [&](int qq, int ri) { return R(KY[w + nw * (qq + 2 * (c0 + 2 * (ri + 2 * n)))]); };
   Cx<R> K[4];
   {
@@ -1105,15 +1127,16 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ) {
   } else {
     long px = prof_begin(ctx, "xgen");
     const unsigned ktiles = unsigned((P->Kp / 64 + kXgTiles - 1) / kXgTiles);
-    xgen_bf16_kernel<<<dim3(unsigned(nwp / 32 * 8), ktiles), 256, xgen_smem_bytes(int(ns)), s>>>(
-        J, P->d_mt_k.p, P->d_mt_w.p, P->d_nnu_f.p, int(nw), int(nwp), int(ns), int(P->nmp), int(ni), P->Kx, P->Kp, P->d_Ah.p,
-        P->d_Al.p);
+    xgen_bf16_kernel<<<dim3(unsigned(nwp / 32 * 8), ktiles, 1), 256, xgen_smem_bytes(int(ns)), s>>>(
+        J, 0, nullptr, P->d_mt_k.p, P->d_mt_w.p, P->d_nnu_f.p, int(nw), int(nwp), int(ns), int(P->nmp), int(ni), P->Kx,
+        P->Kp, P->d_Ah.p, P->d_Al.p);
     EPSP_LAUNCHED(ctx);
     prof_end(ctx, px);
     int sp = tc_gemm_launch(ctx, P->opA, P->opG, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N, 16, P->d_err.p, "tc_ladder");
     sum_parts_kernel<<<div_up(size_t(M * N), 256), 256, 0, s>>>(P->d_part.p, M * N, sp, M * N, P->d_D.p);
     EPSP_LAUNCHED(ctx);
-    y_split_kernel<<<div_up(size_t(8 * N * P->Kp2), 256), 256, 0, s>>>(P->d_D.p, int(nw), int(nwp), N, P->Kp2, P->d_Yh.p, P->d_Yl.p);
+    y_split_kernel<<<dim3(div_up(size_t(8 * N * P->Kp2), 256), 1), 256, 0, s>>>(P->d_D.p, M, int(nw), int(nwp), N, P->Kp2,
+                                                                               P->d_Yh.p, P->d_Yl.p);
     EPSP_LAUNCHED(ctx);
     int sp2 = tc_gemm_launch(ctx, P->opKK, P->opY, int(nw), int(8 * N), int(nw), P->d_part2.p, nw, nw * 8 * N, 16, P->d_err.p,
                              "tc_ladder_kk");
@@ -1121,11 +1144,11 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ) {
     EPSP_LAUNCHED(ctx);
   }
   if (P->path == EPSP_PATH_GEMM_BF16)
-    finish_gemm_kernel<float><<<div_up(size_t(nw * 6 * ni), 256), 256, 0, s>>>(P->d_D.p, P->d_KY.p, P->d_Gm.p, P->d_Gp.p,
-                                                                              int(nw), int(nwp), int(ni), LJ);
+    finish_gemm_kernel<float><<<dim3(div_up(size_t(nw * 6 * ni), 256), 1), 256, 0, s>>>(
+        P->d_D.p, M, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ);
   else
-    finish_gemm_kernel<double><<<div_up(size_t(nw * 6 * ni), 256), 256, 0, s>>>(P->d_D.p, P->d_KY.p, P->d_Gm.p, P->d_Gp.p,
-                                                                               int(nw), int(nwp), int(ni), LJ);
+    finish_gemm_kernel<double><<<dim3(div_up(size_t(nw * 6 * ni), 256), 1), 256, 0, s>>>(
+        P->d_D.p, M, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ);
   EPSP_LAUNCHED(ctx);
 }
 
@@ -1250,6 +1273,7 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
         if (!solved) {
           if (V.empty()) V.emplace_back();
           if (V[0].n != size_t(n)) V[0].alloc(ctx, size_t(n));
+          V[0].zero(s);
           axpby_kernel<<<eb, 256, 0, s>>>(make_double2(1.0 / rNorm, 0), W.p, make_double2(0, 0), V[0].p, n);
           EPSP_LAUNCHED(ctx);
           z.push_back(beta);
@@ -1307,6 +1331,7 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
             if (!(solved || tired || breakdown)) {
               if (V.size() < size_t(inner + 1)) V.emplace_back();
               if (V[size_t(inner)].n != size_t(n)) V[size_t(inner)].alloc(ctx, size_t(n));
+              V[size_t(inner)].zero(s);
               axpby_kernel<<<eb, 256, 0, s>>>(make_double2(1.0 / Hbis, 0), W.p, make_double2(0, 0), V[size_t(inner)].p, n);
               EPSP_LAUNCHED(ctx);
               z.push_back(zeta);
@@ -1380,6 +1405,544 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// (T, Ω) pairs as simultaneous right-hand sides (GEMM_BF16)
+// ---------------------------------------------------------------------------------------------
+
+struct PairParams {
+  double mu, T, Om;
+  int iT, pad;
+};
+
+// contour_greens! of every pair of the batch: slot z uses Σ of temperature pp[z].iT, its own
+// interpolation tables [z][nω] and writes Gm, Gp + 4 nω ni z.
+__global__ void propagators_batch_kernel(const double2* __restrict__ S_all, const double* __restrict__ ws, int nw,
+                                         const int32_t* __restrict__ jm_all, const double* __restrict__ tm_all,
+                                         const int32_t* __restrict__ jp_all, const double* __restrict__ tp_all,
+                                         const double* __restrict__ eps_i, const PairParams* __restrict__ pp,
+                                         double2* __restrict__ Gm_all, double2* __restrict__ Gp_all, int ni) {
+  int w = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y;
+  const long z = blockIdx.z;
+  if (w >= nw) return;
+  const PairParams q = pp[z];
+  const double2* col = S_all + long(nw) * ni * q.iT + long(nw) * i;
+  for (int side = 0; side < 2; ++side) {
+    int j = side == 0 ? jm_all[z * nw + w] : jp_all[z * nw + w];
+    double t = side == 0 ? tm_all[z * nw + w] : tp_all[z * nw + w];
+    double2 lo = col[j], hi = col[j + 1];
+    double sr = (1 - t) * lo.x + t * hi.x, si = (1 - t) * lo.y + t * hi.y;
+    double x = side == 0 ? ws[w] - q.Om / 2 : ws[w] + q.Om / 2;
+    double2 GR = cinv_d(x - eps_i[i] - sr, -si);
+    double2 GA = make_double2(GR.x, -GR.y);
+    double fac = 1 - 2 * occ_fermion_d(x - q.mu, q.T);
+    double2 GK = cscale(csub(GR, GA), fac);
+    double2 g[4] = {cscale(cadd(cadd(GR, GA), GK), 0.5), cscale(cadd(csub(GR, GA), GK), 0.5),
+                    cscale(cadd(csub(GA, GR), GK), 0.5), cscale(csub(csub(GK, GR), GA), 0.5)};
+    double2* G = (side == 0 ? Gm_all : Gp_all) + z * 4l * nw * ni;
+    for (int c = 0; c < 4; ++c) G[w + long(nw) * (c + 4 * i)] = g[c];
+  }
+}
+
+__global__ void attach_bare_batch_kernel(const double2* __restrict__ Gm_all, const double2* __restrict__ Gp_all,
+                                         const double* __restrict__ v, int nw, int ni, double2* __restrict__ J0_all) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  const long n = long(nw) * 24 * ni;
+  if (idx >= n) return;
+  const long z = blockIdx.y;
+  const double2* Gm = Gm_all + z * 4l * nw * ni;
+  const double2* Gp = Gp_all + z * 4l * nw * ni;
+  long w = idx % nw;
+  long r = idx / nw;
+  int c12 = int(r % 4), cart = int((r / 4) % 3), c0 = int((r / 12) % 2);
+  long i = r / 24;
+  int c1 = c12 % 2, c2 = c12 / 2;
+  double2 a = Gm[w + long(nw) * (c1 + 2 * c0 + 4 * i)];
+  double2 b = Gp[w + long(nw) * (c0 + 2 * c2 + 4 * i)];
+  J0_all[z * n + idx] = cmul(cscale(a, v[cart + 3 * i]), b);
+}
+
+__global__ void __launch_bounds__(256) cond_sum_batch_kernel(const double2* __restrict__ J_all, const double* __restrict__ Ww,
+                                                             int nw, int ni, double2* __restrict__ Y_all) {
+  __shared__ double sr[256], si[256];
+  const long z = blockIdx.y;
+  const double2* J = J_all + z * 24l * nw * ni;
+  int b = blockIdx.x % 3;
+  long i = blockIdx.x / 3;
+  double ar = 0, ai = 0;
+  for (int w = threadIdx.x; w < nw; w += 256) {
+    double2 x = J[jidx(nw, w, 3, b, 0, i)], y = J[jidx(nw, w, 0, b, 1, i)];
+    ar += Ww[w] * (x.x + y.x);
+    ai += Ww[w] * (x.y + y.y);
+  }
+  sr[threadIdx.x] = ar;
+  si[threadIdx.x] = ai;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      sr[threadIdx.x] += sr[threadIdx.x + st];
+      si[threadIdx.x] += si[threadIdx.x + st];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) Y_all[z * 3 * ni + b + 3 * i] = make_double2(sr[0], si[0]);
+}
+
+// Batched BLAS-1 over the right-hand sides r = rmap[z] of vectors stored [r][n].
+constexpr int kDotBlocksB = 256;
+
+__global__ void __launch_bounds__(256) dot_partial_batch_kernel(const double2* __restrict__ U, const double2* __restrict__ V,
+                                                                long n, const int* __restrict__ rmap,
+                                                                double2* __restrict__ part) {
+  __shared__ double sr[256], si[256];
+  const long r = rmap[blockIdx.y];
+  const double2* u = U + n * r;
+  const double2* v = V + n * r;
+  double ar = 0, ai = 0;
+  for (long k = long(blockIdx.x) * 256 + threadIdx.x; k < n; k += long(gridDim.x) * 256) {
+    double2 a = u[k], b = v[k];
+    ar += a.x * b.x + a.y * b.y;  // conj(a) b
+    ai += a.x * b.y - a.y * b.x;
+  }
+  sr[threadIdx.x] = ar;
+  si[threadIdx.x] = ai;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      sr[threadIdx.x] += sr[threadIdx.x + st];
+      si[threadIdx.x] += si[threadIdx.x + st];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[long(blockIdx.y) * gridDim.x + blockIdx.x] = make_double2(sr[0], si[0]);
+}
+
+// out[rmap[z]] = Σ_b part[z][b] in order.
+__global__ void __launch_bounds__(256) dot_final_batch_kernel(const double2* __restrict__ part, int np,
+                                                              const int* __restrict__ rmap, double2* __restrict__ out) {
+  __shared__ double sr[256], si[256];
+  double ar = 0, ai = 0;
+  for (int k = threadIdx.x; k < np; k += 256) {
+    ar += part[long(blockIdx.x) * np + k].x;
+    ai += part[long(blockIdx.x) * np + k].y;
+  }
+  sr[threadIdx.x] = ar;
+  si[threadIdx.x] = ai;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      sr[threadIdx.x] += sr[threadIdx.x + st];
+      si[threadIdx.x] += si[threadIdx.x + st];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[rmap[blockIdx.x]] = make_double2(sr[0], si[0]);
+}
+
+// Q[r] -= h[r] V[r].
+__global__ void axpy_batch_kernel(double2* __restrict__ Q, const double2* __restrict__ V, const double2* __restrict__ h,
+                                  long n, const int* __restrict__ rmap) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const long r = rmap[blockIdx.y];
+  const double2 hh = h[r], x = V[n * r + k];
+  double2 q = Q[n * r + k];
+  Q[n * r + k] = make_double2(q.x - (hh.x * x.x - hh.y * x.y), q.y - (hh.x * x.y + hh.y * x.x));
+}
+
+// Y[r] = a[r] X[r] + b[r] Y[r] (complex a, b per right-hand side).
+__global__ void axpby_batch_kernel(const double2* __restrict__ a, const double2* __restrict__ X, const double2* __restrict__ b,
+                                   double2* __restrict__ Y, long n, const int* __restrict__ rmap) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const long r = rmap[blockIdx.y];
+  const double2 aa = a[r], bb = b[r], xv = X[n * r + k], yv = Y[n * r + k];
+  Y[n * r + k] = make_double2(aa.x * xv.x - aa.y * xv.y + bb.x * yv.x - bb.y * yv.y,
+                              aa.x * xv.y + aa.y * xv.x + bb.x * yv.y + bb.y * yv.x);
+}
+
+// Y[r] = a[r] X[r] (Y is not read).
+__global__ void scale_batch_kernel(const double2* __restrict__ a, const double2* __restrict__ X, double2* __restrict__ Y,
+                                   long n, const int* __restrict__ rmap) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const long r = rmap[blockIdx.y];
+  const double2 aa = a[r], xv = X[n * r + k];
+  Y[n * r + k] = make_double2(aa.x * xv.x - aa.y * xv.y, aa.x * xv.y + aa.y * xv.x);
+}
+
+__global__ void sub_batch_kernel(const double2* __restrict__ X, const double2* __restrict__ Y, double2* __restrict__ O, long n,
+                                 const int* __restrict__ rmap) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const long r = rmap[blockIdx.y];
+  const double2 x = X[n * r + k], y = Y[n * r + k];
+  O[n * r + k] = make_double2(x.x - y.x, x.y - y.y);
+}
+
+// Buffers of a batch of right-hand sides (capacity cap), tensor maps over them.
+struct LadderBatch {
+  long cap = 0;
+  DBuf<__nv_bfloat16> Ah, Al, Yh, Yl;
+  DBuf<float> part, part2, nnu;
+  DBuf<double> D, KY;
+  DBuf<double2> Gm, Gp, J0, J, LJ, W, dpart, H, coef_a, coef_b;
+  std::vector<DBuf<double2>> V;
+  DBuf<int32_t> jm, jp;
+  DBuf<double> tm, tp;
+  DBuf<PairParams> pp;
+  DBuf<int> rmap;
+  DBuf<double2> Y;
+  TcOperand opA{}, opY{};
+};
+
+static void batch_reserve(LadderPlan* P, LadderBatch& B, long R, int maxiter) {
+  Ctx* ctx = P->ctx;
+  const long nw = P->nw, ni = P->ni, nwp = P->nwp, M = 24 * nwp, N = 3 * ni, n = nw * 24 * ni;
+  B.cap = R;
+  B.Ah.alloc(ctx, size_t(R * M * P->Kp));
+  B.Al.alloc(ctx, size_t(R * M * P->Kp));
+  B.Yh.alloc(ctx, size_t(R * 8 * N * P->Kp2));
+  B.Yl.alloc(ctx, size_t(R * 8 * N * P->Kp2));
+  size_t p1 = 0, p2 = 0;
+  for (long a = 1; a <= R; ++a) {
+    int bn, sp1, sp2;
+    tc_gemm_shape(ctx, int(a * M), int(N), int(P->Kx), 16, 2, &bn, &sp1);
+    tc_gemm_shape(ctx, int(nw), int(a * 8 * N), int(nw), 16, 2, &bn, &sp2);
+    p1 = std::max(p1, size_t(sp1) * size_t(a * M * N));
+    p2 = std::max(p2, size_t(sp2) * size_t(a * nw * 8 * N));
+  }
+  B.part.alloc(ctx, p1);
+  B.part2.alloc(ctx, p2);
+  B.nnu.alloc(ctx, size_t(16 * R));
+  B.D.alloc(ctx, size_t(R * M * N));
+  B.KY.alloc(ctx, size_t(R * nw * 8 * N));
+  B.Gm.alloc(ctx, size_t(R * 4 * nw * ni));
+  B.Gp.alloc(ctx, size_t(R * 4 * nw * ni));
+  for (auto* b : {&B.J0, &B.J, &B.LJ, &B.W}) b->alloc(ctx, size_t(R * n));
+  B.dpart.alloc(ctx, size_t(R * kDotBlocksB));
+  B.H.alloc(ctx, size_t(R * (maxiter + 2)));
+  B.coef_a.alloc(ctx, size_t(R));
+  B.coef_b.alloc(ctx, size_t(R));
+  B.jm.alloc(ctx, size_t(R * nw));
+  B.jp.alloc(ctx, size_t(R * nw));
+  B.tm.alloc(ctx, size_t(R * nw));
+  B.tp.alloc(ctx, size_t(R * nw));
+  B.pp.alloc(ctx, size_t(R));
+  B.rmap.alloc(ctx, size_t(R));
+  B.Y.alloc(ctx, size_t(R * 3 * ni));
+  B.opA = two_part(B.Ah.p, B.Al.p, R * M, P->Kx, P->Kp, kTcBM);
+  B.opY = two_part(B.Yh.p, B.Yl.p, R * 8 * N, nw, P->Kp2, P->bn2);
+}
+
+// LJ[r] = L(X[r]) for the nA right-hand sides listed in the device array rmap (host copy rmap_h).
+static void apply_L_batch(LadderPlan* P, LadderBatch& B, const double2* X, int nA, double2* LJ) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  const long nw = P->nw, ni = P->ni, ns = P->nshift, nwp = P->nwp, M = 24 * nwp, N = 3 * ni, n = nw * 24 * ni;
+  const long Mt = M * nA;
+  long px = prof_begin(ctx, "xgen");
+  const unsigned ktiles = unsigned((P->Kp / 64 + kXgTiles - 1) / kXgTiles);
+  xgen_bf16_kernel<<<dim3(unsigned(nwp / 32 * 8), ktiles, unsigned(nA)), 256, xgen_smem_bytes(int(ns)), s>>>(
+      X, n, B.rmap.p, P->d_mt_k.p, P->d_mt_w.p, B.nnu.p, int(nw), int(nwp), int(ns), int(P->nmp), int(ni), P->Kx, P->Kp,
+      B.Ah.p, B.Al.p);
+  EPSP_LAUNCHED(ctx);
+  prof_end(ctx, px);
+  int sp = tc_gemm_launch(ctx, B.opA, P->opG, int(Mt), int(N), int(P->Kx), B.part.p, Mt, Mt * N, 16, P->d_err.p, "tc_ladder");
+  sum_parts_kernel<<<div_up(size_t(Mt * N), 256), 256, 0, s>>>(B.part.p, Mt * N, sp, Mt * N, B.D.p);
+  EPSP_LAUNCHED(ctx);
+  y_split_kernel<<<dim3(div_up(size_t(8 * N * P->Kp2), 256), unsigned(nA)), 256, 0, s>>>(B.D.p, Mt, int(nw), int(nwp), N,
+                                                                                        P->Kp2, B.Yh.p, B.Yl.p);
+  EPSP_LAUNCHED(ctx);
+  const long N2 = 8 * N * nA;
+  int sp2 = tc_gemm_launch(ctx, P->opKK, B.opY, int(nw), int(N2), int(nw), B.part2.p, nw, nw * N2, 16, P->d_err.p,
+                           "tc_ladder_kk");
+  sum_parts_kernel<<<div_up(size_t(nw * N2), 256), 256, 0, s>>>(B.part2.p, nw * N2, sp2, nw * N2, B.KY.p);
+  EPSP_LAUNCHED(ctx);
+  finish_gemm_kernel<float><<<dim3(div_up(size_t(nw * 6 * ni), 256), unsigned(nA)), 256, 0, s>>>(
+      B.D.p, Mt, B.KY.p, B.Gm.p, B.Gp.p, B.rmap.p, int(nw), int(nwp), int(ni), LJ);
+  EPSP_LAUNCHED(ctx);
+}
+
+// σ of every pair of the batch from the vertices J[z] (conductivity_from_vertex).
+static void conductivity_batch(LadderPlan* P, LadderBatch& B, const double2* J, int nP, const std::vector<PairParams>& pp,
+                               double* sigma_base, const std::vector<long>& idx) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  const long nw = P->nw, ni = P->ni;
+  cond_sum_batch_kernel<<<dim3(unsigned(3 * ni), unsigned(nP)), 256, 0, s>>>(J, P->d_Ww.p, int(nw), int(ni), B.Y.p);
+  EPSP_LAUNCHED(ctx);
+  std::vector<double2> Y(static_cast<size_t>(3 * ni * nP));
+  B.Y.download(Y.data(), Y.size(), s);
+  EPSP_CUDA(cudaStreamSynchronize(s));
+  for (int z = 0; z < nP; ++z) {
+    const double T = pp[size_t(z)].T, Om = pp[size_t(z)].Om;
+    cplx F = Om == 0 ? cplx(0, 1) / (4 * T)
+                     : -1.0 / (cplx(0, 2) * Om * (1 + 2 * (T > 1.4901161193847656e-08 ? 1.0 / std::expm1(Om / T) : 0.0)));
+    double* sig = sigma_base + 9 * idx[size_t(z)];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) {
+        cplx S = 0;
+        for (long i = 0; i < ni; ++i) {
+          const double2 y = Y[size_t(3 * ni * z + b + 3 * i)];
+          S += (P->v_h[size_t(a + 3 * i)] * P->w_i_h[size_t(i)]) * cplx(y.x, y.y);
+        }
+        sig[a + 3 * b] = (F / (2 * 3.14159265358979323846 * cplx(0, 1)) * S).real();
+      }
+  }
+}
+
+// Host state of one right-hand side's GMRES (the recurrences of the sequential solver).
+struct GmresState {
+  double atol = 0, rNorm = 0;
+  std::vector<double> res;
+  std::vector<cplx> R, sv, z;
+  std::vector<double> cv;
+  int inner = 0, nr = 0;
+  bool solved = false, tired = false, breakdown = false, active = false;
+};
+
+void ladder_run_batched(LadderPlan* P, const double* sigma, const double* mu, const double* Tlist, int64_t nT,
+                        const double* Omegas, int64_t nO, double rtol, int32_t maxiter, int32_t max_rhs, double* sb,
+                        double* sl, uint8_t* conv, int32_t* niter, epsp_ladder_history* hist, double* J_out) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  if (P->path != EPSP_PATH_GEMM_BF16) fail(EPSP_EUNSUPPORTED, "batched right-hand sides need a GEMM_BF16 ladder plan");
+  if (maxiter < 1) fail(EPSP_EINVAL, "maxiter must be at least 1, got " + std::to_string(maxiter));
+  if (max_rhs < 1) fail(EPSP_EINVAL, "max_rhs must be at least 1");
+  if (nO < 1) fail(EPSP_EINVAL, "Omegas must hold at least one probe frequency");
+  if (nT < 1 || !sigma || !mu || !Tlist || !Omegas || !sb || !sl || !conv || !niter) fail(EPSP_EINVAL, "an input or output array is NULL");
+  for (int64_t iT = 0; iT < nT; ++iT)
+    if (!(Tlist[iT] >= 0)) fail(EPSP_EINVAL, "Temperature must be positive");
+  const long nw = P->nw, ni = P->ni, slab = nw * ni, n = nw * 24 * ni;
+  const long nPairs = nT * nO;
+  const long R = std::min<long>(max_rhs, nPairs);
+  LadderBatch B;
+  batch_reserve(P, B, R, maxiter);
+  DBuf<double2> S_all;
+  S_all.alloc(ctx, size_t(slab * nT));
+  S_all.upload(reinterpret_cast<const double2*>(sigma), size_t(slab * nT), s);
+  const double btol = std::pow(std::numeric_limits<double>::epsilon(), 0.75);
+  const unsigned eb = div_up(size_t(n), 256);
+  auto dot_batch = [&](const double2* U, const double2* V, int nA, double2* out) {
+    dot_partial_batch_kernel<<<dim3(kDotBlocksB, unsigned(nA)), 256, 0, s>>>(U, V, n, B.rmap.p, B.dpart.p);
+    EPSP_LAUNCHED(ctx);
+    dot_final_batch_kernel<<<unsigned(nA), 256, 0, s>>>(B.dpart.p, kDotBlocksB, B.rmap.p, out);
+    EPSP_LAUNCHED(ctx);
+  };
+  auto set_rmap = [&](const std::vector<int>& rm) { B.rmap.upload(rm.data(), rm.size(), s); };
+  for (long p0 = 0; p0 < nPairs; p0 += R) {
+    const int nP = int(std::min<long>(R, nPairs - p0));
+    std::vector<PairParams> pp(static_cast<size_t>(nP));
+    std::vector<long> idx(static_cast<size_t>(nP));
+    std::vector<int32_t> jm(static_cast<size_t>(nP * nw)), jp(static_cast<size_t>(nP * nw));
+    std::vector<double> tm(static_cast<size_t>(nP * nw)), tp(static_cast<size_t>(nP * nw));
+    std::vector<float> nnu(static_cast<size_t>(16 * nP), 0.f);
+    for (int z = 0; z < nP; ++z) {
+      const long pidx = p0 + z;  // = iO + nO iT
+      const int iT = int(pidx / nO), iO = int(pidx % nO);
+      const double T = Tlist[iT], Om = Omegas[iO];
+      pp[size_t(z)] = PairParams{mu[iT], T, Om, iT, 0};
+      idx[size_t(z)] = pidx;
+      std::vector<double> xm(static_cast<size_t>(nw)), xp(static_cast<size_t>(nw)), t1, t2;
+      std::vector<int32_t> j1, j2;
+      for (long k = 0; k < nw; ++k) {
+        xm[size_t(k)] = P->ws.nodes[size_t(k)] - Om / 2;
+        xp[size_t(k)] = P->ws.nodes[size_t(k)] + Om / 2;
+      }
+      interp_table(P->ws.nodes, xm, j1, t1);
+      interp_table(P->ws.nodes, xp, j2, t2);
+      std::copy(j1.begin(), j1.end(), jm.begin() + z * nw);
+      std::copy(j2.begin(), j2.end(), jp.begin() + z * nw);
+      std::copy(t1.begin(), t1.end(), tm.begin() + z * nw);
+      std::copy(t2.begin(), t2.end(), tp.begin() + z * nw);
+      for (long nu = 0; nu < P->nm && nu < 16; ++nu) {
+        const double w = P->wnu[size_t(nu)];
+        nnu[size_t(16 * z + nu)] = float(w < P->w_ac ? 0.0
+                                                     : (T > 1.4901161193847656e-08 ? (w == 0 ? -0.5 : 1.0 / std::expm1(w / T))
+                                                                                   : (w > 0 ? 0.0 : -1.0)));
+      }
+    }
+    B.jm.upload(jm.data(), jm.size(), s);
+    B.jp.upload(jp.data(), jp.size(), s);
+    B.tm.upload(tm.data(), tm.size(), s);
+    B.tp.upload(tp.data(), tp.size(), s);
+    B.nnu.upload(nnu.data(), nnu.size(), s);
+    B.pp.upload(pp.data(), pp.size(), s);
+    propagators_batch_kernel<<<dim3(div_up(size_t(nw), 128), unsigned(ni), unsigned(nP)), 128, 0, s>>>(
+        S_all.p, P->d_ws.p, int(nw), B.jm.p, B.tm.p, B.jp.p, B.tp.p, P->d_eps_i.p, B.pp.p, B.Gm.p, B.Gp.p, int(ni));
+    EPSP_LAUNCHED(ctx);
+    attach_bare_batch_kernel<<<dim3(eb, unsigned(nP)), 256, 0, s>>>(B.Gm.p, B.Gp.p, P->d_v.p, int(nw), int(ni), B.J0.p);
+    EPSP_LAUNCHED(ctx);
+    conductivity_batch(P, B, B.J0.p, nP, pp, sb, idx);
+    // GMRES per right-hand side from x0 = 0: r0 = J0, ‖J0‖ gives atol and β
+    std::vector<int> all(static_cast<size_t>(nP));
+    for (int z = 0; z < nP; ++z) all[size_t(z)] = z;
+    set_rmap(all);
+    dot_batch(B.J0.p, B.J0.p, nP, B.H.p);
+    std::vector<double2> h(static_cast<size_t>(nP));
+    B.H.download(h.data(), size_t(nP), s);
+    EPSP_CUDA(cudaStreamSynchronize(s));
+    std::vector<GmresState> g(static_cast<size_t>(nP));
+    std::vector<int> act;
+    std::vector<double2> ca(static_cast<size_t>(nP)), cb(static_cast<size_t>(nP));
+    for (int z = 0; z < nP; ++z) {
+      GmresState& q = g[size_t(z)];
+      const double beta = std::sqrt(h[size_t(z)].x);
+      q.atol = rtol * beta;
+      q.rNorm = beta;
+      q.res.push_back(beta);
+      q.solved = beta <= q.atol || beta == 0;
+      if (!q.solved) {
+        q.active = true;
+        q.z.push_back(beta);
+        act.push_back(z);
+        ca[size_t(z)] = make_double2(1.0 / beta, 0);
+      } else {
+        ca[size_t(z)] = make_double2(0, 0);
+      }
+      cb[size_t(z)] = make_double2(0, 0);
+    }
+    if (B.V.empty()) B.V.emplace_back();
+    if (B.V[0].n != size_t(R * n)) B.V[0].alloc(ctx, size_t(R * n));
+    // V0 = J0 / β (every slot; solved ones get 0)
+    B.coef_a.upload(ca.data(), ca.size(), s);
+    scale_batch_kernel<<<dim3(eb, unsigned(nP)), 256, 0, s>>>(B.coef_a.p, B.J0.p, B.V[0].p, n, B.rmap.p);
+    EPSP_LAUNCHED(ctx);
+    int k = 0;
+    while (!act.empty()) {
+      ++k;
+      const int nA = int(act.size());
+      set_rmap(act);
+      apply_L_batch(P, B, B.V[size_t(k - 1)].p, nA, B.LJ.p);  // LJ[r] = L(v_k)
+      sub_batch_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(B.V[size_t(k - 1)].p, B.LJ.p, B.W.p, n, B.rmap.p);
+      EPSP_LAUNCHED(ctx);
+      for (int i = 0; i < k; ++i) {
+        dot_batch(B.V[size_t(i)].p, B.W.p, nA, B.H.p + long(i) * R);
+        axpy_batch_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(B.W.p, B.V[size_t(i)].p, B.H.p + long(i) * R, n, B.rmap.p);
+        EPSP_LAUNCHED(ctx);
+      }
+      dot_batch(B.W.p, B.W.p, nA, B.H.p + long(k) * R);
+      std::vector<double2> hall(static_cast<size_t>((k + 1) * R));
+      B.H.download(hall.data(), hall.size(), s);
+      EPSP_CUDA(cudaStreamSynchronize(s));
+      check_tc_err(P);
+      std::vector<int> next;
+      for (int z : act) {
+        GmresState& q = g[size_t(z)];
+        q.inner = k;
+        for (int i = 0; i < k; ++i) q.R.push_back(cplx(hall[size_t(i * R + z)].x, hall[size_t(i * R + z)].y));
+        const double Hbis = std::sqrt(hall[size_t(k * R + z)].x);
+        for (int i = 0; i < k - 1; ++i) {
+          cplx Rt = q.cv[size_t(i)] * q.R[size_t(q.nr + i)] + q.sv[size_t(i)] * q.R[size_t(q.nr + i + 1)];
+          q.R[size_t(q.nr + i + 1)] = std::conj(q.sv[size_t(i)]) * q.R[size_t(q.nr + i)] - q.cv[size_t(i)] * q.R[size_t(q.nr + i + 1)];
+          q.R[size_t(q.nr + i)] = Rt;
+        }
+        cplx a = q.R[size_t(q.nr + k - 1)];
+        double abs_a = std::abs(a), cc;
+        cplx ss, rho;
+        if (Hbis == 0) {
+          cc = 1;
+          ss = 0;
+          rho = a;
+        } else if (abs_a == 0) {
+          cc = 0;
+          ss = 1;
+          rho = Hbis;
+        } else {
+          double rr = std::hypot(abs_a, Hbis);
+          cplx psi = a / abs_a;
+          cc = abs_a / rr;
+          ss = psi * (Hbis / rr);
+          rho = psi * rr;
+        }
+        q.cv.push_back(cc);
+        q.sv.push_back(ss);
+        q.R[size_t(q.nr + k - 1)] = rho;
+        cplx zeta = std::conj(ss) * q.z[size_t(k - 1)];
+        q.z[size_t(k - 1)] = cc * q.z[size_t(k - 1)];
+        q.rNorm = std::abs(zeta);
+        q.res.push_back(q.rNorm);
+        q.nr += k;
+        q.solved = q.rNorm <= q.atol || q.rNorm + 1.0 <= 1.0;
+        q.breakdown = Hbis <= btol;
+        q.tired = k >= maxiter;
+        if (!(q.solved || q.tired || q.breakdown)) {
+          q.z.push_back(zeta);
+          next.push_back(z);
+          ca[size_t(z)] = make_double2(1.0 / Hbis, 0);
+        } else {
+          q.active = false;
+        }
+      }
+      act = next;
+      if (!act.empty()) {
+        if (B.V.size() < size_t(k + 1)) B.V.emplace_back();
+        if (B.V[size_t(k)].n != size_t(R * n)) B.V[size_t(k)].alloc(ctx, size_t(R * n));
+        set_rmap(act);
+        B.coef_a.upload(ca.data(), ca.size(), s);
+        scale_batch_kernel<<<dim3(eb, unsigned(act.size())), 256, 0, s>>>(B.coef_a.p, B.W.p, B.V[size_t(k)].p, n, B.rmap.p);
+        EPSP_LAUNCHED(ctx);
+      }
+    }
+    // x = Σ_i y_i v_i per right-hand side (x0 = 0)
+    B.J.zero(s);
+    const int kmax = k;
+    std::vector<std::vector<cplx>> ys(static_cast<size_t>(nP));
+    for (int z = 0; z < nP; ++z) {
+      GmresState& q = g[size_t(z)];
+      std::vector<cplx> y = q.z;
+      const int inner = q.inner;
+      for (int i = inner - 1; i >= 0; --i) {
+        int pos = q.nr + i - inner;
+        for (int jj = inner - 1; jj >= i + 1; --jj) {
+          y[size_t(i)] -= q.R[size_t(pos)] * y[size_t(jj)];
+          pos -= jj;
+        }
+        if (std::abs(q.R[size_t(pos)]) <= btol)
+          y[size_t(i)] = 0;
+        else
+          y[size_t(i)] /= q.R[size_t(pos)];
+      }
+      ys[size_t(z)] = y;
+    }
+    for (int i = 0; i < kmax; ++i) {
+      std::vector<int> use;
+      for (int z = 0; z < nP; ++z) {
+        if (g[size_t(z)].inner > i) {
+          use.push_back(z);
+          ca[size_t(z)] = make_double2(ys[size_t(z)][size_t(i)].real(), ys[size_t(z)][size_t(i)].imag());
+          cb[size_t(z)] = make_double2(1, 0);
+        }
+      }
+      if (use.empty()) continue;
+      set_rmap(use);
+      B.coef_a.upload(ca.data(), ca.size(), s);
+      B.coef_b.upload(cb.data(), cb.size(), s);
+      axpby_batch_kernel<<<dim3(eb, unsigned(use.size())), 256, 0, s>>>(B.coef_a.p, B.V[size_t(i)].p, B.coef_b.p, B.J.p, n,
+                                                                         B.rmap.p);
+      EPSP_LAUNCHED(ctx);
+    }
+    conductivity_batch(P, B, B.J.p, nP, pp, sl, idx);
+    for (int z = 0; z < nP; ++z) {
+      const long pidx = idx[size_t(z)];
+      const GmresState& q = g[size_t(z)];
+      conv[pidx] = q.solved ? 1 : 0;
+      niter[pidx] = q.inner;
+      if (hist && hist->norms && hist->nnorms) {
+        int32_t nn = int32_t(std::min<size_t>(q.res.size(), size_t(maxiter + 1)));
+        for (int32_t kk = 0; kk < nn; ++kk) hist->norms[size_t(maxiter + 1) * size_t(pidx) + size_t(kk)] = q.res[size_t(kk)];
+        hist->nnorms[pidx] = nn;
+      }
+      if (hist && hist->nsigma) hist->nsigma[pidx] = 0;
+      if (J_out)
+        EPSP_CUDA(cudaMemcpyAsync(reinterpret_cast<double2*>(J_out) + size_t(n) * size_t(pidx), B.J.p + size_t(n) * size_t(z),
+                                  size_t(n) * sizeof(double2), cudaMemcpyDeviceToHost, s));
+    }
+    EPSP_CUDA(cudaStreamSynchronize(s));
+  }
+}
+
 }  // namespace epsp
 
 using namespace epsp;
@@ -1427,6 +1990,18 @@ epsp_status epsp_ladder_run(epsp_ladder_plan* plan, const double* sigma, const d
   return lguard(P->ctx, [&] {
     ladder_run(P, sigma, mu, Tlist, nT, Omegas, nOmega, solver, rtol, maxiter, sigma_bubble, sigma_ladder, converged, niter,
                hist, J_out);
+  });
+}
+
+epsp_status epsp_ladder_run_batched(epsp_ladder_plan* plan, const double* sigma, const double* mu, const double* Tlist,
+                                    int64_t nT, const double* Omegas, int64_t nOmega, double rtol, int32_t maxiter,
+                                    int32_t max_rhs, double* sigma_bubble, double* sigma_ladder, uint8_t* converged,
+                                    int32_t* niter, epsp_ladder_history* hist, double* J_out) {
+  if (!plan) return EPSP_EINVAL;
+  auto* P = reinterpret_cast<LadderPlan*>(plan);
+  return lguard(P->ctx, [&] {
+    ladder_run_batched(P, sigma, mu, Tlist, nT, Omegas, nOmega, rtol, maxiter, max_rhs, sigma_bubble, sigma_ladder,
+                       converged, niter, hist, J_out);
   });
 }
 

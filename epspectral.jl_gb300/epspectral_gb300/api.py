@@ -72,6 +72,9 @@ def lib():
         "epsp_ladder_run": (C.c_int, [vp, c_double_p, c_double_p, c_double_p, i64, c_double_p, i64, i32, d, i32,
                                       c_double_p, c_double_p, u8p, c_int32_p, P(epsp_ladder_history), c_double_p]),
         "epsp_ladder_apply": (C.c_int, [vp, c_double_p, d, d, d, c_double_p, c_double_p]),
+        "epsp_ladder_run_batched": (C.c_int, [vp, c_double_p, c_double_p, c_double_p, i64, c_double_p, i64, d, i32, i32,
+                                              c_double_p, c_double_p, u8p, c_int32_p, P(epsp_ladder_history),
+                                              c_double_p]),
         "epsp_warmstart_create": (C.c_int, [vp, i32, P(i32), P(vp)]),
         "epsp_warmstart_destroy": (None, [vp]),
         "epsp_warmstart_nparams": (i64, [vp]),
@@ -266,11 +269,18 @@ class LadderPlan:
         self.ctx.check(lib().epsp_ladder_setup(self.ctx.handle, C.byref(self.M.struct), C.byref(self.opts),
                                                C.byref(self.handle)))
 
-    def run(self, sigma, mu, Tlist, Omegas, *, solver="gmres", rtol=1e-2, maxiter=30, store_vertex=False):
-        """The (T, Ω) loops of _loop_ladder (src/ladder.jl:303-379)."""
+    def run(self, sigma, mu, Tlist, Omegas, *, solver="gmres", rtol=1e-2, maxiter=30, store_vertex=False,
+            batch_rhs=None):
+        """The (T, Ω) loops of _loop_ladder (src/ladder.jl:303-379).
+
+        batch_rhs = R solves up to R (T, Ω) pairs together as GMRES right-hand sides, each from
+        x0 = 0 (epsp_ladder_run_batched; GEMM_BF16 plans); None keeps the reference's order and
+        warm starts."""
         M = self.M
         if solver not in ("gmres", "fixed_point"):
             raise ArgumentError(f"solver must be :gmres or :fixed_point, got {solver}")
+        if batch_rhs is not None and solver != "gmres":
+            raise ArgumentError("batched right-hand sides need solver = :gmres")
         if maxiter < 1:
             raise ArgumentError(f"maxiter must be at least 1, got {maxiter}")
         Tlist = np.ascontiguousarray(Tlist, dtype=np.float64)
@@ -282,6 +292,13 @@ class LadderPlan:
         sig = as_complex_F(sigma, (M.nw, M.ni, nT))
         out = LadderOutputs(M.nw, M.ni, nT, len(Omegas), maxiter, store_vertex)
         s = {"gmres": abi.EPSP_SOLVER_GMRES, "fixed_point": abi.EPSP_SOLVER_FIXED_POINT}[solver]
+        if batch_rhs is not None:
+            self.ctx.check(lib().epsp_ladder_run_batched(self.handle, cptr(sig), ptr(mu), ptr(Tlist), nT, ptr(Omegas),
+                                                         len(Omegas), float(rtol), int(maxiter), int(batch_rhs),
+                                                         ptr(out.sigma_bubble), ptr(out.sigma_ladder),
+                                                         out.converged.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                                         ptr(out.niter, C.c_int32), C.byref(out.hist), out.J_ptr()))
+            return out.result()
         self.ctx.check(lib().epsp_ladder_run(self.handle, cptr(sig), ptr(mu), ptr(Tlist), nT, ptr(Omegas),
                                              len(Omegas), s, float(rtol), int(maxiter), ptr(out.sigma_bubble),
                                              ptr(out.sigma_ladder),

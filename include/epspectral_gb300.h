@@ -232,6 +232,19 @@ epsp_status epsp_ladder_run(epsp_ladder_plan* plan, const double* sigma, const d
                             double* sigma_ladder, uint8_t* converged, int32_t* niter,
                             epsp_ladder_history* hist, double* J_out);
 
+/* The (T, Ω) loops of _loop_ladder with the pairs solved together as right-hand sides of GMRES:
+ * up to max_rhs pairs (in the order idx = iΩ + nΩ iT) share every operator application -- their
+ * shifted-vertex operands are stacked into one tensor-core GEMM and one Kramers-Kronig GEMM -- and
+ * run their Arnoldi steps in lockstep, each stopping on its own test (atol = rtol ‖J0‖). Every pair
+ * starts from x0 = 0 (the reference warm-starts each Ω from the previous one, src/ladder.jl:340-353):
+ * σ agrees with epsp_ladder_run to the solver tolerance, niter and the residual history may differ.
+ * GMRES only; GEMM_BF16 plans only (EPSP_EUNSUPPORTED otherwise). Outputs as epsp_ladder_run. */
+epsp_status epsp_ladder_run_batched(epsp_ladder_plan* plan, const double* sigma, const double* mu,
+                                    const double* Tlist, int64_t nT, const double* Omegas, int64_t nOmega,
+                                    double rtol, int32_t maxiter, int32_t max_rhs, double* sigma_bubble,
+                                    double* sigma_ladder, uint8_t* converged, int32_t* niter,
+                                    epsp_ladder_history* hist, double* J_out);
+
 /* One application LJ = L(J) of the ladder kernel at temperature T, chemical potential mu and
  * probe frequency Omega, with sigma_T [nω, ni] complex the self-energy of that temperature:
  * apply_ladder_kernel! (src/ladder.jl:245-296) with the propagators of contour_greens!

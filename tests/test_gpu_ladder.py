@@ -112,3 +112,38 @@ def test_ladder_argument_checks(api, cc):
         api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], [], omega_acoustic=W_AC)
     with pytest.raises(ArgumentError):
         api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], [0.0], gpu_tile=0, omega_acoustic=W_AC)
+
+
+def test_batched_right_hand_sides_match_the_sequential_solves(api, oracle, cc):
+    # 2 temperatures x 3 Ωs = 6 (T, Ω) pairs solved together as GMRES right-hand sides, in batches
+    # of 4 (so one batch is partial), each from x0 = 0. Solved tightly (rtol 1e-9) the batched σ
+    # must equal the sequential tensor-core run's to 2e-5 relative (the operator's BF16 rounding,
+    # met along other Krylov paths) and the FP64 oracle's to 1e-4;
+    # at the loop's usual rtol 1e-2 each pair's σ_ladder must agree with the sequential one to the
+    # solver tolerance.
+    c = cc
+    s = c["setup"]
+    Omegas = [0.0, 0.05, 0.1]
+    plan = api.LadderPlan(s, path="gemm_bf16", omega_acoustic=W_AC)
+    tight = dict(rtol=1e-9, maxiter=60)
+    seq = plan.run(c["sigma"], c["mu"], c["Tlist"], Omegas, store_vertex=True, **tight)
+    bat = plan.run(c["sigma"], c["mu"], c["Tlist"], Omegas, batch_rhs=4, store_vertex=True, **tight)
+    assert bat["converged"].all() and seq["converged"].all()
+    assert rel(bat["sigma_bubble"], seq["sigma_bubble"]) <= 1e-12
+    assert rel(bat["sigma_ladder"], seq["sigma_ladder"]) <= 2e-5
+    ref = oracle.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], Omegas, solver="gmres", omega_acoustic=W_AC, **tight)
+    assert rel(bat["sigma_ladder"], ref["sigma_ladder"]) <= 1e-4
+    # the stored vertices: every pair's J equals the sequential solve's (both converged tightly)
+    for iT in range(2):
+        for iO in range(3):
+            assert rel(bat["J"][..., iO, iT], seq["J"][..., iO, iT]) <= 1e-4
+    loose_seq = plan.run(c["sigma"], c["mu"], c["Tlist"], Omegas, rtol=1e-2, maxiter=30)
+    loose_bat = plan.run(c["sigma"], c["mu"], c["Tlist"], Omegas, rtol=1e-2, maxiter=30, batch_rhs=8)
+    assert loose_bat["converged"].all()
+    for iT in range(2):
+        for iO in range(3):
+            a, b = loose_bat["sigma_ladder"][:, :, iO, iT], loose_seq["sigma_ladder"][:, :, iO, iT]
+            assert np.linalg.norm(a - b) <= 3e-2 * np.linalg.norm(b)
+    with pytest.raises(ArgumentError):
+        plan.run(c["sigma"], c["mu"], c["Tlist"], Omegas, solver="fixed_point", batch_rhs=4)
+    plan.close()
