@@ -278,6 +278,7 @@ def run_ours(args, world, rank, local):
     out["scgd0_iters_without_warm_start"] = int(r_cold["niter"])
     out["warm_start"] = warm_info
     out["ladder_s_per_omega"] = float(np.median(tl))
+    out["ladder_gemm_autotune"] = lp.gemm_config()
     out["ladder_gmres_iters"] = int(l["niter"][0, 0])
     out["gpu_launches"] = int(launches)
     # roofline of the dominant kernel: the ladder's tensor-core contraction
@@ -335,8 +336,50 @@ def run_ours(args, world, rank, local):
         max_abs_dsigma_without_warm_start_eV=float(np.max(np.abs(r_cold["sigma"] - r64["sigma"]))),
         abs_dmu_eV=float(abs(r["mu"][0] - r64["mu"][0])),
         rel_sigma_ladder=float(np.linalg.norm(l["sigma_ladder"] - l64["sigma_ladder"]) / np.linalg.norm(l64["sigma_ladder"])))
+    out["batched_c3"] = batched_c3(s, ctx, ws)
     out["cpu_baseline"] = cpu_baseline(s, T, r64, plain["fp64_scgd0_iters"], plain["fp64_ladder_gmres_iters"])
     print(json.dumps(out), flush=True)
+
+
+def batched_c3(s, ctx, ws) -> dict:
+    """The same model batched (8 temperatures 100-800 K, ladder at 32 Ωs on [0, 0.5] eV): scGD0 of
+    all temperatures in one run (one launch per kernel per iteration, learned warm start) against
+    the temperatures one by one, and the 256 (T, Ω) pairs as GMRES right-hand sides (batches of 8,
+    each from x0 = 0) against the reference's sequential order with warm starts. Device seconds."""
+    from epspectral_gb300 import api, synthetic
+    Ts = list(np.linspace(100.0, 800.0, 8) * synthetic.KELVIN)
+    Om = list(np.linspace(0.0, 0.5, 32))
+    mus = [synthetic.bare_mu(s, t, 1.0) for t in Ts]
+    occ8 = dict(Tlist=Ts, nlist=[0.0] * 8, nelec=1.0, spin_degeneracy=2.0, type="metal")
+    sp = api.Scgd0Plan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
+    sp.run(occ8, eta_init=ETA_INIT, tol=TOL, maxiter=MAXITER, mu_start=mus, warm=ws)  # warm-up
+    ctx.timer_begin()
+    r8 = sp.run(occ8, eta_init=ETA_INIT, tol=TOL, maxiter=MAXITER, mu_start=mus, warm=ws)
+    t_batched = ctx.timer_end() / 1e3
+    t_single, it_single = 0.0, []
+    for t, m in zip(Ts, mus):
+        o1 = dict(Tlist=[t], nlist=[0.0], nelec=1.0, spin_degeneracy=2.0, type="metal")
+        ctx.timer_begin()
+        r1 = sp.run(o1, eta_init=ETA_INIT, tol=TOL, maxiter=MAXITER, mu_start=[m], warm=ws)
+        t_single += ctx.timer_end() / 1e3
+        it_single.append(int(r1["iters_total"]))
+    sp.close()
+    lp = api.LadderPlan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
+    ctx.timer_begin()
+    lb = lp.run(r8["sigma"], r8["mu"], Ts, Om, rtol=L_RTOL, maxiter=L_MAXITER, batch_rhs=8)
+    t_lb = ctx.timer_end() / 1e3
+    ctx.timer_begin()
+    ls = lp.run(r8["sigma"], r8["mu"], Ts, Om, rtol=L_RTOL, maxiter=L_MAXITER)
+    t_ls = ctx.timer_end() / 1e3
+    lp.close()
+    rel = float(np.max(np.abs(lb["sigma_ladder"] - ls["sigma_ladder"])) / np.max(np.abs(ls["sigma_ladder"])))
+    return dict(workload="8 T (100-800 K) x 32 Omega (0-0.5 eV), same model",
+                scgd0_8T_batched_s=t_batched, scgd0_8T_iters=int(r8["iters_total"]),
+                scgd0_8T_one_by_one_s=t_single, scgd0_one_by_one_iters=it_single,
+                ladder_256_pairs_batched_s=t_lb, ladder_batched_s_per_omega=t_lb / 256,
+                ladder_256_pairs_sequential_s=t_ls, ladder_sequential_s_per_omega=t_ls / 256,
+                ladder_batched_vs_sequential_max_rel_dsigma=rel,
+                ladder_converged=bool(lb["converged"].all() and ls["converged"].all()))
 
 
 def cpu_samples(s, T, sigma, mu, reps=1):

@@ -74,8 +74,10 @@ struct LadderPlan {
   DBuf<__nv_bfloat16> d_Ah, d_Al, d_Gh, d_Gl;
   DBuf<float> d_part;
   DBuf<int> d_err;
-  TcOperand opA{}, opG{};
-  int bn = 128, splits = 1;
+  TcOperand opA{}, opG{}, opG128{}, opG256{};
+  int bn = 128, splits = 1;  // the contraction's tile shape, picked by the autotuner at setup
+  std::vector<TcTune> tune_all;
+  float tune_ms_heuristic = 0.f;
   // exchange (both paths)
   DBuf<double> d_Y, d_KY;
   // per (T, Ω)
@@ -975,12 +977,31 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       split_rows_plain_kernel<<<div_up(size_t(N * P->Kp), 256), 256, 0, s>>>(P->d_Gt.p, N, P->Kx, P->Kx, P->Kp, P->d_Gh.p,
                                                                               P->d_Gl.p);
       EPSP_LAUNCHED(ctx);
-      tc_gemm_shape(ctx, int(M), int(N), int(P->Kx), 16, 2, &P->bn, &P->splits);
-      P->d_part.alloc(ctx, size_t(P->splits) * size_t(M * N));
+      // the contraction's tile shape: the autotuner times the candidates on these operands (A
+      // zeroed) and keeps the fastest; the partial buffer holds the largest split count tried
+      int bn_h = 128, sp_h = 1;
+      tc_gemm_shape(ctx, int(M), int(N), int(P->Kx), 16, 2, &bn_h, &sp_h);
+      const int max_sp = 2 * std::max(tc_splits_for(ctx, int(M), int(N), int(P->Kx), 128),
+                                       tc_splits_for(ctx, int(M), int(N), int(P->Kx), 256));
+      P->d_part.alloc(ctx, size_t(max_sp) * size_t(M * N));
       P->d_err.alloc(ctx, 1);
       P->d_err.zero(s);
+      P->d_Ah.zero(s);
+      P->d_Al.zero(s);
       P->opA = two_part(P->d_Ah.p, P->d_Al.p, M, P->Kx, P->Kp, kTcBM);
-      P->opG = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, P->bn);
+      P->opG128 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 128);
+      P->opG256 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 256);
+      const TcTune best = tc_gemm_autotune(ctx, P->opA, P->opG128, P->opG256, int(M), int(N), int(P->Kx), P->d_part.p, M,
+                                           M * N, max_sp, P->d_err.p, 2, &P->tune_all);
+      for (const auto& c : P->tune_all)
+        if (c.bn == bn_h && c.splits == sp_h) P->tune_ms_heuristic = c.ms;
+      P->bn = best.bn;
+      P->splits = best.splits;
+      P->opG = P->bn == 256 ? P->opG256 : P->opG128;
+      int terr = 0;
+      P->d_err.download(&terr, 1, s);
+      EPSP_CUDA(cudaStreamSynchronize(s));
+      if (terr) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out while tuning (bounded device wait)");
       // the Kramers-Kronig image on the tensor cores: A = KK [nω][nω'], B = Y [8N][nω']
       P->d_KKh.alloc(ctx, size_t(nw * P->Kp2));
       P->d_KKl.alloc(ctx, size_t(nw * P->Kp2));
@@ -1132,7 +1153,8 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ) {
         P->Kp, P->d_Ah.p, P->d_Al.p);
     EPSP_LAUNCHED(ctx);
     prof_end(ctx, px);
-    int sp = tc_gemm_launch(ctx, P->opA, P->opG, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N, 16, P->d_err.p, "tc_ladder");
+    int sp = tc_gemm_launch_with(ctx, P->opA, P->opG, P->bn, P->splits, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N,
+                                 P->d_err.p, "tc_ladder");
     sum_parts_kernel<<<div_up(size_t(M * N), 256), 256, 0, s>>>(P->d_part.p, M * N, sp, M * N, P->d_D.p);
     EPSP_LAUNCHED(ctx);
     y_split_kernel<<<dim3(div_up(size_t(8 * N * P->Kp2), 256), 1), 256, 0, s>>>(P->d_D.p, M, int(nw), int(nwp), N, P->Kp2,
@@ -1606,8 +1628,8 @@ static void batch_reserve(LadderPlan* P, LadderBatch& B, long R, int maxiter) {
   B.Yl.alloc(ctx, size_t(R * 8 * N * P->Kp2));
   size_t p1 = 0, p2 = 0;
   for (long a = 1; a <= R; ++a) {
-    int bn, sp1, sp2;
-    tc_gemm_shape(ctx, int(a * M), int(N), int(P->Kx), 16, 2, &bn, &sp1);
+    int bn, sp2;
+    const int sp1 = tc_splits_for(ctx, int(a * M), int(N), int(P->Kx), P->bn);
     tc_gemm_shape(ctx, int(nw), int(a * 8 * N), int(nw), 16, 2, &bn, &sp2);
     p1 = std::max(p1, size_t(sp1) * size_t(a * M * N));
     p2 = std::max(p2, size_t(sp2) * size_t(a * nw * 8 * N));
@@ -1648,7 +1670,8 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const double2* X, int n
       B.Ah.p, B.Al.p);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, px);
-  int sp = tc_gemm_launch(ctx, B.opA, P->opG, int(Mt), int(N), int(P->Kx), B.part.p, Mt, Mt * N, 16, P->d_err.p, "tc_ladder");
+  int sp = tc_gemm_launch_with(ctx, B.opA, P->opG, P->bn, 0, int(Mt), int(N), int(P->Kx), B.part.p, Mt, Mt * N, P->d_err.p,
+                               "tc_ladder");
   sum_parts_kernel<<<div_up(size_t(Mt * N), 256), 256, 0, s>>>(B.part.p, Mt * N, sp, Mt * N, B.D.p);
   EPSP_LAUNCHED(ctx);
   y_split_kernel<<<dim3(div_up(size_t(8 * N * P->Kp2), 256), unsigned(nA)), 256, 0, s>>>(B.D.p, Mt, int(nw), int(nwp), N,
@@ -2003,6 +2026,20 @@ epsp_status epsp_ladder_run_batched(epsp_ladder_plan* plan, const double* sigma,
     ladder_run_batched(P, sigma, mu, Tlist, nT, Omegas, nOmega, rtol, maxiter, max_rhs, sigma_bubble, sigma_ladder,
                        converged, niter, hist, J_out);
   });
+}
+
+epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, int32_t* splits, double* ms_chosen,
+                                    double* ms_heuristic) {
+  if (!plan || !bn || !splits) return EPSP_EINVAL;
+  auto* P = reinterpret_cast<const LadderPlan*>(plan);
+  *bn = P->bn;
+  *splits = P->splits;
+  double best = 0;
+  for (const auto& c : P->tune_all)
+    if (c.bn == P->bn && c.splits == P->splits) best = c.ms;
+  if (ms_chosen) *ms_chosen = best;
+  if (ms_heuristic) *ms_heuristic = P->tune_ms_heuristic;
+  return EPSP_OK;
 }
 
 epsp_status epsp_ladder_apply(epsp_ladder_plan* plan, const double* sigma_T, double mu, double T, double Omega, const double* J,

@@ -2,6 +2,8 @@
 #include "tc_gemm.cuh"
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <mutex>
 
 namespace epsp {
@@ -84,6 +86,89 @@ int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int 
     launch<128, 3, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   prof_end(ctx, pi);
   return splits;
+}
+
+int tc_splits_for(Ctx* ctx, int M, int N, int K, int bn) {
+  const int kblocks = (K + kTcBK - 1) / kTcBK;
+  const int tiles = ((M + kTcBM - 1) / kTcBM) * ((N + bn - 1) / bn);
+  int sp = std::min(std::max(1, (ctx->sm_count + tiles - 1) / tiles), std::max(1, std::min(16, kblocks)));
+  const int per = (kblocks + sp - 1) / sp;
+  return std::max(1, (kblocks + per - 1) / per);
+}
+
+int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn, int splits, int M, int N, int K,
+                        float* out, long ld_out, long split_stride, int* d_err, const char* prof_name) {
+  if (A.ns != 2 || B.ns != 2) fail(EPSP_EINVAL, "explicit tile shapes are for two-part operands");
+  if (bn != 128 && bn != 256) fail(EPSP_EINVAL, "tile width must be 128 or 256");
+  const int kblocks = (K + kTcBK - 1) / kTcBK;
+  if (splits <= 0) splits = tc_splits_for(ctx, M, N, K, bn);
+  splits = std::max(1, std::min(splits, kblocks));
+  const int per = (kblocks + splits - 1) / splits;
+  splits = (kblocks + per - 1) / per;
+  long pi = prof_begin(ctx, prof_name);
+  if (bn == 256)
+    launch<256, 2, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+  else
+    launch<128, 3, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+  prof_end(ctx, pi);
+  return splits;
+}
+
+// Tuned shapes are kept for the process, per device and product shape, so later plans of the same
+// sizes reuse the measurement.
+namespace {
+std::mutex g_tune_mu;
+std::map<std::array<long, 5>, std::vector<TcTune>> g_tune_cache;
+}  // namespace
+
+TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, const TcOperand& B256, int M, int N, int K,
+                        float* out, long ld_out, long split_stride, int max_splits, int* d_err, int reps,
+                        std::vector<TcTune>* all) {
+  const std::array<long, 5> key{ctx->device, M, N, K, max_splits};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      TcTune best = it->second.front();
+      for (const auto& c : it->second)
+        if (c.ms < best.ms) best = c;
+      if (all) *all = it->second;
+      return best;
+    }
+  }
+  std::vector<TcTune> cand;
+  for (int bn : {256, 128}) {
+    const int tiles = ((M + kTcBM - 1) / kTcBM) * ((N + bn - 1) / bn);
+    const int h = std::max(1, (ctx->sm_count + tiles - 1) / tiles);
+    for (int sp : {h, 2 * h})
+      if (sp <= max_splits) cand.push_back(TcTune{bn, sp, 0.f});
+  }
+  cudaEvent_t e0, e1;
+  EPSP_CUDA(cudaEventCreate(&e0));
+  EPSP_CUDA(cudaEventCreate(&e1));
+  TcTune best{};
+  best.ms = 3.4e38f;
+  for (auto& c : cand) {
+    const TcOperand& B = c.bn == 256 ? B256 : B128;
+    tc_gemm_launch_with(ctx, A, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune");
+    EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
+    for (int r = 0; r < reps; ++r)
+      tc_gemm_launch_with(ctx, A, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune");
+    EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
+    EPSP_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    c.ms = ms / float(reps);
+    if (c.ms < best.ms) best = c;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (all) *all = cand;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = cand;
+  }
+  return best;
 }
 
 }  // namespace epsp

@@ -22,6 +22,8 @@
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
+#include <vector>
+
 namespace epsp {
 
 constexpr int kTcBM = 128, kTcBK = 64;
@@ -260,6 +262,30 @@ int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int 
 
 // The BN and split count tc_gemm_launch picks for (M, N, K), ns parts, at most max_splits splits.
 void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* bn, int* splits, int kb_cap = 0);
+
+// Launch with an explicit tile width bn (128: three pipeline stages; 256: two; two-part operands
+// only) and split count (0: the heuristic's count for that bn); B's tensor maps must have boxes of
+// bn rows. Returns the splits used.
+int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn, int splits, int M, int N, int K,
+                        float* out, long ld_out, long split_stride, int* d_err, const char* prof_name = "tc_gemm");
+
+// The split count tc_gemm_launch_with uses for splits = 0.
+int tc_splits_for(Ctx* ctx, int M, int N, int K, int bn);
+
+// One measured candidate of the autotuner.
+struct TcTune {
+  int bn = 0, splits = 0;
+  float ms = 0.f;
+};
+
+// The autotuner: times every candidate tile shape (bn 128 with three stages, bn 256 with two; the
+// heuristic split count and twice it, within max_splits) of one two-part product on its own
+// operands -- CUDA events on ctx's stream, one untimed and `reps` timed launches each -- and returns
+// the fastest; every candidate's time goes to *all when given. B128 / B256: B's maps with boxes of
+// 128 / 256 rows.
+TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, const TcOperand& B256, int M, int N, int K,
+                        float* out, long ld_out, long split_stride, int max_splits, int* d_err, int reps,
+                        std::vector<TcTune>* all = nullptr);
 
 // x = Σ_p x_p with x_p BF16, p < ns (round to nearest at every step).
 __device__ __forceinline__ void split_bf16_n(float x, int ns, __nv_bfloat16* out) {

@@ -72,6 +72,7 @@ def lib():
         "epsp_ladder_run": (C.c_int, [vp, c_double_p, c_double_p, c_double_p, i64, c_double_p, i64, i32, d, i32,
                                       c_double_p, c_double_p, u8p, c_int32_p, P(epsp_ladder_history), c_double_p]),
         "epsp_ladder_apply": (C.c_int, [vp, c_double_p, d, d, d, c_double_p, c_double_p]),
+        "epsp_ladder_gemm_config": (C.c_int, [vp, P(i32), P(i32), P(d), P(d)]),
         "epsp_ladder_run_batched": (C.c_int, [vp, c_double_p, c_double_p, c_double_p, i64, c_double_p, i64, d, i32, i32,
                                               c_double_p, c_double_p, u8p, c_int32_p, P(epsp_ladder_history),
                                               c_double_p]),
@@ -268,6 +269,12 @@ class LadderPlan:
         self.handle = C.c_void_p()
         self.ctx.check(lib().epsp_ladder_setup(self.ctx.handle, C.byref(self.M.struct), C.byref(self.opts),
                                                C.byref(self.handle)))
+
+    def gemm_config(self) -> dict:
+        """The contraction's tile shape chosen by the autotuner at setup (GEMM_BF16 plans)."""
+        bn, sp, ms, mh = C.c_int32(), C.c_int32(), C.c_double(), C.c_double()
+        self.ctx.check(lib().epsp_ladder_gemm_config(self.handle, C.byref(bn), C.byref(sp), C.byref(ms), C.byref(mh)))
+        return dict(bn=bn.value, splits=sp.value, ms=ms.value, ms_heuristic=mh.value)
 
     def run(self, sigma, mu, Tlist, Omegas, *, solver="gmres", rtol=1e-2, maxiter=30, store_vertex=False,
             batch_rhs=None):

@@ -245,6 +245,13 @@ epsp_status epsp_ladder_run_batched(epsp_ladder_plan* plan, const double* sigma,
                                     double* sigma_ladder, uint8_t* converged, int32_t* niter,
                                     epsp_ladder_history* hist, double* J_out);
 
+/* The tile shape the autotuner picked at setup for the ladder's tensor-core contraction (GEMM_BF16
+ * plans; no counterpart in the reference): tile width bn (128 or 256), split count, and the timed
+ * milliseconds per launch of the choice and of the fixed heuristic's shape (0 when not a GEMM_BF16
+ * plan). */
+epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, int32_t* splits, double* ms_chosen,
+                                    double* ms_heuristic);
+
 /* One application LJ = L(J) of the ladder kernel at temperature T, chemical potential mu and
  * probe frequency Omega, with sigma_T [nω, ni] complex the self-energy of that temperature:
  * apply_ladder_kernel! (src/ladder.jl:245-296) with the propagators of contour_greens!
