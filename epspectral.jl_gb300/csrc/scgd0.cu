@@ -900,16 +900,18 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   const double br0 = P->wsa.nodes.front() - 0.1, br1 = P->wsa.nodes.back() + 0.1;  // src/scgd0.jl:197
   if (mu_smem_bytes(nwa) > 48 * 1024)
     EPSP_CUDA(cudaFuncSetAttribute(mu_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(mu_smem_bytes(nwa))));
-  DBuf<unsigned long long> d_err;
-  DBuf<double> d_mu, d_minA;
-  DBuf<int> d_status;
-  d_err.alloc(ctx, size_t(nT));
-  d_mu.alloc(ctx, size_t(nT));
-  d_minA.alloc(ctx, size_t(nT));
-  d_status.alloc(ctx, size_t(nT));
-  std::vector<unsigned long long> h_err(static_cast<size_t>(nT));
-  std::vector<double> h_mu(static_cast<size_t>(nT)), h_minA(static_cast<size_t>(nT));
-  std::vector<int> h_status(static_cast<size_t>(nT));
+  // the per-iteration results in one buffer (one copy back per iteration): err bits [nT], μ [nT],
+  // min ∫A [nT], μ status [nT] (as int), the tensor-core wait flag
+  const size_t npack = size_t(4 * nT + 1);
+  DBuf<double> d_pack;
+  d_pack.alloc(ctx, npack);
+  d_pack.zero(s);
+  auto* d_err = reinterpret_cast<unsigned long long*>(d_pack.p);
+  double* d_mu = d_pack.p + nT;
+  double* d_minA = d_pack.p + 2 * nT;
+  int* d_status = reinterpret_cast<int*>(d_pack.p + 3 * nT);
+  int* d_tcerr = reinterpret_cast<int*>(d_pack.p + 4 * nT);
+  std::vector<double> h_pack(npack);
   int32_t niter = 0;
   const unsigned eb = div_up(size_t(slab), 256);
   // Every active temperature of an iteration is processed by the same launches (slot a ->
@@ -927,6 +929,20 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   if (P->path == EPSP_PATH_GEMM_BF16) tc_reserve(P, nT);
   std::vector<TParams> h_tp(static_cast<size_t>(nT));
   std::vector<int> slots;
+  // CUDA graph of the iteration body (tensor-core path; not while one of its kernels is profiled)
+  static const char* kBodyProfiles[] = {"kbuild", "tc_fm", "tc_kk", "mu"};
+  bool use_graph = P->path == EPSP_PATH_GEMM_BF16;
+  for (const char* nm : kBodyProfiles)
+    if (ctx->prof_name == nm) use_graph = false;
+  cudaGraphExec_t gexec = nullptr;
+  struct ExecGuard {
+    cudaGraphExec_t* e;
+    ~ExecGuard() {
+      if (*e) cudaGraphExecDestroy(*e);
+    }
+  } eguard{&gexec};
+  int graph_nA = -1;
+  int64_t graph_launches = 0;
   for (int32_t iter = 1; iter <= maxiter; ++iter) {
     auto t0 = std::chrono::steady_clock::now();
     slots.clear();
@@ -944,57 +960,93 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
     const int nA = int(slots.size());
     d_slots.upload(slots.data(), slots.size(), s);
     d_tp.upload(h_tp.data(), h_tp.size(), s);
-    d_err.zero(s);
-    d_status.zero(s);
-    clamp_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(S.p, Sin_b.p, slab, d_slots.p, d_tp.p);
-    EPSP_LAUNCHED(ctx);
-    if (P->path == EPSP_PATH_GEMM_BF16) {
-      tc_iterate(P, nA, d_slots.p, slots.data(), d_tp.p, Sin_b.p, Snew.p);
-    } else {
-      for (int a = 0; a < nA; ++a) {
-        const int64_t iT = slots[size_t(a)];
-        P->d_ImS.zero(s);
-        scgd0_imsigma(P, Sin_b.p + slab * a, mu[size_t(iT)], occ->Tlist[iT], P->d_ImS.p);
-        long pk = prof_begin(ctx, "kk");
-        gemm_f64(ctx, false, int(nw), int(ni), int(nw), 1.0, P->d_KK.p, nw, P->d_ImS.p, nw, 0.0, P->d_ReS.p, nw);
-        assemble_kernel<<<eb, 256, 0, s>>>(P->d_ReS.p, P->d_ImS.p, Snew.p + slab * iT, slab);
-        EPSP_LAUNCHED(ctx);
-        prof_end(ctx, pk);
+    // the launches of one iteration; on the tensor-core path they are captured once per active set
+    // into a CUDA graph and replayed (μ, T come from the device, so a replay sees the current ones)
+    auto body = [&] {
+      EPSP_CUDA(cudaMemsetAsync(d_err, 0, size_t(nT) * 8, s));
+      EPSP_CUDA(cudaMemsetAsync(d_status, 0, size_t(nT) * sizeof(int), s));
+      clamp_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(S.p, Sin_b.p, slab, d_slots.p, d_tp.p);
+      EPSP_LAUNCHED(ctx);
+      if (P->path == EPSP_PATH_GEMM_BF16) {
+        tc_iterate(P, nA, d_slots.p, slots.data(), d_tp.p, Sin_b.p, Snew.p);
+        EPSP_CUDA(cudaMemcpyAsync(d_tcerr, tc_err_ptr(P), sizeof(int), cudaMemcpyDeviceToDevice, s));
+      } else {
+        for (int a = 0; a < nA; ++a) {
+          const int64_t iT = slots[size_t(a)];
+          P->d_ImS.zero(s);
+          scgd0_imsigma(P, Sin_b.p + slab * a, mu[size_t(iT)], occ->Tlist[iT], P->d_ImS.p);
+          long pk = prof_begin(ctx, "kk");
+          gemm_f64(ctx, false, int(nw), int(ni), int(nw), 1.0, P->d_KK.p, nw, P->d_ImS.p, nw, 0.0, P->d_ReS.p, nw);
+          assemble_kernel<<<eb, 256, 0, s>>>(P->d_ReS.p, P->d_ImS.p, Snew.p + slab * iT, slab);
+          EPSP_LAUNCHED(ctx);
+          prof_end(ctx, pk);
+        }
       }
-    }
-    if (P->nmult > 0) {
-      multiplet_kernel<<<dim3(div_up(size_t(nw * P->nmult), 256), unsigned(nA)), 256, 0, s>>>(
-          Snew.p, int(nw), slab, d_slots.p, P->d_mptr.p, P->d_midx.p, P->nmult);
+      if (P->nmult > 0) {
+        multiplet_kernel<<<dim3(div_up(size_t(nw * P->nmult), 256), unsigned(nA)), 256, 0, s>>>(
+            Snew.p, int(nw), slab, d_slots.p, P->d_mptr.p, P->d_midx.p, P->nmult);
+        EPSP_LAUNCHED(ctx);
+      }
+      auto spectral_A = P->path == EPSP_PATH_GEMM_BF16 ? spectral_A_kernel<true> : spectral_A_kernel<false>;
+      spectral_A<<<dim3(div_up(size_t(nwa), 256), unsigned(ni), unsigned(nA)), 256, 0, s>>>(
+          Snew.p, int(nw), slab, d_slots.p, P->d_wsa.p, int(nwa), P->d_jsp.p, P->d_tsp.p, P->d_eps_i.p, A_b.p, int(ni));
       EPSP_LAUNCHED(ctx);
-    }
-    auto spectral_A = P->path == EPSP_PATH_GEMM_BF16 ? spectral_A_kernel<true> : spectral_A_kernel<false>;
-    spectral_A<<<dim3(div_up(size_t(nwa), 256), unsigned(ni), unsigned(nA)), 256, 0, s>>>(
-        Snew.p, int(nw), slab, d_slots.p, P->d_wsa.p, int(nwa), P->d_jsp.p, P->d_tsp.p, P->d_eps_i.p, A_b.p, int(ni));
-    EPSP_LAUNCHED(ctx);
-    spectral_colsum_kernel<<<dim3(unsigned(ni), unsigned(nA)), 256, 0, s>>>(A_b.p, int(nwa), int(ni), P->d_Wa.p,
-                                                                          colsum_b.p);
-    EPSP_LAUNCHED(ctx);
-    min_kernel<<<unsigned(nA), 256, 0, s>>>(colsum_b.p, int(ni), d_slots.p, d_minA.p);
-    EPSP_LAUNCHED(ctx);
-    if (!fix_mu) {
-      spectral_D_kernel<<<dim3(div_up(size_t(nwa), 32), unsigned(nA)), 256, 0, s>>>(A_b.p, int(nwa), int(ni), P->d_w_i.p,
-                                                                                   P->d_Wa.p, D_b.p);
+      spectral_colsum_kernel<<<dim3(unsigned(ni), unsigned(nA)), 256, 0, s>>>(A_b.p, int(nwa), int(ni), P->d_Wa.p,
+                                                                            colsum_b.p);
       EPSP_LAUNCHED(ctx);
-      long pm = prof_begin(ctx, "mu");
-      mu_solve_kernel<<<unsigned(kMuCluster * nA), kMuThreads, mu_smem_bytes(nwa), s>>>(
-          D_b.p, P->d_wsa.p, int(nwa), d_slots.p, d_tp.p, P->W, P->nstates_base, occ->spin_degeneracy, br0, br1, d_mu.p,
-          d_status.p);
+      min_kernel<<<unsigned(nA), 256, 0, s>>>(colsum_b.p, int(ni), d_slots.p, d_minA);
       EPSP_LAUNCHED(ctx);
-      prof_end(ctx, pm);
+      if (!fix_mu) {
+        spectral_D_kernel<<<dim3(div_up(size_t(nwa), 32), unsigned(nA)), 256, 0, s>>>(A_b.p, int(nwa), int(ni), P->d_w_i.p,
+                                                                                     P->d_Wa.p, D_b.p);
+        EPSP_LAUNCHED(ctx);
+        long pm = prof_begin(ctx, "mu");
+        mu_solve_kernel<<<unsigned(kMuCluster * nA), kMuThreads, mu_smem_bytes(nwa), s>>>(
+            D_b.p, P->d_wsa.p, int(nwa), d_slots.p, d_tp.p, P->W, P->nstates_base, occ->spin_degeneracy, br0, br1, d_mu,
+            d_status);
+        EPSP_LAUNCHED(ctx);
+        prof_end(ctx, pm);
+      }
+      err_copy_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(Snew.p, S.p, slab, d_slots.p, d_err);
+      EPSP_LAUNCHED(ctx);
+    };
+    if (use_graph && iter > 1) {
+      if (graph_nA != nA) {
+        if (gexec) cudaGraphExecDestroy(gexec), gexec = nullptr;
+        const int64_t l0 = ctx->launches;
+        cudaGraph_t g = nullptr;
+        EPSP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        try {
+          body();
+        } catch (...) {
+          cudaStreamEndCapture(s, &g);
+          if (g) cudaGraphDestroy(g);
+          throw;
+        }
+        EPSP_CUDA(cudaStreamEndCapture(s, &g));
+        cudaError_t ie = cudaGraphInstantiate(&gexec, g, 0);
+        cudaGraphDestroy(g);
+        EPSP_CUDA(ie);
+        graph_launches = ctx->launches - l0;
+        ctx->launches = l0;
+        graph_nA = nA;
+      }
+      EPSP_CUDA(cudaGraphLaunch(gexec, s));
+      ctx->launches += graph_launches;
+    } else {
+      body();
     }
-    err_copy_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(Snew.p, S.p, slab, d_slots.p, d_err.p);
-    EPSP_LAUNCHED(ctx);
-    d_err.download(h_err.data(), size_t(nT), s);
-    d_mu.download(h_mu.data(), size_t(nT), s);
-    d_minA.download(h_minA.data(), size_t(nT), s);
-    d_status.download(h_status.data(), size_t(nT), s);
+    d_pack.download(h_pack.data(), npack, s);
     EPSP_CUDA(cudaStreamSynchronize(s));
-    if (P->path == EPSP_PATH_GEMM_BF16) tc_check(P);
+    if (P->path == EPSP_PATH_GEMM_BF16) {
+      int tcerr = 0;
+      std::memcpy(&tcerr, &h_pack[size_t(4 * nT)], sizeof(int));
+      if (tcerr) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+    }
+    const auto* h_err = reinterpret_cast<const unsigned long long*>(h_pack.data());
+    const double* h_mu = h_pack.data() + nT;
+    const double* h_minA = h_pack.data() + 2 * nT;
+    const auto* h_status = reinterpret_cast<const int*>(h_pack.data() + 3 * nT);
     for (int64_t iT = 0; iT < nT; ++iT) {
       if (!active[size_t(iT)]) continue;
       hist->min_spectral_weight[iT + nT * (iter - 1)] = h_minA[size_t(iT)];

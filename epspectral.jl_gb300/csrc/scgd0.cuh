@@ -60,5 +60,7 @@ void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, co
                 const double2* d_Sin_b, double2* d_Snew_all);
 // Fails with EPSP_EDEVICE_TIMEOUT if a tensor-core GEMM's bounded wait ran out (synchronises).
 void tc_check(Scgd0Plan* P);
+// The device flag the tensor-core GEMMs set when a bounded wait runs out.
+int* tc_err_ptr(Scgd0Plan* P);
 
 }  // namespace epsp
