@@ -84,6 +84,9 @@ struct LadderPlan {
   DBuf<double2> d_Gm, d_Gp, d_Sm, d_Sp, d_ST;
   DBuf<int32_t> d_jm, d_jp;
   DBuf<double> d_tm, d_tp;
+  std::vector<int32_t> h_jm, h_jp;  // host copies behind the last upload of the tables
+  std::vector<double> h_tm, h_tp;
+  double tab_Om = std::numeric_limits<double>::quiet_NaN();
   double cur_T = 0, cur_mu = 0, cur_Om = 0;
 };
 
@@ -416,8 +419,8 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
   const float* nnu = nnu_all + 16 * rhs;
   const long row_base = long(blockIdx.z) * 24 * nwp;
   const int W = ns + 2, win = 32 + 2 * W;
-  float2* s_j = reinterpret_cast<float2*>(xg_smem);                               // [4][win] (re, im)
-  float (*tile)[64][33] = reinterpret_cast<float (*)[64][33]>(s_j + 4 * win);    // [4][64][33]
+  float2* s_jbuf = reinterpret_cast<float2*>(xg_smem);                               // [2][4][win] (re, im)
+  float (*tile)[64][33] = reinterpret_cast<float (*)[64][33]>(s_jbuf + 8 * win);    // [4][64][33]
   const int nblk = nwp / 32;
   const int j0 = (blockIdx.x % nblk) * 32, comp = blockIdx.x / nblk;
   const int cc = comp % 4, c0 = comp / 4;
@@ -442,24 +445,43 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
     }
   }
   const long kt0 = long(blockIdx.y) * kXgTiles;
+  // The vertex window of the 4 pairs (b, i') of a K-tile (4 win <= 2 x 256 values) is loaded into
+  // registers one K-tile ahead and stored into the other half of a double buffer, so its global
+  // latency hides behind the current K-tile's arithmetic.
+  float2 pre[2];
+  auto load_window = [&](long k0) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int e = threadIdx.x + 256 * q;
+      float2 v = make_float2(0.f, 0.f);
+      if (e < 4 * win && k0 < Kp) {
+        const int g = e / win, node = j0 - W + e % win;
+        const long pair = (k0 / 16) + g;  // (b, i') index = k / 16
+        if (node >= 0 && node < nw && pair < 3l * ni) {
+          const int b = int(pair % 3);
+          const long ip = pair / 3;
+          const double2 z = J[jidx(nw, node, c12, b, c0, ip)];
+          v = make_float2(float(z.x), float(z.y));
+        }
+      }
+      pre[q] = v;
+    }
+  };
+  auto store_window = [&](float2* dst) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int e = threadIdx.x + 256 * q;
+      if (e < 4 * win) dst[e] = pre[q];
+    }
+  };
+  load_window(kt0 * 64);
+  store_window(s_jbuf);
   for (int kt = 0; kt < kXgTiles; ++kt) {
     const long k0 = (kt0 + kt) * 64;
     if (k0 >= Kp) break;
-    __syncthreads();
-    // vertex window of the 4 pairs (b, i') of this K-tile
-    for (int e = threadIdx.x; e < 4 * win; e += 256) {
-      const int g = e / win, node = j0 - W + e % win;
-      const long pair = (k0 / 16) + g;  // (b, i') index = k / 16
-      float2 v = make_float2(0.f, 0.f);
-      if (node >= 0 && node < nw && pair < 3l * ni) {
-        const int b = int(pair % 3);
-        const long ip = pair / 3;
-        const double2 z = J[jidx(nw, node, c12, b, c0, ip)];
-        v = make_float2(float(z.x), float(z.y));
-      }
-      s_j[e] = v;
-    }
-    __syncthreads();
+    float2* s_j = s_jbuf + (kt & 1) * 4 * win;
+    __syncthreads();  // s_j complete; the previous K-tile's rows are written out
+    if (kt + 1 < kXgTiles) load_window(k0 + 64);
 #pragma unroll
     for (int p = 0; p < 8; ++p) {
       const int h = p & 1, g = p >> 1;
@@ -506,12 +528,15 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
       *reinterpret_cast<uint4*>(Ah + off) = *reinterpret_cast<const uint4*>(hh);
       *reinterpret_cast<uint4*>(Al + off) = *reinterpret_cast<const uint4*>(ll);
     }
+    // the next window goes to the other buffer (its readers finished at the barrier above); the
+    // barrier at the top of the next K-tile publishes it and retires this K-tile's tiles
+    if (kt + 1 < kXgTiles) store_window(s_jbuf + ((kt + 1) & 1) * 4 * win);
   }
 }
 
 static size_t xgen_smem_bytes(int ns) {
   const int W = ns + 2, win = 32 + 2 * W;
-  return size_t(4 * win) * sizeof(float2) + size_t(4 * 64 * 33) * 4;
+  return size_t(8 * win) * sizeof(float2) + size_t(4 * 64 * 33) * 4;
 }
 
 // Y (rows q = 0, 2 of D) as the BF16 hi/lo B operand of the Kramers-Kronig GEMM: row (qq, c0, ri, n),
@@ -1041,23 +1066,26 @@ static void set_propagators(LadderPlan* P, double mu, double T, double Om) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
   const long nw = P->nw, ni = P->ni;
-  std::vector<double> xm(static_cast<size_t>(nw)), xp(static_cast<size_t>(nw)), tm, tp;
-  std::vector<int32_t> jm, jp;
-  for (long k = 0; k < nw; ++k) {
-    xm[size_t(k)] = P->ws.nodes[size_t(k)] - Om / 2;
-    xp[size_t(k)] = P->ws.nodes[size_t(k)] + Om / 2;
+  if (!(P->tab_Om == Om)) {  // the interpolation tables depend on Ω only
+    // the previous uploads from these host tables must be done before they are rebuilt
+    EPSP_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> xm(static_cast<size_t>(nw)), xp(static_cast<size_t>(nw));
+    for (long k = 0; k < nw; ++k) {
+      xm[size_t(k)] = P->ws.nodes[size_t(k)] - Om / 2;
+      xp[size_t(k)] = P->ws.nodes[size_t(k)] + Om / 2;
+    }
+    interp_table(P->ws.nodes, xm, P->h_jm, P->h_tm);
+    interp_table(P->ws.nodes, xp, P->h_jp, P->h_tp);
+    P->d_jm.upload(P->h_jm.data(), size_t(nw), s);
+    P->d_jp.upload(P->h_jp.data(), size_t(nw), s);
+    P->d_tm.upload(P->h_tm.data(), size_t(nw), s);
+    P->d_tp.upload(P->h_tp.data(), size_t(nw), s);
+    P->tab_Om = Om;
   }
-  interp_table(P->ws.nodes, xm, jm, tm);
-  interp_table(P->ws.nodes, xp, jp, tp);
-  P->d_jm.upload(jm.data(), size_t(nw), s);
-  P->d_jp.upload(jp.data(), size_t(nw), s);
-  P->d_tm.upload(tm.data(), size_t(nw), s);
-  P->d_tp.upload(tp.data(), size_t(nw), s);
   propagators_kernel<<<dim3(div_up(size_t(nw), 128), unsigned(ni)), 128, 0, s>>>(P->d_ST.p, P->d_ws.p, int(nw), P->d_jm.p,
                                                                                 P->d_tm.p, P->d_jp.p, P->d_tp.p, P->d_eps_i.p,
                                                                                 mu, T, Om, P->d_Gm.p, P->d_Gp.p, int(ni));
   EPSP_LAUNCHED(ctx);
-  EPSP_CUDA(cudaStreamSynchronize(s));  // the host tables above are freed on return
   P->cur_T = T;
   P->cur_mu = mu;
   P->cur_Om = Om;
@@ -1274,7 +1302,8 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
         // Krylov.gmres(A, b[, x0]; atol = rtol ‖J0‖, rtol = 0, itmax = maxiter), restart = false,
         // MGS, Givens (src/ladder.jl:340-353).
         const bool warm = iO > 0;
-        const double atol = rtol * nrm_host(P, J0.p, n, part, scal);
+        const double nJ0 = nrm_host(P, J0.p, n, part, scal);
+        const double atol = rtol * nJ0;
         std::vector<double> res;
         // r0 = b - A x0 (warm) or b
         if (warm) {
@@ -1284,7 +1313,7 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
         } else {
           EPSP_CUDA(cudaMemcpyAsync(W.p, J0.p, size_t(n) * sizeof(double2), cudaMemcpyDeviceToDevice, s));
         }
-        const double beta = nrm_host(P, W.p, n, part, scal);
+        const double beta = warm ? nrm_host(P, W.p, n, part, scal) : nJ0;  // a cold start's r0 is J0
         double rNorm = beta;
         res.push_back(beta);
         bool solved = rNorm <= atol, breakdown = false;
