@@ -13,7 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "epspectral_gb300")
 LIB = os.path.join(OUT_DIR, "libepspectral_gb300.so")
 OBJ_DIR = os.path.join(HERE, "_build")
-SOURCES = ["context.cu", "scgd0.cu", "scgd0_tc.cu", "tc_gemm.cu", "ladder.cu", "noalloc.cu", "mlp.cu"]
+SOURCES = ["context.cu", "scgd0.cu", "scgd0_tc.cu", "tc_gemm.cu", "ladder.cu", "noalloc.cu", "mlp.cu", "g2stream.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-warn-spills"]

@@ -1,0 +1,85 @@
+// g2stream.cu -- host side of the star-order g2 stream (g2stream.cuh).
+#include "g2stream.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+namespace epsp {
+
+size_t g2_elem_bytes(int dtype) { return dtype == EPSP_F64 ? 8 : (dtype == EPSP_F32 ? 4 : 2); }
+
+namespace {
+struct PinnedBuf {
+  void* p = nullptr;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+};
+struct Events {
+  cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaStream_t copy = nullptr;
+  ~Events() {
+    for (auto x : e)
+      if (x) cudaEventDestroy(x);
+    if (copy) cudaStreamDestroy(copy);
+  }
+};
+}  // namespace
+
+void stream_g2_by_columns(Ctx* ctx, const epsp_model* m, const std::vector<int32_t>& order,
+                          const std::vector<int32_t>& cptr, long chunk_f,
+                          const std::function<void(const void*, long, long, long)>& fn) {
+  const long nc = long(cptr.size()) - 1;
+  if (nc < 1) return;
+  const size_t slab = size_t(m->nm) * size_t(m->ni) * g2_elem_bytes(m->g2_dtype);  // bytes of one member
+  chunk_f = std::max<long>(chunk_f, 1);
+  // chunk boundaries over whole columns
+  std::vector<long> cb{0};
+  long maxm = 0;
+  for (long c = 0; c < nc;) {
+    long c1 = c + 1;
+    while (c1 < nc && cptr[size_t(c1 + 1)] - cptr[size_t(c)] <= chunk_f) ++c1;
+    maxm = std::max<long>(maxm, cptr[size_t(c1)] - cptr[size_t(c)]);
+    cb.push_back(c1);
+    c = c1;
+  }
+  const long nchunk = long(cb.size()) - 1;
+  const size_t bytes = size_t(std::max<long>(maxm, 1)) * slab;
+  cudaStream_t s = ctx->stream;
+  PinnedBuf host[2];
+  DBuf<uint8_t> dev[2];
+  Events ev;
+  EPSP_CUDA(cudaStreamCreateWithFlags(&ev.copy, cudaStreamNonBlocking));
+  for (auto& e : ev.e) EPSP_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  const int nb = nchunk > 1 ? 2 : 1;
+  for (int b = 0; b < nb; ++b) {
+    if (cudaHostAlloc(&host[b].p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+      (void)cudaGetLastError();
+      fail(EPSP_ENOMEM, "page-locked staging of " + std::to_string(bytes) + " bytes for the g2 stream failed");
+    }
+    dev[b].alloc(ctx, bytes);
+  }
+  cudaEvent_t* copied = ev.e;
+  cudaEvent_t* consumed = ev.e + 2;
+  const auto* g2 = static_cast<const uint8_t*>(m->g2);
+  for (long k = 0; k < nchunk; ++k) {
+    const int b = int(k % nb);
+    const long c0 = cb[size_t(k)], c1 = cb[size_t(k + 1)];
+    const long p0 = cptr[size_t(c0)], p1 = cptr[size_t(c1)];
+    // the staging buffer's previous copy must be done before it is refilled
+    if (k >= nb) EPSP_CUDA(cudaEventSynchronize(copied[b]));
+    auto* dst = static_cast<uint8_t*>(host[b].p);
+    for (long p = p0; p < p1; ++p) std::memcpy(dst + size_t(p - p0) * slab, g2 + size_t(order[size_t(p)]) * slab, slab);
+    // the device buffer's previous chunk must be consumed before it is overwritten
+    if (k >= nb) EPSP_CUDA(cudaStreamWaitEvent(ev.copy, consumed[b], 0));
+    EPSP_CUDA(cudaMemcpyAsync(dev[b].p, host[b].p, size_t(p1 - p0) * slab, cudaMemcpyHostToDevice, ev.copy));
+    EPSP_CUDA(cudaEventRecord(copied[b], ev.copy));
+    EPSP_CUDA(cudaStreamWaitEvent(s, copied[b], 0));
+    fn(dev[b].p, c0, c1, p0);
+    EPSP_CUDA(cudaEventRecord(consumed[b], s));
+  }
+  EPSP_CUDA(cudaStreamSynchronize(s));
+  EPSP_CUDA(cudaStreamSynchronize(ev.copy));
+}
+
+}  // namespace epsp

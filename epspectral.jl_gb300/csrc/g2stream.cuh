@@ -1,0 +1,35 @@
+// g2stream.cuh -- the caller's host g2 [nm, ni, nf] streamed through the device in star order.
+#pragma once
+#include "common.cuh"
+
+#include <functional>
+#include <vector>
+
+namespace epsp {
+
+// g2's element as FP64 (FP64, FP32 or BF16 bit patterns in uint16_t storage).
+template <class T>
+__device__ __forceinline__ double load_g2(const T* p, long k);
+template <>
+__device__ __forceinline__ double load_g2<double>(const double* p, long k) { return p[k]; }
+template <>
+__device__ __forceinline__ double load_g2<float>(const float* p, long k) { return double(p[k]); }
+template <>
+__device__ __forceinline__ double load_g2<uint16_t>(const uint16_t* p, long k) {
+  return double(__uint_as_float(uint32_t(p[k]) << 16));
+}
+
+size_t g2_elem_bytes(int dtype);
+
+// Streams g2 through the device by column sets: column c holds the inner states order[p] for p in
+// [cptr[c], cptr[c + 1]). Chunks are whole columns with at most chunk_f members (one column may
+// exceed it alone). Each chunk is gathered on the host into page-locked staging as [nm, ni, p - p0]
+// (member-major slabs of g2[:, :, order[p]]) and copied on a second stream into one of two device
+// buffers while the previous chunk is consumed on ctx->stream; fn(d_chunk, c0, c1, p0) enqueues
+// the consumer of columns [c0, c1) on ctx->stream. Returns when every chunk has been consumed.
+// The caller's g2 is read only.
+void stream_g2_by_columns(Ctx* ctx, const epsp_model* m, const std::vector<int32_t>& order,
+                          const std::vector<int32_t>& cptr, long chunk_f,
+                          const std::function<void(const void*, long, long, long)>& fn);
+
+}  // namespace epsp

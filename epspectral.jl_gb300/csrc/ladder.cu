@@ -18,6 +18,7 @@
 // and the channel combinations are folded into the A operand rows: 6 combinations q per
 // (c0, re/im) instead of the 16 of (c12, type) x sign, and K = nm·3·ni instead of nshift·3·ni.
 #include "common.cuh"
+#include "g2stream.cuh"
 #include "gemm_f64.cuh"
 #include "tc_gemm.cuh"
 
@@ -316,22 +317,25 @@ __global__ void finish_direct_kernel(const double* __restrict__ Cp, const double
 
 // ---- GEMM paths: per-mode regrouped shift sums ----
 
-// G̃[(ν, b, i'), (a, i)] = Σ_{f in star(i')} R_f[a, b] w_f g2[ν, i, f], zero for ν below ω_acoustic.
-// One thread per (ν, i), looping over the stars in order.
-__global__ void coupling_rot_kernel(const double* __restrict__ g2, const double* __restrict__ R, const double* __restrict__ w_f,
-                                    const int32_t* __restrict__ by_star, const int32_t* __restrict__ star_ptr,
-                                    const double* __restrict__ wnu, double w_ac, int nm, int nmp, int ni, long Kx,
-                                    double* __restrict__ Gt) {
+// G̃[(ν, b, i'), (a, i)] = Σ_{f in star(i')} R_f[a, b] w_f g2[ν, i, f] (star sums of the regrouped
+// paths; modes below ω_acoustic are 0), for the stars [c0, c1) of one streamed chunk: g2c
+// [nm, ni, p - p0] holds their members p in star order.
+template <class T>
+__global__ void coupling_rot_chunk_kernel(const T* __restrict__ g2c, const double* __restrict__ R,
+                                          const double* __restrict__ w_f, const int32_t* __restrict__ by_star,
+                                          const int32_t* __restrict__ star_ptr, long c0, long c1, long p0,
+                                          const double* __restrict__ wnu, double w_ac, int nm, int nmp, int ni, long Kx,
+                                          double* __restrict__ Gt) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= long(nm) * ni) return;
   int nu = int(idx % nm), i = int(idx / nm);
   bool skip = wnu[nu] < w_ac;
-  for (int ip = 0; ip < ni; ++ip) {
+  for (long ip = c0; ip < c1; ++ip) {
     double acc[3][3] = {};
     if (!skip)
       for (int p = star_ptr[ip]; p < star_ptr[ip + 1]; ++p) {
         long f = by_star[p];
-        double g = w_f[f] * g2[nu + long(nm) * (i + long(ni) * f)];
+        double g = w_f[f] * load_g2(g2c, nu + long(nm) * (i + long(ni) * (p - p0)));
         for (int b = 0; b < 3; ++b)
           for (int a = 0; a < 3; ++a) acc[a][b] += R[a + 3 * (b + 3 * f)] * g;
       }
@@ -874,8 +878,10 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
     P->d_wlo = to_device(ctx, wlo);
     P->d_whi = to_device(ctx, whi);
   }
-  auto g2d = g2_as_double(m);
-  P->d_g2 = to_device(ctx, g2d);
+  if (P->path == EPSP_PATH_DIRECT_FP64) {  // the shift-grid coupling reads g2 in every application
+    auto g2d = g2_as_double(m);
+    P->d_g2 = to_device(ctx, g2d);
+  }
   P->d_wf = to_device(ctx, m->w_f, size_t(nf));
   P->d_R = to_device(ctx, m->R, size_t(9 * nf));
   if (P->path == EPSP_PATH_DIRECT_FP64) {
@@ -949,10 +955,30 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
     P->Kx = P->nmp * 3 * ni;
     P->d_Gt.alloc(ctx, size_t(P->Kx * 3 * ni));
     P->d_Gt.zero(s);
-    coupling_rot_kernel<<<div_up(size_t(nm * ni), 128), 128, 0, s>>>(P->d_g2.p, P->d_R.p, P->d_wf.p, P->d_by_star.p,
-                                                                     P->d_star_ptr.p, d_wnu.p, P->w_ac, int(nm), int(P->nmp),
-                                                                     int(ni), P->Kx, P->d_Gt.p);
-    EPSP_LAUNCHED(ctx);
+    // G̃ needs g2 once: it streams through the device star by star (gpu_tile inner states per chunk,
+    // or up to 1 GiB of g2), copies overlapped with the sums; g2 stays in the caller's memory
+    {
+      const size_t member_bytes = size_t(nm * ni) * g2_elem_bytes(m->g2_dtype);
+      const long chunk_f =
+          opts->gpu_tile > 0 ? long(opts->gpu_tile) : std::max<long>(1, long((size_t(1) << 30) / member_bytes));
+      const unsigned grid = div_up(size_t(nm * ni), 128);
+      stream_g2_by_columns(ctx, m, by_star, sp, chunk_f, [&](const void* g2c, long c0, long c1, long p0) {
+        if (m->g2_dtype == EPSP_F64)
+          coupling_rot_chunk_kernel<double><<<grid, 128, 0, s>>>(static_cast<const double*>(g2c), P->d_R.p, P->d_wf.p,
+                                                                P->d_by_star.p, P->d_star_ptr.p, c0, c1, p0, d_wnu.p,
+                                                                P->w_ac, int(nm), int(P->nmp), int(ni), P->Kx, P->d_Gt.p);
+        else if (m->g2_dtype == EPSP_F32)
+          coupling_rot_chunk_kernel<float><<<grid, 128, 0, s>>>(static_cast<const float*>(g2c), P->d_R.p, P->d_wf.p,
+                                                               P->d_by_star.p, P->d_star_ptr.p, c0, c1, p0, d_wnu.p,
+                                                               P->w_ac, int(nm), int(P->nmp), int(ni), P->Kx, P->d_Gt.p);
+        else
+          coupling_rot_chunk_kernel<uint16_t><<<grid, 128, 0, s>>>(static_cast<const uint16_t*>(g2c), P->d_R.p, P->d_wf.p,
+                                                                  P->d_by_star.p, P->d_star_ptr.p, c0, c1, p0, d_wnu.p,
+                                                                  P->w_ac, int(nm), int(P->nmp), int(ni), P->Kx,
+                                                                  P->d_Gt.p);
+        EPSP_LAUNCHED(ctx);
+      });
+    }
     const long M = 24 * P->nwp, N = 3 * ni;
     P->d_D.alloc(ctx, size_t(M * N));
     if (P->path == EPSP_PATH_GEMM_FP64) {

@@ -9,6 +9,7 @@
 //                  K_t [nω, nc·nm] the kernel tensor of one iteration and temperature
 //   spectral    :  A [nωa, ni] double, D [nωa], column sums [ni]
 #include "common.cuh"
+#include "g2stream.cuh"
 #include "gemm_f64.cuh"
 #include "scgd0.cuh"
 #include "warmstart.cuh"
@@ -39,16 +40,6 @@ __global__ void kk_build_kernel(const double* __restrict__ xs, int n, double* __
 
 // g2 [nm, ni, nf] (any storage type) -> g2_t [nm, nf, ni] double (src/scgd0.jl:275-278), and
 // ωq_t[ν, f, i] = ωph[ν, iq_kk[iks_i[i], iks_f[f]]] (gather_pair_table!, src/scgd0.jl:270).
-template <class T>
-__device__ __forceinline__ double load_g2(const T* p, long k);
-template <>
-__device__ __forceinline__ double load_g2<double>(const double* p, long k) { return p[k]; }
-template <>
-__device__ __forceinline__ double load_g2<float>(const float* p, long k) { return double(p[k]); }
-template <>
-__device__ __forceinline__ double load_g2<uint16_t>(const uint16_t* p, long k) {
-  return double(__uint_as_float(uint32_t(p[k]) << 16));
-}
 
 template <class T>
 __global__ void permute_g2_kernel(const T* __restrict__ g2, int nm, int ni, long nf, long f0, long nfc,
@@ -189,22 +180,24 @@ __global__ void kbuild_f64_kernel(const double* __restrict__ ws, int nw, CellTab
   Kt[iw + long(nw) * kc] = out;
 }
 
-// G[(ν, c), i] = Σ_{f in c} w_f g2[ν, i, f] over the inner states of column set c in star order;
-// rows of modes below ω_acoustic are 0 (they are skipped before g2 is read in the reference).
+// G[(ν, c), i] = Σ_{f in c} w_f g2[ν, i, f] over the inner states of column set c in star order,
+// for the column sets [c0, c1) of one streamed chunk: g2c [nm, ni, p - p0] holds their members p.
+// Rows of modes below ω_acoustic are 0 (they are skipped before g2 is read in the reference).
 template <class T>
-__global__ void coupling_sum_kernel(const T* __restrict__ g2, int nm, int ni, const int32_t* __restrict__ cptr,
-                                    const int32_t* __restrict__ members, long nc, const double* __restrict__ w_f,
-                                    const double* __restrict__ wnu, double w_ac, double* __restrict__ G) {
+__global__ void coupling_sum_chunk_kernel(const T* __restrict__ g2c, int nm, int ni, const int32_t* __restrict__ cptr,
+                                          long c0, long c1, long p0, const int32_t* __restrict__ members, long nc,
+                                          const double* __restrict__ w_f, const double* __restrict__ wnu, double w_ac,
+                                          double* __restrict__ G) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= long(nm) * ni) return;
   int nu = int(idx % nm), i = int(idx / nm);
   bool skip = wnu[nu] < w_ac;
-  for (long c = 0; c < nc; ++c) {
+  for (long c = c0; c < c1; ++c) {
     double s = 0.0;
     if (!skip)
       for (int p = cptr[c]; p < cptr[c + 1]; ++p) {
         long f = members[p];
-        s += w_f[f] * load_g2(g2, nu + long(nm) * (i + long(ni) * f));
+        s += w_f[f] * load_g2(g2c, nu + long(nm) * (i + long(ni) * (p - p0)));
       }
     G[(nu + nm * c) + long(nm) * nc * i] = s;
   }
@@ -746,20 +739,26 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
     auto d_cptr = to_device(ctx, cptr);
     auto d_mem = to_device(ctx, members);
     auto d_wf = to_device(ctx, m->w_f, size_t(nf));
-    // raw g2 on the device for the coupling sums
-    const size_t elem = m->g2_dtype == EPSP_F64 ? 8 : (m->g2_dtype == EPSP_F32 ? 4 : 2);
-    DBuf<uint8_t> g2raw;
-    g2raw.alloc(ctx, size_t(nm * ni * nf) * elem);
-    g2raw.upload(static_cast<const uint8_t*>(m->g2), size_t(nm * ni * nf) * elem, s);
+    // The coupling sums need g2 once: it streams through the device in star order, gpu_tile inner
+    // states per chunk (or up to 1 GiB of g2 per chunk), copies overlapped with the sums; g2
+    // stays in the caller's host memory.
     P->d_G.alloc(ctx, size_t(nm * P->nc * ni));
-    unsigned grid = div_up(size_t(nm * ni), 128);
-    if (m->g2_dtype == EPSP_F64)
-      coupling_sum_kernel<double><<<grid, 128, 0, s>>>(reinterpret_cast<const double*>(g2raw.p), int(nm), int(ni), d_cptr.p, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac, P->d_G.p);
-    else if (m->g2_dtype == EPSP_F32)
-      coupling_sum_kernel<float><<<grid, 128, 0, s>>>(reinterpret_cast<const float*>(g2raw.p), int(nm), int(ni), d_cptr.p, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac, P->d_G.p);
-    else
-      coupling_sum_kernel<uint16_t><<<grid, 128, 0, s>>>(reinterpret_cast<const uint16_t*>(g2raw.p), int(nm), int(ni), d_cptr.p, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac, P->d_G.p);
-    EPSP_LAUNCHED(ctx);
+    const size_t member_bytes = size_t(nm * ni) * g2_elem_bytes(m->g2_dtype);
+    const long chunk_f = opts->gpu_tile > 0 ? long(opts->gpu_tile) : std::max<long>(1, long((size_t(1) << 30) / member_bytes));
+    const unsigned grid = div_up(size_t(nm * ni), 128);
+    stream_g2_by_columns(ctx, m, members, cptr, chunk_f, [&](const void* g2c, long c0, long c1, long p0) {
+      if (m->g2_dtype == EPSP_F64)
+        coupling_sum_chunk_kernel<double><<<grid, 128, 0, s>>>(static_cast<const double*>(g2c), int(nm), int(ni), d_cptr.p, c0,
+                                                              c1, p0, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac, P->d_G.p);
+      else if (m->g2_dtype == EPSP_F32)
+        coupling_sum_chunk_kernel<float><<<grid, 128, 0, s>>>(static_cast<const float*>(g2c), int(nm), int(ni), d_cptr.p, c0,
+                                                             c1, p0, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac, P->d_G.p);
+      else
+        coupling_sum_chunk_kernel<uint16_t><<<grid, 128, 0, s>>>(static_cast<const uint16_t*>(g2c), int(nm), int(ni), d_cptr.p,
+                                                                c0, c1, p0, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac,
+                                                                P->d_G.p);
+      EPSP_LAUNCHED(ctx);
+    });
     // The cells of ω ± ω_ν, by the lookup of _interp_linear_grid (src/frequency_grids.jl:207-219):
     // the value there is (1 - t) Σ[j] + t Σ[j + 1], which is Σ[0] below the grid (t = 0) and Σ[end]
     // above it (t = 1).

@@ -147,3 +147,14 @@ def test_batched_right_hand_sides_match_the_sequential_solves(api, oracle, cc):
     with pytest.raises(ArgumentError):
         plan.run(c["sigma"], c["mu"], c["Tlist"], Omegas, solver="fixed_point", batch_rhs=4)
     plan.close()
+
+
+def test_streamed_g2_gives_the_resident_ladder(api, cc):
+    # the regrouped paths build G̃ from g2 streamed star by star (gpu_tile inner states per chunk):
+    # bitwise the one-chunk result
+    c = cc
+    s = c["setup"]
+    for path in ("gemm_fp64", "gemm_bf16"):
+        one = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], [0.1], path=path, omega_acoustic=W_AC)
+        got = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], [0.1], path=path, gpu_tile=5, omega_acoustic=W_AC)
+        assert np.array_equal(got["sigma_ladder"], one["sigma_ladder"]), path

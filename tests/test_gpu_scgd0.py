@@ -158,3 +158,19 @@ def test_temperatures_batched_in_one_launch_match_single_runs(api, oracle, cubic
             else:
                 assert np.max(np.abs(got["sigma"][:, :, t] - one["sigma"][:, :, 0])) <= 1e-6
                 assert np.max(np.abs(got["sigma"][:, :, t] - ref["sigma"][:, :, t])) <= 1e-5
+
+
+def test_streamed_g2_gives_the_resident_result(api, cubic_small):
+    # gpu_tile streams g2 through the device in star-order chunks of that many inner states (the
+    # caller's host g2 is never resident); the coupling sums run in the same order, so the GEMM
+    # paths' results are bitwise those of one chunk. FP32 and BF16 storage.
+    s = cubic_small
+    o = occ(0.0, Tlist=(300 * synthetic.KELVIN,))
+    kw = dict(eta_init=0.05, tol=0.0, maxiter=2, mu_start=[-0.5], omega_acoustic=W_AC)
+    for g2 in (s["g2"], synthetic.float32_to_bf16_bits(s["g2"])):
+        ss = dict(s, g2=np.asfortranarray(g2))
+        for path in ("gemm_fp64", "gemm_bf16"):
+            one = api.loop_scgd0(ss, o, path=path, **kw)
+            for tile in (7, 100):
+                got = api.loop_scgd0(ss, o, path=path, gpu_tile=tile, **kw)
+                assert np.array_equal(got["sigma"], one["sigma"]) and np.array_equal(got["mu"], one["mu"]), (path, tile)
