@@ -150,15 +150,23 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
   best.ms = 3.4e38f;
   for (auto& c : cand) {
     const TcOperand& B = c.bn == 256 ? B256 : B128;
-    tc_gemm_launch_with(ctx, A, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune");
+    // the untimed launch is timed too: a candidate slower than 20 ms is judged on it alone
+    float ms = 0.f;
     EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
-    for (int r = 0; r < reps; ++r)
-      tc_gemm_launch_with(ctx, A, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune");
+    tc_gemm_launch_with(ctx, A, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune");
     EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
     EPSP_CUDA(cudaEventSynchronize(e1));
-    float ms = 0.f;
     EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    c.ms = ms / float(reps);
+    c.ms = ms;
+    if (ms < 20.f && reps > 0) {
+      EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
+      for (int r = 0; r < reps; ++r)
+        tc_gemm_launch_with(ctx, A, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune");
+      EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
+      EPSP_CUDA(cudaEventSynchronize(e1));
+      EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      c.ms = ms / float(reps);
+    }
     if (c.ms < best.ms) best = c;
   }
   cudaEventDestroy(e0);

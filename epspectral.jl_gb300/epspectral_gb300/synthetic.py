@@ -101,14 +101,16 @@ def cubic_t2g_setup(N: int = 16, t: float = 0.26, tp: float = 0.08, nmodes: int 
                     wph_min: float = 0.010, wph_max: float = 0.080, g2_logmean: float = math.log(1e-3),
                     g2_logsigma: float = 1.0, g2_scale: float = 1.0, seed: int = 0,
                     ws: FrequencyGrid | None = None, omegas_spectral: FrequencyGrid | None = None,
-                    g2_dtype=np.float32, degen_cutoff: float = 1e-8) -> dict:
+                    g2_dtype=np.float32, degen_cutoff: float = 1e-8, g2_chunk: int | None = None) -> dict:
     """Three-band cubic t2g model on an N^3 Γ-centred grid with O_h symmetry.
 
     Outer states: the irreducible k points (folded components sorted, 0 <= n1 <= n2 <= n3 <= N/2)
     times the three bands sorted by energy; inner states: all N^3 k points times three bands. Each
     inner state's IBZ representative has the same sorted band energies, assigned bitwise, and the
     rotation R_f is the signed permutation g with k_f = g k_rep (R_f v_rep = v_f). Multiplets chain
-    levels at one k closer than `degen_cutoff` (src/scgd0.jl:144-160).
+    levels at one k closer than `degen_cutoff` (src/scgd0.jl:144-160). With g2_chunk, g2 is drawn
+    g2_chunk inner states at a time (another seeded stream; for sizes whose FP64 draw would not fit
+    in memory at once).
     """
     rng = np.random.default_rng(seed)
     half = N // 2
@@ -167,12 +169,21 @@ def cubic_t2g_setup(N: int = 16, t: float = 0.26, tp: float = 0.08, nmodes: int 
         iq_kk[k, :] = d[0] + N * (d[1] + N * d[2])
     wph = np.linspace(wph_min, wph_max, nmodes)
     omega_ph = np.asfortranarray(np.repeat(wph[:, None], nkf, axis=1))
-    g2 = (g2_scale * np.exp(rng.normal(g2_logmean, g2_logsigma, size=(nmodes, ni, nf)))).astype(np.float32)
-    g2 = np.asfortranarray(g2)
-    if g2_dtype == np.float64:
-        g2 = np.asfortranarray(g2.astype(np.float64))
-    elif g2_dtype == "bf16":
-        g2 = np.asfortranarray(float32_to_bf16_bits(g2))
+    if g2_chunk:
+        dt = np.uint16 if g2_dtype == "bf16" else np.dtype(g2_dtype)
+        g2 = np.empty((nmodes, ni, nf), dtype=dt, order="F")
+        for f0 in range(0, nf, g2_chunk):
+            f1 = min(nf, f0 + g2_chunk)
+            x = rng.standard_normal(size=(nmodes, ni, f1 - f0), dtype=np.float32)
+            x = np.float32(g2_scale) * np.exp(np.float32(g2_logmean) + np.float32(g2_logsigma) * x)
+            g2[:, :, f0:f1] = float32_to_bf16_bits(x) if g2_dtype == "bf16" else x.astype(dt)
+    else:
+        g2 = (g2_scale * np.exp(rng.normal(g2_logmean, g2_logsigma, size=(nmodes, ni, nf)))).astype(np.float32)
+        g2 = np.asfortranarray(g2)
+        if g2_dtype == np.float64:
+            g2 = np.asfortranarray(g2.astype(np.float64))
+        elif g2_dtype == "bf16":
+            g2 = np.asfortranarray(float32_to_bf16_bits(g2))
     multiplets = []
     for k in range(nrep):
         es = [eps_i[3 * k + b] for b in range(3)]
