@@ -409,9 +409,11 @@ __global__ void xgen_f64_kernel(const double2* __restrict__ J, const int32_t* __
 // with the tent weights folded in) in registers. Tiles are transposed through shared memory so
 // that the BF16 rows are written 16 bytes at a time.
 constexpr int kXgTiles = 8;
+constexpr int kXgPreMax = 8;  // prefetch slots per thread: windows of up to 4 x 512 values (nshift <= 222)
 
 // Batched over blockIdx.z: slot z makes the rows z 24 nwp.. of A from the vertex J + jstride r and
 // the occupations nnu + 16 r of right-hand side r = rmap[z] (r = z without rmap).
+template <int kXgPre>
 __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restrict__ J_all, long jstride,
                                                         const int* __restrict__ rmap, const int32_t* __restrict__ mt_k,
                                                         const float* __restrict__ mt_w, const float* __restrict__ nnu_all,
@@ -449,13 +451,13 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
     }
   }
   const long kt0 = long(blockIdx.y) * kXgTiles;
-  // The vertex window of the 4 pairs (b, i') of a K-tile (4 win <= 2 x 256 values) is loaded into
-  // registers one K-tile ahead and stored into the other half of a double buffer, so its global
-  // latency hides behind the current K-tile's arithmetic.
-  float2 pre[2];
+  // The vertex window of the 4 pairs (b, i') of a K-tile (4 win <= 256 kXgPre values, chosen at
+  // launch) is loaded into registers one K-tile ahead and stored into the other half of a double
+  // buffer, so its global latency hides behind the current K-tile's arithmetic.
+  float2 pre[kXgPre];
   auto load_window = [&](long k0) {
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
+    for (int q = 0; q < kXgPre; ++q) {
       const int e = threadIdx.x + 256 * q;
       float2 v = make_float2(0.f, 0.f);
       if (e < 4 * win && k0 < Kp) {
@@ -473,7 +475,7 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
   };
   auto store_window = [&](float2* dst) {
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
+    for (int q = 0; q < kXgPre; ++q) {
       const int e = threadIdx.x + 256 * q;
       if (e < 4 * win) dst[e] = pre[q];
     }
@@ -535,6 +537,21 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
     // the next window goes to the other buffer (its readers finished at the barrier above); the
     // barrier at the top of the next K-tile publishes it and retires this K-tile's tiles
     if (kt + 1 < kXgTiles) store_window(s_jbuf + ((kt + 1) & 1) * 4 * win);
+  }
+}
+
+static int xgen_pre(long ns) {
+  const long v = 4 * (32 + 2 * (ns + 2));
+  return v <= 512 ? 2 : (v <= 1024 ? 4 : 8);
+}
+
+// xgen_bf16_kernel with the fewest prefetch slots that hold the window.
+template <class... A>
+static void launch_xgen(long ns, dim3 grid, size_t smem, cudaStream_t s, A... args) {
+  switch (xgen_pre(ns)) {
+    case 2: xgen_bf16_kernel<2><<<grid, 256, smem, s>>>(args...); break;
+    case 4: xgen_bf16_kernel<4><<<grid, 256, smem, s>>>(args...); break;
+    default: xgen_bf16_kernel<8><<<grid, 256, smem, s>>>(args...); break;
   }
 }
 
@@ -1065,7 +1082,11 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       P->d_part2.alloc(ctx, size_t(P->splits2) * size_t(nw * 8 * N));
       P->opKK = two_part(P->d_KKh.p, P->d_KKl.p, nw, nw, P->Kp2, kTcBM);
       P->opY = two_part(P->d_Yh.p, P->d_Yl.p, 8 * N, nw, P->Kp2, P->bn2);
-      EPSP_CUDA(cudaFuncSetAttribute(xgen_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(xgen_smem_bytes(int(ns)))));
+      if (4 * (32 + 2 * (ns + 2)) > 256 * kXgPreMax)
+        fail(EPSP_EUNSUPPORTED, "the shift grid is too fine for the BF16 operand kernel (nshift = " + std::to_string(ns) +
+                                    " > 222); use EPSP_PATH_GEMM_FP64");
+      for (auto fn : {xgen_bf16_kernel<2>, xgen_bf16_kernel<4>, xgen_bf16_kernel<8>})
+        EPSP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(xgen_smem_bytes(int(ns)))));
     }
     EPSP_CUDA(cudaStreamSynchronize(s));
   } else {
@@ -1202,9 +1223,10 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ) {
   } else {
     long px = prof_begin(ctx, "xgen");
     const unsigned ktiles = unsigned((P->Kp / 64 + kXgTiles - 1) / kXgTiles);
-    xgen_bf16_kernel<<<dim3(unsigned(nwp / 32 * 8), ktiles, 1), 256, xgen_smem_bytes(int(ns)), s>>>(
-        J, 0, nullptr, P->d_mt_k.p, P->d_mt_w.p, P->d_nnu_f.p, int(nw), int(nwp), int(ns), int(P->nmp), int(ni), P->Kx,
-        P->Kp, P->d_Ah.p, P->d_Al.p);
+    launch_xgen(ns, dim3(unsigned(nwp / 32 * 8), ktiles, 1), xgen_smem_bytes(int(ns)), s, J, long(0),
+                static_cast<const int*>(nullptr), static_cast<const int32_t*>(P->d_mt_k.p),
+                static_cast<const float*>(P->d_mt_w.p), static_cast<const float*>(P->d_nnu_f.p), int(nw), int(nwp),
+                int(ns), int(P->nmp), int(ni), P->Kx, P->Kp, P->d_Ah.p, P->d_Al.p);
     EPSP_LAUNCHED(ctx);
     prof_end(ctx, px);
     int sp = tc_gemm_launch_with(ctx, P->opA, P->opG, P->bn, P->splits, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N,
@@ -1720,9 +1742,10 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const double2* X, int n
   const long Mt = M * nA;
   long px = prof_begin(ctx, "xgen");
   const unsigned ktiles = unsigned((P->Kp / 64 + kXgTiles - 1) / kXgTiles);
-  xgen_bf16_kernel<<<dim3(unsigned(nwp / 32 * 8), ktiles, unsigned(nA)), 256, xgen_smem_bytes(int(ns)), s>>>(
-      X, n, B.rmap.p, P->d_mt_k.p, P->d_mt_w.p, B.nnu.p, int(nw), int(nwp), int(ns), int(P->nmp), int(ni), P->Kx, P->Kp,
-      B.Ah.p, B.Al.p);
+  launch_xgen(ns, dim3(unsigned(nwp / 32 * 8), ktiles, unsigned(nA)), xgen_smem_bytes(int(ns)), s, X, n,
+              static_cast<const int*>(B.rmap.p), static_cast<const int32_t*>(P->d_mt_k.p),
+              static_cast<const float*>(P->d_mt_w.p), static_cast<const float*>(B.nnu.p), int(nw), int(nwp), int(ns),
+              int(P->nmp), int(ni), P->Kx, P->Kp, B.Ah.p, B.Al.p);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, px);
   int sp = tc_gemm_launch_with(ctx, B.opA, P->opG, P->bn, 0, int(Mt), int(N), int(P->Kx), B.part.p, Mt, Mt * N, P->d_err.p,

@@ -158,3 +158,23 @@ def test_streamed_g2_gives_the_resident_ladder(api, cc):
         one = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], [0.1], path=path, omega_acoustic=W_AC)
         got = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], [0.1], path=path, gpu_tile=5, omega_acoustic=W_AC)
         assert np.array_equal(got["sigma_ladder"], one["sigma_ladder"]), path
+
+
+@pytest.mark.parametrize("unit", [0.001, 0.0005])
+def test_apply_on_fine_shift_grids(api, oracle, unit):
+    # Fine grids make the shift window wide (nshift = 81 and 161 here, vertex windows of 4 x 198
+    # and 4 x 358 nodes): the operand kernel then stages its window with 4 and 8 prefetch slots per
+    # thread. One application against the oracle on both regrouped paths.
+    from epspectral_gb300 import graded_frequency_grid, synthetic
+    ws = graded_frequency_grid([(-0.2, 0.2, unit), (-0.8, 0.8, 10 * unit)])
+    s = synthetic.cubic_t2g_setup(N=4, ws=ws, g2_dtype=np.float64, seed=3)
+    nw, ni = len(ws), s["eps_i"].size
+    sig = np.asfortranarray(np.full((nw, ni), complex(0.001, -0.02)))
+    J = R.pseudorandom_complex(nw, 4, 3, 2, ni, seed=2.1)
+    J[0] = 0
+    J[-1] = 0
+    T = 300 * synthetic.KELVIN
+    ref = oracle.apply_ladder_kernel(s, J, sig, 0.0, T, 0.05, omega_acoustic=W_AC)
+    for path, tol in (("gemm_fp64", 1e-10), ("gemm_bf16", 1e-4)):
+        got = api.apply_ladder_kernel(s, J, sig, 0.0, T, 0.05, omega_acoustic=W_AC, path=path)
+        assert np.all(np.isfinite(got)) and rel(got, ref) <= tol, (path, rel(got, ref))
