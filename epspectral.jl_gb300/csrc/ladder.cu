@@ -75,8 +75,8 @@ struct LadderPlan {
   DBuf<__nv_bfloat16> d_Ah, d_Al, d_Gh, d_Gl;
   DBuf<float> d_part;
   DBuf<int> d_err;
-  TcOperand opA{}, opG{}, opG128{}, opG256{};
-  int bn = 128, splits = 1;  // the contraction's tile shape, picked by the autotuner at setup
+  TcOperand opA{}, opG{}, opA64{}, opG128{}, opG256{}, opA32{}, opG256_32{};
+  int bn = 128, splits = 1, bk = kTcBK;  // the contraction's tile shape, picked by the autotuner at setup
   std::vector<TcTune> tune_all;
   float tune_ms_heuristic = 0.f;
   // exchange (both paths)
@@ -783,11 +783,12 @@ static void check_ladder_model(const epsp_model* m) {
     if (m->iq_kk[k] < 0 || m->iq_kk[k] >= m->nq) fail(EPSP_EINVAL, "iq_kk out of range");
 }
 
-static TcOperand two_part(const void* hi, const void* lo, long rows, long cols, long ld, int box_rows) {
+static TcOperand two_part(const void* hi, const void* lo, long rows, long cols, long ld, int box_rows, int bk = kTcBK) {
   TcOperand op;
   op.ns = 2;
-  op.m[0] = make_tmap_bf16(hi, rows, cols, ld, box_rows);
-  op.m[1] = make_tmap_bf16(lo, rows, cols, ld, box_rows);
+  op.bk = bk;
+  op.m[0] = make_tmap_bf16(hi, rows, cols, ld, box_rows, bk);
+  op.m[1] = make_tmap_bf16(lo, rows, cols, ld, box_rows, bk);
   op.m[2] = op.m[0];
   return op;
 }
@@ -1056,16 +1057,20 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       P->d_err.zero(s);
       P->d_Ah.zero(s);
       P->d_Al.zero(s);
-      P->opA = two_part(P->d_Ah.p, P->d_Al.p, M, P->Kx, P->Kp, kTcBM);
+      P->opA64 = two_part(P->d_Ah.p, P->d_Al.p, M, P->Kx, P->Kp, kTcBM);
       P->opG128 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 128);
       P->opG256 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 256);
-      const TcTune best = tc_gemm_autotune(ctx, P->opA, P->opG128, P->opG256, int(M), int(N), int(P->Kx), P->d_part.p, M,
-                                           M * N, max_sp, P->d_err.p, 2, &P->tune_all);
+      P->opA32 = two_part(P->d_Ah.p, P->d_Al.p, M, P->Kx, P->Kp, kTcBM, 32);
+      P->opG256_32 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 256, 32);
+      const TcTune best = tc_gemm_autotune(ctx, P->opA64, P->opG128, P->opG256, int(M), int(N), int(P->Kx), P->d_part.p, M,
+                                           M * N, max_sp, P->d_err.p, 2, &P->tune_all, &P->opA32, &P->opG256_32);
       for (const auto& c : P->tune_all)
-        if (c.bn == bn_h && c.splits == sp_h) P->tune_ms_heuristic = c.ms;
+        if (c.bn == bn_h && c.splits == sp_h && c.bk == kTcBK) P->tune_ms_heuristic = c.ms;
       P->bn = best.bn;
       P->splits = best.splits;
-      P->opG = P->bn == 256 ? P->opG256 : P->opG128;
+      P->bk = best.bk;
+      P->opA = P->bk == 32 ? P->opA32 : P->opA64;
+      P->opG = P->bk == 32 ? P->opG256_32 : (P->bn == 256 ? P->opG256 : P->opG128);
       int terr = 0;
       P->d_err.download(&terr, 1, s);
       EPSP_CUDA(cudaStreamSynchronize(s));
@@ -1730,7 +1735,7 @@ static void batch_reserve(LadderPlan* P, LadderBatch& B, long R, int maxiter) {
   B.pp.alloc(ctx, size_t(R));
   B.rmap.alloc(ctx, size_t(R));
   B.Y.alloc(ctx, size_t(R * 3 * ni));
-  B.opA = two_part(B.Ah.p, B.Al.p, R * M, P->Kx, P->Kp, kTcBM);
+  B.opA = two_part(B.Ah.p, B.Al.p, R * M, P->Kx, P->Kp, kTcBM, P->bk);
   B.opY = two_part(B.Yh.p, B.Yl.p, R * 8 * N, nw, P->Kp2, P->bn2);
 }
 
@@ -2106,15 +2111,33 @@ epsp_status epsp_ladder_run_batched(epsp_ladder_plan* plan, const double* sigma,
   });
 }
 
-epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, int32_t* splits, double* ms_chosen,
-                                    double* ms_heuristic) {
+epsp_status epsp_ladder_set_gemm_config(epsp_ladder_plan* plan, int32_t bn, int32_t splits, int32_t bk) {
+  if (!plan) return EPSP_EINVAL;
+  auto* P = reinterpret_cast<LadderPlan*>(plan);
+  return lguard(P->ctx, [&] {
+    if (P->path != EPSP_PATH_GEMM_BF16) fail(EPSP_EUNSUPPORTED, "tile shapes apply to GEMM_BF16 plans");
+    const bool ok = (bk == 64 && (bn == 128 || bn == 256)) || (bk == 32 && bn == 256);
+    if (!ok) fail(EPSP_EINVAL, "tile shape must be bn 128 or 256 with bk 64, or bn 256 with bk 32");
+    const int max_sp = int(P->d_part.n / size_t(24 * P->nwp * 3 * P->ni));
+    if (splits < 1 || splits > max_sp) fail(EPSP_EINVAL, "splits must be in [1, " + std::to_string(max_sp) + "]");
+    P->bn = bn;
+    P->splits = splits;
+    P->bk = bk;
+    P->opA = bk == 32 ? P->opA32 : P->opA64;
+    P->opG = bk == 32 ? P->opG256_32 : (bn == 256 ? P->opG256 : P->opG128);
+  });
+}
+
+epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, int32_t* splits, int32_t* bk,
+                                    double* ms_chosen, double* ms_heuristic) {
   if (!plan || !bn || !splits) return EPSP_EINVAL;
   auto* P = reinterpret_cast<const LadderPlan*>(plan);
   *bn = P->bn;
   *splits = P->splits;
+  if (bk) *bk = P->bk;
   double best = 0;
   for (const auto& c : P->tune_all)
-    if (c.bn == P->bn && c.splits == P->splits) best = c.ms;
+    if (c.bn == P->bn && c.splits == P->splits && c.bk == P->bk) best = c.ms;
   if (ms_chosen) *ms_chosen = best;
   if (ms_heuristic) *ms_heuristic = P->tune_ms_heuristic;
   return EPSP_OK;

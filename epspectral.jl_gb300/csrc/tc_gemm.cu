@@ -22,17 +22,18 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-CUtensorMap make_tmap_bf16(const void* base, long rows, long cols, long ld, int box_rows) {
+CUtensorMap make_tmap_bf16(const void* base, long rows, long cols, long ld, int box_rows, int bk) {
   if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || (ld * 2) % 16 != 0)
     fail(EPSP_EINVAL, "tensor map base and row stride must be 16-byte aligned");
+  if (bk != 64 && bk != 32) fail(EPSP_EINVAL, "tensor map K box must be 64 or 32 columns");
   CUtensorMap m;
   cuuint64_t dims[2] = {cuuint64_t(cols), cuuint64_t(rows)};
   cuuint64_t strides[1] = {cuuint64_t(ld * 2)};
-  cuuint32_t box[2] = {cuuint32_t(kTcBK), cuuint32_t(box_rows)};
+  cuuint32_t box[2] = {cuuint32_t(bk), cuuint32_t(box_rows)};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) fail(EPSP_ECUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string(int(r)));
   return m;
 }
@@ -50,13 +51,15 @@ void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* b
   *splits = sp;
 }
 
-template <int BN, int STAGES, int NS>
+template <int BN, int STAGES, int NS, int BK = kTcBK>
 static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int kblocks, int per, int splits,
                    float* out, long ld_out, long split_stride, int* d_err) {
-  using L = TcSmem<BN, STAGES, NS>;
+  using L = TcSmem<BN, STAGES, NS, BK>;
+  if (A.bk != BK || B.bk != BK) fail(EPSP_EINVAL, "operand tensor maps were built for another K block");
   static bool configured = false;  // one process, one attribute setting per instantiation
   if (!configured) {
-    EPSP_CUDA(cudaFuncSetAttribute(tc_gemm_split_kernel<BN, STAGES, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::kBytes));
+    EPSP_CUDA(cudaFuncSetAttribute(tc_gemm_split_kernel<BN, STAGES, NS, BK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   L::kBytes));
     configured = true;
   }
   TcMaps maps;
@@ -65,8 +68,8 @@ static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int 
     maps.b[p] = B.m[p < NS ? p : 0];
   }
   dim3 grid((N + BN - 1) / BN, (M + kTcBM - 1) / kTcBM, splits);
-  tc_gemm_split_kernel<BN, STAGES, NS><<<grid, 128, L::kBytes, ctx->stream>>>(maps, M, N, kblocks, per, out, ld_out,
-                                                                              split_stride, d_err);
+  tc_gemm_split_kernel<BN, STAGES, NS, BK><<<grid, 128, L::kBytes, ctx->stream>>>(maps, M, N, kblocks, per, out, ld_out,
+                                                                                  split_stride, d_err);
   EPSP_LAUNCHED(ctx);
 }
 
@@ -100,13 +103,17 @@ int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn
                         float* out, long ld_out, long split_stride, int* d_err, const char* prof_name) {
   if (A.ns != 2 || B.ns != 2) fail(EPSP_EINVAL, "explicit tile shapes are for two-part operands");
   if (bn != 128 && bn != 256) fail(EPSP_EINVAL, "tile width must be 128 or 256");
-  const int kblocks = (K + kTcBK - 1) / kTcBK;
+  const int bk = A.bk;
+  if (bk == 32 && bn != 256) fail(EPSP_EINVAL, "K blocks of 32 come with tile width 256");
+  const int kblocks = (K + bk - 1) / bk;
   if (splits <= 0) splits = tc_splits_for(ctx, M, N, K, bn);
   splits = std::max(1, std::min(splits, kblocks));
   const int per = (kblocks + splits - 1) / splits;
   splits = (kblocks + per - 1) / per;
   long pi = prof_begin(ctx, prof_name);
-  if (bn == 256)
+  if (bk == 32)
+    launch<256, 4, 2, 32>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+  else if (bn == 256)
     launch<256, 2, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   else
     launch<128, 3, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
@@ -123,8 +130,8 @@ std::map<std::array<long, 5>, std::vector<TcTune>> g_tune_cache;
 
 TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, const TcOperand& B256, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int max_splits, int* d_err, int reps,
-                        std::vector<TcTune>* all) {
-  const std::array<long, 5> key{ctx->device, M, N, K, max_splits};
+                        std::vector<TcTune>* all, const TcOperand* A32, const TcOperand* B256_32) {
+  const std::array<long, 5> key{ctx->device, M, N, K, max_splits + (A32 && B256_32 ? 1000 : 0)};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
@@ -141,23 +148,29 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
     const int tiles = ((M + kTcBM - 1) / kTcBM) * ((N + bn - 1) / bn);
     const int h = std::max(1, (ctx->sm_count + tiles - 1) / tiles);
     for (int sp : {h, 2 * h})
-      if (sp <= max_splits) cand.push_back(TcTune{bn, sp, 0.f});
+      if (sp <= max_splits) {
+        cand.push_back(TcTune{bn, sp, kTcBK, 0.f});
+        if (bn == 256 && A32 && B256_32) cand.push_back(TcTune{bn, sp, 32, 0.f});
+      }
   }
   cudaEvent_t e0, e1;
   EPSP_CUDA(cudaEventCreate(&e0));
   EPSP_CUDA(cudaEventCreate(&e1));
   TcTune best{};
   best.ms = 3.4e38f;
+  auto opA = [&](const TcTune& c) -> const TcOperand& { return c.bk == 32 ? *A32 : A; };
+  auto opB = [&](const TcTune& c) -> const TcOperand& { return c.bk == 32 ? *B256_32 : (c.bn == 256 ? B256 : B128); };
   // one untimed launch first, so that no candidate pays the first launch's costs
   if (!cand.empty())
-    tc_gemm_launch_with(ctx, A, cand[0].bn == 256 ? B256 : B128, cand[0].bn, cand[0].splits, M, N, K, out, ld_out,
-                        split_stride, d_err, "autotune");
+    tc_gemm_launch_with(ctx, opA(cand[0]), opB(cand[0]), cand[0].bn, cand[0].splits, M, N, K, out, ld_out, split_stride,
+                        d_err, "autotune");
   for (auto& c : cand) {
-    const TcOperand& B = c.bn == 256 ? B256 : B128;
+    const TcOperand& A_ = opA(c);
+    const TcOperand& B = opB(c);
     // the untimed launch is timed too: a candidate slower than 20 ms is judged on it alone
     float ms = 0.f;
     EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
-    tc_gemm_launch_with(ctx, A, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune");
+    tc_gemm_launch_with(ctx, A_, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune");
     EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
     EPSP_CUDA(cudaEventSynchronize(e1));
     EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
@@ -165,7 +178,7 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
     if (ms < 20.f && reps > 0) {
       EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
       for (int r = 0; r < reps; ++r)
-        tc_gemm_launch_with(ctx, A, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune");
+        tc_gemm_launch_with(ctx, A_, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune");
       EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
       EPSP_CUDA(cudaEventSynchronize(e1));
       EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));

@@ -67,6 +67,18 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
   return uint64_t((addr >> 4) & 0x3FFF) | (uint64_t(1024 >> 4) << 32) | (uint64_t(1) << 46) | (uint64_t(2) << 61);
 }
+// The same with 64-byte swizzle: rows of 64 B (32 BF16), 8-row groups 512 B apart.
+__device__ __forceinline__ uint64_t sw64_desc(uint32_t addr) {
+  return uint64_t((addr >> 4) & 0x3FFF) | (uint64_t(512 >> 4) << 32) | (uint64_t(1) << 46) | (uint64_t(4) << 61);
+}
+// The descriptor for K blocks of BK elements (64: 128-byte rows, 32: 64-byte rows).
+template <int BK>
+__device__ __forceinline__ uint64_t sw_desc(uint32_t addr) {
+  if constexpr (BK == 64)
+    return sw128_desc(addr);
+  else
+    return sw64_desc(addr);
+}
 
 // Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, M = 128, N = n.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int n) {
@@ -103,10 +115,10 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 
 // NS = 2: operands split x = x0 + x1 (hi, lo), products 00, 01, 10 (BF16x3, ~2^-16 relative);
 // NS = 3: x = x0 + x1 + x2 (hi, mid, lo), products 00, 01, 10, 02, 11, 20 (six, ~2^-23 relative).
-template <int BN, int STAGES, int NS>
+template <int BN, int STAGES, int NS, int BK = kTcBK>
 struct TcSmem {
-  static constexpr int kA = kTcBM * kTcBK * 2;   // bytes of one A tile
-  static constexpr int kB = BN * kTcBK * 2;      // bytes of one B tile
+  static constexpr int kA = kTcBM * BK * 2;   // bytes of one A tile
+  static constexpr int kB = BN * BK * 2;      // bytes of one B tile
   static constexpr int kStage = NS * kA + NS * kB;
   static constexpr int kBars = 2 * STAGES + 1;
   static constexpr int kBytes = STAGES * kStage + 8 * kBars + 16 + 1024;  // + alignment slack
@@ -116,11 +128,11 @@ struct TcMaps {
   CUtensorMap a[3], b[3];
 };
 
-template <int BN, int STAGES, int NS>
+template <int BN, int STAGES, int NS, int BK = kTcBK>
 __global__ void __launch_bounds__(128, 1)
     tc_gemm_split_kernel(const __grid_constant__ TcMaps maps, int M, int N, int kblocks, int kb_per_split,
                          float* __restrict__ out, long ld_out, long split_stride, int* __restrict__ err) {
-  using L = TcSmem<BN, STAGES, NS>;
+  using L = TcSmem<BN, STAGES, NS, BK>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * L::kStage);
@@ -162,7 +174,7 @@ __global__ void __launch_bounds__(128, 1)
       uint8_t* st = smem + s * L::kStage;
       const uint32_t fb = full0 + 8 * s;
       mbar_expect_tx(fb, L::kStage);
-      const int kc = (kb0 + kb) * kTcBK;
+      const int kc = (kb0 + kb) * BK;
 #pragma unroll
       for (int p = 0; p < NS; ++p) {
         tma_load_2d(smem_u32(st + p * L::kA), &maps.a[p], kc, m0, fb);
@@ -189,16 +201,16 @@ __global__ void __launch_bounds__(128, 1)
       const uint32_t a0 = smem_u32(smem + s * L::kStage);
       const uint32_t b0 = a0 + NS * L::kA;
 #pragma unroll
-      for (int ks = 0; ks < kTcBK / 16; ++ks) {
-        const uint32_t off = ks * 32;  // 16 BF16 along K inside the 128-byte swizzle row
+      for (int ks = 0; ks < BK / 16; ++ks) {
+        const uint32_t off = ks * 32;  // 16 BF16 along K inside the swizzled row
         // the split products of increasing order: 00; 01, 10; (NS = 3) 02, 11, 20
-        umma_bf16(tmem, sw128_desc(a0 + off), sw128_desc(b0 + off), idesc, (kb | ks) != 0);
-        umma_bf16(tmem, sw128_desc(a0 + off), sw128_desc(b0 + L::kB + off), idesc, 1);
-        umma_bf16(tmem, sw128_desc(a0 + L::kA + off), sw128_desc(b0 + off), idesc, 1);
+        umma_bf16(tmem, sw_desc<BK>(a0 + off), sw_desc<BK>(b0 + off), idesc, (kb | ks) != 0);
+        umma_bf16(tmem, sw_desc<BK>(a0 + off), sw_desc<BK>(b0 + L::kB + off), idesc, 1);
+        umma_bf16(tmem, sw_desc<BK>(a0 + L::kA + off), sw_desc<BK>(b0 + off), idesc, 1);
         if constexpr (NS == 3) {
-          umma_bf16(tmem, sw128_desc(a0 + off), sw128_desc(b0 + 2 * L::kB + off), idesc, 1);
-          umma_bf16(tmem, sw128_desc(a0 + L::kA + off), sw128_desc(b0 + L::kB + off), idesc, 1);
-          umma_bf16(tmem, sw128_desc(a0 + 2 * L::kA + off), sw128_desc(b0 + off), idesc, 1);
+          umma_bf16(tmem, sw_desc<BK>(a0 + off), sw_desc<BK>(b0 + 2 * L::kB + off), idesc, 1);
+          umma_bf16(tmem, sw_desc<BK>(a0 + L::kA + off), sw_desc<BK>(b0 + L::kB + off), idesc, 1);
+          umma_bf16(tmem, sw_desc<BK>(a0 + 2 * L::kA + off), sw_desc<BK>(b0 + off), idesc, 1);
         }
       }
       umma_commit(empty0 + 8 * s);
@@ -245,12 +257,15 @@ __global__ void __launch_bounds__(128, 1)
 
 // A 2-D BF16 tensor map over a row-major [rows][ld] array (K contiguous, rows of `cols` valid
 // elements), box = 64 x box_rows, 128-byte swizzle; out-of-range elements read as zero.
-CUtensorMap make_tmap_bf16(const void* base, long rows, long cols, long ld, int box_rows);
+// A 2-D tensor map of a row-major BF16 matrix [rows][cols] (row stride ld elements) whose box is
+// bk columns (64: 128-byte swizzle; 32: 64-byte swizzle) by box_rows rows.
+CUtensorMap make_tmap_bf16(const void* base, long rows, long cols, long ld, int box_rows, int bk = kTcBK);
 
 // The BF16 parts of one operand: ns = 2 (hi, lo) or 3 (hi, mid, lo) tensor maps.
 struct TcOperand {
   CUtensorMap m[3];
   int ns = 2;
+  int bk = kTcBK;  // K columns of the maps' box
 };
 
 // Launches the split-precision product of A [M][K] and B [N][K] (K-major, both split into A.ns
@@ -268,13 +283,15 @@ void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* b
 // bn rows. Returns the splits used.
 int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn, int splits, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int* d_err, const char* prof_name = "tc_gemm");
+// The variant with K blocks of 32 (64-byte swizzle) and four pipeline stages, bn = 256; A and B
+// maps built with bk = 32.
 
 // The split count tc_gemm_launch_with uses for splits = 0.
 int tc_splits_for(Ctx* ctx, int M, int N, int K, int bn);
 
 // One measured candidate of the autotuner.
 struct TcTune {
-  int bn = 0, splits = 0;
+  int bn = 0, splits = 0, bk = kTcBK;
   float ms = 0.f;
 };
 
@@ -285,7 +302,8 @@ struct TcTune {
 // 128 / 256 rows.
 TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, const TcOperand& B256, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int max_splits, int* d_err, int reps,
-                        std::vector<TcTune>* all = nullptr);
+                        std::vector<TcTune>* all = nullptr, const TcOperand* A32 = nullptr,
+                        const TcOperand* B256_32 = nullptr);
 
 // x = Σ_p x_p with x_p BF16, p < ns (round to nearest at every step).
 __device__ __forceinline__ void split_bf16_n(float x, int ns, __nv_bfloat16* out) {

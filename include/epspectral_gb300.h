@@ -246,11 +246,15 @@ epsp_status epsp_ladder_run_batched(epsp_ladder_plan* plan, const double* sigma,
                                     epsp_ladder_history* hist, double* J_out);
 
 /* The tile shape the autotuner picked at setup for the ladder's tensor-core contraction (GEMM_BF16
- * plans; no counterpart in the reference): tile width bn (128 or 256), split count, and the timed
- * milliseconds per launch of the choice and of the fixed heuristic's shape (0 when not a GEMM_BF16
- * plan). */
-epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, int32_t* splits, double* ms_chosen,
-                                    double* ms_heuristic);
+ * plans; no counterpart in the reference): tile width bn (128 or 256), split count, K block bk (64
+ * or 32; may be NULL), and the timed milliseconds per launch of the choice and of the fixed
+ * heuristic's shape (0 when not a GEMM_BF16 plan). */
+epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, int32_t* splits, int32_t* bk,
+                                    double* ms_chosen, double* ms_heuristic);
+/* Overrides the autotuner's choice: tile width bn (128 or 256) with K blocks bk = 64 (128-byte
+ * swizzle; two or three pipeline stages), or bn 256 with bk = 32 (64-byte swizzle, four stages);
+ * splits within what the plan's partial buffer holds. */
+epsp_status epsp_ladder_set_gemm_config(epsp_ladder_plan* plan, int32_t bn, int32_t splits, int32_t bk);
 
 /* One application LJ = L(J) of the ladder kernel at temperature T, chemical potential mu and
  * probe frequency Omega, with sigma_T [nω, ni] complex the self-energy of that temperature:

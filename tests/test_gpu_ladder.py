@@ -178,3 +178,30 @@ def test_apply_on_fine_shift_grids(api, oracle, unit):
     for path, tol in (("gemm_fp64", 1e-10), ("gemm_bf16", 1e-4)):
         got = api.apply_ladder_kernel(s, J, sig, 0.0, T, 0.05, omega_acoustic=W_AC, path=path)
         assert np.all(np.isfinite(got)) and rel(got, ref) <= tol, (path, rel(got, ref))
+
+
+@pytest.mark.parametrize("unit", [0.01, 0.001])
+def test_every_contraction_tile_shape_matches_the_oracle(api, oracle, cc, unit):
+    # the autotuner's candidates, each forced: BN 128 and 256 with K blocks of 64 (128-byte
+    # swizzle), BN 256 with K blocks of 32 (64-byte swizzle, four stages), one and two splits
+    from epspectral_gb300 import graded_frequency_grid, synthetic
+    c = cc
+    s = c["setup"] if unit == 0.01 else synthetic.cubic_t2g_setup(
+        N=4, ws=graded_frequency_grid([(-0.2, 0.2, unit), (-0.8, 0.8, 10 * unit)]), g2_dtype=np.float64, seed=3)
+    nw, ni = len(s["omegas"]), s["eps_i"].size
+    sig = c["sigma"][:, :, 0] if unit == 0.01 else np.asfortranarray(np.full((nw, ni), complex(0.001, -0.02)))
+    J = R.pseudorandom_complex(nw, 4, 3, 2, ni, seed=0.7)
+    J[0] = 0
+    J[-1] = 0
+    T = c["Tlist"][0]
+    ref = oracle.apply_ladder_kernel(s, J, sig, c["mu"][0], T, 0.07, omega_acoustic=W_AC)
+    plan = api.LadderPlan(s, path="gemm_bf16", omega_acoustic=W_AC)
+    assert plan.gemm_config()["bn"] in (128, 256)
+    for bn, bk in ((128, 64), (256, 64), (256, 32)):
+        for sp in (1, 2):
+            plan.set_gemm_config(bn, sp, bk)
+            got = plan.apply(J, sig, c["mu"][0], T, 0.07)
+            assert np.all(np.isfinite(got)) and rel(got, ref) <= 1e-4, (bn, bk, sp, rel(got, ref))
+    with pytest.raises(ArgumentError):
+        plan.set_gemm_config(128, 1, 32)
+    plan.close()
