@@ -124,6 +124,14 @@ struct DBuf {
   }
 };
 
+// Work buffers kept by a plan across calls: (re)allocated only when they must grow.
+template <class T>
+bool ensure(DBuf<T>& b, Ctx* c, size_t count) {
+  if (b.p && b.n >= count) return false;
+  b.alloc(c, count);
+  return true;
+}
+
 template <class T>
 DBuf<T> to_device(Ctx* c, const T* h, size_t count) {
   DBuf<T> b;

@@ -89,6 +89,10 @@ struct LadderPlan {
   std::vector<double> h_tm, h_tp;
   double tab_Om = std::numeric_limits<double>::quiet_NaN();
   double cur_T = 0, cur_mu = 0, cur_Om = 0;
+  // work buffers of the solves, kept across runs
+  DBuf<double2> w_J0, w_J, w_LJ, w_W, w_part, w_scal, w_H, w_Y;
+  std::vector<DBuf<double2>> w_V;
+  std::shared_ptr<void> w_batch;  // the LadderBatch of the batched solves, kept across runs
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -1325,16 +1329,20 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
   const long nw = P->nw, ni = P->ni;
   const long n = nw * 24 * ni;
   const unsigned eb = div_up(size_t(n), 256);
-  DBuf<double2> J0, J, LJ, W, part, scal, Hdev, Ybuf;
-  J0.alloc(ctx, size_t(n));
-  J.alloc(ctx, size_t(n));
-  LJ.alloc(ctx, size_t(n));
-  W.alloc(ctx, size_t(n));
-  part.alloc(ctx, kDotBlocks);
-  scal.alloc(ctx, 1);
-  Hdev.alloc(ctx, size_t(maxiter + 2));
-  Ybuf.alloc(ctx, size_t(3 * ni));
-  std::vector<DBuf<double2>> V;
+  DBuf<double2>& J0 = P->w_J0;
+  DBuf<double2>& J = P->w_J;
+  DBuf<double2>& LJ = P->w_LJ;
+  DBuf<double2>& W = P->w_W;
+  DBuf<double2>& part = P->w_part;
+  DBuf<double2>& scal = P->w_scal;
+  DBuf<double2>& Hdev = P->w_H;
+  DBuf<double2>& Ybuf = P->w_Y;
+  for (auto* b : {&J0, &J, &LJ, &W}) ensure(*b, ctx, size_t(n));
+  ensure(part, ctx, size_t(kDotBlocks));
+  ensure(scal, ctx, 1);
+  ensure(Hdev, ctx, size_t(maxiter + 2));
+  ensure(Ybuf, ctx, size_t(3 * ni));
+  std::vector<DBuf<double2>>& V = P->w_V;
   const double btol = std::pow(std::numeric_limits<double>::epsilon(), 0.75);
   for (int64_t iT = 0; iT < nT; ++iT) {
     const double T = Tlist[iT];
@@ -1687,6 +1695,7 @@ __global__ void sub_batch_kernel(const double2* __restrict__ X, const double2* _
 // Buffers of a batch of right-hand sides (capacity cap), tensor maps over them.
 struct LadderBatch {
   long cap = 0;
+  int bk = 0;  // K block of the A maps
   DBuf<__nv_bfloat16> Ah, Al, Yh, Yl;
   DBuf<float> part, part2, nnu;
   DBuf<double> D, KY;
@@ -1736,6 +1745,7 @@ static void batch_reserve(LadderPlan* P, LadderBatch& B, long R, int maxiter) {
   B.rmap.alloc(ctx, size_t(R));
   B.Y.alloc(ctx, size_t(R * 3 * ni));
   B.opA = two_part(B.Ah.p, B.Al.p, R * M, P->Kx, P->Kp, kTcBM, P->bk);
+  B.bk = P->bk;
   B.opY = two_part(B.Yh.p, B.Yl.p, R * 8 * N, nw, P->Kp2, P->bn2);
 }
 
@@ -1823,8 +1833,15 @@ void ladder_run_batched(LadderPlan* P, const double* sigma, const double* mu, co
   const long nw = P->nw, ni = P->ni, slab = nw * ni, n = nw * 24 * ni;
   const long nPairs = nT * nO;
   const long R = std::min<long>(max_rhs, nPairs);
-  LadderBatch B;
-  batch_reserve(P, B, R, maxiter);
+  auto* Bp = static_cast<LadderBatch*>(P->w_batch.get());
+  if (!Bp || Bp->cap < R || Bp->H.n < size_t(R * (maxiter + 2)) || Bp->bk != P->bk) {
+    P->w_batch.reset();  // free the old buffers before the new ones are allocated
+    auto nb = std::make_shared<LadderBatch>();
+    batch_reserve(P, *nb, R, maxiter);
+    P->w_batch = nb;
+    Bp = nb.get();
+  }
+  LadderBatch& B = *Bp;
   DBuf<double2> S_all;
   S_all.alloc(ctx, size_t(slab * nT));
   S_all.upload(reinterpret_cast<const double2*>(sigma), size_t(slab * nT), s);

@@ -17,6 +17,8 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cmath>
+#include <array>
 #include <chrono>
 #include <limits>
 
@@ -877,9 +879,10 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
     if (!(occ->Tlist[iT] >= 0)) fail(EPSP_EINVAL, "Temperature must be positive");
   const long nw = P->nw, ni = P->ni, nwa = P->nwa;
   const long slab = nw * ni;
-  DBuf<double2> S, Snew;
-  S.alloc(ctx, size_t(slab * nT));
-  Snew.alloc(ctx, size_t(slab * nT));
+  DBuf<double2>& S = P->w_S;
+  DBuf<double2>& Snew = P->w_Snew;
+  if (ensure(S, ctx, size_t(slab * nT))) ++P->w_gen;
+  if (ensure(Snew, ctx, size_t(slab * nT))) ++P->w_gen;
   if (sigma_init) {
     for (long k = 0; k < 2 * slab * nT; ++k)
       if (!std::isfinite(sigma_init[k])) fail(EPSP_EINVAL, "Sigma_init must be finite");
@@ -902,8 +905,8 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   // the per-iteration results in one buffer (one copy back per iteration): err bits [nT], μ [nT],
   // min ∫A [nT], μ status [nT] (as int), the tensor-core wait flag
   const size_t npack = size_t(4 * nT + 1);
-  DBuf<double> d_pack;
-  d_pack.alloc(ctx, npack);
+  DBuf<double>& d_pack = P->w_pack;
+  if (ensure(d_pack, ctx, npack)) ++P->w_gen;
   d_pack.zero(s);
   auto* d_err = reinterpret_cast<unsigned long long*>(d_pack.p);
   double* d_mu = d_pack.p + nT;
@@ -915,17 +918,25 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   const unsigned eb = div_up(size_t(slab), 256);
   // Every active temperature of an iteration is processed by the same launches (slot a ->
   // temperature slots[a]); per-temperature T, μ, η_min, target and branch live on the device.
-  DBuf<int> d_slots;
-  DBuf<TParams> d_tp;
-  DBuf<double2> Sin_b;
-  DBuf<double> A_b, colsum_b, D_b;
-  d_slots.alloc(ctx, size_t(nT));
-  d_tp.alloc(ctx, size_t(nT));
-  Sin_b.alloc(ctx, size_t(slab * nT));
-  A_b.alloc(ctx, size_t(nwa * ni * nT));
-  colsum_b.alloc(ctx, size_t(ni * nT));
-  D_b.alloc(ctx, size_t(nwa * nT));
-  if (P->path == EPSP_PATH_GEMM_BF16) tc_reserve(P, nT);
+  DBuf<int>& d_slots = P->w_slots;
+  DBuf<TParams>& d_tp = P->w_tp;
+  DBuf<double2>& Sin_b = P->w_Sin;
+  DBuf<double>& A_b = P->w_A;
+  DBuf<double>& colsum_b = P->w_colsum;
+  DBuf<double>& D_b = P->w_D;
+  bool grown = false;
+  grown |= ensure(d_slots, ctx, size_t(nT));
+  grown |= ensure(d_tp, ctx, size_t(nT));
+  grown |= ensure(Sin_b, ctx, size_t(slab * nT));
+  grown |= ensure(A_b, ctx, size_t(nwa * ni * nT));
+  grown |= ensure(colsum_b, ctx, size_t(ni * nT));
+  grown |= ensure(D_b, ctx, size_t(nwa * nT));
+  if (P->path == EPSP_PATH_GEMM_BF16) {
+    const long cap0 = tc_capacity(P);
+    tc_reserve(P, nT);
+    grown |= tc_capacity(P) != cap0;
+  }
+  if (grown) ++P->w_gen;
   std::vector<TParams> h_tp(static_cast<size_t>(nT));
   std::vector<int> slots;
   // CUDA graph of the iteration body (tensor-core path; not while one of its kernels is profiled)
@@ -933,15 +944,11 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   bool use_graph = P->path == EPSP_PATH_GEMM_BF16;
   for (const char* nm : kBodyProfiles)
     if (ctx->prof_name == nm) use_graph = false;
-  cudaGraphExec_t gexec = nullptr;
-  struct ExecGuard {
-    cudaGraphExec_t* e;
-    ~ExecGuard() {
-      if (*e) cudaGraphExecDestroy(*e);
-    }
-  } eguard{&gexec};
-  int graph_nA = -1;
-  int64_t graph_launches = 0;
+  // a replayed graph bakes in the buffers, nT, fix_mu, the spin degeneracy and the active count
+  auto graph_key = [&](int nA) {
+    return std::array<long, 6>{long(nA), long(nT), long(fix_mu), P->w_gen,
+                               long(std::llround(occ->spin_degeneracy * 1e6)), long(P->path)};
+  };
   for (int32_t iter = 1; iter <= maxiter; ++iter) {
     auto t0 = std::chrono::steady_clock::now();
     slots.clear();
@@ -1010,8 +1017,9 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
       EPSP_LAUNCHED(ctx);
     };
     if (use_graph && iter > 1) {
-      if (graph_nA != nA) {
-        if (gexec) cudaGraphExecDestroy(gexec), gexec = nullptr;
+      const auto key = graph_key(nA);
+      if (!P->graph || !std::equal(key.begin(), key.end(), P->graph_key)) {
+        if (P->graph) cudaGraphExecDestroy(P->graph), P->graph = nullptr;
         const int64_t l0 = ctx->launches;
         cudaGraph_t g = nullptr;
         EPSP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -1023,15 +1031,16 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
           throw;
         }
         EPSP_CUDA(cudaStreamEndCapture(s, &g));
-        cudaError_t ie = cudaGraphInstantiate(&gexec, g, 0);
+        cudaError_t ie = cudaGraphInstantiate(&P->graph, g, 0);
         cudaGraphDestroy(g);
+        if (ie != cudaSuccess) P->graph = nullptr;
         EPSP_CUDA(ie);
-        graph_launches = ctx->launches - l0;
+        P->graph_launches = ctx->launches - l0;
         ctx->launches = l0;
-        graph_nA = nA;
+        std::copy(key.begin(), key.end(), P->graph_key);
       }
-      EPSP_CUDA(cudaGraphLaunch(gexec, s));
-      ctx->launches += graph_launches;
+      EPSP_CUDA(cudaGraphLaunch(P->graph, s));
+      ctx->launches += P->graph_launches;
     } else {
       body();
     }

@@ -46,6 +46,19 @@ struct Scgd0Plan {
   // iteration buffers
   DBuf<double2> d_Sin;
   DBuf<double> d_ImS, d_ReS, d_A, d_colsum, d_D;
+  // work buffers of scgd0_run, kept across runs (grown when a run needs more temperatures)
+  DBuf<double2> w_S, w_Snew, w_Sin;
+  DBuf<double> w_A, w_colsum, w_D, w_pack;
+  DBuf<int> w_slots;
+  DBuf<TParams> w_tp;
+  long w_gen = 0;  // bumped whenever one of them is reallocated
+  // the captured iteration of the last run, reused while its key matches
+  cudaGraphExec_t graph = nullptr;
+  long graph_key[6] = {-1, -1, -1, -1, -1, -1};
+  long graph_launches = 0;
+  ~Scgd0Plan() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
 };
 
 // Tensor-core pieces of the GEMM_BF16 path, in scgd0_tc.cu.
@@ -54,6 +67,8 @@ void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS);
 void tc_kk_assemble(Scgd0Plan* P, double2* d_Snew);
 // Buffers and tensor maps for up to nT temperatures in one iteration.
 void tc_reserve(Scgd0Plan* P, long nT);
+// The temperatures tc_reserve's buffers hold now.
+long tc_capacity(Scgd0Plan* P);
 // Σ_new of nA active temperatures at once: slot a reads the clamped Σ_in + a nω ni and writes
 // Snew_all + slots_h[a] nω ni (temperature index); per-temperature T and μ from tp (device).
 void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, const TParams* d_tp,

@@ -379,6 +379,8 @@ void tc_check(Scgd0Plan* P) { check_err(P); }
 
 int* tc_err_ptr(Scgd0Plan* P) { return P->tc->err.p; }
 
+long tc_capacity(Scgd0Plan* P) { return P->tc->ImS_b.p ? P->tc->capT : 0; }
+
 void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, const TParams* d_tp,
                 const double2* d_Sin_b, double2* d_Snew_all) {
   (void)slots_h;
