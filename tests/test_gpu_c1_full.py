@@ -1,0 +1,55 @@
+"""The CPU-runnable benchmark configuration at its full size, GPU against the oracle: the 1D Holstein
+chain (ε_k = -2t cos k, t = 1 eV, nk = 64 with k -> -k symmetry: 33 outer states, one Einstein mode
+ω0 = 0.1 eV, g = 0.2 eV so g2 = g²/(2ω0) = 0.2 eV², T = 300 K, half filling, ωs uniform on [-3, 3] eV
+at 5 meV: 1201 nodes, η_init = 10 meV; ladder at Ω = 0, 0.05, 0.1 eV by GMRES with rtol 1e-2).
+At these parameters the scGD0 iteration does not settle (max|ΔΣ| stays of order 1 eV over hundreds
+of iterations, in the oracle as on the GPU), so the loops are compared over a fixed number of
+iterations (tol = 0): the FP64 paths to 1e-10 relative in Σ, μ and the err history after five, the
+tensor-core path to |ΔΣ| <= 1e-5 eV after two; the ladder on the oracle's Σ to 1e-10 (FP64) and
+1e-4 (BF16) in σ with the same GMRES iteration counts.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+W_AC = 1e-4
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
+
+
+def test_holstein_c1_scgd0_and_ladder_at_full_size(oracle):
+    from epspectral_gb300 import FrequencyGrid, api, synthetic
+    ws = FrequencyGrid.uniform(-3.0, 3.0, 0.005)
+    assert len(ws) == 1201
+    w0, g = 0.1, 0.2
+    s = synthetic.holstein_1d_setup(64, 1.0, w0, g * g / (2 * w0), ws)
+    T = 300 * synthetic.KELVIN
+    occ = dict(Tlist=[T], nlist=[0.0], nelec=1.0, spin_degeneracy=2.0, type="metal")
+    mu0 = synthetic.bare_mu(s, T, 1.0)
+    kw = dict(eta_init=0.01, tol=0.0, maxiter=5, mu_start=[mu0], omega_acoustic=W_AC)
+    ref = oracle.loop_scgd0(s, occ, **kw)
+    for path in ("direct_fp64", "gemm_fp64"):
+        got = api.loop_scgd0(s, occ, path=path, **kw)
+        assert got["niter"] == ref["niter"] == 5, path
+        assert rel(got["sigma"], ref["sigma"]) <= 1e-10, path
+        assert abs(got["mu"][0] - ref["mu"][0]) <= 1e-10 * max(1.0, abs(ref["mu"][0])), path
+        assert np.allclose(got["history"]["err"], ref["history"]["err"], rtol=1e-8, atol=0), path
+    kw2 = dict(kw, maxiter=2)
+    ref2 = oracle.loop_scgd0(s, occ, **kw2)
+    bf = api.loop_scgd0(s, occ, path="gemm_bf16", **kw2)
+    assert np.max(np.abs(bf["sigma"] - ref2["sigma"])) <= 1e-5
+    assert abs(bf["mu"][0] - ref2["mu"][0]) <= 1e-5
+    Omegas = [0.0, 0.05, 0.1]
+    lk = dict(solver="gmres", rtol=1e-2, maxiter=30, omega_acoustic=W_AC)
+    lref = oracle.loop_ladder(s, ref["sigma"], ref["mu"], [T], Omegas, **lk)
+    assert lref["converged"].all()
+    for path, tol in (("direct_fp64", 1e-10), ("gemm_fp64", 1e-10), ("gemm_bf16", 1e-4)):
+        got = api.loop_ladder(s, ref["sigma"], ref["mu"], [T], Omegas, path=path, **lk)
+        assert got["converged"].all(), path
+        assert rel(got["sigma_bubble"], lref["sigma_bubble"]) <= tol, path
+        assert rel(got["sigma_ladder"], lref["sigma_ladder"]) <= tol, path
+        if tol == 1e-10:
+            assert np.array_equal(got["niter"], lref["niter"]), path
