@@ -647,10 +647,12 @@ __device__ __forceinline__ Cx<R> cxadd(Cx<R> a, Cx<R> b) {
 // Batched over blockIdx.y: slot z reads rows z 24 nwp.. of D (column stride ldD) and KY + z nω 24ni,
 // and writes LJ + 24 nω ni r with the propagators Gm, Gp + 4 nω ni r of right-hand side r = rmap[z]
 // (r = z without rmap).
+// With X_all, it writes X - L(X) instead of L(X) (the GMRES operator applied to X, in one pass).
 template <class R>
 __global__ void finish_gemm_kernel(const double* __restrict__ D_all, long ldD, const double* __restrict__ KY_all,
                                    const double2* __restrict__ Gm_all, const double2* __restrict__ Gp_all,
-                                   const int* __restrict__ rmap, int nw, int nwp, int ni, double2* __restrict__ LJ_all) {
+                                   const int* __restrict__ rmap, int nw, int nwp, int ni, double2* __restrict__ LJ_all,
+                                   const double2* __restrict__ X_all = nullptr) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= long(nw) * 6 * ni) return;
   const long z = blockIdx.y;
@@ -691,7 +693,13 @@ __global__ void finish_gemm_kernel(const double* __restrict__ D_all, long ldD, c
       z = cxadd(z, cxmul(cxmul(gm[c1 + 2], K[1]), gp[0 + 2 * c2]));
       z = cxadd(z, cxmul(cxmul(gm[c1], K[2]), gp[1 + 2 * c2]));
       z = cxadd(z, cxmul(cxmul(gm[c1 + 2], K[3]), gp[1 + 2 * c2]));
-      LJ[jidx(nw, w, c1 + 2 * c2, a, c0, i)] = make_double2(-double(z.x), -double(z.y));
+      const long o = jidx(nw, w, c1 + 2 * c2, a, c0, i);
+      double2 v = make_double2(-double(z.x), -double(z.y));
+      if (X_all) {
+        const double2 x = X_all[rhs * 24l * nw * ni + o];
+        v = make_double2(x.x - v.x, x.y - v.y);
+      }
+      LJ[o] = v;
     }
 }
 
@@ -755,6 +763,37 @@ __global__ void axpby_kernel(double2 a, const double2* __restrict__ x, double2 b
   if (k >= n) return;
   double2 xv = x[k], yv = y[k];
   y[k] = make_double2(a.x * xv.x - a.y * xv.y + b.x * yv.x - b.y * yv.y, a.x * xv.y + a.y * xv.x + b.x * yv.y + b.y * yv.x);
+}
+
+// y = a x (y is not read).
+__global__ void scale_kernel(double2 a, const double2* __restrict__ x, double2* __restrict__ y, long n) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double2 xv = x[k];
+  y[k] = make_double2(a.x * xv.x - a.y * xv.y, a.x * xv.y + a.y * xv.x);
+}
+
+// q -= h v (h from device memory) and the block partials of |q|^2 of the result, in the order of
+// dot_partial_kernel (the norm of what the projection leaves, in the same pass).
+__global__ void __launch_bounds__(256) axpy_norm_kernel(double2* __restrict__ q, const double2* __restrict__ v,
+                                                        const double2* __restrict__ h, long n, double2* __restrict__ part) {
+  __shared__ double sr[256];
+  const double2 hh = *h;
+  double ar = 0;
+  for (long k = long(blockIdx.x) * 256 + threadIdx.x; k < n; k += long(gridDim.x) * 256) {
+    const double2 x = v[k];
+    double2 a = q[k];
+    a = make_double2(a.x - (hh.x * x.x - hh.y * x.y), a.y - (hh.x * x.y + hh.y * x.x));
+    q[k] = a;
+    ar += a.x * a.x + a.y * a.y;
+  }
+  sr[threadIdx.x] = ar;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sr[threadIdx.x] += sr[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = make_double2(sr[0], 0.0);
 }
 
 __global__ void sub_kernel(const double2* __restrict__ x, const double2* __restrict__ y, double2* __restrict__ out, long n) {
@@ -1168,7 +1207,8 @@ static void build_Bt(LadderPlan* P, double T) {
 }
 
 // LJ = L(J) with the current propagators (apply_ladder_kernel!, src/ladder.jl:245-296).
-static void apply_L(LadderPlan* P, const double2* J, double2* LJ) {
+// With X (GEMM paths only), LJ receives X - L(J) instead.
+static void apply_L(LadderPlan* P, const double2* J, double2* LJ, const double2* X = nullptr) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
   const long nw = P->nw, ni = P->ni, ns = P->nshift;
@@ -1252,10 +1292,10 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ) {
   }
   if (P->path == EPSP_PATH_GEMM_BF16)
     finish_gemm_kernel<float><<<dim3(div_up(size_t(nw * 6 * ni), 256), 1), 256, 0, s>>>(
-        P->d_D.p, M, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ);
+        P->d_D.p, M, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
   else
     finish_gemm_kernel<double><<<dim3(div_up(size_t(nw * 6 * ni), 256), 1), 256, 0, s>>>(
-        P->d_D.p, M, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ);
+        P->d_D.p, M, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
   EPSP_LAUNCHED(ctx);
 }
 
@@ -1355,9 +1395,13 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
       EPSP_LAUNCHED(ctx);
       conductivity_dev(P, J0.p, Om, T, Ybuf, sb + 9 * idx);
       auto op = [&](const double2* x, double2* y) {  // y = x - L(x)
-        apply_L(P, x, LJ.p);
-        sub_kernel<<<eb, 256, 0, s>>>(x, LJ.p, y, n);
-        EPSP_LAUNCHED(ctx);
+        if (P->path == EPSP_PATH_DIRECT_FP64) {
+          apply_L(P, x, LJ.p);
+          sub_kernel<<<eb, 256, 0, s>>>(x, LJ.p, y, n);
+          EPSP_LAUNCHED(ctx);
+        } else {
+          apply_L(P, x, y, x);  // the last pass of the operator forms x - L(x)
+        }
       };
       if (solver == EPSP_SOLVER_GMRES) {
         // Krylov.gmres(A, b[, x0]; atol = rtol ‖J0‖, rtol = 0, itmax = maxiter), restart = false,
@@ -1371,10 +1415,9 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
           op(J.p, W.p);
           axpby_kernel<<<eb, 256, 0, s>>>(make_double2(1, 0), J0.p, make_double2(-1, 0), W.p, n);
           EPSP_LAUNCHED(ctx);
-        } else {
-          EPSP_CUDA(cudaMemcpyAsync(W.p, J0.p, size_t(n) * sizeof(double2), cudaMemcpyDeviceToDevice, s));
         }
-        const double beta = warm ? nrm_host(P, W.p, n, part, scal) : nJ0;  // a cold start's r0 is J0
+        const double2* r0 = warm ? W.p : J0.p;  // a cold start's r0 is J0 itself
+        const double beta = warm ? nrm_host(P, W.p, n, part, scal) : nJ0;
         double rNorm = beta;
         res.push_back(beta);
         bool solved = rNorm <= atol, breakdown = false;
@@ -1385,8 +1428,7 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
         if (!solved) {
           if (V.empty()) V.emplace_back();
           if (V[0].n != size_t(n)) V[0].alloc(ctx, size_t(n));
-          V[0].zero(s);
-          axpby_kernel<<<eb, 256, 0, s>>>(make_double2(1.0 / rNorm, 0), W.p, make_double2(0, 0), V[0].p, n);
+          scale_kernel<<<eb, 256, 0, s>>>(make_double2(1.0 / rNorm, 0), r0, V[0].p, n);
           EPSP_LAUNCHED(ctx);
           z.push_back(beta);
           int nr = 0;
@@ -1396,14 +1438,27 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
             op(V[size_t(inner - 1)].p, W.p);  // q = A v_k
             for (int i = 0; i < inner; ++i) {
               dot_dev(P, V[size_t(i)].p, W.p, n, part, Hdev.p + i);
-              axpy_dev_kernel<<<eb, 256, 0, s>>>(W.p, V[size_t(i)].p, Hdev.p + i, n);
-              EPSP_LAUNCHED(ctx);
+              if (i + 1 < inner) {
+                axpy_dev_kernel<<<eb, 256, 0, s>>>(W.p, V[size_t(i)].p, Hdev.p + i, n);
+                EPSP_LAUNCHED(ctx);
+              } else {  // the last projection and the norm of what remains, in one pass
+                axpy_norm_kernel<<<kDotBlocks, 256, 0, s>>>(W.p, V[size_t(i)].p, Hdev.p + i, n, part.p);
+                EPSP_LAUNCHED(ctx);
+                dot_final_kernel<<<1, 256, 0, s>>>(part.p, kDotBlocks, Hdev.p + inner);
+                EPSP_LAUNCHED(ctx);
+              }
             }
-            dot_dev(P, W.p, W.p, n, part, Hdev.p + inner);
-            std::vector<double2> hcol(size_t(inner + 1));
-            Hdev.download(hcol.data(), size_t(inner + 1), s);
+            const bool tc = P->path == EPSP_PATH_GEMM_BF16;
+            if (tc)  // the tensor-core wait flag rides along with the Hessenberg column
+              EPSP_CUDA(cudaMemcpyAsync(Hdev.p + inner + 1, P->d_err.p, sizeof(int), cudaMemcpyDeviceToDevice, s));
+            std::vector<double2> hcol(size_t(inner + 2));
+            Hdev.download(hcol.data(), size_t(inner + (tc ? 2 : 1)), s);
             EPSP_CUDA(cudaStreamSynchronize(s));
-            check_tc_err(P);
+            if (tc) {
+              int e = 0;
+              std::memcpy(&e, &hcol[size_t(inner + 1)], sizeof(int));
+              if (e) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+            }
             for (int i = 0; i < inner; ++i) R.push_back(cplx(hcol[size_t(i)].x, hcol[size_t(i)].y));
             const double Hbis = std::sqrt(hcol[size_t(inner)].x);
             for (int i = 0; i < inner - 1; ++i) {
@@ -1443,8 +1498,7 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
             if (!(solved || tired || breakdown)) {
               if (V.size() < size_t(inner + 1)) V.emplace_back();
               if (V[size_t(inner)].n != size_t(n)) V[size_t(inner)].alloc(ctx, size_t(n));
-              V[size_t(inner)].zero(s);
-              axpby_kernel<<<eb, 256, 0, s>>>(make_double2(1.0 / Hbis, 0), W.p, make_double2(0, 0), V[size_t(inner)].p, n);
+              scale_kernel<<<eb, 256, 0, s>>>(make_double2(1.0 / Hbis, 0), W.p, V[size_t(inner)].p, n);
               EPSP_LAUNCHED(ctx);
               z.push_back(zeta);
             }
@@ -1462,10 +1516,12 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
               y[size_t(i)] /= R[size_t(pos)];
           }
           // x = x0 + V y (x0 = J for a warm start, else 0)
-          if (!warm) J.zero(s);
           for (int i = 0; i < inner; ++i) {
-            axpby_kernel<<<eb, 256, 0, s>>>(make_double2(y[size_t(i)].real(), y[size_t(i)].imag()), V[size_t(i)].p,
-                                            make_double2(1, 0), J.p, n);
+            const double2 yi = make_double2(y[size_t(i)].real(), y[size_t(i)].imag());
+            if (i == 0 && !warm)
+              scale_kernel<<<eb, 256, 0, s>>>(yi, V[0].p, J.p, n);
+            else
+              axpby_kernel<<<eb, 256, 0, s>>>(yi, V[size_t(i)].p, make_double2(1, 0), J.p, n);
             EPSP_LAUNCHED(ctx);
           }
         } else if (!warm) {
