@@ -108,6 +108,22 @@ __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_doub
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
 
+// Complex arithmetic in R (double for the FP64 path; float for the BF16 path, whose products carry
+// ~1e-5 relative error already and where FP64 would make this kernel compute-bound).
+template <class R>
+struct Cx {
+  R x, y;
+};
+template <class R>
+__device__ __forceinline__ Cx<R> cxmul(Cx<R> a, Cx<R> b) {
+  return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+template <class R>
+__device__ __forceinline__ Cx<R> cxadd(Cx<R> a, Cx<R> b) {
+  return {a.x + b.x, a.y + b.y};
+}
+
+
 // Julia's inv(::ComplexF64) (Smith's algorithm).
 __device__ __forceinline__ double2 cinv_d(double c, double d) {
   if (fabs(d) <= fabs(c)) {
@@ -118,8 +134,54 @@ __device__ __forceinline__ double2 cinv_d(double c, double d) {
   return make_double2(r * t, -t);
 }
 
+// One contour component set at x = ωs ∓ Ω/2 (contour_greens!, src/ladder_kernel.jl:27-57): G^R =
+// 1/(x - ε - Σ(x)), G^A, G^K = (G^R - G^A)(1 - 2f), combined into the four Keldysh components.
+// F32 (tensor-core path): the difference x - ε - Re Σ in FP64, the reciprocal and the occupation
+// in FP32 (FP64 division and exp would make the kernel compute-bound on the FP64 units).
+template <bool F32>
+__device__ __forceinline__ void contour_g(const double2* __restrict__ col, int j, double t, double x, double eps,
+                                          double mu, double T, double2* __restrict__ G, int w, int nw, int i) {
+  const double2 lo = col[j], hi = col[j + 1];
+  const double sr = (1 - t) * lo.x + t * hi.x, si = (1 - t) * lo.y + t * hi.y;
+  double2 g[4];
+  if constexpr (F32) {
+    const float c = float(x - eps - sr), d = float(-si);
+    float gr, gi;  // Smith's 1/(c + i d)
+    if (fabsf(d) <= fabsf(c)) {
+      const float r = d / c, tt = 1.f / (c + d * r);
+      gr = tt;
+      gi = -r * tt;
+    } else {
+      const float r = c / d, tt = 1.f / (d + c * r);
+      gr = r * tt;
+      gi = -tt;
+    }
+    const float Tf = float(T);
+    const float f = Tf > 1.4901161193847656e-08f ? 1.f / (expf(float(x - mu) / Tf) + 1.f)
+                                                 : (x - mu > 0 ? 0.f : (x - mu < 0 ? 1.f : 0.5f));
+    const float fac = 1.f - 2.f * f;
+    // GR = (gr, gi), GA = (gr, -gi), GK = (GR - GA) fac = (0, 2 gi fac)
+    const float kk = 2.f * gi * fac;
+    g[0] = make_double2(double(gr), double(0.5f * kk));                 // (GR + GA + GK) / 2
+    g[1] = make_double2(0.0, double(0.5f * (2.f * gi + kk)));           // (GR - GA + GK) / 2
+    g[2] = make_double2(0.0, double(0.5f * (-2.f * gi + kk)));          // (GA - GR + GK) / 2
+    g[3] = make_double2(double(-gr), double(0.5f * kk));                // (GK - GR - GA) / 2
+  } else {
+    double2 GR = cinv_d(x - eps - sr, -si);
+    double2 GA = make_double2(GR.x, -GR.y);
+    double fac = 1 - 2 * occ_fermion_d(x - mu, T);
+    double2 GK = cscale(csub(GR, GA), fac);
+    g[0] = cscale(cadd(cadd(GR, GA), GK), 0.5);
+    g[1] = cscale(cadd(csub(GR, GA), GK), 0.5);
+    g[2] = cscale(cadd(csub(GA, GR), GK), 0.5);
+    g[3] = cscale(csub(csub(GK, GR), GA), 0.5);
+  }
+  for (int c = 0; c < 4; ++c) G[w + long(nw) * (c + 4 * i)] = g[c];
+}
+
 // contour_greens! (src/ladder_kernel.jl:27-57) of the self-energy read at ωs ∓ Ω/2 by the
 // interpolation tables (jm, tm), (jp, tp) (src/ladder.jl:321-334).
+template <bool F32>
 __global__ void propagators_kernel(const double2* __restrict__ ST, const double* __restrict__ ws, int nw,
                                    const int32_t* __restrict__ jm, const double* __restrict__ tm,
                                    const int32_t* __restrict__ jp, const double* __restrict__ tp,
@@ -129,24 +191,13 @@ __global__ void propagators_kernel(const double2* __restrict__ ST, const double*
   int i = blockIdx.y;
   if (w >= nw) return;
   const double2* col = ST + long(nw) * i;
-  for (int side = 0; side < 2; ++side) {
-    int j = side == 0 ? jm[w] : jp[w];
-    double t = side == 0 ? tm[w] : tp[w];
-    double2 lo = col[j], hi = col[j + 1];
-    double sr = (1 - t) * lo.x + t * hi.x, si = (1 - t) * lo.y + t * hi.y;
-    double x = side == 0 ? ws[w] - Om / 2 : ws[w] + Om / 2;
-    double2 GR = cinv_d(x - eps_i[i] - sr, -si);
-    double2 GA = make_double2(GR.x, -GR.y);
-    double fac = 1 - 2 * occ_fermion_d(x - mu, T);
-    double2 GK = cscale(csub(GR, GA), fac);
-    double2 g[4] = {cscale(cadd(cadd(GR, GA), GK), 0.5), cscale(cadd(csub(GR, GA), GK), 0.5),
-                    cscale(cadd(csub(GA, GR), GK), 0.5), cscale(csub(csub(GK, GR), GA), 0.5)};
-    double2* G = side == 0 ? Gm : Gp;
-    for (int c = 0; c < 4; ++c) G[w + long(nw) * (c + 4 * i)] = g[c];
-  }
+  contour_g<F32>(col, jm[w], tm[w], ws[w] - Om / 2, eps_i[i], mu, T, Gm, w, nw, i);
+  contour_g<F32>(col, jp[w], tp[w], ws[w] + Om / 2, eps_i[i], mu, T, Gp, w, nw, i);
 }
 
 // attach_greens_to_bare_vertex! (src/ladder_kernel.jl:70-73, 97-99): J0^{c1c2,c0} = Gm^{c1c0} v Gp^{c0c2}.
+// F32 (tensor-core path): the products in FP32.
+template <bool F32>
 __global__ void attach_bare_kernel(const double2* __restrict__ Gm, const double2* __restrict__ Gp,
                                    const double* __restrict__ v, int nw, int ni, double2* __restrict__ J0) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -158,7 +209,14 @@ __global__ void attach_bare_kernel(const double2* __restrict__ Gm, const double2
   int c1 = c12 % 2, c2 = c12 / 2;
   double2 a = Gm[w + long(nw) * (c1 + 2 * c0 + 4 * i)];
   double2 b = Gp[w + long(nw) * (c0 + 2 * c2 + 4 * i)];
-  J0[idx] = cmul(cscale(a, v[cart + 3 * i]), b);
+  if constexpr (F32) {
+    const float vv = float(v[cart + 3 * i]);
+    const Cx<float> av{float(a.x) * vv, float(a.y) * vv}, bb{float(b.x), float(b.y)};
+    const Cx<float> z = cxmul(av, bb);
+    J0[idx] = make_double2(double(z.x), double(z.y));
+  } else {
+    J0[idx] = cmul(cscale(a, v[cart + 3 * i]), b);
+  }
 }
 
 // Y[b, i] = Σ_ω Wω[ω] (J[ω, 22, b, c0=1, i] + J[ω, 11, b, c0=2, i]), the inner sum of
@@ -629,20 +687,6 @@ __global__ void y_gemm_kernel(const double* __restrict__ D, int nw, int nwp, lon
   Y[idx] = D[w + long(nwp) * (q + 6 * (c0 + 2 * ri)) + 24l * nwp * n];
 }
 
-// Complex arithmetic in R (double for the FP64 path; float for the BF16 path, whose products carry
-// ~1e-5 relative error already and where FP64 would make this kernel compute-bound).
-template <class R>
-struct Cx {
-  R x, y;
-};
-template <class R>
-__device__ __forceinline__ Cx<R> cxmul(Cx<R> a, Cx<R> b) {
-  return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
-}
-template <class R>
-__device__ __forceinline__ Cx<R> cxadd(Cx<R> a, Cx<R> b) {
-  return {a.x + b.x, a.y + b.y};
-}
 
 // Batched over blockIdx.y: slot z reads rows z 24 nwp.. of D (column stride ldD) and KY + z nω 24ni,
 // and writes LJ + 24 nω ni r with the propagators Gm, Gp + 4 nω ni r of right-hand side r = rmap[z]
@@ -1177,7 +1221,8 @@ static void set_propagators(LadderPlan* P, double mu, double T, double Om) {
     P->d_tp.upload(P->h_tp.data(), size_t(nw), s);
     P->tab_Om = Om;
   }
-  propagators_kernel<<<dim3(div_up(size_t(nw), 128), unsigned(ni)), 128, 0, s>>>(P->d_ST.p, P->d_ws.p, int(nw), P->d_jm.p,
+  auto propagators = P->path == EPSP_PATH_GEMM_BF16 ? propagators_kernel<true> : propagators_kernel<false>;
+  propagators<<<dim3(div_up(size_t(nw), 128), unsigned(ni)), 128, 0, s>>>(P->d_ST.p, P->d_ws.p, int(nw), P->d_jm.p,
                                                                                 P->d_tm.p, P->d_jp.p, P->d_tp.p, P->d_eps_i.p,
                                                                                 mu, T, Om, P->d_Gm.p, P->d_Gp.p, int(ni));
   EPSP_LAUNCHED(ctx);
@@ -1391,7 +1436,10 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
       const double Om = Omegas[iO];
       const int64_t idx = iO + nO * iT;
       set_propagators(P, mu[iT], T, Om);
-      attach_bare_kernel<<<eb, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
+      if (P->path == EPSP_PATH_GEMM_BF16)
+        attach_bare_kernel<true><<<eb, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
+      else
+        attach_bare_kernel<false><<<eb, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
       EPSP_LAUNCHED(ctx);
       conductivity_dev(P, J0.p, Om, T, Ybuf, sb + 9 * idx);
       auto op = [&](const double2* x, double2* y) {  // y = x - L(x)
@@ -1595,21 +1643,10 @@ __global__ void propagators_batch_kernel(const double2* __restrict__ S_all, cons
   if (w >= nw) return;
   const PairParams q = pp[z];
   const double2* col = S_all + long(nw) * ni * q.iT + long(nw) * i;
-  for (int side = 0; side < 2; ++side) {
-    int j = side == 0 ? jm_all[z * nw + w] : jp_all[z * nw + w];
-    double t = side == 0 ? tm_all[z * nw + w] : tp_all[z * nw + w];
-    double2 lo = col[j], hi = col[j + 1];
-    double sr = (1 - t) * lo.x + t * hi.x, si = (1 - t) * lo.y + t * hi.y;
-    double x = side == 0 ? ws[w] - q.Om / 2 : ws[w] + q.Om / 2;
-    double2 GR = cinv_d(x - eps_i[i] - sr, -si);
-    double2 GA = make_double2(GR.x, -GR.y);
-    double fac = 1 - 2 * occ_fermion_d(x - q.mu, q.T);
-    double2 GK = cscale(csub(GR, GA), fac);
-    double2 g[4] = {cscale(cadd(cadd(GR, GA), GK), 0.5), cscale(cadd(csub(GR, GA), GK), 0.5),
-                    cscale(cadd(csub(GA, GR), GK), 0.5), cscale(csub(csub(GK, GR), GA), 0.5)};
-    double2* G = (side == 0 ? Gm_all : Gp_all) + z * 4l * nw * ni;
-    for (int c = 0; c < 4; ++c) G[w + long(nw) * (c + 4 * i)] = g[c];
-  }
+  contour_g<true>(col, jm_all[z * nw + w], tm_all[z * nw + w], ws[w] - q.Om / 2, eps_i[i], q.mu, q.T,
+                  Gm_all + z * 4l * nw * ni, w, nw, i);
+  contour_g<true>(col, jp_all[z * nw + w], tp_all[z * nw + w], ws[w] + q.Om / 2, eps_i[i], q.mu, q.T,
+                  Gp_all + z * 4l * nw * ni, w, nw, i);
 }
 
 __global__ void attach_bare_batch_kernel(const double2* __restrict__ Gm_all, const double2* __restrict__ Gp_all,
@@ -1627,7 +1664,10 @@ __global__ void attach_bare_batch_kernel(const double2* __restrict__ Gm_all, con
   int c1 = c12 % 2, c2 = c12 / 2;
   double2 a = Gm[w + long(nw) * (c1 + 2 * c0 + 4 * i)];
   double2 b = Gp[w + long(nw) * (c0 + 2 * c2 + 4 * i)];
-  J0_all[z * n + idx] = cmul(cscale(a, v[cart + 3 * i]), b);
+  const float vv = float(v[cart + 3 * i]);
+  const Cx<float> av{float(a.x) * vv, float(a.y) * vv}, bb{float(b.x), float(b.y)};
+  const Cx<float> zz = cxmul(av, bb);
+  J0_all[z * n + idx] = make_double2(double(zz.x), double(zz.y));
 }
 
 __global__ void __launch_bounds__(256) cond_sum_batch_kernel(const double2* __restrict__ J_all, const double* __restrict__ Ww,

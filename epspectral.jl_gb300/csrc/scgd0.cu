@@ -9,6 +9,7 @@
 //                  K_t [nω, nc·nm] the kernel tensor of one iteration and temperature
 //   spectral    :  A [nωa, ni] double, D [nωa], column sums [ni]
 #include "common.cuh"
+#include "fp_pair.cuh"
 #include "g2stream.cuh"
 #include "gemm_f64.cuh"
 #include "scgd0.cuh"
@@ -252,18 +253,12 @@ __device__ __forceinline__ double imag_inv_d(double c, double d) {
 
 // Spectral functions on ωs_spectral (src/scgd0.jl:303-305): A[a, i] = -Im(1/(ωa - ε_i -
 // Σ(ωa)))/π with Σ read by the table (j_sp, t_sp) (apply_interpolation_table!).
-__device__ __forceinline__ float imag_inv_f(float c, float d) {
-  if (fabsf(d) <= fabsf(c)) {
-    const float r = d / c;
-    return -r * (1.f / (c + d * r));
-  }
-  const float r = c / d;
-  return -(1.f / (d + c * r));
-}
 
 // F32: the interpolation and the cancelling difference ωa - ε_i - Re Σ stay FP64, the reciprocal
 // is FP32 (the tensor-core path, whose Σ carries ~1e-6 eV already; FP64 division would make the
-// kernel compute-bound on the FP64 units).
+// kernel compute-bound on the FP64 units). Forming the interpolation in FP32 as well leaves an
+// absolute error ~1e-8 eV in the difference, which near a quasiparticle pole puts ~1e-5 into A
+// and, through μ, a floor of ~1e-7 eV under the iteration's convergence.
 template <bool F32>
 __global__ void spectral_A_kernel(const double2* __restrict__ Sall, int nw, long slab, const int* __restrict__ slots,
                                   const double* __restrict__ wsa, int nwa, const int32_t* __restrict__ jsp,
@@ -528,6 +523,8 @@ static size_t mu_smem_bytes(long nwa) {
 // err = max |Σ_new - Σ| over one temperature, and Σ ← Σ_new (src/scgd0.jl:326-328). The maximum of
 // non-negative doubles is taken on their bit patterns, which order the same way; NaN wins, as in
 // Julia's maximum.
+// F32 (tensor-core path): the differences in FP64, their magnitude in FP32.
+template <bool F32>
 __global__ void err_copy_kernel(const double2* __restrict__ Snew_all, double2* __restrict__ S_all, long n,
                                 const int* __restrict__ slots, unsigned long long* __restrict__ errbits_all) {
   __shared__ unsigned long long sh[256];
@@ -539,7 +536,11 @@ __global__ void err_copy_kernel(const double2* __restrict__ Snew_all, double2* _
   unsigned long long e = 0;
   if (k < n) {
     double2 a = Snew[k], b = S[k];
-    double d = hypot(a.x - b.x, a.y - b.y);
+    double d;
+    if constexpr (F32)
+      d = double(hypotf(float(a.x - b.x), float(a.y - b.y)));
+    else
+      d = hypot(a.x - b.x, a.y - b.y);
     e = (unsigned long long)__double_as_longlong(d);
     S[k] = a;
   }
@@ -1013,7 +1014,10 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
         EPSP_LAUNCHED(ctx);
         prof_end(ctx, pm);
       }
-      err_copy_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(Snew.p, S.p, slab, d_slots.p, d_err);
+      if (P->path == EPSP_PATH_GEMM_BF16)
+        err_copy_kernel<true><<<dim3(eb, unsigned(nA)), 256, 0, s>>>(Snew.p, S.p, slab, d_slots.p, d_err);
+      else
+        err_copy_kernel<false><<<dim3(eb, unsigned(nA)), 256, 0, s>>>(Snew.p, S.p, slab, d_slots.p, d_err);
       EPSP_LAUNCHED(ctx);
     };
     if (use_graph && iter > 1) {

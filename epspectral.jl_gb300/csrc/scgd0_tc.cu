@@ -9,6 +9,7 @@
 // iteration's own convergence test compares successive Σ to tol (1e-6 eV for the benchmark), and a
 // two-way split's ~2^-16 rounding of the map (~2e-6 eV here) would stall it above that.
 #include "scgd0.cuh"
+#include "fp_pair.cuh"
 #include "tc_gemm.cuh"
 
 #include <algorithm>
@@ -37,11 +38,6 @@ struct Scgd0Plan::Tc {
   DBuf<double> ImS_b;
 };
 
-__device__ __forceinline__ float2 split_df(double x) {
-  const float h = float(x);
-  return make_float2(h, float(x - double(h)));
-}
-
 __global__ void split_df_kernel(const double* __restrict__ x, long n, float2* __restrict__ out) {
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k < n) out[k] = split_df(x[k]);
@@ -58,26 +54,6 @@ __global__ void sigma_f32_kernel(const double2* __restrict__ S, long n, float4* 
   const double2 z = S[k];
   const float2 r = split_df(z.x);
   out[k] = make_float4(r.x, r.y, float(z.y), 0.f);
-}
-
-// s + e = a + b exactly (Knuth's two-sum; additions only, so no contraction into FMA applies).
-__device__ __forceinline__ float two_sum(float a, float b, float& e) {
-  const float s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-  return s;
-}
-
-// Re z = (x - ε) - Re Σ(x) with Re Σ(x) = lo + t (hi - lo): the cancelling part x - ε - lo is
-// evaluated exactly on the float pairs (two two-sums on the high words, the low words added after),
-// the small interpolation step t (hi - lo) in FP32.
-__device__ __forceinline__ float re_z(float2 x, float2 e, float4 lo, float4 hi, float t) {
-  float e1, e2;
-  const float s1 = two_sum(x.x, -e.x, e1);
-  const float s2 = two_sum(s1, -lo.x, e2);
-  const float r = s2 + (e1 + e2 + ((x.y - e.y) - lo.y));
-  const float d = (hi.x - lo.x) + (hi.y - lo.y);
-  return r - t * d;
 }
 
 // Kernel tensor of the recast Fan-Migdal sum (see kbuild_f64_kernel in scgd0.cu), written as BF16
