@@ -18,6 +18,7 @@ const PATHS = (direct_fp64 = Int32(0), gemm_fp64 = Int32(1), gemm_bf16 = Int32(2
 Base.@kwdef struct GB300Backend
     device::Int = 0
     path::Symbol = :gemm_bf16
+    batch_rhs::Union{Nothing, Int} = nothing   # solve up to this many (T, Ω) pairs together (GMRES, :gemm_bf16)
 end
 
 struct Grid
@@ -173,11 +174,21 @@ function loop_ladder(ladder, Σ, μ, Tlist, Ωs; solver, rtol, maxiter, store_ve
             check(ctx, ccall((:epsp_ladder_setup, LIB), Cint, (Ptr{Cvoid}, Ref{Model}, Ref{Options}, Ref{Ptr{Cvoid}}),
                 ctx, m, opts, plan))
             try
-                check(ctx, ccall((:epsp_ladder_run, LIB), Cint,
-                    (Ptr{Cvoid}, Ptr{ComplexF64}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Int32, Float64,
-                     Int32, Ptr{Float64}, Ptr{Float64}, Ptr{UInt8}, Ptr{Int32}, Ptr{Cvoid}, Ptr{ComplexF64}),
-                    plan[], Σh, μh, Th, nT, Ωh, nΩ, solver === :gmres ? 0 : 1, rtol, maxiter, σb, σl, conv, niter,
-                    C_NULL, J === nothing ? Ptr{ComplexF64}(C_NULL) : pointer(J)))
+                Jp = J === nothing ? Ptr{ComplexF64}(C_NULL) : pointer(J)
+                if backend.batch_rhs !== nothing && solver === :gmres
+                    # every (T, Ω) pair from x0 = 0, up to batch_rhs of them per operator application
+                    check(ctx, ccall((:epsp_ladder_run_batched, LIB), Cint,
+                        (Ptr{Cvoid}, Ptr{ComplexF64}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Float64,
+                         Int32, Int32, Ptr{Float64}, Ptr{Float64}, Ptr{UInt8}, Ptr{Int32}, Ptr{Cvoid}, Ptr{ComplexF64}),
+                        plan[], Σh, μh, Th, nT, Ωh, nΩ, rtol, maxiter, backend.batch_rhs, σb, σl, conv, niter,
+                        C_NULL, Jp))
+                else
+                    check(ctx, ccall((:epsp_ladder_run, LIB), Cint,
+                        (Ptr{Cvoid}, Ptr{ComplexF64}, Ptr{Float64}, Ptr{Float64}, Int64, Ptr{Float64}, Int64, Int32, Float64,
+                         Int32, Ptr{Float64}, Ptr{Float64}, Ptr{UInt8}, Ptr{Int32}, Ptr{Cvoid}, Ptr{ComplexF64}),
+                        plan[], Σh, μh, Th, nT, Ωh, nΩ, solver === :gmres ? 0 : 1, rtol, maxiter, σb, σl, conv, niter,
+                        C_NULL, Jp))
+                end
             finally
                 ccall((:epsp_ladder_plan_destroy, LIB), Cvoid, (Ptr{Cvoid},), plan[])
             end
