@@ -50,7 +50,7 @@ FP64_SCGD0_ITERS = 12
 FP64_LADDER_APPLIES = 2
 # DRAM bytes (read + write) of one ladder-contraction launch of this workload, from one Nsight
 # Compute capture of the same kernel on a GB300 (profiles/tc_ladder_gemm_c2.md)
-TC_LADDER_TRAFFIC_BYTES = 4.414e9 + 0.177e9
+TC_LADDER_TRAFFIC_BYTES = 4.414e9 + 0.350e9
 # learned warm start: training and held-out runs, epochs
 WARM_TRAIN_RUNS, WARM_HELDOUT_RUNS, WARM_EPOCHS = 256, 32, 40
 
@@ -80,8 +80,59 @@ def setup_bytes(s) -> int:
     return n
 
 
+class _NvmlClocks:
+    """Read-only NVML queries (SM clock, its maximum, power, clock-event reasons) through the driver's
+    libnvidia-ml, for sampling at millisecond intervals; None where the library is absent."""
+
+    # nvmlClocksEventReason* bits of the NVML API
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    @classmethod
+    def open(cls, device: int):
+        import ctypes
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return None
+        except (OSError, AttributeError):
+            return None
+        self = cls()
+        self.ct, self.lib = ctypes, lib
+        self.h = ctypes.c_void_p()
+        bus = None
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(device)
+            bus = f"{pr.pci_domain_id:08X}:{pr.pci_bus_id:02X}:{pr.pci_device_id:02X}.0"
+        except Exception:
+            pass
+        ok = bus is not None and lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(self.h)) == 0
+        if not ok and lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(device), ctypes.byref(self.h)) != 0:
+            lib.nvmlShutdown()
+            return None
+        self.reason_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        v = ctypes.c_uint()
+        self.max_mhz = float(v.value) if lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(v)) == 0 else None
+        return self
+
+    def sample(self):
+        ct, lib = self.ct, self.lib
+        mhz, mw, bits = ct.c_uint(), ct.c_uint(), ct.c_ulonglong()
+        if lib.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(mhz)) != 0:
+            return None
+        lib.nvmlDeviceGetPowerUsage(self.h, ct.byref(mw))
+        self.reason_fn(self.h, ct.byref(bits))
+        return float(mhz.value), mw.value / 1e3, [n for b, n in self.REASONS.items() if bits.value & b]
+
+    def close(self):
+        self.lib.nvmlShutdown()
+
+
 class ClockSampler:
-    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+    """SM clock, power and clock-event reasons sampled while the timed region runs: NVML every 2 ms
+    (the timed region lasts a fraction of a second), else nvidia-smi every 100 ms."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -90,9 +141,17 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
+        self.nvml = None
         self.lines = []
+        self.samples = []
+        self.stop = threading.Event()
 
     def __enter__(self):
+        self.nvml = _NvmlClocks.open(self.device)
+        if self.nvml is not None:
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "100"],
@@ -103,11 +162,22 @@ class ClockSampler:
             self.proc = None
         return self
 
+    def _poll(self):
+        while not self.stop.is_set():
+            x = self.nvml.sample()
+            if x is not None:
+                self.samples.append(x)
+            self.stop.wait(0.002)
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        if self.nvml is not None:
+            self.stop.set()
+            self.t.join(timeout=5)
+            self.nvml.close()
         if self.proc:
             self.proc.terminate()
             try:
@@ -116,6 +186,13 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        if self.nvml is not None:
+            sm = [x[0] for x in self.samples]
+            reasons = sorted({r for x in self.samples for r in x[2]})
+            return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": self.nvml.max_mhz,
+                    "sm_min_mhz": float(min(sm)) if sm else None, "reasons": reasons, "samples": len(sm),
+                    "power_w_median": float(np.median([x[1] for x in self.samples])) if sm else None,
+                    "source": "NVML every 2 ms"}
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
@@ -131,7 +208,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "nvidia-smi every 100 ms"}
 
 
 def peaks():

@@ -197,15 +197,17 @@ __global__ void propagators_kernel(const double2* __restrict__ ST, const double*
 
 // attach_greens_to_bare_vertex! (src/ladder_kernel.jl:70-73, 97-99): J0^{c1c2,c0} = Gm^{c1c0} v Gp^{c0c2}.
 // F32 (tensor-core path): the products in FP32.
+// Grid (nω / 256, 6 ni, 4): blockIdx.y = cart + 3 (c0 + 2 i), blockIdx.z = c12 (the column
+// c12 + 4 blockIdx.y of J0).
 template <bool F32>
 __global__ void attach_bare_kernel(const double2* __restrict__ Gm, const double2* __restrict__ Gp,
                                    const double* __restrict__ v, int nw, int ni, double2* __restrict__ J0) {
-  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= long(nw) * 24 * ni) return;
-  long w = idx % nw;
-  long r = idx / nw;
-  int c12 = int(r % 4), cart = int((r / 4) % 3), c0 = int((r / 12) % 2);
-  long i = r / 24;
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nw) return;
+  const int c12 = blockIdx.z, rest = blockIdx.y;
+  const long idx = (long(c12) + 4l * rest) * nw + w;
+  const int cart = rest % 3, c0 = (rest / 3) % 2;
+  const long i = rest / 6;
   int c1 = c12 % 2, c2 = c12 / 2;
   double2 a = Gm[w + long(nw) * (c1 + 2 * c0 + 4 * i)];
   double2 b = Gp[w + long(nw) * (c0 + 2 * c2 + 4 * i)];
@@ -688,28 +690,27 @@ __global__ void y_gemm_kernel(const double* __restrict__ D, int nw, int nwp, lon
 }
 
 
-// Batched over blockIdx.y: slot z reads rows z 24 nwp.. of D (column stride ldD) and KY + z nω 24ni,
-// and writes LJ + 24 nω ni r with the propagators Gm, Gp + 4 nω ni r of right-hand side r = rmap[z]
-// (r = z without rmap).
+// Grid (nω / 256, 6 ni, slots): blockIdx.y is the (a, c0, i) row set; slot z = blockIdx.z reads rows
+// z 24 nwp.. of D (column stride ldD) and KY + z nω 24ni, and writes LJ + 24 nω ni r with the
+// propagators Gm, Gp + 4 nω ni r of right-hand side r = rmap[z] (r = z without rmap).
 // With X_all, it writes X - L(X) instead of L(X) (the GMRES operator applied to X, in one pass).
 template <class R>
 __global__ void finish_gemm_kernel(const double* __restrict__ D_all, long ldD, const double* __restrict__ KY_all,
                                    const double2* __restrict__ Gm_all, const double2* __restrict__ Gp_all,
                                    const int* __restrict__ rmap, int nw, int nwp, int ni, double2* __restrict__ LJ_all,
                                    const double2* __restrict__ X_all = nullptr) {
-  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= long(nw) * 6 * ni) return;
-  const long z = blockIdx.y;
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nw) return;
+  const int r = blockIdx.y;  // (a, c0, i)
+  const long z = blockIdx.z;
   const long rhs = rmap ? rmap[z] : z;
   const double* D = D_all + z * 24 * nwp;
   const double* KY = KY_all + z * long(nw) * 24 * ni;
   const double2* Gm = Gm_all + rhs * 4l * nw * ni;
   const double2* Gp = Gp_all + rhs * 4l * nw * ni;
   double2* LJ = LJ_all + rhs * 24l * nw * ni;
-  long w = idx % nw;
-  long r = idx / nw;
-  int a = int(r % 3), c0 = int((r / 3) % 2);
-  long i = r / 6;
+  const int a = r % 3, c0 = (r / 3) % 2;
+  const long i = r / 6;
   const long n = a + 3 * i;
   auto d = [&](int q, int ri) { return R(D[w + long(nwp) * (q + 6 * (c0 + 2 * ri)) + ldD * n]); };
   auto ky = [&](int qq, int ri) { return R(KY[w + nw * (qq + 2 * (c0 + 2 * (ri + 2 * n)))]); };
@@ -1057,6 +1058,8 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
     P->nmp = (nm + 15) / 16 * 16;
     if (P->path == EPSP_PATH_GEMM_BF16 && P->nmp != 16)
       fail(EPSP_EUNSUPPORTED, "the BF16x3 ladder path takes at most 16 modes; use EPSP_PATH_GEMM_FP64");
+    if (6 * ni > 65535)  // the channel-algebra kernels put (a, c0, i) on the grid's y dimension
+      fail(EPSP_EUNSUPPORTED, "the GEMM ladder paths take at most 10922 outer states");
     P->Kx = P->nmp * 3 * ni;
     P->d_Gt.alloc(ctx, size_t(P->Kx * 3 * ni));
     P->d_Gt.zero(s);
@@ -1336,10 +1339,10 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ, const double2*
     EPSP_LAUNCHED(ctx);
   }
   if (P->path == EPSP_PATH_GEMM_BF16)
-    finish_gemm_kernel<float><<<dim3(div_up(size_t(nw * 6 * ni), 256), 1), 256, 0, s>>>(
+    finish_gemm_kernel<float><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), 1), 256, 0, s>>>(
         P->d_D.p, M, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
   else
-    finish_gemm_kernel<double><<<dim3(div_up(size_t(nw * 6 * ni), 256), 1), 256, 0, s>>>(
+    finish_gemm_kernel<double><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), 1), 256, 0, s>>>(
         P->d_D.p, M, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
   EPSP_LAUNCHED(ctx);
 }
@@ -1436,10 +1439,11 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
       const double Om = Omegas[iO];
       const int64_t idx = iO + nO * iT;
       set_propagators(P, mu[iT], T, Om);
+      const dim3 ab(div_up(size_t(nw), 256), unsigned(6 * ni), 4);
       if (P->path == EPSP_PATH_GEMM_BF16)
-        attach_bare_kernel<true><<<eb, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
+        attach_bare_kernel<true><<<ab, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
       else
-        attach_bare_kernel<false><<<eb, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
+        attach_bare_kernel<false><<<ab, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
       EPSP_LAUNCHED(ctx);
       conductivity_dev(P, J0.p, Om, T, Ybuf, sb + 9 * idx);
       auto op = [&](const double2* x, double2* y) {  // y = x - L(x)
@@ -1871,7 +1875,7 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const double2* X, int n
                            "tc_ladder_kk");
   sum_parts_kernel<<<div_up(size_t(nw * N2), 256), 256, 0, s>>>(B.part2.p, nw * N2, sp2, nw * N2, B.KY.p);
   EPSP_LAUNCHED(ctx);
-  finish_gemm_kernel<float><<<dim3(div_up(size_t(nw * 6 * ni), 256), unsigned(nA)), 256, 0, s>>>(
+  finish_gemm_kernel<float><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), unsigned(nA)), 256, 0, s>>>(
       B.D.p, Mt, B.KY.p, B.Gm.p, B.Gp.p, B.rmap.p, int(nw), int(nwp), int(ni), LJ);
   EPSP_LAUNCHED(ctx);
 }
