@@ -254,12 +254,7 @@ __device__ __forceinline__ double imag_inv_d(double c, double d) {
 // Spectral functions on ωs_spectral (src/scgd0.jl:303-305): A[a, i] = -Im(1/(ωa - ε_i -
 // Σ(ωa)))/π with Σ read by the table (j_sp, t_sp) (apply_interpolation_table!).
 
-// F32: the interpolation and the cancelling difference ωa - ε_i - Re Σ stay FP64, the reciprocal
-// is FP32 (the tensor-core path, whose Σ carries ~1e-6 eV already; FP64 division would make the
-// kernel compute-bound on the FP64 units). Forming the interpolation in FP32 as well leaves an
-// absolute error ~1e-8 eV in the difference, which near a quasiparticle pole puts ~1e-5 into A
-// and, through μ, a floor of ~1e-7 eV under the iteration's convergence.
-template <bool F32>
+// FP64 paths (the tensor-core path has its own FP32 kernels below).
 __global__ void spectral_A_kernel(const double2* __restrict__ Sall, int nw, long slab, const int* __restrict__ slots,
                                   const double* __restrict__ wsa, int nwa, const int32_t* __restrict__ jsp,
                                   const double* __restrict__ tsp, const double* __restrict__ eps_i,
@@ -276,10 +271,7 @@ __global__ void spectral_A_kernel(const double2* __restrict__ Sall, int nw, long
   double sr = (1 - t) * lo.x + t * hi.x;
   double si = (1 - t) * lo.y + t * hi.y;
   const double c = wsa[a] - eps_i[i] - sr;
-  if constexpr (F32)
-    A[a + long(nwa) * i] = double(-imag_inv_f(float(c), float(-si)) * 0.318309886183790671538f);
-  else
-    A[a + long(nwa) * i] = -imag_inv_d(c, -si) / 3.14159265358979323846;
+  A[a + long(nwa) * i] = -imag_inv_d(c, -si) / 3.14159265358979323846;
 }
 
 // Fixed-order block reduction helpers (deterministic for a fixed block size).
@@ -334,6 +326,105 @@ __global__ void __launch_bounds__(256) spectral_D_kernel(const double* __restric
   }
 }
 
+// The tensor-core path's spectral functions, in FP32 without FP64 arithmetic per (a, i) element.
+// With ωa = ω_j + d_a (j = j_sp(a), t = t_sp(a)), the denominator's real part is
+//   ωa - ε_i - [(1 - t) ReΣ_j + t ReΣ_{j+1}] = d_a - v_j - t δ_j,
+//   v_j = ε_i - ω_j + ReΣ_j,  δ_j = ReΣ_{j+1} - ReΣ_j,
+// where v_j and δ_j are formed in FP64 once per grid node (nω ni, not nωa ni) and rounded to FP32.
+// Near a pole all three terms are of the size of the grid spacing, so the FP32 difference keeps an
+// absolute error ~1e-7 h (~1e-10 eV). (Interpolating Σ in FP32 and subtracting it from ωa - ε_i
+// instead leaves ~1e-8 eV, which near a pole puts ~1e-5 into A and, through μ, a floor of ~1e-7 eV
+// under the iteration's convergence.)
+// spectral_prep: P[i][j] = (v_j, δ_j, ImΣ_j, ImΣ_{j+1}) of slot blockIdx.z. Grid (nω / 256, ni, slots).
+__global__ void spectral_prep_f32_kernel(const double2* __restrict__ Sall, int nw, long slab, const int* __restrict__ slots,
+                                         const double* __restrict__ ws, const double* __restrict__ eps_i,
+                                         float4* __restrict__ Pall, double* __restrict__ minA_all) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)  // the minimum of spectral_fin starts at +inf
+    minA_all[slots[blockIdx.z]] = INFINITY;
+  if (j >= nw) return;
+  const int i = blockIdx.y;
+  const double2* col = Sall + slab * slots[blockIdx.z] + long(nw) * i;
+  const double2 lo = col[j];
+  const double2 hi = j + 1 < nw ? col[j + 1] : lo;
+  Pall[slab * blockIdx.z + long(nw) * i + j] =
+      make_float4(float(eps_i[i] - ws[j] + lo.x), float(hi.x - lo.x), float(lo.y), float(hi.y));
+}
+
+// A[a, i] = -Im(1/(d_a - v_j - t δ_j + i((1-t) ImΣ_j + t ImΣ_{j+1})))/π, never stored: a block of
+// 256 nodes a and one chunk of states i accumulates Σ_i A w_i per node (Dpart[slot][chunk][a]) and
+// Σ_a A Wa per state (Cpart[slot][i][a-block], summed over the block's warps in warp order), both in
+// FP32 over at most ichunk resp. 256 terms. Grid (nωa / 256, ni / ichunk, slots).
+constexpr int kSpecChunk = 32;
+__global__ void __launch_bounds__(256) spectral_ad_f32_kernel(const float4* __restrict__ Pall, int nw, long slab,
+                                                              const int32_t* __restrict__ jsp, const float* __restrict__ dsp,
+                                                              const float* __restrict__ tsp, const float* __restrict__ Waf,
+                                                              const float* __restrict__ w_if, int nwa, int ni,
+                                                              float* __restrict__ Dpart, float* __restrict__ Cpart) {
+  __shared__ float sh[8][kSpecChunk];
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
+  const int i0 = blockIdx.y * kSpecChunk, i1 = min(ni, i0 + kSpecChunk);
+  const int nab = gridDim.x, nch = gridDim.y;
+  const bool ok = a < nwa;
+  const int j = ok ? jsp[a] : 0;
+  const float d = ok ? dsp[a] : 0.f, t = ok ? tsp[a] : 0.f, wa = ok ? Waf[a] : 0.f;
+  const float4* P = Pall + slab * blockIdx.z + j;
+  float dsum = 0.f;
+  for (int i = i0; i < i1; ++i) {
+    float A = 0.f;
+    if (ok) {
+      const float4 p = P[long(nw) * i];
+      const float c = d - p.x - t * p.y;
+      const float si = (1.f - t) * p.z + t * p.w;
+      // -Im(1/(c - i si))/π = -si/(π (c² + si²)); Smith's form only where the square underflows
+      const float den = fmaf(c, c, si * si);
+      A = (den > 1e-30f ? __fdividef(-si, den) : -imag_inv_f(c, -si)) * 0.318309886183790671538f;
+    }
+    dsum += A * w_if[i];
+    float cs = A * wa;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cs += __shfl_xor_sync(0xffffffffu, cs, o);
+    if (lane == 0) sh[wid][i - i0] = cs;
+  }
+  if (ok) Dpart[(long(blockIdx.z) * nch + blockIdx.y) * nwa + a] = dsum;
+  __syncthreads();
+  if (threadIdx.x < i1 - i0) {
+    float c = 0.f;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) c += sh[w][threadIdx.x];
+    Cpart[(long(blockIdx.z) * ni + i0 + threadIdx.x) * nab + blockIdx.x] = c;
+  }
+}
+
+// D[a] = Wa[a] Σ_chunk Dpart (FP64, chunk order) for blocks x < nab; the blocks after them give one
+// warp to each state i: ∫A_i = Σ Cpart over the node blocks (FP64: lanes in strides of 32, then a
+// shuffle tree), whose minimum over i goes to minA[slots[z]] by an atomic minimum of the bit
+// patterns (∫A_i >= 0, so they order as the values; spectral_prep_f32_kernel sets +inf first).
+// Grid (nab + ni / 8, slots).
+__global__ void __launch_bounds__(256) spectral_fin_f32_kernel(const float* __restrict__ Dpart, const float* __restrict__ Cpart,
+                                                               int nch, int nab, const double* __restrict__ Wa, int nwa, int ni,
+                                                               const int* __restrict__ slots, double* __restrict__ Dall,
+                                                               double* __restrict__ minA_all) {
+  const long z = blockIdx.y;
+  if (int(blockIdx.x) < nab) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nwa) return;
+    double s = 0;
+    for (int c = 0; c < nch; ++c) s += double(Dpart[(z * nch + c) * nwa + a]);
+    Dall[z * nwa + a] = s * Wa[a];
+    return;
+  }
+  const int i = (int(blockIdx.x) - nab) * 8 + int(threadIdx.x) / 32, lane = threadIdx.x % 32;
+  if (i >= ni) return;
+  const float* c = Cpart + (z * ni + i) * nab;
+  double s = 0;
+  for (int b = lane; b < nab; b += 32) s += double(c[b]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) atomicMin(reinterpret_cast<unsigned long long*>(minA_all + slots[z]), (unsigned long long)__double_as_longlong(s));
+}
+
 __global__ void __launch_bounds__(256) min_kernel(const double* __restrict__ xall, int n, const int* __restrict__ slots,
                                                   double* __restrict__ out_all) {
   __shared__ double sh[256];
@@ -365,19 +456,24 @@ __device__ __forceinline__ double float_middle_d(double x, double y) {
 // bisects to adjacent floats (Roots.find_zero on a bracket, ~64 evaluations); here a safeguarded
 // Newton iteration on the same bracket finds the same root (n is increasing in μ, with
 // dn/dμ = g Σ_a D_a f(1 - f)/T), falling back to Roots' floating-point midpoint whenever the
-// Newton step leaves the bracket, and stops at a step below 2^-50 max(|μ|, 1) or at adjacent floats.
+// Newton step leaves the bracket, and stops at a step below 2^-46 max(|μ|, 1) (the rounding noise of
+// n(μ) moves the root by ~1e-15) or at adjacent floats.
 // One cluster of kMuCluster CTAs per temperature: each CTA sums a slice of ωs_spectral in fixed
 // order, the partials are combined through distributed shared memory in rank order, so every
 // thread of the cluster holds the same totals and takes the same branches.
-// The first round evaluates n at both bracket ends and at the start x0 together. Every CTA keeps
-// E_a = exp((ωa - x0)/T) of its slice in shared memory, so that near x0 the occupations cost one
-// product and one division: exp((ωa - μ)/T) = E_a exp((x0 - μ)/T) (used while |μ - x0| <= 30 T;
-// farther out, and at T ~ 0, exp is evaluated directly).
+// The per-node work of the first round runs beforehand across the whole GPU (mu_prep_kernel): the
+// terms D_a f(ωa; a), D_a f(ωa; b), D_a f0, D_a f0 (1 - f0) at both bracket ends and at the start x0,
+// and E_a = exp((ωa - x0)/T), so that near x0 a later round's occupations cost one product and one
+// reciprocal: exp((ωa - μ)/T) = E_a exp((x0 - μ)/T) (used while |μ - x0| <= 30 T; farther out, and at
+// T ~ 0, exp is evaluated directly). The cluster then only sums.
 // status: 0 ok, 1 no sign change on the bracket.
 constexpr int kMuCluster = 8;
 constexpr int kMuThreads = 512;
 constexpr int kMuWarps = kMuThreads / 32;
-constexpr int kMuTableMax = 16384;  // slice length up to which E is tabulated (128 KiB)
+constexpr int kMuPrepThreads = 64;
+constexpr int kMuTerms = 6;              // first-round terms per node
+constexpr double kMuProbe = 8.0;         // the probes x0 -+ 8 T
+constexpr double kMuProbeExp = 2980.957987041728;  // e^8
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
@@ -385,139 +481,237 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
+// 1/x for x >= 1 to within an ulp or two of FP64 division: an FP32 reciprocal refined by two
+// Newton-Raphson steps r <- r (2 - x r) (each squares the relative error: 6e-8 -> 4e-15 -> FP64
+// rounding), on the FMA units instead of FP64 division; x beyond the FP32 range gives 0 (1/x is
+// then below 3e-39).
+__device__ __forceinline__ double recip_ge1(double x) {
+  const float xf = float(x);
+  if (isinf(xf)) return 0.0;
+  double r = double(__frcp_rn(xf));
+  r = fma(r, fma(-x, r, 1.0), r);
+  r = fma(r, fma(-x, r, 1.0), r);
+  return r;
+}
+
+// Shared by mu_prep_kernel and mu_solve_kernel: the start x0 of slot's temperature on the bracket.
+__device__ __forceinline__ double mu_start(double guess, double a, double b) {
+  return (guess > a && guess < b) ? guess : float_middle_d(a, b);
+}
+
+// Occupation from y = exp((ωa - μ)/T) (electrons: 1/(1 + y); holes: y/(1 + y)).
+__device__ __forceinline__ double occ_from_y(double y, int holes) {
+  const double r = recip_ge1(1.0 + y);
+  if (holes) return isinf(y) ? 1.0 : y * r;
+  return r;
+}
+
+// Grid (nωa / kMuPrepThreads, slots): E[slot][a] and R1[slot][q][a], q: the first round's terms at
+// the bracket ends, f0 and f0 (1 - f0) at x0, and the occupations at x0 -+ kMuProbe T (which narrow
+// the bracket before the first Newton step).
+__global__ void __launch_bounds__(kMuPrepThreads)
+    mu_prep_kernel(const double* __restrict__ Dall, const double* __restrict__ wsa, int nwa, const int* __restrict__ slots,
+                   const TParams* __restrict__ tp, double br0, double br1, double* __restrict__ E_all,
+                   double* __restrict__ R1_all) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nwa) return;
+  const long slot = blockIdx.y;
+  const int t = slots[slot];
+  const double T = tp[t].T;
+  const int holes = tp[t].holes;
+  const double x0 = mu_start(tp[t].mu, br0, br1);
+  const bool warm = T > 1.4901161193847656e-08;
+  auto occ = [&](double wa, double mu) { return occ_fermion_d(holes ? mu - wa : wa - mu, T); };
+  const double wa = wsa[k], d = Dall[slot * nwa + k];
+  auto from_E = [&](double y) { return holes ? (isinf(y) ? 1.0 : y / (1.0 + y)) : 1.0 / (y + 1.0); };
+  double f0, fl, fr, E = 0;
+  if (warm) {
+    E = exp((wa - x0) / T);
+    f0 = from_E(E);
+    fl = from_E(E * kMuProbeExp);  // at x0 - kMuProbe T: exp((ωa - x0)/T + kMuProbe)
+    fr = from_E(E / kMuProbeExp);
+  } else {
+    f0 = occ(wa, x0);
+    fl = fr = f0;
+  }
+  E_all[slot * nwa + k] = E;
+  double* R1 = R1_all + slot * kMuTerms * nwa;
+  R1[k] = d * occ(wa, br0);
+  R1[nwa + k] = d * occ(wa, br1);
+  R1[2 * nwa + k] = d * f0;
+  R1[3 * nwa + k] = d * (f0 * (1 - f0));
+  R1[4 * nwa + k] = d * fl;
+  R1[5 * nwa + k] = d * fr;
+}
+
 __global__ void __cluster_dims__(kMuCluster, 1, 1) __launch_bounds__(kMuThreads)
     mu_solve_kernel(const double* __restrict__ Dall, const double* __restrict__ wsa, int nwa, const int* __restrict__ slots,
                     const TParams* __restrict__ tp, double W, double base, double gs, double br0, double br1,
-                    double* __restrict__ mu_all, int* __restrict__ status_all) {
+                    const double* __restrict__ E_all, const double* __restrict__ R1_all, double* __restrict__ mu_all,
+                    int* __restrict__ status_all, int* __restrict__ evals_all) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned rank = cluster.block_rank();
   // one cluster per active temperature
   const int slot = blockIdx.x / kMuCluster, t = slots[slot];
   const double* D = Dall + long(nwa) * slot;
+  const double* E = E_all + long(nwa) * slot;
+  const double* R1 = R1_all + long(kMuTerms) * nwa * slot;
   const double T = tp[t].T, n_target = tp[t].n_target, guess = tp[t].mu;
   const int holes = tp[t].holes;
   double* mu_out = mu_all + t;
   int* status = status_all + t;
-  extern __shared__ double s_E[];
-  __shared__ double sh[4][kMuWarps];
-  __shared__ double part[4];
+  __shared__ double sv[kMuTerms][kMuThreads];
+  __shared__ double part[2][kMuTerms];
+  __shared__ double tot[kMuTerms];
   const int chunk = (nwa + kMuCluster - 1) / kMuCluster;
   const int a0 = int(rank) * chunk, a1 = min(nwa, a0 + chunk);
   const bool warm = T > 1.4901161193847656e-08;
-  const bool table = warm && chunk <= kMuTableMax;
   const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
-  // fixed-order totals of up to 4 per-thread sums over the cluster
-  auto reduce = [&](double (&v)[4], int nv) {
-    for (int q = 0; q < nv; ++q) {
-      const double w = warp_sum_d(v[q]);
-      if (lane == 0) sh[q][wid] = w;
-    }
+  // Fixed-order totals of up to kMuTerms per-thread sums over the cluster: warp q adds the CTA's
+  // per-thread values of sum q (lanes in strides of 32, then a shuffle tree), so the FP64 adds run in
+  // nv warps rather than in all of them; the CTA partials alternate between two buffers, so one
+  // cluster barrier per round suffices (a CTA can only overwrite a buffer after the next round's
+  // barrier, when every CTA has read it). One thread per total reads the remote partials (not every
+  // thread: that serialises on the owners' shared memory).
+  int round = 0;
+  auto reduce = [&](double* v, int nv) {
+    for (int q = 0; q < nv; ++q) sv[q][threadIdx.x] = v[q];
     __syncthreads();
+    double* pb = part[round & 1];
+    if (wid < nv) {
+      double t = 0;
+      for (int k = lane; k < kMuThreads; k += 32) t += sv[wid][k];
+      t = warp_sum_d(t);
+      if (lane == 0) pb[wid] = t;
+    }
+    cluster.sync();
     if (threadIdx.x < nv) {
       double t = 0;
-      for (int k = 0; k < kMuWarps; ++k) t += sh[threadIdx.x][k];
-      part[threadIdx.x] = t;
+      for (unsigned r = 0; r < kMuCluster; ++r) t += cluster.map_shared_rank(pb, r)[threadIdx.x];
+      tot[threadIdx.x] = t;
     }
-    cluster.sync();
-    for (int q = 0; q < nv; ++q) {
-      double t = 0;
-      for (unsigned r = 0; r < kMuCluster; ++r) t += cluster.map_shared_rank(part, r)[q];
-      v[q] = t;
-    }
-    cluster.sync();
+    __syncthreads();
+    for (int q = 0; q < nv; ++q) v[q] = tot[q];
+    ++round;
   };
   auto occ = [&](double wa, double mu) { return occ_fermion_d(holes ? mu - wa : wa - mu, T); };
-  auto from_y = [&](double y) {  // the occupation from y = exp((ωa - μ)/T)
-    if (holes) return isinf(y) ? 1.0 : y / (1.0 + y);
-    return 1.0 / (y + 1.0);
-  };
   auto total = [&](double t1) { return (holes ? (W - t1 + base) * gs : (t1 + base) * gs) - n_target; };
-  double a = br0, b = br1;
-  const double x0 = (guess > a && guess < b) ? guess : float_middle_d(a, b);
-  // round 1: n(a), n(b), n(x0) and n'(x0)
-  double fa, fb, F, dF;
-  {
-    double v[4] = {0, 0, 0, 0};
-    for (int k = a0 + int(threadIdx.x); k < a1; k += kMuThreads) {
-      const double wa = wsa[k], d = D[k];
-      double f0;
-      if (table) {
-        const double E = exp((wa - x0) / T);
-        s_E[k - a0] = E;
-        f0 = from_y(E);
-      } else {
-        f0 = occ(wa, x0);
-      }
-      v[0] += d * occ(wa, a);
-      v[1] += d * occ(wa, b);
-      v[2] += d * f0;
-      v[3] += d * (f0 * (1 - f0));
-    }
-    reduce(v, 4);
-    fa = total(v[0]);
-    fb = total(v[1]);
-    F = total(v[2]);
-    dF = warm ? gs * v[3] / T : 0.0;
-  }
-  if (fa * fb > 0) {
-    if (rank == 0 && threadIdx.x == 0) *status = 1;
-    return;
-  }
-  double result;
-  if (fa == 0) {
-    result = a;
-  } else if (fb == 0) {
-    result = b;
-  } else {
-    double x = x0;
+  // The bracket and the Newton step are scalar work: thread 0 of every CTA does it (each holds the
+  // same totals, so all CTAs take the same steps) and publishes the next point through shared
+  // memory, instead of every thread repeating it on the FP64 units.
+  __shared__ double s_x, s_scale;
+  __shared__ int s_fact, s_stop;
+  double a = br0, b = br1, fa = 0, fb = 0, x = mu_start(guess, br0, br1), result = x;
+  const double x0 = x;
+  int it = 0;
+  bool failed = false;
+  auto newton = [&](double F, double dF) -> int {  // 1: done (result set)
     result = x;
-    for (int it = 0; it < 400; ++it) {
-      if (it > 0) {
-        const double sx = (x0 - x) / T;
-        const bool fact = table && fabs(sx) <= 30.0;
-        const double scale = fact ? exp(sx) : 0.0;
-        double v[4] = {0, 0, 0, 0};
-        for (int k = a0 + int(threadIdx.x); k < a1; k += kMuThreads) {
-          const double f = fact ? from_y(s_E[k - a0] * scale) : occ(wsa[k], x);
-          v[0] += D[k] * f;
-          v[1] += D[k] * (f * (1 - f));
-        }
-        reduce(v, 2);
-        F = total(v[0]);
-        dF = warm ? gs * v[1] / T : 0.0;
-      }
-      result = x;
-      if (F == 0) break;
-      if (signbit(F) == signbit(fa)) {
-        a = x;
-        fa = F;
+    if (F == 0) return 1;
+    if (signbit(F) == signbit(fa)) {
+      a = x;
+      fa = F;
+    } else {
+      b = x;
+      fb = F;
+    }
+    double xn = x - F / dF;
+    // a converged Newton step ends the solve even when it rounds onto the end the bracket update
+    // just moved to x (otherwise the safeguard below would bisect down to adjacent floats)
+    if (dF > 0 && fabs(xn - x) <= 0x1p-46 * fmax(fabs(x), 1.0)) {
+      result = xn;
+      return 1;
+    }
+    if (!(dF > 0) || !(xn > a && xn < b)) xn = float_middle_d(a, b);
+    if (xn == a || xn == b) {
+      result = fabs(fa) <= fabs(fb) ? a : b;
+      return 1;
+    }
+    x = xn;
+    return ++it >= 400 ? 1 : 0;
+  };
+  auto publish = [&](int stop) {
+    const double sx = (x0 - x) / T;
+    const bool fact = warm && fabs(sx) <= 30.0;
+    s_x = x;
+    s_scale = fact ? exp(sx) : 0.0;
+    s_fact = fact ? 1 : 0;
+    s_stop = stop;
+  };
+  // round 1: n(a), n(b), n(x0), n'(x0) and n(x0 -+ 8T) from the prepared terms
+  {
+    double v[kMuTerms] = {0, 0, 0, 0, 0, 0};
+    for (int k = a0 + int(threadIdx.x); k < a1; k += kMuThreads)
+#pragma unroll
+      for (int q = 0; q < kMuTerms; ++q) v[q] += R1[q * nwa + k];
+    reduce(v, kMuTerms);
+    if (threadIdx.x == 0) {
+      fa = total(v[0]);
+      fb = total(v[1]);
+      int stop = 1;
+      if (fa * fb > 0) {
+        failed = true;
+      } else if (fa == 0) {
+        result = a;
+      } else if (fb == 0) {
+        result = b;
       } else {
-        b = x;
-        fb = F;
+        // the probes narrow the bracket to the side (or the 16 T window) that holds the sign change
+        const double xl = x0 - kMuProbe * T, xr = x0 + kMuProbe * T;
+        const double fl = total(v[4]), fr = total(v[5]);
+        const double F0 = total(v[2]), dF0 = warm ? gs * v[3] / T : 0.0;
+        if (warm && xl > a && xr < b && fl != 0 && fr != 0 && signbit(fl) == signbit(fr)) {
+          // x0 lies outside the narrowed bracket: its Newton step (or the midpoint) starts round 2
+          if (signbit(fl) != signbit(fa)) {
+            b = xl;
+            fb = fl;
+          } else {
+            a = xr;
+            fa = fr;
+          }
+          double xn = x0 - F0 / dF0;
+          if (!(dF0 > 0) || !(xn > a && xn < b)) xn = float_middle_d(a, b);
+          x = xn;
+          stop = 0;
+        } else {
+          if (warm && xl > a && xr < b && fl != 0 && fr != 0) {
+            a = xl;
+            fa = fl;
+            b = xr;
+            fb = fr;
+          }
+          stop = newton(F0, dF0);
+        }
       }
-      double xn = x - F / dF;
-      if (!(dF > 0) || !(xn > a && xn < b)) xn = float_middle_d(a, b);
-      if (xn == a || xn == b) {
-        result = fabs(fa) <= fabs(fb) ? a : b;
-        break;
-      }
-      if (fabs(xn - x) <= 0x1p-50 * fmax(fabs(x), 1.0)) {
-        result = xn;
-        break;
-      }
-      x = xn;
+      publish(stop);
+    }
+    __syncthreads();
+  }
+  while (!s_stop) {
+    const double xr = s_x, scale = s_scale;
+    const bool fact = s_fact != 0;
+    double v[2] = {0, 0};
+    for (int k = a0 + int(threadIdx.x); k < a1; k += kMuThreads) {
+      const double f = fact ? occ_from_y(E[k] * scale, holes) : occ(wsa[k], xr);
+      v[0] += D[k] * f;
+      v[1] += D[k] * (f * (1 - f));
+    }
+    reduce(v, 2);
+    if (threadIdx.x == 0) publish(newton(total(v[0]), warm ? gs * v[1] / T : 0.0));
+    __syncthreads();
+  }
+  // no CTA leaves while another may still read its partials
+  cluster.sync();
+  if (rank == 0 && threadIdx.x == 0) {
+    evals_all[t] = round;
+    if (failed) {
+      *status = 1;
+    } else {
+      *mu_out = result;
+      *status = 0;
     }
   }
-  if (rank == 0 && threadIdx.x == 0) {
-    *mu_out = result;
-    *status = 0;
-  }
-}
-
-static size_t mu_smem_bytes(long nwa) {
-  const long chunk = (nwa + kMuCluster - 1) / kMuCluster;
-  return chunk <= kMuTableMax ? size_t(chunk) * sizeof(double) : 0;
 }
 
 // err = max |Σ_new - Σ| over one temperature, and Σ ← Σ_new (src/scgd0.jl:326-328). The maximum of
@@ -657,6 +851,20 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
   P->d_Wa = to_device(ctx, trapezoid_weights(P->wsa.nodes));
   P->d_eps_i = to_device(ctx, m->eps_i, size_t(m->ni));
   P->d_w_i = to_device(ctx, m->w_i, size_t(m->ni));
+  {
+    std::vector<float> dspf(jsp.size()), tspf(jsp.size()), Waf(jsp.size()), w_if(static_cast<size_t>(m->ni));
+    const std::vector<double> Wa = trapezoid_weights(P->wsa.nodes);
+    for (size_t a = 0; a < jsp.size(); ++a) {
+      dspf[a] = float(P->wsa.nodes[a] - P->ws.nodes[size_t(jsp[a])]);
+      tspf[a] = float(tsp[a]);
+      Waf[a] = float(Wa[a]);
+    }
+    for (size_t i = 0; i < w_if.size(); ++i) w_if[i] = float(m->w_i[i]);
+    P->d_dspf = to_device(ctx, dspf);
+    P->d_tspf = to_device(ctx, tspf);
+    P->d_Waf = to_device(ctx, Waf);
+    P->d_w_if = to_device(ctx, w_if);
+  }
   if (m->nmult > 0) {
     P->nmult = m->nmult;
     P->d_mptr = to_device(ctx, m->mult_ptr, size_t(m->nmult + 1));
@@ -901,10 +1109,8 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   for (int32_t k = 0; k < maxiter; ++k) hist->wall[k] = 0;
   for (int64_t k = 0; k < nT; ++k) hist->iter_frozen[k] = 0;
   const double br0 = P->wsa.nodes.front() - 0.1, br1 = P->wsa.nodes.back() + 0.1;  // src/scgd0.jl:197
-  if (mu_smem_bytes(nwa) > 48 * 1024)
-    EPSP_CUDA(cudaFuncSetAttribute(mu_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(mu_smem_bytes(nwa))));
   // the per-iteration results in one buffer (one copy back per iteration): err bits [nT], μ [nT],
-  // min ∫A [nT], μ status [nT] (as int), the tensor-core wait flag
+  // min ∫A [nT], μ status [nT] and evaluations [nT] (ints, in nT doubles), the tensor-core wait flag
   const size_t npack = size_t(4 * nT + 1);
   DBuf<double>& d_pack = P->w_pack;
   if (ensure(d_pack, ctx, npack)) ++P->w_gen;
@@ -913,6 +1119,7 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   double* d_mu = d_pack.p + nT;
   double* d_minA = d_pack.p + 2 * nT;
   int* d_status = reinterpret_cast<int*>(d_pack.p + 3 * nT);
+  int* d_evals = d_status + nT;
   int* d_tcerr = reinterpret_cast<int*>(d_pack.p + 4 * nT);
   std::vector<double> h_pack(npack);
   int32_t niter = 0;
@@ -929,9 +1136,19 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   grown |= ensure(d_slots, ctx, size_t(nT));
   grown |= ensure(d_tp, ctx, size_t(nT));
   grown |= ensure(Sin_b, ctx, size_t(slab * nT));
-  grown |= ensure(A_b, ctx, size_t(nwa * ni * nT));
-  grown |= ensure(colsum_b, ctx, size_t(ni * nT));
+  const bool f32_spec = P->path == EPSP_PATH_GEMM_BF16;
+  const int spec_nab = int(div_up(size_t(nwa), 256)), spec_nch = int(div_up(size_t(ni), size_t(kSpecChunk)));
+  if (f32_spec) {
+    grown |= ensure(P->w_Pf, ctx, size_t(slab * nT));
+    grown |= ensure(P->w_Dpart, ctx, size_t(long(spec_nch) * nwa * nT));
+    grown |= ensure(P->w_Cpart, ctx, size_t(long(spec_nab) * ni * nT));
+  } else {
+    grown |= ensure(A_b, ctx, size_t(nwa * ni * nT));
+    grown |= ensure(colsum_b, ctx, size_t(ni * nT));
+  }
   grown |= ensure(D_b, ctx, size_t(nwa * nT));
+  grown |= ensure(P->w_E, ctx, size_t(nwa * nT));
+  grown |= ensure(P->w_R1, ctx, size_t(kMuTerms * nwa * nT));
   if (P->path == EPSP_PATH_GEMM_BF16) {
     const long cap0 = tc_capacity(P);
     tc_reserve(P, nT);
@@ -941,7 +1158,7 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   std::vector<TParams> h_tp(static_cast<size_t>(nT));
   std::vector<int> slots;
   // CUDA graph of the iteration body (tensor-core path; not while one of its kernels is profiled)
-  static const char* kBodyProfiles[] = {"kbuild", "tc_fm", "tc_kk", "mu"};
+  static const char* kBodyProfiles[] = {"kbuild", "tc_fm", "tc_kk", "finalize", "spectral", "mu"};
   bool use_graph = P->path == EPSP_PATH_GEMM_BF16;
   for (const char* nm : kBodyProfiles)
     if (ctx->prof_name == nm) use_graph = false;
@@ -971,7 +1188,7 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
     // into a CUDA graph and replayed (μ, T come from the device, so a replay sees the current ones)
     auto body = [&] {
       EPSP_CUDA(cudaMemsetAsync(d_err, 0, size_t(nT) * 8, s));
-      EPSP_CUDA(cudaMemsetAsync(d_status, 0, size_t(nT) * sizeof(int), s));
+      EPSP_CUDA(cudaMemsetAsync(d_status, 0, size_t(2 * nT) * sizeof(int), s));
       clamp_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(S.p, Sin_b.p, slab, d_slots.p, d_tp.p);
       EPSP_LAUNCHED(ctx);
       if (P->path == EPSP_PATH_GEMM_BF16) {
@@ -994,23 +1211,42 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
             Snew.p, int(nw), slab, d_slots.p, P->d_mptr.p, P->d_midx.p, P->nmult);
         EPSP_LAUNCHED(ctx);
       }
-      auto spectral_A = P->path == EPSP_PATH_GEMM_BF16 ? spectral_A_kernel<true> : spectral_A_kernel<false>;
-      spectral_A<<<dim3(div_up(size_t(nwa), 256), unsigned(ni), unsigned(nA)), 256, 0, s>>>(
-          Snew.p, int(nw), slab, d_slots.p, P->d_wsa.p, int(nwa), P->d_jsp.p, P->d_tsp.p, P->d_eps_i.p, A_b.p, int(ni));
-      EPSP_LAUNCHED(ctx);
-      spectral_colsum_kernel<<<dim3(unsigned(ni), unsigned(nA)), 256, 0, s>>>(A_b.p, int(nwa), int(ni), P->d_Wa.p,
-                                                                            colsum_b.p);
-      EPSP_LAUNCHED(ctx);
-      min_kernel<<<unsigned(nA), 256, 0, s>>>(colsum_b.p, int(ni), d_slots.p, d_minA);
-      EPSP_LAUNCHED(ctx);
-      if (!fix_mu) {
-        spectral_D_kernel<<<dim3(div_up(size_t(nwa), 32), unsigned(nA)), 256, 0, s>>>(A_b.p, int(nwa), int(ni), P->d_w_i.p,
-                                                                                     P->d_Wa.p, D_b.p);
+      long psp = prof_begin(ctx, "spectral");
+      if (f32_spec) {
+        spectral_prep_f32_kernel<<<dim3(div_up(size_t(nw), 256), unsigned(ni), unsigned(nA)), 256, 0, s>>>(
+            Snew.p, int(nw), slab, d_slots.p, P->d_ws.p, P->d_eps_i.p, P->w_Pf.p, d_minA);
         EPSP_LAUNCHED(ctx);
+        spectral_ad_f32_kernel<<<dim3(unsigned(spec_nab), unsigned(spec_nch), unsigned(nA)), 256, 0, s>>>(
+            P->w_Pf.p, int(nw), slab, P->d_jsp.p, P->d_dspf.p, P->d_tspf.p, P->d_Waf.p, P->d_w_if.p, int(nwa), int(ni),
+            P->w_Dpart.p, P->w_Cpart.p);
+        EPSP_LAUNCHED(ctx);
+        spectral_fin_f32_kernel<<<dim3(unsigned(spec_nab + div_up(size_t(ni), 8)), unsigned(nA)), 256, 0, s>>>(
+            P->w_Dpart.p, P->w_Cpart.p, spec_nch, spec_nab, P->d_Wa.p, int(nwa), int(ni), d_slots.p, D_b.p, d_minA);
+        EPSP_LAUNCHED(ctx);
+      } else {
+        spectral_A_kernel<<<dim3(div_up(size_t(nwa), 256), unsigned(ni), unsigned(nA)), 256, 0, s>>>(
+            Snew.p, int(nw), slab, d_slots.p, P->d_wsa.p, int(nwa), P->d_jsp.p, P->d_tsp.p, P->d_eps_i.p, A_b.p, int(ni));
+        EPSP_LAUNCHED(ctx);
+        spectral_colsum_kernel<<<dim3(unsigned(ni), unsigned(nA)), 256, 0, s>>>(A_b.p, int(nwa), int(ni), P->d_Wa.p,
+                                                                              colsum_b.p);
+        EPSP_LAUNCHED(ctx);
+        min_kernel<<<unsigned(nA), 256, 0, s>>>(colsum_b.p, int(ni), d_slots.p, d_minA);
+        EPSP_LAUNCHED(ctx);
+        if (!fix_mu) {
+          spectral_D_kernel<<<dim3(div_up(size_t(nwa), 32), unsigned(nA)), 256, 0, s>>>(A_b.p, int(nwa), int(ni),
+                                                                                       P->d_w_i.p, P->d_Wa.p, D_b.p);
+          EPSP_LAUNCHED(ctx);
+        }
+      }
+      prof_end(ctx, psp);
+      if (!fix_mu) {
         long pm = prof_begin(ctx, "mu");
-        mu_solve_kernel<<<unsigned(kMuCluster * nA), kMuThreads, mu_smem_bytes(nwa), s>>>(
-            D_b.p, P->d_wsa.p, int(nwa), d_slots.p, d_tp.p, P->W, P->nstates_base, occ->spin_degeneracy, br0, br1, d_mu,
-            d_status);
+        mu_prep_kernel<<<dim3(div_up(size_t(nwa), kMuPrepThreads), unsigned(nA)), kMuPrepThreads, 0, s>>>(
+            D_b.p, P->d_wsa.p, int(nwa), d_slots.p, d_tp.p, br0, br1, P->w_E.p, P->w_R1.p);
+        EPSP_LAUNCHED(ctx);
+        mu_solve_kernel<<<unsigned(kMuCluster * nA), kMuThreads, 0, s>>>(
+            D_b.p, P->d_wsa.p, int(nwa), d_slots.p, d_tp.p, P->W, P->nstates_base, occ->spin_degeneracy, br0, br1,
+            P->w_E.p, P->w_R1.p, d_mu, d_status, d_evals);
         EPSP_LAUNCHED(ctx);
         prof_end(ctx, pm);
       }
@@ -1082,6 +1318,9 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
         active[size_t(iT)] = 0;
         hist->iter_frozen[iT] = iter;
       }
+      if (P->verbosity >= 2)
+        std::fprintf(stderr, "scgd0 iteration %d, T = %.6g: err = %.3e, mu = %.15g, mu evaluations %d\n", int(iter),
+                     occ->Tlist[iT], err, mu[size_t(iT)], fix_mu ? 0 : h_status[size_t(nT + iT)]);
     }
     if (warm && iter == 1 && iter < maxiter)
       for (int64_t iT = 0; iT < nT; ++iT)

@@ -25,6 +25,8 @@ struct Scgd0Plan {
   // grid tables
   DBuf<int32_t> d_jtab, d_jsp;
   DBuf<double> d_ws, d_wsa, d_tsp, d_Wa, d_eps_i, d_w_i, d_KK;
+  // FP32 copies for the tensor-core path's spectral functions: ωa - ω_j(a), t(a), Wa, w_i
+  DBuf<float> d_dspf, d_tspf, d_Waf, d_w_if;
   CellTableDev ct{};
   long nmult = 0;
   DBuf<int32_t> d_mptr, d_midx;
@@ -49,6 +51,10 @@ struct Scgd0Plan {
   // work buffers of scgd0_run, kept across runs (grown when a run needs more temperatures)
   DBuf<double2> w_S, w_Snew, w_Sin;
   DBuf<double> w_A, w_colsum, w_D, w_pack;
+  // μ solve tables (E, first-round terms) and the FP32 spectral path's per-node Σ terms and partials
+  DBuf<double> w_E, w_R1;
+  DBuf<float4> w_Pf;
+  DBuf<float> w_Dpart, w_Cpart;
   DBuf<int> w_slots;
   DBuf<TParams> w_tp;
   long w_gen = 0;  // bumped whenever one of them is reallocated

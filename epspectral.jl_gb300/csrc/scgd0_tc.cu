@@ -33,6 +33,8 @@ struct Scgd0Plan::Tc {
   DBuf<float2> xf, ef;
   DBuf<float> tf, Ff;
   DBuf<float4> Sf;
+  // 1 for modes below the acoustic cutoff (left out of the sum)
+  DBuf<uint8_t> skip;
   // batched iteration: capacity in temperatures, ImΣ of every slot
   long capT = 1;
   DBuf<double> ImS_b;
@@ -65,15 +67,15 @@ __global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, long slab, con
                                                           const int32_t* __restrict__ cell_j,
                                                           const float* __restrict__ cell_t,
                                                           const float2* __restrict__ cell_x,
-                                                          const double* __restrict__ wnu, int nm,
+                                                          const uint8_t* __restrict__ skip, int nm,
                                                           const float2* __restrict__ eps_c,
-                                                          const int32_t* __restrict__ col_c, long nk,
-                                                          const float* __restrict__ F_all, double w_ac,
+                                                          const int32_t* __restrict__ col_c, int nk,
+                                                          const float* __restrict__ F_all,
                                                           __nv_bfloat16* __restrict__ K0, __nv_bfloat16* __restrict__ K1,
                                                           __nv_bfloat16* __restrict__ K2, long Kp) {
   __shared__ float tile[64][33];
   const int w0 = blockIdx.x * 32;
-  const long k0 = long(blockIdx.y) * 64;
+  const int k0 = blockIdx.y * 64;
   const int tw = threadIdx.x % 32, tk = threadIdx.x / 32;
   const int iw = w0 + tw;
   const long nwm = long(nw) * nm;
@@ -84,12 +86,11 @@ __global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, long slab, con
 #pragma unroll 2
   for (int r = 0; r < 8; ++r) {
     const int kl = tk + 8 * r;
-    const long k = k0 + kl;
+    const int k = k0 + kl;  // 32-bit index arithmetic: nk < 2^30
     float v = 0.f;
     if (iw < nw && k < nk) {
-      const int nu = int(k % nm);
-      const long c = k / nm;
-      if (!(wnu[nu] < w_ac)) {
+      const int c = k / nm, nu = k - c * nm;
+      if (!skip[nu]) {
         const float4* col = Sf + long(nw) * col_c[c];
         const float2 e = eps_c[c];
         const long ia = iw + long(nw) * nu, ie = ia + nwm;
@@ -100,8 +101,10 @@ __global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, long slab, con
         const float zer = re_z(cell_x[ie], e, le, he, te);
         const float sia = (1.f - ta) * la.z + ta * ha.z;  // Im Σ(x)
         const float sie = (1.f - te) * le.z + te * he.z;
-        const float ga = sia / (zar * zar + sia * sia);  // Im 1/z with Im z = -Im Σ
-        const float ge = sie / (zer * zer + sie * sie);
+        // Im 1/z with Im z = -Im Σ; the K tensor carries FP32 precision, so an approximate
+        // division (2 ulp; denominators here lie far inside its range) is enough
+        const float ga = __fdividef(sia, zar * zar + sia * sia);
+        const float ge = __fdividef(sie, zer * zer + sie * sie);
         v = ga * F[ia] + ge * F[ie];
       }
     }
@@ -248,6 +251,14 @@ void tc_setup(Scgd0Plan* P) {
   }
   T->err.alloc(ctx, 1);
   T->err.zero(s);
+  {
+    std::vector<double> wnu(static_cast<size_t>(P->nm));
+    P->d_wnu.download(wnu.data(), wnu.size(), s);
+    EPSP_CUDA(cudaStreamSynchronize(s));
+    std::vector<uint8_t> skip(wnu.size());
+    for (size_t nu = 0; nu < wnu.size(); ++nu) skip[nu] = wnu[nu] < P->w_ac ? 1 : 0;
+    T->skip = to_device(ctx, skip);
+  }
   // B of the contraction: G [nk, ni] column-major is G^T row-major [ni][nk].
   split3_rows_kernel<<<div_up(size_t(ni * T->Kp), 256), 256, 0, s>>>(P->d_G.p, nk, ni, nk, T->Kp, false, T->G[0].p,
                                                                      T->G[1].p, T->G[2].p);
@@ -298,8 +309,8 @@ void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS) {
   to_f32_kernel<<<div_up(size_t(nwm), 256), 256, 0, s>>>(P->d_Fe.p, nwm, T->Ff.p + nwm);
   EPSP_LAUNCHED(ctx);
   kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), 32), unsigned(T->Kp / 64), 1), 256, 0, s>>>(
-      int(nw), nw * ni, T->Sf.p, P->d_cell_j.p, T->tf.p, T->xf.p, P->d_wnu.p, int(P->nm), T->ef.p, P->d_colc.p, nk,
-      T->Ff.p, P->w_ac, T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
+      int(nw), nw * ni, T->Sf.p, P->d_cell_j.p, T->tf.p, T->xf.p, T->skip.p, int(P->nm), T->ef.p, P->d_colc.p, int(nk),
+      T->Ff.p, T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pk);
   const long slab = nw * ni;
@@ -373,26 +384,32 @@ void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, co
       P->d_ws.p, int(nw), P->d_wnu.p, int(P->nm), d_slots, d_tp, P->w_ac, T->Ff.p);
   EPSP_LAUNCHED(ctx);
   kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), 32), unsigned(T->Kp / 64), unsigned(nA)), 256, 0, s>>>(
-      int(nw), slab, T->Sf.p, P->d_cell_j.p, T->tf.p, T->xf.p, P->d_wnu.p, int(P->nm), T->ef.p, P->d_colc.p, nk, T->Ff.p,
-      P->w_ac, T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
+      int(nw), slab, T->Sf.p, P->d_cell_j.p, T->tf.p, T->xf.p, T->skip.p, int(P->nm), T->ef.p, P->d_colc.p, int(nk),
+      T->Ff.p, T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pk);
   // ImΣ of every slot: the stacked K_t rows times G
   const long M = long(nA) * nw;
   int sp = tc_gemm_launch(ctx, T->opK, T->opG, int(M), int(ni), int(nk), T->part.p, M, M * ni, 16, T->err.p, "tc_fm",
                           kKbCap);
+  long pf = prof_begin(ctx, "finalize");
   finalize_fm_batch_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(T->part.p, int(nw), slab, nA, sp, M * ni, T->ImS_b.p);
   EPSP_LAUNCHED(ctx);
+  prof_end(ctx, pf);
   // ReΣ = KK ImΣ for every slot at once (columns: the slots' states in order)
+  pf = prof_begin(ctx, "finalize");
   split3_rows_kernel<<<div_up(size_t(nA * ni * T->Kp2), 256), 256, 0, s>>>(T->ImS_b.p, nw, nA * ni, nw, T->Kp2, false,
                                                                             T->Im[0].p, T->Im[1].p, T->Im[2].p);
   EPSP_LAUNCHED(ctx);
+  prof_end(ctx, pf);
   const long N2 = long(nA) * ni;
   int sp2 = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(N2), int(nw), T->part.p, nw, nw * N2, 16, T->err.p,
                            "tc_kk", kKbCap);
+  pf = prof_begin(ctx, "finalize");
   finalize_kk_batch_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(T->part.p, slab, sp2, nw * N2, T->ImS_b.p, d_slots,
                                                                    d_Snew_all);
   EPSP_LAUNCHED(ctx);
+  prof_end(ctx, pf);
 }
 
 }  // namespace epsp

@@ -175,11 +175,13 @@ def _options(path, gpu_tile, omega_acoustic, verbosity=0):
 class Scgd0Plan:
     """Device-resident tables of one setup (the `setup` half of _loop_scgd0)."""
 
-    def __init__(self, setup, *, path="direct_fp64", gpu_tile=None, omega_acoustic, ctx: Context | None = None):
+    def __init__(self, setup, *, path="direct_fp64", gpu_tile=None, omega_acoustic, ctx: Context | None = None,
+                 verbosity=0):
+        """verbosity >= 2 logs each iteration (err, μ, μ-solve evaluations per temperature) to stderr."""
         self.ctx = ctx or default_context()
         self.M = ModelArrays(setup)
         self.setup = setup
-        self.opts = _options(path, gpu_tile, omega_acoustic)
+        self.opts = _options(path, gpu_tile, omega_acoustic, verbosity)
         self.handle = C.c_void_p()
         self.ctx.check(lib().epsp_scgd0_setup(self.ctx.handle, C.byref(self.M.struct), C.byref(self.opts),
                                               C.byref(self.handle)))
