@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <type_traits>
 #include <complex>
 #include <limits>
 #include <memory>
@@ -89,9 +90,15 @@ struct LadderPlan {
   std::vector<double> h_tm, h_tp;
   double tab_Om = std::numeric_limits<double>::quiet_NaN();
   double cur_T = 0, cur_mu = 0, cur_Om = 0;
-  // work buffers of the solves, kept across runs
+  // GEMM_BF16: D and KY in FP32, the propagators as FP32 complex
+  DBuf<float> d_Df, d_KYf;
+  DBuf<float2> d_Gmf, d_Gpf;
+  // work buffers of the solves, kept across runs (vertex vectors: FP64 complex on the FP64 paths,
+  // FP32 complex on the tensor-core path)
   DBuf<double2> w_J0, w_J, w_LJ, w_W, w_part, w_scal, w_H, w_Y;
   std::vector<DBuf<double2>> w_V;
+  DBuf<float2> w_J0f, w_Jf, w_LJf, w_Wf;
+  std::vector<DBuf<float2>> w_Vf;
   std::shared_ptr<void> w_batch;  // the LadderBatch of the batched solves, kept across runs
 };
 
@@ -123,6 +130,24 @@ __device__ __forceinline__ Cx<R> cxadd(Cx<R> a, Cx<R> b) {
   return {a.x + b.x, a.y + b.y};
 }
 
+// Complex element types of the vertex vectors: double2 on the FP64 paths; float2 on the tensor-core
+// path, whose vertices carry ~1e-6 relative error from the BF16 split products already (FP32
+// storage halves their traffic and keeps their arithmetic off the FP64 units, 1/64 of FP32 here).
+template <class V>
+struct VecOf;
+template <>
+struct VecOf<double2> {
+  using R = double;
+  static __device__ __forceinline__ double2 make(double x, double y) { return make_double2(x, y); }
+};
+template <>
+struct VecOf<float2> {
+  using R = float;
+  static __device__ __forceinline__ float2 make(float x, float y) { return make_float2(x, y); }
+};
+template <class R>
+using Vec2 = std::conditional_t<std::is_same_v<R, float>, float2, double2>;
+
 
 // Julia's inv(::ComplexF64) (Smith's algorithm).
 __device__ __forceinline__ double2 cinv_d(double c, double d) {
@@ -140,10 +165,10 @@ __device__ __forceinline__ double2 cinv_d(double c, double d) {
 // in FP32 (FP64 division and exp would make the kernel compute-bound on the FP64 units).
 template <bool F32>
 __device__ __forceinline__ void contour_g(const double2* __restrict__ col, int j, double t, double x, double eps,
-                                          double mu, double T, double2* __restrict__ G, int w, int nw, int i) {
+                                          double mu, double T, Vec2<std::conditional_t<F32, float, double>>* __restrict__ G,
+                                          int w, int nw, int i) {
   const double2 lo = col[j], hi = col[j + 1];
   const double sr = (1 - t) * lo.x + t * hi.x, si = (1 - t) * lo.y + t * hi.y;
-  double2 g[4];
   if constexpr (F32) {
     const float c = float(x - eps - sr), d = float(-si);
     float gr, gi;  // Smith's 1/(c + i d)
@@ -162,21 +187,22 @@ __device__ __forceinline__ void contour_g(const double2* __restrict__ col, int j
     const float fac = 1.f - 2.f * f;
     // GR = (gr, gi), GA = (gr, -gi), GK = (GR - GA) fac = (0, 2 gi fac)
     const float kk = 2.f * gi * fac;
-    g[0] = make_double2(double(gr), double(0.5f * kk));                 // (GR + GA + GK) / 2
-    g[1] = make_double2(0.0, double(0.5f * (2.f * gi + kk)));           // (GR - GA + GK) / 2
-    g[2] = make_double2(0.0, double(0.5f * (-2.f * gi + kk)));          // (GA - GR + GK) / 2
-    g[3] = make_double2(double(-gr), double(0.5f * kk));                // (GK - GR - GA) / 2
+    G[w + long(nw) * (0 + 4 * i)] = make_float2(gr, 0.5f * kk);                  // (GR + GA + GK) / 2
+    G[w + long(nw) * (1 + 4 * i)] = make_float2(0.f, 0.5f * (2.f * gi + kk));    // (GR - GA + GK) / 2
+    G[w + long(nw) * (2 + 4 * i)] = make_float2(0.f, 0.5f * (-2.f * gi + kk));   // (GA - GR + GK) / 2
+    G[w + long(nw) * (3 + 4 * i)] = make_float2(-gr, 0.5f * kk);                 // (GK - GR - GA) / 2
   } else {
     double2 GR = cinv_d(x - eps - sr, -si);
     double2 GA = make_double2(GR.x, -GR.y);
     double fac = 1 - 2 * occ_fermion_d(x - mu, T);
     double2 GK = cscale(csub(GR, GA), fac);
+    double2 g[4];
     g[0] = cscale(cadd(cadd(GR, GA), GK), 0.5);
     g[1] = cscale(cadd(csub(GR, GA), GK), 0.5);
     g[2] = cscale(cadd(csub(GA, GR), GK), 0.5);
     g[3] = cscale(csub(csub(GK, GR), GA), 0.5);
+    for (int c = 0; c < 4; ++c) G[w + long(nw) * (c + 4 * i)] = g[c];
   }
-  for (int c = 0; c < 4; ++c) G[w + long(nw) * (c + 4 * i)] = g[c];
 }
 
 // contour_greens! (src/ladder_kernel.jl:27-57) of the self-energy read at ωs ∓ Ω/2 by the
@@ -186,7 +212,8 @@ __global__ void propagators_kernel(const double2* __restrict__ ST, const double*
                                    const int32_t* __restrict__ jm, const double* __restrict__ tm,
                                    const int32_t* __restrict__ jp, const double* __restrict__ tp,
                                    const double* __restrict__ eps_i, double mu, double T, double Om,
-                                   double2* __restrict__ Gm, double2* __restrict__ Gp, int ni) {
+                                   Vec2<std::conditional_t<F32, float, double>>* __restrict__ Gm,
+                                   Vec2<std::conditional_t<F32, float, double>>* __restrict__ Gp, int ni) {
   int w = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y;
   if (w >= nw) return;
@@ -195,44 +222,53 @@ __global__ void propagators_kernel(const double2* __restrict__ ST, const double*
   contour_g<F32>(col, jp[w], tp[w], ws[w] + Om / 2, eps_i[i], mu, T, Gp, w, nw, i);
 }
 
-// attach_greens_to_bare_vertex! (src/ladder_kernel.jl:70-73, 97-99): J0^{c1c2,c0} = Gm^{c1c0} v Gp^{c0c2}.
-// F32 (tensor-core path): the products in FP32.
-// Grid (nω / 256, 6 ni, 4): blockIdx.y = cart + 3 (c0 + 2 i), blockIdx.z = c12 (the column
+// attach_greens_to_bare_vertex! (src/ladder_kernel.jl:70-73, 97-99): J0^{c1c2,c0} = Gm^{c1c0} v Gp^{c0c2}
+// (float2: the tensor-core path, products in FP32).
+// Grid (nω / 256, 6 ni, 4 slots): blockIdx.y = cart + 3 (c0 + 2 i), c12 = blockIdx.z % 4 (the column
 // c12 + 4 blockIdx.y of J0).
-template <bool F32>
-__global__ void attach_bare_kernel(const double2* __restrict__ Gm, const double2* __restrict__ Gp,
-                                   const double* __restrict__ v, int nw, int ni, double2* __restrict__ J0) {
+// Batched over slots: blockIdx.z = c12 + 4 z writes J0 + z 24 nω ni from Gm, Gp + z 4 nω ni.
+template <class V>
+__global__ void attach_bare_kernel(const V* __restrict__ Gm_all, const V* __restrict__ Gp_all,
+                                   const double* __restrict__ v, int nw, int ni, V* __restrict__ J0_all) {
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= nw) return;
-  const int c12 = blockIdx.z, rest = blockIdx.y;
-  const long idx = (long(c12) + 4l * rest) * nw + w;
+  const int c12 = blockIdx.z % 4, rest = blockIdx.y;
+  const long z = blockIdx.z / 4;
+  const V* Gm = Gm_all + z * 4l * nw * ni;
+  const V* Gp = Gp_all + z * 4l * nw * ni;
+  const long idx = z * 24l * nw * ni + (long(c12) + 4l * rest) * nw + w;
   const int cart = rest % 3, c0 = (rest / 3) % 2;
   const long i = rest / 6;
   int c1 = c12 % 2, c2 = c12 / 2;
-  double2 a = Gm[w + long(nw) * (c1 + 2 * c0 + 4 * i)];
-  double2 b = Gp[w + long(nw) * (c0 + 2 * c2 + 4 * i)];
-  if constexpr (F32) {
+  const V a = Gm[w + long(nw) * (c1 + 2 * c0 + 4 * i)];
+  const V b = Gp[w + long(nw) * (c0 + 2 * c2 + 4 * i)];
+  if constexpr (std::is_same_v<V, float2>) {
     const float vv = float(v[cart + 3 * i]);
-    const Cx<float> av{float(a.x) * vv, float(a.y) * vv}, bb{float(b.x), float(b.y)};
-    const Cx<float> z = cxmul(av, bb);
-    J0[idx] = make_double2(double(z.x), double(z.y));
+    const Cx<float> av{a.x * vv, a.y * vv}, bb{b.x, b.y};
+    const Cx<float> zz = cxmul(av, bb);
+    J0_all[idx] = make_float2(zz.x, zz.y);
   } else {
-    J0[idx] = cmul(cscale(a, v[cart + 3 * i]), b);
+    J0_all[idx] = cmul(cscale(a, v[cart + 3 * i]), b);
   }
 }
 
 // Y[b, i] = Σ_ω Wω[ω] (J[ω, 22, b, c0=1, i] + J[ω, 11, b, c0=2, i]), the inner sum of
 // conductivity_from_vertex (src/ladder_kernel.jl:116-122); fixed-order block sum.
-__global__ void __launch_bounds__(256) cond_sum_kernel(const double2* __restrict__ J, const double* __restrict__ Ww, int nw,
-                                                       int ni, double2* __restrict__ Y) {
+// Batched over blockIdx.y: slot z reads J + z 24 nω ni and writes Y + z 3 ni.
+template <class V>
+__global__ void __launch_bounds__(256) cond_sum_kernel(const V* __restrict__ J_all, const double* __restrict__ Ww, int nw,
+                                                       int ni, double2* __restrict__ Y_all) {
   __shared__ double sr[256], si[256];
+  const long z = blockIdx.y;
+  const V* J = J_all + z * 24l * nw * ni;
+  double2* Y = Y_all + z * 3l * ni;
   int b = blockIdx.x % 3;
   long i = blockIdx.x / 3;
   double ar = 0, ai = 0;
   for (int w = threadIdx.x; w < nw; w += 256) {
-    double2 x = J[jidx(nw, w, 3, b, 0, i)], y = J[jidx(nw, w, 0, b, 1, i)];
-    ar += Ww[w] * (x.x + y.x);
-    ai += Ww[w] * (x.y + y.y);
+    const V x = J[jidx(nw, w, 3, b, 0, i)], y = J[jidx(nw, w, 0, b, 1, i)];
+    ar += Ww[w] * double(x.x + y.x);
+    ai += Ww[w] * double(x.y + y.y);
   }
   sr[threadIdx.x] = ar;
   si[threadIdx.x] = ai;
@@ -478,14 +514,14 @@ constexpr int kXgPreMax = 8;  // prefetch slots per thread: windows of up to 4 x
 // Batched over blockIdx.z: slot z makes the rows z 24 nwp.. of A from the vertex J + jstride r and
 // the occupations nnu + 16 r of right-hand side r = rmap[z] (r = z without rmap).
 template <int kXgPre>
-__global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restrict__ J_all, long jstride,
+__global__ void __launch_bounds__(256) xgen_bf16_kernel(const float2* __restrict__ J_all, long jstride,
                                                         const int* __restrict__ rmap, const int32_t* __restrict__ mt_k,
                                                         const float* __restrict__ mt_w, const float* __restrict__ nnu_all,
                                                         int nw, int nwp, int ns, int nmp, int ni, long Kx, long Kp,
                                                         __nv_bfloat16* __restrict__ Ah, __nv_bfloat16* __restrict__ Al) {
   extern __shared__ float xg_smem[];
   const int rhs = rmap ? rmap[blockIdx.z] : int(blockIdx.z);
-  const double2* J = J_all + jstride * rhs;
+  const float2* J = J_all + jstride * rhs;
   const float* nnu = nnu_all + 16 * rhs;
   const long row_base = long(blockIdx.z) * 24 * nwp;
   const int W = ns + 2, win = 32 + 2 * W;
@@ -530,8 +566,7 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const double2* __restric
         if (node >= 0 && node < nw && pair < 3l * ni) {
           const int b = int(pair % 3);
           const long ip = pair / 3;
-          const double2 z = J[jidx(nw, node, c12, b, c0, ip)];
-          v = make_float2(float(z.x), float(z.y));
+          v = J[jidx(nw, node, c12, b, c0, ip)];
         }
       }
       pre[q] = v;
@@ -628,7 +663,7 @@ static size_t xgen_smem_bytes(int ns) {
 // K = ω' contiguous, stride Kp2.
 // Batched over blockIdx.y: slot z reads rows z 24 nwp.. of D (column stride ldD) and writes rows
 // z 8N.. of Y.
-__global__ void y_split_kernel(const double* __restrict__ D, long ldD, int nw, int nwp, long N, long Kp2,
+__global__ void y_split_kernel(const float* __restrict__ D, long ldD, int nw, int nwp, long N, long Kp2,
                                __nv_bfloat16* __restrict__ Yh, __nv_bfloat16* __restrict__ Yl) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= 8 * N * Kp2) return;
@@ -637,7 +672,7 @@ __global__ void y_split_kernel(const double* __restrict__ D, long ldD, int nw, i
   int qq = int(r % 2), c0 = int((r / 2) % 2), ri = int((r / 4) % 2);
   long n = r / 8;
   float x = 0.f;
-  if (w < nw) x = float(D[z * 24 * nwp + w + long(nwp) * ((qq == 0 ? 0 : 2) + 6 * (c0 + 2 * ri)) + ldD * n]);
+  if (w < nw) x = D[z * 24 * nwp + w + long(nwp) * ((qq == 0 ? 0 : 2) + 6 * (c0 + 2 * ri)) + ldD * n];
   __nv_bfloat16 h = __float2bfloat16_rn(x);
   const long o = z * 8 * N * Kp2 + idx;
   Yh[o] = h;
@@ -669,12 +704,12 @@ __global__ void split_rows_t2_kernel(const double* __restrict__ S, long ldr, lon
 }
 
 // Sum of split-K partials into D (FP64).
-__global__ void sum_parts_kernel(const float* __restrict__ part, long n, int splits, long stride, double* __restrict__ D) {
+__global__ void sum_parts_kernel(const float* __restrict__ part, long n, int splits, long stride, float* __restrict__ D) {
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= n) return;
   float s = 0.f;
   for (int p = 0; p < splits; ++p) s += part[k + stride * p];
-  D[k] = double(s);
+  D[k] = s;
 }
 
 // Y of the regrouped path: the rows q = 0 (c12 = 11) and q = 2 (c12 = 22) of D, as [nω, (qq, c0, ri, n)].
@@ -694,21 +729,24 @@ __global__ void y_gemm_kernel(const double* __restrict__ D, int nw, int nwp, lon
 // z 24 nwp.. of D (column stride ldD) and KY + z nω 24ni, and writes LJ + 24 nω ni r with the
 // propagators Gm, Gp + 4 nω ni r of right-hand side r = rmap[z] (r = z without rmap).
 // With X_all, it writes X - L(X) instead of L(X) (the GMRES operator applied to X, in one pass).
+// R = float (tensor-core path): D, KY in FP32 and the propagators and vertices FP32 complex; R =
+// double: all FP64.
 template <class R>
-__global__ void finish_gemm_kernel(const double* __restrict__ D_all, long ldD, const double* __restrict__ KY_all,
-                                   const double2* __restrict__ Gm_all, const double2* __restrict__ Gp_all,
-                                   const int* __restrict__ rmap, int nw, int nwp, int ni, double2* __restrict__ LJ_all,
-                                   const double2* __restrict__ X_all = nullptr) {
+__global__ void finish_gemm_kernel(const R* __restrict__ D_all, long ldD, const R* __restrict__ KY_all,
+                                   const Vec2<R>* __restrict__ Gm_all, const Vec2<R>* __restrict__ Gp_all,
+                                   const int* __restrict__ rmap, int nw, int nwp, int ni, Vec2<R>* __restrict__ LJ_all,
+                                   const Vec2<R>* __restrict__ X_all = nullptr) {
+  using V = Vec2<R>;
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= nw) return;
   const int r = blockIdx.y;  // (a, c0, i)
   const long z = blockIdx.z;
   const long rhs = rmap ? rmap[z] : z;
-  const double* D = D_all + z * 24 * nwp;
-  const double* KY = KY_all + z * long(nw) * 24 * ni;
-  const double2* Gm = Gm_all + rhs * 4l * nw * ni;
-  const double2* Gp = Gp_all + rhs * 4l * nw * ni;
-  double2* LJ = LJ_all + rhs * 24l * nw * ni;
+  const R* D = D_all + z * 24 * nwp;
+  const R* KY = KY_all + z * long(nw) * 24 * ni;
+  const V* Gm = Gm_all + rhs * 4l * nw * ni;
+  const V* Gp = Gp_all + rhs * 4l * nw * ni;
+  V* LJ = LJ_all + rhs * 24l * nw * ni;
   const int a = r % 3, c0 = (r / 3) % 2;
   const long i = r / 6;
   const long n = a + 3 * i;
@@ -726,9 +764,9 @@ __global__ void finish_gemm_kernel(const double* __restrict__ D_all, long ldD, c
   Cx<R> gm[4], gp[4];
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
-    const double2 a = Gm[w + long(nw) * (c + 4 * i)], b = Gp[w + long(nw) * (c + 4 * i)];
-    gm[c] = {R(a.x), R(a.y)};
-    gp[c] = {R(b.x), R(b.y)};
+    const V a = Gm[w + long(nw) * (c + 4 * i)], b = Gp[w + long(nw) * (c + 4 * i)];
+    gm[c] = {a.x, a.y};
+    gp[c] = {b.x, b.y};
   }
 #pragma unroll
   for (int c1 = 0; c1 < 2; ++c1)
@@ -739,27 +777,60 @@ __global__ void finish_gemm_kernel(const double* __restrict__ D_all, long ldD, c
       z = cxadd(z, cxmul(cxmul(gm[c1], K[2]), gp[1 + 2 * c2]));
       z = cxadd(z, cxmul(cxmul(gm[c1 + 2], K[3]), gp[1 + 2 * c2]));
       const long o = jidx(nw, w, c1 + 2 * c2, a, c0, i);
-      double2 v = make_double2(-double(z.x), -double(z.y));
+      V v = VecOf<V>::make(-z.x, -z.y);
       if (X_all) {
-        const double2 x = X_all[rhs * 24l * nw * ni + o];
-        v = make_double2(x.x - v.x, x.y - v.y);
+        const V x = X_all[rhs * 24l * nw * ni + o];
+        v = VecOf<V>::make(x.x - v.x, x.y - v.y);
       }
       LJ[o] = v;
     }
 }
 
-// ---- GMRES BLAS-1 (FP64, fixed-order reductions) ----
+// ---- GMRES BLAS-1 (fixed-order reductions) ----
+// V = double2: FP64 throughout. V = float2: FP32 elements and products, each thread's sums carried
+// in FP32 over runs of 8 elements and added into FP64, the block and grid sums in FP64.
+// Batched over blockIdx.y: slot z works on the vectors of right-hand side r = rmap[z] (r = z without
+// rmap), stored n apart.
 
 constexpr int kDotBlocks = 1024;
+constexpr int kRun = 8;  // elements per FP32 run of the float2 reductions
 
-__global__ void __launch_bounds__(256) dot_partial_kernel(const double2* __restrict__ u, const double2* __restrict__ v, long n,
-                                                          double2* __restrict__ part) {
+template <class V>
+__device__ __forceinline__ long slot_rhs(const int* rmap) {
+  return rmap ? rmap[blockIdx.y] : long(blockIdx.y);
+}
+
+// part[z gridDim.x + block] = block partial of conj(u) v.
+template <class V>
+__global__ void __launch_bounds__(256) dot_partial_kernel(const V* __restrict__ U, const V* __restrict__ Vv, long n,
+                                                          const int* __restrict__ rmap, double2* __restrict__ part) {
   __shared__ double sr[256], si[256];
+  const long r = slot_rhs<V>(rmap);
+  const V* u = U + n * r;
+  const V* v = Vv + n * r;
   double ar = 0, ai = 0;
-  for (long k = long(blockIdx.x) * 256 + threadIdx.x; k < n; k += long(gridDim.x) * 256) {
-    double2 a = u[k], b = v[k];
-    ar += a.x * b.x + a.y * b.y;  // conj(a) b
-    ai += a.x * b.y - a.y * b.x;
+  if constexpr (std::is_same_v<V, double2>) {
+    for (long k = long(blockIdx.x) * 256 + threadIdx.x; k < n; k += long(gridDim.x) * 256) {
+      double2 a = u[k], b = v[k];
+      ar += a.x * b.x + a.y * b.y;  // conj(a) b
+      ai += a.x * b.y - a.y * b.x;
+    }
+  } else {
+    float fr = 0.f, fi = 0.f;
+    int run = 0;
+    for (long k = long(blockIdx.x) * 256 + threadIdx.x; k < n; k += long(gridDim.x) * 256) {
+      const float2 a = u[k], b = v[k];
+      fr += a.x * b.x + a.y * b.y;
+      fi += a.x * b.y - a.y * b.x;
+      if (++run == kRun) {
+        ar += fr;
+        ai += fi;
+        fr = fi = 0.f;
+        run = 0;
+      }
+    }
+    ar += fr;
+    ai += fi;
   }
   sr[threadIdx.x] = ar;
   si[threadIdx.x] = ai;
@@ -771,15 +842,17 @@ __global__ void __launch_bounds__(256) dot_partial_kernel(const double2* __restr
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) part[blockIdx.x] = make_double2(sr[0], si[0]);
+  if (threadIdx.x == 0) part[long(blockIdx.y) * gridDim.x + blockIdx.x] = make_double2(sr[0], si[0]);
 }
 
-__global__ void __launch_bounds__(256) dot_final_kernel(const double2* __restrict__ part, int np, double2* __restrict__ out) {
+// out[rmap[z]] (out[z] without rmap) = Σ_b part[z][b] in order; one block per slot.
+__global__ void __launch_bounds__(256) dot_final_kernel(const double2* __restrict__ part, int np, const int* __restrict__ rmap,
+                                                        double2* __restrict__ out) {
   __shared__ double sr[256], si[256];
   double ar = 0, ai = 0;
   for (int k = threadIdx.x; k < np; k += 256) {
-    ar += part[k].x;
-    ai += part[k].y;
+    ar += part[long(blockIdx.x) * np + k].x;
+    ai += part[long(blockIdx.x) * np + k].y;
   }
   sr[threadIdx.x] = ar;
   si[threadIdx.x] = ai;
@@ -791,47 +864,82 @@ __global__ void __launch_bounds__(256) dot_final_kernel(const double2* __restric
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) *out = make_double2(sr[0], si[0]);
+  if (threadIdx.x == 0) out[rmap ? rmap[blockIdx.x] : int(blockIdx.x)] = make_double2(sr[0], si[0]);
 }
 
-// q -= h v with h read from device memory.
-__global__ void axpy_dev_kernel(double2* __restrict__ q, const double2* __restrict__ v, const double2* __restrict__ h, long n) {
+// Q[r] -= h[r] V[r] with h from device memory (one coefficient per right-hand side).
+template <class V>
+__global__ void axpy_dev_kernel(V* __restrict__ Q, const V* __restrict__ X, const double2* __restrict__ h, long n,
+                                const int* __restrict__ rmap) {
+  using R = typename VecOf<V>::R;
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  double2 hh = *h, x = v[k];
-  q[k] = make_double2(q[k].x - (hh.x * x.x - hh.y * x.y), q[k].y - (hh.x * x.y + hh.y * x.x));
+  const long r = slot_rhs<V>(rmap);
+  const double2 hd = h[r];
+  const R hx = R(hd.x), hy = R(hd.y);
+  const V x = X[n * r + k], q = Q[n * r + k];
+  Q[n * r + k] = VecOf<V>::make(q.x - (hx * x.x - hy * x.y), q.y - (hx * x.y + hy * x.x));
 }
 
-// y = a x + b y (complex a, b from the host).
-__global__ void axpby_kernel(double2 a, const double2* __restrict__ x, double2 b, double2* __restrict__ y, long n) {
+// Y[r] = a X[r] + b Y[r]: complex a, b from the host (a_dev, b_dev null) or per right-hand side
+// from device memory.
+template <class V>
+__global__ void axpby_kernel(double2 a, const double2* __restrict__ a_dev, const V* __restrict__ X, double2 b,
+                             const double2* __restrict__ b_dev, V* __restrict__ Y, long n, const int* __restrict__ rmap) {
+  using R = typename VecOf<V>::R;
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  double2 xv = x[k], yv = y[k];
-  y[k] = make_double2(a.x * xv.x - a.y * xv.y + b.x * yv.x - b.y * yv.y, a.x * xv.y + a.y * xv.x + b.x * yv.y + b.y * yv.x);
+  const long r = slot_rhs<V>(rmap);
+  if (a_dev) a = a_dev[r];
+  if (b_dev) b = b_dev[r];
+  const R ax = R(a.x), ay = R(a.y), bx = R(b.x), by = R(b.y);
+  const V xv = X[n * r + k], yv = Y[n * r + k];
+  Y[n * r + k] = VecOf<V>::make(ax * xv.x - ay * xv.y + bx * yv.x - by * yv.y, ax * xv.y + ay * xv.x + bx * yv.y + by * yv.x);
 }
 
-// y = a x (y is not read).
-__global__ void scale_kernel(double2 a, const double2* __restrict__ x, double2* __restrict__ y, long n) {
+// Y[r] = a X[r] (Y is not read); a from the host or per right-hand side from device memory.
+template <class V>
+__global__ void scale_kernel(double2 a, const double2* __restrict__ a_dev, const V* __restrict__ X, V* __restrict__ Y, long n,
+                             const int* __restrict__ rmap) {
+  using R = typename VecOf<V>::R;
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  const double2 xv = x[k];
-  y[k] = make_double2(a.x * xv.x - a.y * xv.y, a.x * xv.y + a.y * xv.x);
+  const long r = slot_rhs<V>(rmap);
+  if (a_dev) a = a_dev[r];
+  const R ax = R(a.x), ay = R(a.y);
+  const V xv = X[n * r + k];
+  Y[n * r + k] = VecOf<V>::make(ax * xv.x - ay * xv.y, ax * xv.y + ay * xv.x);
 }
 
 // q -= h v (h from device memory) and the block partials of |q|^2 of the result, in the order of
-// dot_partial_kernel (the norm of what the projection leaves, in the same pass).
-__global__ void __launch_bounds__(256) axpy_norm_kernel(double2* __restrict__ q, const double2* __restrict__ v,
+// dot_partial_kernel (the norm of what the projection leaves, in the same pass). Single vectors.
+template <class V>
+__global__ void __launch_bounds__(256) axpy_norm_kernel(V* __restrict__ q, const V* __restrict__ v,
                                                         const double2* __restrict__ h, long n, double2* __restrict__ part) {
+  using R = typename VecOf<V>::R;
   __shared__ double sr[256];
-  const double2 hh = *h;
+  const double2 hd = *h;
+  const R hx = R(hd.x), hy = R(hd.y);
   double ar = 0;
+  R fr = 0;
+  int run = 0;
   for (long k = long(blockIdx.x) * 256 + threadIdx.x; k < n; k += long(gridDim.x) * 256) {
-    const double2 x = v[k];
-    double2 a = q[k];
-    a = make_double2(a.x - (hh.x * x.x - hh.y * x.y), a.y - (hh.x * x.y + hh.y * x.x));
+    const V x = v[k];
+    V a = q[k];
+    a = VecOf<V>::make(a.x - (hx * x.x - hy * x.y), a.y - (hx * x.y + hy * x.x));
     q[k] = a;
-    ar += a.x * a.x + a.y * a.y;
+    if constexpr (std::is_same_v<V, double2>) {
+      ar += a.x * a.x + a.y * a.y;
+    } else {
+      fr += a.x * a.x + a.y * a.y;
+      if (++run == kRun) {
+        ar += fr;
+        fr = 0;
+        run = 0;
+      }
+    }
   }
+  ar += double(fr);
   sr[threadIdx.x] = ar;
   __syncthreads();
   for (int st = 128; st > 0; st >>= 1) {
@@ -841,14 +949,33 @@ __global__ void __launch_bounds__(256) axpy_norm_kernel(double2* __restrict__ q,
   if (threadIdx.x == 0) part[blockIdx.x] = make_double2(sr[0], 0.0);
 }
 
-__global__ void sub_kernel(const double2* __restrict__ x, const double2* __restrict__ y, double2* __restrict__ out, long n) {
+// O[r] = X[r] - Y[r] resp. X[r] + Y[r].
+template <class V>
+__global__ void sub_kernel(const V* __restrict__ X, const V* __restrict__ Y, V* __restrict__ O, long n,
+                           const int* __restrict__ rmap) {
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k < n) out[k] = make_double2(x[k].x - y[k].x, x[k].y - y[k].y);
+  if (k >= n) return;
+  const long r = slot_rhs<V>(rmap);
+  const V x = X[n * r + k], y = Y[n * r + k];
+  O[n * r + k] = VecOf<V>::make(x.x - y.x, x.y - y.y);
 }
 
-__global__ void add_kernel(const double2* __restrict__ x, const double2* __restrict__ y, double2* __restrict__ out, long n) {
+template <class V>
+__global__ void add_kernel(const V* __restrict__ X, const V* __restrict__ Y, V* __restrict__ O, long n) {
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k < n) out[k] = make_double2(x[k].x + y[k].x, x[k].y + y[k].y);
+  if (k >= n) return;
+  const V x = X[k], y = Y[k];
+  O[k] = VecOf<V>::make(x.x + y.x, x.y + y.y);
+}
+
+// FP32 <-> FP64 complex copies at the boundary of the tensor-core path (host vertices are FP64).
+__global__ void to_f2_kernel(const double2* __restrict__ x, long n, float2* __restrict__ y) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) y[k] = make_float2(float(x[k].x), float(x[k].y));
+}
+__global__ void to_d2_kernel(const float2* __restrict__ x, long n, double2* __restrict__ y) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < n) y[k] = make_double2(double(x[k].x), double(x[k].y));
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1088,7 +1215,10 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       });
     }
     const long M = 24 * P->nwp, N = 3 * ni;
-    P->d_D.alloc(ctx, size_t(M * N));
+    if (P->path == EPSP_PATH_GEMM_BF16)
+      P->d_Df.alloc(ctx, size_t(M * N));
+    else
+      P->d_D.alloc(ctx, size_t(M * N));
     if (P->path == EPSP_PATH_GEMM_FP64) {
       P->d_Af.alloc(ctx, size_t(M * P->Kx));
     } else {
@@ -1187,10 +1317,16 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
   } else {
     fail(EPSP_EINVAL, "unknown path");
   }
-  P->d_Y.alloc(ctx, size_t(nw * 48 * ni));
-  P->d_KY.alloc(ctx, size_t(nw * 48 * ni));
-  P->d_Gm.alloc(ctx, size_t(nw * 4 * ni));
-  P->d_Gp.alloc(ctx, size_t(nw * 4 * ni));
+  if (P->path == EPSP_PATH_GEMM_BF16) {
+    P->d_KYf.alloc(ctx, size_t(nw * 24 * ni));
+    P->d_Gmf.alloc(ctx, size_t(nw * 4 * ni));
+    P->d_Gpf.alloc(ctx, size_t(nw * 4 * ni));
+  } else {
+    P->d_Y.alloc(ctx, size_t(nw * 48 * ni));
+    P->d_KY.alloc(ctx, size_t(nw * 48 * ni));
+    P->d_Gm.alloc(ctx, size_t(nw * 4 * ni));
+    P->d_Gp.alloc(ctx, size_t(nw * 4 * ni));
+  }
   P->d_ST.alloc(ctx, size_t(nw * ni));
   P->d_jm.alloc(ctx, size_t(nw));
   P->d_jp.alloc(ctx, size_t(nw));
@@ -1224,10 +1360,13 @@ static void set_propagators(LadderPlan* P, double mu, double T, double Om) {
     P->d_tp.upload(P->h_tp.data(), size_t(nw), s);
     P->tab_Om = Om;
   }
-  auto propagators = P->path == EPSP_PATH_GEMM_BF16 ? propagators_kernel<true> : propagators_kernel<false>;
-  propagators<<<dim3(div_up(size_t(nw), 128), unsigned(ni)), 128, 0, s>>>(P->d_ST.p, P->d_ws.p, int(nw), P->d_jm.p,
-                                                                                P->d_tm.p, P->d_jp.p, P->d_tp.p, P->d_eps_i.p,
-                                                                                mu, T, Om, P->d_Gm.p, P->d_Gp.p, int(ni));
+  const dim3 grid(div_up(size_t(nw), 128), unsigned(ni));
+  if (P->path == EPSP_PATH_GEMM_BF16)
+    propagators_kernel<true><<<grid, 128, 0, s>>>(P->d_ST.p, P->d_ws.p, int(nw), P->d_jm.p, P->d_tm.p, P->d_jp.p, P->d_tp.p,
+                                                   P->d_eps_i.p, mu, T, Om, P->d_Gmf.p, P->d_Gpf.p, int(ni));
+  else
+    propagators_kernel<false><<<grid, 128, 0, s>>>(P->d_ST.p, P->d_ws.p, int(nw), P->d_jm.p, P->d_tm.p, P->d_jp.p,
+                                                    P->d_tp.p, P->d_eps_i.p, mu, T, Om, P->d_Gm.p, P->d_Gp.p, int(ni));
   EPSP_LAUNCHED(ctx);
   P->cur_T = T;
   P->cur_mu = mu;
@@ -1255,12 +1394,31 @@ static void build_Bt(LadderPlan* P, double T) {
 }
 
 // LJ = L(J) with the current propagators (apply_ladder_kernel!, src/ladder.jl:245-296).
-// With X (GEMM paths only), LJ receives X - L(J) instead.
+// The Bose occupations of the modes at T, for the regrouped GEMM paths (uploaded when T changes).
+static void set_mode_occupations(LadderPlan* P, double T) {
+  if (P->Bt_T == T) return;
+  cudaStream_t s = P->ctx->stream;
+  std::vector<double> nnu(size_t(P->nm));
+  std::vector<float> nf16(16, 0.f);
+  for (long nu = 0; nu < P->nm; ++nu) {
+    double w = P->wnu[size_t(nu)];
+    nnu[size_t(nu)] = w < P->w_ac ? 0.0 : (T > 1.4901161193847656e-08 ? (w == 0 ? -0.5 : 1.0 / std::expm1(w / T)) : (w > 0 ? 0.0 : -1.0));
+    if (nu < 16) nf16[size_t(nu)] = float(nnu[size_t(nu)]);
+  }
+  P->d_nnu.upload(nnu.data(), size_t(P->nm), s);
+  P->d_nnu_f.upload(nf16.data(), 16, s);
+  EPSP_CUDA(cudaStreamSynchronize(s));
+  P->Bt_T = T;
+}
+
+// LJ = L(J) on the FP64 paths (DIRECT_FP64, GEMM_FP64). With X (GEMM_FP64 only), LJ receives
+// X - L(J) instead.
 static void apply_L(LadderPlan* P, const double2* J, double2* LJ, const double2* X = nullptr) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
   const long nw = P->nw, ni = P->ni, ns = P->nshift;
   const double T = P->cur_T;
+  if (P->path == EPSP_PATH_GEMM_BF16) fail(EPSP_EINVAL, "internal: FP64 vertices on the tensor-core path");
   if (P->path == EPSP_PATH_DIRECT_FP64) {
     build_Bt(P, T);
     const long nrow = 16 * nw, ncol = 6 * ni;
@@ -1288,62 +1446,56 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ, const double2*
     EPSP_LAUNCHED(ctx);
     return;
   }
-  // regrouped GEMM paths
-  if (P->Bt_T != T) {
-    std::vector<double> nnu(size_t(P->nm));
-    std::vector<float> nf16(16, 0.f);
-    for (long nu = 0; nu < P->nm; ++nu) {
-      double w = P->wnu[size_t(nu)];
-      nnu[size_t(nu)] = w < P->w_ac ? 0.0 : (T > 1.4901161193847656e-08 ? (w == 0 ? -0.5 : 1.0 / std::expm1(w / T)) : (w > 0 ? 0.0 : -1.0));
-      if (nu < 16) nf16[size_t(nu)] = float(nnu[size_t(nu)]);
-    }
-    P->d_nnu.upload(nnu.data(), size_t(P->nm), s);
-    P->d_nnu_f.upload(nf16.data(), 16, s);
-    EPSP_CUDA(cudaStreamSynchronize(s));
-    P->Bt_T = T;
-  }
+  // regrouped GEMM path, FP64
+  set_mode_occupations(P, T);
   const long nwp = P->nwp, M = 24 * nwp, N = 3 * ni;
-  if (P->path == EPSP_PATH_GEMM_FP64) {
-    long px = prof_begin(ctx, "xgen");
-    xgen_f64_kernel<<<div_up(size_t(M * P->Kx), 256), 256, 0, s>>>(J, P->d_klo.p, P->d_wlo.p, P->d_whi.p, P->d_mnu.p, P->d_rnu.p,
-                                                                   P->d_nnu.p, int(nw), int(nwp), int(ns), int(P->nm),
-                                                                   int(P->nmp), int(ni), P->d_Af.p);
-    EPSP_LAUNCHED(ctx);
-    prof_end(ctx, px);
-    long pg = prof_begin(ctx, "ladder_gemm");
-    gemm_f64(ctx, false, int(M), int(N), int(P->Kx), 1.0, P->d_Af.p, M, P->d_Gt.p, P->Kx, 0.0, P->d_D.p, M);
-    prof_end(ctx, pg);
-    const long ny = nw * 8 * N;
-    y_gemm_kernel<<<div_up(size_t(ny), 256), 256, 0, s>>>(P->d_D.p, int(nw), int(nwp), N, P->d_Y.p);
-    EPSP_LAUNCHED(ctx);
-    gemm_f64(ctx, false, int(nw), int(8 * N), int(nw), 1.0, P->d_KK.p, nw, P->d_Y.p, nw, 0.0, P->d_KY.p, nw);
-  } else {
-    long px = prof_begin(ctx, "xgen");
-    const unsigned ktiles = unsigned((P->Kp / 64 + kXgTiles - 1) / kXgTiles);
-    launch_xgen(ns, dim3(unsigned(nwp / 32 * 8), ktiles, 1), xgen_smem_bytes(int(ns)), s, J, long(0),
-                static_cast<const int*>(nullptr), static_cast<const int32_t*>(P->d_mt_k.p),
-                static_cast<const float*>(P->d_mt_w.p), static_cast<const float*>(P->d_nnu_f.p), int(nw), int(nwp),
-                int(ns), int(P->nmp), int(ni), P->Kx, P->Kp, P->d_Ah.p, P->d_Al.p);
-    EPSP_LAUNCHED(ctx);
-    prof_end(ctx, px);
-    int sp = tc_gemm_launch_with(ctx, P->opA, P->opG, P->bn, P->splits, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N,
-                                 P->d_err.p, "tc_ladder");
-    sum_parts_kernel<<<div_up(size_t(M * N), 256), 256, 0, s>>>(P->d_part.p, M * N, sp, M * N, P->d_D.p);
-    EPSP_LAUNCHED(ctx);
-    y_split_kernel<<<dim3(div_up(size_t(8 * N * P->Kp2), 256), 1), 256, 0, s>>>(P->d_D.p, M, int(nw), int(nwp), N, P->Kp2,
-                                                                               P->d_Yh.p, P->d_Yl.p);
-    EPSP_LAUNCHED(ctx);
-    int sp2 = tc_gemm_launch(ctx, P->opKK, P->opY, int(nw), int(8 * N), int(nw), P->d_part2.p, nw, nw * 8 * N, 16, P->d_err.p,
-                             "tc_ladder_kk");
-    sum_parts_kernel<<<div_up(size_t(nw * 8 * N), 256), 256, 0, s>>>(P->d_part2.p, nw * 8 * N, sp2, nw * 8 * N, P->d_KY.p);
-    EPSP_LAUNCHED(ctx);
-  }
-  if (P->path == EPSP_PATH_GEMM_BF16)
-    finish_gemm_kernel<float><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), 1), 256, 0, s>>>(
-        P->d_D.p, M, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
-  else
-    finish_gemm_kernel<double><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), 1), 256, 0, s>>>(
-        P->d_D.p, M, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
+  long px = prof_begin(ctx, "xgen");
+  xgen_f64_kernel<<<div_up(size_t(M * P->Kx), 256), 256, 0, s>>>(J, P->d_klo.p, P->d_wlo.p, P->d_whi.p, P->d_mnu.p, P->d_rnu.p,
+                                                                 P->d_nnu.p, int(nw), int(nwp), int(ns), int(P->nm),
+                                                                 int(P->nmp), int(ni), P->d_Af.p);
+  EPSP_LAUNCHED(ctx);
+  prof_end(ctx, px);
+  long pg = prof_begin(ctx, "ladder_gemm");
+  gemm_f64(ctx, false, int(M), int(N), int(P->Kx), 1.0, P->d_Af.p, M, P->d_Gt.p, P->Kx, 0.0, P->d_D.p, M);
+  prof_end(ctx, pg);
+  const long ny = nw * 8 * N;
+  y_gemm_kernel<<<div_up(size_t(ny), 256), 256, 0, s>>>(P->d_D.p, int(nw), int(nwp), N, P->d_Y.p);
+  EPSP_LAUNCHED(ctx);
+  gemm_f64(ctx, false, int(nw), int(8 * N), int(nw), 1.0, P->d_KK.p, nw, P->d_Y.p, nw, 0.0, P->d_KY.p, nw);
+  finish_gemm_kernel<double><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), 1), 256, 0, s>>>(
+      P->d_D.p, M, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
+  EPSP_LAUNCHED(ctx);
+}
+
+// The tensor-core path (GEMM_BF16), FP32 vertices: LJ = L(J), or X - L(J) with X.
+static void apply_L(LadderPlan* P, const float2* J, float2* LJ, const float2* X = nullptr) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  const long nw = P->nw, ni = P->ni, ns = P->nshift;
+  if (P->path != EPSP_PATH_GEMM_BF16) fail(EPSP_EINVAL, "internal: FP32 vertices on an FP64 path");
+  set_mode_occupations(P, P->cur_T);
+  const long nwp = P->nwp, M = 24 * nwp, N = 3 * ni;
+  long px = prof_begin(ctx, "xgen");
+  const unsigned ktiles = unsigned((P->Kp / 64 + kXgTiles - 1) / kXgTiles);
+  launch_xgen(ns, dim3(unsigned(nwp / 32 * 8), ktiles, 1), xgen_smem_bytes(int(ns)), s, J, long(0),
+              static_cast<const int*>(nullptr), static_cast<const int32_t*>(P->d_mt_k.p),
+              static_cast<const float*>(P->d_mt_w.p), static_cast<const float*>(P->d_nnu_f.p), int(nw), int(nwp),
+              int(ns), int(P->nmp), int(ni), P->Kx, P->Kp, P->d_Ah.p, P->d_Al.p);
+  EPSP_LAUNCHED(ctx);
+  prof_end(ctx, px);
+  int sp = tc_gemm_launch_with(ctx, P->opA, P->opG, P->bn, P->splits, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N,
+                               P->d_err.p, "tc_ladder");
+  sum_parts_kernel<<<div_up(size_t(M * N), 256), 256, 0, s>>>(P->d_part.p, M * N, sp, M * N, P->d_Df.p);
+  EPSP_LAUNCHED(ctx);
+  y_split_kernel<<<dim3(div_up(size_t(8 * N * P->Kp2), 256), 1), 256, 0, s>>>(P->d_Df.p, M, int(nw), int(nwp), N, P->Kp2,
+                                                                             P->d_Yh.p, P->d_Yl.p);
+  EPSP_LAUNCHED(ctx);
+  int sp2 = tc_gemm_launch(ctx, P->opKK, P->opY, int(nw), int(8 * N), int(nw), P->d_part2.p, nw, nw * 8 * N, 16, P->d_err.p,
+                           "tc_ladder_kk");
+  sum_parts_kernel<<<div_up(size_t(nw * 8 * N), 256), 256, 0, s>>>(P->d_part2.p, nw * 8 * N, sp2, nw * 8 * N, P->d_KYf.p);
+  EPSP_LAUNCHED(ctx);
+  finish_gemm_kernel<float><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), 1), 256, 0, s>>>(
+      P->d_Df.p, M, P->d_KYf.p, P->d_Gmf.p, P->d_Gpf.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
   EPSP_LAUNCHED(ctx);
 }
 
@@ -1359,17 +1511,18 @@ static void check_tc_err(LadderPlan* P) {
 // solves (src/ladder.jl:327-375)
 // ---------------------------------------------------------------------------------------------
 
-static cplx dot_dev(LadderPlan* P, const double2* u, const double2* v, long n, DBuf<double2>& part, double2* out_dev) {
+template <class V>
+static void dot_dev(LadderPlan* P, const V* u, const V* v, long n, DBuf<double2>& part, double2* out_dev) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
-  dot_partial_kernel<<<kDotBlocks, 256, 0, s>>>(u, v, n, part.p);
+  dot_partial_kernel<V><<<dim3(kDotBlocks, 1), 256, 0, s>>>(u, v, n, nullptr, part.p);
   EPSP_LAUNCHED(ctx);
-  dot_final_kernel<<<1, 256, 0, s>>>(part.p, kDotBlocks, out_dev);
+  dot_final_kernel<<<1, 256, 0, s>>>(part.p, kDotBlocks, nullptr, out_dev);
   EPSP_LAUNCHED(ctx);
-  return cplx();
 }
 
-static double nrm_host(LadderPlan* P, const double2* u, long n, DBuf<double2>& part, DBuf<double2>& scal) {
+template <class V>
+static double nrm_host(LadderPlan* P, const V* u, long n, DBuf<double2>& part, DBuf<double2>& scal) {
   dot_dev(P, u, u, n, part, scal.p);
   double2 r;
   scal.download(&r, 1, P->ctx->stream);
@@ -1378,11 +1531,12 @@ static double nrm_host(LadderPlan* P, const double2* u, long n, DBuf<double2>& p
 }
 
 // conductivity_from_vertex (src/ladder_kernel.jl:116-122) of the device vertex J.
-static void conductivity_dev(LadderPlan* P, const double2* J, double Om, double T, DBuf<double2>& Ybuf, double* sigma) {
+template <class V>
+static void conductivity_dev(LadderPlan* P, const V* J, double Om, double T, DBuf<double2>& Ybuf, double* sigma) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
   const long nw = P->nw, ni = P->ni;
-  cond_sum_kernel<<<unsigned(3 * ni), 256, 0, s>>>(J, P->d_Ww.p, int(nw), int(ni), Ybuf.p);
+  cond_sum_kernel<V><<<dim3(unsigned(3 * ni), 1), 256, 0, s>>>(J, P->d_Ww.p, int(nw), int(ni), Ybuf.p);
   EPSP_LAUNCHED(ctx);
   std::vector<double2> Y(size_t(3 * ni));
   Ybuf.download(Y.data(), size_t(3 * ni), s);
@@ -1397,15 +1551,34 @@ static void conductivity_dev(LadderPlan* P, const double2* J, double Om, double 
     }
 }
 
+// A device vertex copied into host FP64 memory (FP32 vertices widened on the way).
+static void vertex_to_host(LadderPlan* P, const double2* J, long n, double* out) {
+  EPSP_CUDA(cudaMemcpyAsync(out, J, size_t(n) * sizeof(double2), cudaMemcpyDeviceToHost, P->ctx->stream));
+  EPSP_CUDA(cudaStreamSynchronize(P->ctx->stream));
+}
+static void vertex_to_host(LadderPlan* P, const float2* J, long n, double* out) {
+  std::vector<float2> h(static_cast<size_t>(n));
+  EPSP_CUDA(cudaMemcpyAsync(h.data(), J, size_t(n) * sizeof(float2), cudaMemcpyDeviceToHost, P->ctx->stream));
+  EPSP_CUDA(cudaStreamSynchronize(P->ctx->stream));
+  for (long k = 0; k < n; ++k) {
+    out[2 * k] = double(h[size_t(k)].x);
+    out[2 * k + 1] = double(h[size_t(k)].y);
+  }
+}
+
 static double mat3_norm(const double* a) {
   double s = 0;
   for (int k = 0; k < 9; ++k) s += a[k] * a[k];
   return std::sqrt(s);
 }
 
-void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const double* Tlist, int64_t nT, const double* Omegas,
-                int64_t nO, int32_t solver, double rtol, int32_t maxiter, double* sb, double* sl, uint8_t* conv, int32_t* niter,
-                epsp_ladder_history* hist, double* J_out) {
+// The solves of ladder_run with vertex vectors of element type V (double2 on the FP64 paths, float2
+// on the tensor-core path).
+template <class V>
+static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, const double* Tlist, int64_t nT,
+                         const double* Omegas, int64_t nO, int32_t solver, double rtol, int32_t maxiter, double* sb,
+                         double* sl, uint8_t* conv, int32_t* niter, epsp_ladder_history* hist, double* J_out,
+                         DBuf<V>& J0, DBuf<V>& J, DBuf<V>& LJ, DBuf<V>& W, std::vector<DBuf<V>>& Vb) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
   if (solver != EPSP_SOLVER_GMRES && solver != EPSP_SOLVER_FIXED_POINT) fail(EPSP_EINVAL, "solver must be :gmres or :fixed_point");
@@ -1417,10 +1590,6 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
   const long nw = P->nw, ni = P->ni;
   const long n = nw * 24 * ni;
   const unsigned eb = div_up(size_t(n), 256);
-  DBuf<double2>& J0 = P->w_J0;
-  DBuf<double2>& J = P->w_J;
-  DBuf<double2>& LJ = P->w_LJ;
-  DBuf<double2>& W = P->w_W;
   DBuf<double2>& part = P->w_part;
   DBuf<double2>& scal = P->w_scal;
   DBuf<double2>& Hdev = P->w_H;
@@ -1430,7 +1599,7 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
   ensure(scal, ctx, 1);
   ensure(Hdev, ctx, size_t(maxiter + 2));
   ensure(Ybuf, ctx, size_t(3 * ni));
-  std::vector<DBuf<double2>>& V = P->w_V;
+  std::vector<DBuf<V>>& Vk = Vb;
   const double btol = std::pow(std::numeric_limits<double>::epsilon(), 0.75);
   for (int64_t iT = 0; iT < nT; ++iT) {
     const double T = Tlist[iT];
@@ -1440,16 +1609,16 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
       const int64_t idx = iO + nO * iT;
       set_propagators(P, mu[iT], T, Om);
       const dim3 ab(div_up(size_t(nw), 256), unsigned(6 * ni), 4);
-      if (P->path == EPSP_PATH_GEMM_BF16)
-        attach_bare_kernel<true><<<ab, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
+      if constexpr (std::is_same_v<V, float2>)
+        attach_bare_kernel<float2><<<ab, 256, 0, s>>>(P->d_Gmf.p, P->d_Gpf.p, P->d_v.p, int(nw), int(ni), J0.p);
       else
-        attach_bare_kernel<false><<<ab, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
+        attach_bare_kernel<double2><<<ab, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
       EPSP_LAUNCHED(ctx);
       conductivity_dev(P, J0.p, Om, T, Ybuf, sb + 9 * idx);
-      auto op = [&](const double2* x, double2* y) {  // y = x - L(x)
+      auto op = [&](const V* x, V* y) {  // y = x - L(x)
         if (P->path == EPSP_PATH_DIRECT_FP64) {
           apply_L(P, x, LJ.p);
-          sub_kernel<<<eb, 256, 0, s>>>(x, LJ.p, y, n);
+          sub_kernel<V><<<eb, 256, 0, s>>>(x, LJ.p, y, n, nullptr);
           EPSP_LAUNCHED(ctx);
         } else {
           apply_L(P, x, y, x);  // the last pass of the operator forms x - L(x)
@@ -1465,10 +1634,10 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
         // r0 = b - A x0 (warm) or b
         if (warm) {
           op(J.p, W.p);
-          axpby_kernel<<<eb, 256, 0, s>>>(make_double2(1, 0), J0.p, make_double2(-1, 0), W.p, n);
+          axpby_kernel<V><<<eb, 256, 0, s>>>(make_double2(1, 0), nullptr, J0.p, make_double2(-1, 0), nullptr, W.p, n, nullptr);
           EPSP_LAUNCHED(ctx);
         }
-        const double2* r0 = warm ? W.p : J0.p;  // a cold start's r0 is J0 itself
+        const V* r0 = warm ? W.p : J0.p;  // a cold start's r0 is J0 itself
         const double beta = warm ? nrm_host(P, W.p, n, part, scal) : nJ0;
         double rNorm = beta;
         res.push_back(beta);
@@ -1478,25 +1647,25 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
         std::vector<double> cv;
         if (beta == 0) solved = true;
         if (!solved) {
-          if (V.empty()) V.emplace_back();
-          if (V[0].n != size_t(n)) V[0].alloc(ctx, size_t(n));
-          scale_kernel<<<eb, 256, 0, s>>>(make_double2(1.0 / rNorm, 0), r0, V[0].p, n);
+          if (Vk.empty()) Vk.emplace_back();
+          if (Vk[0].n != size_t(n)) Vk[0].alloc(ctx, size_t(n));
+          scale_kernel<V><<<eb, 256, 0, s>>>(make_double2(1.0 / rNorm, 0), nullptr, r0, Vk[0].p, n, nullptr);
           EPSP_LAUNCHED(ctx);
           z.push_back(beta);
           int nr = 0;
           bool tired = false;
           while (!(solved || tired || breakdown)) {
             ++inner;
-            op(V[size_t(inner - 1)].p, W.p);  // q = A v_k
+            op(Vk[size_t(inner - 1)].p, W.p);  // q = A v_k
             for (int i = 0; i < inner; ++i) {
-              dot_dev(P, V[size_t(i)].p, W.p, n, part, Hdev.p + i);
+              dot_dev(P, Vk[size_t(i)].p, W.p, n, part, Hdev.p + i);
               if (i + 1 < inner) {
-                axpy_dev_kernel<<<eb, 256, 0, s>>>(W.p, V[size_t(i)].p, Hdev.p + i, n);
+                axpy_dev_kernel<V><<<eb, 256, 0, s>>>(W.p, Vk[size_t(i)].p, Hdev.p + i, n, nullptr);
                 EPSP_LAUNCHED(ctx);
               } else {  // the last projection and the norm of what remains, in one pass
-                axpy_norm_kernel<<<kDotBlocks, 256, 0, s>>>(W.p, V[size_t(i)].p, Hdev.p + i, n, part.p);
+                axpy_norm_kernel<V><<<kDotBlocks, 256, 0, s>>>(W.p, Vk[size_t(i)].p, Hdev.p + i, n, part.p);
                 EPSP_LAUNCHED(ctx);
-                dot_final_kernel<<<1, 256, 0, s>>>(part.p, kDotBlocks, Hdev.p + inner);
+                dot_final_kernel<<<1, 256, 0, s>>>(part.p, kDotBlocks, nullptr, Hdev.p + inner);
                 EPSP_LAUNCHED(ctx);
               }
             }
@@ -1548,9 +1717,9 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
             breakdown = Hbis <= btol;
             tired = inner >= maxiter;
             if (!(solved || tired || breakdown)) {
-              if (V.size() < size_t(inner + 1)) V.emplace_back();
-              if (V[size_t(inner)].n != size_t(n)) V[size_t(inner)].alloc(ctx, size_t(n));
-              scale_kernel<<<eb, 256, 0, s>>>(make_double2(1.0 / Hbis, 0), W.p, V[size_t(inner)].p, n);
+              if (Vk.size() < size_t(inner + 1)) Vk.emplace_back();
+              if (Vk[size_t(inner)].n != size_t(n)) Vk[size_t(inner)].alloc(ctx, size_t(n));
+              scale_kernel<V><<<eb, 256, 0, s>>>(make_double2(1.0 / Hbis, 0), nullptr, W.p, Vk[size_t(inner)].p, n, nullptr);
               EPSP_LAUNCHED(ctx);
               z.push_back(zeta);
             }
@@ -1571,9 +1740,9 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
           for (int i = 0; i < inner; ++i) {
             const double2 yi = make_double2(y[size_t(i)].real(), y[size_t(i)].imag());
             if (i == 0 && !warm)
-              scale_kernel<<<eb, 256, 0, s>>>(yi, V[0].p, J.p, n);
+              scale_kernel<V><<<eb, 256, 0, s>>>(yi, nullptr, Vk[0].p, J.p, n, nullptr);
             else
-              axpby_kernel<<<eb, 256, 0, s>>>(yi, V[size_t(i)].p, make_double2(1, 0), J.p, n);
+              axpby_kernel<V><<<eb, 256, 0, s>>>(yi, nullptr, Vk[size_t(i)].p, make_double2(1, 0), nullptr, J.p, n, nullptr);
             EPSP_LAUNCHED(ctx);
           }
         } else if (!warm) {
@@ -1589,13 +1758,13 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
         if (hist && hist->nsigma) hist->nsigma[idx] = 0;
       } else {
         // J ← J0 + L(J) from J0 until the relative change of σ is below rtol (src/ladder.jl:354-369)
-        EPSP_CUDA(cudaMemcpyAsync(J.p, J0.p, size_t(n) * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        EPSP_CUDA(cudaMemcpyAsync(J.p, J0.p, size_t(n) * sizeof(V), cudaMemcpyDeviceToDevice, s));
         double sprev[9] = {}, scur[9];
         conv[idx] = 0;
         int32_t ns_ = 0;
         for (int32_t it = 1; it <= maxiter; ++it) {
           apply_L(P, J.p, LJ.p);
-          add_kernel<<<eb, 256, 0, s>>>(J0.p, LJ.p, J.p, n);
+          add_kernel<V><<<eb, 256, 0, s>>>(J0.p, LJ.p, J.p, n);
           EPSP_LAUNCHED(ctx);
           check_tc_err(P);
           conductivity_dev(P, J.p, Om, T, Ybuf, scur);
@@ -1617,12 +1786,20 @@ void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const doub
         if (hist && hist->nnorms) hist->nnorms[idx] = 0;
       }
       conductivity_dev(P, J.p, Om, T, Ybuf, sl + 9 * idx);
-      if (J_out) {
-        J.download(reinterpret_cast<double2*>(J_out) + size_t(n) * size_t(idx), size_t(n), s);
-        EPSP_CUDA(cudaStreamSynchronize(s));
-      }
+      if (J_out) vertex_to_host(P, J.p, n, J_out + 2 * size_t(n) * size_t(idx));
     }
   }
+}
+
+void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const double* Tlist, int64_t nT, const double* Omegas,
+                int64_t nO, int32_t solver, double rtol, int32_t maxiter, double* sb, double* sl, uint8_t* conv, int32_t* niter,
+                epsp_ladder_history* hist, double* J_out) {
+  if (P->path == EPSP_PATH_GEMM_BF16)
+    ladder_run_t<float2>(P, sigma, mu, Tlist, nT, Omegas, nO, solver, rtol, maxiter, sb, sl, conv, niter, hist, J_out,
+                         P->w_J0f, P->w_Jf, P->w_LJf, P->w_Wf, P->w_Vf);
+  else
+    ladder_run_t<double2>(P, sigma, mu, Tlist, nT, Omegas, nO, solver, rtol, maxiter, sb, sl, conv, niter, hist, J_out,
+                          P->w_J0, P->w_J, P->w_LJ, P->w_W, P->w_V);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1640,7 +1817,7 @@ __global__ void propagators_batch_kernel(const double2* __restrict__ S_all, cons
                                          const int32_t* __restrict__ jm_all, const double* __restrict__ tm_all,
                                          const int32_t* __restrict__ jp_all, const double* __restrict__ tp_all,
                                          const double* __restrict__ eps_i, const PairParams* __restrict__ pp,
-                                         double2* __restrict__ Gm_all, double2* __restrict__ Gp_all, int ni) {
+                                         float2* __restrict__ Gm_all, float2* __restrict__ Gp_all, int ni) {
   int w = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y;
   const long z = blockIdx.z;
@@ -1653,144 +1830,8 @@ __global__ void propagators_batch_kernel(const double2* __restrict__ S_all, cons
                   Gp_all + z * 4l * nw * ni, w, nw, i);
 }
 
-__global__ void attach_bare_batch_kernel(const double2* __restrict__ Gm_all, const double2* __restrict__ Gp_all,
-                                         const double* __restrict__ v, int nw, int ni, double2* __restrict__ J0_all) {
-  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  const long n = long(nw) * 24 * ni;
-  if (idx >= n) return;
-  const long z = blockIdx.y;
-  const double2* Gm = Gm_all + z * 4l * nw * ni;
-  const double2* Gp = Gp_all + z * 4l * nw * ni;
-  long w = idx % nw;
-  long r = idx / nw;
-  int c12 = int(r % 4), cart = int((r / 4) % 3), c0 = int((r / 12) % 2);
-  long i = r / 24;
-  int c1 = c12 % 2, c2 = c12 / 2;
-  double2 a = Gm[w + long(nw) * (c1 + 2 * c0 + 4 * i)];
-  double2 b = Gp[w + long(nw) * (c0 + 2 * c2 + 4 * i)];
-  const float vv = float(v[cart + 3 * i]);
-  const Cx<float> av{float(a.x) * vv, float(a.y) * vv}, bb{float(b.x), float(b.y)};
-  const Cx<float> zz = cxmul(av, bb);
-  J0_all[z * n + idx] = make_double2(double(zz.x), double(zz.y));
-}
-
-__global__ void __launch_bounds__(256) cond_sum_batch_kernel(const double2* __restrict__ J_all, const double* __restrict__ Ww,
-                                                             int nw, int ni, double2* __restrict__ Y_all) {
-  __shared__ double sr[256], si[256];
-  const long z = blockIdx.y;
-  const double2* J = J_all + z * 24l * nw * ni;
-  int b = blockIdx.x % 3;
-  long i = blockIdx.x / 3;
-  double ar = 0, ai = 0;
-  for (int w = threadIdx.x; w < nw; w += 256) {
-    double2 x = J[jidx(nw, w, 3, b, 0, i)], y = J[jidx(nw, w, 0, b, 1, i)];
-    ar += Ww[w] * (x.x + y.x);
-    ai += Ww[w] * (x.y + y.y);
-  }
-  sr[threadIdx.x] = ar;
-  si[threadIdx.x] = ai;
-  __syncthreads();
-  for (int st = 128; st > 0; st >>= 1) {
-    if (threadIdx.x < st) {
-      sr[threadIdx.x] += sr[threadIdx.x + st];
-      si[threadIdx.x] += si[threadIdx.x + st];
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) Y_all[z * 3 * ni + b + 3 * i] = make_double2(sr[0], si[0]);
-}
-
-// Batched BLAS-1 over the right-hand sides r = rmap[z] of vectors stored [r][n].
+// The batched BLAS-1 are the kernels above with blockIdx.y over the slots and rmap.
 constexpr int kDotBlocksB = 256;
-
-__global__ void __launch_bounds__(256) dot_partial_batch_kernel(const double2* __restrict__ U, const double2* __restrict__ V,
-                                                                long n, const int* __restrict__ rmap,
-                                                                double2* __restrict__ part) {
-  __shared__ double sr[256], si[256];
-  const long r = rmap[blockIdx.y];
-  const double2* u = U + n * r;
-  const double2* v = V + n * r;
-  double ar = 0, ai = 0;
-  for (long k = long(blockIdx.x) * 256 + threadIdx.x; k < n; k += long(gridDim.x) * 256) {
-    double2 a = u[k], b = v[k];
-    ar += a.x * b.x + a.y * b.y;  // conj(a) b
-    ai += a.x * b.y - a.y * b.x;
-  }
-  sr[threadIdx.x] = ar;
-  si[threadIdx.x] = ai;
-  __syncthreads();
-  for (int st = 128; st > 0; st >>= 1) {
-    if (threadIdx.x < st) {
-      sr[threadIdx.x] += sr[threadIdx.x + st];
-      si[threadIdx.x] += si[threadIdx.x + st];
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) part[long(blockIdx.y) * gridDim.x + blockIdx.x] = make_double2(sr[0], si[0]);
-}
-
-// out[rmap[z]] = Σ_b part[z][b] in order.
-__global__ void __launch_bounds__(256) dot_final_batch_kernel(const double2* __restrict__ part, int np,
-                                                              const int* __restrict__ rmap, double2* __restrict__ out) {
-  __shared__ double sr[256], si[256];
-  double ar = 0, ai = 0;
-  for (int k = threadIdx.x; k < np; k += 256) {
-    ar += part[long(blockIdx.x) * np + k].x;
-    ai += part[long(blockIdx.x) * np + k].y;
-  }
-  sr[threadIdx.x] = ar;
-  si[threadIdx.x] = ai;
-  __syncthreads();
-  for (int st = 128; st > 0; st >>= 1) {
-    if (threadIdx.x < st) {
-      sr[threadIdx.x] += sr[threadIdx.x + st];
-      si[threadIdx.x] += si[threadIdx.x + st];
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) out[rmap[blockIdx.x]] = make_double2(sr[0], si[0]);
-}
-
-// Q[r] -= h[r] V[r].
-__global__ void axpy_batch_kernel(double2* __restrict__ Q, const double2* __restrict__ V, const double2* __restrict__ h,
-                                  long n, const int* __restrict__ rmap) {
-  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const long r = rmap[blockIdx.y];
-  const double2 hh = h[r], x = V[n * r + k];
-  double2 q = Q[n * r + k];
-  Q[n * r + k] = make_double2(q.x - (hh.x * x.x - hh.y * x.y), q.y - (hh.x * x.y + hh.y * x.x));
-}
-
-// Y[r] = a[r] X[r] + b[r] Y[r] (complex a, b per right-hand side).
-__global__ void axpby_batch_kernel(const double2* __restrict__ a, const double2* __restrict__ X, const double2* __restrict__ b,
-                                   double2* __restrict__ Y, long n, const int* __restrict__ rmap) {
-  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const long r = rmap[blockIdx.y];
-  const double2 aa = a[r], bb = b[r], xv = X[n * r + k], yv = Y[n * r + k];
-  Y[n * r + k] = make_double2(aa.x * xv.x - aa.y * xv.y + bb.x * yv.x - bb.y * yv.y,
-                              aa.x * xv.y + aa.y * xv.x + bb.x * yv.y + bb.y * yv.x);
-}
-
-// Y[r] = a[r] X[r] (Y is not read).
-__global__ void scale_batch_kernel(const double2* __restrict__ a, const double2* __restrict__ X, double2* __restrict__ Y,
-                                   long n, const int* __restrict__ rmap) {
-  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const long r = rmap[blockIdx.y];
-  const double2 aa = a[r], xv = X[n * r + k];
-  Y[n * r + k] = make_double2(aa.x * xv.x - aa.y * xv.y, aa.x * xv.y + aa.y * xv.x);
-}
-
-__global__ void sub_batch_kernel(const double2* __restrict__ X, const double2* __restrict__ Y, double2* __restrict__ O, long n,
-                                 const int* __restrict__ rmap) {
-  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const long r = rmap[blockIdx.y];
-  const double2 x = X[n * r + k], y = Y[n * r + k];
-  O[n * r + k] = make_double2(x.x - y.x, x.y - y.y);
-}
 
 // Buffers of a batch of right-hand sides (capacity cap), tensor maps over them.
 struct LadderBatch {
@@ -1798,9 +1839,10 @@ struct LadderBatch {
   int bk = 0;  // K block of the A maps
   DBuf<__nv_bfloat16> Ah, Al, Yh, Yl;
   DBuf<float> part, part2, nnu;
-  DBuf<double> D, KY;
-  DBuf<double2> Gm, Gp, J0, J, LJ, W, dpart, H, coef_a, coef_b;
-  std::vector<DBuf<double2>> V;
+  DBuf<float> D, KY;
+  DBuf<float2> Gm, Gp, J0, J, LJ, W;
+  DBuf<double2> dpart, H, coef_a, coef_b;
+  std::vector<DBuf<float2>> V;
   DBuf<int32_t> jm, jp;
   DBuf<double> tm, tp;
   DBuf<PairParams> pp;
@@ -1850,7 +1892,7 @@ static void batch_reserve(LadderPlan* P, LadderBatch& B, long R, int maxiter) {
 }
 
 // LJ[r] = L(X[r]) for the nA right-hand sides listed in the device array rmap (host copy rmap_h).
-static void apply_L_batch(LadderPlan* P, LadderBatch& B, const double2* X, int nA, double2* LJ) {
+static void apply_L_batch(LadderPlan* P, LadderBatch& B, const float2* X, int nA, float2* LJ) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
   const long nw = P->nw, ni = P->ni, ns = P->nshift, nwp = P->nwp, M = 24 * nwp, N = 3 * ni, n = nw * 24 * ni;
@@ -1881,12 +1923,12 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const double2* X, int n
 }
 
 // σ of every pair of the batch from the vertices J[z] (conductivity_from_vertex).
-static void conductivity_batch(LadderPlan* P, LadderBatch& B, const double2* J, int nP, const std::vector<PairParams>& pp,
+static void conductivity_batch(LadderPlan* P, LadderBatch& B, const float2* J, int nP, const std::vector<PairParams>& pp,
                                double* sigma_base, const std::vector<long>& idx) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
   const long nw = P->nw, ni = P->ni;
-  cond_sum_batch_kernel<<<dim3(unsigned(3 * ni), unsigned(nP)), 256, 0, s>>>(J, P->d_Ww.p, int(nw), int(ni), B.Y.p);
+  cond_sum_kernel<float2><<<dim3(unsigned(3 * ni), unsigned(nP)), 256, 0, s>>>(J, P->d_Ww.p, int(nw), int(ni), B.Y.p);
   EPSP_LAUNCHED(ctx);
   std::vector<double2> Y(static_cast<size_t>(3 * ni * nP));
   B.Y.download(Y.data(), Y.size(), s);
@@ -1947,10 +1989,10 @@ void ladder_run_batched(LadderPlan* P, const double* sigma, const double* mu, co
   S_all.upload(reinterpret_cast<const double2*>(sigma), size_t(slab * nT), s);
   const double btol = std::pow(std::numeric_limits<double>::epsilon(), 0.75);
   const unsigned eb = div_up(size_t(n), 256);
-  auto dot_batch = [&](const double2* U, const double2* V, int nA, double2* out) {
-    dot_partial_batch_kernel<<<dim3(kDotBlocksB, unsigned(nA)), 256, 0, s>>>(U, V, n, B.rmap.p, B.dpart.p);
+  auto dot_batch = [&](const float2* U, const float2* V, int nA, double2* out) {
+    dot_partial_kernel<float2><<<dim3(kDotBlocksB, unsigned(nA)), 256, 0, s>>>(U, V, n, B.rmap.p, B.dpart.p);
     EPSP_LAUNCHED(ctx);
-    dot_final_batch_kernel<<<unsigned(nA), 256, 0, s>>>(B.dpart.p, kDotBlocksB, B.rmap.p, out);
+    dot_final_kernel<<<unsigned(nA), 256, 0, s>>>(B.dpart.p, kDotBlocksB, B.rmap.p, out);
     EPSP_LAUNCHED(ctx);
   };
   auto set_rmap = [&](const std::vector<int>& rm) { B.rmap.upload(rm.data(), rm.size(), s); };
@@ -1995,7 +2037,8 @@ void ladder_run_batched(LadderPlan* P, const double* sigma, const double* mu, co
     propagators_batch_kernel<<<dim3(div_up(size_t(nw), 128), unsigned(ni), unsigned(nP)), 128, 0, s>>>(
         S_all.p, P->d_ws.p, int(nw), B.jm.p, B.tm.p, B.jp.p, B.tp.p, P->d_eps_i.p, B.pp.p, B.Gm.p, B.Gp.p, int(ni));
     EPSP_LAUNCHED(ctx);
-    attach_bare_batch_kernel<<<dim3(eb, unsigned(nP)), 256, 0, s>>>(B.Gm.p, B.Gp.p, P->d_v.p, int(nw), int(ni), B.J0.p);
+    attach_bare_kernel<float2><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), unsigned(4 * nP)), 256, 0, s>>>(
+        B.Gm.p, B.Gp.p, P->d_v.p, int(nw), int(ni), B.J0.p);
     EPSP_LAUNCHED(ctx);
     conductivity_batch(P, B, B.J0.p, nP, pp, sb, idx);
     // GMRES per right-hand side from x0 = 0: r0 = J0, ‖J0‖ gives atol and β
@@ -2030,7 +2073,7 @@ void ladder_run_batched(LadderPlan* P, const double* sigma, const double* mu, co
     if (B.V[0].n != size_t(R * n)) B.V[0].alloc(ctx, size_t(R * n));
     // V0 = J0 / β (every slot; solved ones get 0)
     B.coef_a.upload(ca.data(), ca.size(), s);
-    scale_batch_kernel<<<dim3(eb, unsigned(nP)), 256, 0, s>>>(B.coef_a.p, B.J0.p, B.V[0].p, n, B.rmap.p);
+    scale_kernel<float2><<<dim3(eb, unsigned(nP)), 256, 0, s>>>(make_double2(0, 0), B.coef_a.p, B.J0.p, B.V[0].p, n, B.rmap.p);
     EPSP_LAUNCHED(ctx);
     int k = 0;
     while (!act.empty()) {
@@ -2038,11 +2081,12 @@ void ladder_run_batched(LadderPlan* P, const double* sigma, const double* mu, co
       const int nA = int(act.size());
       set_rmap(act);
       apply_L_batch(P, B, B.V[size_t(k - 1)].p, nA, B.LJ.p);  // LJ[r] = L(v_k)
-      sub_batch_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(B.V[size_t(k - 1)].p, B.LJ.p, B.W.p, n, B.rmap.p);
+      sub_kernel<float2><<<dim3(eb, unsigned(nA)), 256, 0, s>>>(B.V[size_t(k - 1)].p, B.LJ.p, B.W.p, n, B.rmap.p);
       EPSP_LAUNCHED(ctx);
       for (int i = 0; i < k; ++i) {
         dot_batch(B.V[size_t(i)].p, B.W.p, nA, B.H.p + long(i) * R);
-        axpy_batch_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(B.W.p, B.V[size_t(i)].p, B.H.p + long(i) * R, n, B.rmap.p);
+        axpy_dev_kernel<float2><<<dim3(eb, unsigned(nA)), 256, 0, s>>>(B.W.p, B.V[size_t(i)].p, B.H.p + long(i) * R, n,
+                                                                       B.rmap.p);
         EPSP_LAUNCHED(ctx);
       }
       dot_batch(B.W.p, B.W.p, nA, B.H.p + long(k) * R);
@@ -2104,7 +2148,8 @@ void ladder_run_batched(LadderPlan* P, const double* sigma, const double* mu, co
         if (B.V[size_t(k)].n != size_t(R * n)) B.V[size_t(k)].alloc(ctx, size_t(R * n));
         set_rmap(act);
         B.coef_a.upload(ca.data(), ca.size(), s);
-        scale_batch_kernel<<<dim3(eb, unsigned(act.size())), 256, 0, s>>>(B.coef_a.p, B.W.p, B.V[size_t(k)].p, n, B.rmap.p);
+        scale_kernel<float2><<<dim3(eb, unsigned(act.size())), 256, 0, s>>>(make_double2(0, 0), B.coef_a.p, B.W.p,
+                                                                             B.V[size_t(k)].p, n, B.rmap.p);
         EPSP_LAUNCHED(ctx);
       }
     }
@@ -2142,8 +2187,8 @@ void ladder_run_batched(LadderPlan* P, const double* sigma, const double* mu, co
       set_rmap(use);
       B.coef_a.upload(ca.data(), ca.size(), s);
       B.coef_b.upload(cb.data(), cb.size(), s);
-      axpby_batch_kernel<<<dim3(eb, unsigned(use.size())), 256, 0, s>>>(B.coef_a.p, B.V[size_t(i)].p, B.coef_b.p, B.J.p, n,
-                                                                         B.rmap.p);
+      axpby_kernel<float2><<<dim3(eb, unsigned(use.size())), 256, 0, s>>>(make_double2(0, 0), B.coef_a.p, B.V[size_t(i)].p,
+                                                                           make_double2(0, 0), B.coef_b.p, B.J.p, n, B.rmap.p);
       EPSP_LAUNCHED(ctx);
     }
     conductivity_batch(P, B, B.J.p, nP, pp, sl, idx);
@@ -2158,9 +2203,7 @@ void ladder_run_batched(LadderPlan* P, const double* sigma, const double* mu, co
         hist->nnorms[pidx] = nn;
       }
       if (hist && hist->nsigma) hist->nsigma[pidx] = 0;
-      if (J_out)
-        EPSP_CUDA(cudaMemcpyAsync(reinterpret_cast<double2*>(J_out) + size_t(n) * size_t(pidx), B.J.p + size_t(n) * size_t(z),
-                                  size_t(n) * sizeof(double2), cudaMemcpyDeviceToHost, s));
+      if (J_out) vertex_to_host(P, B.J.p + size_t(n) * size_t(z), n, J_out + 2 * size_t(n) * size_t(pidx));
     }
     EPSP_CUDA(cudaStreamSynchronize(s));
   }
@@ -2274,9 +2317,22 @@ epsp_status epsp_ladder_apply(epsp_ladder_plan* plan, const double* sigma_T, dou
     dJ.alloc(P->ctx, size_t(n));
     dLJ.alloc(P->ctx, size_t(n));
     dJ.upload(reinterpret_cast<const double2*>(J), size_t(n), s);
-    apply_L(P, dJ.p, dLJ.p);
-    dLJ.download(reinterpret_cast<double2*>(LJ), size_t(n), s);
-    EPSP_CUDA(cudaStreamSynchronize(s));
+    if (P->path == EPSP_PATH_GEMM_BF16) {  // FP32 vertices on the device
+      DBuf<float2> fJ, fLJ;
+      fJ.alloc(P->ctx, size_t(n));
+      fLJ.alloc(P->ctx, size_t(n));
+      to_f2_kernel<<<div_up(size_t(n), 256), 256, 0, s>>>(dJ.p, n, fJ.p);
+      EPSP_LAUNCHED(P->ctx);
+      apply_L(P, fJ.p, fLJ.p);
+      to_d2_kernel<<<div_up(size_t(n), 256), 256, 0, s>>>(fLJ.p, n, dLJ.p);
+      EPSP_LAUNCHED(P->ctx);
+      dLJ.download(reinterpret_cast<double2*>(LJ), size_t(n), s);
+      EPSP_CUDA(cudaStreamSynchronize(s));
+    } else {
+      apply_L(P, dJ.p, dLJ.p);
+      dLJ.download(reinterpret_cast<double2*>(LJ), size_t(n), s);
+      EPSP_CUDA(cudaStreamSynchronize(s));
+    }
     check_tc_err(P);
   });
 }

@@ -92,11 +92,12 @@ def test_loop_matches_oracle(api, oracle, cc):
 
 
 def test_holstein_current_correction_vanishes(api, hsym):
-    # test/test_ladder_holstein.jl:5-26 on the GPU paths
+    # test/test_ladder_holstein.jl:5-26 on the GPU paths; the tensor-core path keeps its vertices in
+    # FP32, so there the correction vanishes to FP32 rounding (a surviving correction is ~1e-2)
     c = hsym
-    for path in ("direct_fp64", "gemm_fp64", "gemm_bf16"):
+    for path, tol in (("direct_fp64", 1e-9), ("gemm_fp64", 1e-9), ("gemm_bf16", 1e-6)):
         out = api.loop_ladder(c["setup"], c["sigma"], c["mu"], c["Tlist"], [0.0, 0.2], path=path, omega_acoustic=W_AC)
-        assert np.linalg.norm(out["sigma_ladder"] - out["sigma_bubble"]) <= 1e-9 * np.linalg.norm(out["sigma_bubble"])
+        assert np.linalg.norm(out["sigma_ladder"] - out["sigma_bubble"]) <= tol * np.linalg.norm(out["sigma_bubble"])
         assert out["converged"].all()
 
 
@@ -116,22 +117,24 @@ def test_ladder_argument_checks(api, cc):
 
 def test_batched_right_hand_sides_match_the_sequential_solves(api, oracle, cc):
     # 2 temperatures x 3 Ωs = 6 (T, Ω) pairs solved together as GMRES right-hand sides, in batches
-    # of 4 (so one batch is partial), each from x0 = 0. Solved tightly (rtol 1e-9) the batched σ
-    # must equal the sequential tensor-core run's to 2e-5 relative (the operator's BF16 rounding,
-    # met along other Krylov paths) and the FP64 oracle's to 1e-4;
+    # of 4 (so one batch is partial), each from x0 = 0. Solved tightly (rtol 1e-6: the path's Krylov
+    # vectors are FP32, so its residuals settle near 1e-7) the batched σ must equal the sequential
+    # tensor-core run's to 2e-5 relative (the operator's BF16 rounding, met along other Krylov
+    # paths) and the FP64 oracle's (solved to 1e-9) to 1e-4;
     # at the loop's usual rtol 1e-2 each pair's σ_ladder must agree with the sequential one to the
     # solver tolerance.
     c = cc
     s = c["setup"]
     Omegas = [0.0, 0.05, 0.1]
     plan = api.LadderPlan(s, path="gemm_bf16", omega_acoustic=W_AC)
-    tight = dict(rtol=1e-9, maxiter=60)
+    tight = dict(rtol=1e-6, maxiter=60)
     seq = plan.run(c["sigma"], c["mu"], c["Tlist"], Omegas, store_vertex=True, **tight)
     bat = plan.run(c["sigma"], c["mu"], c["Tlist"], Omegas, batch_rhs=4, store_vertex=True, **tight)
     assert bat["converged"].all() and seq["converged"].all()
     assert rel(bat["sigma_bubble"], seq["sigma_bubble"]) <= 1e-12
     assert rel(bat["sigma_ladder"], seq["sigma_ladder"]) <= 2e-5
-    ref = oracle.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], Omegas, solver="gmres", omega_acoustic=W_AC, **tight)
+    ref = oracle.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], Omegas, solver="gmres", omega_acoustic=W_AC,
+                             rtol=1e-9, maxiter=60)
     assert rel(bat["sigma_ladder"], ref["sigma_ladder"]) <= 1e-4
     # the stored vertices: every pair's J equals the sequential solve's (both converged tightly)
     for iT in range(2):
