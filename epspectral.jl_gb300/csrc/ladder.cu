@@ -618,6 +618,9 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const float2* __restrict
       }
     }
     __syncthreads();
+    // write-out: a warp takes 4 rows x 8 column chunks of 8, i.e. whole 128-byte row segments (an
+    // 8 x 4 split of the warp avoids the 2-way bank conflicts of the transposed reads but writes
+    // 64-byte segments, and measured slower)
     const int wr = threadIdx.x / 8, kc = (threadIdx.x % 8) * 8;
     for (int t4 = 0; t4 < 2 * nq; ++t4) {
       const int q = qbase + t4 / 2, ri = t4 % 2;
@@ -1603,7 +1606,9 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
   const double btol = std::pow(std::numeric_limits<double>::epsilon(), 0.75);
   for (int64_t iT = 0; iT < nT; ++iT) {
     const double T = Tlist[iT];
+    long pu = prof_begin(ctx, "ladder_io");
     P->d_ST.upload(reinterpret_cast<const double2*>(sigma) + size_t(nw * ni * iT), size_t(nw * ni), s);
+    prof_end(ctx, pu);
     for (int64_t iO = 0; iO < nO; ++iO) {
       const double Om = Omegas[iO];
       const int64_t idx = iO + nO * iT;

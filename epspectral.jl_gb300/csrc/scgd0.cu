@@ -70,6 +70,13 @@ __global__ void gather_wq_kernel(const double* __restrict__ wph, const int32_t* 
   wqt[idx] = wph[nu + long(nm) * q];
 }
 
+// Σ = Σ_new = -i η_init everywhere (the start without Σ_init, src/scgd0.jl:226).
+__global__ void fill_start_kernel(double2* __restrict__ S, double2* __restrict__ Snew, long n, double eta_init) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  S[k] = Snew[k] = make_double2(0.0, -eta_init);
+}
+
 // Σ_in = Re Σ + i min(Im Σ, -η_min) (src/scgd0.jl:256-260), for the active temperatures: slot a
 // (blockIdx.y) reads Σ of temperature slots[a] and writes Sin + a n.
 __global__ void clamp_kernel(const double2* __restrict__ S, double2* __restrict__ Sin, long n,
@@ -1095,13 +1102,14 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   if (sigma_init) {
     for (long k = 0; k < 2 * slab * nT; ++k)
       if (!std::isfinite(sigma_init[k])) fail(EPSP_EINVAL, "Sigma_init must be finite");
+    long pu = prof_begin(ctx, "scgd0_io");
     S.upload(reinterpret_cast<const double2*>(sigma_init), size_t(slab * nT), s);
+    prof_end(ctx, pu);
+    EPSP_CUDA(cudaMemcpyAsync(Snew.p, S.p, size_t(slab * nT) * sizeof(double2), cudaMemcpyDeviceToDevice, s));
   } else {
-    std::vector<double2> init(size_t(slab * nT), make_double2(0.0, -eta_init));
-    S.upload(init.data(), init.size(), s);
-    EPSP_CUDA(cudaStreamSynchronize(s));
+    fill_start_kernel<<<div_up(size_t(slab * nT), 256), 256, 0, s>>>(S.p, Snew.p, slab * nT, eta_init);
+    EPSP_LAUNCHED(ctx);
   }
-  EPSP_CUDA(cudaMemcpyAsync(Snew.p, S.p, size_t(slab * nT) * sizeof(double2), cudaMemcpyDeviceToDevice, s));
   std::vector<double> mu(mu_start, mu_start + nT);
   std::vector<char> active(static_cast<size_t>(nT), 1);
   const double nan = std::numeric_limits<double>::quiet_NaN();
@@ -1158,7 +1166,7 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   std::vector<TParams> h_tp(static_cast<size_t>(nT));
   std::vector<int> slots;
   // CUDA graph of the iteration body (tensor-core path; not while one of its kernels is profiled)
-  static const char* kBodyProfiles[] = {"kbuild", "tc_fm", "tc_kk", "finalize", "spectral", "mu"};
+  static const char* kBodyProfiles[] = {"kprep", "kbuild", "tc_fm", "tc_kk", "finalize", "spectral", "mu"};
   bool use_graph = P->path == EPSP_PATH_GEMM_BF16;
   for (const char* nm : kBodyProfiles)
     if (ctx->prof_name == nm) use_graph = false;
@@ -1332,7 +1340,9 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
     if (std::none_of(active.begin(), active.end(), [](char a) { return a != 0; })) break;
   }
   hist->niter = niter;
+  long pd = prof_begin(ctx, "scgd0_io");
   S.download(reinterpret_cast<double2*>(sigma_out), size_t(slab * nT), s);
+  prof_end(ctx, pd);
   EPSP_CUDA(cudaStreamSynchronize(s));
   for (int64_t iT = 0; iT < nT; ++iT) {
     mu_out[iT] = mu[size_t(iT)];

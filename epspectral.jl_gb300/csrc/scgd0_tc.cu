@@ -59,76 +59,110 @@ __global__ void sigma_f32_kernel(const double2* __restrict__ S, long n, float4* 
 }
 
 // Kernel tensor of the recast Fan-Migdal sum (see kbuild_f64_kernel in scgd0.cu), written as BF16
-// split rows K_t[ω][k] through a shared-memory transpose. The cells of ω ± ω_ν come from the setup
-// table; Re z = (x - ε) - Re Σ(x), which cancels near the quasiparticle pole, is formed exactly from
-// float pairs (re_z), and Im Σ(x), the reciprocal and the occupation products are FP32: the kernel
-// runs on the FP32 units only.
-__global__ void __launch_bounds__(256) kbuild_bf16_kernel(int nw, long slab, const float4* __restrict__ Sf_all,
+// split rows K_t[ω][k], k = c nm + ν, through a shared-memory transpose. The cells of ω ± ω_ν come
+// from the setup table; Re z = (x - ε) - Re Σ(x), which cancels near the quasiparticle pole, is
+// formed exactly from float pairs (re_z), and Im Σ(x), the reciprocal and the occupation products
+// are FP32: the kernel runs on the FP32 units only.
+// Grid (nω / 16, Kp / (kKbCols nm), slots), 256 threads: thread (node ω0 + t % 16, modes t / 16,
+// t / 16 + 16, ..) loads the cells and occupations of its (ω, ν) once and runs over the block's
+// kKbCols columns c (their Σ column and energy from shared memory), so per element only the two
+// interpolations of Σ and the arithmetic remain. Dynamic shared memory: the tile [kKbCols nm][17]
+// floats. kKbCols nm must be a multiple of 8, so that the write-out's 16-byte chunks never
+// straddle two blocks (nor Kp, a multiple of 64).
+constexpr int kKbCols = 8;
+constexpr int kKbW = 16;
+__global__ void __launch_bounds__(256, 6) kbuild_bf16_kernel(int nw, long slab, const float4* __restrict__ Sf_all,
                                                           const int32_t* __restrict__ cell_j,
                                                           const float* __restrict__ cell_t,
                                                           const float2* __restrict__ cell_x,
                                                           const uint8_t* __restrict__ skip, int nm,
                                                           const float2* __restrict__ eps_c,
-                                                          const int32_t* __restrict__ col_c, int nk,
+                                                          const int32_t* __restrict__ col_c, int nc,
                                                           const float* __restrict__ F_all,
                                                           __nv_bfloat16* __restrict__ K0, __nv_bfloat16* __restrict__ K1,
                                                           __nv_bfloat16* __restrict__ K2, long Kp) {
-  __shared__ float tile[64][33];
-  const int w0 = blockIdx.x * 32;
-  const int k0 = blockIdx.y * 64;
-  const int tw = threadIdx.x % 32, tk = threadIdx.x / 32;
+  extern __shared__ float kb_tile[];  // [kKbCols nm][kKbW + 1]
+  __shared__ int s_col[kKbCols];
+  __shared__ float2 s_eps[kKbCols];
+  const int w0 = blockIdx.x * kKbW;
+  const int cbeg = blockIdx.y * kKbCols;
+  const int tw = threadIdx.x % kKbW, tm = threadIdx.x / kKbW;
   const int iw = w0 + tw;
-  const long nwm = long(nw) * nm;
-  // slot blockIdx.z: its clamped Σ, its occupation tables, its nω rows of K_t
+  const int nwm = nw * nm;
   const float4* Sf = Sf_all + slab * blockIdx.z;
-  const float* F = F_all + 2 * nwm * blockIdx.z;
-  const long krow0 = long(nw) * blockIdx.z;
-#pragma unroll 2
-  for (int r = 0; r < 8; ++r) {
-    const int kl = tk + 8 * r;
-    const int k = k0 + kl;  // 32-bit index arithmetic: nk < 2^30
-    float v = 0.f;
-    if (iw < nw && k < nk) {
-      const int c = k / nm, nu = k - c * nm;
-      if (!skip[nu]) {
-        const float4* col = Sf + long(nw) * col_c[c];
-        const float2 e = eps_c[c];
-        const long ia = iw + long(nw) * nu, ie = ia + nwm;
-        const int ja = cell_j[ia], je = cell_j[ie];
-        const float ta = cell_t[ia], te = cell_t[ie];
+  const float* F = F_all + 2l * nwm * blockIdx.z;
+  if (threadIdx.x < kKbCols) {
+    const int c = cbeg + threadIdx.x;
+    s_col[threadIdx.x] = c < nc ? nw * col_c[c] : -1;
+    s_eps[threadIdx.x] = c < nc ? eps_c[c] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  for (int nu = tm; nu < nm; nu += 256 / kKbW) {
+    const bool on = iw < nw && !skip[nu];
+    int ja = 0, je = 0;
+    float ta = 0.f, te = 0.f, Fa = 0.f, Fe = 0.f;
+    float2 xa = make_float2(0.f, 0.f), xe = xa;
+    if (on) {
+      const int ia = iw + nw * nu, ie = ia + nwm;
+      ja = cell_j[ia];
+      je = cell_j[ie];
+      ta = cell_t[ia];
+      te = cell_t[ie];
+      xa = cell_x[ia];
+      xe = cell_x[ie];
+      Fa = F[ia];
+      Fe = F[ie];
+    }
+#pragma unroll 4
+    for (int cl = 0; cl < kKbCols; ++cl) {
+      const int co = s_col[cl];
+      float v = 0.f;
+      if (on && co >= 0) {
+        const float4* col = Sf + co;
+        const float2 e = s_eps[cl];
         const float4 la = col[ja], ha = col[ja + 1], le = col[je], he = col[je + 1];
-        const float zar = re_z(cell_x[ia], e, la, ha, ta);
-        const float zer = re_z(cell_x[ie], e, le, he, te);
+        const float zar = re_z(xa, e, la, ha, ta);
+        const float zer = re_z(xe, e, le, he, te);
         const float sia = (1.f - ta) * la.z + ta * ha.z;  // Im Σ(x)
         const float sie = (1.f - te) * le.z + te * he.z;
         // Im 1/z with Im z = -Im Σ; the K tensor carries FP32 precision, so an approximate
         // division (2 ulp; denominators here lie far inside its range) is enough
         const float ga = __fdividef(sia, zar * zar + sia * sia);
         const float ge = __fdividef(sie, zer * zer + sie * sie);
-        v = ga * F[ia] + ge * F[ie];
+        v = ga * Fa + ge * Fe;
       }
+      kb_tile[(cl * nm + nu) * (kKbW + 1) + tw] = v;
     }
-    tile[kl][tw] = v;
   }
   __syncthreads();
-  const int wr = threadIdx.x / 8, kc = (threadIdx.x % 8) * 8;
-  const int ow = w0 + wr;
-  if (ow < nw) {
-    __align__(16) __nv_bfloat16 p0[8], p1[8], p2[8];
+  // write-out: the block's columns [cbeg nm, (cbeg + kKbCols) nm) of rows ω0.., 8 BF16 per store; a
+  // half-warp writes one row's chunks (contiguous)
+  const long kbeg = long(cbeg) * nm;
+  const int nchunk = kKbCols * nm / 8;
+  const long krow0 = long(nw) * blockIdx.z;
+  for (int wr = threadIdx.x / 16; wr < kKbW; wr += 16) {
+    for (int ch = threadIdx.x % 16; ch < nchunk; ch += 16) {
+      const int ow = w0 + wr;
+      const long k = kbeg + 8 * ch;
+      if (ow >= nw || k >= Kp) continue;
+      __align__(16) __nv_bfloat16 p0[8], p1[8], p2[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      __nv_bfloat16 q[3];
-      split_bf16_n(tile[kc + j][wr], 3, q);
-      p0[j] = q[0];
-      p1[j] = q[1];
-      p2[j] = q[2];
+      for (int j = 0; j < 8; ++j) {
+        __nv_bfloat16 q[3];
+        split_bf16_n(kb_tile[(8 * ch + j) * (kKbW + 1) + wr], 3, q);
+        p0[j] = q[0];
+        p1[j] = q[1];
+        p2[j] = q[2];
+      }
+      const long off = (krow0 + ow) * Kp + k;
+      *reinterpret_cast<uint4*>(K0 + off) = *reinterpret_cast<const uint4*>(p0);
+      *reinterpret_cast<uint4*>(K1 + off) = *reinterpret_cast<const uint4*>(p1);
+      *reinterpret_cast<uint4*>(K2 + off) = *reinterpret_cast<const uint4*>(p2);
     }
-    const long off = (krow0 + ow) * Kp + k0 + kc;
-    *reinterpret_cast<uint4*>(K0 + off) = *reinterpret_cast<const uint4*>(p0);
-    *reinterpret_cast<uint4*>(K1 + off) = *reinterpret_cast<const uint4*>(p1);
-    *reinterpret_cast<uint4*>(K2 + off) = *reinterpret_cast<const uint4*>(p2);
   }
 }
+
+static size_t kbuild_smem_bytes(long nm) { return size_t(kKbCols * nm * (kKbW + 1)) * sizeof(float); }
 
 // out_p[r * ld + c] = part p of S(r, c) for c < cols, 0 for cols <= c < ld, with S(r, c) =
 // S[c + ldc r] (transposed = false: rows of the output are columns of the column-major S) or
@@ -243,6 +277,11 @@ void tc_setup(Scgd0Plan* P) {
   T->Kp = pad64(nk);
   T->Kp2 = pad64(nw);
   if (nw > (1l << 30) || ni > (1l << 30) || nk > (1l << 30)) fail(EPSP_EINVAL, "sizes beyond the 32-bit tile grid");
+  if (kbuild_smem_bytes(P->nm) > size_t(227 * 1024))
+    fail(EPSP_EUNSUPPORTED, "the BF16 scGD0 path takes at most 427 modes; use EPSP_PATH_GEMM_FP64");
+  if (kbuild_smem_bytes(P->nm) > size_t(48 * 1024))
+    EPSP_CUDA(cudaFuncSetAttribute(kbuild_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   int(kbuild_smem_bytes(P->nm))));
   for (int p = 0; p < kNs; ++p) {
     T->Kt[p].alloc(ctx, size_t(nw * T->Kp));
     T->G[p].alloc(ctx, size_t(ni * T->Kp));
@@ -308,9 +347,10 @@ void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS) {
   EPSP_LAUNCHED(ctx);
   to_f32_kernel<<<div_up(size_t(nwm), 256), 256, 0, s>>>(P->d_Fe.p, nwm, T->Ff.p + nwm);
   EPSP_LAUNCHED(ctx);
-  kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), 32), unsigned(T->Kp / 64), 1), 256, 0, s>>>(
-      int(nw), nw * ni, T->Sf.p, P->d_cell_j.p, T->tf.p, T->xf.p, T->skip.p, int(P->nm), T->ef.p, P->d_colc.p, int(nk),
-      T->Ff.p, T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
+  kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), kKbW), unsigned(div_up(size_t(T->Kp), size_t(kKbCols * P->nm))), 1), 256,
+                       kbuild_smem_bytes(P->nm), s>>>(int(nw), nw * ni, T->Sf.p, P->d_cell_j.p, T->tf.p, T->xf.p,
+                                                      T->skip.p, int(P->nm), T->ef.p, P->d_colc.p, int(P->nc), T->Ff.p,
+                                                      T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pk);
   const long slab = nw * ni;
@@ -377,15 +417,19 @@ void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, co
   if (nA > T->capT) fail(EPSP_EINVAL, "more active temperatures than reserved");
   const long nw = P->nw, ni = P->ni, nk = P->nm * P->nc, nwm = nw * P->nm, slab = nw * ni;
   const unsigned eb = div_up(size_t(slab), 256);
-  long pk = prof_begin(ctx, "kbuild");
+  long pp = prof_begin(ctx, "kprep");
   sigma_f32_batch_kernel<<<div_up(size_t(slab * nA), 256), 256, 0, s>>>(d_Sin_b, slab, nA, T->Sf.p);
   EPSP_LAUNCHED(ctx);
   occ_table_f32_kernel<<<dim3(div_up(size_t(nwm), 256), unsigned(nA)), 256, 0, s>>>(
       P->d_ws.p, int(nw), P->d_wnu.p, int(P->nm), d_slots, d_tp, P->w_ac, T->Ff.p);
   EPSP_LAUNCHED(ctx);
-  kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), 32), unsigned(T->Kp / 64), unsigned(nA)), 256, 0, s>>>(
-      int(nw), slab, T->Sf.p, P->d_cell_j.p, T->tf.p, T->xf.p, T->skip.p, int(P->nm), T->ef.p, P->d_colc.p, int(nk),
-      T->Ff.p, T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
+  prof_end(ctx, pp);
+  long pk = prof_begin(ctx, "kbuild");
+  kbuild_bf16_kernel<<<dim3(div_up(size_t(nw), kKbW), unsigned(div_up(size_t(T->Kp), size_t(kKbCols * P->nm))),
+                            unsigned(nA)),
+                       256, kbuild_smem_bytes(P->nm), s>>>(int(nw), slab, T->Sf.p, P->d_cell_j.p, T->tf.p, T->xf.p,
+                                                           T->skip.p, int(P->nm), T->ef.p, P->d_colc.p, int(P->nc), T->Ff.p,
+                                                           T->Kt[0].p, T->Kt[1].p, T->Kt[2].p, T->Kp);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pk);
   // ImΣ of every slot: the stacked K_t rows times G
