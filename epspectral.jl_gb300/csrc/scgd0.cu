@@ -88,6 +88,18 @@ __global__ void clamp_kernel(const double2* __restrict__ S, double2* __restrict_
   Sin[long(a) * n + k] = make_double2(z.x, fmin(z.y, -tp[t].eta_min));
 }
 
+// The same clamp for the tensor-core path, written straight into its FP32 form {Re Σ as a float
+// pair, Im Σ, 0} (slot a at Sf + a n).
+__global__ void clamp_f32_kernel(const double2* __restrict__ S, float4* __restrict__ Sf, long n,
+                                 const int* __restrict__ slots, const TParams* __restrict__ tp) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int a = blockIdx.y, t = slots[a];
+  const double2 z = S[long(t) * n + k];
+  const float2 r = split_df(z.x);
+  Sf[long(a) * n + k] = make_float4(r.x, r.y, float(fmin(z.y, -tp[t].eta_min)), 0.f);
+}
+
 // The reference's Fan-Migdal sum, term by term in FP64: for each (ω, i), the sum over νf of
 // _fan_migdal_imsigma_term (src/scgd0_kernel.jl:27-39) in ascending νf, added to ImΣ
 // (src/scgd0_kernel.jl:74-86). One thread per (ω, i); the block's νf tile (g2, ωq, n_B(ωq) and the
@@ -1143,7 +1155,7 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   bool grown = false;
   grown |= ensure(d_slots, ctx, size_t(nT));
   grown |= ensure(d_tp, ctx, size_t(nT));
-  grown |= ensure(Sin_b, ctx, size_t(slab * nT));
+  if (P->path != EPSP_PATH_GEMM_BF16) grown |= ensure(Sin_b, ctx, size_t(slab * nT));  // the tensor-core path clamps into FP32
   const bool f32_spec = P->path == EPSP_PATH_GEMM_BF16;
   const int spec_nab = int(div_up(size_t(nwa), 256)), spec_nch = int(div_up(size_t(ni), size_t(kSpecChunk)));
   if (f32_spec) {
@@ -1197,10 +1209,13 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
     auto body = [&] {
       EPSP_CUDA(cudaMemsetAsync(d_err, 0, size_t(nT) * 8, s));
       EPSP_CUDA(cudaMemsetAsync(d_status, 0, size_t(2 * nT) * sizeof(int), s));
-      clamp_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(S.p, Sin_b.p, slab, d_slots.p, d_tp.p);
+      if (P->path == EPSP_PATH_GEMM_BF16)
+        clamp_f32_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(S.p, tc_sigma_f32(P), slab, d_slots.p, d_tp.p);
+      else
+        clamp_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(S.p, Sin_b.p, slab, d_slots.p, d_tp.p);
       EPSP_LAUNCHED(ctx);
       if (P->path == EPSP_PATH_GEMM_BF16) {
-        tc_iterate(P, nA, d_slots.p, slots.data(), d_tp.p, Sin_b.p, Snew.p);
+        tc_iterate(P, nA, d_slots.p, slots.data(), d_tp.p, nullptr, Snew.p);
         EPSP_CUDA(cudaMemcpyAsync(d_tcerr, tc_err_ptr(P), sizeof(int), cudaMemcpyDeviceToDevice, s));
       } else {
         for (int a = 0; a < nA; ++a) {

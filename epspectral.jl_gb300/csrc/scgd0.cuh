@@ -77,8 +77,11 @@ void tc_reserve(Scgd0Plan* P, long nT);
 long tc_capacity(Scgd0Plan* P);
 // Σ_new of nA active temperatures at once: slot a reads the clamped Σ_in + a nω ni and writes
 // Snew_all + slots_h[a] nω ni (temperature index); per-temperature T and μ from tp (device).
+// With d_Sin_b null, the slots' clamped Σ are already in the FP32 buffer tc_sigma_f32 returns.
 void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, const TParams* d_tp,
                 const double2* d_Sin_b, double2* d_Snew_all);
+// The FP32 form of the clamped Σ of every reserved temperature ({Re hi, Re lo, Im, 0}, slot-major).
+float4* tc_sigma_f32(Scgd0Plan* P);
 // Fails with EPSP_EDEVICE_TIMEOUT if a tensor-core GEMM's bounded wait ran out (synchronises).
 void tc_check(Scgd0Plan* P);
 // The device flag the tensor-core GEMMs set when a bounded wait runs out.

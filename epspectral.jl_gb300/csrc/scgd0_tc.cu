@@ -233,8 +233,12 @@ __global__ void sigma_f32_batch_kernel(const double2* __restrict__ S, long n, in
 }
 
 // ImΣ of slot a: ImS[a][ω + nω i] = Σ_s part[s][(a nω + ω) + M i], M = nA nω (the stacked rows).
+// With Im0 (the batched iteration), it also writes ImΣ split into the KK product's B operand (whose
+// padding columns nω.. Kp2 stay zero from the reservation).
 __global__ void finalize_fm_batch_kernel(const float* __restrict__ part, int nw, long slab, int nA, int splits,
-                                         long stride, double* __restrict__ ImS) {
+                                         long stride, double* __restrict__ ImS, __nv_bfloat16* __restrict__ Im0 = nullptr,
+                                         __nv_bfloat16* __restrict__ Im1 = nullptr, __nv_bfloat16* __restrict__ Im2 = nullptr,
+                                         long Kp2 = 0) {
   const long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= slab) return;
   const int a = blockIdx.y;
@@ -243,6 +247,14 @@ __global__ void finalize_fm_batch_kernel(const float* __restrict__ part, int nw,
   float acc = 0.f;
   for (int p = 0; p < splits; ++p) acc += part[src + stride * p];
   ImS[slab * a + k] = double(acc);
+  if (Im0) {  // and the B operand of the Kramers-Kronig product: row a ni + i, column ω, three parts
+    __nv_bfloat16 q[3];
+    split_bf16_n(acc, 3, q);
+    const long o = (long(a) * (slab / nw) + i) * Kp2 + w;
+    Im0[o] = q[0];
+    Im1[o] = q[1];
+    Im2[o] = q[2];
+  }
 }
 
 // Σ_new of temperature slots[a] = Σ_s part[s][a slab + k] + i ImS[a][k] (the KK product's columns
@@ -385,6 +397,7 @@ void tc_reserve(Scgd0Plan* P, long nT) {
   for (int p = 0; p < kNs; ++p) {
     T->Kt[p].alloc(ctx, size_t(nT * nw * T->Kp));
     T->Im[p].alloc(ctx, size_t(nT * ni * T->Kp2));
+    T->Im[p].zero(ctx->stream);  // the padding columns nω.. Kp2 of the KK operand stay zero
   }
   T->Sf.alloc(ctx, size_t(nT * slab));
   T->Ff.alloc(ctx, size_t(nT * 2 * nwm));
@@ -408,6 +421,8 @@ int* tc_err_ptr(Scgd0Plan* P) { return P->tc->err.p; }
 
 long tc_capacity(Scgd0Plan* P) { return P->tc->ImS_b.p ? P->tc->capT : 0; }
 
+float4* tc_sigma_f32(Scgd0Plan* P) { return P->tc->Sf.p; }
+
 void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, const TParams* d_tp,
                 const double2* d_Sin_b, double2* d_Snew_all) {
   (void)slots_h;
@@ -418,9 +433,12 @@ void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, co
   const long nw = P->nw, ni = P->ni, nk = P->nm * P->nc, nwm = nw * P->nm, slab = nw * ni;
   const unsigned eb = div_up(size_t(slab), 256);
   long pp = prof_begin(ctx, "kprep");
-  sigma_f32_batch_kernel<<<div_up(size_t(slab * nA), 256), 256, 0, s>>>(d_Sin_b, slab, nA, T->Sf.p);
-  EPSP_LAUNCHED(ctx);
-  occ_table_f32_kernel<<<dim3(div_up(size_t(nwm), 256), unsigned(nA)), 256, 0, s>>>(
+  if (d_Sin_b) {
+    sigma_f32_batch_kernel<<<div_up(size_t(slab * nA), 256), 256, 0, s>>>(d_Sin_b, slab, nA, T->Sf.p);
+    EPSP_LAUNCHED(ctx);
+  }
+  // small blocks: the FP64 exponentials of the table spread over every SM
+  occ_table_f32_kernel<<<dim3(div_up(size_t(nwm), 64), unsigned(nA)), 64, 0, s>>>(
       P->d_ws.p, int(nw), P->d_wnu.p, int(P->nm), d_slots, d_tp, P->w_ac, T->Ff.p);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pp);
@@ -436,14 +454,11 @@ void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, co
   const long M = long(nA) * nw;
   int sp = tc_gemm_launch(ctx, T->opK, T->opG, int(M), int(ni), int(nk), T->part.p, M, M * ni, 16, T->err.p, "tc_fm",
                           kKbCap);
+  // ImΣ of every slot, and its BF16 split as the B operand of ReΣ = KK ImΣ (columns: the slots'
+  // states in order)
   long pf = prof_begin(ctx, "finalize");
-  finalize_fm_batch_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(T->part.p, int(nw), slab, nA, sp, M * ni, T->ImS_b.p);
-  EPSP_LAUNCHED(ctx);
-  prof_end(ctx, pf);
-  // ReΣ = KK ImΣ for every slot at once (columns: the slots' states in order)
-  pf = prof_begin(ctx, "finalize");
-  split3_rows_kernel<<<div_up(size_t(nA * ni * T->Kp2), 256), 256, 0, s>>>(T->ImS_b.p, nw, nA * ni, nw, T->Kp2, false,
-                                                                            T->Im[0].p, T->Im[1].p, T->Im[2].p);
+  finalize_fm_batch_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(T->part.p, int(nw), slab, nA, sp, M * ni, T->ImS_b.p,
+                                                                   T->Im[0].p, T->Im[1].p, T->Im[2].p, T->Kp2);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pf);
   const long N2 = long(nA) * ni;
