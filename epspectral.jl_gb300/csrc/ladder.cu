@@ -90,12 +90,12 @@ struct LadderPlan {
   std::vector<double> h_tm, h_tp;
   double tab_Om = std::numeric_limits<double>::quiet_NaN();
   double cur_T = 0, cur_mu = 0, cur_Om = 0;
-  // GEMM_BF16: D and KY in FP32, the propagators as FP32 complex
-  DBuf<float> d_Df, d_KYf;
+  // GEMM_BF16: KY in FP32, the propagators as FP32 complex
+  DBuf<float> d_KYf;
   DBuf<float2> d_Gmf, d_Gpf;
   // work buffers of the solves, kept across runs (vertex vectors: FP64 complex on the FP64 paths,
   // FP32 complex on the tensor-core path)
-  DBuf<double2> w_J0, w_J, w_LJ, w_W, w_part, w_scal, w_H, w_Y;
+  DBuf<double2> w_J0, w_J, w_LJ, w_W, w_part, w_H, w_Y;
   std::vector<DBuf<double2>> w_V;
   DBuf<float2> w_J0f, w_Jf, w_LJf, w_Wf;
   std::vector<DBuf<float2>> w_Vf;
@@ -666,20 +666,27 @@ static size_t xgen_smem_bytes(int ns) {
 // K = ω' contiguous, stride Kp2.
 // Batched over blockIdx.y: slot z reads rows z 24 nwp.. of D (column stride ldD) and writes rows
 // z 8N.. of Y.
-__global__ void y_split_kernel(const float* __restrict__ D, long ldD, int nw, int nwp, long N, long Kp2,
-                               __nv_bfloat16* __restrict__ Yh, __nv_bfloat16* __restrict__ Yl) {
-  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= 8 * N * Kp2) return;
-  const long z = blockIdx.y;
-  long w = idx % Kp2, r = idx / Kp2;
-  int qq = int(r % 2), c0 = int((r / 2) % 2), ri = int((r / 4) % 2);
-  long n = r / 8;
-  float x = 0.f;
-  if (w < nw) x = D[z * 24 * nwp + w + long(nwp) * ((qq == 0 ? 0 : 2) + 6 * (c0 + 2 * ri)) + ldD * n];
-  __nv_bfloat16 h = __float2bfloat16_rn(x);
-  const long o = z * 8 * N * Kp2 + idx;
-  Yh[o] = h;
-  Yl[o] = __float2bfloat16_rn(x - __bfloat162float(h));
+// D is read as the sum of its dsplits split-K partials D + p dstride (in ascending p, as the FP32
+// sum the GEMM's split-K parts take elsewhere). Grid (Kp2 / 256, N, slots): thread (ω', n) writes
+// the 8 rows (qq, c0, ri, n).
+__global__ void y_split_kernel(const float* __restrict__ D, long ldD, int dsplits, long dstride, int nw, int nwp, long N,
+                               long Kp2, __nv_bfloat16* __restrict__ Yh, __nv_bfloat16* __restrict__ Yl) {
+  const long w = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (w >= Kp2) return;
+  const long n = blockIdx.y, z = blockIdx.z;
+#pragma unroll
+  for (int r8 = 0; r8 < 8; ++r8) {
+    const int qq = r8 % 2, c0 = (r8 / 2) % 2, ri = r8 / 4;
+    float x = 0.f;
+    if (w < nw) {
+      const long src = z * 24 * nwp + w + long(nwp) * ((qq == 0 ? 0 : 2) + 6 * (c0 + 2 * ri)) + ldD * n;
+      for (int p = 0; p < dsplits; ++p) x += D[src + dstride * p];
+    }
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    const long o = z * 8 * N * Kp2 + (r8 + 8 * n) * Kp2 + w;
+    Yh[o] = h;
+    Yl[o] = __float2bfloat16_rn(x - __bfloat162float(h));
+  }
 }
 
 __global__ void split_rows_plain_kernel(const double* __restrict__ S, long rows, long cols, long ld, long Kp,
@@ -732,10 +739,10 @@ __global__ void y_gemm_kernel(const double* __restrict__ D, int nw, int nwp, lon
 // z 24 nwp.. of D (column stride ldD) and KY + z nω 24ni, and writes LJ + 24 nω ni r with the
 // propagators Gm, Gp + 4 nω ni r of right-hand side r = rmap[z] (r = z without rmap).
 // With X_all, it writes X - L(X) instead of L(X) (the GMRES operator applied to X, in one pass).
-// R = float (tensor-core path): D, KY in FP32 and the propagators and vertices FP32 complex; R =
-// double: all FP64.
+// R = float (tensor-core path): D (as dsplits split-K partials dstride apart, summed in ascending
+// order), KY in FP32 and the propagators and vertices FP32 complex; R = double: all FP64.
 template <class R>
-__global__ void finish_gemm_kernel(const R* __restrict__ D_all, long ldD, const R* __restrict__ KY_all,
+__global__ void finish_gemm_kernel(const R* __restrict__ D_all, long ldD, int dsplits, long dstride, const R* __restrict__ KY_all,
                                    const Vec2<R>* __restrict__ Gm_all, const Vec2<R>* __restrict__ Gp_all,
                                    const int* __restrict__ rmap, int nw, int nwp, int ni, Vec2<R>* __restrict__ LJ_all,
                                    const Vec2<R>* __restrict__ X_all = nullptr) {
@@ -753,7 +760,22 @@ __global__ void finish_gemm_kernel(const R* __restrict__ D_all, long ldD, const 
   const int a = r % 3, c0 = (r / 3) % 2;
   const long i = r / 6;
   const long n = a + 3 * i;
-  auto d = [&](int q, int ri) { return R(D[w + long(nwp) * (q + 6 * (c0 + 2 * ri)) + ldD * n]); };
+  // the 8 values of D this thread reads (rows q = 1, 3, 4, 5 of re and im; q = 0, 2 enter through
+  // KY), summed over the split-K partials with all loads of a partial issued together
+  R dv[2][6];
+#pragma unroll
+  for (int ri = 0; ri < 2; ++ri)
+#pragma unroll
+    for (int q = 0; q < 6; ++q) dv[ri][q] = 0;
+  for (int p = 0; p < dsplits; ++p) {
+    const R* src = D + w + ldD * n + dstride * p;
+#pragma unroll
+    for (int ri = 0; ri < 2; ++ri)
+#pragma unroll
+      for (int q = 1; q < 6; ++q)
+        if (q != 2) dv[ri][q] += src[long(nwp) * (q + 6 * (c0 + 2 * ri))];
+  }
+  auto d = [&](int q, int ri) { return dv[ri][q]; };
   auto ky = [&](int qq, int ri) { return R(KY[w + nw * (qq + 2 * (c0 + 2 * (ri + 2 * n)))]); };
   Cx<R> K[4];
   {
@@ -819,21 +841,25 @@ __global__ void __launch_bounds__(256) dot_partial_kernel(const V* __restrict__ 
       ai += a.x * b.y - a.y * b.x;
     }
   } else {
-    float fr = 0.f, fi = 0.f;
-    int run = 0;
-    for (long k = long(blockIdx.x) * 256 + threadIdx.x; k < n; k += long(gridDim.x) * 256) {
-      const float2 a = u[k], b = v[k];
-      fr += a.x * b.x + a.y * b.y;
-      fi += a.x * b.y - a.y * b.x;
-      if (++run == kRun) {
-        ar += fr;
-        ai += fi;
-        fr = fi = 0.f;
-        run = 0;
+    // runs of kRun strided elements, their loads issued together
+    const long stride = long(gridDim.x) * 256;
+    for (long k0 = long(blockIdx.x) * 256 + threadIdx.x; k0 < n; k0 += stride * kRun) {
+      float2 a[kRun], b[kRun];
+#pragma unroll
+      for (int q = 0; q < kRun; ++q) {
+        const long k = k0 + stride * q;
+        a[q] = k < n ? u[k] : make_float2(0.f, 0.f);
+        b[q] = k < n ? v[k] : make_float2(0.f, 0.f);
       }
+      float fr = 0.f, fi = 0.f;
+#pragma unroll
+      for (int q = 0; q < kRun; ++q) {
+        fr += a[q].x * b[q].x + a[q].y * b[q].y;
+        fi += a[q].x * b[q].y - a[q].y * b[q].x;
+      }
+      ar += fr;
+      ai += fi;
     }
-    ar += fr;
-    ai += fi;
   }
   sr[threadIdx.x] = ar;
   si[threadIdx.x] = ai;
@@ -924,25 +950,40 @@ __global__ void __launch_bounds__(256) axpy_norm_kernel(V* __restrict__ q, const
   const double2 hd = *h;
   const R hx = R(hd.x), hy = R(hd.y);
   double ar = 0;
-  R fr = 0;
-  int run = 0;
-  for (long k = long(blockIdx.x) * 256 + threadIdx.x; k < n; k += long(gridDim.x) * 256) {
-    const V x = v[k];
-    V a = q[k];
-    a = VecOf<V>::make(a.x - (hx * x.x - hy * x.y), a.y - (hx * x.y + hy * x.x));
-    q[k] = a;
-    if constexpr (std::is_same_v<V, double2>) {
+  if constexpr (std::is_same_v<V, double2>) {
+    for (long k = long(blockIdx.x) * 256 + threadIdx.x; k < n; k += long(gridDim.x) * 256) {
+      const V x = v[k];
+      V a = q[k];
+      a = VecOf<V>::make(a.x - (hx * x.x - hy * x.y), a.y - (hx * x.y + hy * x.x));
+      q[k] = a;
       ar += a.x * a.x + a.y * a.y;
-    } else {
-      fr += a.x * a.x + a.y * a.y;
-      if (++run == kRun) {
-        ar += fr;
-        fr = 0;
-        run = 0;
+    }
+  } else {
+    // runs of kRun strided elements, their loads issued together
+    const long stride = long(gridDim.x) * 256;
+    for (long k0 = long(blockIdx.x) * 256 + threadIdx.x; k0 < n; k0 += stride * kRun) {
+      V xs[kRun], as[kRun];
+#pragma unroll
+      for (int t = 0; t < kRun; ++t) {
+        const long k = k0 + stride * t;
+        if (k < n) {
+          xs[t] = v[k];
+          as[t] = q[k];
+        }
       }
+      float fr = 0.f;
+#pragma unroll
+      for (int t = 0; t < kRun; ++t) {
+        const long k = k0 + stride * t;
+        if (k < n) {
+          const V a = VecOf<V>::make(as[t].x - (hx * xs[t].x - hy * xs[t].y), as[t].y - (hx * xs[t].y + hy * xs[t].x));
+          q[k] = a;
+          fr += a.x * a.x + a.y * a.y;
+        }
+      }
+      ar += fr;
     }
   }
-  ar += double(fr);
   sr[threadIdx.x] = ar;
   __syncthreads();
   for (int st = 128; st > 0; st >>= 1) {
@@ -1218,10 +1259,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       });
     }
     const long M = 24 * P->nwp, N = 3 * ni;
-    if (P->path == EPSP_PATH_GEMM_BF16)
-      P->d_Df.alloc(ctx, size_t(M * N));
-    else
-      P->d_D.alloc(ctx, size_t(M * N));
+    if (P->path != EPSP_PATH_GEMM_BF16) P->d_D.alloc(ctx, size_t(M * N));  // the tensor-core path keeps D as split-K parts
     if (P->path == EPSP_PATH_GEMM_FP64) {
       P->d_Af.alloc(ctx, size_t(M * P->Kx));
     } else {
@@ -1466,7 +1504,7 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ, const double2*
   EPSP_LAUNCHED(ctx);
   gemm_f64(ctx, false, int(nw), int(8 * N), int(nw), 1.0, P->d_KK.p, nw, P->d_Y.p, nw, 0.0, P->d_KY.p, nw);
   finish_gemm_kernel<double><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), 1), 256, 0, s>>>(
-      P->d_D.p, M, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
+      P->d_D.p, M, 1, 0, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
   EPSP_LAUNCHED(ctx);
 }
 
@@ -1488,18 +1526,21 @@ static void apply_L(LadderPlan* P, const float2* J, float2* LJ, const float2* X 
   prof_end(ctx, px);
   int sp = tc_gemm_launch_with(ctx, P->opA, P->opG, P->bn, P->splits, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N,
                                P->d_err.p, "tc_ladder");
-  sum_parts_kernel<<<div_up(size_t(M * N), 256), 256, 0, s>>>(P->d_part.p, M * N, sp, M * N, P->d_Df.p);
+  // D stays as the contraction's split-K partials; y_split and finish add them as they read
+  long pl = prof_begin(ctx, "lsum");
+  y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), 1), 256, 0, s>>>(P->d_part.p, M, sp, M * N, int(nw), int(nwp),
+                                                                                  N, P->Kp2, P->d_Yh.p, P->d_Yl.p);
   EPSP_LAUNCHED(ctx);
-  y_split_kernel<<<dim3(div_up(size_t(8 * N * P->Kp2), 256), 1), 256, 0, s>>>(P->d_Df.p, M, int(nw), int(nwp), N, P->Kp2,
-                                                                             P->d_Yh.p, P->d_Yl.p);
-  EPSP_LAUNCHED(ctx);
+  prof_end(ctx, pl);
   int sp2 = tc_gemm_launch(ctx, P->opKK, P->opY, int(nw), int(8 * N), int(nw), P->d_part2.p, nw, nw * 8 * N, 16, P->d_err.p,
                            "tc_ladder_kk");
+  pl = prof_begin(ctx, "lfinish");
   sum_parts_kernel<<<div_up(size_t(nw * 8 * N), 256), 256, 0, s>>>(P->d_part2.p, nw * 8 * N, sp2, nw * 8 * N, P->d_KYf.p);
   EPSP_LAUNCHED(ctx);
   finish_gemm_kernel<float><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), 1), 256, 0, s>>>(
-      P->d_Df.p, M, P->d_KYf.p, P->d_Gmf.p, P->d_Gpf.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
+      P->d_part.p, M, sp, M * N, P->d_KYf.p, P->d_Gmf.p, P->d_Gpf.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
   EPSP_LAUNCHED(ctx);
+  prof_end(ctx, pl);
 }
 
 static void check_tc_err(LadderPlan* P) {
@@ -1524,34 +1565,41 @@ static void dot_dev(LadderPlan* P, const V* u, const V* v, long n, DBuf<double2>
   EPSP_LAUNCHED(ctx);
 }
 
+// conductivity_from_vertex (src/ladder_kernel.jl:116-122), in two halves: the device sums Y[b, i] of
+// a vertex into Ydev (cond_launch, asynchronous), and σ from Y on the host (sigma_from_Y).
 template <class V>
-static double nrm_host(LadderPlan* P, const V* u, long n, DBuf<double2>& part, DBuf<double2>& scal) {
-  dot_dev(P, u, u, n, part, scal.p);
-  double2 r;
-  scal.download(&r, 1, P->ctx->stream);
-  EPSP_CUDA(cudaStreamSynchronize(P->ctx->stream));
-  return std::sqrt(r.x);
+static void cond_launch(LadderPlan* P, const V* J, double2* Ydev) {
+  Ctx* ctx = P->ctx;
+  cond_sum_kernel<V><<<dim3(unsigned(3 * P->ni), 1), 256, 0, ctx->stream>>>(J, P->d_Ww.p, int(P->nw), int(P->ni), Ydev);
+  EPSP_LAUNCHED(ctx);
 }
 
-// conductivity_from_vertex (src/ladder_kernel.jl:116-122) of the device vertex J.
-template <class V>
-static void conductivity_dev(LadderPlan* P, const V* J, double Om, double T, DBuf<double2>& Ybuf, double* sigma) {
-  Ctx* ctx = P->ctx;
-  cudaStream_t s = ctx->stream;
-  const long nw = P->nw, ni = P->ni;
-  cond_sum_kernel<V><<<dim3(unsigned(3 * ni), 1), 256, 0, s>>>(J, P->d_Ww.p, int(nw), int(ni), Ybuf.p);
-  EPSP_LAUNCHED(ctx);
-  std::vector<double2> Y(size_t(3 * ni));
-  Ybuf.download(Y.data(), size_t(3 * ni), s);
-  EPSP_CUDA(cudaStreamSynchronize(s));
+static void sigma_from_Y(LadderPlan* P, const cplx* Y, double Om, double T, double* sigma) {
+  const long ni = P->ni;
   cplx F = Om == 0 ? cplx(0, 1) / (4 * T)
                    : -1.0 / (cplx(0, 2) * Om * (1 + 2 * (T > 1.4901161193847656e-08 ? 1.0 / std::expm1(Om / T) : 0.0)));
   for (int a = 0; a < 3; ++a)
     for (int b = 0; b < 3; ++b) {
       cplx S = 0;
-      for (long i = 0; i < ni; ++i) S += (P->v_h[size_t(a + 3 * i)] * P->w_i_h[size_t(i)]) * cplx(Y[size_t(b + 3 * i)].x, Y[size_t(b + 3 * i)].y);
+      for (long i = 0; i < ni; ++i) S += (P->v_h[size_t(a + 3 * i)] * P->w_i_h[size_t(i)]) * Y[size_t(b + 3 * i)];
       sigma[a + 3 * b] = (F / (2 * 3.14159265358979323846 * cplx(0, 1)) * S).real();
     }
+}
+
+// Both halves with a synchronisation in between.
+template <class V>
+static void conductivity_dev(LadderPlan* P, const V* J, double Om, double T, DBuf<double2>& Ybuf, double* sigma) {
+  cudaStream_t s = P->ctx->stream;
+  cond_launch(P, J, Ybuf.p);
+  std::vector<cplx> Y(size_t(3 * P->ni));
+  EPSP_CUDA(cudaMemcpyAsync(Y.data(), Ybuf.p, Y.size() * sizeof(cplx), cudaMemcpyDeviceToHost, s));
+  EPSP_CUDA(cudaStreamSynchronize(s));
+  sigma_from_Y(P, Y.data(), Om, T, sigma);
+}
+
+// c[0] = 1/sqrt(Re x[0]) (the scale of the first Krylov vector, without a round trip to the host).
+__global__ void rsqrt_coef_kernel(const double2* __restrict__ x, double2* __restrict__ c) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) c[0] = make_double2(1.0 / sqrt(x[0].x), 0.0);
 }
 
 // A device vertex copied into host FP64 memory (FP32 vertices widened on the way).
@@ -1594,14 +1642,12 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
   const long n = nw * 24 * ni;
   const unsigned eb = div_up(size_t(n), 256);
   DBuf<double2>& part = P->w_part;
-  DBuf<double2>& scal = P->w_scal;
   DBuf<double2>& Hdev = P->w_H;
   DBuf<double2>& Ybuf = P->w_Y;
   for (auto* b : {&J0, &J, &LJ, &W}) ensure(*b, ctx, size_t(n));
   ensure(part, ctx, size_t(kDotBlocks));
-  ensure(scal, ctx, 1);
-  ensure(Hdev, ctx, size_t(maxiter + 2));
-  ensure(Ybuf, ctx, size_t(3 * ni));
+  ensure(Hdev, ctx, size_t(maxiter + 5));  // Hessenberg column, wait flag, ‖J0‖², β², 1/β
+  ensure(Ybuf, ctx, size_t(3 * ni * (maxiter + 2)));  // σ sums of J0, x0 and each Krylov vector
   std::vector<DBuf<V>>& Vk = Vb;
   const double btol = std::pow(std::numeric_limits<double>::epsilon(), 0.75);
   for (int64_t iT = 0; iT < nT; ++iT) {
@@ -1612,6 +1658,7 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
     for (int64_t iO = 0; iO < nO; ++iO) {
       const double Om = Omegas[iO];
       const int64_t idx = iO + nO * iT;
+      long plp = prof_begin(ctx, "lprep");
       set_propagators(P, mu[iT], T, Om);
       const dim3 ab(div_up(size_t(nw), 256), unsigned(6 * ni), 4);
       if constexpr (std::is_same_v<V, float2>)
@@ -1619,7 +1666,6 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
       else
         attach_bare_kernel<double2><<<ab, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
       EPSP_LAUNCHED(ctx);
-      conductivity_dev(P, J0.p, Om, T, Ybuf, sb + 9 * idx);
       auto op = [&](const V* x, V* y) {  // y = x - L(x)
         if (P->path == EPSP_PATH_DIRECT_FP64) {
           apply_L(P, x, LJ.p);
@@ -1631,117 +1677,156 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
       };
       if (solver == EPSP_SOLVER_GMRES) {
         // Krylov.gmres(A, b[, x0]; atol = rtol ‖J0‖, rtol = 0, itmax = maxiter), restart = false,
-        // MGS, Givens (src/ladder.jl:340-353).
+        // MGS, Givens (src/ladder.jl:340-353). The host reads the device once per iteration: the
+        // first operator application starts before ‖J0‖ and β are known (the first Krylov vector
+        // is scaled on the device), and they come back with the first Hessenberg column. σ of the
+        // solution is Σ y_i σ(v_i) (+ σ(x0)) from the per-vector sums, unless the vertex itself is
+        // wanted (stored, or the next Ω's start), when x is formed and summed.
         const bool warm = iO > 0;
-        const double nJ0 = nrm_host(P, J0.p, n, part, scal);
-        const double atol = rtol * nJ0;
-        std::vector<double> res;
-        // r0 = b - A x0 (warm) or b
-        if (warm) {
+        const bool needJ = J_out != nullptr || iO + 1 < nO;
+        const long ny = 3 * ni;
+        const size_t hN0 = size_t(maxiter + 2), hB2 = size_t(maxiter + 3), hC = size_t(maxiter + 4);
+        cond_launch(P, J0.p, Ybuf.p);  // slot 0: σ_bubble
+        dot_dev(P, J0.p, J0.p, n, part, Hdev.p + hN0);
+        const V* r0 = J0.p;  // a cold start's r0 is J0 itself
+        if (warm) {          // r0 = b - A x0
+          if (!needJ) cond_launch(P, J.p, Ybuf.p + ny);  // slot 1: σ(x0)
           op(J.p, W.p);
           axpby_kernel<V><<<eb, 256, 0, s>>>(make_double2(1, 0), nullptr, J0.p, make_double2(-1, 0), nullptr, W.p, n, nullptr);
           EPSP_LAUNCHED(ctx);
+          dot_dev(P, W.p, W.p, n, part, Hdev.p + hB2);
+          r0 = W.p;
         }
-        const V* r0 = warm ? W.p : J0.p;  // a cold start's r0 is J0 itself
-        const double beta = warm ? nrm_host(P, W.p, n, part, scal) : nJ0;
-        double rNorm = beta;
-        res.push_back(beta);
-        bool solved = rNorm <= atol, breakdown = false;
-        int inner = 0;
+        rsqrt_coef_kernel<<<1, 32, 0, s>>>(Hdev.p + (warm ? hB2 : hN0), Hdev.p + hC);
+        EPSP_LAUNCHED(ctx);
+        if (Vk.empty()) Vk.emplace_back();
+        if (Vk[0].n != size_t(n)) Vk[0].alloc(ctx, size_t(n));
+        scale_kernel<V><<<eb, 256, 0, s>>>(make_double2(0, 0), Hdev.p + hC, r0, Vk[0].p, n, nullptr);
+        EPSP_LAUNCHED(ctx);
+        prof_end(ctx, plp);
+        plp = -1;
+        double nJ0 = 0, atol = 0, beta = 0, rNorm = 0;
+        std::vector<double> res;
+        bool solved = false, breakdown = false, tired = false;
+        int inner = 0, nr = 0;
         std::vector<cplx> R, sv, z;
         std::vector<double> cv;
-        if (beta == 0) solved = true;
-        if (!solved) {
-          if (Vk.empty()) Vk.emplace_back();
-          if (Vk[0].n != size_t(n)) Vk[0].alloc(ctx, size_t(n));
-          scale_kernel<V><<<eb, 256, 0, s>>>(make_double2(1.0 / rNorm, 0), nullptr, r0, Vk[0].p, n, nullptr);
-          EPSP_LAUNCHED(ctx);
-          z.push_back(beta);
-          int nr = 0;
-          bool tired = false;
-          while (!(solved || tired || breakdown)) {
-            ++inner;
-            op(Vk[size_t(inner - 1)].p, W.p);  // q = A v_k
-            for (int i = 0; i < inner; ++i) {
-              dot_dev(P, Vk[size_t(i)].p, W.p, n, part, Hdev.p + i);
-              if (i + 1 < inner) {
-                axpy_dev_kernel<V><<<eb, 256, 0, s>>>(W.p, Vk[size_t(i)].p, Hdev.p + i, n, nullptr);
-                EPSP_LAUNCHED(ctx);
-              } else {  // the last projection and the norm of what remains, in one pass
-                axpy_norm_kernel<V><<<kDotBlocks, 256, 0, s>>>(W.p, Vk[size_t(i)].p, Hdev.p + i, n, part.p);
-                EPSP_LAUNCHED(ctx);
-                dot_final_kernel<<<1, 256, 0, s>>>(part.p, kDotBlocks, nullptr, Hdev.p + inner);
-                EPSP_LAUNCHED(ctx);
-              }
-            }
-            const bool tc = P->path == EPSP_PATH_GEMM_BF16;
-            if (tc)  // the tensor-core wait flag rides along with the Hessenberg column
-              EPSP_CUDA(cudaMemcpyAsync(Hdev.p + inner + 1, P->d_err.p, sizeof(int), cudaMemcpyDeviceToDevice, s));
-            std::vector<double2> hcol(size_t(inner + 2));
-            Hdev.download(hcol.data(), size_t(inner + (tc ? 2 : 1)), s);
-            EPSP_CUDA(cudaStreamSynchronize(s));
-            if (tc) {
-              int e = 0;
-              std::memcpy(&e, &hcol[size_t(inner + 1)], sizeof(int));
-              if (e) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
-            }
-            for (int i = 0; i < inner; ++i) R.push_back(cplx(hcol[size_t(i)].x, hcol[size_t(i)].y));
-            const double Hbis = std::sqrt(hcol[size_t(inner)].x);
-            for (int i = 0; i < inner - 1; ++i) {
-              cplx Rt = cv[size_t(i)] * R[size_t(nr + i)] + sv[size_t(i)] * R[size_t(nr + i + 1)];
-              R[size_t(nr + i + 1)] = std::conj(sv[size_t(i)]) * R[size_t(nr + i)] - cv[size_t(i)] * R[size_t(nr + i + 1)];
-              R[size_t(nr + i)] = Rt;
-            }
-            cplx a = R[size_t(nr + inner - 1)];
-            double abs_a = std::abs(a), cc;
-            cplx ss, rho;
-            if (Hbis == 0) {
-              cc = 1;
-              ss = 0;
-              rho = a;
-            } else if (abs_a == 0) {
-              cc = 0;
-              ss = 1;
-              rho = Hbis;
-            } else {
-              double rr = std::hypot(abs_a, Hbis);
-              cplx psi = a / abs_a;
-              cc = abs_a / rr;
-              ss = psi * (Hbis / rr);
-              rho = psi * rr;
-            }
-            cv.push_back(cc);
-            sv.push_back(ss);
-            R[size_t(nr + inner - 1)] = rho;
-            cplx zeta = std::conj(ss) * z[size_t(inner - 1)];
-            z[size_t(inner - 1)] = cc * z[size_t(inner - 1)];
-            rNorm = std::abs(zeta);
-            res.push_back(rNorm);
-            nr += inner;
-            solved = rNorm <= atol || rNorm + 1.0 <= 1.0;
-            breakdown = Hbis <= btol;
-            tired = inner >= maxiter;
-            if (!(solved || tired || breakdown)) {
-              if (Vk.size() < size_t(inner + 1)) Vk.emplace_back();
-              if (Vk[size_t(inner)].n != size_t(n)) Vk[size_t(inner)].alloc(ctx, size_t(n));
-              scale_kernel<V><<<eb, 256, 0, s>>>(make_double2(1.0 / Hbis, 0), nullptr, W.p, Vk[size_t(inner)].p, n, nullptr);
+        std::vector<cplx> Yb(static_cast<size_t>(ny)), Yx0(static_cast<size_t>(ny), cplx(0, 0));
+        std::vector<std::vector<cplx>> Yv;
+        const bool tc = P->path == EPSP_PATH_GEMM_BF16;
+        std::vector<double2> hcol(size_t(maxiter + 5));
+        while (!(solved || tired || breakdown)) {
+          ++inner;
+          op(Vk[size_t(inner - 1)].p, W.p);  // q = A v_k
+          if (!needJ) cond_launch(P, Vk[size_t(inner - 1)].p, Ybuf.p + (2 + (inner - 1)) * ny);
+          long pbl = prof_begin(ctx, "lblas");
+          for (int i = 0; i < inner; ++i) {
+            dot_dev(P, Vk[size_t(i)].p, W.p, n, part, Hdev.p + i);
+            if (i + 1 < inner) {
+              axpy_dev_kernel<V><<<eb, 256, 0, s>>>(W.p, Vk[size_t(i)].p, Hdev.p + i, n, nullptr);
               EPSP_LAUNCHED(ctx);
-              z.push_back(zeta);
+            } else {  // the last projection and the norm of what remains, in one pass
+              axpy_norm_kernel<V><<<kDotBlocks, 256, 0, s>>>(W.p, Vk[size_t(i)].p, Hdev.p + i, n, part.p);
+              EPSP_LAUNCHED(ctx);
+              dot_final_kernel<<<1, 256, 0, s>>>(part.p, kDotBlocks, nullptr, Hdev.p + inner);
+              EPSP_LAUNCHED(ctx);
             }
           }
-          std::vector<cplx> y = z;
-          for (int i = inner - 1; i >= 0; --i) {
-            int pos = nr + i - inner;
-            for (int jj = inner - 1; jj >= i + 1; --jj) {
-              y[size_t(i)] -= R[size_t(pos)] * y[size_t(jj)];
-              pos -= jj;
-            }
-            if (std::abs(R[size_t(pos)]) <= btol)
-              y[size_t(i)] = 0;
-            else
-              y[size_t(i)] /= R[size_t(pos)];
+          if (tc)  // the tensor-core wait flag rides along with the Hessenberg column
+            EPSP_CUDA(cudaMemcpyAsync(Hdev.p + maxiter + 1, P->d_err.p, sizeof(int), cudaMemcpyDeviceToDevice, s));
+          Hdev.download(hcol.data(), hcol.size(), s);
+          if (inner == 1) {
+            EPSP_CUDA(cudaMemcpyAsync(Yb.data(), Ybuf.p, size_t(ny) * sizeof(cplx), cudaMemcpyDeviceToHost, s));
+            if (warm && !needJ)
+              EPSP_CUDA(cudaMemcpyAsync(Yx0.data(), Ybuf.p + ny, size_t(ny) * sizeof(cplx), cudaMemcpyDeviceToHost, s));
           }
+          if (!needJ) {
+            Yv.emplace_back(static_cast<size_t>(ny));
+            EPSP_CUDA(cudaMemcpyAsync(Yv.back().data(), Ybuf.p + (2 + (inner - 1)) * ny, size_t(ny) * sizeof(cplx),
+                                      cudaMemcpyDeviceToHost, s));
+          }
+          prof_end(ctx, pbl);
+          EPSP_CUDA(cudaStreamSynchronize(s));
+          if (tc) {
+            int e = 0;
+            std::memcpy(&e, &hcol[size_t(maxiter + 1)], sizeof(int));
+            if (e) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+          }
+          if (inner == 1) {
+            nJ0 = std::sqrt(hcol[hN0].x);
+            atol = rtol * nJ0;
+            beta = warm ? std::sqrt(hcol[hB2].x) : nJ0;
+            rNorm = beta;
+            res.push_back(beta);
+            if (beta <= atol || beta == 0) {  // solved at x0: the speculative first step is dropped
+              solved = true;
+              inner = 0;
+              Yv.clear();
+              break;
+            }
+            z.push_back(beta);
+          }
+          for (int i = 0; i < inner; ++i) R.push_back(cplx(hcol[size_t(i)].x, hcol[size_t(i)].y));
+          const double Hbis = std::sqrt(hcol[size_t(inner)].x);
+          for (int i = 0; i < inner - 1; ++i) {
+            cplx Rt = cv[size_t(i)] * R[size_t(nr + i)] + sv[size_t(i)] * R[size_t(nr + i + 1)];
+            R[size_t(nr + i + 1)] = std::conj(sv[size_t(i)]) * R[size_t(nr + i)] - cv[size_t(i)] * R[size_t(nr + i + 1)];
+            R[size_t(nr + i)] = Rt;
+          }
+          cplx a = R[size_t(nr + inner - 1)];
+          double abs_a = std::abs(a), cc;
+          cplx ss, rho;
+          if (Hbis == 0) {
+            cc = 1;
+            ss = 0;
+            rho = a;
+          } else if (abs_a == 0) {
+            cc = 0;
+            ss = 1;
+            rho = Hbis;
+          } else {
+            double rr = std::hypot(abs_a, Hbis);
+            cplx psi = a / abs_a;
+            cc = abs_a / rr;
+            ss = psi * (Hbis / rr);
+            rho = psi * rr;
+          }
+          cv.push_back(cc);
+          sv.push_back(ss);
+          R[size_t(nr + inner - 1)] = rho;
+          cplx zeta = std::conj(ss) * z[size_t(inner - 1)];
+          z[size_t(inner - 1)] = cc * z[size_t(inner - 1)];
+          rNorm = std::abs(zeta);
+          res.push_back(rNorm);
+          nr += inner;
+          solved = rNorm <= atol || rNorm + 1.0 <= 1.0;
+          breakdown = Hbis <= btol;
+          tired = inner >= maxiter;
+          if (!(solved || tired || breakdown)) {
+            if (Vk.size() < size_t(inner + 1)) Vk.emplace_back();
+            if (Vk[size_t(inner)].n != size_t(n)) Vk[size_t(inner)].alloc(ctx, size_t(n));
+            scale_kernel<V><<<eb, 256, 0, s>>>(make_double2(1.0 / Hbis, 0), nullptr, W.p, Vk[size_t(inner)].p, n, nullptr);
+            EPSP_LAUNCHED(ctx);
+            z.push_back(zeta);
+          }
+        }
+        std::vector<cplx> y = z;
+        for (int i = inner - 1; i >= 0; --i) {
+          int pos = nr + i - inner;
+          for (int jj = inner - 1; jj >= i + 1; --jj) {
+            y[size_t(i)] -= R[size_t(pos)] * y[size_t(jj)];
+            pos -= jj;
+          }
+          if (std::abs(R[size_t(pos)]) <= btol)
+            y[size_t(i)] = 0;
+          else
+            y[size_t(i)] /= R[size_t(pos)];
+        }
+        sigma_from_Y(P, Yb.data(), Om, T, sb + 9 * idx);
+        if (needJ) {
           // x = x0 + V y (x0 = J for a warm start, else 0)
+          long psl = prof_begin(ctx, "lsol");
+          if (inner == 0 && !warm) J.zero(s);
           for (int i = 0; i < inner; ++i) {
             const double2 yi = make_double2(y[size_t(i)].real(), y[size_t(i)].imag());
             if (i == 0 && !warm)
@@ -1750,8 +1835,14 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
               axpby_kernel<V><<<eb, 256, 0, s>>>(yi, nullptr, Vk[size_t(i)].p, make_double2(1, 0), nullptr, J.p, n, nullptr);
             EPSP_LAUNCHED(ctx);
           }
-        } else if (!warm) {
-          J.zero(s);
+          prof_end(ctx, psl);
+          conductivity_dev(P, J.p, Om, T, Ybuf, sl + 9 * idx);
+          if (J_out) vertex_to_host(P, J.p, n, J_out + 2 * size_t(n) * size_t(idx));
+        } else {
+          std::vector<cplx> Yx = Yx0;  // σ is linear in the vertex
+          for (int i = 0; i < inner; ++i)
+            for (long k = 0; k < ny; ++k) Yx[size_t(k)] += y[size_t(i)] * Yv[size_t(i)][size_t(k)];
+          sigma_from_Y(P, Yx.data(), Om, T, sl + 9 * idx);
         }
         conv[idx] = solved ? 1 : 0;
         niter[idx] = inner;
@@ -1763,6 +1854,9 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
         if (hist && hist->nsigma) hist->nsigma[idx] = 0;
       } else {
         // J ← J0 + L(J) from J0 until the relative change of σ is below rtol (src/ladder.jl:354-369)
+        prof_end(ctx, plp);
+        plp = -1;
+        conductivity_dev(P, J0.p, Om, T, Ybuf, sb + 9 * idx);
         EPSP_CUDA(cudaMemcpyAsync(J.p, J0.p, size_t(n) * sizeof(V), cudaMemcpyDeviceToDevice, s));
         double sprev[9] = {}, scur[9];
         conv[idx] = 0;
@@ -1789,9 +1883,9 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
         }
         if (hist && hist->nsigma) hist->nsigma[idx] = ns_;
         if (hist && hist->nnorms) hist->nnorms[idx] = 0;
+        conductivity_dev(P, J.p, Om, T, Ybuf, sl + 9 * idx);
+        if (J_out) vertex_to_host(P, J.p, n, J_out + 2 * size_t(n) * size_t(idx));
       }
-      conductivity_dev(P, J.p, Om, T, Ybuf, sl + 9 * idx);
-      if (J_out) vertex_to_host(P, J.p, n, J_out + 2 * size_t(n) * size_t(idx));
     }
   }
 }
@@ -1844,7 +1938,7 @@ struct LadderBatch {
   int bk = 0;  // K block of the A maps
   DBuf<__nv_bfloat16> Ah, Al, Yh, Yl;
   DBuf<float> part, part2, nnu;
-  DBuf<float> D, KY;
+  DBuf<float> KY;
   DBuf<float2> Gm, Gp, J0, J, LJ, W;
   DBuf<double2> dpart, H, coef_a, coef_b;
   std::vector<DBuf<float2>> V;
@@ -1875,7 +1969,6 @@ static void batch_reserve(LadderPlan* P, LadderBatch& B, long R, int maxiter) {
   B.part.alloc(ctx, p1);
   B.part2.alloc(ctx, p2);
   B.nnu.alloc(ctx, size_t(16 * R));
-  B.D.alloc(ctx, size_t(R * M * N));
   B.KY.alloc(ctx, size_t(R * nw * 8 * N));
   B.Gm.alloc(ctx, size_t(R * 4 * nw * ni));
   B.Gp.alloc(ctx, size_t(R * 4 * nw * ni));
@@ -1912,10 +2005,8 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const float2* X, int nA
   prof_end(ctx, px);
   int sp = tc_gemm_launch_with(ctx, B.opA, P->opG, P->bn, 0, int(Mt), int(N), int(P->Kx), B.part.p, Mt, Mt * N, P->d_err.p,
                                "tc_ladder");
-  sum_parts_kernel<<<div_up(size_t(Mt * N), 256), 256, 0, s>>>(B.part.p, Mt * N, sp, Mt * N, B.D.p);
-  EPSP_LAUNCHED(ctx);
-  y_split_kernel<<<dim3(div_up(size_t(8 * N * P->Kp2), 256), unsigned(nA)), 256, 0, s>>>(B.D.p, Mt, int(nw), int(nwp), N,
-                                                                                        P->Kp2, B.Yh.p, B.Yl.p);
+  y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), unsigned(nA)), 256, 0, s>>>(
+      B.part.p, Mt, sp, Mt * N, int(nw), int(nwp), N, P->Kp2, B.Yh.p, B.Yl.p);
   EPSP_LAUNCHED(ctx);
   const long N2 = 8 * N * nA;
   int sp2 = tc_gemm_launch(ctx, P->opKK, B.opY, int(nw), int(N2), int(nw), B.part2.p, nw, nw * N2, 16, P->d_err.p,
@@ -1923,7 +2014,7 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const float2* X, int nA
   sum_parts_kernel<<<div_up(size_t(nw * N2), 256), 256, 0, s>>>(B.part2.p, nw * N2, sp2, nw * N2, B.KY.p);
   EPSP_LAUNCHED(ctx);
   finish_gemm_kernel<float><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), unsigned(nA)), 256, 0, s>>>(
-      B.D.p, Mt, B.KY.p, B.Gm.p, B.Gp.p, B.rmap.p, int(nw), int(nwp), int(ni), LJ);
+      B.part.p, Mt, sp, Mt * N, B.KY.p, B.Gm.p, B.Gp.p, B.rmap.p, int(nw), int(nwp), int(ni), LJ);
   EPSP_LAUNCHED(ctx);
 }
 
