@@ -163,35 +163,45 @@ __device__ __forceinline__ double2 cinv_d(double c, double d) {
 // 1/(x - ε - Σ(x)), G^A, G^K = (G^R - G^A)(1 - 2f), combined into the four Keldysh components.
 // F32 (tensor-core path): the difference x - ε - Re Σ in FP64, the reciprocal and the occupation
 // in FP32 (FP64 division and exp would make the kernel compute-bound on the FP64 units).
+// The four Keldysh components at one point in FP32 (the tensor-core path's contour_g).
+__device__ __forceinline__ void contour_f32(const double2* __restrict__ col, int j, double t, double x, double eps,
+                                            double mu, double T, float2 (&g)[4]) {
+  const double2 lo = col[j], hi = col[j + 1];
+  const double sr = (1 - t) * lo.x + t * hi.x, si = (1 - t) * lo.y + t * hi.y;
+  const float c = float(x - eps - sr), d = float(-si);
+  float gr, gi;  // Smith's 1/(c + i d)
+  if (fabsf(d) <= fabsf(c)) {
+    const float r = d / c, tt = 1.f / (c + d * r);
+    gr = tt;
+    gi = -r * tt;
+  } else {
+    const float r = c / d, tt = 1.f / (d + c * r);
+    gr = r * tt;
+    gi = -tt;
+  }
+  const float Tf = float(T);
+  const float f = Tf > 1.4901161193847656e-08f ? 1.f / (expf(float(x - mu) / Tf) + 1.f)
+                                               : (x - mu > 0 ? 0.f : (x - mu < 0 ? 1.f : 0.5f));
+  const float fac = 1.f - 2.f * f;
+  // GR = (gr, gi), GA = (gr, -gi), GK = (GR - GA) fac = (0, 2 gi fac)
+  const float kk = 2.f * gi * fac;
+  g[0] = make_float2(gr, 0.5f * kk);                 // (GR + GA + GK) / 2
+  g[1] = make_float2(0.f, 0.5f * (2.f * gi + kk));   // (GR - GA + GK) / 2
+  g[2] = make_float2(0.f, 0.5f * (-2.f * gi + kk));  // (GA - GR + GK) / 2
+  g[3] = make_float2(-gr, 0.5f * kk);                // (GK - GR - GA) / 2
+}
+
 template <bool F32>
 __device__ __forceinline__ void contour_g(const double2* __restrict__ col, int j, double t, double x, double eps,
                                           double mu, double T, Vec2<std::conditional_t<F32, float, double>>* __restrict__ G,
                                           int w, int nw, int i) {
-  const double2 lo = col[j], hi = col[j + 1];
-  const double sr = (1 - t) * lo.x + t * hi.x, si = (1 - t) * lo.y + t * hi.y;
   if constexpr (F32) {
-    const float c = float(x - eps - sr), d = float(-si);
-    float gr, gi;  // Smith's 1/(c + i d)
-    if (fabsf(d) <= fabsf(c)) {
-      const float r = d / c, tt = 1.f / (c + d * r);
-      gr = tt;
-      gi = -r * tt;
-    } else {
-      const float r = c / d, tt = 1.f / (d + c * r);
-      gr = r * tt;
-      gi = -tt;
-    }
-    const float Tf = float(T);
-    const float f = Tf > 1.4901161193847656e-08f ? 1.f / (expf(float(x - mu) / Tf) + 1.f)
-                                                 : (x - mu > 0 ? 0.f : (x - mu < 0 ? 1.f : 0.5f));
-    const float fac = 1.f - 2.f * f;
-    // GR = (gr, gi), GA = (gr, -gi), GK = (GR - GA) fac = (0, 2 gi fac)
-    const float kk = 2.f * gi * fac;
-    G[w + long(nw) * (0 + 4 * i)] = make_float2(gr, 0.5f * kk);                  // (GR + GA + GK) / 2
-    G[w + long(nw) * (1 + 4 * i)] = make_float2(0.f, 0.5f * (2.f * gi + kk));    // (GR - GA + GK) / 2
-    G[w + long(nw) * (2 + 4 * i)] = make_float2(0.f, 0.5f * (-2.f * gi + kk));   // (GA - GR + GK) / 2
-    G[w + long(nw) * (3 + 4 * i)] = make_float2(-gr, 0.5f * kk);                 // (GK - GR - GA) / 2
+    float2 g[4];
+    contour_f32(col, j, t, x, eps, mu, T, g);
+    for (int c = 0; c < 4; ++c) G[w + long(nw) * (c + 4 * i)] = g[c];
   } else {
+    const double2 lo = col[j], hi = col[j + 1];
+    const double sr = (1 - t) * lo.x + t * hi.x, si = (1 - t) * lo.y + t * hi.y;
     double2 GR = cinv_d(x - eps - sr, -si);
     double2 GA = make_double2(GR.x, -GR.y);
     double fac = 1 - 2 * occ_fermion_d(x - mu, T);
@@ -281,6 +291,80 @@ __global__ void __launch_bounds__(256) cond_sum_kernel(const V* __restrict__ J_a
     __syncthreads();
   }
   if (threadIdx.x == 0) Y[b + 3 * i] = make_double2(sr[0], si[0]);
+}
+
+// The start of a tensor-core solve in one pass per outer state i (block i, threads over ω): the
+// propagators Gm, Gp (propagators_kernel<true>), the bare vertex J0 = Gm v Gp
+// (attach_bare_kernel<float2>), its σ sums Y[b, i] (cond_sum_kernel: the same per-thread order and
+// block tree) and the block partial of ‖J0‖² (FP32 per thread and ω, FP64 across).
+__global__ void __launch_bounds__(256) prep_vertex_f32_kernel(const double2* __restrict__ ST, const double* __restrict__ ws,
+                                                              int nw, const int32_t* __restrict__ jm,
+                                                              const double* __restrict__ tm, const int32_t* __restrict__ jp,
+                                                              const double* __restrict__ tp, const double* __restrict__ eps_i,
+                                                              double mu, double T, double Om, const double* __restrict__ v,
+                                                              const double* __restrict__ Ww, int ni, float2* __restrict__ Gm,
+                                                              float2* __restrict__ Gp, float2* __restrict__ J0,
+                                                              double2* __restrict__ Y, double2* __restrict__ part) {
+  __shared__ double sr[256], si[256];
+  const int i = blockIdx.x;
+  const double2* col = ST + long(nw) * i;
+  const double e = eps_i[i];
+  const float vc[3] = {float(v[3 * i]), float(v[3 * i + 1]), float(v[3 * i + 2])};
+  double yr[3] = {0, 0, 0}, yi[3] = {0, 0, 0}, nrm = 0;
+  for (int w = threadIdx.x; w < nw; w += 256) {
+    float2 gm[4], gp[4];
+    contour_f32(col, jm[w], tm[w], ws[w] - Om / 2, e, mu, T, gm);
+    contour_f32(col, jp[w], tp[w], ws[w] + Om / 2, e, mu, T, gp);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      Gm[w + long(nw) * (c + 4 * i)] = gm[c];
+      Gp[w + long(nw) * (c + 4 * i)] = gp[c];
+    }
+    float n2 = 0.f;
+    float2 j3[3];  // J0[ω, c12 = 3, b, c0 = 0], which Y adds to J0[ω, c12 = 0, b, c0 = 1]
+#pragma unroll
+    for (int c0 = 0; c0 < 2; ++c0)
+#pragma unroll
+      for (int cart = 0; cart < 3; ++cart)
+#pragma unroll
+        for (int c12 = 0; c12 < 4; ++c12) {
+          const int c1 = c12 % 2, c2 = c12 / 2;
+          const float2 a = gm[c1 + 2 * c0], b = gp[c0 + 2 * c2];
+          const Cx<float> av{a.x * vc[cart], a.y * vc[cart]}, bb{b.x, b.y};
+          const Cx<float> z = cxmul(av, bb);
+          J0[jidx(nw, w, c12, cart, c0, i)] = make_float2(z.x, z.y);
+          n2 += z.x * z.x + z.y * z.y;
+          if (c12 == 3 && c0 == 0) j3[cart] = make_float2(z.x, z.y);
+          if (c12 == 0 && c0 == 1) {  // as cond_sum_kernel: the two added in FP32, then weighted in FP64
+            yr[cart] += Ww[w] * double(j3[cart].x + z.x);
+            yi[cart] += Ww[w] * double(j3[cart].y + z.y);
+          }
+        }
+    nrm += double(n2);
+  }
+  auto block_sum = [&](double a, double b, double& ra, double& rb) {
+    sr[threadIdx.x] = a;
+    si[threadIdx.x] = b;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+      if (threadIdx.x < st) {
+        sr[threadIdx.x] += sr[threadIdx.x + st];
+        si[threadIdx.x] += si[threadIdx.x + st];
+      }
+      __syncthreads();
+    }
+    ra = sr[0];
+    rb = si[0];
+    __syncthreads();
+  };
+  for (int b = 0; b < 3; ++b) {
+    double ra, rb;
+    block_sum(yr[b], yi[b], ra, rb);
+    if (threadIdx.x == 0) Y[b + 3 * i] = make_double2(ra, rb);
+  }
+  double ra, rb;
+  block_sum(nrm, 0.0, ra, rb);
+  if (threadIdx.x == 0) part[i] = make_double2(ra, 0.0);
 }
 
 // ---- DIRECT_FP64: the reference's shift grid ----
@@ -1380,8 +1464,9 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
 // operator
 // ---------------------------------------------------------------------------------------------
 
-// Propagators of (T, μ, Ω) from Σ_T on the device (d_ST).
-static void set_propagators(LadderPlan* P, double mu, double T, double Om) {
+// Propagators of (T, μ, Ω) from Σ_T on the device (d_ST); with launch = false only the
+// interpolation tables of Ω (for a kernel that forms the propagators itself).
+static void set_propagators(LadderPlan* P, double mu, double T, double Om, bool launch = true) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
   const long nw = P->nw, ni = P->ni;
@@ -1401,6 +1486,10 @@ static void set_propagators(LadderPlan* P, double mu, double T, double Om) {
     P->d_tp.upload(P->h_tp.data(), size_t(nw), s);
     P->tab_Om = Om;
   }
+  P->cur_T = T;
+  P->cur_mu = mu;
+  P->cur_Om = Om;
+  if (!launch) return;
   const dim3 grid(div_up(size_t(nw), 128), unsigned(ni));
   if (P->path == EPSP_PATH_GEMM_BF16)
     propagators_kernel<true><<<grid, 128, 0, s>>>(P->d_ST.p, P->d_ws.p, int(nw), P->d_jm.p, P->d_tm.p, P->d_jp.p, P->d_tp.p,
@@ -1409,9 +1498,6 @@ static void set_propagators(LadderPlan* P, double mu, double T, double Om) {
     propagators_kernel<false><<<grid, 128, 0, s>>>(P->d_ST.p, P->d_ws.p, int(nw), P->d_jm.p, P->d_tm.p, P->d_jp.p,
                                                     P->d_tp.p, P->d_eps_i.p, mu, T, Om, P->d_Gm.p, P->d_Gp.p, int(ni));
   EPSP_LAUNCHED(ctx);
-  P->cur_T = T;
-  P->cur_mu = mu;
-  P->cur_Om = Om;
 }
 
 // B̃ of temperature T for every chunk (the B build and star sum of src/ladder.jl:257-281).
@@ -1645,7 +1731,7 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
   DBuf<double2>& Hdev = P->w_H;
   DBuf<double2>& Ybuf = P->w_Y;
   for (auto* b : {&J0, &J, &LJ, &W}) ensure(*b, ctx, size_t(n));
-  ensure(part, ctx, size_t(kDotBlocks));
+  ensure(part, ctx, size_t(std::max<long>(kDotBlocks, ni)));
   ensure(Hdev, ctx, size_t(maxiter + 5));  // Hessenberg column, wait flag, ‖J0‖², β², 1/β
   ensure(Ybuf, ctx, size_t(3 * ni * (maxiter + 2)));  // σ sums of J0, x0 and each Krylov vector
   std::vector<DBuf<V>>& Vk = Vb;
@@ -1659,13 +1745,22 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
       const double Om = Omegas[iO];
       const int64_t idx = iO + nO * iT;
       long plp = prof_begin(ctx, "lprep");
-      set_propagators(P, mu[iT], T, Om);
-      const dim3 ab(div_up(size_t(nw), 256), unsigned(6 * ni), 4);
-      if constexpr (std::is_same_v<V, float2>)
-        attach_bare_kernel<float2><<<ab, 256, 0, s>>>(P->d_Gmf.p, P->d_Gpf.p, P->d_v.p, int(nw), int(ni), J0.p);
-      else
+      const size_t hN0 = size_t(maxiter + 2), hB2 = size_t(maxiter + 3), hC = size_t(maxiter + 4);
+      if constexpr (std::is_same_v<V, float2>) {
+        // propagators, J0, its σ sums (slot 0) and ‖J0‖² in one pass
+        set_propagators(P, mu[iT], T, Om, false);
+        prep_vertex_f32_kernel<<<unsigned(ni), 256, 0, s>>>(P->d_ST.p, P->d_ws.p, int(nw), P->d_jm.p, P->d_tm.p, P->d_jp.p,
+                                                            P->d_tp.p, P->d_eps_i.p, mu[iT], T, Om, P->d_v.p, P->d_Ww.p,
+                                                            int(ni), P->d_Gmf.p, P->d_Gpf.p, J0.p, Ybuf.p, part.p);
+        EPSP_LAUNCHED(ctx);
+        dot_final_kernel<<<1, 256, 0, s>>>(part.p, int(ni), nullptr, Hdev.p + hN0);
+        EPSP_LAUNCHED(ctx);
+      } else {
+        set_propagators(P, mu[iT], T, Om);
+        const dim3 ab(div_up(size_t(nw), 256), unsigned(6 * ni), 4);
         attach_bare_kernel<double2><<<ab, 256, 0, s>>>(P->d_Gm.p, P->d_Gp.p, P->d_v.p, int(nw), int(ni), J0.p);
-      EPSP_LAUNCHED(ctx);
+        EPSP_LAUNCHED(ctx);
+      }
       auto op = [&](const V* x, V* y) {  // y = x - L(x)
         if (P->path == EPSP_PATH_DIRECT_FP64) {
           apply_L(P, x, LJ.p);
@@ -1685,9 +1780,10 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
         const bool warm = iO > 0;
         const bool needJ = J_out != nullptr || iO + 1 < nO;
         const long ny = 3 * ni;
-        const size_t hN0 = size_t(maxiter + 2), hB2 = size_t(maxiter + 3), hC = size_t(maxiter + 4);
-        cond_launch(P, J0.p, Ybuf.p);  // slot 0: σ_bubble
-        dot_dev(P, J0.p, J0.p, n, part, Hdev.p + hN0);
+        if constexpr (!std::is_same_v<V, float2>) {
+          cond_launch(P, J0.p, Ybuf.p);  // slot 0: σ_bubble
+          dot_dev(P, J0.p, J0.p, n, part, Hdev.p + hN0);
+        }
         const V* r0 = J0.p;  // a cold start's r0 is J0 itself
         if (warm) {          // r0 = b - A x0
           if (!needJ) cond_launch(P, J.p, Ybuf.p + ny);  // slot 1: σ(x0)

@@ -273,10 +273,15 @@ __global__ void finalize_kk_batch_kernel(const float* __restrict__ part, long sl
 
 static long pad64(long x) { return (x + 63) / 64 * 64; }
 
+// K block of the three-part products' operand maps (64: two 96 KB pipeline stages; 32: four of
+// 48 KB, measured no faster on these short products).
+constexpr int kScgd0Bk = 64;
+
 static TcOperand operand(DBuf<__nv_bfloat16>* parts, long rows, long cols, long ld, int box_rows) {
   TcOperand op;
   op.ns = kNs;
-  for (int p = 0; p < kNs; ++p) op.m[p] = make_tmap_bf16(parts[p].p, rows, cols, ld, box_rows);
+  op.bk = kScgd0Bk;
+  for (int p = 0; p < kNs; ++p) op.m[p] = make_tmap_bf16(parts[p].p, rows, cols, ld, box_rows, kScgd0Bk);
   return op;
 }
 

@@ -42,13 +42,36 @@ void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* b
   const int BN = (ns == 2 && N > 128) ? 256 : 128;
   const int tiles = ((M + kTcBM - 1) / kTcBM) * ((N + BN - 1) / BN);
   const int kblocks = (K + kTcBK - 1) / kTcBK;
-  int sp = std::max(1, (ctx->sm_count + tiles - 1) / tiles);
-  if (kb_cap > 0) sp = std::max(sp, (kblocks + kb_cap - 1) / kb_cap);
-  sp = std::min({sp, std::max(1, max_splits), std::max(1, kblocks)});
-  const int per = (kblocks + sp - 1) / sp;
-  sp = std::max(1, (kblocks + per - 1) / per);
+  const int cap = std::min(std::max(1, max_splits), std::max(1, kblocks));
+  if (kb_cap <= 0) {  // fill the SMs once; no accumulation bound
+    int sp = std::min(std::max(1, (ctx->sm_count + tiles - 1) / tiles), cap);
+    const int per = (kblocks + sp - 1) / sp;
+    *bn = BN;
+    *splits = std::max(1, (kblocks + per - 1) / per);
+    return;
+  }
+  int lo = std::min(std::max(1, (kblocks + kb_cap - 1) / kb_cap), cap);
+  // With an accumulation bound (the scGD0 products): one CTA per SM (the operand stages fill shared
+  // memory), so a launch takes ceil(CTAs / SMs) rounds of ceil(kblocks / splits) K blocks each,
+  // plus a CTA's fixed cost (pipeline fill, TMEM, the epilogue's partial slab) of about three K
+  // blocks. Take the split count with the shortest such critical path (ties: fewer splits, whose
+  // partial sums cost less), from the smallest the accumulation bound allows up to a little past
+  // the one that first fills every SM.
+  const int hi = std::min(cap, std::max(lo, 2 * ((ctx->sm_count + tiles - 1) / tiles) + 8));
+  int best = lo;
+  long best_cost = -1;
+  for (int sp = lo; sp <= hi; ++sp) {
+    const int per = (kblocks + sp - 1) / sp;
+    const int used = (kblocks + per - 1) / per;
+    const long rounds = (long(tiles) * used + ctx->sm_count - 1) / ctx->sm_count;
+    const long cost = rounds * (per + 3);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = used;
+    }
+  }
   *bn = BN;
-  *splits = sp;
+  *splits = best;
 }
 
 template <int BN, int STAGES, int NS, int BK = kTcBK>
@@ -76,12 +99,19 @@ static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int 
 int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int K, float* out, long ld_out,
                    long split_stride, int max_splits, int* d_err, const char* prof_name, int kb_cap) {
   if (A.ns != B.ns || (A.ns != 2 && A.ns != 3)) fail(EPSP_EINVAL, "operands must be split into 2 or 3 parts alike");
+  if (A.bk != B.bk) fail(EPSP_EINVAL, "operands built for different K blocks");
   int BN, splits;
-  tc_gemm_shape(ctx, M, N, K, max_splits, A.ns, &BN, &splits, kb_cap);
-  const int kblocks = (K + kTcBK - 1) / kTcBK;
+  tc_gemm_shape(ctx, M, N, K, max_splits, A.ns, &BN, &splits, kb_cap);  // splits from K blocks of 64
+  const int bk = A.bk;
+  const int kblocks = (K + bk - 1) / bk;
   const int per = (kblocks + splits - 1) / splits;
+  splits = (kblocks + per - 1) / per;
   long pi = prof_begin(ctx, prof_name);
-  if (A.ns == 3)
+  if (A.ns == 3 && bk == 32)  // three-part operands in K blocks of 32: four stages
+    launch<128, 4, 3, 32>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+  else if (bk != kTcBK)
+    fail(EPSP_EINVAL, "K blocks of 32 are for three-part operands here (tc_gemm_launch_with takes two-part ones)");
+  else if (A.ns == 3)
     launch<128, 2, 3>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   else if (BN == 256)
     launch<256, 2, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
