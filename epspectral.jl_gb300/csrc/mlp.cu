@@ -9,6 +9,7 @@
 // epoch over the warm-start set is tens of milliseconds), every reduction in fixed order, so a
 // training run is bitwise reproducible.
 #include "common.cuh"
+#include "tc_gemm.cuh"
 #include "warmstart.cuh"
 
 #include <cuda_bf16.h>
@@ -220,6 +221,17 @@ struct Mlp {
   DBuf<float> x_mean, x_std, y_mean;  // feature standardisation for the in-iteration hook
   float y_scale = 1.f;
   bool scaled = false;
+  long wgen = 0;  // bumped whenever the weights change (set_params, train)
+  // Tensor-core inference: weights as the B operand [d_{l+1}][d_l padded to 8] (hi = the BF16
+  // weights, lo = 0), activations as the A operand (BF16 hi/lo of the FP32 values) [cap][d_l
+  // padded], split-K partials; rebuilt when wgen or the row capacity changes.
+  struct Infer {
+    long wgen = -1, cap = 0;
+    std::vector<int> dpad, bn;
+    std::vector<DBuf<__nv_bfloat16>> Wh, Wl, Ah, Al;
+    std::vector<TcOperand> opA, opB;
+    DBuf<float> part;
+  } inf;
 };
 
 // X[i][j] = (feature j of state i - x_mean[j]) / x_std[j]: Re Σ(ω_j), Im Σ(ω_j), T, μ, scale, ε_i - μ.
@@ -275,6 +287,133 @@ static void ensure_cap(Mlp* P, long n) {
   const size_t wmax = size_t(2) * size_t(ctx->sm_count) * 64 * 64;
   P->work.alloc(ctx, wmax);
   P->cap = n;
+}
+
+// ---- tensor-core inference (the scGD0 hook on the tensor-core path) ----
+
+// out[r][c] = in[r][c] for c < cols, 0 for cols <= c < ldo (BF16 rows padded to 16 bytes).
+__global__ void pad_rows_bf16_kernel(const __nv_bfloat16* __restrict__ in, long rows, int cols, int ldo,
+                                     __nv_bfloat16* __restrict__ out) {
+  const long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= rows * ldo) return;
+  const long r = k / ldo;
+  const int c = int(k % ldo);
+  out[k] = c < cols ? in[r * cols + c] : __float2bfloat16_rn(0.f);
+}
+
+// A operand of the first product: X [n][d] FP32 rows split into BF16 hi/lo rows of ldo.
+__global__ void split_rows_mlp_kernel(const float* __restrict__ X, int n, int d, int ldo, __nv_bfloat16* __restrict__ oh,
+                                      __nv_bfloat16* __restrict__ ol) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+  if (j >= d || i >= n) return;
+  const float x = X[long(i) * d + j];
+  const __nv_bfloat16 h = __float2bfloat16_rn(x);
+  oh[long(i) * ldo + j] = h;
+  ol[long(i) * ldo + j] = __float2bfloat16_rn(x - __bfloat162float(h));
+}
+
+// z = Σ_s part[s][m + n j] + b[j] (the product's column-major FP32 splits, in order); SiLU when act;
+// into the next product's A operand (BF16 hi/lo rows of ldo) or, for the last layer, X [n][dout].
+__global__ void bias_act_split_kernel(const float* __restrict__ part, int splits, long stride, int n, int dout,
+                                      const float* __restrict__ b, bool act, __nv_bfloat16* __restrict__ oh,
+                                      __nv_bfloat16* __restrict__ ol, int ldo, float* __restrict__ X) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (m >= n) return;
+  float z = 0.f;
+  for (int p = 0; p < splits; ++p) z += part[stride * p + m + long(n) * j];
+  z += b[j];
+  const float x = act ? z * sigmoidf_(z) : z;
+  if (oh) {
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    oh[long(m) * ldo + j] = h;
+    ol[long(m) * ldo + j] = __float2bfloat16_rn(x - __bfloat162float(h));
+  } else {
+    X[long(m) * dout + j] = x;
+  }
+}
+
+static void infer_reserve(Mlp* P, long n) {
+  Mlp::Infer& I = P->inf;
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  const bool grow = n > I.cap;
+  if (I.wgen == P->wgen && !grow) return;
+  const int L = P->L;
+  if (I.dpad.empty()) {
+    I.dpad.resize(size_t(L));
+    I.bn.resize(size_t(L));
+    I.Wh.resize(size_t(L));
+    I.Wl.resize(size_t(L));
+    I.Ah.resize(size_t(L));
+    I.Al.resize(size_t(L));
+    I.opA.resize(size_t(L));
+    I.opB.resize(size_t(L));
+    for (int l = 0; l < L; ++l) {
+      const int din = P->dims[size_t(l)], dout = P->dims[size_t(l + 1)];
+      I.dpad[size_t(l)] = (din + 7) / 8 * 8;
+      int bn, sp;
+      tc_gemm_shape(ctx, 1, dout, din, 16, 2, &bn, &sp);  // the tile width depends on N only
+      I.bn[size_t(l)] = bn;
+      I.Wh[size_t(l)].alloc(ctx, size_t(dout) * size_t(I.dpad[size_t(l)]));
+      I.Wl[size_t(l)].alloc(ctx, size_t(dout) * size_t(I.dpad[size_t(l)]));
+      I.Wl[size_t(l)].zero(s);  // the weights are exact in BF16: no low part
+      I.opB[size_t(l)].ns = 2;
+      I.opB[size_t(l)].m[0] = make_tmap_bf16(I.Wh[size_t(l)].p, dout, din, I.dpad[size_t(l)], bn);
+      I.opB[size_t(l)].m[1] = make_tmap_bf16(I.Wl[size_t(l)].p, dout, din, I.dpad[size_t(l)], bn);
+    }
+  }
+  if (I.wgen != P->wgen) {
+    for (int l = 0; l < L; ++l) {
+      const int din = P->dims[size_t(l)], dout = P->dims[size_t(l + 1)], dp = I.dpad[size_t(l)];
+      pad_rows_bf16_kernel<<<div_up(size_t(dout) * size_t(dp), 256), 256, 0, s>>>(P->Wbf[size_t(l)].p, dout, din, dp,
+                                                                                 I.Wh[size_t(l)].p);
+      EPSP_LAUNCHED(ctx);
+    }
+    I.wgen = P->wgen;
+  }
+  if (grow) {
+    size_t part = 0;
+    for (int l = 0; l < L; ++l) {
+      const int din = P->dims[size_t(l)], dout = P->dims[size_t(l + 1)], dp = I.dpad[size_t(l)];
+      I.Ah[size_t(l)].alloc(ctx, size_t(n) * size_t(dp));
+      I.Al[size_t(l)].alloc(ctx, size_t(n) * size_t(dp));
+      I.Ah[size_t(l)].zero(s);  // the padding columns stay zero
+      I.Al[size_t(l)].zero(s);
+      I.opA[size_t(l)].ns = 2;
+      I.opA[size_t(l)].m[0] = make_tmap_bf16(I.Ah[size_t(l)].p, n, din, dp, kTcBM);
+      I.opA[size_t(l)].m[1] = make_tmap_bf16(I.Al[size_t(l)].p, n, din, dp, kTcBM);
+      int bn, sp;
+      tc_gemm_shape(ctx, int(n), dout, dp, 16, 2, &bn, &sp);
+      part = std::max(part, size_t(sp) * size_t(n) * size_t(dout));
+    }
+    I.part.alloc(ctx, part);
+    I.cap = n;
+  }
+}
+
+// Forward over the rows in P->X[0] (n rows) on the tensor cores: each product A x W^T with A the
+// FP32 activations as BF16 hi + lo (three products, the weights' lo part is zero: FP32-accurate
+// activations times the BF16 weights, as the SIMT forward), FP32 accumulation; output in P->X[L].
+// Bounded waits report to d_err.
+static void forward_tc(Mlp* P, long n, int* d_err) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  infer_reserve(P, n);
+  Mlp::Infer& I = P->inf;
+  const int d0 = P->dims[0];
+  split_rows_mlp_kernel<<<dim3(div_up(size_t(d0), 256), unsigned(n)), 256, 0, s>>>(P->X[0].p, int(n), d0, I.dpad[0],
+                                                                                 I.Ah[0].p, I.Al[0].p);
+  EPSP_LAUNCHED(ctx);
+  for (int l = 0; l < P->L; ++l) {
+    const int dout = P->dims[size_t(l + 1)], dp = I.dpad[size_t(l)];
+    const int sp = tc_gemm_launch(ctx, I.opA[size_t(l)], I.opB[size_t(l)], int(n), dout, dp, I.part.p, n, n * long(dout),
+                                  16, d_err, "mlp");
+    const bool last = l + 1 == P->L;
+    bias_act_split_kernel<<<dim3(div_up(size_t(n), 128), unsigned(dout)), 128, 0, s>>>(
+        I.part.p, sp, n * long(dout), int(n), dout, P->b[size_t(l)].p, !last, last ? nullptr : I.Ah[size_t(l + 1)].p,
+        last ? nullptr : I.Al[size_t(l + 1)].p, last ? 0 : I.dpad[size_t(l + 1)], P->X[size_t(P->L)].p);
+    EPSP_LAUNCHED(ctx);
+  }
 }
 
 // Forward over the rows in P->X[0] (n rows); output in P->X[L].
@@ -356,7 +495,7 @@ struct epsp_warmstart {
 namespace epsp {
 
 void warmstart_correct(epsp_warmstart* w, Ctx* ctx, double2* S_T, long nw, long ni, const double* d_eps_i, double T,
-                       double mu, double scale) {
+                       double mu, double scale, int* tc_err) {
   Mlp& P = w->m;
   if (P.ctx != ctx) fail(EPSP_EINVAL, "the warm-start network belongs to another context");
   if (P.dims[0] != 2 * nw + 4 || P.dims.back() != 2 * nw)
@@ -368,7 +507,10 @@ void warmstart_correct(epsp_warmstart* w, Ctx* ctx, double2* S_T, long nw, long 
   features_kernel<<<dim3(div_up(size_t(2 * nw + 4), 256), unsigned(ni)), 256, 0, s>>>(
       S_T, int(nw), int(ni), d_eps_i, T, mu, scale, P.x_mean.p, P.x_std.p, P.X[0].p);
   EPSP_LAUNCHED(ctx);
-  forward(&P, ni);
+  if (tc_err)
+    forward_tc(&P, ni, tc_err);
+  else
+    forward(&P, ni);
   correct_kernel<<<dim3(div_up(size_t(nw), 256), unsigned(ni)), 256, 0, s>>>(S_T, int(nw), P.X[size_t(P.L)].p, P.y_scale,
                                                                             P.y_mean.p);
   EPSP_LAUNCHED(ctx);
@@ -461,6 +603,7 @@ epsp_status epsp_warmstart_set_params(epsp_warmstart* w, const float* params) {
       P.vb[size_t(l)].zero(s);
     }
     P.d_step.zero(s);
+    ++P.wgen;
     EPSP_CUDA(cudaStreamSynchronize(s));
   });
 }
@@ -631,6 +774,7 @@ epsp_status epsp_warmstart_train(epsp_warmstart* w, const float* X, const float*
     P.dataX.release();
     P.dataY.release();
     P.loss_sum.alloc(P.ctx, 1);
+    ++P.wgen;
   });
 }
 

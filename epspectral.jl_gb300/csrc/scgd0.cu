@@ -1349,7 +1349,7 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
       for (int64_t iT = 0; iT < nT; ++iT)
         if (active[size_t(iT)])
           warmstart_correct(warm, ctx, S.p + slab * iT, nw, ni, P->d_eps_i.p, occ->Tlist[iT], mu[size_t(iT)],
-                            warm_scale[iT]);
+                            warm_scale[iT], P->path == EPSP_PATH_GEMM_BF16 ? tc_err_ptr(P) : nullptr);
     hist->wall[iter - 1] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     niter = iter;
     if (std::none_of(active.begin(), active.end(), [](char a) { return a != 0; })) break;
