@@ -565,7 +565,7 @@ __global__ void __launch_bounds__(kMuPrepThreads)
 
 __global__ void __cluster_dims__(kMuCluster, 1, 1) __launch_bounds__(kMuThreads)
     mu_solve_kernel(const double* __restrict__ Dall, const double* __restrict__ wsa, int nwa, const int* __restrict__ slots,
-                    const TParams* __restrict__ tp, double W, double base, double gs, double br0, double br1,
+                    TParams* __restrict__ tp, double W, double base, double gs, double br0, double br1,
                     const double* __restrict__ E_all, const double* __restrict__ R1_all, double* __restrict__ mu_all,
                     int* __restrict__ status_all, int* __restrict__ evals_all) {
   namespace cg = cooperative_groups;
@@ -728,6 +728,7 @@ __global__ void __cluster_dims__(kMuCluster, 1, 1) __launch_bounds__(kMuThreads)
       *status = 1;
     } else {
       *mu_out = result;
+      tp[t].mu = result;  // the next iteration's μ, without a round trip to the host
       *status = 0;
     }
   }
@@ -1141,7 +1142,11 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   int* d_status = reinterpret_cast<int*>(d_pack.p + 3 * nT);
   int* d_evals = d_status + nT;
   int* d_tcerr = reinterpret_cast<int*>(d_pack.p + 4 * nT);
-  std::vector<double> h_pack(npack);
+  // host side of the readback and of the slot list: pinned
+  P->h_pin.ensure(npack * sizeof(double) + size_t(nT) * sizeof(int));
+  double* h_pack = static_cast<double*>(P->h_pin.p);
+  int* h_slots = reinterpret_cast<int*>(h_pack + npack);
+  std::vector<int> up_slots;  // the slot list on the device (uploaded when it changes)
   int32_t niter = 0;
   const unsigned eb = div_up(size_t(slab), 256);
   // Every active temperature of an iteration is processed by the same launches (slot a ->
@@ -1202,8 +1207,13 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
       q.pad = 0;
     }
     const int nA = int(slots.size());
-    d_slots.upload(slots.data(), slots.size(), s);
-    d_tp.upload(h_tp.data(), h_tp.size(), s);
+    if (slots != up_slots) {
+      std::copy(slots.begin(), slots.end(), h_slots);
+      EPSP_CUDA(cudaMemcpyAsync(d_slots.p, h_slots, slots.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+      up_slots = slots;
+    }
+    // T, η_min, target and branch are fixed for the run; μ is written on the device by the μ solve
+    if (iter == 1) d_tp.upload(h_tp.data(), h_tp.size(), s);
     // the launches of one iteration; on the tensor-core path they are captured once per active set
     // into a CUDA graph and replayed (μ, T come from the device, so a replay sees the current ones)
     auto body = [&] {
@@ -1307,17 +1317,17 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
     } else {
       body();
     }
-    d_pack.download(h_pack.data(), npack, s);
+    EPSP_CUDA(cudaMemcpyAsync(h_pack, d_pack.p, npack * sizeof(double), cudaMemcpyDeviceToHost, s));
     EPSP_CUDA(cudaStreamSynchronize(s));
     if (P->path == EPSP_PATH_GEMM_BF16) {
       int tcerr = 0;
       std::memcpy(&tcerr, &h_pack[size_t(4 * nT)], sizeof(int));
       if (tcerr) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
     }
-    const auto* h_err = reinterpret_cast<const unsigned long long*>(h_pack.data());
-    const double* h_mu = h_pack.data() + nT;
-    const double* h_minA = h_pack.data() + 2 * nT;
-    const auto* h_status = reinterpret_cast<const int*>(h_pack.data() + 3 * nT);
+    const auto* h_err = reinterpret_cast<const unsigned long long*>(h_pack);
+    const double* h_mu = h_pack + nT;
+    const double* h_minA = h_pack + 2 * nT;
+    const auto* h_status = reinterpret_cast<const int*>(h_pack + 3 * nT);
     for (int64_t iT = 0; iT < nT; ++iT) {
       if (!active[size_t(iT)]) continue;
       hist->min_spectral_weight[iT + nT * (iter - 1)] = h_minA[size_t(iT)];

@@ -13,6 +13,23 @@ struct TParams {
   int holes, pad;
 };
 
+// Pinned host memory (page-locked: small copies to and from it are direct DMA, without staging).
+struct HostPinned {
+  void* p = nullptr;
+  size_t bytes = 0;
+  void ensure(size_t n) {
+    if (n <= bytes) return;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    EPSP_CUDA(cudaHostAlloc(&p, n, cudaHostAllocDefault));
+    bytes = n;
+  }
+  ~HostPinned() {
+    if (p) cudaFreeHost(p);
+  }
+};
+
 struct Scgd0Plan {
   Ctx* ctx = nullptr;
   int path = EPSP_PATH_DIRECT_FP64;
@@ -58,6 +75,7 @@ struct Scgd0Plan {
   DBuf<int> w_slots;
   DBuf<TParams> w_tp;
   long w_gen = 0;  // bumped whenever one of them is reallocated
+  HostPinned h_pin;  // the per-iteration readback and the slot list
   // the captured iteration of the last run, reused while its key matches
   cudaGraphExec_t graph = nullptr;
   long graph_key[6] = {-1, -1, -1, -1, -1, -1};
