@@ -1289,7 +1289,13 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
         err_copy_kernel<false><<<dim3(eb, unsigned(nA)), 256, 0, s>>>(Snew.p, S.p, slab, d_slots.p, d_err);
       EPSP_LAUNCHED(ctx);
     };
-    if (use_graph && iter > 1) {
+    // iteration 1 replays a graph a previous run captured with the same key; otherwise it runs
+    // eagerly (first launches set kernel attributes) and iteration 2 captures
+    const bool have_graph = P->graph && [&] {
+      const auto k = graph_key(nA);
+      return std::equal(k.begin(), k.end(), P->graph_key);
+    }();
+    if (use_graph && (iter > 1 || have_graph)) {
       const auto key = graph_key(nA);
       if (!P->graph || !std::equal(key.begin(), key.end(), P->graph_key)) {
         if (P->graph) cudaGraphExecDestroy(P->graph), P->graph = nullptr;
