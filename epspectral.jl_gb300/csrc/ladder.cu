@@ -78,6 +78,7 @@ struct LadderPlan {
   DBuf<int> d_err;
   TcOperand opA{}, opG{}, opA64{}, opG128{}, opG256{}, opA32{}, opG256_32{};
   int bn = 128, splits = 1, bk = kTcBK;  // the contraction's tile shape, picked by the autotuner at setup
+  bool persist = false;                  // ... and whether it runs as the persistent kernel
   std::vector<TcTune> tune_all;
   float tune_ms_heuristic = 0.f;
   // exchange (both paths)
@@ -1410,10 +1411,11 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       const TcTune best = tc_gemm_autotune(ctx, P->opA64, P->opG128, P->opG256, int(M), int(N), int(P->Kx), P->d_part.p, M,
                                            M * N, max_sp, P->d_err.p, 2, &P->tune_all, &P->opA32, &P->opG256_32);
       for (const auto& c : P->tune_all)
-        if (c.bn == bn_h && c.splits == sp_h && c.bk == kTcBK) P->tune_ms_heuristic = c.ms;
+        if (c.bn == bn_h && c.splits == sp_h && c.bk == kTcBK && !c.persist) P->tune_ms_heuristic = c.ms;
       P->bn = best.bn;
       P->splits = best.splits;
       P->bk = best.bk;
+      P->persist = best.persist;
       P->opA = P->bk == 32 ? P->opA32 : P->opA64;
       P->opG = P->bk == 32 ? P->opG256_32 : (P->bn == 256 ? P->opG256 : P->opG128);
       int terr = 0;
@@ -1611,7 +1613,7 @@ static void apply_L(LadderPlan* P, const float2* J, float2* LJ, const float2* X 
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, px);
   int sp = tc_gemm_launch_with(ctx, P->opA, P->opG, P->bn, P->splits, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N,
-                               P->d_err.p, "tc_ladder");
+                               P->d_err.p, "tc_ladder", P->persist);
   // D stays as the contraction's split-K partials; y_split and finish add them as they read
   long pl = prof_begin(ctx, "lsum");
   y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), 1), 256, 0, s>>>(P->d_part.p, M, sp, M * N, int(nw), int(nwp),
@@ -2100,7 +2102,7 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const float2* X, int nA
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, px);
   int sp = tc_gemm_launch_with(ctx, B.opA, P->opG, P->bn, 0, int(Mt), int(N), int(P->Kx), B.part.p, Mt, Mt * N, P->d_err.p,
-                               "tc_ladder");
+                               "tc_ladder", P->persist);
   y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), unsigned(nA)), 256, 0, s>>>(
       B.part.p, Mt, sp, Mt * N, int(nw), int(nwp), N, P->Kp2, B.Yh.p, B.Yl.p);
   EPSP_LAUNCHED(ctx);
@@ -2477,6 +2479,23 @@ epsp_status epsp_ladder_set_gemm_config(epsp_ladder_plan* plan, int32_t bn, int3
     P->bk = bk;
     P->opA = bk == 32 ? P->opA32 : P->opA64;
     P->opG = bk == 32 ? P->opG256_32 : (bn == 256 ? P->opG256 : P->opG128);
+    if (!(bn == 256 && bk == 32)) P->persist = false;
+  });
+}
+
+epsp_status epsp_ladder_gemm_persistent(const epsp_ladder_plan* plan, int32_t* on) {
+  if (!plan || !on) return EPSP_EINVAL;
+  *on = reinterpret_cast<const LadderPlan*>(plan)->persist ? 1 : 0;
+  return EPSP_OK;
+}
+
+epsp_status epsp_ladder_set_gemm_persistent(epsp_ladder_plan* plan, int32_t on) {
+  if (!plan) return EPSP_EINVAL;
+  auto* P = reinterpret_cast<LadderPlan*>(plan);
+  return lguard(P->ctx, [&] {
+    if (P->path != EPSP_PATH_GEMM_BF16) fail(EPSP_EUNSUPPORTED, "tile shapes apply to GEMM_BF16 plans");
+    if (on && !(P->bn == 256 && P->bk == 32)) fail(EPSP_EINVAL, "the persistent kernel takes bn 256 with bk 32");
+    P->persist = on != 0;
   });
 }
 
@@ -2489,7 +2508,7 @@ epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, i
   if (bk) *bk = P->bk;
   double best = 0;
   for (const auto& c : P->tune_all)
-    if (c.bn == P->bn && c.splits == P->splits && c.bk == P->bk) best = c.ms;
+    if (c.bn == P->bn && c.splits == P->splits && c.bk == P->bk && c.persist == P->persist) best = c.ms;
   if (ms_chosen) *ms_chosen = best;
   if (ms_heuristic) *ms_heuristic = P->tune_ms_heuristic;
   return EPSP_OK;

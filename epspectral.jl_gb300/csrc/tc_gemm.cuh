@@ -253,6 +253,205 @@ __global__ void __launch_bounds__(128, 1)
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
 }
 
+// ---- persistent variant ----
+// One CTA per SM runs the (N tile, M tile, split) items i = blockIdx.x, blockIdx.x + gridDim.x, ...
+// (N tiles fastest, the launch order of the one-tile kernel), 192 threads:
+//   warp 0, lane 0 : TMA producer; the operand ring runs on across items;
+//   warp 1, lane 0 : MMA issuer; item t accumulates in TMEM columns (t % 2) BN.. (two accumulators);
+//   warps 2-5      : epilogue of item t (TMEM lane quarter = warp % 4) while the MMAs of item t + 1
+//                    run into the other accumulator; they release an accumulator by one arrive each.
+// Per tile the MMAs run in the one-tile kernel's order, so the results are bitwise the same.
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+template <int BN, int STAGES, int NS, int BK>
+struct TcPSmem {
+  static constexpr int kA = kTcBM * BK * 2;
+  static constexpr int kB = BN * BK * 2;
+  static constexpr int kStage = NS * kA + NS * kB;
+  static constexpr int kBars = 2 * STAGES + 5;  // full, empty, accumulator full x2, empty x2, done
+  static constexpr int kBytes = STAGES * kStage + 8 * kBars + 16 + 1024;
+};
+
+template <int BN, int STAGES, int NS, int BK>
+__global__ void __launch_bounds__(192, 1)
+    tc_gemm_persist_kernel(const __grid_constant__ TcMaps maps, int M, int N, int kblocks, int kb_per_split, int nN,
+                           int nM, int nitems, float* __restrict__ out, long ld_out, long split_stride,
+                           int* __restrict__ err) {
+  using L = TcPSmem<BN, STAGES, NS, BK>;
+  static_assert(2 * BN <= 512, "two accumulators must fit TMEM");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * L::kStage);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + L::kBars);
+  __shared__ int s_abort;
+  const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * STAGES, accf0 = full0 + 16 * STAGES,
+                 acce0 = accf0 + 16, done_bar = accf0 + 32;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  auto coords = [&](int item, int& n0, int& m0, int& z, int& kb0, int& nkb) {
+    n0 = (item % nN) * BN;
+    m0 = ((item / nN) % nM) * kTcBM;
+    z = item / (nN * nM);
+    kb0 = z * kb_per_split;
+    nkb = max(0, min(kblocks, kb0 + kb_per_split) - kb0);
+  };
+  auto aborted = [&] { return *(volatile int*)&s_abort != 0; };
+
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int s = 0; s < 2 * STAGES; ++s) mbar_init(smem_u32(bars + s), 1);
+    mbar_init(accf0, 1);
+    mbar_init(accf0 + 8, 1);
+    mbar_init(acce0, 4);
+    mbar_init(acce0 + 8, 4);
+    mbar_init(done_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(2 * BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // producer
+    int g = 0;
+    bool stop = false;
+    for (int item = blockIdx.x; item < nitems && !stop; item += gridDim.x) {
+      int n0, m0, z, kb0, nkb;
+      coords(item, n0, m0, z, kb0, nkb);
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = g % STAGES;
+        const uint32_t ph = (g / STAGES) & 1;
+        if (g >= STAGES && !mbar_wait(empty0 + 8 * s, ph ^ 1)) {
+          atomicExch(&s_abort, 1);
+          stop = true;
+          break;
+        }
+        if (aborted()) {
+          stop = true;
+          break;
+        }
+        uint8_t* st = smem + s * L::kStage;
+        const uint32_t fb = full0 + 8 * s;
+        mbar_expect_tx(fb, L::kStage);
+        const int kc = (kb0 + kb) * BK;
+#pragma unroll
+        for (int p = 0; p < NS; ++p) {
+          tma_load_2d(smem_u32(st + p * L::kA), &maps.a[p], kc, m0, fb);
+          tma_load_2d(smem_u32(st + NS * L::kA + p * L::kB), &maps.b[p], kc, n0, fb);
+        }
+        ++g;
+      }
+    }
+    if (aborted()) {
+      // wind down: wait (bounded) for the copies this thread issued into stages not yet consumed
+      for (int k = max(0, g - STAGES); k < g; ++k) mbar_wait(full0 + 8 * (k % STAGES), (k / STAGES) & 1);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    constexpr uint32_t idesc = idesc_bf16_f32(BN);
+    int g = 0, t = 0;
+    bool stop = false;
+    for (int item = blockIdx.x; item < nitems && !stop; item += gridDim.x, ++t) {
+      int n0, m0, z, kb0, nkb;
+      coords(item, n0, m0, z, kb0, nkb);
+      const int b = t & 1;
+      const uint32_t acc = tmem + uint32_t(b * BN);
+      if (t >= 2 && !mbar_wait(acce0 + 8 * b, ((t >> 1) & 1) ^ 1)) {  // the epilogue drained it
+        atomicExch(&s_abort, 1);
+        break;
+      }
+      tc_fence_after();
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = g % STAGES;
+        const uint32_t ph = (g / STAGES) & 1;
+        if (!mbar_wait(full0 + 8 * s, ph)) {
+          atomicExch(&s_abort, 1);
+          stop = true;
+          break;
+        }
+        if (aborted()) {
+          stop = true;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(smem + s * L::kStage);
+        const uint32_t b0 = a0 + NS * L::kA;
+#pragma unroll
+        for (int ks = 0; ks < BK / 16; ++ks) {
+          const uint32_t off = ks * 32;
+          umma_bf16(acc, sw_desc<BK>(a0 + off), sw_desc<BK>(b0 + off), idesc, (kb | ks) != 0);
+          if constexpr (NS >= 2) {
+            umma_bf16(acc, sw_desc<BK>(a0 + off), sw_desc<BK>(b0 + L::kB + off), idesc, 1);
+            umma_bf16(acc, sw_desc<BK>(a0 + L::kA + off), sw_desc<BK>(b0 + off), idesc, 1);
+          }
+          if constexpr (NS == 3) {
+            umma_bf16(acc, sw_desc<BK>(a0 + off), sw_desc<BK>(b0 + 2 * L::kB + off), idesc, 1);
+            umma_bf16(acc, sw_desc<BK>(a0 + L::kA + off), sw_desc<BK>(b0 + L::kB + off), idesc, 1);
+            umma_bf16(acc, sw_desc<BK>(a0 + 2 * L::kA + off), sw_desc<BK>(b0 + off), idesc, 1);
+          }
+        }
+        umma_commit(empty0 + 8 * s);
+        ++g;
+      }
+      umma_commit(accf0 + 8 * b);  // completes when the item's MMAs have
+    }
+    umma_commit(done_bar);  // completes when every MMA issued above has
+  } else if (warp >= 2) {
+    // epilogue
+    const int q = warp % 4;
+    int t = 0;
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x, ++t) {
+      if (aborted()) break;
+      int n0, m0, z, kb0, nkb;
+      coords(item, n0, m0, z, kb0, nkb);
+      const int b = t & 1;
+      if (!mbar_wait(accf0 + 8 * b, (t >> 1) & 1)) {
+        atomicExch(&s_abort, 1);
+        break;
+      }
+      tc_fence_after();
+      if (aborted()) break;
+      const int row = m0 + q * 32 + lane;
+      float* o = out + long(z) * split_stride;
+#pragma unroll 1
+      for (int c = 0; c < BN; c += 32) {
+        float v[32];
+        tmem_ld32(tmem + (uint32_t(q * 32) << 16) + uint32_t(b * BN + c), v);
+        if (nkb == 0) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] = 0.f;
+        }
+        if (row < M) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int n = n0 + c + j;
+            if (n < N) o[row + ld_out * long(n)] = v[j];
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acce0 + 8 * b);
+    }
+  }
+  __syncwarp();
+  // every MMA issued has completed before TMEM is freed (bounded)
+  if (!mbar_wait(done_bar, 0)) atomicExch(&s_abort, 1);
+  tc_fence_after();
+  __syncthreads();
+  if (aborted() && threadIdx.x == 0) atomicExch(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
+}
+
 // ---- host side ----
 
 // A 2-D BF16 tensor map over a row-major [rows][ld] array (K contiguous, rows of `cols` valid
@@ -282,7 +481,8 @@ void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* b
 // only) and split count (0: the heuristic's count for that bn); B's tensor maps must have boxes of
 // bn rows. Returns the splits used.
 int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn, int splits, int M, int N, int K,
-                        float* out, long ld_out, long split_stride, int* d_err, const char* prof_name = "tc_gemm");
+                        float* out, long ld_out, long split_stride, int* d_err, const char* prof_name = "tc_gemm",
+                        bool persist = false);
 // The variant with K blocks of 32 (64-byte swizzle) and four pipeline stages, bn = 256; A and B
 // maps built with bk = 32.
 
@@ -293,6 +493,7 @@ int tc_splits_for(Ctx* ctx, int M, int N, int K, int bn);
 struct TcTune {
   int bn = 0, splits = 0, bk = kTcBK;
   float ms = 0.f;
+  bool persist = false;  // the persistent kernel (one CTA per SM, two accumulators)
 };
 
 // The autotuner: times every candidate tile shape (bn 128 with three stages, bn 256 with two; the

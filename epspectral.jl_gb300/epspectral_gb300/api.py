@@ -74,6 +74,8 @@ def lib():
         "epsp_ladder_apply": (C.c_int, [vp, c_double_p, d, d, d, c_double_p, c_double_p]),
         "epsp_ladder_gemm_config": (C.c_int, [vp, P(i32), P(i32), P(i32), P(d), P(d)]),
         "epsp_ladder_set_gemm_config": (C.c_int, [vp, i32, i32, i32]),
+        "epsp_ladder_gemm_persistent": (C.c_int, [vp, P(i32)]),
+        "epsp_ladder_set_gemm_persistent": (C.c_int, [vp, i32]),
         "epsp_ladder_run_batched": (C.c_int, [vp, c_double_p, c_double_p, c_double_p, i64, c_double_p, i64, d, i32, i32,
                                               c_double_p, c_double_p, u8p, c_int32_p, P(epsp_ladder_history),
                                               c_double_p]),
@@ -278,11 +280,16 @@ class LadderPlan:
         bn, sp, bk, ms, mh = C.c_int32(), C.c_int32(), C.c_int32(), C.c_double(), C.c_double()
         self.ctx.check(lib().epsp_ladder_gemm_config(self.handle, C.byref(bn), C.byref(sp), C.byref(bk), C.byref(ms),
                                                      C.byref(mh)))
-        return dict(bn=bn.value, splits=sp.value, bk=bk.value, ms=ms.value, ms_heuristic=mh.value)
+        on = C.c_int32()
+        self.ctx.check(lib().epsp_ladder_gemm_persistent(self.handle, C.byref(on)))
+        return dict(bn=bn.value, splits=sp.value, bk=bk.value, persistent=bool(on.value), ms=ms.value,
+                    ms_heuristic=mh.value)
 
-    def set_gemm_config(self, bn: int, splits: int, bk: int = 64):
-        """Overrides the autotuner's tile shape of the contraction (GEMM_BF16 plans)."""
+    def set_gemm_config(self, bn: int, splits: int, bk: int = 64, persistent: bool = False):
+        """Overrides the autotuner's tile shape of the contraction (GEMM_BF16 plans); persistent: one
+        CTA per SM over all tiles (bn 256, bk 32 only)."""
         self.ctx.check(lib().epsp_ladder_set_gemm_config(self.handle, int(bn), int(splits), int(bk)))
+        self.ctx.check(lib().epsp_ladder_set_gemm_persistent(self.handle, 1 if persistent else 0))
 
     def run(self, sigma, mu, Tlist, Omegas, *, solver="gmres", rtol=1e-2, maxiter=30, store_vertex=False,
             batch_rhs=None):

@@ -255,6 +255,11 @@ epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, i
  * swizzle; two or three pipeline stages), or bn 256 with bk = 32 (64-byte swizzle, four stages);
  * splits within what the plan's partial buffer holds. */
 epsp_status epsp_ladder_set_gemm_config(epsp_ladder_plan* plan, int32_t bn, int32_t splits, int32_t bk);
+/* Whether the contraction runs as the persistent kernel (one CTA per SM over all tiles, two TMEM
+ * accumulators so that a tile's epilogue overlaps the next tile's products; bn 256 with bk 32
+ * only): read, and set (on = 0 or 1; EPSP_EINVAL for another tile shape). Same results bitwise. */
+epsp_status epsp_ladder_gemm_persistent(const epsp_ladder_plan* plan, int32_t* on);
+epsp_status epsp_ladder_set_gemm_persistent(epsp_ladder_plan* plan, int32_t on);
 
 /* One application LJ = L(J) of the ladder kernel at temperature T, chemical potential mu and
  * probe frequency Omega, with sigma_T [nω, ni] complex the self-energy of that temperature:

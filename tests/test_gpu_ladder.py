@@ -205,6 +205,14 @@ def test_every_contraction_tile_shape_matches_the_oracle(api, oracle, cc, unit):
             plan.set_gemm_config(bn, sp, bk)
             got = plan.apply(J, sig, c["mu"][0], T, 0.07)
             assert np.all(np.isfinite(got)) and rel(got, ref) <= 1e-4, (bn, bk, sp, rel(got, ref))
+            if (bn, bk) == (256, 32):
+                # the persistent kernel (one CTA per SM over all tiles, two TMEM accumulators) runs
+                # every tile's products in the same order: bitwise the same result
+                plan.set_gemm_config(bn, sp, bk, persistent=True)
+                assert plan.gemm_config()["persistent"]
+                assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp)
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(128, 1, 32)
+    with pytest.raises(ArgumentError):
+        plan.set_gemm_config(128, 1, 64, persistent=True)
     plan.close()
