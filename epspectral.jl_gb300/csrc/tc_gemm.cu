@@ -135,12 +135,12 @@ int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int 
     launch<128, 4, 3, 32>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   else if (bk != kTcBK)
     fail(EPSP_EINVAL, "K blocks of 32 are for three-part operands here (tc_gemm_launch_with takes two-part ones)");
-  else if (A.ns == 3)
-    launch<128, 2, 3>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+  else if (A.ns == 3)  // the persistent kernel: each SM's tiles back to back, epilogues overlapped
+    launch_persist<128, 2, 3, 64>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   else if (BN == 256)
-    launch<256, 2, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    launch_persist<256, 2, 2, 64>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   else
-    launch<128, 3, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    launch_persist<128, 3, 2, 64>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   prof_end(ctx, pi);
   return splits;
 }
