@@ -91,8 +91,7 @@ struct LadderPlan {
   std::vector<double> h_tm, h_tp;
   double tab_Om = std::numeric_limits<double>::quiet_NaN();
   double cur_T = 0, cur_mu = 0, cur_Om = 0;
-  // GEMM_BF16: KY in FP32, the propagators as FP32 complex
-  DBuf<float> d_KYf;
+  // GEMM_BF16: the propagators as FP32 complex
   DBuf<float2> d_Gmf, d_Gpf;
   // work buffers of the solves, kept across runs (vertex vectors: FP64 complex on the FP64 paths,
   // FP32 complex on the tensor-core path)
@@ -798,15 +797,6 @@ __global__ void split_rows_t2_kernel(const double* __restrict__ S, long ldr, lon
   ol[idx] = __float2bfloat16_rn(x - __bfloat162float(h));
 }
 
-// Sum of split-K partials into D (FP64).
-__global__ void sum_parts_kernel(const float* __restrict__ part, long n, int splits, long stride, float* __restrict__ D) {
-  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  float s = 0.f;
-  for (int p = 0; p < splits; ++p) s += part[k + stride * p];
-  D[k] = s;
-}
-
 // Y of the regrouped path: the rows q = 0 (c12 = 11) and q = 2 (c12 = 22) of D, as [nω, (qq, c0, ri, n)].
 __global__ void y_gemm_kernel(const double* __restrict__ D, int nw, int nwp, long ncol, double* __restrict__ Y) {
   long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -824,10 +814,11 @@ __global__ void y_gemm_kernel(const double* __restrict__ D, int nw, int nwp, lon
 // z 24 nwp.. of D (column stride ldD) and KY + z nω 24ni, and writes LJ + 24 nω ni r with the
 // propagators Gm, Gp + 4 nω ni r of right-hand side r = rmap[z] (r = z without rmap).
 // With X_all, it writes X - L(X) instead of L(X) (the GMRES operator applied to X, in one pass).
-// R = float (tensor-core path): D (as dsplits split-K partials dstride apart, summed in ascending
-// order), KY in FP32 and the propagators and vertices FP32 complex; R = double: all FP64.
+// R = float (tensor-core path): D and KY (as split-K partials, summed in ascending order) in FP32 and
+// the propagators and vertices FP32 complex; R = double: all FP64.
 template <class R>
 __global__ void finish_gemm_kernel(const R* __restrict__ D_all, long ldD, int dsplits, long dstride, const R* __restrict__ KY_all,
+                                   int kysplits, long kystride,
                                    const Vec2<R>* __restrict__ Gm_all, const Vec2<R>* __restrict__ Gp_all,
                                    const int* __restrict__ rmap, int nw, int nwp, int ni, Vec2<R>* __restrict__ LJ_all,
                                    const Vec2<R>* __restrict__ X_all = nullptr) {
@@ -861,7 +852,17 @@ __global__ void finish_gemm_kernel(const R* __restrict__ D_all, long ldD, int ds
         if (q != 2) dv[ri][q] += src[long(nwp) * (q + 6 * (c0 + 2 * ri))];
   }
   auto d = [&](int q, int ri) { return dv[ri][q]; };
-  auto ky = [&](int qq, int ri) { return R(KY[w + nw * (qq + 2 * (c0 + 2 * (ri + 2 * n)))]); };
+  // KY as kysplits split-K partials kystride apart, summed in ascending order, the 4 values of a
+  // partial loaded together
+  R kv[2][2] = {{0, 0}, {0, 0}};  // [qq][ri]
+  for (int p = 0; p < kysplits; ++p) {
+    const R* src = KY + w + kystride * p;
+#pragma unroll
+    for (int qq = 0; qq < 2; ++qq)
+#pragma unroll
+      for (int ri = 0; ri < 2; ++ri) kv[qq][ri] += src[nw * (qq + 2 * (c0 + 2 * (ri + 2 * n)))];
+  }
+  auto ky = [&](int qq, int ri) { return kv[qq][ri]; };
   Cx<R> K[4];
   {
     const Cx<R> y0{ky(0, 0), ky(0, 1)};
@@ -1445,7 +1446,6 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
     fail(EPSP_EINVAL, "unknown path");
   }
   if (P->path == EPSP_PATH_GEMM_BF16) {
-    P->d_KYf.alloc(ctx, size_t(nw * 24 * ni));
     P->d_Gmf.alloc(ctx, size_t(nw * 4 * ni));
     P->d_Gpf.alloc(ctx, size_t(nw * 4 * ni));
   } else {
@@ -1592,7 +1592,7 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ, const double2*
   EPSP_LAUNCHED(ctx);
   gemm_f64(ctx, false, int(nw), int(8 * N), int(nw), 1.0, P->d_KK.p, nw, P->d_Y.p, nw, 0.0, P->d_KY.p, nw);
   finish_gemm_kernel<double><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), 1), 256, 0, s>>>(
-      P->d_D.p, M, 1, 0, P->d_KY.p, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
+      P->d_D.p, M, 1, 0, P->d_KY.p, 1, 0, P->d_Gm.p, P->d_Gp.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
   EPSP_LAUNCHED(ctx);
 }
 
@@ -1623,10 +1623,9 @@ static void apply_L(LadderPlan* P, const float2* J, float2* LJ, const float2* X 
   int sp2 = tc_gemm_launch(ctx, P->opKK, P->opY, int(nw), int(8 * N), int(nw), P->d_part2.p, nw, nw * 8 * N, 16, P->d_err.p,
                            "tc_ladder_kk");
   pl = prof_begin(ctx, "lfinish");
-  sum_parts_kernel<<<div_up(size_t(nw * 8 * N), 256), 256, 0, s>>>(P->d_part2.p, nw * 8 * N, sp2, nw * 8 * N, P->d_KYf.p);
-  EPSP_LAUNCHED(ctx);
   finish_gemm_kernel<float><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), 1), 256, 0, s>>>(
-      P->d_part.p, M, sp, M * N, P->d_KYf.p, P->d_Gmf.p, P->d_Gpf.p, nullptr, int(nw), int(nwp), int(ni), LJ, X);
+      P->d_part.p, M, sp, M * N, P->d_part2.p, sp2, nw * 8 * N, P->d_Gmf.p, P->d_Gpf.p, nullptr, int(nw), int(nwp),
+      int(ni), LJ, X);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pl);
 }
@@ -2036,7 +2035,6 @@ struct LadderBatch {
   int bk = 0;  // K block of the A maps
   DBuf<__nv_bfloat16> Ah, Al, Yh, Yl;
   DBuf<float> part, part2, nnu;
-  DBuf<float> KY;
   DBuf<float2> Gm, Gp, J0, J, LJ, W;
   DBuf<double2> dpart, H, coef_a, coef_b;
   std::vector<DBuf<float2>> V;
@@ -2067,7 +2065,6 @@ static void batch_reserve(LadderPlan* P, LadderBatch& B, long R, int maxiter) {
   B.part.alloc(ctx, p1);
   B.part2.alloc(ctx, p2);
   B.nnu.alloc(ctx, size_t(16 * R));
-  B.KY.alloc(ctx, size_t(R * nw * 8 * N));
   B.Gm.alloc(ctx, size_t(R * 4 * nw * ni));
   B.Gp.alloc(ctx, size_t(R * 4 * nw * ni));
   for (auto* b : {&B.J0, &B.J, &B.LJ, &B.W}) b->alloc(ctx, size_t(R * n));
@@ -2109,10 +2106,8 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const float2* X, int nA
   const long N2 = 8 * N * nA;
   int sp2 = tc_gemm_launch(ctx, P->opKK, B.opY, int(nw), int(N2), int(nw), B.part2.p, nw, nw * N2, 16, P->d_err.p,
                            "tc_ladder_kk");
-  sum_parts_kernel<<<div_up(size_t(nw * N2), 256), 256, 0, s>>>(B.part2.p, nw * N2, sp2, nw * N2, B.KY.p);
-  EPSP_LAUNCHED(ctx);
   finish_gemm_kernel<float><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), unsigned(nA)), 256, 0, s>>>(
-      B.part.p, Mt, sp, Mt * N, B.KY.p, B.Gm.p, B.Gp.p, B.rmap.p, int(nw), int(nwp), int(ni), LJ);
+      B.part.p, Mt, sp, Mt * N, B.part2.p, sp2, nw * N2, B.Gm.p, B.Gp.p, B.rmap.p, int(nw), int(nwp), int(ni), LJ);
   EPSP_LAUNCHED(ctx);
 }
 
