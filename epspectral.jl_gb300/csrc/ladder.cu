@@ -63,8 +63,8 @@ struct LadderPlan {
   // padded to nmp (a multiple of 16)
   long nwp = 0, nmp = 0;
   long Kx = 0, Kp = 0, Kp2 = 0;
-  DBuf<int32_t> d_mt_k;          // [nwp, nmp, 2][2] first nodes of the two shift tables of a mode
-  DBuf<float> d_mt_w;            // [nwp, nmp, 2][4] their weights (1 - r) wlo, (1 - r) whi, r wlo, r whi
+  DBuf<int32_t> d_mt_k;          // [nwp, nmp, 2] first node p0 of the three nodes a mode's two shift tables read
+  DBuf<float> d_mt_w;            // [nwp, nmp, 2][4] the weights of p0, p0 + 1, p0 + 2 (tent weights folded in), 0
   DBuf<float> d_nnu_f;
   DBuf<__nv_bfloat16> d_KKh, d_KKl, d_Yh, d_Yl;
   DBuf<float> d_part2;
@@ -619,8 +619,8 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const float2* __restrict
   const int qbase = cc < 2 ? 2 * cc : cc + 2;  // 0, 2, 4, 5
   const int tr = threadIdx.x % 32, tk = threadIdx.x / 32;
   const int j = j0 + tr;
-  int ka[2][2], kb[2][2];
-  float w[2][2][4], nB[2];
+  int ka[2][2];
+  float w[2][2][3], nB[2];
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int nu = tk + 8 * h;
@@ -628,10 +628,11 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const float2* __restrict
 #pragma unroll
     for (int sg = 0; sg < 2; ++sg) {
       const long g = (long(j) * nmp + nu) * 2 + sg;  // [j][nu][s] with nmp == 16 per K-group
-      ka[h][sg] = mt_k[g * 2] - (j0 - W);
-      kb[h][sg] = mt_k[g * 2 + 1] - (j0 - W);
-#pragma unroll
-      for (int t = 0; t < 4; ++t) w[h][sg][t] = mt_w[g * 4 + t];
+      ka[h][sg] = mt_k[g] - (j0 - W);
+      const float4 wv = reinterpret_cast<const float4*>(mt_w)[g];
+      w[h][sg][0] = wv.x;
+      w[h][sg][1] = wv.y;
+      w[h][sg][2] = wv.z;
     }
   }
   const long kt0 = long(blockIdx.y) * kXgTiles;
@@ -681,9 +682,9 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const float2* __restrict
         const float2* jw = s_j + g * win;
 #pragma unroll
         for (int sg = 0; sg < 2; ++sg) {
-          const float2 u0 = jw[ka[h][sg]], u1 = jw[ka[h][sg] + 1], u2 = jw[kb[h][sg]], u3 = jw[kb[h][sg] + 1];
-          xs[sg].x = w[h][sg][0] * u0.x + w[h][sg][1] * u1.x + w[h][sg][2] * u2.x + w[h][sg][3] * u3.x;
-          xs[sg].y = w[h][sg][0] * u0.y + w[h][sg][1] * u1.y + w[h][sg][2] * u2.y + w[h][sg][3] * u3.y;
+          const float2 u0 = jw[ka[h][sg]], u1 = jw[ka[h][sg] + 1], u2 = jw[ka[h][sg] + 2];
+          xs[sg].x = w[h][sg][0] * u0.x + w[h][sg][1] * u1.x + w[h][sg][2] * u2.x;
+          xs[sg].y = w[h][sg][0] * u0.y + w[h][sg][1] * u1.y + w[h][sg][2] * u2.y;
         }
       }
       const float n = nB[h];
@@ -1350,10 +1351,13 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       P->d_Af.alloc(ctx, size_t(M * P->Kx));
     } else {
       // mode tables: for node j, mode ν and sign s, the two shift tables (m_ν, m_ν + 1) with the
-      // tent weights (1 - r_ν, r_ν) folded into their interpolation weights (FP32).
+      // tent weights (1 - r_ν, r_ν) folded into their interpolation weights (FP32). The two tables'
+      // lower nodes differ by at most one (the grid's spacing is a multiple of its unit, the shift
+      // step), so their four taps lie on three consecutive nodes p0, p0 + 1, p0 + 2: one node and
+      // three weights per entry (the fourth weight slot is zero).
       {
         const long nwp = P->nwp;
-        std::vector<int32_t> hk(size_t(nwp * 16 * 2 * 2));
+        std::vector<int32_t> hk(size_t(nwp * 16 * 2));
         std::vector<float> hw(size_t(nwp * 16 * 2 * 4), 0.f);
         std::vector<int32_t> klo(size_t(nw * ns * 2));
         std::vector<double> wlo(klo.size()), whi(klo.size());
@@ -1365,21 +1369,29 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
           for (long nu = 0; nu < 16; ++nu)
             for (long sg = 0; sg < 2; ++sg) {
               const size_t e = size_t((j * 16 + nu) * 2 + sg);
-              hk[2 * e] = hk[2 * e + 1] = int32_t(j);
+              hk[e] = int32_t(j);
               if (j >= nw || nu >= nm || P->wnu[size_t(nu)] < P->w_ac) continue;
               const long mm = P->m_nu[size_t(nu)];
               const double r = P->r_nu[size_t(nu)];
               const size_t t0 = size_t(j + nw * (mm + ns * sg));
-              hk[2 * e] = klo[t0];
-              hw[4 * e] = float((1 - r) * wlo[t0]);
-              hw[4 * e + 1] = float((1 - r) * whi[t0]);
-              hk[2 * e + 1] = hk[2 * e];
+              long ka = klo[t0], kb = ka;
+              double tw[4] = {(1 - r) * wlo[t0], (1 - r) * whi[t0], 0.0, 0.0};
               if (mm + 1 < ns && r != 0.0) {
                 const size_t t1 = size_t(j + nw * (mm + 1 + ns * sg));
-                hk[2 * e + 1] = klo[t1];
-                hw[4 * e + 2] = float(r * wlo[t1]);
-                hw[4 * e + 3] = float(r * whi[t1]);
+                kb = klo[t1];
+                tw[2] = r * wlo[t1];
+                tw[3] = r * whi[t1];
               }
+              if (std::labs(kb - ka) > 1)
+                fail(EPSP_EUNSUPPORTED, "neighbouring shift tables more than one node apart (the grid spacing is below its unit)");
+              const long p0 = std::min(ka, kb);
+              double cw[3] = {0, 0, 0};
+              cw[ka - p0] += tw[0];
+              cw[ka + 1 - p0] += tw[1];
+              cw[kb - p0] += tw[2];
+              cw[kb + 1 - p0] += tw[3];
+              hk[e] = int32_t(p0);
+              for (int t = 0; t < 3; ++t) hw[4 * e + size_t(t)] = float(cw[t]);
             }
         P->d_mt_k = to_device(ctx, hk);
         P->d_mt_w = to_device(ctx, hw);
