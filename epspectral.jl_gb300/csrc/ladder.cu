@@ -759,18 +759,24 @@ __global__ void y_split_kernel(const float* __restrict__ D, long ldD, int dsplit
   const long w = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (w >= Kp2) return;
   const long n = blockIdx.y, z = blockIdx.z;
+  float x[8];
+#pragma unroll
+  for (int r8 = 0; r8 < 8; ++r8) x[r8] = 0.f;
+  if (w < nw)
+    for (int p = 0; p < dsplits; ++p) {  // the 8 loads of a partial issued together
+      const float* src = D + z * 24 * nwp + w + ldD * n + dstride * p;
+#pragma unroll
+      for (int r8 = 0; r8 < 8; ++r8) {
+        const int qq = r8 % 2, c0 = (r8 / 2) % 2, ri = r8 / 4;
+        x[r8] += src[long(nwp) * ((qq == 0 ? 0 : 2) + 6 * (c0 + 2 * ri))];
+      }
+    }
 #pragma unroll
   for (int r8 = 0; r8 < 8; ++r8) {
-    const int qq = r8 % 2, c0 = (r8 / 2) % 2, ri = r8 / 4;
-    float x = 0.f;
-    if (w < nw) {
-      const long src = z * 24 * nwp + w + long(nwp) * ((qq == 0 ? 0 : 2) + 6 * (c0 + 2 * ri)) + ldD * n;
-      for (int p = 0; p < dsplits; ++p) x += D[src + dstride * p];
-    }
-    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    const __nv_bfloat16 h = __float2bfloat16_rn(x[r8]);
     const long o = z * 8 * N * Kp2 + (r8 + 8 * n) * Kp2 + w;
     Yh[o] = h;
-    Yl[o] = __float2bfloat16_rn(x - __bfloat162float(h));
+    Yl[o] = __float2bfloat16_rn(x[r8] - __bfloat162float(h));
   }
 }
 
