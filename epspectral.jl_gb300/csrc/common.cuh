@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -35,6 +36,30 @@ inline void cuda_check(cudaError_t e, const char* what, const char* file, int li
 
 // ---- context ----
 
+// Pinned host memory (page-locked: copies to and from it are direct DMA, without staging).
+struct HostPinned {
+  void* p = nullptr;
+  size_t bytes = 0;
+  void ensure(size_t n) {
+    if (n <= bytes) return;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    if (cudaHostAlloc(&p, n, cudaHostAllocDefault) != cudaSuccess) {
+      p = nullptr;
+      (void)cudaGetLastError();
+      fail(EPSP_ENOMEM, "page-locked host allocation of " + std::to_string(n) + " bytes failed");
+    }
+    bytes = n;
+  }
+  HostPinned() = default;
+  HostPinned(const HostPinned&) = delete;
+  HostPinned& operator=(const HostPinned&) = delete;
+  ~HostPinned() {
+    if (p) cudaFreeHost(p);
+  }
+};
+
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -48,6 +73,34 @@ struct Ctx {
   // Host-side test hook: the next allocation of at least `fail_alloc_bytes` fails (0 = off).
   size_t fail_alloc_bytes = 0;
   cudaEvent_t timer[2] = {nullptr, nullptr};
+  // host time spent in device allocations (for the set-up phase log)
+  double alloc_ms = 0;
+  long alloc_calls = 0;
+  // the g2 stream's double-buffered staging, kept for the next plan of this context
+  HostPinned g2_stage[2];
+};
+
+// Set-up phase log (verbosity >= 2): host milliseconds of each phase since the previous mark (the
+// stream synchronised, so device work is included) and of the device allocations in it, to stderr.
+struct PhaseLog {
+  Ctx* ctx;
+  const char* who;
+  bool on;
+  std::chrono::steady_clock::time_point t;
+  double a0;
+  long c0;
+  PhaseLog(Ctx* c, const char* w, int verbosity)
+      : ctx(c), who(w), on(verbosity >= 2), t(std::chrono::steady_clock::now()), a0(c->alloc_ms), c0(c->alloc_calls) {}
+  void mark(const char* phase) {
+    if (!on) return;
+    cudaStreamSynchronize(ctx->stream);
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "%s set-up: %-28s %8.2f ms (allocations %.2f ms in %ld)\n", who, phase,
+                 std::chrono::duration<double, std::milli>(now - t).count(), ctx->alloc_ms - a0, ctx->alloc_calls - c0);
+    t = now;
+    a0 = ctx->alloc_ms;
+    c0 = ctx->alloc_calls;
+  }
 };
 
 // Records the start event of a profiled launch; returns the pair index or -1.
@@ -106,7 +159,12 @@ struct DBuf {
       c->fail_alloc_bytes = 0;
       fail(EPSP_ENOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed (test hook)");
     }
+    const auto t0 = std::chrono::steady_clock::now();
     cudaError_t e = cudaMalloc(&p, bytes);
+    if (c) {
+      c->alloc_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      ++c->alloc_calls;
+    }
     if (e != cudaSuccess) {
       p = nullptr;
       (void)cudaGetLastError();
@@ -143,6 +201,10 @@ template <class T>
 DBuf<T> to_device(Ctx* c, const std::vector<T>& h) {
   return to_device(c, h.data(), h.size());
 }
+
+// The Kramers-Kronig matrix of a grid (src/frequency_grids.jl:30-44), built on the device into K
+// [n, n] (column-major) from the nodes padded by one spacing at either end; returns when K is made.
+void kk_matrix_to_device(Ctx* ctx, const std::vector<double>& nodes, DBuf<double>& K);
 
 inline unsigned div_up(size_t a, size_t b) { return unsigned((a + b - 1) / b); }
 

@@ -3,18 +3,13 @@
 
 #include <algorithm>
 #include <cstring>
+#include <thread>
 
 namespace epsp {
 
 size_t g2_elem_bytes(int dtype) { return dtype == EPSP_F64 ? 8 : (dtype == EPSP_F32 ? 4 : 2); }
 
 namespace {
-struct PinnedBuf {
-  void* p = nullptr;
-  ~PinnedBuf() {
-    if (p) cudaFreeHost(p);
-  }
-};
 struct Events {
   cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaStream_t copy = nullptr;
@@ -46,30 +41,45 @@ void stream_g2_by_columns(Ctx* ctx, const epsp_model* m, const std::vector<int32
   const long nchunk = long(cb.size()) - 1;
   const size_t bytes = size_t(std::max<long>(maxm, 1)) * slab;
   cudaStream_t s = ctx->stream;
-  PinnedBuf host[2];
+  HostPinned* host = ctx->g2_stage;  // kept by the context for the next plan
   DBuf<uint8_t> dev[2];
   Events ev;
   EPSP_CUDA(cudaStreamCreateWithFlags(&ev.copy, cudaStreamNonBlocking));
   for (auto& e : ev.e) EPSP_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   const int nb = nchunk > 1 ? 2 : 1;
   for (int b = 0; b < nb; ++b) {
-    if (cudaHostAlloc(&host[b].p, bytes, cudaHostAllocDefault) != cudaSuccess) {
-      (void)cudaGetLastError();
-      fail(EPSP_ENOMEM, "page-locked staging of " + std::to_string(bytes) + " bytes for the g2 stream failed");
-    }
+    host[b].ensure(bytes);
     dev[b].alloc(ctx, bytes);
   }
+  // the star-order gather of a chunk into the staging buffer, over up to 16 host threads
+  const int nthreads = int(std::clamp<unsigned>(std::thread::hardware_concurrency(), 1u, 16u));
+  auto gather = [&](uint8_t* dst, long p0, long p1) {
+    const auto* src = static_cast<const uint8_t*>(m->g2);
+    auto part = [&](long a, long b) {
+      for (long p = a; p < b; ++p) std::memcpy(dst + size_t(p - p0) * slab, src + size_t(order[size_t(p)]) * slab, slab);
+    };
+    const long n = p1 - p0;
+    if (nthreads == 1 || size_t(n) * slab < (size_t(8) << 20)) {
+      part(p0, p1);
+      return;
+    }
+    const long per = (n + nthreads - 1) / nthreads;
+    std::vector<std::thread> th;
+    for (int t = 0; t < nthreads; ++t) {
+      const long a = p0 + t * per, b = std::min(p1, a + per);
+      if (a < b) th.emplace_back(part, a, b);
+    }
+    for (auto& x : th) x.join();
+  };
   cudaEvent_t* copied = ev.e;
   cudaEvent_t* consumed = ev.e + 2;
-  const auto* g2 = static_cast<const uint8_t*>(m->g2);
   for (long k = 0; k < nchunk; ++k) {
     const int b = int(k % nb);
     const long c0 = cb[size_t(k)], c1 = cb[size_t(k + 1)];
     const long p0 = cptr[size_t(c0)], p1 = cptr[size_t(c1)];
     // the staging buffer's previous copy must be done before it is refilled
     if (k >= nb) EPSP_CUDA(cudaEventSynchronize(copied[b]));
-    auto* dst = static_cast<uint8_t*>(host[b].p);
-    for (long p = p0; p < p1; ++p) std::memcpy(dst + size_t(p - p0) * slab, g2 + size_t(order[size_t(p)]) * slab, slab);
+    gather(static_cast<uint8_t*>(host[b].p), p0, p1);
     // the device buffer's previous chunk must be consumed before it is overwritten
     if (k >= nb) EPSP_CUDA(cudaStreamWaitEvent(ev.copy, consumed[b], 0));
     EPSP_CUDA(cudaMemcpyAsync(dev[b].p, host[b].p, size_t(p1 - p0) * slab, cudaMemcpyHostToDevice, ev.copy));

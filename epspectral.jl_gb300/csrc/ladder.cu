@@ -1183,6 +1183,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
   P->ws = make_grid(m->omegas, "omegas");
   P->nw = P->ws.n;
   P->h = P->ws.unit;
+  PhaseLog plog(ctx, "ladder", opts->verbosity);
   const long nm = P->nm, ni = P->ni, nf = P->nf, nw = P->nw;
   // nshift = ceil(max ωph / dω_unit) + 2 (src/ladder.jl:151)
   double mx = -std::numeric_limits<double>::infinity();
@@ -1199,24 +1200,8 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
   P->d_eps_i = to_device(ctx, m->eps_i, size_t(ni));
   P->d_v = to_device(ctx, m->v, size_t(3 * ni));
   // KK (src/frequency_grids.jl:30-44), through the same device builder as the scGD0 plan
-  {
-    const auto& w = P->ws.nodes;
-    std::vector<double> xs(size_t(nw + 2));
-    xs[0] = w[0] - (w[1] - w[0]);
-    for (long j = 0; j < nw; ++j) xs[size_t(j + 1)] = w[size_t(j)];
-    xs[size_t(nw + 1)] = w[size_t(nw - 1)] + (w[size_t(nw - 1)] - w[size_t(nw - 2)]);
-    // K[i, j] = lskk(xs[i+1], xs[j], xs[j+1], xs[j+2]) / π on the host (setup, O(nω²))
-    std::vector<double> K(size_t(nw * nw));
-    auto xlogx = [](double x) { return x == 0 ? 0.0 : x * std::log(std::fabs(x)); };
-    for (long j = 0; j < nw; ++j)
-      for (long i = 0; i < nw; ++i) {
-        double x = xs[size_t(i + 1)], x1 = xs[size_t(j)], x2 = xs[size_t(j + 1)], x3 = xs[size_t(j + 2)];
-        K[size_t(i + nw * j)] = (xlogx(x1 - x) / (x2 - x1) - xlogx(x2 - x) * (x3 - x1) / (x2 - x1) / (x3 - x2) +
-                                 xlogx(x3 - x) / (x3 - x2)) /
-                                3.14159265358979323846;
-      }
-    P->d_KK = to_device(ctx, K);
-  }
+  kk_matrix_to_device(ctx, P->ws.nodes, P->d_KK);
+  plog.mark("grid, KK matrix");
   // stars: sortperm(f_to_i) (stable) and the cumulative star sizes (src/ladder.jl:144-149)
   std::vector<int32_t> by_star(static_cast<size_t>(nf));
   for (long f = 0; f < nf; ++f) by_star[size_t(f)] = int32_t(f);
@@ -1327,12 +1312,13 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
     P->Kx = P->nmp * 3 * ni;
     P->d_Gt.alloc(ctx, size_t(P->Kx * 3 * ni));
     P->d_Gt.zero(s);
+    plog.mark("stars, shift tables");
     // G̃ needs g2 once: it streams through the device star by star (gpu_tile inner states per chunk,
-    // or up to 1 GiB of g2), copies overlapped with the sums; g2 stays in the caller's memory
+    // or about 64 MiB of g2), copies overlapped with the sums; g2 stays in the caller's memory
     {
       const size_t member_bytes = size_t(nm * ni) * g2_elem_bytes(m->g2_dtype);
       const long chunk_f =
-          opts->gpu_tile > 0 ? long(opts->gpu_tile) : std::max<long>(1, long((size_t(1) << 30) / member_bytes));
+          opts->gpu_tile > 0 ? long(opts->gpu_tile) : std::max<long>(1, long((size_t(64) << 20) / member_bytes));
       const unsigned grid = div_up(size_t(nm * ni), 128);
       stream_g2_by_columns(ctx, m, by_star, sp, chunk_f, [&](const void* g2c, long c0, long c1, long p0) {
         if (m->g2_dtype == EPSP_F64)
@@ -1356,6 +1342,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
     if (P->path == EPSP_PATH_GEMM_FP64) {
       P->d_Af.alloc(ctx, size_t(M * P->Kx));
     } else {
+      plog.mark("g2 streamed, G~ built");
       // mode tables: for node j, mode ν and sign s, the two shift tables (m_ν, m_ν + 1) with the
       // tent weights (1 - r_ν, r_ν) folded into their interpolation weights (FP32). The two tables'
       // lower nodes differ by at most one (the grid's spacing is a multiple of its unit, the shift
@@ -1411,6 +1398,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       split_rows_plain_kernel<<<div_up(size_t(N * P->Kp), 256), 256, 0, s>>>(P->d_Gt.p, N, P->Kx, P->Kx, P->Kp, P->d_Gh.p,
                                                                               P->d_Gl.p);
       EPSP_LAUNCHED(ctx);
+      plog.mark("mode tables, operand buffers");
       // the contraction's tile shape: the autotuner times the candidates on these operands (A
       // zeroed) and keeps the fastest; the partial buffer holds the largest split count tried
       int bn_h = 128, sp_h = 1;
@@ -1441,6 +1429,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       P->d_err.download(&terr, 1, s);
       EPSP_CUDA(cudaStreamSynchronize(s));
       if (terr) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out while tuning (bounded device wait)");
+      plog.mark("tile shape (autotuner or cache)");
       // the Kramers-Kronig image on the tensor cores: A = KK [nω][nω'], B = Y [8N][nω']
       P->d_KKh.alloc(ctx, size_t(nw * P->Kp2));
       P->d_KKl.alloc(ctx, size_t(nw * P->Kp2));
@@ -1477,6 +1466,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
   P->d_jp.alloc(ctx, size_t(nw));
   P->d_tm.alloc(ctx, size_t(nw));
   P->d_tp.alloc(ctx, size_t(nw));
+  plog.mark("KK operands, per-(T, Ω) buffers");
   return guard.release();
 }
 

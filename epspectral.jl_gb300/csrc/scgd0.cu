@@ -41,6 +41,20 @@ __global__ void kk_build_kernel(const double* __restrict__ xs, int n, double* __
   K[idx] = v / 3.14159265358979323846;
 }
 
+void kk_matrix_to_device(Ctx* ctx, const std::vector<double>& w, DBuf<double>& K) {
+  const long n = long(w.size());
+  if (n < 2) fail(EPSP_EINVAL, "the Kramers-Kronig matrix needs at least two nodes");
+  std::vector<double> xs(size_t(n + 2));
+  xs[0] = w[0] - (w[1] - w[0]);
+  for (long j = 0; j < n; ++j) xs[size_t(j + 1)] = w[size_t(j)];
+  xs[size_t(n + 1)] = w[size_t(n - 1)] + (w[size_t(n - 1)] - w[size_t(n - 2)]);
+  auto d_xs = to_device(ctx, xs);
+  K.alloc(ctx, size_t(n * n));
+  kk_build_kernel<<<div_up(size_t(n * n), 256), 256, 0, ctx->stream>>>(d_xs.p, int(n), K.p);
+  EPSP_LAUNCHED(ctx);
+  EPSP_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
 // g2 [nm, ni, nf] (any storage type) -> g2_t [nm, nf, ni] double (src/scgd0.jl:275-278), and
 // ωq_t[ν, f, i] = ωph[ν, iq_kk[iks_i[i], iks_f[f]]] (gather_pair_table!, src/scgd0.jl:270).
 
@@ -856,6 +870,7 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
   P->W = m->W;
   P->nstates_base = m->nstates_base;
   P->gpu_tile = opts->gpu_tile;
+  PhaseLog plog(ctx, "scgd0", P->verbosity);
   cudaStream_t s = ctx->stream;
   // grid tables
   CellTableHost ct = make_cell_table(P->ws);
@@ -890,19 +905,8 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
     P->d_mptr = to_device(ctx, m->mult_ptr, size_t(m->nmult + 1));
     P->d_midx = to_device(ctx, m->mult_idx, size_t(m->mult_ptr[m->nmult]));
   }
-  // Kramers-Kronig matrix on the device from the padded nodes (src/frequency_grids.jl:30-44).
-  {
-    const auto& w = P->ws.nodes;
-    std::vector<double> xs(size_t(P->nw + 2));
-    xs[0] = w[0] - (w[1] - w[0]);
-    for (int64_t j = 0; j < P->nw; ++j) xs[size_t(j + 1)] = w[size_t(j)];
-    xs[size_t(P->nw + 1)] = w[size_t(P->nw - 1)] + (w[size_t(P->nw - 1)] - w[size_t(P->nw - 2)]);
-    auto d_xs = to_device(ctx, xs);
-    P->d_KK.alloc(ctx, size_t(P->nw * P->nw));
-    kk_build_kernel<<<div_up(size_t(P->nw * P->nw), 256), 256, 0, s>>>(d_xs.p, int(P->nw), P->d_KK.p);
-    EPSP_LAUNCHED(ctx);
-    EPSP_CUDA(cudaStreamSynchronize(s));
-  }
+  plog.mark("grid tables");
+  kk_matrix_to_device(ctx, P->ws.nodes, P->d_KK);
   const long nm = m->nm, ni = m->ni, nf = m->nf;
   if (P->path == EPSP_PATH_DIRECT_FP64) {
     // nf_chunk of src/scgd0.jl:201-202; the chunks fix the order of the f sum.
@@ -970,12 +974,13 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
     auto d_cptr = to_device(ctx, cptr);
     auto d_mem = to_device(ctx, members);
     auto d_wf = to_device(ctx, m->w_f, size_t(nf));
+    plog.mark("KK matrix, column sets");
     // The coupling sums need g2 once: it streams through the device in star order, gpu_tile inner
-    // states per chunk (or up to 1 GiB of g2 per chunk), copies overlapped with the sums; g2
+    // states per chunk (or about 64 MiB of g2 per chunk), copies overlapped with the sums; g2
     // stays in the caller's host memory.
     P->d_G.alloc(ctx, size_t(nm * P->nc * ni));
     const size_t member_bytes = size_t(nm * ni) * g2_elem_bytes(m->g2_dtype);
-    const long chunk_f = opts->gpu_tile > 0 ? long(opts->gpu_tile) : std::max<long>(1, long((size_t(1) << 30) / member_bytes));
+    const long chunk_f = opts->gpu_tile > 0 ? long(opts->gpu_tile) : std::max<long>(1, long((size_t(64) << 20) / member_bytes));
     const unsigned grid = div_up(size_t(nm * ni), 128);
     stream_g2_by_columns(ctx, m, members, cptr, chunk_f, [&](const void* g2c, long c0, long c1, long p0) {
       if (m->g2_dtype == EPSP_F64)
@@ -990,6 +995,7 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
                                                                 P->d_G.p);
       EPSP_LAUNCHED(ctx);
     });
+    plog.mark("g2 streamed, coupling sums");
     // The cells of ω ± ω_ν, by the lookup of _interp_linear_grid (src/frequency_grids.jl:207-219):
     // the value there is (1 - t) Σ[j] + t Σ[j + 1], which is Σ[0] below the grid (t = 0) and Σ[end]
     // above it (t = 1).
@@ -1032,6 +1038,7 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
   } else {
     fail(EPSP_EINVAL, "unknown path");
   }
+  plog.mark("cells, tensor-core operands");
   // iteration buffers
   P->d_Sin.alloc(ctx, size_t(P->nw * ni));
   P->d_ImS.alloc(ctx, size_t(P->nw * ni));
@@ -1039,6 +1046,7 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
   P->d_A.alloc(ctx, size_t(P->nwa * ni));
   P->d_colsum.alloc(ctx, size_t(ni));
   P->d_D.alloc(ctx, size_t(P->nwa));
+  plog.mark("iteration buffers");
   return guard.release();
 }
 

@@ -13,23 +13,6 @@ struct TParams {
   int holes, pad;
 };
 
-// Pinned host memory (page-locked: small copies to and from it are direct DMA, without staging).
-struct HostPinned {
-  void* p = nullptr;
-  size_t bytes = 0;
-  void ensure(size_t n) {
-    if (n <= bytes) return;
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    bytes = 0;
-    EPSP_CUDA(cudaHostAlloc(&p, n, cudaHostAllocDefault));
-    bytes = n;
-  }
-  ~HostPinned() {
-    if (p) cudaFreeHost(p);
-  }
-};
-
 struct Scgd0Plan {
   Ctx* ctx = nullptr;
   int path = EPSP_PATH_DIRECT_FP64;

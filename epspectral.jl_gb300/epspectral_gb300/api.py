@@ -179,7 +179,8 @@ class Scgd0Plan:
 
     def __init__(self, setup, *, path="direct_fp64", gpu_tile=None, omega_acoustic, ctx: Context | None = None,
                  verbosity=0):
-        """verbosity >= 2 logs each iteration (err, μ, μ-solve evaluations per temperature) to stderr."""
+        """verbosity >= 2 logs the set-up phases' times and each iteration (err, μ, μ-solve evaluations
+        per temperature) to stderr."""
         self.ctx = ctx or default_context()
         self.M = ModelArrays(setup)
         self.setup = setup
@@ -264,13 +265,15 @@ def loop_scgd0(setup, occ, *, eta_init, tol, maxiter=20, eta_min=None, fix_mu=Fa
 class LadderPlan:
     """Device-resident tables of one ladder setup (_setup_ladder + _ladder_workspace)."""
 
-    def __init__(self, setup, *, path="direct_fp64", gpu_tile=None, omega_acoustic, ctx: Context | None = None):
+    def __init__(self, setup, *, path="direct_fp64", gpu_tile=None, omega_acoustic, ctx: Context | None = None,
+                 verbosity=0):
+        """verbosity >= 2 logs the set-up phases' times to stderr."""
         if not (omega_acoustic > 0):
             raise ArgumentError(f"ω_acoustic must be positive, got {omega_acoustic}: the shift-grid coupling build "
                                 "has no row for a negative phonon frequency")
         self.ctx = ctx or default_context()
         self.M = ModelArrays(setup)
-        self.opts = _options(path, gpu_tile, omega_acoustic)
+        self.opts = _options(path, gpu_tile, omega_acoustic, verbosity)
         self.handle = C.c_void_p()
         self.ctx.check(lib().epsp_ladder_setup(self.ctx.handle, C.byref(self.M.struct), C.byref(self.opts),
                                                C.byref(self.handle)))
