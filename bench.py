@@ -42,15 +42,18 @@ T_K = 300.0
 ETA_INIT, TOL, MAXITER = 0.01, 1e-6, 50
 OMEGA, L_RTOL, L_MAXITER = 0.1, 1e-2, 30
 W_AC = 1e-4
+# The ladder contraction's precision on the timed path: one TF32 product (operands rounded to TF32,
+# FP32 accumulation); the BF16x3 path is timed beside it. scGD0 stays on BF16x3 split precision.
+LADDER_PATH = "gemm_tf32"
 # Iteration counts of this workload on the FP64 path (scGD0 iterations to tol, ladder operator
 # applications per Ω: GMRES iterations plus none for a cold start), measured on a GB300 by this
 # script's FP64 leg; the reference arm, which cannot run the workload to the end on the CPU, times
 # bounded samples and scales them by these counts.
 FP64_SCGD0_ITERS = 12
 FP64_LADDER_APPLIES = 2
-# DRAM bytes (read + write) of one ladder-contraction launch of this workload, from one Nsight
-# Compute capture of the same kernel on a GB300 (profiles/tc_ladder_gemm_c2.md)
-TC_LADDER_TRAFFIC_BYTES = 4.414e9 + 0.350e9
+# DRAM bytes (read + write) of one ladder-contraction launch of this workload (the TF32 kernel),
+# from one Nsight Compute capture of the same kernel on a GB300 (profiles/tc_ladder_gemm_c2.md)
+TC_LADDER_TRAFFIC_BYTES = 4.413e9 + 0.350e9
 # learned warm start: training and held-out runs, epochs
 WARM_TRAIN_RUNS, WARM_HELDOUT_RUNS, WARM_EPOCHS = 256, 32, 40
 
@@ -68,7 +71,8 @@ def bench_config(s, world) -> dict:
     """The workload, the same on both arms."""
     return dict(workload="3-band cubic t2g nk=16^3, 495 outer / 12288 inner states, 15 modes, graded "
                          "1251-node grid, T=300 K; scGD0 to 1e-6 eV + ladder at one Omega=0.1 eV",
-                ni=int(s["eps_i"].size), nf=int(s["eps_f"].size), nw=len(s["omegas"]), nm=15, path="gemm_bf16",
+                ni=int(s["eps_i"].size), nf=int(s["eps_f"].size), nw=len(s["omegas"]), nm=15,
+                path=f"scgd0 gemm_bf16, ladder {LADDER_PATH}",
                 warm_start=True, l2="flushed between steps (512 MB write)", parallelism=f"replicas x{world}")
 
 
@@ -306,7 +310,7 @@ def run_ours(args, world, rank, local):
     if args.save_warm:
         ws.save(args.save_warm)
     sp = api.Scgd0Plan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
-    lp = api.LadderPlan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
+    lp = api.LadderPlan(s, path=LADDER_PATH, omega_acoustic=W_AC, ctx=ctx)
     nw, ni = len(s["omegas"]), s["eps_i"].size
 
     def step():
@@ -341,7 +345,9 @@ def run_ours(args, world, rank, local):
     value = total / (args.steps * world)
     out = dict(metric=METRIC, value=value, unit="s", n_gpus=world, steps=args.steps, warmup=args.warmup,
                ms_per_step=1e3 * total / args.steps, higher_is_better=False,
-               scaling="weak", vs_baseline=None, dtype="bf16x3 GEMMs (fp32 accumulate), fp64 reductions",
+               scaling="weak", vs_baseline=None,
+               dtype="scGD0: bf16x3 GEMMs; ladder: tf32 contraction, bf16x3 Kramers-Kronig product (fp32 accumulate); "
+                     "fp64 reductions",
                data="synthetic (seeded 3-band t2g model, log-normal g2)",
                config=bench_config(s, world))
     if rank != 0:
@@ -365,12 +371,16 @@ def run_ours(args, world, rank, local):
         flops = 2.0 * M * N * K
         burst, sust, hbm, src = peaks()
         achieved = flops / avg_s / 1e12
-        out["roofline"] = dict(kernel="tc_gemm_bf16 (ladder contraction)", bound="tensor", achieved=achieved,
-                               peak=sust, unit="TFLOP/s", frac=achieved / sust, traffic=TC_LADDER_TRAFFIC_BYTES,
+        # TF32 runs at half the BF16 rate (BF16x3: three products per useful flop), so the tensor
+        # pipe's load against the BF16 peak is 2x (3x) the useful fraction
+        per_flop = 2 if LADDER_PATH == "gemm_tf32" else 3
+        out["roofline"] = dict(kernel=f"tc_gemm {LADDER_PATH[5:]} (ladder contraction)", bound="tensor",
+                               achieved=achieved, peak=sust, unit="TFLOP/s", frac=achieved / sust,
+                               traffic=TC_LADDER_TRAFFIC_BYTES,
                                traffic_source="ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
                                               "(profiles/tc_ladder_gemm_c2.md)",
                                peak_source=f"{src} bf16 sustained", launches=prof_n, avg_ms=1e3 * avg_s,
-                               flops_per_launch=flops, tensor_pipe_frac=3 * achieved / sust)
+                               flops_per_launch=flops, tensor_pipe_frac=per_flop * achieved / sust)
     out["clocks"] = clk.summary()
     # end to end through the public API from host arrays
     t0 = time.perf_counter()
@@ -378,7 +388,7 @@ def run_ours(args, world, rank, local):
     r_e = sp_e.run(occ, eta_init=ETA_INIT, tol=TOL, maxiter=MAXITER, mu_start=[mu0], warm=ws)
     sp_e.close()
     l_e = api.loop_ladder(s, r_e["sigma"], r_e["mu"], [T], [OMEGA], rtol=L_RTOL, maxiter=L_MAXITER,
-                          omega_acoustic=W_AC, path="gemm_bf16", ctx=ctx)
+                          omega_acoustic=W_AC, path=LADDER_PATH, ctx=ctx)
     e2e = time.perf_counter() - t0
     out["e2e"] = dict(value=e2e, unit="s", h2d_bytes_per_step=2 * setup_bytes(s) + 16 * nw * ni,
                       d2h_bytes_per_step=16 * nw * ni + 8 * 9 * 2)
@@ -396,6 +406,17 @@ def run_ours(args, world, rank, local):
     plain["recast_fp64_ladder_s_per_omega"] = ctx.timer_end() / 1e3
     plain["fp64_ladder_gmres_iters"] = int(l64["niter"][0, 0])
     lp64.close()
+    # the BF16x3 ladder on the same Σ as the timed TF32 one (median of 5 runs)
+    lpb = api.LadderPlan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
+    tb = []
+    for _ in range(6):
+        ctx.timer_begin()
+        lb = lpb.run(r["sigma"], r["mu"], [T], [OMEGA], rtol=L_RTOL, maxiter=L_MAXITER)
+        tb.append(ctx.timer_end() / 1e3)
+    out["ladder_bf16x3"] = dict(s_per_omega=float(np.median(tb[1:])), gemm=lpb.gemm_config(),
+                                rel_sigma_vs_timed_path=float(np.linalg.norm(lb["sigma_ladder"] - l["sigma_ladder"]) /
+                                                              np.linalg.norm(lb["sigma_ladder"])))
+    lpb.close()
     dp = api.Scgd0Plan(s, path="direct_fp64", omega_acoustic=W_AC, ctx=ctx)
     ctx.timer_begin()
     dp.run(occ, eta_init=ETA_INIT, tol=0.0, maxiter=1, mu_start=[mu0])
@@ -441,7 +462,7 @@ def batched_c3(s, ctx, ws) -> dict:
         t_single += ctx.timer_end() / 1e3
         it_single.append(int(r1["iters_total"]))
     sp.close()
-    lp = api.LadderPlan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
+    lp = api.LadderPlan(s, path=LADDER_PATH, omega_acoustic=W_AC, ctx=ctx)
     ctx.timer_begin()
     lb = lp.run(r8["sigma"], r8["mu"], Ts, Om, rtol=L_RTOL, maxiter=L_MAXITER, batch_rhs=8)
     t_lb = ctx.timer_end() / 1e3

@@ -74,11 +74,13 @@ struct LadderPlan {
   DBuf<int32_t> d_mnu;
   DBuf<double> d_rnu, d_nnu;
   DBuf<__nv_bfloat16> d_Ah, d_Al, d_Gh, d_Gl;
+  DBuf<float> d_At, d_Gtf;  // GEMM_TF32: A and G̃ as TF32-rounded FP32, rows of Kp
   DBuf<float> d_part;
   DBuf<int> d_err;
   TcOperand opA{}, opG{}, opA64{}, opG128{}, opG256{}, opA32{}, opG256_32{};
   int bn = 128, splits = 1, bk = kTcBK;  // the contraction's tile shape, picked by the autotuner at setup
   bool persist = false;                  // ... and whether it runs as the persistent kernel
+  int cm = 1;                            // ... in clusters of cm CTAs sharing the B tile
   std::vector<TcTune> tune_all;
   float tune_ms_heuristic = 0.f;
   // exchange (both paths)
@@ -591,18 +593,20 @@ __global__ void xgen_f64_kernel(const double2* __restrict__ J, const int32_t* __
 // nodes can reach (nodes j0 - W .. j0 + 32 + W, W = nshift + 2, zero outside the grid) in shared
 // memory; each thread holds the mode-table entries it needs (two shift tables per mode and sign,
 // with the tent weights folded in) in registers. Tiles are transposed through shared memory so
-// that the BF16 rows are written 16 bytes at a time.
+// that the BF16 rows are written 16 bytes at a time. With kTf32 the operand is one FP32 matrix At
+// of TF32-rounded values (the same 4 bytes per element) instead of the BF16 hi/lo pair.
 constexpr int kXgTiles = 8;
 constexpr int kXgPreMax = 8;  // prefetch slots per thread: windows of up to 4 x 512 values (nshift <= 222)
 
 // Batched over blockIdx.z: slot z makes the rows z 24 nwp.. of A from the vertex J + jstride r and
 // the occupations nnu + 16 r of right-hand side r = rmap[z] (r = z without rmap).
-template <int kXgPre>
+template <int kXgPre, bool kTf32>
 __global__ void __launch_bounds__(256) xgen_bf16_kernel(const float2* __restrict__ J_all, long jstride,
                                                         const int* __restrict__ rmap, const int32_t* __restrict__ mt_k,
                                                         const float* __restrict__ mt_w, const float* __restrict__ nnu_all,
                                                         int nw, int nwp, int ns, int nmp, int ni, long Kx, long Kp,
-                                                        __nv_bfloat16* __restrict__ Ah, __nv_bfloat16* __restrict__ Al) {
+                                                        __nv_bfloat16* __restrict__ Ah, __nv_bfloat16* __restrict__ Al,
+                                                        float* __restrict__ At) {
   extern __shared__ float xg_smem[];
   const int rhs = rmap ? rmap[blockIdx.z] : int(blockIdx.z);
   const float2* J = J_all + jstride * rhs;
@@ -707,6 +711,22 @@ __global__ void __launch_bounds__(256) xgen_bf16_kernel(const float2* __restrict
     // 8 x 4 split of the warp avoids the 2-way bank conflicts of the transposed reads but writes
     // 64-byte segments, and measured slower)
     const int wr = threadIdx.x / 8, kc = (threadIdx.x % 8) * 8;
+    if constexpr (kTf32) {
+      // FP32 rows: 8 lanes cover 128 contiguous bytes per store (columns kq.. and 32 + kq..); the
+      // transposed reads are conflict-free in this order
+      const int kq = (threadIdx.x % 8) * 4;
+      for (int t4 = 0; t4 < 2 * nq; ++t4) {
+        const int q = qbase + t4 / 2, ri = t4 % 2;
+        const float4 lo = make_float4(round_tf32(tile[t4][kq][wr]), round_tf32(tile[t4][kq + 1][wr]),
+                                      round_tf32(tile[t4][kq + 2][wr]), round_tf32(tile[t4][kq + 3][wr]));
+        const float4 hi = make_float4(round_tf32(tile[t4][32 + kq][wr]), round_tf32(tile[t4][33 + kq][wr]),
+                                      round_tf32(tile[t4][34 + kq][wr]), round_tf32(tile[t4][35 + kq][wr]));
+        const long row = row_base + long(q + 6 * (c0 + 2 * ri)) * nwp + j0 + wr;
+        const long off = row * Kp + k0 + kq;
+        *reinterpret_cast<float4*>(At + off) = lo;
+        *reinterpret_cast<float4*>(At + off + 32) = hi;
+      }
+    } else
     for (int t4 = 0; t4 < 2 * nq; ++t4) {
       const int q = qbase + t4 / 2, ri = t4 % 2;
       __align__(16) __nv_bfloat16 hh[8], ll[8];
@@ -733,13 +753,20 @@ static int xgen_pre(long ns) {
 }
 
 // xgen_bf16_kernel with the fewest prefetch slots that hold the window.
-template <class... A>
-static void launch_xgen(long ns, dim3 grid, size_t smem, cudaStream_t s, A... args) {
+template <bool kTf32, class... A>
+static void launch_xgen_t(long ns, dim3 grid, size_t smem, cudaStream_t s, A... args) {
   switch (xgen_pre(ns)) {
-    case 2: xgen_bf16_kernel<2><<<grid, 256, smem, s>>>(args...); break;
-    case 4: xgen_bf16_kernel<4><<<grid, 256, smem, s>>>(args...); break;
-    default: xgen_bf16_kernel<8><<<grid, 256, smem, s>>>(args...); break;
+    case 2: xgen_bf16_kernel<2, kTf32><<<grid, 256, smem, s>>>(args...); break;
+    case 4: xgen_bf16_kernel<4, kTf32><<<grid, 256, smem, s>>>(args...); break;
+    default: xgen_bf16_kernel<8, kTf32><<<grid, 256, smem, s>>>(args...); break;
   }
+}
+template <class... A>
+static void launch_xgen(bool tf32, long ns, dim3 grid, size_t smem, cudaStream_t s, A... args) {
+  if (tf32)
+    launch_xgen_t<true>(ns, grid, smem, s, args...);
+  else
+    launch_xgen_t<false>(ns, grid, smem, s, args...);
 }
 
 static size_t xgen_smem_bytes(int ns) {
@@ -790,6 +817,15 @@ __global__ void split_rows_plain_kernel(const double* __restrict__ S, long rows,
   __nv_bfloat16 h = __float2bfloat16_rn(x);
   oh[idx] = h;
   ol[idx] = __float2bfloat16_rn(x - __bfloat162float(h));
+}
+
+// out[r * Kp + c] = S[c + ld r] rounded to TF32 (0 past cols): the TF32 form of split_rows_plain.
+__global__ void round_rows_tf32_kernel(const double* __restrict__ S, long rows, long cols, long ld, long Kp,
+                                       float* __restrict__ out) {
+  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= rows * Kp) return;
+  long r = idx / Kp, c = idx % Kp;
+  out[idx] = c < cols ? round_tf32(float(S[c + ld * r])) : 0.f;
 }
 
 // out[r * Kp + c] = split(S[r + ldr c]) for c < cols (a column-major matrix read by rows).
@@ -1135,6 +1171,32 @@ static void check_ladder_model(const epsp_model* m) {
     if (m->iq_kk[k] < 0 || m->iq_kk[k] >= m->nq) fail(EPSP_EINVAL, "iq_kk out of range");
 }
 
+// The tensor-core paths: the contraction on tcgen05 (BF16x3 or TF32), FP32 vertices.
+static bool tc_path(int path) { return path == EPSP_PATH_GEMM_BF16 || path == EPSP_PATH_GEMM_TF32; }
+
+static TcOperand one_part_tf32(const float* a, long rows, long cols, long ld, int box_rows, int bk = 32) {
+  TcOperand op;
+  op.ns = 1;
+  op.bk = bk;
+  op.tf32 = true;
+  op.m[0] = make_tmap_f32(a, rows, cols, ld, box_rows, bk);
+  op.m[1] = op.m[0];
+  op.m[2] = op.m[0];
+  op.base[0] = op.base[1] = op.base[2] = a;
+  op.rows = rows;
+  op.cols = cols;
+  op.ld = ld;
+  return op;
+}
+
+// The contraction's operands for the plan's tile shape: BF16x3 maps with K boxes of 64 (opA64,
+// opG128, opG256) or 32 (opA32, opG256_32); TF32 maps have K boxes of 32 only.
+static void pick_contraction_operands(LadderPlan* P) {
+  const bool narrow = P->path == EPSP_PATH_GEMM_BF16 && P->bk == 32;
+  P->opA = narrow ? P->opA32 : P->opA64;
+  P->opG = narrow ? P->opG256_32 : (P->bn == 256 ? P->opG256 : P->opG128);
+}
+
 static TcOperand two_part(const void* hi, const void* lo, long rows, long cols, long ld, int box_rows, int bk = kTcBK) {
   TcOperand op;
   op.ns = 2;
@@ -1142,6 +1204,11 @@ static TcOperand two_part(const void* hi, const void* lo, long rows, long cols, 
   op.m[0] = make_tmap_bf16(hi, rows, cols, ld, box_rows, bk);
   op.m[1] = make_tmap_bf16(lo, rows, cols, ld, box_rows, bk);
   op.m[2] = op.m[0];
+  op.base[0] = op.base[2] = hi;
+  op.base[1] = lo;
+  op.rows = rows;
+  op.cols = cols;
+  op.ld = ld;
   return op;
 }
 
@@ -1277,7 +1344,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
     P->d_Cp.alloc(ctx, size_t(16 * nw * 6 * ni));
     P->d_Cm.alloc(ctx, size_t(16 * nw * 6 * ni));
     EPSP_CUDA(cudaStreamSynchronize(s));
-  } else if (P->path == EPSP_PATH_GEMM_FP64 || P->path == EPSP_PATH_GEMM_BF16) {
+  } else if (P->path == EPSP_PATH_GEMM_FP64 || tc_path(P->path)) {
     P->wnu.assign(size_t(nm), 0.0);
     for (long nu = 0; nu < nm; ++nu) {
       double w0 = m->omega_ph[nu];
@@ -1305,8 +1372,8 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
     auto d_wnu = to_device(ctx, P->wnu);
     P->nwp = (nw + 31) / 32 * 32;
     P->nmp = (nm + 15) / 16 * 16;
-    if (P->path == EPSP_PATH_GEMM_BF16 && P->nmp != 16)
-      fail(EPSP_EUNSUPPORTED, "the BF16x3 ladder path takes at most 16 modes; use EPSP_PATH_GEMM_FP64");
+    if (tc_path(P->path) && P->nmp != 16)
+      fail(EPSP_EUNSUPPORTED, "the tensor-core ladder paths take at most 16 modes; use EPSP_PATH_GEMM_FP64");
     if (6 * ni > 65535)  // the channel-algebra kernels put (a, c0, i) on the grid's y dimension
       fail(EPSP_EUNSUPPORTED, "the GEMM ladder paths take at most 10922 outer states");
     P->Kx = P->nmp * 3 * ni;
@@ -1338,7 +1405,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       });
     }
     const long M = 24 * P->nwp, N = 3 * ni;
-    if (P->path != EPSP_PATH_GEMM_BF16) P->d_D.alloc(ctx, size_t(M * N));  // the tensor-core path keeps D as split-K parts
+    if (!tc_path(P->path)) P->d_D.alloc(ctx, size_t(M * N));  // the tensor-core paths keep D as split-K parts
     if (P->path == EPSP_PATH_GEMM_FP64) {
       P->d_Af.alloc(ctx, size_t(M * P->Kx));
     } else {
@@ -1391,12 +1458,20 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       }
       P->Kp = (P->Kx + 63) / 64 * 64;
       P->Kp2 = (nw + 63) / 64 * 64;
-      P->d_Ah.alloc(ctx, size_t(M * P->Kp));
-      P->d_Al.alloc(ctx, size_t(M * P->Kp));
-      P->d_Gh.alloc(ctx, size_t(N * P->Kp));
-      P->d_Gl.alloc(ctx, size_t(N * P->Kp));
-      split_rows_plain_kernel<<<div_up(size_t(N * P->Kp), 256), 256, 0, s>>>(P->d_Gt.p, N, P->Kx, P->Kx, P->Kp, P->d_Gh.p,
-                                                                              P->d_Gl.p);
+      const bool tf = P->path == EPSP_PATH_GEMM_TF32;
+      if (tf) {
+        P->d_At.alloc(ctx, size_t(M * P->Kp));
+        P->d_Gtf.alloc(ctx, size_t(N * P->Kp));
+        round_rows_tf32_kernel<<<div_up(size_t(N * P->Kp), 256), 256, 0, s>>>(P->d_Gt.p, N, P->Kx, P->Kx, P->Kp,
+                                                                               P->d_Gtf.p);
+      } else {
+        P->d_Ah.alloc(ctx, size_t(M * P->Kp));
+        P->d_Al.alloc(ctx, size_t(M * P->Kp));
+        P->d_Gh.alloc(ctx, size_t(N * P->Kp));
+        P->d_Gl.alloc(ctx, size_t(N * P->Kp));
+        split_rows_plain_kernel<<<div_up(size_t(N * P->Kp), 256), 256, 0, s>>>(P->d_Gt.p, N, P->Kx, P->Kx, P->Kp,
+                                                                                P->d_Gh.p, P->d_Gl.p);
+      }
       EPSP_LAUNCHED(ctx);
       plog.mark("mode tables, operand buffers");
       // the contraction's tile shape: the autotuner times the candidates on these operands (A
@@ -1408,23 +1483,30 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       P->d_part.alloc(ctx, size_t(max_sp) * size_t(M * N));
       P->d_err.alloc(ctx, 1);
       P->d_err.zero(s);
-      P->d_Ah.zero(s);
-      P->d_Al.zero(s);
-      P->opA64 = two_part(P->d_Ah.p, P->d_Al.p, M, P->Kx, P->Kp, kTcBM);
-      P->opG128 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 128);
-      P->opG256 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 256);
-      P->opA32 = two_part(P->d_Ah.p, P->d_Al.p, M, P->Kx, P->Kp, kTcBM, 32);
-      P->opG256_32 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 256, 32);
-      const TcTune best = tc_gemm_autotune(ctx, P->opA64, P->opG128, P->opG256, int(M), int(N), int(P->Kx), P->d_part.p, M,
-                                           M * N, max_sp, P->d_err.p, 2, &P->tune_all, &P->opA32, &P->opG256_32);
+      if (tf) {  // one TF32 map per operand, K boxes of 32 (128 bytes); opA32 / opG256_32 alias them
+        P->d_At.zero(s);
+        P->opA64 = P->opA32 = one_part_tf32(P->d_At.p, M, P->Kx, P->Kp, kTcBM);
+        P->opG128 = one_part_tf32(P->d_Gtf.p, N, P->Kx, P->Kp, 128);
+        P->opG256 = P->opG256_32 = one_part_tf32(P->d_Gtf.p, N, P->Kx, P->Kp, 256);
+      } else {
+        P->d_Ah.zero(s);
+        P->d_Al.zero(s);
+        P->opA64 = two_part(P->d_Ah.p, P->d_Al.p, M, P->Kx, P->Kp, kTcBM);
+        P->opG128 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 128);
+        P->opG256 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 256);
+        P->opA32 = two_part(P->d_Ah.p, P->d_Al.p, M, P->Kx, P->Kp, kTcBM, 32);
+        P->opG256_32 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 256, 32);
+      }
+      const TcTune best = tc_gemm_autotune(ctx, P->opA64, P->opG128, P->opG256, int(M), int(N), int(P->Kx), P->d_part.p,
+                                           M, M * N, max_sp, P->d_err.p, 2, &P->tune_all, &P->opA32, &P->opG256_32);
       for (const auto& c : P->tune_all)
-        if (c.bn == bn_h && c.splits == sp_h && c.bk == kTcBK && !c.persist) P->tune_ms_heuristic = c.ms;
+        if (c.bn == bn_h && c.splits == sp_h && c.bk == (tf ? 32 : kTcBK) && !c.persist) P->tune_ms_heuristic = c.ms;
       P->bn = best.bn;
       P->splits = best.splits;
       P->bk = best.bk;
       P->persist = best.persist;
-      P->opA = P->bk == 32 ? P->opA32 : P->opA64;
-      P->opG = P->bk == 32 ? P->opG256_32 : (P->bn == 256 ? P->opG256 : P->opG128);
+      P->cm = best.cm;
+      pick_contraction_operands(P);
       int terr = 0;
       P->d_err.download(&terr, 1, s);
       EPSP_CUDA(cudaStreamSynchronize(s));
@@ -1445,14 +1527,15 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       if (4 * (32 + 2 * (ns + 2)) > 256 * kXgPreMax)
         fail(EPSP_EUNSUPPORTED, "the shift grid is too fine for the BF16 operand kernel (nshift = " + std::to_string(ns) +
                                     " > 222); use EPSP_PATH_GEMM_FP64");
-      for (auto fn : {xgen_bf16_kernel<2>, xgen_bf16_kernel<4>, xgen_bf16_kernel<8>})
+      for (auto fn : {xgen_bf16_kernel<2, false>, xgen_bf16_kernel<4, false>, xgen_bf16_kernel<8, false>,
+                      xgen_bf16_kernel<2, true>, xgen_bf16_kernel<4, true>, xgen_bf16_kernel<8, true>})
         EPSP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(xgen_smem_bytes(int(ns)))));
     }
     EPSP_CUDA(cudaStreamSynchronize(s));
   } else {
     fail(EPSP_EINVAL, "unknown path");
   }
-  if (P->path == EPSP_PATH_GEMM_BF16) {
+  if (tc_path(P->path)) {
     P->d_Gmf.alloc(ctx, size_t(nw * 4 * ni));
     P->d_Gpf.alloc(ctx, size_t(nw * 4 * ni));
   } else {
@@ -1501,7 +1584,7 @@ static void set_propagators(LadderPlan* P, double mu, double T, double Om, bool 
   P->cur_Om = Om;
   if (!launch) return;
   const dim3 grid(div_up(size_t(nw), 128), unsigned(ni));
-  if (P->path == EPSP_PATH_GEMM_BF16)
+  if (tc_path(P->path))
     propagators_kernel<true><<<grid, 128, 0, s>>>(P->d_ST.p, P->d_ws.p, int(nw), P->d_jm.p, P->d_tm.p, P->d_jp.p, P->d_tp.p,
                                                    P->d_eps_i.p, mu, T, Om, P->d_Gmf.p, P->d_Gpf.p, int(ni));
   else
@@ -1555,7 +1638,7 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ, const double2*
   cudaStream_t s = ctx->stream;
   const long nw = P->nw, ni = P->ni, ns = P->nshift;
   const double T = P->cur_T;
-  if (P->path == EPSP_PATH_GEMM_BF16) fail(EPSP_EINVAL, "internal: FP64 vertices on the tensor-core path");
+  if (tc_path(P->path)) fail(EPSP_EINVAL, "internal: FP64 vertices on the tensor-core path");
   if (P->path == EPSP_PATH_DIRECT_FP64) {
     build_Bt(P, T);
     const long nrow = 16 * nw, ncol = 6 * ni;
@@ -1609,19 +1692,19 @@ static void apply_L(LadderPlan* P, const float2* J, float2* LJ, const float2* X 
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
   const long nw = P->nw, ni = P->ni, ns = P->nshift;
-  if (P->path != EPSP_PATH_GEMM_BF16) fail(EPSP_EINVAL, "internal: FP32 vertices on an FP64 path");
+  if (!tc_path(P->path)) fail(EPSP_EINVAL, "internal: FP32 vertices on an FP64 path");
   set_mode_occupations(P, P->cur_T);
   const long nwp = P->nwp, M = 24 * nwp, N = 3 * ni;
   long px = prof_begin(ctx, "xgen");
   const unsigned ktiles = unsigned((P->Kp / 64 + kXgTiles - 1) / kXgTiles);
-  launch_xgen(ns, dim3(unsigned(nwp / 32 * 8), ktiles, 1), xgen_smem_bytes(int(ns)), s, J, long(0),
-              static_cast<const int*>(nullptr), static_cast<const int32_t*>(P->d_mt_k.p),
+  launch_xgen(P->path == EPSP_PATH_GEMM_TF32, ns, dim3(unsigned(nwp / 32 * 8), ktiles, 1), xgen_smem_bytes(int(ns)), s, J,
+              long(0), static_cast<const int*>(nullptr), static_cast<const int32_t*>(P->d_mt_k.p),
               static_cast<const float*>(P->d_mt_w.p), static_cast<const float*>(P->d_nnu_f.p), int(nw), int(nwp),
-              int(ns), int(P->nmp), int(ni), P->Kx, P->Kp, P->d_Ah.p, P->d_Al.p);
+              int(ns), int(P->nmp), int(ni), P->Kx, P->Kp, P->d_Ah.p, P->d_Al.p, P->d_At.p);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, px);
   int sp = tc_gemm_launch_with(ctx, P->opA, P->opG, P->bn, P->splits, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N,
-                               P->d_err.p, "tc_ladder", P->persist);
+                               P->d_err.p, "tc_ladder", P->persist, P->cm);
   // D stays as the contraction's split-K partials; y_split and finish add them as they read
   long pl = prof_begin(ctx, "lsum");
   y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), 1), 256, 0, s>>>(P->d_part.p, M, sp, M * N, int(nw), int(nwp),
@@ -1639,7 +1722,7 @@ static void apply_L(LadderPlan* P, const float2* J, float2* LJ, const float2* X 
 }
 
 static void check_tc_err(LadderPlan* P) {
-  if (P->path != EPSP_PATH_GEMM_BF16) return;
+  if (!tc_path(P->path)) return;
   int e = 0;
   P->d_err.download(&e, 1, P->ctx->stream);
   EPSP_CUDA(cudaStreamSynchronize(P->ctx->stream));
@@ -1818,7 +1901,7 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
         std::vector<double> cv;
         std::vector<cplx> Yb(static_cast<size_t>(ny)), Yx0(static_cast<size_t>(ny), cplx(0, 0));
         std::vector<std::vector<cplx>> Yv;
-        const bool tc = P->path == EPSP_PATH_GEMM_BF16;
+        const bool tc = tc_path(P->path);
         std::vector<double2> hcol(size_t(maxiter + 5));
         while (!(solved || tired || breakdown)) {
           ++inner;
@@ -1998,7 +2081,7 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
 void ladder_run(LadderPlan* P, const double* sigma, const double* mu, const double* Tlist, int64_t nT, const double* Omegas,
                 int64_t nO, int32_t solver, double rtol, int32_t maxiter, double* sb, double* sl, uint8_t* conv, int32_t* niter,
                 epsp_ladder_history* hist, double* J_out) {
-  if (P->path == EPSP_PATH_GEMM_BF16)
+  if (tc_path(P->path))
     ladder_run_t<float2>(P, sigma, mu, Tlist, nT, Omegas, nO, solver, rtol, maxiter, sb, sl, conv, niter, hist, J_out,
                          P->w_J0f, P->w_Jf, P->w_LJf, P->w_Wf, P->w_Vf);
   else
@@ -2042,6 +2125,7 @@ struct LadderBatch {
   long cap = 0;
   int bk = 0;  // K block of the A maps
   DBuf<__nv_bfloat16> Ah, Al, Yh, Yl;
+  DBuf<float> At;  // GEMM_TF32: the A operand as TF32-rounded FP32
   DBuf<float> part, part2, nnu;
   DBuf<float2> Gm, Gp, J0, J, LJ, W;
   DBuf<double2> dpart, H, coef_a, coef_b;
@@ -2058,8 +2142,13 @@ static void batch_reserve(LadderPlan* P, LadderBatch& B, long R, int maxiter) {
   Ctx* ctx = P->ctx;
   const long nw = P->nw, ni = P->ni, nwp = P->nwp, M = 24 * nwp, N = 3 * ni, n = nw * 24 * ni;
   B.cap = R;
-  B.Ah.alloc(ctx, size_t(R * M * P->Kp));
-  B.Al.alloc(ctx, size_t(R * M * P->Kp));
+  const bool tf = P->path == EPSP_PATH_GEMM_TF32;
+  if (tf) {
+    B.At.alloc(ctx, size_t(R * M * P->Kp));
+  } else {
+    B.Ah.alloc(ctx, size_t(R * M * P->Kp));
+    B.Al.alloc(ctx, size_t(R * M * P->Kp));
+  }
   B.Yh.alloc(ctx, size_t(R * 8 * N * P->Kp2));
   B.Yl.alloc(ctx, size_t(R * 8 * N * P->Kp2));
   size_t p1 = 0, p2 = 0;
@@ -2087,7 +2176,8 @@ static void batch_reserve(LadderPlan* P, LadderBatch& B, long R, int maxiter) {
   B.pp.alloc(ctx, size_t(R));
   B.rmap.alloc(ctx, size_t(R));
   B.Y.alloc(ctx, size_t(R * 3 * ni));
-  B.opA = two_part(B.Ah.p, B.Al.p, R * M, P->Kx, P->Kp, kTcBM, P->bk);
+  B.opA = tf ? one_part_tf32(B.At.p, R * M, P->Kx, P->Kp, kTcBM, P->bk)
+             : two_part(B.Ah.p, B.Al.p, R * M, P->Kx, P->Kp, kTcBM, P->bk);
   B.bk = P->bk;
   B.opY = two_part(B.Yh.p, B.Yl.p, R * 8 * N, nw, P->Kp2, P->bn2);
 }
@@ -2100,14 +2190,15 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const float2* X, int nA
   const long Mt = M * nA;
   long px = prof_begin(ctx, "xgen");
   const unsigned ktiles = unsigned((P->Kp / 64 + kXgTiles - 1) / kXgTiles);
-  launch_xgen(ns, dim3(unsigned(nwp / 32 * 8), ktiles, unsigned(nA)), xgen_smem_bytes(int(ns)), s, X, n,
-              static_cast<const int*>(B.rmap.p), static_cast<const int32_t*>(P->d_mt_k.p),
-              static_cast<const float*>(P->d_mt_w.p), static_cast<const float*>(B.nnu.p), int(nw), int(nwp), int(ns),
-              int(P->nmp), int(ni), P->Kx, P->Kp, B.Ah.p, B.Al.p);
+  launch_xgen(P->path == EPSP_PATH_GEMM_TF32, ns, dim3(unsigned(nwp / 32 * 8), ktiles, unsigned(nA)),
+              xgen_smem_bytes(int(ns)), s, X, n, static_cast<const int*>(B.rmap.p),
+              static_cast<const int32_t*>(P->d_mt_k.p), static_cast<const float*>(P->d_mt_w.p),
+              static_cast<const float*>(B.nnu.p), int(nw), int(nwp), int(ns), int(P->nmp), int(ni), P->Kx, P->Kp, B.Ah.p,
+              B.Al.p, B.At.p);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, px);
   int sp = tc_gemm_launch_with(ctx, B.opA, P->opG, P->bn, 0, int(Mt), int(N), int(P->Kx), B.part.p, Mt, Mt * N, P->d_err.p,
-                               "tc_ladder", P->persist);
+                               "tc_ladder", P->persist, P->cm);
   y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), unsigned(nA)), 256, 0, s>>>(
       B.part.p, Mt, sp, Mt * N, int(nw), int(nwp), N, P->Kp2, B.Yh.p, B.Yl.p);
   EPSP_LAUNCHED(ctx);
@@ -2162,7 +2253,8 @@ void ladder_run_batched(LadderPlan* P, const double* sigma, const double* mu, co
                         double* sl, uint8_t* conv, int32_t* niter, epsp_ladder_history* hist, double* J_out) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
-  if (P->path != EPSP_PATH_GEMM_BF16) fail(EPSP_EUNSUPPORTED, "batched right-hand sides need a GEMM_BF16 ladder plan");
+  if (!tc_path(P->path))
+    fail(EPSP_EUNSUPPORTED, "batched right-hand sides need a tensor-core ladder plan (GEMM_BF16 or GEMM_TF32)");
   if (maxiter < 1) fail(EPSP_EINVAL, "maxiter must be at least 1, got " + std::to_string(maxiter));
   if (max_rhs < 1) fail(EPSP_EINVAL, "max_rhs must be at least 1");
   if (nO < 1) fail(EPSP_EINVAL, "Omegas must hold at least one probe frequency");
@@ -2472,17 +2564,21 @@ epsp_status epsp_ladder_set_gemm_config(epsp_ladder_plan* plan, int32_t bn, int3
   if (!plan) return EPSP_EINVAL;
   auto* P = reinterpret_cast<LadderPlan*>(plan);
   return lguard(P->ctx, [&] {
-    if (P->path != EPSP_PATH_GEMM_BF16) fail(EPSP_EUNSUPPORTED, "tile shapes apply to GEMM_BF16 plans");
-    const bool ok = (bk == 64 && (bn == 128 || bn == 256)) || (bk == 32 && bn == 256);
-    if (!ok) fail(EPSP_EINVAL, "tile shape must be bn 128 or 256 with bk 64, or bn 256 with bk 32");
+    if (!tc_path(P->path)) fail(EPSP_EUNSUPPORTED, "tile shapes apply to tensor-core plans (GEMM_BF16, GEMM_TF32)");
+    const bool tf = P->path == EPSP_PATH_GEMM_TF32;
+    const bool ok = tf ? (bk == 32 && (bn == 128 || bn == 256))
+                       : ((bk == 64 && (bn == 128 || bn == 256)) || (bk == 32 && bn == 256));
+    if (!ok)
+      fail(EPSP_EINVAL, tf ? "TF32 tile shape must be bn 128 or 256 with bk 32"
+                           : "tile shape must be bn 128 or 256 with bk 64, or bn 256 with bk 32");
     const int max_sp = int(P->d_part.n / size_t(24 * P->nwp * 3 * P->ni));
     if (splits < 1 || splits > max_sp) fail(EPSP_EINVAL, "splits must be in [1, " + std::to_string(max_sp) + "]");
     P->bn = bn;
     P->splits = splits;
     P->bk = bk;
-    P->opA = bk == 32 ? P->opA32 : P->opA64;
-    P->opG = bk == 32 ? P->opG256_32 : (bn == 256 ? P->opG256 : P->opG128);
-    if (!(bn == 256 && bk == 32)) P->persist = false;
+    pick_contraction_operands(P);
+    if (!tf && !(bn == 256 && bk == 32)) P->persist = false;
+    P->cm = 1;
   });
 }
 
@@ -2496,9 +2592,30 @@ epsp_status epsp_ladder_set_gemm_persistent(epsp_ladder_plan* plan, int32_t on) 
   if (!plan) return EPSP_EINVAL;
   auto* P = reinterpret_cast<LadderPlan*>(plan);
   return lguard(P->ctx, [&] {
-    if (P->path != EPSP_PATH_GEMM_BF16) fail(EPSP_EUNSUPPORTED, "tile shapes apply to GEMM_BF16 plans");
-    if (on && !(P->bn == 256 && P->bk == 32)) fail(EPSP_EINVAL, "the persistent kernel takes bn 256 with bk 32");
+    if (!tc_path(P->path)) fail(EPSP_EUNSUPPORTED, "tile shapes apply to tensor-core plans (GEMM_BF16, GEMM_TF32)");
+    if (on && P->path == EPSP_PATH_GEMM_BF16 && !(P->bn == 256 && P->bk == 32))
+      fail(EPSP_EINVAL, "the persistent BF16x3 kernel takes bn 256 with bk 32");
     P->persist = on != 0;
+    if (!P->persist) P->cm = 1;
+  });
+}
+
+epsp_status epsp_ladder_gemm_cluster(const epsp_ladder_plan* plan, int32_t* cm) {
+  if (!plan || !cm) return EPSP_EINVAL;
+  *cm = reinterpret_cast<const LadderPlan*>(plan)->cm;
+  return EPSP_OK;
+}
+
+epsp_status epsp_ladder_set_gemm_cluster(epsp_ladder_plan* plan, int32_t cm) {
+  if (!plan) return EPSP_EINVAL;
+  auto* P = reinterpret_cast<LadderPlan*>(plan);
+  return lguard(P->ctx, [&] {
+    if (!tc_path(P->path)) fail(EPSP_EUNSUPPORTED, "tile shapes apply to tensor-core plans (GEMM_BF16, GEMM_TF32)");
+    if (cm != 1 && cm != 2 && cm != 4) fail(EPSP_EINVAL, "clusters of 1, 2 or 4 CTAs");
+    if (cm > 1 && !P->persist) fail(EPSP_EINVAL, "clusters are for the persistent kernel");
+    if (cm > 2 && P->bn == 128) fail(EPSP_EINVAL, "tile width 128 takes clusters of at most 2");
+    if (cm > 1 && P->path == EPSP_PATH_GEMM_BF16 && P->bn != 256) fail(EPSP_EINVAL, "BF16x3 clusters take bn 256");
+    P->cm = cm;
   });
 }
 
@@ -2511,7 +2628,7 @@ epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, i
   if (bk) *bk = P->bk;
   double best = 0;
   for (const auto& c : P->tune_all)
-    if (c.bn == P->bn && c.splits == P->splits && c.bk == P->bk && c.persist == P->persist) best = c.ms;
+    if (c.bn == P->bn && c.splits == P->splits && c.bk == P->bk && c.persist == P->persist && c.cm == P->cm) best = c.ms;
   if (ms_chosen) *ms_chosen = best;
   if (ms_heuristic) *ms_heuristic = P->tune_ms_heuristic;
   return EPSP_OK;
@@ -2531,7 +2648,7 @@ epsp_status epsp_ladder_apply(epsp_ladder_plan* plan, const double* sigma_T, dou
     dJ.alloc(P->ctx, size_t(n));
     dLJ.alloc(P->ctx, size_t(n));
     dJ.upload(reinterpret_cast<const double2*>(J), size_t(n), s);
-    if (P->path == EPSP_PATH_GEMM_BF16) {  // FP32 vertices on the device
+    if (tc_path(P->path)) {  // FP32 vertices on the device
       DBuf<float2> fJ, fLJ;
       fJ.alloc(P->ctx, size_t(n));
       fLJ.alloc(P->ctx, size_t(n));

@@ -858,6 +858,8 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
   std::unique_ptr<Scgd0Plan> guard(P);
   P->ctx = ctx;
   P->path = opts->path;
+  if (P->path == EPSP_PATH_GEMM_TF32)
+    fail(EPSP_EUNSUPPORTED, "GEMM_TF32 is a ladder path; scGD0 plans take DIRECT_FP64, GEMM_FP64 or GEMM_BF16");
   P->w_ac = opts->omega_acoustic;
   P->verbosity = opts->verbosity;
   P->nm = m->nm;

@@ -1,4 +1,4 @@
-// tc_gemm.cu -- host side of the tcgen05 BF16x3 GEMM: tensor maps, tile shape and split-K choice.
+// tc_gemm.cu -- host side of the tcgen05 GEMMs (BF16x3, TF32): tensor maps, tile shape, split-K choice.
 #include "tc_gemm.cuh"
 
 #include <algorithm>
@@ -33,6 +33,22 @@ CUtensorMap make_tmap_bf16(const void* base, long rows, long cols, long ld, int 
   cuuint32_t estr[2] = {1, 1};
   CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) fail(EPSP_ECUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string(int(r)));
+  return m;
+}
+
+CUtensorMap make_tmap_f32(const void* base, long rows, long cols, long ld, int box_rows, int bk) {
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || (ld * 4) % 16 != 0)
+    fail(EPSP_EINVAL, "tensor map base and row stride must be 16-byte aligned");
+  if (bk != 32 && bk != 16) fail(EPSP_EINVAL, "FP32 tensor map K box must be 32 or 16 columns");
+  CUtensorMap m;
+  cuuint64_t dims[2] = {cuuint64_t(cols), cuuint64_t(rows)};
+  cuuint64_t strides[1] = {cuuint64_t(ld * 4)};
+  cuuint32_t box[2] = {cuuint32_t(bk), cuuint32_t(box_rows)};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, bk == 32 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) fail(EPSP_ECUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string(int(r)));
   return m;
@@ -74,15 +90,16 @@ void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* b
   *splits = best;
 }
 
-template <int BN, int STAGES, int NS, int BK = kTcBK>
+template <int BN, int STAGES, int NS, int BK = kTcBK, bool TF32 = false>
 static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int kblocks, int per, int splits,
                    float* out, long ld_out, long split_stride, int* d_err) {
-  using L = TcSmem<BN, STAGES, NS, BK>;
+  using L = TcSmem<BN, STAGES, NS, BK, TF32>;
   if (A.bk != BK || B.bk != BK) fail(EPSP_EINVAL, "operand tensor maps were built for another K block");
+  if (A.tf32 != TF32 || B.tf32 != TF32) fail(EPSP_EINVAL, "operand tensor maps were built for another element type");
   static bool configured = false;  // one process, one attribute setting per instantiation
   if (!configured) {
-    EPSP_CUDA(cudaFuncSetAttribute(tc_gemm_split_kernel<BN, STAGES, NS, BK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   L::kBytes));
+    EPSP_CUDA(cudaFuncSetAttribute(tc_gemm_split_kernel<BN, STAGES, NS, BK, TF32>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, L::kBytes));
     configured = true;
   }
   TcMaps maps;
@@ -91,37 +108,68 @@ static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int 
     maps.b[p] = B.m[p < NS ? p : 0];
   }
   dim3 grid((N + BN - 1) / BN, (M + kTcBM - 1) / kTcBM, splits);
-  tc_gemm_split_kernel<BN, STAGES, NS, BK><<<grid, 128, L::kBytes, ctx->stream>>>(maps, M, N, kblocks, per, out, ld_out,
-                                                                                  split_stride, d_err);
+  tc_gemm_split_kernel<BN, STAGES, NS, BK, TF32><<<grid, 128, L::kBytes, ctx->stream>>>(maps, M, N, kblocks, per, out,
+                                                                                        ld_out, split_stride, d_err);
   EPSP_LAUNCHED(ctx);
 }
 
-template <int BN, int STAGES, int NS, int BK>
+// Part p of an operand mapped again with boxes of box_rows rows (from the matrix behind its maps).
+static CUtensorMap remap(const TcOperand& op, int p, int box_rows) {
+  if (!op.base[p]) fail(EPSP_EINVAL, "internal: operand without its matrix description");
+  return op.tf32 ? make_tmap_f32(op.base[p], op.rows, op.cols, op.ld, box_rows, op.bk)
+                 : make_tmap_bf16(op.base[p], op.rows, op.cols, op.ld, box_rows, op.bk);
+}
+
+template <int BN, int STAGES, int NS, int BK, bool TF32 = false, int CM = 1>
 static void launch_persist(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int kblocks, int per,
                            int splits, float* out, long ld_out, long split_stride, int* d_err) {
-  using L = TcPSmem<BN, STAGES, NS, BK>;
+  using L = TcPSmem<BN, STAGES, NS, BK, TF32>;
   if (A.bk != BK || B.bk != BK) fail(EPSP_EINVAL, "operand tensor maps were built for another K block");
+  if (A.tf32 != TF32 || B.tf32 != TF32) fail(EPSP_EINVAL, "operand tensor maps were built for another element type");
+  auto* kern = tc_gemm_persist_kernel<BN, STAGES, NS, BK, TF32, CM>;
+  cudaLaunchAttribute cl;
+  cl.id = cudaLaunchAttributeClusterDimension;
+  cl.val.clusterDim.x = CM;
+  cl.val.clusterDim.y = 1;
+  cl.val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.blockDim = dim3(192);
+  cfg.dynamicSmemBytes = L::kBytes;
+  cfg.stream = ctx->stream;
+  cfg.attrs = &cl;
+  cfg.numAttrs = 1;
   static bool configured = false;  // one process, one attribute setting per instantiation
+  static int max_clusters = 0;     // clusters of CM CTAs resident at once
   if (!configured) {
-    EPSP_CUDA(cudaFuncSetAttribute(tc_gemm_persist_kernel<BN, STAGES, NS, BK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   L::kBytes));
+    EPSP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::kBytes));
+    if (CM > 1) {
+      cfg.gridDim = dim3(unsigned(CM * std::max(1, ctx->sm_count / CM)));
+      EPSP_CUDA(cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg));
+      if (max_clusters < 1) fail(EPSP_EUNSUPPORTED, "no cluster of " + std::to_string(CM) + " GEMM CTAs fits on the device");
+    }
     configured = true;
   }
   TcMaps maps;
   for (int p = 0; p < 3; ++p) {
     maps.a[p] = A.m[p < NS ? p : 0];
-    maps.b[p] = B.m[p < NS ? p : 0];
+    maps.b[p] = CM == 1 ? B.m[p < NS ? p : 0] : remap(B, p < NS ? p : 0, BN / CM);  // B slices of BN / CM rows
   }
   const int nN = (N + BN - 1) / BN, nM = (M + kTcBM - 1) / kTcBM;
-  const int nitems = nN * nM * splits;
-  const int grid = std::min(nitems, ctx->sm_count);
-  tc_gemm_persist_kernel<BN, STAGES, NS, BK><<<grid, 192, L::kBytes, ctx->stream>>>(
-      maps, M, N, kblocks, per, nN, nM, nitems, out, ld_out, split_stride, d_err);
+  const int nitems = nN * ((nM + CM - 1) / CM) * splits;  // (N tile, M tile group, split)
+  if (CM == 1) {
+    const int grid = std::min(nitems, ctx->sm_count);
+    kern<<<grid, 192, L::kBytes, ctx->stream>>>(maps, M, N, kblocks, per, nN, nM, nitems, out, ld_out, split_stride,
+                                                d_err);
+  } else {
+    cfg.gridDim = dim3(unsigned(CM * std::min(nitems, max_clusters)));
+    EPSP_CUDA(cudaLaunchKernelEx(&cfg, kern, maps, M, N, kblocks, per, nN, nM, nitems, out, ld_out, split_stride, d_err));
+  }
   EPSP_LAUNCHED(ctx);
 }
 
 int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int K, float* out, long ld_out,
                    long split_stride, int max_splits, int* d_err, const char* prof_name, int kb_cap) {
+  if (A.tf32 || B.tf32) fail(EPSP_EINVAL, "TF32 operands take tc_gemm_launch_with");
   if (A.ns != B.ns || (A.ns != 2 && A.ns != 3)) fail(EPSP_EINVAL, "operands must be split into 2 or 3 parts alike");
   if (A.bk != B.bk) fail(EPSP_EINVAL, "operands built for different K blocks");
   int BN, splits;
@@ -154,9 +202,39 @@ int tc_splits_for(Ctx* ctx, int M, int N, int K, int bn) {
 }
 
 int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn, int splits, int M, int N, int K,
-                        float* out, long ld_out, long split_stride, int* d_err, const char* prof_name, bool persist) {
-  if (A.ns != 2 || B.ns != 2) fail(EPSP_EINVAL, "explicit tile shapes are for two-part operands");
+                        float* out, long ld_out, long split_stride, int* d_err, const char* prof_name, bool persist,
+                        int cm) {
   if (bn != 128 && bn != 256) fail(EPSP_EINVAL, "tile width must be 128 or 256");
+  if (cm != 1 && cm != 2 && cm != 4) fail(EPSP_EINVAL, "clusters of 1, 2 or 4 CTAs");
+  if (cm > 1 && !persist) fail(EPSP_EINVAL, "clusters are for the persistent kernel");
+  if (cm > 1 && (bn == 128 ? cm > 2 : false)) fail(EPSP_EINVAL, "tile width 128 takes clusters of at most 2");
+  if (A.tf32 || B.tf32) {
+    if (!(A.tf32 && B.tf32 && A.ns == 1 && B.ns == 1 && A.bk == 32 && B.bk == 32))
+      fail(EPSP_EINVAL, "TF32 operands are one-part maps with K boxes of 32 on both sides");
+    const int kblocks = (K + 31) / 32;
+    if (splits <= 0) splits = tc_splits_for(ctx, M, N, K, bn);
+    splits = std::max(1, std::min(splits, kblocks));
+    const int per = (kblocks + splits - 1) / splits;
+    splits = (kblocks + per - 1) / per;
+    long pi = prof_begin(ctx, prof_name);
+    if (persist && bn == 256 && cm == 4)
+      launch_persist<256, 4, 1, 32, true, 4>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    else if (persist && bn == 256 && cm == 2)
+      launch_persist<256, 4, 1, 32, true, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    else if (persist && bn == 256)
+      launch_persist<256, 4, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    else if (persist && cm == 2)
+      launch_persist<128, 6, 1, 32, true, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    else if (persist)
+      launch_persist<128, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    else if (bn == 256)
+      launch<256, 4, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    else
+      launch<128, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    prof_end(ctx, pi);
+    return splits;
+  }
+  if (A.ns != 2 || B.ns != 2) fail(EPSP_EINVAL, "explicit tile shapes are for two-part operands");
   const int bk = A.bk;
   if (bk == 32 && bn != 256) fail(EPSP_EINVAL, "K blocks of 32 come with tile width 256");
   const int kblocks = (K + bk - 1) / bk;
@@ -166,7 +244,11 @@ int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn
   splits = (kblocks + per - 1) / per;
   if (persist && !(bk == 32 && bn == 256)) fail(EPSP_EINVAL, "the persistent kernel takes tile width 256 with K blocks of 32");
   long pi = prof_begin(ctx, prof_name);
-  if (persist)
+  if (persist && cm == 4)
+    launch_persist<256, 4, 2, 32, false, 4>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+  else if (persist && cm == 2)
+    launch_persist<256, 4, 2, 32, false, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+  else if (persist)
     launch_persist<256, 4, 2, 32>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   else if (bk == 32)
     launch<256, 4, 2, 32>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
@@ -188,7 +270,7 @@ std::map<std::array<long, 5>, std::vector<TcTune>> g_tune_cache;
 TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, const TcOperand& B256, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int max_splits, int* d_err, int reps,
                         std::vector<TcTune>* all, const TcOperand* A32, const TcOperand* B256_32) {
-  const std::array<long, 5> key{ctx->device, M, N, K, max_splits + (A32 && B256_32 ? 1000 : 0)};
+  const std::array<long, 5> key{ctx->device, M, N, K, max_splits + (A32 && B256_32 ? 1000 : 0) + (A.tf32 ? 2000 : 0)};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
@@ -206,10 +288,17 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
     const int h = std::max(1, (ctx->sm_count + tiles - 1) / tiles);
     for (int sp : {h, 2 * h})
       if (sp <= max_splits) {
+        if (A.tf32) {  // TF32: either tile width, either kernel (the persistent one in clusters too)
+          cand.push_back(TcTune{bn, sp, 32, 0.f});
+          cand.push_back(TcTune{bn, sp, 32, 0.f, true});
+          cand.push_back(TcTune{bn, sp, 32, 0.f, true, 2});
+          if (bn == 256) cand.push_back(TcTune{bn, sp, 32, 0.f, true, 4});
+          continue;
+        }
         cand.push_back(TcTune{bn, sp, kTcBK, 0.f});
         if (bn == 256 && A32 && B256_32) {
           cand.push_back(TcTune{bn, sp, 32, 0.f});
-          cand.push_back(TcTune{bn, sp, 32, 0.f, true});
+          for (int cm : {1, 2, 4}) cand.push_back(TcTune{bn, sp, 32, 0.f, true, cm});
         }
       }
   }
@@ -218,19 +307,23 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
   EPSP_CUDA(cudaEventCreate(&e1));
   TcTune best{};
   best.ms = 3.4e38f;
-  auto opA = [&](const TcTune& c) -> const TcOperand& { return c.bk == 32 ? *A32 : A; };
-  auto opB = [&](const TcTune& c) -> const TcOperand& { return c.bk == 32 ? *B256_32 : (c.bn == 256 ? B256 : B128); };
+  // A32 / B256_32: the BF16 operands with K boxes of 32 (TF32 operands have one K box, 32)
+  auto opA = [&](const TcTune& c) -> const TcOperand& { return c.bk == 32 && !A.tf32 ? *A32 : A; };
+  auto opB = [&](const TcTune& c) -> const TcOperand& {
+    return c.bk == 32 && !A.tf32 ? *B256_32 : (c.bn == 256 ? B256 : B128);
+  };
   // one untimed launch first, so that no candidate pays the first launch's costs
   if (!cand.empty())
     tc_gemm_launch_with(ctx, opA(cand[0]), opB(cand[0]), cand[0].bn, cand[0].splits, M, N, K, out, ld_out, split_stride,
-                        d_err, "autotune", cand[0].persist);
+                        d_err, "autotune", cand[0].persist, cand[0].cm);
   for (auto& c : cand) {
     const TcOperand& A_ = opA(c);
     const TcOperand& B = opB(c);
     // the untimed launch is timed too: a candidate slower than 20 ms is judged on it alone
     float ms = 0.f;
     EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
-    tc_gemm_launch_with(ctx, A_, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune", c.persist);
+    tc_gemm_launch_with(ctx, A_, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune", c.persist,
+                        c.cm);
     EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
     EPSP_CUDA(cudaEventSynchronize(e1));
     EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
@@ -239,7 +332,7 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
       EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
       for (int r = 0; r < reps; ++r)
         tc_gemm_launch_with(ctx, A_, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune",
-                            c.persist);
+                            c.persist, c.cm);
       EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
       EPSP_CUDA(cudaEventSynchronize(e1));
       EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));

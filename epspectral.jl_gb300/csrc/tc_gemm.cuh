@@ -1,9 +1,12 @@
-// tc_gemm.cuh -- BF16x3 split-precision GEMM on the sm_103a tensor cores (tcgen05 + TMA + TMEM).
+// tc_gemm.cuh -- split-precision and TF32 GEMMs on the sm_103a tensor cores (tcgen05 + TMA + TMEM).
 //
 //   D[m, n] (FP32) = Σ_k A[m, k] B[n, k]   with   A ≈ A_hi + A_lo,  B ≈ B_hi + B_lo  (BF16 each)
 //   evaluated as A_hi·B_hi + A_hi·B_lo + A_lo·B_hi, all three products accumulated in one TMEM
 //   accumulator (FP32). A [M][K] and B [N][K] are row-major with K contiguous ("K-major"), row
 //   stride `ldk` elements (a multiple of 8, so rows start on 16-byte boundaries).
+//   The TF32 variant (TF32 = true, one part per operand) runs one kind::tf32 product of FP32
+//   operands already rounded to TF32 (10-bit mantissa): half the BF16 rate per product, so two
+//   thirds of the BF16x3 tensor time for the same operand bytes, at ~2^-11 relative per element.
 //
 // One CTA of 128 threads computes a 128 x BN tile of D over a range of 64-wide K blocks (split-K
 // over blockIdx.z; each split writes its own FP32 slab, summed afterwards in fixed order):
@@ -61,6 +64,25 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       "l"(map), "r"(c0), "r"(c1), "r"(bar)
       : "memory");
 }
+// The same box written to the same shared-memory offset of every CTA of the cluster in `mask`,
+// each completing bytes on its own mbarrier at offset `bar`.
+__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar,
+                                               uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, {%2, "
+      "%3}], [%4], %5;" ::"r"(dst),
+      "l"(map), "r"(c0), "r"(c1), "r"(bar), "h"(mask)
+      : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// Every thread of every CTA of the cluster (a hardware barrier; all of them reach it).
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 
 // Shared-memory matrix descriptor of a K-major operand tile with 128-byte swizzle: rows of 128 B
 // (64 BF16), 8-row groups 1024 B apart (stride byte offset), descriptor version 1.
@@ -71,27 +93,54 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
 __device__ __forceinline__ uint64_t sw64_desc(uint32_t addr) {
   return uint64_t((addr >> 4) & 0x3FFF) | (uint64_t(512 >> 4) << 32) | (uint64_t(1) << 46) | (uint64_t(4) << 61);
 }
-// The descriptor for K blocks of BK elements (64: 128-byte rows, 32: 64-byte rows).
-template <int BK>
+// The descriptor for K rows of RB bytes (128: 64 BF16 or 32 TF32; 64: 32 BF16).
+template <int RB>
 __device__ __forceinline__ uint64_t sw_desc(uint32_t addr) {
-  if constexpr (BK == 64)
+  static_assert(RB == 128 || RB == 64, "K rows of 128 or 64 bytes");
+  if constexpr (RB == 128)
     return sw128_desc(addr);
   else
     return sw64_desc(addr);
 }
 
-// Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major, M = 128, N = n.
-__host__ __device__ constexpr uint32_t idesc_bf16_f32(int n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(128 >> 4) << 24);
+// Instruction descriptor of kind::f16 (A and B BF16) or kind::tf32 (A and B TF32): D FP32, both
+// K-major, M = 128, N = n.
+template <bool TF32 = false>
+__host__ __device__ constexpr uint32_t idesc_f32acc(int n) {
+  return (1u << 4) | ((TF32 ? 2u : 1u) << 7) | ((TF32 ? 2u : 1u) << 10) | (uint32_t(n >> 3) << 17) |
+         (uint32_t(128 >> 4) << 24);
 }
 
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+// One MMA: K = 16 BF16 (kind::f16) or K = 8 TF32 (kind::tf32), 32 bytes of each operand row.
+template <bool TF32 = false>
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+  if constexpr (TF32)
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+  else
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+
+// x rounded to TF32 (nearest, ties away from zero), as an FP32 value with the low 13 bits zero.
+__device__ __forceinline__ float round_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
 }
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+// The same, arriving on the mbarrier at offset `bar` of every CTA of the cluster in `mask`.
+__device__ __forceinline__ void umma_commit_mc(uint32_t bar, uint16_t mask) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+                   bar),
+               "h"(mask)
+               : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -114,11 +163,14 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 }
 
 // NS = 2: operands split x = x0 + x1 (hi, lo), products 00, 01, 10 (BF16x3, ~2^-16 relative);
-// NS = 3: x = x0 + x1 + x2 (hi, mid, lo), products 00, 01, 10, 02, 11, 20 (six, ~2^-23 relative).
-template <int BN, int STAGES, int NS, int BK = kTcBK>
+// NS = 3: x = x0 + x1 + x2 (hi, mid, lo), products 00, 01, 10, 02, 11, 20 (six, ~2^-23 relative);
+// NS = 1 with TF32: one TF32 product. BK counts elements (2 bytes, or 4 with TF32) per K row.
+template <int BN, int STAGES, int NS, int BK = kTcBK, bool TF32 = false>
 struct TcSmem {
-  static constexpr int kA = kTcBM * BK * 2;   // bytes of one A tile
-  static constexpr int kB = BN * BK * 2;      // bytes of one B tile
+  static constexpr int kES = TF32 ? 4 : 2;     // bytes per element
+  static constexpr int kRB = BK * kES;         // bytes of one K row
+  static constexpr int kA = kTcBM * kRB;       // bytes of one A tile
+  static constexpr int kB = BN * kRB;          // bytes of one B tile
   static constexpr int kStage = NS * kA + NS * kB;
   static constexpr int kBars = 2 * STAGES + 1;
   static constexpr int kBytes = STAGES * kStage + 8 * kBars + 16 + 1024;  // + alignment slack
@@ -128,11 +180,12 @@ struct TcMaps {
   CUtensorMap a[3], b[3];
 };
 
-template <int BN, int STAGES, int NS, int BK = kTcBK>
+template <int BN, int STAGES, int NS, int BK = kTcBK, bool TF32 = false>
 __global__ void __launch_bounds__(128, 1)
     tc_gemm_split_kernel(const __grid_constant__ TcMaps maps, int M, int N, int kblocks, int kb_per_split,
                          float* __restrict__ out, long ld_out, long split_stride, int* __restrict__ err) {
-  using L = TcSmem<BN, STAGES, NS, BK>;
+  using L = TcSmem<BN, STAGES, NS, BK, TF32>;
+  static_assert(!TF32 || NS == 1, "TF32 operands have one part");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * L::kStage);
@@ -188,7 +241,7 @@ __global__ void __launch_bounds__(128, 1)
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
-    constexpr uint32_t idesc = idesc_bf16_f32(BN);
+    constexpr uint32_t idesc = idesc_f32acc<TF32>(BN);
     for (int kb = 0; kb < nkb; ++kb) {
       const int s = kb % STAGES;
       const uint32_t ph = (kb / STAGES) & 1;
@@ -201,16 +254,18 @@ __global__ void __launch_bounds__(128, 1)
       const uint32_t a0 = smem_u32(smem + s * L::kStage);
       const uint32_t b0 = a0 + NS * L::kA;
 #pragma unroll
-      for (int ks = 0; ks < BK / 16; ++ks) {
-        const uint32_t off = ks * 32;  // 16 BF16 along K inside the swizzled row
+      for (int ks = 0; ks < L::kRB / 32; ++ks) {
+        const uint32_t off = ks * 32;  // 16 BF16 (8 TF32) along K inside the swizzled row
         // the split products of increasing order: 00; 01, 10; (NS = 3) 02, 11, 20
-        umma_bf16(tmem, sw_desc<BK>(a0 + off), sw_desc<BK>(b0 + off), idesc, (kb | ks) != 0);
-        umma_bf16(tmem, sw_desc<BK>(a0 + off), sw_desc<BK>(b0 + L::kB + off), idesc, 1);
-        umma_bf16(tmem, sw_desc<BK>(a0 + L::kA + off), sw_desc<BK>(b0 + off), idesc, 1);
+        umma<TF32>(tmem, sw_desc<L::kRB>(a0 + off), sw_desc<L::kRB>(b0 + off), idesc, (kb | ks) != 0);
+        if constexpr (NS >= 2) {
+          umma<TF32>(tmem, sw_desc<L::kRB>(a0 + off), sw_desc<L::kRB>(b0 + L::kB + off), idesc, 1);
+          umma<TF32>(tmem, sw_desc<L::kRB>(a0 + L::kA + off), sw_desc<L::kRB>(b0 + off), idesc, 1);
+        }
         if constexpr (NS == 3) {
-          umma_bf16(tmem, sw_desc<BK>(a0 + off), sw_desc<BK>(b0 + 2 * L::kB + off), idesc, 1);
-          umma_bf16(tmem, sw_desc<BK>(a0 + L::kA + off), sw_desc<BK>(b0 + L::kB + off), idesc, 1);
-          umma_bf16(tmem, sw_desc<BK>(a0 + 2 * L::kA + off), sw_desc<BK>(b0 + off), idesc, 1);
+          umma<TF32>(tmem, sw_desc<L::kRB>(a0 + off), sw_desc<L::kRB>(b0 + 2 * L::kB + off), idesc, 1);
+          umma<TF32>(tmem, sw_desc<L::kRB>(a0 + L::kA + off), sw_desc<L::kRB>(b0 + L::kB + off), idesc, 1);
+          umma<TF32>(tmem, sw_desc<L::kRB>(a0 + 2 * L::kA + off), sw_desc<L::kRB>(b0 + off), idesc, 1);
         }
       }
       umma_commit(empty0 + 8 * s);
@@ -261,25 +316,38 @@ __global__ void __launch_bounds__(128, 1)
 //   warps 2-5      : epilogue of item t (TMEM lane quarter = warp % 4) while the MMAs of item t + 1
 //                    run into the other accumulator; they release an accumulator by one arrive each.
 // Per tile the MMAs run in the one-tile kernel's order, so the results are bitwise the same.
+// With CM > 1 the grid is made of clusters of CM CTAs on CM consecutive M tiles of one N tile (an
+// item is then such a group, the cluster's index in place of blockIdx.x): they share the B tile,
+// which each CTA loads 1/CM of (B's maps have boxes of BN / CM rows) and multicasts to the cluster,
+// so B's L2-to-SM traffic falls by CM. A stage is refilled only when every CTA of the cluster has
+// consumed it: each MMA commit arrives on the empty barrier of every CTA (count CM). Before the
+// first multicast the cluster synchronises (its barriers initialised); before exit each producer
+// waits for the last arrivals on its own empty barriers, so nothing remains in flight towards it.
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-template <int BN, int STAGES, int NS, int BK>
+template <int BN, int STAGES, int NS, int BK, bool TF32 = false>
 struct TcPSmem {
-  static constexpr int kA = kTcBM * BK * 2;
-  static constexpr int kB = BN * BK * 2;
+  static constexpr int kES = TF32 ? 4 : 2;
+  static constexpr int kRB = BK * kES;
+  static constexpr int kA = kTcBM * kRB;
+  static constexpr int kB = BN * kRB;
   static constexpr int kStage = NS * kA + NS * kB;
   static constexpr int kBars = 2 * STAGES + 5;  // full, empty, accumulator full x2, empty x2, done
   static constexpr int kBytes = STAGES * kStage + 8 * kBars + 16 + 1024;
 };
 
-template <int BN, int STAGES, int NS, int BK>
+template <int BN, int STAGES, int NS, int BK, bool TF32 = false, int CM = 1>
 __global__ void __launch_bounds__(192, 1)
     tc_gemm_persist_kernel(const __grid_constant__ TcMaps maps, int M, int N, int kblocks, int kb_per_split, int nN,
                            int nM, int nitems, float* __restrict__ out, long ld_out, long split_stride,
                            int* __restrict__ err) {
-  using L = TcPSmem<BN, STAGES, NS, BK>;
+  using L = TcPSmem<BN, STAGES, NS, BK, TF32>;
+  static_assert(!TF32 || NS == 1, "TF32 operands have one part");
+  static_assert(CM == 1 || CM == 2 || CM == 4, "clusters of 1, 2 or 4 CTAs");
+  static_assert((BN / CM) % 8 == 0, "B slices of whole 8-row swizzle groups");
+  constexpr uint16_t kMask = uint16_t((1u << CM) - 1);
   static_assert(2 * BN <= 512, "two accumulators must fit TMEM");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -289,10 +357,13 @@ __global__ void __launch_bounds__(192, 1)
   const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * STAGES, accf0 = full0 + 16 * STAGES,
                  acce0 = accf0 + 16, done_bar = accf0 + 32;
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int crank = CM > 1 ? int(cluster_ctarank()) : 0;
+  const int first = int(blockIdx.x) / CM, stride = int(gridDim.x) / CM;  // this cluster's items
+  const int nMg = (nM + CM - 1) / CM;                                       // M tile groups
   auto coords = [&](int item, int& n0, int& m0, int& z, int& kb0, int& nkb) {
     n0 = (item % nN) * BN;
-    m0 = ((item / nN) % nM) * kTcBM;
-    z = item / (nN * nM);
+    m0 = (((item / nN) % nMg) * CM + crank) * kTcBM;
+    z = item / (nN * nMg);
     kb0 = z * kb_per_split;
     nkb = max(0, min(kblocks, kb0 + kb_per_split) - kb0);
   };
@@ -300,7 +371,8 @@ __global__ void __launch_bounds__(192, 1)
 
   if (threadIdx.x == 0) {
     s_abort = 0;
-    for (int s = 0; s < 2 * STAGES; ++s) mbar_init(smem_u32(bars + s), 1);
+    for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(bars + s), 1);
+    for (int s = STAGES; s < 2 * STAGES; ++s) mbar_init(smem_u32(bars + s), CM);
     mbar_init(accf0, 1);
     mbar_init(accf0 + 8, 1);
     mbar_init(acce0, 4);
@@ -317,12 +389,13 @@ __global__ void __launch_bounds__(192, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  if constexpr (CM > 1) cluster_sync_all();  // every CTA's barriers initialised before any multicast
 
   if (warp == 0 && lane == 0) {
     // producer
     int g = 0;
     bool stop = false;
-    for (int item = blockIdx.x; item < nitems && !stop; item += gridDim.x) {
+    for (int item = first; item < nitems && !stop; item += stride) {
       int n0, m0, z, kb0, nkb;
       coords(item, n0, m0, z, kb0, nkb);
       for (int kb = 0; kb < nkb; ++kb) {
@@ -344,7 +417,11 @@ __global__ void __launch_bounds__(192, 1)
 #pragma unroll
         for (int p = 0; p < NS; ++p) {
           tma_load_2d(smem_u32(st + p * L::kA), &maps.a[p], kc, m0, fb);
-          tma_load_2d(smem_u32(st + NS * L::kA + p * L::kB), &maps.b[p], kc, n0, fb);
+          if constexpr (CM == 1)
+            tma_load_2d(smem_u32(st + NS * L::kA + p * L::kB), &maps.b[p], kc, n0, fb);
+          else  // this CTA's slice of the shared B tile, to every CTA of the cluster
+            tma_load_2d_mc(smem_u32(st + NS * L::kA + p * L::kB + crank * (L::kB / CM)), &maps.b[p], kc,
+                           n0 + crank * (BN / CM), fb, kMask);
         }
         ++g;
       }
@@ -353,12 +430,20 @@ __global__ void __launch_bounds__(192, 1)
       // wind down: wait (bounded) for the copies this thread issued into stages not yet consumed
       for (int k = max(0, g - STAGES); k < g; ++k) mbar_wait(full0 + 8 * (k % STAGES), (k / STAGES) & 1);
     }
+    if constexpr (CM > 1) {
+      // the cluster's last releases of this CTA's stages (remote MMA commits) have landed (bounded)
+      for (int k = max(0, g - STAGES); k < g; ++k)
+        if (!mbar_wait(empty0 + 8 * (k % STAGES), (k / STAGES) & 1)) {
+          atomicExch(&s_abort, 1);
+          break;
+        }
+    }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
-    constexpr uint32_t idesc = idesc_bf16_f32(BN);
+    constexpr uint32_t idesc = idesc_f32acc<TF32>(BN);
     int g = 0, t = 0;
     bool stop = false;
-    for (int item = blockIdx.x; item < nitems && !stop; item += gridDim.x, ++t) {
+    for (int item = first; item < nitems && !stop; item += stride, ++t) {
       int n0, m0, z, kb0, nkb;
       coords(item, n0, m0, z, kb0, nkb);
       const int b = t & 1;
@@ -384,20 +469,23 @@ __global__ void __launch_bounds__(192, 1)
         const uint32_t a0 = smem_u32(smem + s * L::kStage);
         const uint32_t b0 = a0 + NS * L::kA;
 #pragma unroll
-        for (int ks = 0; ks < BK / 16; ++ks) {
+        for (int ks = 0; ks < L::kRB / 32; ++ks) {
           const uint32_t off = ks * 32;
-          umma_bf16(acc, sw_desc<BK>(a0 + off), sw_desc<BK>(b0 + off), idesc, (kb | ks) != 0);
+          umma<TF32>(acc, sw_desc<L::kRB>(a0 + off), sw_desc<L::kRB>(b0 + off), idesc, (kb | ks) != 0);
           if constexpr (NS >= 2) {
-            umma_bf16(acc, sw_desc<BK>(a0 + off), sw_desc<BK>(b0 + L::kB + off), idesc, 1);
-            umma_bf16(acc, sw_desc<BK>(a0 + L::kA + off), sw_desc<BK>(b0 + off), idesc, 1);
+            umma<TF32>(acc, sw_desc<L::kRB>(a0 + off), sw_desc<L::kRB>(b0 + L::kB + off), idesc, 1);
+            umma<TF32>(acc, sw_desc<L::kRB>(a0 + L::kA + off), sw_desc<L::kRB>(b0 + off), idesc, 1);
           }
           if constexpr (NS == 3) {
-            umma_bf16(acc, sw_desc<BK>(a0 + off), sw_desc<BK>(b0 + 2 * L::kB + off), idesc, 1);
-            umma_bf16(acc, sw_desc<BK>(a0 + L::kA + off), sw_desc<BK>(b0 + L::kB + off), idesc, 1);
-            umma_bf16(acc, sw_desc<BK>(a0 + 2 * L::kA + off), sw_desc<BK>(b0 + off), idesc, 1);
+            umma<TF32>(acc, sw_desc<L::kRB>(a0 + off), sw_desc<L::kRB>(b0 + 2 * L::kB + off), idesc, 1);
+            umma<TF32>(acc, sw_desc<L::kRB>(a0 + L::kA + off), sw_desc<L::kRB>(b0 + L::kB + off), idesc, 1);
+            umma<TF32>(acc, sw_desc<L::kRB>(a0 + 2 * L::kA + off), sw_desc<L::kRB>(b0 + off), idesc, 1);
           }
         }
-        umma_commit(empty0 + 8 * s);
+        if constexpr (CM == 1)
+          umma_commit(empty0 + 8 * s);
+        else
+          umma_commit_mc(empty0 + 8 * s, kMask);  // the stage is free in this CTA for every CTA's producer
         ++g;
       }
       umma_commit(accf0 + 8 * b);  // completes when the item's MMAs have
@@ -407,7 +495,7 @@ __global__ void __launch_bounds__(192, 1)
     // epilogue
     const int q = warp % 4;
     int t = 0;
-    for (int item = blockIdx.x; item < nitems; item += gridDim.x, ++t) {
+    for (int item = first; item < nitems; item += stride, ++t) {
       if (aborted()) break;
       int n0, m0, z, kb0, nkb;
       coords(item, n0, m0, z, kb0, nkb);
@@ -449,6 +537,7 @@ __global__ void __launch_bounds__(192, 1)
   if (aborted() && threadIdx.x == 0) atomicExch(err, 1);
   tc_fence_before();
   __syncthreads();
+  if constexpr (CM > 1) cluster_sync_all();  // no CTA leaves while a cluster peer still runs
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
 }
 
@@ -459,12 +548,20 @@ __global__ void __launch_bounds__(192, 1)
 // A 2-D tensor map of a row-major BF16 matrix [rows][cols] (row stride ld elements) whose box is
 // bk columns (64: 128-byte swizzle; 32: 64-byte swizzle) by box_rows rows.
 CUtensorMap make_tmap_bf16(const void* base, long rows, long cols, long ld, int box_rows, int bk = kTcBK);
+// The same over an FP32 matrix (TF32 operands): box bk = 32 columns (128 bytes, 128-byte swizzle)
+// or 16 (64 bytes, 64-byte swizzle).
+CUtensorMap make_tmap_f32(const void* base, long rows, long cols, long ld, int box_rows, int bk = 32);
 
-// The BF16 parts of one operand: ns = 2 (hi, lo) or 3 (hi, mid, lo) tensor maps.
+// The parts of one operand: ns = 2 (hi, lo) or 3 (hi, mid, lo) BF16 tensor maps, or one FP32 map
+// of TF32-rounded values (tf32, ns = 1, bk = 32).
 struct TcOperand {
   CUtensorMap m[3];
   int ns = 2;
   int bk = kTcBK;  // K columns of the maps' box
+  bool tf32 = false;
+  // the matrices behind the maps (for maps with other boxes: the B slices of a cluster launch)
+  const void* base[3] = {nullptr, nullptr, nullptr};
+  long rows = 0, cols = 0, ld = 0;
 };
 
 // Launches the split-precision product of A [M][K] and B [N][K] (K-major, both split into A.ns
@@ -477,12 +574,13 @@ int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int 
 // The BN and split count tc_gemm_launch picks for (M, N, K), ns parts, at most max_splits splits.
 void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* bn, int* splits, int kb_cap = 0);
 
-// Launch with an explicit tile width bn (128: three pipeline stages; 256: two; two-part operands
-// only) and split count (0: the heuristic's count for that bn); B's tensor maps must have boxes of
-// bn rows. Returns the splits used.
+// Launch with an explicit tile width bn (128: three pipeline stages; 256: two; two-part BF16 or TF32
+// operands) and split count (0: the heuristic's count for that bn); B's tensor maps must have boxes
+// of bn rows. TF32 operands: bn 128 (six stages) or 256 (four), either kernel. Returns the splits
+// used.
 int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn, int splits, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int* d_err, const char* prof_name = "tc_gemm",
-                        bool persist = false);
+                        bool persist = false, int cm = 1);
 // The variant with K blocks of 32 (64-byte swizzle) and four pipeline stages, bn = 256; A and B
 // maps built with bk = 32.
 
@@ -494,6 +592,7 @@ struct TcTune {
   int bn = 0, splits = 0, bk = kTcBK;
   float ms = 0.f;
   bool persist = false;  // the persistent kernel (one CTA per SM, two accumulators)
+  int cm = 1;            // ... in clusters of cm CTAs sharing the B tile (multicast)
 };
 
 // The autotuner: times every candidate tile shape (bn 128 with three stages, bn 256 with two; the

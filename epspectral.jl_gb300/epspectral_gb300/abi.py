@@ -28,11 +28,11 @@ STATUS_NAMES = {
 
 EPSP_F64, EPSP_F32, EPSP_BF16 = 0, 1, 2
 EPSP_METAL, EPSP_SEMICONDUCTOR = 0, 1
-EPSP_PATH_DIRECT_FP64, EPSP_PATH_GEMM_FP64, EPSP_PATH_GEMM_BF16 = 0, 1, 2
+EPSP_PATH_DIRECT_FP64, EPSP_PATH_GEMM_FP64, EPSP_PATH_GEMM_BF16, EPSP_PATH_GEMM_TF32 = 0, 1, 2, 3
 EPSP_SOLVER_GMRES, EPSP_SOLVER_FIXED_POINT = 0, 1
 
 PATHS = {"direct_fp64": EPSP_PATH_DIRECT_FP64, "gemm_fp64": EPSP_PATH_GEMM_FP64,
-         "gemm_bf16": EPSP_PATH_GEMM_BF16}
+         "gemm_bf16": EPSP_PATH_GEMM_BF16, "gemm_tf32": EPSP_PATH_GEMM_TF32}
 
 c_double_p = C.POINTER(C.c_double)
 c_int32_p = C.POINTER(C.c_int32)

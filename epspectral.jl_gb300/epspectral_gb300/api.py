@@ -76,6 +76,8 @@ def lib():
         "epsp_ladder_set_gemm_config": (C.c_int, [vp, i32, i32, i32]),
         "epsp_ladder_gemm_persistent": (C.c_int, [vp, P(i32)]),
         "epsp_ladder_set_gemm_persistent": (C.c_int, [vp, i32]),
+        "epsp_ladder_gemm_cluster": (C.c_int, [vp, P(i32)]),
+        "epsp_ladder_set_gemm_cluster": (C.c_int, [vp, i32]),
         "epsp_ladder_run_batched": (C.c_int, [vp, c_double_p, c_double_p, c_double_p, i64, c_double_p, i64, d, i32, i32,
                                               c_double_p, c_double_p, u8p, c_int32_p, P(epsp_ladder_history),
                                               c_double_p]),
@@ -279,27 +281,30 @@ class LadderPlan:
                                                C.byref(self.handle)))
 
     def gemm_config(self) -> dict:
-        """The contraction's tile shape chosen by the autotuner at setup (GEMM_BF16 plans)."""
+        """The contraction's tile shape chosen by the autotuner at setup (GEMM_BF16 / GEMM_TF32 plans)."""
         bn, sp, bk, ms, mh = C.c_int32(), C.c_int32(), C.c_int32(), C.c_double(), C.c_double()
         self.ctx.check(lib().epsp_ladder_gemm_config(self.handle, C.byref(bn), C.byref(sp), C.byref(bk), C.byref(ms),
                                                      C.byref(mh)))
-        on = C.c_int32()
+        on, cm = C.c_int32(), C.c_int32()
         self.ctx.check(lib().epsp_ladder_gemm_persistent(self.handle, C.byref(on)))
-        return dict(bn=bn.value, splits=sp.value, bk=bk.value, persistent=bool(on.value), ms=ms.value,
-                    ms_heuristic=mh.value)
+        self.ctx.check(lib().epsp_ladder_gemm_cluster(self.handle, C.byref(cm)))
+        return dict(bn=bn.value, splits=sp.value, bk=bk.value, persistent=bool(on.value), cluster=cm.value,
+                    ms=ms.value, ms_heuristic=mh.value)
 
-    def set_gemm_config(self, bn: int, splits: int, bk: int = 64, persistent: bool = False):
-        """Overrides the autotuner's tile shape of the contraction (GEMM_BF16 plans); persistent: one
-        CTA per SM over all tiles (bn 256, bk 32 only)."""
+    def set_gemm_config(self, bn: int, splits: int, bk: int = 64, persistent: bool = False, cluster: int = 1):
+        """Overrides the autotuner's tile shape of the contraction (GEMM_BF16 / GEMM_TF32 plans);
+        persistent: one CTA per SM over all tiles (BF16: bn 256, bk 32 only; TF32: bk 32, either bn);
+        cluster: the persistent kernel in clusters of 2 or 4 CTAs sharing the B tile (multicast)."""
         self.ctx.check(lib().epsp_ladder_set_gemm_config(self.handle, int(bn), int(splits), int(bk)))
         self.ctx.check(lib().epsp_ladder_set_gemm_persistent(self.handle, 1 if persistent else 0))
+        self.ctx.check(lib().epsp_ladder_set_gemm_cluster(self.handle, int(cluster)))
 
     def run(self, sigma, mu, Tlist, Omegas, *, solver="gmres", rtol=1e-2, maxiter=30, store_vertex=False,
             batch_rhs=None):
         """The (T, Ω) loops of _loop_ladder (src/ladder.jl:303-379).
 
         batch_rhs = R solves up to R (T, Ω) pairs together as GMRES right-hand sides, each from
-        x0 = 0 (epsp_ladder_run_batched; GEMM_BF16 plans); None keeps the reference's order and
+        x0 = 0 (epsp_ladder_run_batched; GEMM_BF16 / GEMM_TF32 plans); None keeps the reference's order and
         warm starts."""
         M = self.M
         if solver not in ("gmres", "fixed_point"):

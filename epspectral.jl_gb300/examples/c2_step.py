@@ -1,9 +1,10 @@
 """Example: the benchmark step on the 3-band t2g model at 16^3 k points -- scGD0 to 1e-6 eV on the
 tensor-core path (from a trained warm start when --warm names a saved network, e.g. the one
-`bench.py --save-warm` writes), then the ladder σ(Ω) at Ω = 0.1 eV by GMRES -- repeated --steps
-times, each part inside an NVTX range ("scgd0", "ladder") so that Nsight Compute can select it.
+`bench.py --save-warm` writes), then the ladder σ(Ω) at Ω = 0.1 eV by GMRES (the contraction in
+TF32, or --ladder-path gemm_bf16 for BF16x3) -- repeated --steps times, each part inside an NVTX
+range ("scgd0", "ladder") so that Nsight Compute can select it.
 
-    python epspectral.jl_gb300/examples/c2_step.py [--warm net.npz] [--steps N]
+    python epspectral.jl_gb300/examples/c2_step.py [--warm net.npz] [--steps N] [--ladder-path P]
 """
 import argparse
 import os
@@ -28,6 +29,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--warm", default=None)
     ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--ladder-path", default="gemm_tf32", choices=("gemm_tf32", "gemm_bf16"))
     a = ap.parse_args()
     push, pop = nvtx()
     s = synthetic.cubic_t2g_setup(N=16, seed=0)
@@ -37,7 +39,7 @@ def main():
     ctx = api.Context(0)
     ws = W.WarmStart.load(a.warm, ctx=ctx) if a.warm else None
     sp = api.Scgd0Plan(s, path="gemm_bf16", omega_acoustic=1e-4, ctx=ctx)
-    lp = api.LadderPlan(s, path="gemm_bf16", omega_acoustic=1e-4, ctx=ctx)
+    lp = api.LadderPlan(s, path=a.ladder_path, omega_acoustic=1e-4, ctx=ctx)
     for k in range(a.steps):
         push("scgd0")
         ctx.timer_begin()

@@ -12,12 +12,13 @@ module EPSpectralGB300
 const LIB = get(ENV, "EPSPECTRAL_GB300_LIB", joinpath(@__DIR__, "..", "epspectral_gb300", "libepspectral_gb300.so"))
 
 const EPSP_OK, EPSP_EINVAL, EPSP_ENOMEM, EPSP_ENOROOT_MU = 0, 1, 2, 3
-const PATHS = (direct_fp64 = Int32(0), gemm_fp64 = Int32(1), gemm_bf16 = Int32(2))
+const PATHS = (direct_fp64 = Int32(0), gemm_fp64 = Int32(1), gemm_bf16 = Int32(2), gemm_tf32 = Int32(3))
 
 """The backend value `run_scgd0(...; backend = GB300Backend())` selects."""
 Base.@kwdef struct GB300Backend
     device::Int = 0
     path::Symbol = :gemm_bf16
+    ladder_path::Union{Nothing, Symbol} = nothing  # the ladder's path when it differs (e.g. :gemm_tf32, ladder only)
     batch_rhs::Union{Nothing, Int} = nothing   # solve up to this many (T, Ω) pairs together (GMRES, :gemm_bf16)
 end
 
@@ -169,7 +170,8 @@ function loop_ladder(ladder, Σ, μ, Tlist, Ωs; solver, rtol, maxiter, store_ve
         J = store_vertex ? zeros(ComplexF64, nω, 4, 3, 2, ni, nΩ, nT) : nothing
         GC.@preserve a Σh μh Th Ωh σb σl conv niter J begin
             m = Ref(model_struct(a))
-            opts = Ref(Options(getfield(PATHS, backend.path), verbosity, gpu_tile === nothing ? 0 : gpu_tile, ω_acoustic))
+            lpath = backend.ladder_path === nothing ? backend.path : backend.ladder_path
+            opts = Ref(Options(getfield(PATHS, lpath), verbosity, gpu_tile === nothing ? 0 : gpu_tile, ω_acoustic))
             plan = Ref{Ptr{Cvoid}}(C_NULL)
             check(ctx, ccall((:epsp_ladder_setup, LIB), Cint, (Ptr{Cvoid}, Ref{Model}, Ref{Options}, Ref{Ptr{Cvoid}}),
                 ctx, m, opts, plan))

@@ -59,8 +59,12 @@ enum { EPSP_METAL = 0, EPSP_SEMICONDUCTOR = 1 };
  *                coupling matrix, the ladder's shift sums regrouped per mode; FP64 arithmetic.
  *  GEMM_BF16X3 : as GEMM_FP64, with the contractions on the tcgen05 tensor cores in BF16 hi/lo
  *                split precision (three products, FP32 accumulation); the chemical-potential
- *                bisection, the carrier integral and the GMRES orthogonalisation stay FP64. */
-enum { EPSP_PATH_DIRECT_FP64 = 0, EPSP_PATH_GEMM_FP64 = 1, EPSP_PATH_GEMM_BF16 = 2 };
+ *                bisection, the carrier integral and the GMRES orthogonalisation stay FP64.
+ *  GEMM_TF32   : ladder plans only: as GEMM_BF16X3, with the ladder contraction as one TF32 product
+ *                (operands rounded to TF32, FP32 accumulation): two thirds of the BF16X3 tensor
+ *                time, ~2^-11 relative rounding per operand element. scGD0 plans refuse it
+ *                (EPSP_EUNSUPPORTED). */
+enum { EPSP_PATH_DIRECT_FP64 = 0, EPSP_PATH_GEMM_FP64 = 1, EPSP_PATH_GEMM_BF16 = 2, EPSP_PATH_GEMM_TF32 = 3 };
 
 /* Ladder solver (src/ladder.jl:340-369). */
 enum { EPSP_SOLVER_GMRES = 0, EPSP_SOLVER_FIXED_POINT = 1 };
@@ -256,10 +260,17 @@ epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, i
  * splits within what the plan's partial buffer holds. */
 epsp_status epsp_ladder_set_gemm_config(epsp_ladder_plan* plan, int32_t bn, int32_t splits, int32_t bk);
 /* Whether the contraction runs as the persistent kernel (one CTA per SM over all tiles, two TMEM
- * accumulators so that a tile's epilogue overlaps the next tile's products; bn 256 with bk 32
- * only): read, and set (on = 0 or 1; EPSP_EINVAL for another tile shape). Same results bitwise. */
+ * accumulators so that a tile's epilogue overlaps the next tile's products; GEMM_BF16: bn 256 with
+ * bk 32 only; GEMM_TF32: either bn): read, and set (on = 0 or 1; EPSP_EINVAL for another tile
+ * shape; off resets the cluster size to 1). Same results bitwise. */
 epsp_status epsp_ladder_gemm_persistent(const epsp_ladder_plan* plan, int32_t* on);
 epsp_status epsp_ladder_set_gemm_persistent(epsp_ladder_plan* plan, int32_t on);
+/* The persistent contraction's cluster size cm (1, 2 or 4; 2 at most with bn 128; cm > 1 needs the
+ * persistent kernel): cm CTAs on consecutive M tiles share the B tile through TMA multicast, each
+ * loading 1/cm of it, which cuts B's L2-to-SM traffic by cm. Read, and set (EPSP_EINVAL outside
+ * those rules). Same results bitwise; epsp_ladder_set_gemm_config resets it to 1. */
+epsp_status epsp_ladder_gemm_cluster(const epsp_ladder_plan* plan, int32_t* cm);
+epsp_status epsp_ladder_set_gemm_cluster(epsp_ladder_plan* plan, int32_t cm);
 
 /* One application LJ = L(J) of the ladder kernel at temperature T, chemical potential mu and
  * probe frequency Omega, with sigma_T [nω, ni] complex the self-energy of that temperature:

@@ -708,7 +708,7 @@ void conductivity(const double* J, const double* v, const double* w_i, const dou
 void ladder_contract_sample(const Ladder& L, double T, double w_ac, const double* J, int64_t ia, int64_t ib) {
   const Model& M = L.M;
   const epsp_model* mp = M.m;
-  const int64_t nw = M.nw, ni = M.ni, nm = M.nm, ns = L.nshift;
+  const int64_t nw = M.nw, nm = M.nm, ns = L.nshift;
   const int64_t nrow = nw * 16, nsel = ib - ia, ncol = 6 * nsel;
   std::vector<double> Cp(size_t(nrow * ncol), 0.0), Cm(size_t(nrow * ncol), 0.0);
   for (const auto& ch : L.chunks) {

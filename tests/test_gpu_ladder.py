@@ -59,7 +59,8 @@ def test_apply_matches_oracle(api, oracle, request, case, Omega, k):
     for iT in range(2):
         args = (J, c["sigma"][:, :, iT], c["mu"][iT], c["Tlist"][iT], Omega)
         ref = oracle.apply_ladder_kernel(s, *args, omega_acoustic=W_AC)
-        for path, tol in (("direct_fp64", 1e-10), ("gemm_fp64", 1e-10), ("gemm_bf16", 1e-4)):
+        # TF32 rounds both operands of the contraction to 11 significant bits (2^-12 relative)
+        for path, tol in (("direct_fp64", 1e-10), ("gemm_fp64", 1e-10), ("gemm_bf16", 1e-4), ("gemm_tf32", 1e-3)):
             for tile in ((None, 7) if path == "direct_fp64" else (None,)):
                 got = api.apply_ladder_kernel(s, *args, omega_acoustic=W_AC, path=path, gpu_tile=tile)
                 assert rel(got, ref) <= tol, (path, tile, rel(got, ref))
@@ -81,8 +82,9 @@ def test_loop_matches_oracle(api, oracle, cc):
         again = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], Omegas, path=path, **kw)
         assert np.array_equal(again["J"], got["J"]) and np.array_equal(again["sigma_ladder"], got["sigma_ladder"])
         assert all(np.array_equal(a["norms"], b["norms"]) for a, b in zip(again["history"].ravel(), got["history"].ravel()))
-    bf = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], Omegas, path="gemm_bf16", **kw)
-    assert rel(bf["sigma_ladder"], ref["sigma_ladder"]) <= 1e-4
+    for path in ("gemm_bf16", "gemm_tf32"):  # the mixed-precision contract: σ to 1e-4 relative
+        bf = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], Omegas, path=path, **kw)
+        assert rel(bf["sigma_ladder"], ref["sigma_ladder"]) <= 1e-4, (path, rel(bf["sigma_ladder"], ref["sigma_ladder"]))
     # fixed point, streamed-size chunks, Ω > 0 (test/test_ladder_gpu.jl:134-139)
     fk = dict(solver="fixed_point", rtol=1e-6, maxiter=200, omega_acoustic=W_AC)
     fref = oracle.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], [0.1], **fk)
@@ -95,7 +97,7 @@ def test_holstein_current_correction_vanishes(api, hsym):
     # test/test_ladder_holstein.jl:5-26 on the GPU paths; the tensor-core path keeps its vertices in
     # FP32, so there the correction vanishes to FP32 rounding (a surviving correction is ~1e-2)
     c = hsym
-    for path, tol in (("direct_fp64", 1e-9), ("gemm_fp64", 1e-9), ("gemm_bf16", 1e-6)):
+    for path, tol in (("direct_fp64", 1e-9), ("gemm_fp64", 1e-9), ("gemm_bf16", 1e-6), ("gemm_tf32", 1e-4)):
         out = api.loop_ladder(c["setup"], c["sigma"], c["mu"], c["Tlist"], [0.0, 0.2], path=path, omega_acoustic=W_AC)
         assert np.linalg.norm(out["sigma_ladder"] - out["sigma_bubble"]) <= tol * np.linalg.norm(out["sigma_bubble"])
         assert out["converged"].all()
@@ -152,12 +154,36 @@ def test_batched_right_hand_sides_match_the_sequential_solves(api, oracle, cc):
     plan.close()
 
 
+def test_tf32_batched_right_hand_sides(api, oracle, cc):
+    # the batched solves on the TF32 path: σ of every pair against the FP64 oracle to 1e-4
+    # relative (rtol 1e-5: the operator's TF32 rounding is ~1e-4 per element, the Krylov vectors
+    # FP32), and each pair against the sequential TF32 solve
+    c = cc
+    s = c["setup"]
+    Omegas = [0.0, 0.05, 0.1]
+    plan = api.LadderPlan(s, path="gemm_tf32", omega_acoustic=W_AC)
+    kw = dict(rtol=1e-5, maxiter=60)
+    seq = plan.run(c["sigma"], c["mu"], c["Tlist"], Omegas, **kw)
+    bat = plan.run(c["sigma"], c["mu"], c["Tlist"], Omegas, batch_rhs=4, **kw)
+    assert bat["converged"].all() and seq["converged"].all()
+    ref = oracle.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], Omegas, solver="gmres", omega_acoustic=W_AC,
+                             rtol=1e-9, maxiter=60)
+    assert rel(bat["sigma_ladder"], ref["sigma_ladder"]) <= 1e-4, rel(bat["sigma_ladder"], ref["sigma_ladder"])
+    assert rel(seq["sigma_ladder"], ref["sigma_ladder"]) <= 1e-4, rel(seq["sigma_ladder"], ref["sigma_ladder"])
+    plan.close()
+
+
+def test_tf32_is_a_ladder_path_only(api, cc):
+    with pytest.raises(api.EpspError):
+        api.Scgd0Plan(cc["setup"], path="gemm_tf32", omega_acoustic=W_AC)
+
+
 def test_streamed_g2_gives_the_resident_ladder(api, cc):
     # the regrouped paths build G̃ from g2 streamed star by star (gpu_tile inner states per chunk):
     # bitwise the one-chunk result
     c = cc
     s = c["setup"]
-    for path in ("gemm_fp64", "gemm_bf16"):
+    for path in ("gemm_fp64", "gemm_bf16", "gemm_tf32"):
         one = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], [0.1], path=path, omega_acoustic=W_AC)
         got = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], [0.1], path=path, gpu_tile=5, omega_acoustic=W_AC)
         assert np.array_equal(got["sigma_ladder"], one["sigma_ladder"]), path
@@ -178,7 +204,7 @@ def test_apply_on_fine_shift_grids(api, oracle, unit):
     J[-1] = 0
     T = 300 * synthetic.KELVIN
     ref = oracle.apply_ladder_kernel(s, J, sig, 0.0, T, 0.05, omega_acoustic=W_AC)
-    for path, tol in (("gemm_fp64", 1e-10), ("gemm_bf16", 1e-4)):
+    for path, tol in (("gemm_fp64", 1e-10), ("gemm_bf16", 1e-4), ("gemm_tf32", 1e-3)):
         got = api.apply_ladder_kernel(s, J, sig, 0.0, T, 0.05, omega_acoustic=W_AC, path=path)
         assert np.all(np.isfinite(got)) and rel(got, ref) <= tol, (path, rel(got, ref))
 
@@ -206,13 +232,37 @@ def test_every_contraction_tile_shape_matches_the_oracle(api, oracle, cc, unit):
             got = plan.apply(J, sig, c["mu"][0], T, 0.07)
             assert np.all(np.isfinite(got)) and rel(got, ref) <= 1e-4, (bn, bk, sp, rel(got, ref))
             if (bn, bk) == (256, 32):
-                # the persistent kernel (one CTA per SM over all tiles, two TMEM accumulators) runs
-                # every tile's products in the same order: bitwise the same result
-                plan.set_gemm_config(bn, sp, bk, persistent=True)
-                assert plan.gemm_config()["persistent"]
-                assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp)
+                # the persistent kernel (one CTA per SM over all tiles, two TMEM accumulators), alone
+                # and in clusters of 2 and 4 CTAs sharing B by multicast, runs every tile's products
+                # in the same order: bitwise the same result
+                for cm in (1, 2, 4):
+                    plan.set_gemm_config(bn, sp, bk, persistent=True, cluster=cm)
+                    assert plan.gemm_config()["persistent"] and plan.gemm_config()["cluster"] == cm
+                    assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, cm)
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(128, 1, 32)
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(128, 1, 64, persistent=True)
+    with pytest.raises(ArgumentError):
+        plan.set_gemm_config(256, 1, 32, persistent=False, cluster=2)
+    plan.close()
+    # TF32: one product per K step of 8 (K boxes of 32 FP32 = 128 bytes), BN 128 (six stages) and
+    # 256 (four), one and two splits, each also as the persistent kernel (bitwise the same)
+    plan = api.LadderPlan(s, path="gemm_tf32", omega_acoustic=W_AC)
+    assert plan.gemm_config()["bk"] == 32
+    for bn, bk in ((128, 32), (256, 32)):
+        for sp in (1, 2):
+            plan.set_gemm_config(bn, sp, bk)
+            got = plan.apply(J, sig, c["mu"][0], T, 0.07)
+            assert np.all(np.isfinite(got)) and rel(got, ref) <= 1e-3, (bn, bk, sp, rel(got, ref))
+            for cm in ((1, 2, 4) if (bn, bk) == (256, 32) else (1, 2)):
+                plan.set_gemm_config(bn, sp, bk, persistent=True, cluster=cm)
+                assert plan.gemm_config()["persistent"] and plan.gemm_config()["cluster"] == cm
+                assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, cm)
+    with pytest.raises(ArgumentError):
+        plan.set_gemm_config(256, 1, 64)
+    with pytest.raises(ArgumentError):
+        plan.set_gemm_config(128, 1, 32, persistent=True, cluster=4)
+    with pytest.raises(ArgumentError):
+        plan.set_gemm_config(128, 1, 16)
     plan.close()
