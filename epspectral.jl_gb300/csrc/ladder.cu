@@ -81,6 +81,7 @@ struct LadderPlan {
   int bn = 128, splits = 1, bk = kTcBK;  // the contraction's tile shape, picked by the autotuner at setup
   bool persist = false;                  // ... and whether it runs as the persistent kernel
   int cm = 1;                            // ... in clusters of cm CTAs sharing the B tile
+  bool pair = false;                     // ... or as the CTA-pair kernel (cta_group::2)
   std::vector<TcTune> tune_all;
   float tune_ms_heuristic = 0.f;
   // exchange (both paths)
@@ -1506,6 +1507,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       P->bk = best.bk;
       P->persist = best.persist;
       P->cm = best.cm;
+      P->pair = best.pair;
       pick_contraction_operands(P);
       int terr = 0;
       P->d_err.download(&terr, 1, s);
@@ -1704,7 +1706,7 @@ static void apply_L(LadderPlan* P, const float2* J, float2* LJ, const float2* X 
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, px);
   int sp = tc_gemm_launch_with(ctx, P->opA, P->opG, P->bn, P->splits, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N,
-                               P->d_err.p, "tc_ladder", P->persist, P->cm);
+                               P->d_err.p, "tc_ladder", P->persist, P->cm, P->pair);
   // D stays as the contraction's split-K partials; y_split and finish add them as they read
   long pl = prof_begin(ctx, "lsum");
   y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), 1), 256, 0, s>>>(P->d_part.p, M, sp, M * N, int(nw), int(nwp),
@@ -2198,7 +2200,7 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const float2* X, int nA
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, px);
   int sp = tc_gemm_launch_with(ctx, B.opA, P->opG, P->bn, 0, int(Mt), int(N), int(P->Kx), B.part.p, Mt, Mt * N, P->d_err.p,
-                               "tc_ladder", P->persist, P->cm);
+                               "tc_ladder", P->persist, P->cm, P->pair);
   y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), unsigned(nA)), 256, 0, s>>>(
       B.part.p, Mt, sp, Mt * N, int(nw), int(nwp), N, P->Kp2, B.Yh.p, B.Yl.p);
   EPSP_LAUNCHED(ctx);
@@ -2579,6 +2581,7 @@ epsp_status epsp_ladder_set_gemm_config(epsp_ladder_plan* plan, int32_t bn, int3
     pick_contraction_operands(P);
     if (!tf && !(bn == 256 && bk == 32)) P->persist = false;
     P->cm = 1;
+    P->pair = false;
   });
 }
 
@@ -2597,6 +2600,7 @@ epsp_status epsp_ladder_set_gemm_persistent(epsp_ladder_plan* plan, int32_t on) 
       fail(EPSP_EINVAL, "the persistent BF16x3 kernel takes bn 256 with bk 32");
     P->persist = on != 0;
     if (!P->persist) P->cm = 1;
+    if (P->persist) P->pair = false;
   });
 }
 
@@ -2619,6 +2623,27 @@ epsp_status epsp_ladder_set_gemm_cluster(epsp_ladder_plan* plan, int32_t cm) {
   });
 }
 
+epsp_status epsp_ladder_gemm_pair(const epsp_ladder_plan* plan, int32_t* on) {
+  if (!plan || !on) return EPSP_EINVAL;
+  *on = reinterpret_cast<const LadderPlan*>(plan)->pair ? 1 : 0;
+  return EPSP_OK;
+}
+
+epsp_status epsp_ladder_set_gemm_pair(epsp_ladder_plan* plan, int32_t on) {
+  if (!plan) return EPSP_EINVAL;
+  auto* P = reinterpret_cast<LadderPlan*>(plan);
+  return lguard(P->ctx, [&] {
+    if (!tc_path(P->path)) fail(EPSP_EUNSUPPORTED, "tile shapes apply to tensor-core plans (GEMM_BF16, GEMM_TF32)");
+    if (on && (P->bn != 256 || P->bk != 32))
+      fail(EPSP_EINVAL, "the CTA-pair kernel takes bn 256 with bk 32");
+    P->pair = on != 0;
+    if (P->pair) {
+      P->persist = false;
+      P->cm = 1;
+    }
+  });
+}
+
 epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, int32_t* splits, int32_t* bk,
                                     double* ms_chosen, double* ms_heuristic) {
   if (!plan || !bn || !splits) return EPSP_EINVAL;
@@ -2628,7 +2653,9 @@ epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, i
   if (bk) *bk = P->bk;
   double best = 0;
   for (const auto& c : P->tune_all)
-    if (c.bn == P->bn && c.splits == P->splits && c.bk == P->bk && c.persist == P->persist && c.cm == P->cm) best = c.ms;
+    if (c.bn == P->bn && c.splits == P->splits && c.bk == P->bk && c.persist == P->persist && c.cm == P->cm &&
+        c.pair == P->pair)
+      best = c.ms;
   if (ms_chosen) *ms_chosen = best;
   if (ms_heuristic) *ms_heuristic = P->tune_ms_heuristic;
   return EPSP_OK;

@@ -167,6 +167,40 @@ static void launch_persist(Ctx* ctx, const TcOperand& A, const TcOperand& B, int
   EPSP_LAUNCHED(ctx);
 }
 
+// The CTA-pair kernel: clusters of two CTAs, each pair one 256 x BN tile (B halves of BN / 2 rows).
+template <int BN, int STAGES, int NS, int BK, bool TF32>
+static void launch_pair(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int kblocks, int per,
+                        int splits, float* out, long ld_out, long split_stride, int* d_err) {
+  using L = TcPairSmem<BN, STAGES, NS, BK, TF32>;
+  if (A.bk != BK || B.bk != BK) fail(EPSP_EINVAL, "operand tensor maps were built for another K block");
+  if (A.tf32 != TF32 || B.tf32 != TF32) fail(EPSP_EINVAL, "operand tensor maps were built for another element type");
+  auto* kern = tc_gemm_pair_kernel<BN, STAGES, NS, BK, TF32>;
+  static bool configured = false;  // one process, one attribute setting per instantiation
+  if (!configured) {
+    EPSP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::kBytes));
+    configured = true;
+  }
+  TcMaps maps;
+  for (int p = 0; p < 3; ++p) {
+    maps.a[p] = A.m[p < NS ? p : 0];
+    maps.b[p] = remap(B, p < NS ? p : 0, BN / 2);
+  }
+  cudaLaunchAttribute cl;
+  cl.id = cudaLaunchAttributeClusterDimension;
+  cl.val.clusterDim.x = 2;
+  cl.val.clusterDim.y = 1;
+  cl.val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(2 * ((N + BN - 1) / BN)), unsigned((M + 2 * kTcBM - 1) / (2 * kTcBM)), unsigned(splits));
+  cfg.blockDim = dim3(128);
+  cfg.dynamicSmemBytes = L::kBytes;
+  cfg.stream = ctx->stream;
+  cfg.attrs = &cl;
+  cfg.numAttrs = 1;
+  EPSP_CUDA(cudaLaunchKernelEx(&cfg, kern, maps, M, N, kblocks, per, out, ld_out, split_stride, d_err));
+  EPSP_LAUNCHED(ctx);
+}
+
 int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int K, float* out, long ld_out,
                    long split_stride, int max_splits, int* d_err, const char* prof_name, int kb_cap) {
   if (A.tf32 || B.tf32) fail(EPSP_EINVAL, "TF32 operands take tc_gemm_launch_with");
@@ -203,8 +237,10 @@ int tc_splits_for(Ctx* ctx, int M, int N, int K, int bn) {
 
 int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn, int splits, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int* d_err, const char* prof_name, bool persist,
-                        int cm) {
+                        int cm, bool pair) {
   if (bn != 128 && bn != 256) fail(EPSP_EINVAL, "tile width must be 128 or 256");
+  if (pair && (persist || cm != 1 || bn != 256))
+    fail(EPSP_EINVAL, "the CTA-pair kernel is one-tile, tile width 256, without clusters of its own");
   if (cm != 1 && cm != 2 && cm != 4) fail(EPSP_EINVAL, "clusters of 1, 2 or 4 CTAs");
   if (cm > 1 && !persist) fail(EPSP_EINVAL, "clusters are for the persistent kernel");
   if (cm > 1 && (bn == 128 ? cm > 2 : false)) fail(EPSP_EINVAL, "tile width 128 takes clusters of at most 2");
@@ -217,7 +253,9 @@ int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn
     const int per = (kblocks + splits - 1) / splits;
     splits = (kblocks + per - 1) / per;
     long pi = prof_begin(ctx, prof_name);
-    if (persist && bn == 256 && cm == 4)
+    if (pair)
+      launch_pair<256, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    else if (persist && bn == 256 && cm == 4)
       launch_persist<256, 4, 1, 32, true, 4>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
     else if (persist && bn == 256 && cm == 2)
       launch_persist<256, 4, 1, 32, true, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
@@ -243,8 +281,11 @@ int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn
   const int per = (kblocks + splits - 1) / splits;
   splits = (kblocks + per - 1) / per;
   if (persist && !(bk == 32 && bn == 256)) fail(EPSP_EINVAL, "the persistent kernel takes tile width 256 with K blocks of 32");
+  if (pair && bk != 32) fail(EPSP_EINVAL, "the BF16x3 CTA-pair kernel takes K blocks of 32");
   long pi = prof_begin(ctx, prof_name);
-  if (persist && cm == 4)
+  if (pair)
+    launch_pair<256, 6, 2, 32, false>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+  else if (persist && cm == 4)
     launch_persist<256, 4, 2, 32, false, 4>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   else if (persist && cm == 2)
     launch_persist<256, 4, 2, 32, false, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
@@ -292,13 +333,17 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
           cand.push_back(TcTune{bn, sp, 32, 0.f});
           cand.push_back(TcTune{bn, sp, 32, 0.f, true});
           cand.push_back(TcTune{bn, sp, 32, 0.f, true, 2});
-          if (bn == 256) cand.push_back(TcTune{bn, sp, 32, 0.f, true, 4});
+          if (bn == 256) {
+            cand.push_back(TcTune{bn, sp, 32, 0.f, true, 4});
+            cand.push_back(TcTune{bn, sp, 32, 0.f, false, 1, true});  // CTA pairs
+          }
           continue;
         }
         cand.push_back(TcTune{bn, sp, kTcBK, 0.f});
         if (bn == 256 && A32 && B256_32) {
           cand.push_back(TcTune{bn, sp, 32, 0.f});
           for (int cm : {1, 2, 4}) cand.push_back(TcTune{bn, sp, 32, 0.f, true, cm});
+          cand.push_back(TcTune{bn, sp, 32, 0.f, false, 1, true});  // CTA pairs
         }
       }
   }
@@ -315,7 +360,7 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
   // one untimed launch first, so that no candidate pays the first launch's costs
   if (!cand.empty())
     tc_gemm_launch_with(ctx, opA(cand[0]), opB(cand[0]), cand[0].bn, cand[0].splits, M, N, K, out, ld_out, split_stride,
-                        d_err, "autotune", cand[0].persist, cand[0].cm);
+                        d_err, "autotune", cand[0].persist, cand[0].cm, cand[0].pair);
   for (auto& c : cand) {
     const TcOperand& A_ = opA(c);
     const TcOperand& B = opB(c);
@@ -323,7 +368,7 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
     float ms = 0.f;
     EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
     tc_gemm_launch_with(ctx, A_, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune", c.persist,
-                        c.cm);
+                        c.cm, c.pair);
     EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
     EPSP_CUDA(cudaEventSynchronize(e1));
     EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
@@ -332,7 +377,7 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
       EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
       for (int r = 0; r < reps; ++r)
         tc_gemm_launch_with(ctx, A_, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune",
-                            c.persist, c.cm);
+                            c.persist, c.cm, c.pair);
       EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
       EPSP_CUDA(cudaEventSynchronize(e1));
       EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));

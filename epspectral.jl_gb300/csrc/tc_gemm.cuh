@@ -541,6 +541,192 @@ __global__ void __launch_bounds__(192, 1)
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
 }
 
+// ---- CTA-pair variant (tcgen05 cta_group::2) ----
+// A cluster of two CTAs computes a 256 x BN tile: rank r holds A rows m0 + 128 r.. and B rows
+// n0 + (BN / 2) r.. in its own shared memory (32 KB per TF32 stage instead of 48, so six stages fit
+// where four did), and one thread of rank 0 (the leader) issues every MMA with M = 256, which reads
+// both CTAs' operands and accumulates each CTA's 128 rows in that CTA's TMEM. Both CTAs' copies
+// complete on the leader's full barrier (expect_tx of both stages, set by the leader); the leader's
+// commits arrive on the empty barriers of both CTAs (each CTA's producer refills only its own
+// stages) and on both done barriers. TMEM is allocated and freed by a warp of each CTA together.
+// Per tile the K order is the one-tile kernel's, so the results are bitwise the same.
+template <int BN, int STAGES, int NS, int BK, bool TF32>
+struct TcPairSmem {
+  static constexpr int kES = TF32 ? 4 : 2;
+  static constexpr int kRB = BK * kES;
+  static constexpr int kA = kTcBM * kRB;       // this CTA's 128 A rows
+  static constexpr int kBh = (BN / 2) * kRB;   // this CTA's half of the B tile
+  static constexpr int kStage = NS * kA + NS * kBh;
+  static constexpr int kBars = 2 * STAGES + 1;  // full, empty, done
+  static constexpr int kBytes = STAGES * kStage + 8 * kBars + 16 + 1024;
+};
+
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+// A tiled load into this CTA's shared memory completing on an mbarrier of either CTA of the pair.
+__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(dst),
+      "l"(map), "r"(c0), "r"(c1), "r"(bar)
+      : "memory");
+}
+template <bool TF32>
+__device__ __forceinline__ void umma_pair(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+  if constexpr (TF32)
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+  else
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit_pair(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
+      "h"(uint16_t(3))
+      : "memory");
+}
+// Instruction descriptor with M = 256 (the pair's tile).
+template <bool TF32>
+__host__ __device__ constexpr uint32_t idesc_pair(int n) {
+  return (1u << 4) | ((TF32 ? 2u : 1u) << 7) | ((TF32 ? 2u : 1u) << 10) | (uint32_t(n >> 3) << 17) |
+         (uint32_t(256 >> 4) << 24);
+}
+
+template <int BN, int STAGES, int NS, int BK, bool TF32>
+__global__ void __launch_bounds__(128, 1)
+    tc_gemm_pair_kernel(const __grid_constant__ TcMaps maps, int M, int N, int kblocks, int kb_per_split,
+                        float* __restrict__ out, long ld_out, long split_stride, int* __restrict__ err) {
+  using L = TcPairSmem<BN, STAGES, NS, BK, TF32>;
+  static_assert(!TF32 || NS == 1, "TF32 operands have one part");
+  static_assert((BN / 2) % 8 == 0 && BN <= 256, "B halves of whole 8-row swizzle groups");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * L::kStage);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + L::kBars);
+  __shared__ int s_abort;
+  const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * STAGES, done_bar = full0 + 16 * STAGES;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const uint32_t rank = cluster_ctarank();  // 0: the leader, which issues the MMAs
+  // clusters are consecutive blockIdx.x pairs; N tiles vary fastest, as in the one-tile kernel
+  const int n0 = int(blockIdx.x >> 1) * BN, m0 = int(blockIdx.y) * 2 * kTcBM + int(rank) * kTcBM;
+  const int kb0 = blockIdx.z * kb_per_split;
+  const int nkb = max(0, min(kblocks, kb0 + kb_per_split) - kb0);
+
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int s = 0; s < L::kBars; ++s) mbar_init(smem_u32(bars + s), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)), "r"(BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  cluster_sync_all();  // both CTAs' barriers initialised and TMEM allocated
+
+  if (warp == 0 && lane == 0) {
+    // producer: this CTA's A rows and B half, completing on the leader's full barrier
+    int issued = 0;
+    for (int kb = 0; kb < nkb; ++kb) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (kb / STAGES) & 1;
+      if (kb >= STAGES && !mbar_wait(empty0 + 8 * s, ph ^ 1)) {
+        atomicExch(&s_abort, 1);
+        break;
+      }
+      if (*(volatile int*)&s_abort) break;
+      uint8_t* st = smem + s * L::kStage;
+      const uint32_t fb = mapa_shared(full0 + 8 * s, 0);
+      if (rank == 0) mbar_expect_tx(full0 + 8 * s, 2 * L::kStage);
+      const int kc = (kb0 + kb) * BK;
+#pragma unroll
+      for (int p = 0; p < NS; ++p) {
+        tma_load_2d_pair(smem_u32(st + p * L::kA), &maps.a[p], kc, m0, fb);
+        tma_load_2d_pair(smem_u32(st + NS * L::kA + p * L::kBh), &maps.b[p], kc, n0 + int(rank) * (BN / 2), fb);
+      }
+      issued = kb + 1;
+    }
+    // the leader's last releases of this CTA's stages have landed (bounded)
+    for (int kb = max(0, issued - STAGES); kb < issued; ++kb)
+      if (!mbar_wait(empty0 + 8 * (kb % STAGES), (kb / STAGES) & 1)) {
+        atomicExch(&s_abort, 1);
+        break;
+      }
+  } else if (warp == 1 && lane == 0 && rank == 0) {
+    // MMA issuer (leader only): M = 256 over both CTAs' operands
+    constexpr uint32_t idesc = idesc_pair<TF32>(BN);
+    for (int kb = 0; kb < nkb; ++kb) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (kb / STAGES) & 1;
+      if (!mbar_wait(full0 + 8 * s, ph)) {
+        atomicExch(&s_abort, 1);
+        break;
+      }
+      if (*(volatile int*)&s_abort) break;
+      tc_fence_after();
+      const uint32_t a0 = smem_u32(smem + s * L::kStage);
+      const uint32_t b0 = a0 + NS * L::kA;
+#pragma unroll
+      for (int ks = 0; ks < L::kRB / 32; ++ks) {
+        const uint32_t off = ks * 32;
+        umma_pair<TF32>(tmem, sw_desc<L::kRB>(a0 + off), sw_desc<L::kRB>(b0 + off), idesc, (kb | ks) != 0);
+        if constexpr (NS >= 2) {
+          umma_pair<TF32>(tmem, sw_desc<L::kRB>(a0 + off), sw_desc<L::kRB>(b0 + L::kBh + off), idesc, 1);
+          umma_pair<TF32>(tmem, sw_desc<L::kRB>(a0 + L::kA + off), sw_desc<L::kRB>(b0 + off), idesc, 1);
+        }
+      }
+      umma_commit_pair(empty0 + 8 * s);  // the stage is free in both CTAs
+    }
+    umma_commit_pair(done_bar);  // both CTAs: every MMA issued above has completed
+  }
+  __syncwarp();
+  // epilogue: this CTA's 128 rows from its own TMEM
+  bool ok = true;
+  if (!mbar_wait(done_bar, 0)) {
+    ok = false;
+    atomicExch(&s_abort, 1);
+  }
+  tc_fence_after();
+  __syncthreads();
+  const bool aborted = *(volatile int*)&s_abort != 0;
+  if (aborted && threadIdx.x == 0) atomicExch(err, 1);
+  if (!aborted && ok) {
+    const int row = m0 + warp * 32 + lane;
+    float* o = out + long(blockIdx.z) * split_stride;
+#pragma unroll 1
+    for (int c = 0; c < BN; c += 32) {
+      float v[32];
+      tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c), v);
+      if (nkb == 0) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = 0.f;
+      }
+      if (row < M) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int n = n0 + c + j;
+          if (n < N) o[row + ld_out * long(n)] = v[j];
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  cluster_sync_all();  // neither CTA frees TMEM or leaves while its peer still runs
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+}
+
 // ---- host side ----
 
 // A 2-D BF16 tensor map over a row-major [rows][ld] array (K contiguous, rows of `cols` valid
@@ -577,10 +763,10 @@ void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* b
 // Launch with an explicit tile width bn (128: three pipeline stages; 256: two; two-part BF16 or TF32
 // operands) and split count (0: the heuristic's count for that bn); B's tensor maps must have boxes
 // of bn rows. TF32 operands: bn 128 (six stages) or 256 (four), either kernel. Returns the splits
-// used.
+// used. pair: the CTA-pair kernel (bn 256; BF16 with K blocks of 32, or TF32), six stages.
 int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn, int splits, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int* d_err, const char* prof_name = "tc_gemm",
-                        bool persist = false, int cm = 1);
+                        bool persist = false, int cm = 1, bool pair = false);
 // The variant with K blocks of 32 (64-byte swizzle) and four pipeline stages, bn = 256; A and B
 // maps built with bk = 32.
 
@@ -593,6 +779,7 @@ struct TcTune {
   float ms = 0.f;
   bool persist = false;  // the persistent kernel (one CTA per SM, two accumulators)
   int cm = 1;            // ... in clusters of cm CTAs sharing the B tile (multicast)
+  bool pair = false;     // the CTA-pair kernel (tcgen05 cta_group::2, 256-row tiles)
 };
 
 // The autotuner: times every candidate tile shape (bn 128 with three stages, bn 256 with two; the

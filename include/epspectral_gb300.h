@@ -271,6 +271,11 @@ epsp_status epsp_ladder_set_gemm_persistent(epsp_ladder_plan* plan, int32_t on);
  * those rules). Same results bitwise; epsp_ladder_set_gemm_config resets it to 1. */
 epsp_status epsp_ladder_gemm_cluster(const epsp_ladder_plan* plan, int32_t* cm);
 epsp_status epsp_ladder_set_gemm_cluster(epsp_ladder_plan* plan, int32_t cm);
+/* Whether the contraction runs as the CTA-pair kernel (tcgen05 cta_group::2: two CTAs of a cluster
+ * compute a 256-row tile, each holding its 128 A rows and half of the B tile; bn 256 with bk 32):
+ * read, and set (on = 0 or 1; on turns the persistent kernel off). Same results bitwise. */
+epsp_status epsp_ladder_gemm_pair(const epsp_ladder_plan* plan, int32_t* on);
+epsp_status epsp_ladder_set_gemm_pair(epsp_ladder_plan* plan, int32_t on);
 
 /* One application LJ = L(J) of the ladder kernel at temperature T, chemical potential mu and
  * probe frequency Omega, with sigma_T [nω, ni] complex the self-energy of that temperature:

@@ -239,6 +239,10 @@ def test_every_contraction_tile_shape_matches_the_oracle(api, oracle, cc, unit):
                     plan.set_gemm_config(bn, sp, bk, persistent=True, cluster=cm)
                     assert plan.gemm_config()["persistent"] and plan.gemm_config()["cluster"] == cm
                     assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, cm)
+                # CTA pairs (tcgen05 cta_group::2, 256-row tiles over two CTAs): bitwise the same
+                plan.set_gemm_config(bn, sp, bk, pair=True)
+                assert plan.gemm_config()["pair"]
+                assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, "pair")
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(128, 1, 32)
     with pytest.raises(ArgumentError):
@@ -259,10 +263,16 @@ def test_every_contraction_tile_shape_matches_the_oracle(api, oracle, cc, unit):
                 plan.set_gemm_config(bn, sp, bk, persistent=True, cluster=cm)
                 assert plan.gemm_config()["persistent"] and plan.gemm_config()["cluster"] == cm
                 assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, cm)
+            if bn == 256:
+                plan.set_gemm_config(bn, sp, bk, pair=True)
+                assert plan.gemm_config()["pair"]
+                assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, "pair")
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(256, 1, 64)
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(128, 1, 32, persistent=True, cluster=4)
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(128, 1, 16)
+    with pytest.raises(ArgumentError):
+        plan.set_gemm_config(128, 1, 32, pair=True)
     plan.close()
