@@ -51,9 +51,9 @@ LADDER_PATH = "gemm_tf32"
 # bounded samples and scales them by these counts.
 FP64_SCGD0_ITERS = 12
 FP64_LADDER_APPLIES = 2
-# DRAM bytes (read + write) of one ladder-contraction launch of this workload (the TF32 kernel),
-# from one Nsight Compute capture of the same kernel on a GB300 (profiles/tc_ladder_gemm_c2.md)
-TC_LADDER_TRAFFIC_BYTES = 4.413e9 + 0.350e9
+# DRAM bytes (read + write) of one ladder-contraction launch of this workload (the TF32 CTA-pair
+# kernel), from one Nsight Compute capture of the same kernel on a GB300 (profiles/tc_ladder_gemm_c2.md)
+TC_LADDER_TRAFFIC_BYTES = 4.486e9 + 0.350e9
 # learned warm start: training and held-out runs, epochs
 WARM_TRAIN_RUNS, WARM_HELDOUT_RUNS, WARM_EPOCHS = 256, 32, 40
 

@@ -327,8 +327,12 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
   for (int bn : {256, 128}) {
     const int tiles = ((M + kTcBM - 1) / kTcBM) * ((N + bn - 1) / bn);
     const int h = std::max(1, (ctx->sm_count + tiles - 1) / tiles);
-    for (int sp : {h, 2 * h})
-      if (sp <= max_splits) {
+    // the heuristic count and twice it, within max_splits (so that every shape has candidates)
+    const int cap = std::max(1, max_splits);
+    std::vector<int> counts{std::min(h, cap)};
+    if (std::min(2 * h, cap) != counts[0]) counts.push_back(std::min(2 * h, cap));
+    for (int sp : counts)
+      {
         if (A.tf32) {  // TF32: either tile width, either kernel (the persistent one in clusters too)
           cand.push_back(TcTune{bn, sp, 32, 0.f});
           cand.push_back(TcTune{bn, sp, 32, 0.f, true});
