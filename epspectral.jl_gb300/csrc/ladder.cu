@@ -1833,7 +1833,9 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
   for (int64_t iT = 0; iT < nT; ++iT) {
     const double T = Tlist[iT];
     long pu = prof_begin(ctx, "ladder_io");
-    P->d_ST.upload(reinterpret_cast<const double2*>(sigma) + size_t(nw * ni * iT), size_t(nw * ni), s);
+    // Σ_T from host or device memory (unified addressing: e.g. the scGD0 plan's own Σ)
+    EPSP_CUDA(cudaMemcpyAsync(P->d_ST.p, reinterpret_cast<const double2*>(sigma) + size_t(nw * ni * iT),
+                              size_t(nw * ni) * sizeof(double2), cudaMemcpyDefault, s));
     prof_end(ctx, pu);
     for (int64_t iO = 0; iO < nO; ++iO) {
       const double Om = Omegas[iO];
@@ -2277,7 +2279,7 @@ void ladder_run_batched(LadderPlan* P, const double* sigma, const double* mu, co
   LadderBatch& B = *Bp;
   DBuf<double2> S_all;
   S_all.alloc(ctx, size_t(slab * nT));
-  S_all.upload(reinterpret_cast<const double2*>(sigma), size_t(slab * nT), s);
+  EPSP_CUDA(cudaMemcpyAsync(S_all.p, sigma, size_t(slab * nT) * sizeof(double2), cudaMemcpyDefault, s));
   const double btol = std::pow(std::numeric_limits<double>::epsilon(), 0.75);
   const unsigned eb = div_up(size_t(n), 256);
   auto dot_batch = [&](const float2* U, const float2* V, int nA, double2* out) {

@@ -1111,7 +1111,8 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   if (maxiter < 1) fail(EPSP_EINVAL, "maxiter must be at least 1, got " + std::to_string(maxiter));
   const int64_t nT = occ->nT;
   if (nT < 1) fail(EPSP_EINVAL, "at least one temperature");
-  if (!eta_min || !mu_start || !sigma_out || !mu_out || !converged || !hist || !hist->err || !hist->mu ||
+  // sigma_out may be NULL: Σ then stays on the device (epsp_scgd0_sigma_device)
+  if (!eta_min || !mu_start || !mu_out || !converged || !hist || !hist->err || !hist->mu ||
       !hist->min_spectral_weight || !hist->wall || !hist->iter_frozen)
     fail(EPSP_EINVAL, "an output or input array is NULL");
   for (int64_t iT = 0; iT < nT; ++iT)
@@ -1382,7 +1383,8 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
   }
   hist->niter = niter;
   long pd = prof_begin(ctx, "scgd0_io");
-  S.download(reinterpret_cast<double2*>(sigma_out), size_t(slab * nT), s);
+  if (sigma_out) S.download(reinterpret_cast<double2*>(sigma_out), size_t(slab * nT), s);
+  P->sigma_nT = nT;
   prof_end(ctx, pd);
   EPSP_CUDA(cudaStreamSynchronize(s));
   for (int64_t iT = 0; iT < nT; ++iT) {
@@ -1459,6 +1461,15 @@ epsp_status epsp_scgd0_run_warm(epsp_scgd0_plan* plan, epsp_warmstart* net, cons
       *fallback = 1;
     }
   });
+}
+
+epsp_status epsp_scgd0_sigma_device(const epsp_scgd0_plan* plan, const double** sigma_dev, int64_t* nT) {
+  if (!plan || !sigma_dev) return EPSP_EINVAL;
+  auto* P = reinterpret_cast<const Scgd0Plan*>(plan);
+  if (P->sigma_nT < 1) return EPSP_EINVAL;  // no run yet
+  *sigma_dev = reinterpret_cast<const double*>(P->w_S.p);
+  if (nT) *nT = P->sigma_nT;
+  return EPSP_OK;
 }
 
 epsp_status epsp_scgd0_imsigma(epsp_scgd0_plan* plan, const double* sigma_in, double mu, double T, double* imsigma) {

@@ -50,6 +50,7 @@ struct Scgd0Plan {
   DBuf<double> d_ImS, d_ReS, d_A, d_colsum, d_D;
   // work buffers of scgd0_run, kept across runs (grown when a run needs more temperatures)
   DBuf<double2> w_S, w_Snew, w_Sin;
+  int64_t sigma_nT = 0;  // temperatures of the last run's Σ in w_S (0: no run yet)
   DBuf<double> w_A, w_colsum, w_D, w_pack;
   // μ solve tables (E, first-round terms) and the FP32 spectral path's per-node Σ terms and partials
   DBuf<double> w_E, w_R1;

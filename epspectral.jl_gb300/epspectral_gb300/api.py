@@ -20,7 +20,7 @@ from . import abi
 from .abi import (ModelArrays, OccArrays, c_double_p, c_int32_p, epsp_ladder_history, epsp_model, epsp_occ,
                   epsp_options, epsp_scgd0_history, ptr)
 from .grids import ArgumentError
-from .results import LadderOutputs, Scgd0Outputs, as_complex_F, cptr
+from .results import DeviceSigma, LadderOutputs, Scgd0Outputs, as_complex_F, cptr
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libepspectral_gb300.so")
@@ -79,6 +79,7 @@ def lib():
         "epsp_ladder_gemm_cluster": (C.c_int, [vp, P(i32)]),
         "epsp_ladder_set_gemm_cluster": (C.c_int, [vp, i32]),
         "epsp_ladder_gemm_pair": (C.c_int, [vp, P(i32)]),
+        "epsp_scgd0_sigma_device": (C.c_int, [vp, P(C.c_void_p), P(C.c_int64)]),
         "epsp_ladder_set_gemm_pair": (C.c_int, [vp, i32]),
         "epsp_ladder_run_batched": (C.c_int, [vp, c_double_p, c_double_p, c_double_p, i64, c_double_p, i64, d, i32, i32,
                                               c_double_p, c_double_p, u8p, c_int32_p, P(epsp_ladder_history),
@@ -194,12 +195,13 @@ class Scgd0Plan:
                                               C.byref(self.handle)))
 
     def run(self, occ, *, eta_init, tol, maxiter=20, eta_min=None, fix_mu=False, mu_start=None, sigma_init=None,
-            warm=None, coupling_scale=1.0):
+            warm=None, coupling_scale=1.0, sigma_to_host=True):
         """The iteration of _loop_scgd0 (src/scgd0.jl:246-346).
 
         With `warm` (a trained warmstart.WarmStart, no Σ_init) the run starts from the network's
         Σ_init after the G0D0 iteration, with the plain start as fallback (epsp_scgd0_run_warm);
-        the result then also holds `iters_total` and `fallback`."""
+        the result then also holds `iters_total` and `fallback`. With sigma_to_host=False Σ stays on
+        the device: the result's "sigma" is a DeviceSigma, which LadderPlan.run takes as is."""
         M, O = self.M, OccArrays(occ)
         nT = len(O.Tlist)
         if eta_min is not None and np.ndim(eta_min) > 0 and len(eta_min) != nT:
@@ -212,7 +214,7 @@ class Scgd0Plan:
         if sigma_init is not None and np.shape(sigma_init) != (M.nw, M.ni, nT):
             raise ArgumentError(f"Σ_init must have size (nω, n_i, nT) = {(M.nw, M.ni, nT)}, got {np.shape(sigma_init)}")
         sinit = None if sigma_init is None else as_complex_F(sigma_init, (M.nw, M.ni, nT))
-        out = Scgd0Outputs(M.nw, M.ni, nT, maxiter)
+        out = Scgd0Outputs(M.nw, M.ni, nT, maxiter, sigma_to_host)
         if warm is not None:
             if sinit is not None:
                 raise ArgumentError("Σ_init and a warm start are exclusive")
@@ -223,14 +225,22 @@ class Scgd0Plan:
                                                      int(bool(fix_mu)), ptr(mu0), out.sigma_ptr(), ptr(out.mu),
                                                      out.converged.ctypes.data_as(C.POINTER(C.c_uint8)),
                                                      C.byref(out.hist), C.byref(it), C.byref(fb)))
-            r = out.result()
+            r = self._result(out)
             r["iters_total"], r["fallback"] = int(it.value), bool(fb.value)
             return r
         self.ctx.check(lib().epsp_scgd0_run(self.handle, C.byref(O.struct), ptr(eta_min), float(eta_init),
                                             int(maxiter), float(tol), int(bool(fix_mu)), ptr(mu0), cptr(sinit),
                                             out.sigma_ptr(), ptr(out.mu),
                                             out.converged.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(out.hist)))
-        return out.result()
+        return self._result(out)
+
+    def _result(self, out):
+        r = out.result()
+        if out.sigma is None:
+            p, n = C.c_void_p(), C.c_int64()
+            self.ctx.check(lib().epsp_scgd0_sigma_device(self.handle, C.byref(p), C.byref(n)))
+            r["sigma"] = DeviceSigma(self, p.value, (self.M.nw, self.M.ni, int(n.value)))
+        return r
 
     def imsigma(self, sigma_in, mu, T, imsigma0=None):
         """add_fan_migdal_imsigma! at one temperature (src/scgd0_kernel.jl:59-72)."""
@@ -325,17 +335,23 @@ class LadderPlan:
             raise ArgumentError("Ωs must hold at least one probe frequency")
         nT = len(Tlist)
         mu = np.ascontiguousarray(np.broadcast_to(mu, (nT,)), dtype=np.float64)
-        sig = as_complex_F(sigma, (M.nw, M.ni, nT))
+        if isinstance(sigma, DeviceSigma):  # Σ left on the device by a scGD0 plan
+            if sigma.shape != (M.nw, M.ni, nT):
+                raise ValueError(f"expected shape {(M.nw, M.ni, nT)}, got {sigma.shape}")
+            sig_ptr = sigma.ptr()
+        else:
+            sig = as_complex_F(sigma, (M.nw, M.ni, nT))
+            sig_ptr = cptr(sig)
         out = LadderOutputs(M.nw, M.ni, nT, len(Omegas), maxiter, store_vertex)
         s = {"gmres": abi.EPSP_SOLVER_GMRES, "fixed_point": abi.EPSP_SOLVER_FIXED_POINT}[solver]
         if batch_rhs is not None:
-            self.ctx.check(lib().epsp_ladder_run_batched(self.handle, cptr(sig), ptr(mu), ptr(Tlist), nT, ptr(Omegas),
+            self.ctx.check(lib().epsp_ladder_run_batched(self.handle, sig_ptr, ptr(mu), ptr(Tlist), nT, ptr(Omegas),
                                                          len(Omegas), float(rtol), int(maxiter), int(batch_rhs),
                                                          ptr(out.sigma_bubble), ptr(out.sigma_ladder),
                                                          out.converged.ctypes.data_as(C.POINTER(C.c_uint8)),
                                                          ptr(out.niter, C.c_int32), C.byref(out.hist), out.J_ptr()))
             return out.result()
-        self.ctx.check(lib().epsp_ladder_run(self.handle, cptr(sig), ptr(mu), ptr(Tlist), nT, ptr(Omegas),
+        self.ctx.check(lib().epsp_ladder_run(self.handle, sig_ptr, ptr(mu), ptr(Tlist), nT, ptr(Omegas),
                                              len(Omegas), s, float(rtol), int(maxiter), ptr(out.sigma_bubble),
                                              ptr(out.sigma_ladder),
                                              out.converged.ctypes.data_as(C.POINTER(C.c_uint8)),

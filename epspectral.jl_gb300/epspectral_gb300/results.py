@@ -14,9 +14,21 @@ import numpy as np
 from .abi import c_double_p, c_int32_p, epsp_ladder_history, epsp_scgd0_history, ptr
 
 
+class DeviceSigma:
+    """The self-energy of a scGD0 plan's last run left on the device (epsp_scgd0_sigma_device):
+    Σ [nω, ni, nT] complex, valid until the plan's next run or close. LadderPlan.run takes it as
+    its sigma without a host round trip."""
+
+    def __init__(self, plan, address: int, shape):
+        self.plan, self.address, self.shape = plan, int(address), tuple(shape)
+
+    def ptr(self):
+        return C.cast(C.c_void_p(self.address), c_double_p)
+
+
 class Scgd0Outputs:
-    def __init__(self, nw: int, ni: int, nT: int, maxiter: int):
-        self.sigma = np.zeros((nw, ni, nT), dtype=np.complex128, order="F")
+    def __init__(self, nw: int, ni: int, nT: int, maxiter: int, sigma_to_host: bool = True):
+        self.sigma = np.zeros((nw, ni, nT), dtype=np.complex128, order="F") if sigma_to_host else None
         self.mu = np.zeros(nT)
         self.converged = np.zeros(nT, dtype=np.uint8)
         self.err = np.full((nT, maxiter), np.nan, order="F")
@@ -28,7 +40,7 @@ class Scgd0Outputs:
                                        ptr(self.iter_frozen, C.c_int32), 0, 0)
 
     def sigma_ptr(self):
-        return self.sigma.ctypes.data_as(c_double_p)
+        return c_double_p() if self.sigma is None else self.sigma.ctypes.data_as(c_double_p)
 
     def result(self) -> dict:
         n = int(self.hist.niter)
@@ -86,4 +98,4 @@ def cptr(a: np.ndarray | None):
     return a.ctypes.data_as(c_double_p)
 
 
-__all__ = ["Scgd0Outputs", "LadderOutputs", "as_complex_F", "cptr", "c_int32_p"]
+__all__ = ["DeviceSigma", "Scgd0Outputs", "LadderOutputs", "as_complex_F", "cptr", "c_int32_p"]

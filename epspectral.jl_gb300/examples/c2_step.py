@@ -2,7 +2,8 @@
 tensor-core path (from a trained warm start when --warm names a saved network, e.g. the one
 `bench.py --save-warm` writes), then the ladder σ(Ω) at Ω = 0.1 eV by GMRES (the contraction in
 TF32, or --ladder-path gemm_bf16 for BF16x3) -- repeated --steps times, each part inside an NVTX
-range ("scgd0", "ladder") so that Nsight Compute can select it.
+range ("scgd0", "ladder") so that Nsight Compute can select it. Σ stays on the device between the
+two (the ladder reads the scGD0 plan's copy), as in bench.py's step.
 
     python epspectral.jl_gb300/examples/c2_step.py [--warm net.npz] [--steps N] [--ladder-path P]
 """
@@ -43,7 +44,7 @@ def main():
     for k in range(a.steps):
         push("scgd0")
         ctx.timer_begin()
-        r = sp.run(occ, eta_init=0.01, tol=1e-6, maxiter=50, mu_start=[mu0], warm=ws)
+        r = sp.run(occ, eta_init=0.01, tol=1e-6, maxiter=50, mu_start=[mu0], warm=ws, sigma_to_host=False)
         t_s = ctx.timer_end()
         pop()
         push("ladder")

@@ -193,6 +193,13 @@ epsp_status epsp_scgd0_run(epsp_scgd0_plan* plan, const epsp_occ* occ, const dou
                            const double* mu_start, const double* sigma_init, double* sigma_out,
                            double* mu_out, uint8_t* converged, epsp_scgd0_history* hist);
 
+/* The self-energy of the plan's last run, on the device: Σ [nω, ni, nT] complex FP64, column-major
+ * like sigma_out (nT of that run, may be NULL), valid until the next run or the plan's destruction
+ * (no counterpart in the reference). epsp_scgd0_run takes sigma_out = NULL to leave Σ there only;
+ * epsp_ladder_run and epsp_ladder_run_batched accept this pointer as their sigma. EPSP_EINVAL before
+ * the first run. */
+epsp_status epsp_scgd0_sigma_device(const epsp_scgd0_plan* plan, const double** sigma_dev, int64_t* nT);
+
 /* One Fan-Migdal sum at one temperature: imsigma [nω, ni] += Σ_{νf} term, with sigma_in [nω, ni]
  * complex the clamped input self-energy. add_fan_migdal_imsigma! (src/scgd0_kernel.jl:59-72). */
 epsp_status epsp_scgd0_imsigma(epsp_scgd0_plan* plan, const double* sigma_in, double mu, double T,
@@ -226,7 +233,8 @@ epsp_status epsp_ladder_setup(epsp_ctx* ctx, const epsp_model* model, const epsp
                               epsp_ladder_plan** plan);
 void epsp_ladder_plan_destroy(epsp_ladder_plan* plan);
 
-/* The (T, Ω) loops of _loop_ladder (src/ladder.jl:327-375). sigma [nω, ni, nT] complex, mu [nT],
+/* The (T, Ω) loops of _loop_ladder (src/ladder.jl:327-375). sigma [nω, ni, nT] complex in host or
+ * device memory (unified addressing; e.g. epsp_scgd0_sigma_device's pointer), mu [nT],
  * Tlist [nT], Omegas [nΩ]. Outputs (unsymmetrized, without spin_degeneracy / volume):
  * sigma_bubble, sigma_ladder [3, 3, nΩ, nT]; converged [nΩ, nT]; niter [nΩ, nT]; hist (may be
  * NULL); J_out [nω, 4, 3, 2, ni, nΩ, nT] complex or NULL (store_vertex = false). */

@@ -276,3 +276,32 @@ def test_every_contraction_tile_shape_matches_the_oracle(api, oracle, cc, unit):
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(128, 1, 32, pair=True)
     plan.close()
+
+
+def test_scgd0_sigma_stays_on_the_device_for_the_ladder(api, cc):
+    # epsp_scgd0_run with sigma_out = NULL keeps Σ in the plan (epsp_scgd0_sigma_device); the ladder
+    # reads it there (cudaMemcpyDefault): the same σ, bitwise, as from the downloaded Σ
+    import ctypes as C
+    c = cc
+    s = c["setup"]
+    # the fixture's own scGD0 settings (test_oracle_ladder.cubic_case): two iterations from η = 0.05
+    occ = dict(Tlist=list(c["Tlist"]), nlist=[0.0, 0.0], nelec=1.0, spin_degeneracy=2.0)
+    sp = api.Scgd0Plan(s, path="gemm_bf16", omega_acoustic=W_AC)
+    p, n = C.c_void_p(), C.c_int64()
+    assert api.lib().epsp_scgd0_sigma_device(sp.handle, C.byref(p), C.byref(n)) == 1  # EINVAL before a run
+    kw = dict(eta_init=0.05, eta_min=[0.0, 0.03], tol=0.0, maxiter=2, mu_start=[-0.5, -0.5])
+    host = sp.run(occ, **kw)
+    dev = sp.run(occ, sigma_to_host=False, **kw)
+    assert isinstance(dev["sigma"], api.DeviceSigma) and dev["sigma"].shape == host["sigma"].shape
+    assert np.array_equal(dev["mu"], host["mu"]) and dev["niter"] == host["niter"]
+    lp = api.LadderPlan(s, path="gemm_tf32", omega_acoustic=W_AC)
+    a = lp.run(host["sigma"], host["mu"], c["Tlist"], [0.0, 0.1])
+    b = lp.run(dev["sigma"], dev["mu"], c["Tlist"], [0.0, 0.1])
+    assert np.array_equal(a["sigma_ladder"], b["sigma_ladder"]) and np.array_equal(a["sigma_bubble"], b["sigma_bubble"])
+    bb = lp.run(dev["sigma"], dev["mu"], c["Tlist"], [0.0, 0.1], batch_rhs=4)
+    ab = lp.run(host["sigma"], host["mu"], c["Tlist"], [0.0, 0.1], batch_rhs=4)
+    assert np.array_equal(ab["sigma_ladder"], bb["sigma_ladder"])
+    with pytest.raises(ValueError):
+        lp.run(dev["sigma"], dev["mu"][:1], c["Tlist"][:1], [0.0])
+    lp.close()
+    sp.close()
