@@ -4,9 +4,9 @@ dispersionless modes, g2 stored as BF16 (8.6 GB, drawn in chunks from a seed), a
 tensor-core path: plan set-up with g2 resident in host memory and streamed through the device in
 chunks of --gpu-tile inner states, scGD0 of 8 temperatures (100-800 K) to 1e-6 eV in one batched
 run, the FP64 recast path at one temperature for the error, and the ladder at a few Ωs (seconds per
-Ω). Prints one JSON line.
+Ω; the contraction in TF32, or --ladder-path gemm_bf16). Prints one JSON line.
 
-    python epspectral.jl_gb300/examples/c5_large.py [--gpu-tile 8192] [--omegas 2] [--no-fp64]
+    python epspectral.jl_gb300/examples/c5_large.py [--gpu-tile 8192] [--omegas 2] [--no-fp64] [--ladder-path P]
 """
 import argparse
 import json
@@ -28,6 +28,7 @@ def main():
     ap.add_argument("--gpu-tile", type=int, default=8192)
     ap.add_argument("--omegas", type=int, default=2)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--ladder-path", default="gemm_tf32", choices=("gemm_tf32", "gemm_bf16"))
     a = ap.parse_args()
     out = {}
     t0 = time.perf_counter()
@@ -65,7 +66,8 @@ def main():
         out["abs_dmu_eV_300K"] = float(abs(r["mu"][2] - r64["mu"][0]))
         print(json.dumps({k: out[k] for k in ("fp64_scgd0_300K_s", "max_abs_dsigma_eV_300K")}), flush=True)
     t0 = time.perf_counter()
-    lp = api.LadderPlan(s, path="gemm_bf16", omega_acoustic=1e-4, gpu_tile=a.gpu_tile, ctx=ctx)
+    lp = api.LadderPlan(s, path=a.ladder_path, omega_acoustic=1e-4, gpu_tile=a.gpu_tile, ctx=ctx)
+    out["ladder_path"] = a.ladder_path
     out["ladder_setup_streamed_s"] = time.perf_counter() - t0
     out["ladder_gemm_autotune"] = lp.gemm_config()
     Om = list(np.linspace(0.05, 0.1, a.omegas))
