@@ -45,3 +45,24 @@ def test_context_creation_without_gpu_fails_cleanly(library):
         library.epsp_destroy(h)
     else:
         assert st in (6, 7) and not h.value  # ECUDA or EUNSUPPORTED
+
+
+def test_plan_queries_and_tile_setters_refuse_null_plans(library):
+    """The tuning and hand-off entry points check their pointers before touching a plan (no GPU)."""
+    EINVAL = 1
+    vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+    out_p, out_i, out_n = vp(), i32(), i64()
+    assert library.epsp_scgd0_sigma_device(None, C.byref(out_p), C.byref(out_n)) == EINVAL
+    for get in ("epsp_ladder_gemm_persistent", "epsp_ladder_gemm_cluster", "epsp_ladder_gemm_pair"):
+        assert getattr(library, get)(None, C.byref(out_i)) == EINVAL, get
+    for put in ("epsp_ladder_set_gemm_persistent", "epsp_ladder_set_gemm_cluster", "epsp_ladder_set_gemm_pair"):
+        assert getattr(library, put)(None, i32(1)) == EINVAL, put
+    assert library.epsp_ladder_set_gemm_config(None, i32(256), i32(1), i32(32)) == EINVAL
+
+
+def test_header_declares_the_tensor_core_paths():
+    text = open(HEADER).read()
+    for name, value in (("EPSP_PATH_GEMM_BF16", 2), ("EPSP_PATH_GEMM_TF32", 3)):
+        assert re.search(rf"{name}\s*=\s*{value}\b", text), name
+    from epspectral_gb300 import abi
+    assert abi.PATHS["gemm_tf32"] == 3 and abi.PATHS["gemm_bf16"] == 2
