@@ -331,25 +331,24 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
     const int cap = std::max(1, max_splits);
     std::vector<int> counts{std::min(h, cap)};
     if (std::min(2 * h, cap) != counts[0]) counts.push_back(std::min(2 * h, cap));
-    for (int sp : counts)
-      {
-        if (A.tf32) {  // TF32: either tile width, either kernel (the persistent one in clusters too)
-          cand.push_back(TcTune{bn, sp, 32, 0.f});
-          cand.push_back(TcTune{bn, sp, 32, 0.f, true});
-          cand.push_back(TcTune{bn, sp, 32, 0.f, true, 2});
-          if (bn == 256) {
-            cand.push_back(TcTune{bn, sp, 32, 0.f, true, 4});
-            cand.push_back(TcTune{bn, sp, 32, 0.f, false, 1, true});  // CTA pairs
-          }
-          continue;
-        }
-        cand.push_back(TcTune{bn, sp, kTcBK, 0.f});
-        if (bn == 256 && A32 && B256_32) {
-          cand.push_back(TcTune{bn, sp, 32, 0.f});
-          for (int cm : {1, 2, 4}) cand.push_back(TcTune{bn, sp, 32, 0.f, true, cm});
+    for (int sp : counts) {
+      if (A.tf32) {  // TF32: either tile width, either kernel (the persistent one in clusters too)
+        cand.push_back(TcTune{bn, sp, 32, 0.f});
+        cand.push_back(TcTune{bn, sp, 32, 0.f, true});
+        cand.push_back(TcTune{bn, sp, 32, 0.f, true, 2});
+        if (bn == 256) {
+          cand.push_back(TcTune{bn, sp, 32, 0.f, true, 4});
           cand.push_back(TcTune{bn, sp, 32, 0.f, false, 1, true});  // CTA pairs
         }
+        continue;
       }
+      cand.push_back(TcTune{bn, sp, kTcBK, 0.f});
+      if (bn == 256 && A32 && B256_32) {
+        cand.push_back(TcTune{bn, sp, 32, 0.f});
+        for (int cm : {1, 2, 4}) cand.push_back(TcTune{bn, sp, 32, 0.f, true, cm});
+        cand.push_back(TcTune{bn, sp, 32, 0.f, false, 1, true});  // CTA pairs
+      }
+    }
   }
   cudaEvent_t e0, e1;
   EPSP_CUDA(cudaEventCreate(&e0));

@@ -782,11 +782,14 @@ struct TcTune {
   bool pair = false;     // the CTA-pair kernel (tcgen05 cta_group::2, 256-row tiles)
 };
 
-// The autotuner: times every candidate tile shape (bn 128 with three stages, bn 256 with two; the
-// heuristic split count and twice it, within max_splits) of one two-part product on its own
-// operands -- CUDA events on ctx's stream, one untimed and `reps` timed launches each -- and returns
-// the fastest; every candidate's time goes to *all when given. B128 / B256: B's maps with boxes of
-// 128 / 256 rows.
+// The autotuner: times every candidate tile shape of one two-part BF16 or one-part TF32 product on
+// its own operands -- BF16: bn 128 with three stages, bn 256 with two (K blocks of 64), and with
+// A32 / B256_32 (K blocks of 32) bn 256 one-tile, persistent alone and in clusters of 2 and 4, and
+// CTA pairs; TF32: bn 128 and 256 one-tile, persistent, in clusters, and (bn 256) CTA pairs; each
+// with the heuristic split count and twice it, capped at max_splits -- with CUDA events on ctx's
+// stream (the first launch timed alone, then `reps` timed launches unless it took 20 ms or more),
+// and returns the fastest; every candidate's time goes to *all when given. B128 / B256: B's maps
+// with boxes of 128 / 256 rows. Results are cached per device and shape for the process.
 TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, const TcOperand& B256, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int max_splits, int* d_err, int reps,
                         std::vector<TcTune>* all = nullptr, const TcOperand* A32 = nullptr,
