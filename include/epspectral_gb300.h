@@ -250,7 +250,8 @@ epsp_status epsp_ladder_run(epsp_ladder_plan* plan, const double* sigma, const d
  * run their Arnoldi steps in lockstep, each stopping on its own test (atol = rtol ‖J0‖). Every pair
  * starts from x0 = 0 (the reference warm-starts each Ω from the previous one, src/ladder.jl:340-353):
  * σ agrees with epsp_ladder_run to the solver tolerance, niter and the residual history may differ.
- * GMRES only; GEMM_BF16 plans only (EPSP_EUNSUPPORTED otherwise). Outputs as epsp_ladder_run. */
+ * GMRES only; tensor-core plans only (GEMM_BF16, GEMM_TF32; EPSP_EUNSUPPORTED otherwise). Outputs as
+ * epsp_ladder_run. */
 epsp_status epsp_ladder_run_batched(epsp_ladder_plan* plan, const double* sigma, const double* mu,
                                     const double* Tlist, int64_t nT, const double* Omegas, int64_t nOmega,
                                     double rtol, int32_t maxiter, int32_t max_rhs, double* sigma_bubble,
@@ -258,14 +259,17 @@ epsp_status epsp_ladder_run_batched(epsp_ladder_plan* plan, const double* sigma,
                                     epsp_ladder_history* hist, double* J_out);
 
 /* The tile shape the autotuner picked at setup for the ladder's tensor-core contraction (GEMM_BF16
- * plans; no counterpart in the reference): tile width bn (128 or 256), split count, K block bk (64
- * or 32; may be NULL), and the timed milliseconds per launch of the choice and of the fixed
- * heuristic's shape (0 when not a GEMM_BF16 plan). */
+ * and GEMM_TF32 plans; no counterpart in the reference): tile width bn (128 or 256), split count,
+ * K block bk (64 or 32 on GEMM_BF16, 32 on GEMM_TF32; may be NULL), and the timed milliseconds per
+ * launch of the choice and of the fixed heuristic's shape (0 when not a tensor-core plan). The
+ * kernel choice comes from epsp_ladder_gemm_persistent, _cluster and _pair. */
 epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, int32_t* splits, int32_t* bk,
                                     double* ms_chosen, double* ms_heuristic);
-/* Overrides the autotuner's choice: tile width bn (128 or 256) with K blocks bk = 64 (128-byte
- * swizzle; two or three pipeline stages), or bn 256 with bk = 32 (64-byte swizzle, four stages);
- * splits within what the plan's partial buffer holds. */
+/* Overrides the autotuner's choice: GEMM_BF16: tile width bn (128 or 256) with K blocks bk = 64
+ * (128-byte swizzle; two or three pipeline stages), or bn 256 with bk = 32 (64-byte swizzle, four
+ * stages); GEMM_TF32: bn 128 or 256 with bk = 32 (128-byte swizzle); splits within what the plan's
+ * partial buffer holds. The one-CTA kernel is selected: persistent, cluster and pair settings are
+ * reset (set them after). */
 epsp_status epsp_ladder_set_gemm_config(epsp_ladder_plan* plan, int32_t bn, int32_t splits, int32_t bk);
 /* Whether the contraction runs as the persistent kernel (one CTA per SM over all tiles, two TMEM
  * accumulators so that a tile's epilogue overlaps the next tile's products; GEMM_BF16: bn 256 with
