@@ -1499,7 +1499,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
         P->opG256_32 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 256, 32);
       }
       const TcTune best = tc_gemm_autotune(ctx, P->opA64, P->opG128, P->opG256, int(M), int(N), int(P->Kx), P->d_part.p,
-                                           M, M * N, max_sp, P->d_err.p, 2, &P->tune_all, &P->opA32, &P->opG256_32);
+                                           M, M * N, max_sp, P->d_err.p, 3, &P->tune_all, &P->opA32, &P->opG256_32);
       for (const auto& c : P->tune_all)
         if (c.bn == bn_h && c.splits == sp_h && c.bk == (tf ? 32 : kTcBK) && !c.persist) P->tune_ms_heuristic = c.ms;
       P->bn = best.bn;
@@ -1909,8 +1909,11 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
         std::vector<double2> hcol(size_t(maxiter + 5));
         while (!(solved || tired || breakdown)) {
           ++inner;
+          // a cold start's first Krylov vector is J0 times 1/β: its σ sums are J0's (slot 0) times
+          // the same factor, formed on the host once β is read, instead of another pass
+          const bool v_from_j0 = inner == 1 && !warm;
           op(Vk[size_t(inner - 1)].p, W.p);  // q = A v_k
-          if (!needJ) cond_launch(P, Vk[size_t(inner - 1)].p, Ybuf.p + (2 + (inner - 1)) * ny);
+          if (!needJ && !v_from_j0) cond_launch(P, Vk[size_t(inner - 1)].p, Ybuf.p + (2 + (inner - 1)) * ny);
           long pbl = prof_begin(ctx, "lblas");
           for (int i = 0; i < inner; ++i) {
             dot_dev(P, Vk[size_t(i)].p, W.p, n, part, Hdev.p + i);
@@ -1934,8 +1937,9 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
           }
           if (!needJ) {
             Yv.emplace_back(static_cast<size_t>(ny));
-            EPSP_CUDA(cudaMemcpyAsync(Yv.back().data(), Ybuf.p + (2 + (inner - 1)) * ny, size_t(ny) * sizeof(cplx),
-                                      cudaMemcpyDeviceToHost, s));
+            if (!v_from_j0)
+              EPSP_CUDA(cudaMemcpyAsync(Yv.back().data(), Ybuf.p + (2 + (inner - 1)) * ny, size_t(ny) * sizeof(cplx),
+                                        cudaMemcpyDeviceToHost, s));
           }
           prof_end(ctx, pbl);
           EPSP_CUDA(cudaStreamSynchronize(s));
@@ -1957,6 +1961,11 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
               break;
             }
             z.push_back(beta);
+          }
+          if (v_from_j0 && !needJ) {  // the factor the device scaled J0 by (rsqrt_coef, in R precision)
+            const double c = 1.0 / std::sqrt(hcol[hN0].x);
+            const double cr = tc ? double(float(c)) : c;
+            for (long k = 0; k < ny; ++k) Yv[0][size_t(k)] = Yb[size_t(k)] * cr;
           }
           for (int i = 0; i < inner; ++i) R.push_back(cplx(hcol[size_t(i)].x, hcol[size_t(i)].y));
           const double Hbis = std::sqrt(hcol[size_t(inner)].x);

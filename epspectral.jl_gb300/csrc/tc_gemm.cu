@@ -376,16 +376,18 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
     EPSP_CUDA(cudaEventSynchronize(e1));
     EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     c.ms = ms;
-    if (ms < 20.f && reps > 0) {
-      EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
-      for (int r = 0; r < reps; ++r)
+    // then the best of `reps` launches timed one by one: candidates a few per cent apart are
+    // ranked by their undisturbed time rather than by a mean that one slow launch can tip
+    if (ms < 20.f)
+      for (int r = 0; r < reps; ++r) {
+        EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
         tc_gemm_launch_with(ctx, A_, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune",
                             c.persist, c.cm, c.pair);
-      EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
-      EPSP_CUDA(cudaEventSynchronize(e1));
-      EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      c.ms = ms / float(reps);
-    }
+        EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
+        EPSP_CUDA(cudaEventSynchronize(e1));
+        EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        c.ms = r == 0 ? ms : std::min(c.ms, ms);
+      }
     if (c.ms < best.ms) best = c;
   }
   cudaEventDestroy(e0);

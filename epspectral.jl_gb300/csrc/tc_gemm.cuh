@@ -787,8 +787,8 @@ struct TcTune {
 // A32 / B256_32 (K blocks of 32) bn 256 one-tile, persistent alone and in clusters of 2 and 4, and
 // CTA pairs; TF32: bn 128 and 256 one-tile, persistent, in clusters, and (bn 256) CTA pairs; each
 // with the heuristic split count and twice it, capped at max_splits -- with CUDA events on ctx's
-// stream (the first launch timed alone, then `reps` timed launches unless it took 20 ms or more),
-// and returns the fastest; every candidate's time goes to *all when given. B128 / B256: B's maps
+// stream (a first launch, then unless it took 20 ms or more the best of `reps` launches timed one
+// by one), and returns the fastest; every candidate's time goes to *all when given. B128 / B256: B's maps
 // with boxes of 128 / 256 rows. Results are cached per device and shape for the process.
 TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, const TcOperand& B256, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int max_splits, int* d_err, int reps,
