@@ -191,6 +191,7 @@ class Scgd0Plan:
         self.setup = setup
         self.opts = _options(path, gpu_tile, omega_acoustic, verbosity)
         self.handle = C.c_void_p()
+        self.run_gen = 0  # counts runs: a DeviceSigma is valid for its own run only
         self.ctx.check(lib().epsp_scgd0_setup(self.ctx.handle, C.byref(self.M.struct), C.byref(self.opts),
                                               C.byref(self.handle)))
 
@@ -204,6 +205,7 @@ class Scgd0Plan:
         the device: the result's "sigma" is a DeviceSigma, which LadderPlan.run takes as is."""
         M, O = self.M, OccArrays(occ)
         nT = len(O.Tlist)
+        self.run_gen += 1  # the plan's Σ is about to change
         if eta_min is not None and np.ndim(eta_min) > 0 and len(eta_min) != nT:
             raise ArgumentError(f"eta_min must be a scalar or have one entry per temperature ({nT}), got {len(eta_min)}")
         eta_min = np.ascontiguousarray(np.broadcast_to(0.0 if eta_min is None else eta_min, (nT,)), dtype=np.float64)
@@ -239,7 +241,7 @@ class Scgd0Plan:
         if out.sigma is None:
             p, n = C.c_void_p(), C.c_int64()
             self.ctx.check(lib().epsp_scgd0_sigma_device(self.handle, C.byref(p), C.byref(n)))
-            r["sigma"] = DeviceSigma(self, p.value, (self.M.nw, self.M.ni, int(n.value)))
+            r["sigma"] = DeviceSigma(self, p.value, (self.M.nw, self.M.ni, int(n.value)), self.run_gen)
         return r
 
     def imsigma(self, sigma_in, mu, T, imsigma0=None):

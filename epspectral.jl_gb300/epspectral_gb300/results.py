@@ -17,12 +17,18 @@ from .abi import c_double_p, c_int32_p, epsp_ladder_history, epsp_scgd0_history,
 class DeviceSigma:
     """The self-energy of a scGD0 plan's last run left on the device (epsp_scgd0_sigma_device):
     Σ [nω, ni, nT] complex, valid until the plan's next run or close. LadderPlan.run takes it as
-    its sigma without a host round trip."""
+    its sigma without a host round trip; a stale one (the plan ran again or was closed) raises
+    instead of handing the ladder memory that holds another Σ or none."""
 
-    def __init__(self, plan, address: int, shape):
-        self.plan, self.address, self.shape = plan, int(address), tuple(shape)
+    def __init__(self, plan, address: int, shape, run_gen: int):
+        self.plan, self.address, self.shape, self.run_gen = plan, int(address), tuple(shape), int(run_gen)
+
+    def valid(self) -> bool:
+        return bool(self.plan.handle) and self.plan.run_gen == self.run_gen
 
     def ptr(self):
+        if not self.valid():
+            raise ValueError("this device Σ is stale: its scGD0 plan has run again or was closed")
         return C.cast(C.c_void_p(self.address), c_double_p)
 
 

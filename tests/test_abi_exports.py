@@ -66,3 +66,20 @@ def test_header_declares_the_tensor_core_paths():
         assert re.search(rf"{name}\s*=\s*{value}\b", text), name
     from epspectral_gb300 import abi
     assert abi.PATHS["gemm_tf32"] == 3 and abi.PATHS["gemm_bf16"] == 2
+
+
+def test_device_sigma_refuses_to_outlive_its_run():
+    """A DeviceSigma names its plan's Σ of one run: after another run or a close it raises (no GPU:
+    a stand-in plan object with the two attributes it reads)."""
+    import types
+    from epspectral_gb300.results import DeviceSigma
+    plan = types.SimpleNamespace(handle=C.c_void_p(1234), run_gen=3)
+    d = DeviceSigma(plan, 0xABC0, (4, 2, 1), 3)
+    assert d.valid() and d.ptr()
+    plan.run_gen = 4
+    assert not d.valid()
+    with pytest.raises(ValueError):
+        d.ptr()
+    plan.run_gen, plan.handle = 3, C.c_void_p()
+    with pytest.raises(ValueError):
+        d.ptr()

@@ -303,5 +303,8 @@ def test_scgd0_sigma_stays_on_the_device_for_the_ladder(api, cc):
     assert np.array_equal(ab["sigma_ladder"], bb["sigma_ladder"])
     with pytest.raises(ValueError):
         lp.run(dev["sigma"], dev["mu"][:1], c["Tlist"][:1], [0.0])
+    sp.run(occ, **kw)  # another run replaces the plan's Σ: the old handle is refused on the host
+    with pytest.raises(ValueError):
+        lp.run(dev["sigma"], dev["mu"], c["Tlist"], [0.0])
     lp.close()
     sp.close()
