@@ -10,13 +10,16 @@
 //   the solves at that temperature: it depends on T only), X [16 nω, nshift·3·nip] per chunk and
 //   sign, C± [16 nω, 6 ni] += X B̃, the four channels with the Kramers-Kronig image, then
 //   LJ = -Gm K Gp.
-// GEMM_FP64 / GEMM_BF16X3 (dispersionless modes) regroup the shift sums per mode: a mode of
+// GEMM_FP64 / GEMM_BF16X3 / GEMM_TF32 (dispersionless modes) regroup the shift sums per mode: a mode of
 // frequency ω_ν = (m_ν + r_ν) h contributes (1 - r_ν) S_{m_ν} + r_ν S_{m_ν+1}, the same two shift
 // tables and weights the shift grid gives it, so
 //   U±, V± [row, (a, i)] = Σ_{ν, b, i'} X±_ν[row, (ν, b, i')] (1 or n_ν) G̃[(ν, b, i'), (a, i)],
 //   G̃[(ν, b, i'), (a, i)] = Σ_{f in star(i')} R_f[a, b] w_f g2[ν, i, f]   (T-independent, setup),
 // and the channel combinations are folded into the A operand rows: 6 combinations q per
 // (c0, re/im) instead of the 16 of (c12, type) x sign, and K = nm·3·ni instead of nshift·3·ni.
+// The tensor-core paths keep vertices and Krylov vectors in FP32 and run the contraction on tcgen05
+// with BF16 hi/lo operands (three products) or TF32 operands (one product); the autotuner picks the
+// kernel (one CTA per tile, persistent, multicast clusters, CTA pairs) per plan.
 #include "common.cuh"
 #include "g2stream.cuh"
 #include "gemm_f64.cuh"
