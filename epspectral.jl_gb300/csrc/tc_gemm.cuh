@@ -17,7 +17,7 @@
 //   warps 0-3      : epilogue, tcgen05.ld of TMEM lanes 32w..32w+31 into registers, masked stores.
 // Every mbarrier wait is bounded; on timeout the kernel records the error in *err and winds down
 // (waits, again bounded, for its own copies and MMAs, frees TMEM and returns).
-// Three more kernels below share that pipeline: the persistent one (a CTA per SM over all tiles,
+// Two more kernels below share that pipeline: the persistent one (a CTA per SM over all tiles,
 // two TMEM accumulators, optionally in clusters that multicast the B tile) and the CTA-pair one
 // (tcgen05 cta_group::2: a 256-row tile over two CTAs, each holding half of B).
 #pragma once
