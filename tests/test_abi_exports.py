@@ -83,3 +83,15 @@ def test_device_sigma_refuses_to_outlive_its_run():
     plan.run_gen, plan.handle = 3, C.c_void_p()
     with pytest.raises(ValueError):
         d.ptr()
+
+
+def test_julia_shim_and_integration_name_only_declared_entry_points():
+    """The Julia ccall shim and INTEGRATION.md call nothing the header does not declare."""
+    decl = set(declared())
+    jl = open(os.path.join(PKG, "julia", "EPSpectralGB300.jl")).read()
+    used = set(re.findall(r":(epsp_[a-z0-9_]+)", jl))
+    assert used and not (used - decl), sorted(used - decl)
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    types = set(re.findall(r"\b(epsp_[a-z0-9_]+)\b", re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)))
+    named = set(re.findall(r"\b(epsp_[a-z0-9_]+)\s*\(", text)) | set(re.findall(r"`(epsp_[a-z0-9_]+)`", text))
+    assert not (named - decl - types), sorted(named - decl - types)
