@@ -152,7 +152,10 @@ static void launch_persist(Ctx* ctx, const TcOperand& A, const TcOperand& B, int
   TcMaps maps;
   for (int p = 0; p < 3; ++p) {
     maps.a[p] = A.m[p < NS ? p : 0];
-    maps.b[p] = CM == 1 ? B.m[p < NS ? p : 0] : remap(B, p < NS ? p : 0, BN / CM);  // B slices of BN / CM rows
+    if (p < NS)
+      maps.b[p] = CM == 1 ? B.m[p] : remap(B, p, BN / CM);  // B slices of BN / CM rows
+    else
+      maps.b[p] = maps.b[0];
   }
   const int nN = (N + BN - 1) / BN, nM = (M + kTcBM - 1) / kTcBM;
   const int nitems = nN * ((nM + CM - 1) / CM) * splits;  // (N tile, M tile group, split)
@@ -183,7 +186,7 @@ static void launch_pair(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M,
   TcMaps maps;
   for (int p = 0; p < 3; ++p) {
     maps.a[p] = A.m[p < NS ? p : 0];
-    maps.b[p] = remap(B, p < NS ? p : 0, BN / 2);
+    maps.b[p] = p < NS ? remap(B, p, BN / 2) : maps.b[0];  // B halves of BN / 2 rows, each part encoded once
   }
   cudaLaunchAttribute cl;
   cl.id = cudaLaunchAttributeClusterDimension;
