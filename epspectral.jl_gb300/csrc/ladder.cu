@@ -19,7 +19,7 @@
 // (c0, re/im) instead of the 16 of (c12, type) x sign, and K = nm·3·ni instead of nshift·3·ni.
 // The tensor-core paths keep vertices and Krylov vectors in FP32 and run the contraction on tcgen05
 // with BF16 hi/lo operands (three products) or TF32 operands (one product); the autotuner picks the
-// kernel (one CTA per tile, persistent, multicast clusters, CTA pairs) per plan.
+// kernel (one CTA per tile, persistent, CTA pairs) per plan.
 #include "common.cuh"
 #include "g2stream.cuh"
 #include "gemm_f64.cuh"
@@ -83,7 +83,6 @@ struct LadderPlan {
   TcOperand opA{}, opG{}, opA64{}, opG128{}, opG256{}, opA32{}, opG256_32{};
   int bn = 128, splits = 1, bk = kTcBK;  // the contraction's tile shape, picked by the autotuner at setup
   bool persist = false;                  // ... and whether it runs as the persistent kernel
-  int cm = 1;                            // ... in clusters of cm CTAs sharing the B tile
   bool pair = false;                     // ... or as the CTA-pair kernel (cta_group::2)
   std::vector<TcTune> tune_all;
   float tune_ms_heuristic = 0.f;
@@ -1509,7 +1508,6 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       P->splits = best.splits;
       P->bk = best.bk;
       P->persist = best.persist;
-      P->cm = best.cm;
       P->pair = best.pair;
       pick_contraction_operands(P);
       int terr = 0;
@@ -1709,7 +1707,7 @@ static void apply_L(LadderPlan* P, const float2* J, float2* LJ, const float2* X 
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, px);
   int sp = tc_gemm_launch_with(ctx, P->opA, P->opG, P->bn, P->splits, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N,
-                               P->d_err.p, "tc_ladder", P->persist, P->cm, P->pair);
+                               P->d_err.p, "tc_ladder", P->persist, P->pair);
   // D stays as the contraction's split-K partials; y_split and finish add them as they read
   long pl = prof_begin(ctx, "lsum");
   y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), 1), 256, 0, s>>>(P->d_part.p, M, sp, M * N, int(nw), int(nwp),
@@ -2214,7 +2212,7 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const float2* X, int nA
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, px);
   int sp = tc_gemm_launch_with(ctx, B.opA, P->opG, P->bn, 0, int(Mt), int(N), int(P->Kx), B.part.p, Mt, Mt * N, P->d_err.p,
-                               "tc_ladder", P->persist, P->cm, P->pair);
+                               "tc_ladder", P->persist, P->pair);
   y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), unsigned(nA)), 256, 0, s>>>(
       B.part.p, Mt, sp, Mt * N, int(nw), int(nwp), N, P->Kp2, B.Yh.p, B.Yl.p);
   EPSP_LAUNCHED(ctx);
@@ -2594,7 +2592,6 @@ epsp_status epsp_ladder_set_gemm_config(epsp_ladder_plan* plan, int32_t bn, int3
     P->bk = bk;
     pick_contraction_operands(P);
     if (!tf && !(bn == 256 && bk == 32)) P->persist = false;
-    P->cm = 1;
     P->pair = false;
   });
 }
@@ -2613,27 +2610,7 @@ epsp_status epsp_ladder_set_gemm_persistent(epsp_ladder_plan* plan, int32_t on) 
     if (on && P->path == EPSP_PATH_GEMM_BF16 && !(P->bn == 256 && P->bk == 32))
       fail(EPSP_EINVAL, "the persistent BF16x3 kernel takes bn 256 with bk 32");
     P->persist = on != 0;
-    if (!P->persist) P->cm = 1;
     if (P->persist) P->pair = false;
-  });
-}
-
-epsp_status epsp_ladder_gemm_cluster(const epsp_ladder_plan* plan, int32_t* cm) {
-  if (!plan || !cm) return EPSP_EINVAL;
-  *cm = reinterpret_cast<const LadderPlan*>(plan)->cm;
-  return EPSP_OK;
-}
-
-epsp_status epsp_ladder_set_gemm_cluster(epsp_ladder_plan* plan, int32_t cm) {
-  if (!plan) return EPSP_EINVAL;
-  auto* P = reinterpret_cast<LadderPlan*>(plan);
-  return lguard(P->ctx, [&] {
-    if (!tc_path(P->path)) fail(EPSP_EUNSUPPORTED, "tile shapes apply to tensor-core plans (GEMM_BF16, GEMM_TF32)");
-    if (cm != 1 && cm != 2 && cm != 4) fail(EPSP_EINVAL, "clusters of 1, 2 or 4 CTAs");
-    if (cm > 1 && !P->persist) fail(EPSP_EINVAL, "clusters are for the persistent kernel");
-    if (cm > 2 && P->bn == 128) fail(EPSP_EINVAL, "tile width 128 takes clusters of at most 2");
-    if (cm > 1 && P->path == EPSP_PATH_GEMM_BF16 && P->bn != 256) fail(EPSP_EINVAL, "BF16x3 clusters take bn 256");
-    P->cm = cm;
   });
 }
 
@@ -2651,10 +2628,7 @@ epsp_status epsp_ladder_set_gemm_pair(epsp_ladder_plan* plan, int32_t on) {
     if (on && (P->bn != 256 || P->bk != 32))
       fail(EPSP_EINVAL, "the CTA-pair kernel takes bn 256 with bk 32");
     P->pair = on != 0;
-    if (P->pair) {
-      P->persist = false;
-      P->cm = 1;
-    }
+    if (P->pair) P->persist = false;
   });
 }
 
@@ -2667,8 +2641,7 @@ epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, i
   if (bk) *bk = P->bk;
   double best = 0;
   for (const auto& c : P->tune_all)
-    if (c.bn == P->bn && c.splits == P->splits && c.bk == P->bk && c.persist == P->persist && c.cm == P->cm &&
-        c.pair == P->pair)
+    if (c.bn == P->bn && c.splits == P->splits && c.bk == P->bk && c.persist == P->persist && c.pair == P->pair)
       best = c.ms;
   if (ms_chosen) *ms_chosen = best;
   if (ms_heuristic) *ms_heuristic = P->tune_ms_heuristic;

@@ -120,53 +120,28 @@ static CUtensorMap remap(const TcOperand& op, int p, int box_rows) {
                  : make_tmap_bf16(op.base[p], op.rows, op.cols, op.ld, box_rows, op.bk);
 }
 
-template <int BN, int STAGES, int NS, int BK, bool TF32 = false, int CM = 1>
+template <int BN, int STAGES, int NS, int BK, bool TF32 = false>
 static void launch_persist(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int kblocks, int per,
                            int splits, float* out, long ld_out, long split_stride, int* d_err) {
   using L = TcPSmem<BN, STAGES, NS, BK, TF32>;
   if (A.bk != BK || B.bk != BK) fail(EPSP_EINVAL, "operand tensor maps were built for another K block");
   if (A.tf32 != TF32 || B.tf32 != TF32) fail(EPSP_EINVAL, "operand tensor maps were built for another element type");
-  auto* kern = tc_gemm_persist_kernel<BN, STAGES, NS, BK, TF32, CM>;
-  cudaLaunchAttribute cl;
-  cl.id = cudaLaunchAttributeClusterDimension;
-  cl.val.clusterDim.x = CM;
-  cl.val.clusterDim.y = 1;
-  cl.val.clusterDim.z = 1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.blockDim = dim3(192);
-  cfg.dynamicSmemBytes = L::kBytes;
-  cfg.stream = ctx->stream;
-  cfg.attrs = &cl;
-  cfg.numAttrs = 1;
+  auto* kern = tc_gemm_persist_kernel<BN, STAGES, NS, BK, TF32>;
   static bool configured = false;  // one process, one attribute setting per instantiation
-  static int max_clusters = 0;     // clusters of CM CTAs resident at once
   if (!configured) {
     EPSP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::kBytes));
-    if (CM > 1) {
-      cfg.gridDim = dim3(unsigned(CM * std::max(1, ctx->sm_count / CM)));
-      EPSP_CUDA(cudaOccupancyMaxActiveClusters(&max_clusters, kern, &cfg));
-      if (max_clusters < 1) fail(EPSP_EUNSUPPORTED, "no cluster of " + std::to_string(CM) + " GEMM CTAs fits on the device");
-    }
     configured = true;
   }
   TcMaps maps;
   for (int p = 0; p < 3; ++p) {
     maps.a[p] = A.m[p < NS ? p : 0];
-    if (p < NS)
-      maps.b[p] = CM == 1 ? B.m[p] : remap(B, p, BN / CM);  // B slices of BN / CM rows
-    else
-      maps.b[p] = maps.b[0];
+    maps.b[p] = B.m[p < NS ? p : 0];
   }
   const int nN = (N + BN - 1) / BN, nM = (M + kTcBM - 1) / kTcBM;
-  const int nitems = nN * ((nM + CM - 1) / CM) * splits;  // (N tile, M tile group, split)
-  if (CM == 1) {
-    const int grid = std::min(nitems, ctx->sm_count);
-    kern<<<grid, 192, L::kBytes, ctx->stream>>>(maps, M, N, kblocks, per, nN, nM, nitems, out, ld_out, split_stride,
-                                                d_err);
-  } else {
-    cfg.gridDim = dim3(unsigned(CM * std::min(nitems, max_clusters)));
-    EPSP_CUDA(cudaLaunchKernelEx(&cfg, kern, maps, M, N, kblocks, per, nN, nM, nitems, out, ld_out, split_stride, d_err));
-  }
+  const int nitems = nN * nM * splits;  // (N tile, M tile, split)
+  const int grid = std::min(nitems, ctx->sm_count);
+  kern<<<grid, 192, L::kBytes, ctx->stream>>>(maps, M, N, kblocks, per, nN, nM, nitems, out, ld_out, split_stride,
+                                              d_err);
   EPSP_LAUNCHED(ctx);
 }
 
@@ -240,13 +215,9 @@ int tc_splits_for(Ctx* ctx, int M, int N, int K, int bn) {
 
 int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn, int splits, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int* d_err, const char* prof_name, bool persist,
-                        int cm, bool pair) {
+                        bool pair) {
   if (bn != 128 && bn != 256) fail(EPSP_EINVAL, "tile width must be 128 or 256");
-  if (pair && (persist || cm != 1 || bn != 256))
-    fail(EPSP_EINVAL, "the CTA-pair kernel is one-tile, tile width 256, without clusters of its own");
-  if (cm != 1 && cm != 2 && cm != 4) fail(EPSP_EINVAL, "clusters of 1, 2 or 4 CTAs");
-  if (cm > 1 && !persist) fail(EPSP_EINVAL, "clusters are for the persistent kernel");
-  if (cm > 1 && (bn == 128 ? cm > 2 : false)) fail(EPSP_EINVAL, "tile width 128 takes clusters of at most 2");
+  if (pair && (persist || bn != 256)) fail(EPSP_EINVAL, "the CTA-pair kernel is one-tile, tile width 256");
   if (A.tf32 || B.tf32) {
     if (!(A.tf32 && B.tf32 && A.ns == 1 && B.ns == 1 && A.bk == 32 && B.bk == 32))
       fail(EPSP_EINVAL, "TF32 operands are one-part maps with K boxes of 32 on both sides");
@@ -258,14 +229,8 @@ int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn
     long pi = prof_begin(ctx, prof_name);
     if (pair)
       launch_pair<256, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
-    else if (persist && bn == 256 && cm == 4)
-      launch_persist<256, 4, 1, 32, true, 4>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
-    else if (persist && bn == 256 && cm == 2)
-      launch_persist<256, 4, 1, 32, true, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
     else if (persist && bn == 256)
       launch_persist<256, 4, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
-    else if (persist && cm == 2)
-      launch_persist<128, 6, 1, 32, true, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
     else if (persist)
       launch_persist<128, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
     else if (bn == 256)
@@ -288,10 +253,6 @@ int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn
   long pi = prof_begin(ctx, prof_name);
   if (pair)
     launch_pair<256, 6, 2, 32, false>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
-  else if (persist && cm == 4)
-    launch_persist<256, 4, 2, 32, false, 4>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
-  else if (persist && cm == 2)
-    launch_persist<256, 4, 2, 32, false, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   else if (persist)
     launch_persist<256, 4, 2, 32>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
   else if (bk == 32)
@@ -335,21 +296,17 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
     std::vector<int> counts{std::min(h, cap)};
     if (std::min(2 * h, cap) != counts[0]) counts.push_back(std::min(2 * h, cap));
     for (int sp : counts) {
-      if (A.tf32) {  // TF32: either tile width, either kernel (the persistent one in clusters too)
+      if (A.tf32) {  // TF32: either tile width, either kernel
         cand.push_back(TcTune{bn, sp, 32, 0.f});
         cand.push_back(TcTune{bn, sp, 32, 0.f, true});
-        cand.push_back(TcTune{bn, sp, 32, 0.f, true, 2});
-        if (bn == 256) {
-          cand.push_back(TcTune{bn, sp, 32, 0.f, true, 4});
-          cand.push_back(TcTune{bn, sp, 32, 0.f, false, 1, true});  // CTA pairs
-        }
+        if (bn == 256) cand.push_back(TcTune{bn, sp, 32, 0.f, false, true});  // CTA pairs
         continue;
       }
       cand.push_back(TcTune{bn, sp, kTcBK, 0.f});
       if (bn == 256 && A32 && B256_32) {
         cand.push_back(TcTune{bn, sp, 32, 0.f});
-        for (int cm : {1, 2, 4}) cand.push_back(TcTune{bn, sp, 32, 0.f, true, cm});
-        cand.push_back(TcTune{bn, sp, 32, 0.f, false, 1, true});  // CTA pairs
+        cand.push_back(TcTune{bn, sp, 32, 0.f, true});
+        cand.push_back(TcTune{bn, sp, 32, 0.f, false, true});  // CTA pairs
       }
     }
   }
@@ -366,7 +323,7 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
   // one untimed launch first, so that no candidate pays the first launch's costs
   if (!cand.empty())
     tc_gemm_launch_with(ctx, opA(cand[0]), opB(cand[0]), cand[0].bn, cand[0].splits, M, N, K, out, ld_out, split_stride,
-                        d_err, "autotune", cand[0].persist, cand[0].cm, cand[0].pair);
+                        d_err, "autotune", cand[0].persist, cand[0].pair);
   for (auto& c : cand) {
     const TcOperand& A_ = opA(c);
     const TcOperand& B = opB(c);
@@ -374,7 +331,7 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
     float ms = 0.f;
     EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
     tc_gemm_launch_with(ctx, A_, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune", c.persist,
-                        c.cm, c.pair);
+                        c.pair);
     EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
     EPSP_CUDA(cudaEventSynchronize(e1));
     EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
@@ -385,7 +342,7 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
       for (int r = 0; r < reps; ++r) {
         EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
         tc_gemm_launch_with(ctx, A_, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune",
-                            c.persist, c.cm, c.pair);
+                            c.persist, c.pair);
         EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
         EPSP_CUDA(cudaEventSynchronize(e1));
         EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));

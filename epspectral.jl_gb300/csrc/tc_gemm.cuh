@@ -18,8 +18,9 @@
 // Every mbarrier wait is bounded; on timeout the kernel records the error in *err and winds down
 // (waits, again bounded, for its own copies and MMAs, frees TMEM and returns).
 // Two more kernels below share that pipeline: the persistent one (a CTA per SM over all tiles,
-// two TMEM accumulators, optionally in clusters that multicast the B tile) and the CTA-pair one
-// (tcgen05 cta_group::2: a 256-row tile over two CTAs, each holding half of B).
+// two TMEM accumulators) and the CTA-pair one (tcgen05 cta_group::2: a 256-row tile over two CTAs,
+// each holding half of B). Every TMA load reads this GPU's own memory into the issuing CTA's
+// shared memory (no multicast).
 #pragma once
 
 #include "common.cuh"
@@ -65,16 +66,6 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
       "l"(map), "r"(c0), "r"(c1), "r"(bar)
-      : "memory");
-}
-// The same box written to the same shared-memory offset of every CTA of the cluster in `mask`,
-// each completing bytes on its own mbarrier at offset `bar`.
-__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar,
-                                               uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, {%2, "
-      "%3}], [%4], %5;" ::"r"(dst),
-      "l"(map), "r"(c0), "r"(c1), "r"(bar), "h"(mask)
       : "memory");
 }
 __device__ __forceinline__ uint32_t cluster_ctarank() {
@@ -137,13 +128,6 @@ __device__ __forceinline__ float round_tf32(float x) {
 }
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-// The same, arriving on the mbarrier at offset `bar` of every CTA of the cluster in `mask`.
-__device__ __forceinline__ void umma_commit_mc(uint32_t bar, uint16_t mask) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-                   bar),
-               "h"(mask)
-               : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -319,13 +303,6 @@ __global__ void __launch_bounds__(128, 1)
 //   warps 2-5      : epilogue of item t (TMEM lane quarter = warp % 4) while the MMAs of item t + 1
 //                    run into the other accumulator; they release an accumulator by one arrive each.
 // Per tile the MMAs run in the one-tile kernel's order, so the results are bitwise the same.
-// With CM > 1 the grid is made of clusters of CM CTAs on CM consecutive M tiles of one N tile (an
-// item is then such a group, the cluster's index in place of blockIdx.x): they share the B tile,
-// which each CTA loads 1/CM of (B's maps have boxes of BN / CM rows) and multicasts to the cluster,
-// so B's L2-to-SM traffic falls by CM. A stage is refilled only when every CTA of the cluster has
-// consumed it: each MMA commit arrives on the empty barrier of every CTA (count CM). Before the
-// first multicast the cluster synchronises (its barriers initialised); before exit each producer
-// waits for the last arrivals on its own empty barriers, so nothing remains in flight towards it.
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
@@ -341,16 +318,13 @@ struct TcPSmem {
   static constexpr int kBytes = STAGES * kStage + 8 * kBars + 16 + 1024;
 };
 
-template <int BN, int STAGES, int NS, int BK, bool TF32 = false, int CM = 1>
+template <int BN, int STAGES, int NS, int BK, bool TF32 = false>
 __global__ void __launch_bounds__(192, 1)
     tc_gemm_persist_kernel(const __grid_constant__ TcMaps maps, int M, int N, int kblocks, int kb_per_split, int nN,
                            int nM, int nitems, float* __restrict__ out, long ld_out, long split_stride,
                            int* __restrict__ err) {
   using L = TcPSmem<BN, STAGES, NS, BK, TF32>;
   static_assert(!TF32 || NS == 1, "TF32 operands have one part");
-  static_assert(CM == 1 || CM == 2 || CM == 4, "clusters of 1, 2 or 4 CTAs");
-  static_assert((BN / CM) % 8 == 0, "B slices of whole 8-row swizzle groups");
-  constexpr uint16_t kMask = uint16_t((1u << CM) - 1);
   static_assert(2 * BN <= 512, "two accumulators must fit TMEM");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -360,13 +334,11 @@ __global__ void __launch_bounds__(192, 1)
   const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * STAGES, accf0 = full0 + 16 * STAGES,
                  acce0 = accf0 + 16, done_bar = accf0 + 32;
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int crank = CM > 1 ? int(cluster_ctarank()) : 0;
-  const int first = int(blockIdx.x) / CM, stride = int(gridDim.x) / CM;  // this cluster's items
-  const int nMg = (nM + CM - 1) / CM;                                       // M tile groups
+  const int first = int(blockIdx.x), stride = int(gridDim.x);  // this CTA's items
   auto coords = [&](int item, int& n0, int& m0, int& z, int& kb0, int& nkb) {
     n0 = (item % nN) * BN;
-    m0 = (((item / nN) % nMg) * CM + crank) * kTcBM;
-    z = item / (nN * nMg);
+    m0 = ((item / nN) % nM) * kTcBM;
+    z = item / (nN * nM);
     kb0 = z * kb_per_split;
     nkb = max(0, min(kblocks, kb0 + kb_per_split) - kb0);
   };
@@ -374,8 +346,7 @@ __global__ void __launch_bounds__(192, 1)
 
   if (threadIdx.x == 0) {
     s_abort = 0;
-    for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(bars + s), 1);
-    for (int s = STAGES; s < 2 * STAGES; ++s) mbar_init(smem_u32(bars + s), CM);
+    for (int s = 0; s < 2 * STAGES; ++s) mbar_init(smem_u32(bars + s), 1);
     mbar_init(accf0, 1);
     mbar_init(accf0 + 8, 1);
     mbar_init(acce0, 4);
@@ -392,7 +363,6 @@ __global__ void __launch_bounds__(192, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  if constexpr (CM > 1) cluster_sync_all();  // every CTA's barriers initialised before any multicast
 
   if (warp == 0 && lane == 0) {
     // producer
@@ -420,11 +390,7 @@ __global__ void __launch_bounds__(192, 1)
 #pragma unroll
         for (int p = 0; p < NS; ++p) {
           tma_load_2d(smem_u32(st + p * L::kA), &maps.a[p], kc, m0, fb);
-          if constexpr (CM == 1)
-            tma_load_2d(smem_u32(st + NS * L::kA + p * L::kB), &maps.b[p], kc, n0, fb);
-          else  // this CTA's slice of the shared B tile, to every CTA of the cluster
-            tma_load_2d_mc(smem_u32(st + NS * L::kA + p * L::kB + crank * (L::kB / CM)), &maps.b[p], kc,
-                           n0 + crank * (BN / CM), fb, kMask);
+          tma_load_2d(smem_u32(st + NS * L::kA + p * L::kB), &maps.b[p], kc, n0, fb);
         }
         ++g;
       }
@@ -432,14 +398,6 @@ __global__ void __launch_bounds__(192, 1)
     if (aborted()) {
       // wind down: wait (bounded) for the copies this thread issued into stages not yet consumed
       for (int k = max(0, g - STAGES); k < g; ++k) mbar_wait(full0 + 8 * (k % STAGES), (k / STAGES) & 1);
-    }
-    if constexpr (CM > 1) {
-      // the cluster's last releases of this CTA's stages (remote MMA commits) have landed (bounded)
-      for (int k = max(0, g - STAGES); k < g; ++k)
-        if (!mbar_wait(empty0 + 8 * (k % STAGES), (k / STAGES) & 1)) {
-          atomicExch(&s_abort, 1);
-          break;
-        }
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
@@ -485,10 +443,7 @@ __global__ void __launch_bounds__(192, 1)
             umma<TF32>(acc, sw_desc<L::kRB>(a0 + 2 * L::kA + off), sw_desc<L::kRB>(b0 + off), idesc, 1);
           }
         }
-        if constexpr (CM == 1)
-          umma_commit(empty0 + 8 * s);
-        else
-          umma_commit_mc(empty0 + 8 * s, kMask);  // the stage is free in this CTA for every CTA's producer
+        umma_commit(empty0 + 8 * s);
         ++g;
       }
       umma_commit(accf0 + 8 * b);  // completes when the item's MMAs have
@@ -540,7 +495,6 @@ __global__ void __launch_bounds__(192, 1)
   if (aborted() && threadIdx.x == 0) atomicExch(err, 1);
   tc_fence_before();
   __syncthreads();
-  if constexpr (CM > 1) cluster_sync_all();  // no CTA leaves while a cluster peer still runs
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
 }
 
@@ -748,7 +702,7 @@ struct TcOperand {
   int ns = 2;
   int bk = kTcBK;  // K columns of the maps' box
   bool tf32 = false;
-  // the matrices behind the maps (for maps with other boxes: the B slices of a cluster launch)
+  // the matrices behind the maps (for maps with other boxes: the B halves of a CTA-pair launch)
   const void* base[3] = {nullptr, nullptr, nullptr};
   long rows = 0, cols = 0, ld = 0;
 };
@@ -769,7 +723,7 @@ void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* b
 // used. pair: the CTA-pair kernel (bn 256; BF16 with K blocks of 32, or TF32), six stages.
 int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn, int splits, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int* d_err, const char* prof_name = "tc_gemm",
-                        bool persist = false, int cm = 1, bool pair = false);
+                        bool persist = false, bool pair = false);
 // The variant with K blocks of 32 (64-byte swizzle) and four pipeline stages, bn = 256; A and B
 // maps built with bk = 32.
 
@@ -781,14 +735,13 @@ struct TcTune {
   int bn = 0, splits = 0, bk = kTcBK;
   float ms = 0.f;
   bool persist = false;  // the persistent kernel (one CTA per SM, two accumulators)
-  int cm = 1;            // ... in clusters of cm CTAs sharing the B tile (multicast)
   bool pair = false;     // the CTA-pair kernel (tcgen05 cta_group::2, 256-row tiles)
 };
 
 // The autotuner: times every candidate tile shape of one two-part BF16 or one-part TF32 product on
 // its own operands -- BF16: bn 128 with three stages, bn 256 with two (K blocks of 64), and with
-// A32 / B256_32 (K blocks of 32) bn 256 one-tile, persistent alone and in clusters of 2 and 4, and
-// CTA pairs; TF32: bn 128 and 256 one-tile, persistent, in clusters, and (bn 256) CTA pairs; each
+// A32 / B256_32 (K blocks of 32) bn 256 one-tile, persistent and CTA pairs; TF32: bn 128 and 256
+// one-tile and persistent, and (bn 256) CTA pairs; each
 // with the heuristic split count and twice it, capped at max_splits -- with CUDA events on ctx's
 // stream (a first launch, then unless it took 20 ms or more the best of `reps` launches timed one
 // by one), and returns the fastest; every candidate's time goes to *all when given. B128 / B256: B's maps

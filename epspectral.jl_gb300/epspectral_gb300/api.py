@@ -76,8 +76,6 @@ def lib():
         "epsp_ladder_set_gemm_config": (C.c_int, [vp, i32, i32, i32]),
         "epsp_ladder_gemm_persistent": (C.c_int, [vp, P(i32)]),
         "epsp_ladder_set_gemm_persistent": (C.c_int, [vp, i32]),
-        "epsp_ladder_gemm_cluster": (C.c_int, [vp, P(i32)]),
-        "epsp_ladder_set_gemm_cluster": (C.c_int, [vp, i32]),
         "epsp_ladder_gemm_pair": (C.c_int, [vp, P(i32)]),
         "epsp_scgd0_sigma_device": (C.c_int, [vp, P(C.c_void_p), P(C.c_int64)]),
         "epsp_ladder_set_gemm_pair": (C.c_int, [vp, i32]),
@@ -299,22 +297,18 @@ class LadderPlan:
         bn, sp, bk, ms, mh = C.c_int32(), C.c_int32(), C.c_int32(), C.c_double(), C.c_double()
         self.ctx.check(lib().epsp_ladder_gemm_config(self.handle, C.byref(bn), C.byref(sp), C.byref(bk), C.byref(ms),
                                                      C.byref(mh)))
-        on, cm, pr = C.c_int32(), C.c_int32(), C.c_int32()
+        on, pr = C.c_int32(), C.c_int32()
         self.ctx.check(lib().epsp_ladder_gemm_persistent(self.handle, C.byref(on)))
-        self.ctx.check(lib().epsp_ladder_gemm_cluster(self.handle, C.byref(cm)))
         self.ctx.check(lib().epsp_ladder_gemm_pair(self.handle, C.byref(pr)))
-        return dict(bn=bn.value, splits=sp.value, bk=bk.value, persistent=bool(on.value), cluster=cm.value,
-                    pair=bool(pr.value), ms=ms.value, ms_heuristic=mh.value)
+        return dict(bn=bn.value, splits=sp.value, bk=bk.value, persistent=bool(on.value), pair=bool(pr.value),
+                    ms=ms.value, ms_heuristic=mh.value)
 
-    def set_gemm_config(self, bn: int, splits: int, bk: int = 64, persistent: bool = False, cluster: int = 1,
-                        pair: bool = False):
+    def set_gemm_config(self, bn: int, splits: int, bk: int = 64, persistent: bool = False, pair: bool = False):
         """Overrides the autotuner's tile shape of the contraction (GEMM_BF16 / GEMM_TF32 plans);
         persistent: one CTA per SM over all tiles (BF16: bn 256, bk 32 only; TF32: bk 32, either bn);
-        cluster: the persistent kernel in clusters of 2 or 4 CTAs sharing the B tile (multicast);
         pair: CTA pairs computing 256-row tiles (tcgen05 cta_group::2; bn 256, bk 32)."""
         self.ctx.check(lib().epsp_ladder_set_gemm_config(self.handle, int(bn), int(splits), int(bk)))
         self.ctx.check(lib().epsp_ladder_set_gemm_persistent(self.handle, 1 if persistent else 0))
-        self.ctx.check(lib().epsp_ladder_set_gemm_cluster(self.handle, int(cluster)))
         self.ctx.check(lib().epsp_ladder_set_gemm_pair(self.handle, 1 if pair else 0))
 
     def run(self, sigma, mu, Tlist, Omegas, *, solver="gmres", rtol=1e-2, maxiter=30, store_vertex=False,

@@ -262,27 +262,21 @@ epsp_status epsp_ladder_run_batched(epsp_ladder_plan* plan, const double* sigma,
  * and GEMM_TF32 plans; no counterpart in the reference): tile width bn (128 or 256), split count,
  * K block bk (64 or 32 on GEMM_BF16, 32 on GEMM_TF32; may be NULL), and the timed milliseconds per
  * launch of the choice and of the fixed heuristic's shape (0 when not a tensor-core plan). The
- * kernel choice comes from epsp_ladder_gemm_persistent, _cluster and _pair. */
+ * kernel choice comes from epsp_ladder_gemm_persistent and _pair. */
 epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, int32_t* splits, int32_t* bk,
                                     double* ms_chosen, double* ms_heuristic);
 /* Overrides the autotuner's choice: GEMM_BF16: tile width bn (128 or 256) with K blocks bk = 64
  * (128-byte swizzle; two or three pipeline stages), or bn 256 with bk = 32 (64-byte swizzle, four
  * stages); GEMM_TF32: bn 128 or 256 with bk = 32 (128-byte swizzle); splits within what the plan's
- * partial buffer holds. The one-CTA kernel is selected: persistent, cluster and pair settings are
- * reset (set them after). */
+ * partial buffer holds. The one-CTA kernel is selected: persistent and pair settings are reset
+ * (set them after). */
 epsp_status epsp_ladder_set_gemm_config(epsp_ladder_plan* plan, int32_t bn, int32_t splits, int32_t bk);
 /* Whether the contraction runs as the persistent kernel (one CTA per SM over all tiles, two TMEM
  * accumulators so that a tile's epilogue overlaps the next tile's products; GEMM_BF16: bn 256 with
  * bk 32 only; GEMM_TF32: either bn): read, and set (on = 0 or 1; EPSP_EINVAL for another tile
- * shape; off resets the cluster size to 1). Same results bitwise. */
+ * shape). Same results bitwise. */
 epsp_status epsp_ladder_gemm_persistent(const epsp_ladder_plan* plan, int32_t* on);
 epsp_status epsp_ladder_set_gemm_persistent(epsp_ladder_plan* plan, int32_t on);
-/* The persistent contraction's cluster size cm (1, 2 or 4; 2 at most with bn 128; cm > 1 needs the
- * persistent kernel): cm CTAs on consecutive M tiles share the B tile through TMA multicast, each
- * loading 1/cm of it, which cuts B's L2-to-SM traffic by cm. Read, and set (EPSP_EINVAL outside
- * those rules). Same results bitwise; epsp_ladder_set_gemm_config resets it to 1. */
-epsp_status epsp_ladder_gemm_cluster(const epsp_ladder_plan* plan, int32_t* cm);
-epsp_status epsp_ladder_set_gemm_cluster(epsp_ladder_plan* plan, int32_t cm);
 /* Whether the contraction runs as the CTA-pair kernel (tcgen05 cta_group::2: two CTAs of a cluster
  * compute a 256-row tile, each holding its 128 A rows and half of the B tile; bn 256 with bk 32):
  * read, and set (on = 0 or 1; on turns the persistent kernel off). Same results bitwise. */

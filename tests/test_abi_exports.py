@@ -53,9 +53,9 @@ def test_plan_queries_and_tile_setters_refuse_null_plans(library):
     vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
     out_p, out_i, out_n = vp(), i32(), i64()
     assert library.epsp_scgd0_sigma_device(None, C.byref(out_p), C.byref(out_n)) == EINVAL
-    for get in ("epsp_ladder_gemm_persistent", "epsp_ladder_gemm_cluster", "epsp_ladder_gemm_pair"):
+    for get in ("epsp_ladder_gemm_persistent", "epsp_ladder_gemm_pair"):
         assert getattr(library, get)(None, C.byref(out_i)) == EINVAL, get
-    for put in ("epsp_ladder_set_gemm_persistent", "epsp_ladder_set_gemm_cluster", "epsp_ladder_set_gemm_pair"):
+    for put in ("epsp_ladder_set_gemm_persistent", "epsp_ladder_set_gemm_pair"):
         assert getattr(library, put)(None, i32(1)) == EINVAL, put
     assert library.epsp_ladder_set_gemm_config(None, i32(256), i32(1), i32(32)) == EINVAL
 

@@ -232,13 +232,11 @@ def test_every_contraction_tile_shape_matches_the_oracle(api, oracle, cc, unit):
             got = plan.apply(J, sig, c["mu"][0], T, 0.07)
             assert np.all(np.isfinite(got)) and rel(got, ref) <= 1e-4, (bn, bk, sp, rel(got, ref))
             if (bn, bk) == (256, 32):
-                # the persistent kernel (one CTA per SM over all tiles, two TMEM accumulators), alone
-                # and in clusters of 2 and 4 CTAs sharing B by multicast, runs every tile's products
-                # in the same order: bitwise the same result
-                for cm in (1, 2, 4):
-                    plan.set_gemm_config(bn, sp, bk, persistent=True, cluster=cm)
-                    assert plan.gemm_config()["persistent"] and plan.gemm_config()["cluster"] == cm
-                    assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, cm)
+                # the persistent kernel (one CTA per SM over all tiles, two TMEM accumulators) runs
+                # every tile's products in the same order: bitwise the same result
+                plan.set_gemm_config(bn, sp, bk, persistent=True)
+                assert plan.gemm_config()["persistent"]
+                assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, "persistent")
                 # CTA pairs (tcgen05 cta_group::2, 256-row tiles over two CTAs): bitwise the same
                 plan.set_gemm_config(bn, sp, bk, pair=True)
                 assert plan.gemm_config()["pair"]
@@ -247,8 +245,6 @@ def test_every_contraction_tile_shape_matches_the_oracle(api, oracle, cc, unit):
         plan.set_gemm_config(128, 1, 32)
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(128, 1, 64, persistent=True)
-    with pytest.raises(ArgumentError):
-        plan.set_gemm_config(256, 1, 32, persistent=False, cluster=2)
     plan.close()
     # TF32: one product per K step of 8 (K boxes of 32 FP32 = 128 bytes), BN 128 (six stages) and
     # 256 (four), one and two splits, each also as the persistent kernel (bitwise the same)
@@ -259,18 +255,15 @@ def test_every_contraction_tile_shape_matches_the_oracle(api, oracle, cc, unit):
             plan.set_gemm_config(bn, sp, bk)
             got = plan.apply(J, sig, c["mu"][0], T, 0.07)
             assert np.all(np.isfinite(got)) and rel(got, ref) <= 1e-3, (bn, bk, sp, rel(got, ref))
-            for cm in ((1, 2, 4) if (bn, bk) == (256, 32) else (1, 2)):
-                plan.set_gemm_config(bn, sp, bk, persistent=True, cluster=cm)
-                assert plan.gemm_config()["persistent"] and plan.gemm_config()["cluster"] == cm
-                assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, cm)
+            plan.set_gemm_config(bn, sp, bk, persistent=True)
+            assert plan.gemm_config()["persistent"]
+            assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, "persistent")
             if bn == 256:
                 plan.set_gemm_config(bn, sp, bk, pair=True)
                 assert plan.gemm_config()["pair"]
                 assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, "pair")
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(256, 1, 64)
-    with pytest.raises(ArgumentError):
-        plan.set_gemm_config(128, 1, 32, persistent=True, cluster=4)
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(128, 1, 16)
     with pytest.raises(ArgumentError):
