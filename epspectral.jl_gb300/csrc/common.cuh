@@ -219,12 +219,26 @@ struct GridHost {
 
 GridHost make_grid(const epsp_grid& g, const char* name);
 
+// FrequencyGrid's constructor checks (src/frequency_grids.jl:124-132) on g, without allocating:
+// returns the smallest gap between consecutive offsets (dω_min = unit x that gap).
+int64_t check_grid(const epsp_grid& g, const char* name);
+
 // cell_search_table (src/frequency_grids.jl:184-196)
 struct CellTableHost {
   std::vector<int32_t> jtab;
   double x0 = 0, inv_h = 0;
 };
 CellTableHost make_cell_table(const GridHost& g);
+
+// The two steps of cell_search_table on the strictly increasing nodes x[0..n), shared by the plans
+// and the allocation-free entry point (which fills a fixed array): the bucket width 1 / inv_h,
+// inv_h = 1 / ((1 - 1e-6) dω_min); the table's entry count, the last node's bucket + 1, with the
+// bucket index clamped to 2^40 before it is converted to an integer; and the table itself,
+// jtab[k] = the first node whose bucket is >= k, for k < entries (EPSP_EINVAL when two nodes fall
+// in one bucket).
+inline double cell_inv_h(double dw_min) { return 1.0 / ((1.0 - 1e-6) * dw_min); }
+int64_t cell_table_entries(const double* x, int64_t n, double inv_h);
+void fill_cell_table(const double* x, int64_t n, double inv_h, int32_t* jtab, int64_t entries);
 
 // linear_interpolation_table (src/frequency_grids.jl:65-84), 0-based cells.
 void interp_table(const std::vector<double>& ws, const std::vector<double>& xs, std::vector<int32_t>& j,

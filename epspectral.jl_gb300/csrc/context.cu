@@ -7,45 +7,58 @@
 
 namespace epsp {
 
-GridHost make_grid(const epsp_grid& g, const char* name) {
-  // FrequencyGrid's constructor checks, src/frequency_grids.jl:124-132.
+int64_t check_grid(const epsp_grid& g, const char* name) {
   if (!(std::isfinite(g.origin) && std::isfinite(g.unit) && g.unit > 0))
     fail(EPSP_EINVAL, std::string(name) + ": origin must be finite and unit finite and positive");
   if (g.n < 2 || g.offsets == nullptr) fail(EPSP_EINVAL, std::string(name) + ": a FrequencyGrid needs at least two nodes");
-  GridHost h;
-  h.origin = g.origin;
-  h.unit = g.unit;
-  h.n = g.n;
-  h.offsets.assign(g.offsets, g.offsets + g.n);
   int64_t mg = std::numeric_limits<int64_t>::max();
   for (int64_t j = 0; j + 1 < g.n; ++j) {
     int64_t d = g.offsets[j + 1] - g.offsets[j];
     if (d <= 0) fail(EPSP_EINVAL, std::string(name) + ": offsets must be strictly increasing");
     mg = std::min(mg, d);
   }
+  return mg;
+}
+
+GridHost make_grid(const epsp_grid& g, const char* name) {
+  const int64_t mg = check_grid(g, name);
+  GridHost h;
+  h.origin = g.origin;
+  h.unit = g.unit;
+  h.n = g.n;
+  h.offsets.assign(g.offsets, g.offsets + g.n);
   h.dw_min = g.unit * double(mg);
   h.nodes.resize(size_t(g.n));
   for (int64_t j = 0; j < g.n; ++j) h.nodes[size_t(j)] = g.origin + double(g.offsets[j]) * g.unit;
   return h;
 }
 
+int64_t cell_table_entries(const double* x, int64_t n, double inv_h) {
+  return int64_t(std::min((x[n - 1] - x[0]) * inv_h, std::ldexp(1.0, 40))) + 1;
+}
+
+void fill_cell_table(const double* x, int64_t n, double inv_h, int32_t* jtab, int64_t entries) {
+  // the caller checked entries against its table's capacity, so every bucket below is < 2^40
+  auto bucket = [&](int64_t j) { return int64_t((x[j] - x[0]) * inv_h); };
+  for (int64_t j = 0; j + 1 < n; ++j)
+    if (bucket(j + 1) == bucket(j)) fail(EPSP_EINVAL, "two grid nodes fall in one bucket");
+  int64_t c = 0;
+  for (int64_t k = 0; k < entries; ++k) {
+    while (c < n && bucket(c) < k) ++c;
+    jtab[k] = int32_t(c);
+  }
+}
+
 CellTableHost make_cell_table(const GridHost& g) {
   CellTableHost ct;
   ct.x0 = g.nodes[0];
-  ct.inv_h = 1.0 / ((1.0 - 1e-6) * g.dw_min);
-  double span_b = std::min((g.nodes.back() - ct.x0) * ct.inv_h, std::ldexp(1.0, 40));
-  if (int64_t(span_b) + 1 > (int64_t(1) << 24))
+  ct.inv_h = cell_inv_h(g.dw_min);
+  const int64_t n = int64_t(g.nodes.size());
+  const int64_t entries = cell_table_entries(g.nodes.data(), n, ct.inv_h);
+  if (entries > (int64_t(1) << 24))
     fail(EPSP_EINVAL, "cell search table of more than 2^24 entries: use a grid without a near-coincident pair of nodes");
-  std::vector<int64_t> b(g.nodes.size());
-  for (size_t j = 0; j < g.nodes.size(); ++j) b[j] = int64_t((g.nodes[j] - ct.x0) * ct.inv_h);
-  for (size_t j = 0; j + 1 < b.size(); ++j)
-    if (b[j + 1] == b[j]) fail(EPSP_EINVAL, "two grid nodes fall in one bucket");
-  ct.jtab.resize(size_t(b.back() + 1));
-  size_t c = 0;
-  for (int64_t k = 0; k <= b.back(); ++k) {
-    while (c < b.size() && b[c] < k) ++c;
-    ct.jtab[size_t(k)] = int32_t(c);
-  }
+  ct.jtab.resize(size_t(entries));
+  fill_cell_table(g.nodes.data(), n, ct.inv_h, ct.jtab.data(), entries);
   return ct;
 }
 

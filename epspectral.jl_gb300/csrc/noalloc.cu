@@ -115,41 +115,25 @@ extern "C" epsp_status epsp_scgd0_imsigma_noalloc(epsp_ctx* ctx, int64_t nm, int
       g_scratch_dev[c->device] = p;
     }
     // Grid checks and tables, as FrequencyGrid and cell_search_table (src/frequency_grids.jl:124-196),
-    // into the fixed host staging arrays.
+    // by the helpers the plans use, into the fixed host staging arrays.
     const epsp_grid& g = *omegas;
-    if (!(std::isfinite(g.origin) && std::isfinite(g.unit) && g.unit > 0))
-      fail(EPSP_EINVAL, "omegas: origin must be finite and unit finite and positive");
-    if (g.n < 2 || !g.offsets) fail(EPSP_EINVAL, "omegas: a FrequencyGrid needs at least two nodes");
+    const int64_t mg = check_grid(g, "omegas");
     if (g.n > kNoallocMaxNodes)
       fail(EPSP_EINVAL, "omegas has " + std::to_string(g.n) + " nodes; epsp_scgd0_imsigma_noalloc takes at most " +
                             std::to_string(kNoallocMaxNodes));
-    int64_t mg = INT64_MAX;
-    for (int64_t j = 0; j + 1 < g.n; ++j) {
-      if (g.offsets[j + 1] <= g.offsets[j]) fail(EPSP_EINVAL, "omegas: offsets must be strictly increasing");
-      mg = std::min(mg, g.offsets[j + 1] - g.offsets[j]);
-    }
     for (int64_t j = 0; j < g.n; ++j) g_nodes_host[j] = g.origin + double(g.offsets[j]) * g.unit;
     const double x0 = g_nodes_host[0];
-    const double inv_h = 1.0 / ((1.0 - 1e-6) * (g.unit * double(mg)));
-    const int64_t last_bucket = int64_t((g_nodes_host[g.n - 1] - x0) * inv_h);
-    if (last_bucket + 1 > kNoallocMaxTable)
-      fail(EPSP_EINVAL, "the cell-search table of omegas needs " + std::to_string(last_bucket + 1) +
+    const double inv_h = cell_inv_h(g.unit * double(mg));
+    const int64_t entries = cell_table_entries(g_nodes_host, g.n, inv_h);
+    if (entries > kNoallocMaxTable)
+      fail(EPSP_EINVAL, "the cell-search table of omegas needs " + std::to_string(entries) +
                             " entries; epsp_scgd0_imsigma_noalloc holds at most " + std::to_string(kNoallocMaxTable));
-    int64_t cnt = 0, prev = -1;
-    for (int64_t k = 0; k <= last_bucket; ++k) {
-      while (cnt < g.n && int64_t((g_nodes_host[cnt] - x0) * inv_h) < k) ++cnt;
-      g_table_host[k] = int32_t(cnt);
-    }
-    for (int64_t j = 0; j < g.n; ++j) {
-      const int64_t b = int64_t((g_nodes_host[j] - x0) * inv_h);
-      if (b == prev) fail(EPSP_EINVAL, "omegas: two grid nodes fall in one bucket");
-      prev = b;
-    }
+    fill_cell_table(g_nodes_host, g.n, inv_h, g_table_host, entries);
     unsigned char* base = static_cast<unsigned char*>(g_scratch_dev[c->device]);
     double* d_nodes = reinterpret_cast<double*>(base);
     int32_t* d_table = reinterpret_cast<int32_t*>(base + size_t(kNoallocMaxNodes) * 8);
     EPSP_CUDA(cudaMemcpyAsync(d_nodes, g_nodes_host, size_t(g.n) * 8, cudaMemcpyHostToDevice, c->stream));
-    EPSP_CUDA(cudaMemcpyAsync(d_table, g_table_host, size_t(last_bucket + 1) * 4, cudaMemcpyHostToDevice, c->stream));
+    EPSP_CUDA(cudaMemcpyAsync(d_table, g_table_host, size_t(entries) * 4, cudaMemcpyHostToDevice, c->stream));
     CellTableDev ct{d_table, d_nodes, x0, inv_h, int(g.n)};
     dim3 grid(div_up(size_t(g.n), 128), unsigned(ni));
     fm_direct_noalloc_kernel<<<grid, 128, 0, c->stream>>>(d_nodes, int(g.n), ct, reinterpret_cast<const double2*>(sigma_in),

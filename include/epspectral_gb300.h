@@ -211,12 +211,15 @@ epsp_status epsp_scgd0_imsigma(epsp_scgd0_plan* plan, const double* sigma_in, do
  * allowed passes every array as a device pointer it already owns, in the layouts of epsp_model
  * (g2 [nm, ni, nf] as FP64 here), sigma_in [nω, ni] complex and imsigma [nω, ni] (accumulated into,
  * as epsp_scgd0_imsigma). The library allocates nothing: the grid nodes and the cell-search table
- * live in a fixed static device array of 2.5 MiB (at most 65536 nodes and 2^20 table entries;
- * larger grids are rejected with EPSP_EINVAL), which every device that loads the library keeps until
- * the process exits. The first call on a device looks up that array's address (set-up once per
- * device), so make the first call before any stream capture. Calls share the array and synchronise
- * before returning; calls that overlap on the GPU (other threads, other contexts on the same
- * device) race on it. Index arrays must hold valid indices, as the reference's @inbounds reads. */
+ * live in a fixed static device array of 4.5 MiB (65536 nodes x 8 bytes + 2^20 table entries x 4
+ * bytes; larger grids are rejected with EPSP_EINVAL), which every device that loads the library
+ * keeps until the process exits. The first call on a device looks up that array's address (set-up
+ * once per device), so make the first call before any stream capture. The kernel runs on the
+ * context's own stream, which is not ordered after the caller's streams: the caller's device inputs
+ * must be complete before the call (synchronise the stream that wrote them). The call is
+ * synchronous: it returns after the kernel has finished, so imsigma is ready on return. Calls share
+ * the array; calls that overlap on the GPU (other threads, other contexts on the same device) race
+ * on it. Index arrays must hold valid indices, as the reference's @inbounds reads. */
 epsp_status epsp_scgd0_imsigma_noalloc(epsp_ctx* ctx, int64_t nm, int64_t ni, int64_t nf, const double* g2,
                                        int64_t nq, const double* omega_ph, int64_t nk_i, int64_t nk_f,
                                        const int32_t* iq_kk, const int32_t* iks_i, const int32_t* iks_f,

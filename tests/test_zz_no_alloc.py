@@ -79,3 +79,10 @@ def test_noalloc_matches_plan_path():
             d_iksi.data_ptr(), d_iksf.data_ptr(), d_eps.data_ptr(), d_wf.data_ptr(), d_fti.data_ptr(),
             C.byref(big.struct), w_ac, d_sin.data_ptr(), mu, T, d_out.data_ptr())
     assert st == 1 and b"at most" in lib.epsp_last_error(ctx.handle)
+    # offsets spread over ±2^62 with a gap of 1: the bucket count is clamped before its conversion to
+    # an integer, so the table size is refused (no overflow) and nothing reaches the device
+    wide = GridArrays(FrequencyGrid(0.0, 1.0, np.array([-(2 ** 62), -(2 ** 62) + 1, 2 ** 62], dtype=np.int64)))
+    st = fn(ctx.handle, nm, ni, nf, d_g2.data_ptr(), nq, d_wph.data_ptr(), nk_i, nk_f, d_iq.data_ptr(),
+            d_iksi.data_ptr(), d_iksf.data_ptr(), d_eps.data_ptr(), d_wf.data_ptr(), d_fti.data_ptr(),
+            C.byref(wide.struct), w_ac, d_sin.data_ptr(), mu, T, d_out.data_ptr())
+    assert st == 1 and b"at most" in lib.epsp_last_error(ctx.handle)
