@@ -6,7 +6,9 @@
 # library, and turns its status codes into the reference's errors (ArgumentError for EINVAL and
 # ENOROOT_MU) and its convergence flags into the reference's warnings. Arrays are passed by pointer
 # in their Julia (column-major) layout; index arrays are converted to 0-based Int32 once per call.
-# Not executed in this repository (no Julia toolchain here); see INTEGRATION.md for how to wire it.
+# Not executed in this repository (no Julia toolchain here). To wire it, include this file from
+# EPSpectral.jl and add a method of `_loop_scgd0` / `_loop_ladder` for `backend::GB300Backend` that
+# calls `loop_scgd0` / `loop_ladder` below.
 module EPSpectralGB300
 
 const LIB = get(ENV, "EPSPECTRAL_GB300_LIB", joinpath(@__DIR__, "..", "epspectral_gb300", "libepspectral_gb300.so"))

@@ -304,7 +304,9 @@ void fan_migdal(const Model& M, const CellTable& ct, int64_t nf_chunk, const dou
   if (ib < 0) ib = M.ni;
   for (int64_t f0 = 0; f0 < M.nf; f0 += nf_chunk) {
     int64_t f1 = std::min(M.nf, f0 + nf_chunk);
-#pragma omp parallel for schedule(dynamic, 1)
+    // every (i, ω) element is summed on its own in ascending νf, so the split over threads does not
+    // change the result
+#pragma omp parallel for collapse(2) schedule(dynamic, 8)
     for (int64_t i = ia; i < ib; ++i) {
       for (int64_t iw = 0; iw < M.nw; ++iw) {
         double w = M.ws[iw];
@@ -656,10 +658,11 @@ void attach_bare(const Ladder& L, const std::vector<cplx>& Gm, const std::vector
         }
 }
 
-// attach_greens_to_vertex!, src/ladder_kernel.jl:61-67, 87-89: J = Gm X Gp per (ω, cart, c0, i).
+// attach_greens_to_vertex!, src/ladder_kernel.jl:61-67, 87-89: J = Gm X Gp per (ω, cart, c0, i),
+// for the outer states [ia, ia + n) (all by default); X and J hold those n states only.
 void attach(const Ladder& L, const std::vector<cplx>& Gm, const std::vector<cplx>& Gp,
-            const std::vector<cplx>& X, double* J, double scale) {
-  const int64_t nw = L.M.nw, ni = L.M.ni;
+            const std::vector<cplx>& X, double* J, double scale, int64_t ia = 0, int64_t n = -1) {
+  const int64_t nw = L.M.nw, ni = n < 0 ? L.M.ni : n;
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < ni; ++i)
     for (int c0 = 0; c0 < 2; ++c0)
@@ -667,8 +670,8 @@ void attach(const Ladder& L, const std::vector<cplx>& Gm, const std::vector<cplx
         for (int c12 = 0; c12 < 4; ++c12) {
           int c1 = c12 % 2, c2 = c12 / 2;
           for (int64_t w = 0; w < nw; ++w) {
-            auto gm = [&](int c) { return Gm[size_t(w + nw * (c + 4 * i))]; };
-            auto gp = [&](int c) { return Gp[size_t(w + nw * (c + 4 * i))]; };
+            auto gm = [&](int c) { return Gm[size_t(w + nw * (c + 4 * (ia + i)))]; };
+            auto gp = [&](int c) { return Gp[size_t(w + nw * (c + 4 * (ia + i)))]; };
             auto x = [&](int c) { return X[jidx(nw, w, c, cart, c0, i)]; };
             cplx z = gm(c1) * x(0) * gp(0 + 2 * c2) + gm(c1 + 2) * x(1) * gp(0 + 2 * c2) +
                      gm(c1) * x(2) * gp(1 + 2 * c2) + gm(c1 + 2) * x(3) * gp(1 + 2 * c2);
@@ -702,165 +705,99 @@ void conductivity(const double* J, const double* v, const double* w_i, const dou
     }
 }
 
-// The dominant part of apply_ladder_kernel! for the output columns (a, i, type) of the outer states
-// [ia, ib): B, B̃ and C± += X B̃ over every chunk (src/ladder.jl:254-291), the CPU baseline's
-// bounded sample. Returns nothing; the work is what is timed.
-void ladder_contract_sample(const Ladder& L, double T, double w_ac, const double* J, int64_t ia, int64_t ib) {
+// B (bin_coupling_on_shift_grid!, src/ladder_kernel.jl:195-236) and B̃ (star_sum_coupling!,
+// :240-264) of one chunk for the output columns col = (a, ii, type) of the outer states
+// [ia, ia + nsel): Bt [nk, 6 nsel], nk = nshift·3·nip, rows (m, b, ip).
+void chunk_coupling(const Ladder& L, const Ladder::Chunk& ch, double T, double w_ac, int64_t ia, int64_t nsel,
+                    double* Bt) {
   const Model& M = L.M;
   const epsp_model* mp = M.m;
-  const int64_t nw = M.nw, nm = M.nm, ns = L.nshift;
-  const int64_t nrow = nw * 16, nsel = ib - ia, ncol = 6 * nsel;
-  std::vector<double> Cp(size_t(nrow * ncol), 0.0), Cm(size_t(nrow * ncol), 0.0);
-  for (const auto& ch : L.chunks) {
-    const int64_t nfc = int64_t(ch.fidx.size()), nip = ch.i1 - ch.i0;
-    std::vector<double> B(size_t(ns * nfc * nsel * 2), 0.0);
+  const int64_t nm = M.nm, ns = L.nshift;
+  const int64_t nfc = int64_t(ch.fidx.size()), nip = ch.i1 - ch.i0, ncol = 6 * nsel;
+  std::vector<double> B(size_t(ns * nfc * nsel * 2), 0.0);
 #pragma omp parallel for schedule(static)
-    for (int64_t fc = 0; fc < nfc; ++fc) {
-      int64_t f = ch.fidx[size_t(fc)];
-      for (int type = 0; type < 2; ++type)
-        for (int64_t ii = 0; ii < nsel; ++ii) {
-          int64_t i = ia + ii;
-          double* col = B.data() + ns * (fc + nfc * (ii + nsel * type));
-          for (int64_t nu = 0; nu < nm; ++nu) {
-            double w = M.omega_q(nu, f, i);
-            if (w < w_ac) continue;
-            double x = w / L.h;
-            int64_t lo = int64_t(std::floor(x));
-            double g = M.g2(nu, i, f);
-            for (int64_t m = lo; m <= lo + 1; ++m) {
-              double c = g * std::max(0.0, 1 - std::fabs(x - double(m)));
-              col[m] += type == 0 ? c : c * occ_boson(w, T);
-            }
-          }
-          for (int64_t m = 0; m < ns; ++m) col[m] *= mp->w_f[f];
-        }
-    }
-    const int64_t nk = ns * 3 * nip;
-    std::vector<double> Bt(size_t(nk * ncol));
-#pragma omp parallel for schedule(static)
-    for (int64_t col = 0; col < ncol; ++col) {
-      int64_t a = col % 3, ii = (col / 3) % nsel, type = col / (3 * nsel);
-      for (int64_t ip = 0; ip < nip; ++ip)
-        for (int b = 0; b < 3; ++b)
-          for (int64_t m = 0; m < ns; ++m) {
-            double acc = 0.0;
-            for (int32_t fc = ch.sptr[size_t(ip)]; fc < ch.sptr[size_t(ip + 1)]; ++fc)
-              acc += mp->R[a + 3 * (b + 3 * int64_t(ch.fidx[size_t(fc)]))] * B[size_t(m + ns * (fc + nfc * (ii + nsel * type)))];
-            Bt[size_t(m + ns * (b + 3 * ip) + nk * col)] = acc;
-          }
-    }
-    std::vector<double> X(size_t(nrow * nk));
-    for (int s = 0; s < 2; ++s) {
-      const int32_t* klo = L.klo.data() + nw * ns * s;
-      const double* wlo = L.wlo.data() + nw * ns * s;
-      const double* whi = L.whi.data() + nw * ns * s;
-#pragma omp parallel for schedule(static)
-      for (int64_t kk = 0; kk < nk; ++kk) {
-        int64_t m = kk % ns, b = (kk / ns) % 3, ip = kk / (3 * ns);
-        int64_t i = ch.i0 + ip;
-        for (int c0 = 0; c0 < 2; ++c0)
-          for (int c12 = 0; c12 < 4; ++c12)
-            for (int64_t j = 0; j < nw; ++j) {
-              int64_t k = klo[j + nw * m];
-              size_t a0 = jidx(nw, k, c12, b, c0, i), a1 = jidx(nw, k + 1, c12, b, c0, i);
-              double wl = wlo[j + nw * m], wh = whi[j + nw * m];
-              X[size_t(j + nw * (c12 + 4 * c0) + nrow * kk)] = wl * J[2 * a0] + wh * J[2 * a1];
-              X[size_t(j + nw * (c12 + 4 * (c0 + 2)) + nrow * kk)] = wl * J[2 * a0 + 1] + wh * J[2 * a1 + 1];
-            }
-      }
-      // C += X B̃ threaded over row blocks of C, as the reference does (src/ladder.jl:286-289).
-      double* C = s == 0 ? Cp.data() : Cm.data();
-      const int64_t rb = 256, nrb = (nrow + rb - 1) / rb;
-#pragma omp parallel for schedule(static)
-      for (int64_t blk = 0; blk < nrb; ++blk) {
-        const int64_t r0 = blk * rb, r1 = std::min(nrow, r0 + rb);
-        for (int64_t col = 0; col < ncol; ++col) {
-          double* Cc = C + nrow * col;
-          const double* Bc = Bt.data() + nk * col;
-          for (int64_t k = 0; k < nk; ++k) {
-            double bv = Bc[k];
-            if (bv == 0.0) continue;
-            const double* Xk = X.data() + nrow * k;
-            for (int64_t r = r0; r < r1; ++r) Cc[r] += Xk[r] * bv;
+  for (int64_t fc = 0; fc < nfc; ++fc) {
+    int64_t f = ch.fidx[size_t(fc)];
+    for (int type = 0; type < 2; ++type)
+      for (int64_t ii = 0; ii < nsel; ++ii) {
+        int64_t i = ia + ii;
+        double* col = B.data() + ns * (fc + nfc * (ii + nsel * type));
+        for (int64_t nu = 0; nu < nm; ++nu) {
+          double w = M.omega_q(nu, f, i);
+          if (w < w_ac) continue;
+          double x = w / L.h;
+          int64_t lo = int64_t(std::floor(x));
+          double g = M.g2(nu, i, f);
+          for (int64_t m = lo; m <= lo + 1; ++m) {
+            double c = g * std::max(0.0, 1 - std::fabs(x - double(m)));
+            col[m] += type == 0 ? c : c * occ_boson(w, T);
           }
         }
+        double wf = mp->w_f[f];
+        for (int64_t m = 0; m < ns; ++m) col[m] *= wf;
       }
-    }
+  }
+  const int64_t nk = ns * 3 * nip;
+#pragma omp parallel for schedule(static)
+  for (int64_t col = 0; col < ncol; ++col) {  // col = (a, ii, type)
+    int64_t a = col % 3, ii = (col / 3) % nsel, type = col / (3 * nsel);
+    for (int64_t ip = 0; ip < nip; ++ip)
+      for (int b = 0; b < 3; ++b)
+        for (int64_t m = 0; m < ns; ++m) {
+          double acc = 0.0;
+          for (int32_t fc = ch.sptr[size_t(ip)]; fc < ch.sptr[size_t(ip + 1)]; ++fc)
+            acc += mp->R[a + 3 * (b + 3 * int64_t(ch.fidx[size_t(fc)]))] *
+                   B[size_t(m + ns * (fc + nfc * (ii + nsel * type)))];
+          Bt[size_t(m + ns * (b + 3 * ip) + nk * col)] = acc;
+        }
   }
 }
 
-// apply_ladder_kernel!, src/ladder.jl:245-296.
+// X of one chunk and sign s (gather_shifted_vertex!, src/ladder_kernel.jl:268-288): X [16 nω, nk],
+// rows (j, c12, c0, ri), columns (m, b, ip).
+void chunk_shifted_vertex(const Ladder& L, const Ladder::Chunk& ch, int s, const double* J, double* X) {
+  const int64_t nw = L.M.nw, ns = L.nshift, nrow = nw * 16;
+  const int64_t nk = ns * 3 * (ch.i1 - ch.i0);
+  const int32_t* klo = L.klo.data() + nw * ns * s;
+  const double* wlo = L.wlo.data() + nw * ns * s;
+  const double* whi = L.whi.data() + nw * ns * s;
+#pragma omp parallel for schedule(static)
+  for (int64_t kk = 0; kk < nk; ++kk) {  // kk = (m, b, ip)
+    int64_t m = kk % ns, b = (kk / ns) % 3, ip = kk / (3 * ns);
+    int64_t i = ch.i0 + ip;
+    for (int c0 = 0; c0 < 2; ++c0)
+      for (int c12 = 0; c12 < 4; ++c12)
+        for (int64_t j = 0; j < nw; ++j) {
+          int64_t k = klo[j + nw * m];
+          size_t a0 = jidx(nw, k, c12, b, c0, i), a1 = jidx(nw, k + 1, c12, b, c0, i);
+          double wl = wlo[j + nw * m], wh = whi[j + nw * m];
+          double zr = wl * J[2 * a0] + wh * J[2 * a1];
+          double zi = wl * J[2 * a0 + 1] + wh * J[2 * a1 + 1];
+          X[size_t(j + nw * (c12 + 4 * (c0 + 2 * 0)) + nrow * kk)] = zr;  // row (j, c12, c0, ri)
+          X[size_t(j + nw * (c12 + 4 * (c0 + 2 * 1)) + nrow * kk)] = zi;
+        }
+  }
+}
+
+// apply_ladder_kernel!, src/ladder.jl:245-296, for the output states [ia, ib) (all of them by
+// default): LJ [nω, 4, 3, 2, ib - ia]. An output state's columns of C± and of the exchange part
+// depend on that state's columns of B̃ only, and each is summed in the same order whatever the
+// range, so a range's LJ is bitwise the full LJ's slice.
 void ladder_apply(const Ladder& L, const std::vector<cplx>& Gm, const std::vector<cplx>& Gp, double T,
-                  double w_ac, const double* J, double* LJ) {
+                  double w_ac, const double* J, double* LJ, int64_t ia = 0, int64_t ib = -1) {
   const Model& M = L.M;
-  const epsp_model* mp = M.m;
-  const int64_t nw = M.nw, ni = M.ni, nm = M.nm, ns = L.nshift;
+  if (ib < 0) ib = M.ni;
+  const int64_t nw = M.nw, ni = ib - ia, ns = L.nshift;
   const int64_t nrow = nw * 16, ncol = 6 * ni;
   std::vector<double> Cp(size_t(nrow * ncol), 0.0), Cm(size_t(nrow * ncol), 0.0);
   for (const auto& ch : L.chunks) {
-    const int64_t nfc = int64_t(ch.fidx.size()), nip = ch.i1 - ch.i0;
-    // ωq, nB and B (bin_coupling_on_shift_grid!, src/ladder_kernel.jl:195-236).
-    std::vector<double> B(size_t(ns * nfc * ni * 2), 0.0);
-#pragma omp parallel for schedule(static)
-    for (int64_t fc = 0; fc < nfc; ++fc) {
-      int64_t f = ch.fidx[size_t(fc)];
-      for (int type = 0; type < 2; ++type)
-        for (int64_t i = 0; i < ni; ++i) {
-          double* col = B.data() + ns * (fc + nfc * (i + ni * type));
-          for (int64_t nu = 0; nu < nm; ++nu) {
-            double w = M.omega_q(nu, f, i);
-            if (w < w_ac) continue;
-            double x = w / L.h;
-            int64_t lo = int64_t(std::floor(x));
-            double g = M.g2(nu, i, f);
-            for (int64_t m = lo; m <= lo + 1; ++m) {
-              double c = g * std::max(0.0, 1 - std::fabs(x - double(m)));
-              col[m] += type == 0 ? c : c * occ_boson(w, T);
-            }
-          }
-          double wf = mp->w_f[f];
-          for (int64_t m = 0; m < ns; ++m) col[m] *= wf;
-        }
-    }
-    // B̃ (star_sum_coupling!, :240-264): Bt[m, b, ip, a, i, type].
-    const int64_t nk = ns * 3 * nip;
+    const int64_t nk = ns * 3 * (ch.i1 - ch.i0);
     std::vector<double> Bt(size_t(nk * ncol));
-#pragma omp parallel for schedule(static)
-    for (int64_t col = 0; col < ncol; ++col) {  // col = (a, i, type)
-      int64_t a = col % 3, i = (col / 3) % ni, type = col / (3 * ni);
-      for (int64_t ip = 0; ip < nip; ++ip)
-        for (int b = 0; b < 3; ++b)
-          for (int64_t m = 0; m < ns; ++m) {
-            double acc = 0.0;
-            for (int32_t fc = ch.sptr[size_t(ip)]; fc < ch.sptr[size_t(ip + 1)]; ++fc)
-              acc += mp->R[a + 3 * (b + 3 * int64_t(ch.fidx[size_t(fc)]))] *
-                     B[size_t(m + ns * (fc + nfc * (i + ni * type)))];
-            Bt[size_t(m + ns * (b + 3 * ip) + nk * col)] = acc;
-          }
-    }
-    // X per sign (gather_shifted_vertex!, :268-288) and C_s += X · B̃ (src/ladder.jl:283-290).
+    chunk_coupling(L, ch, T, w_ac, ia, ni, Bt.data());
+    // C_s += X_s · B̃ (src/ladder.jl:283-290)
     std::vector<double> X(size_t(nrow * nk));
     for (int s = 0; s < 2; ++s) {
-      const int32_t* klo = L.klo.data() + nw * ns * s;
-      const double* wlo = L.wlo.data() + nw * ns * s;
-      const double* whi = L.whi.data() + nw * ns * s;
-#pragma omp parallel for schedule(static)
-      for (int64_t kk = 0; kk < nk; ++kk) {  // kk = (m, b, ip)
-        int64_t m = kk % ns, b = (kk / ns) % 3, ip = kk / (3 * ns);
-        int64_t i = ch.i0 + ip;
-        for (int c0 = 0; c0 < 2; ++c0)
-          for (int c12 = 0; c12 < 4; ++c12)
-            for (int64_t j = 0; j < nw; ++j) {
-              int64_t k = klo[j + nw * m];
-              size_t a0 = jidx(nw, k, c12, b, c0, i), a1 = jidx(nw, k + 1, c12, b, c0, i);
-              double wl = wlo[j + nw * m], wh = whi[j + nw * m];
-              double zr = wl * J[2 * a0] + wh * J[2 * a1];
-              double zi = wl * J[2 * a0 + 1] + wh * J[2 * a1 + 1];
-              // row (j, c12, c0, ri)
-              X[size_t(j + nw * (c12 + 4 * (c0 + 2 * 0)) + nrow * kk)] = zr;
-              X[size_t(j + nw * (c12 + 4 * (c0 + 2 * 1)) + nrow * kk)] = zi;
-            }
-      }
+      chunk_shifted_vertex(L, ch, s, J, X.data());
       double* C = s == 0 ? Cp.data() : Cm.data();
 #pragma omp parallel for schedule(static)
       for (int64_t col = 0; col < ncol; ++col) {
@@ -910,7 +847,7 @@ void ladder_apply(const Ladder& L, const std::vector<cplx>& Gm, const std::vecto
             }
             KJ[jidx(nw, w, c12, a, c0, i)] = r;
           }
-  attach(L, Gm, Gp, KJ, LJ, -1.0);  // src/ladder.jl:294-295
+  attach(L, Gm, Gp, KJ, LJ, -1.0, ia, ni);  // src/ladder.jl:294-295
 }
 
 double vnorm(const std::vector<cplx>& x) {
@@ -1296,13 +1233,42 @@ int epsp_oracle_imsigma_sample(const epsp_model* m, const epsp_options* opts, co
   });
 }
 
-int epsp_oracle_ladder_contract_sample(const epsp_model* m, const epsp_options* opts, double T, const double* J,
-                                       int64_t i0, int64_t i1, char* msg, int32_t msglen) {
+int epsp_oracle_ladder_apply_sample(const epsp_model* m, const epsp_options* opts, const double* sigma_T, double mu,
+                                    double T, double Omega, const double* J, int64_t i0, int64_t i1, double* LJ,
+                                    char* msg, int32_t msglen) {
   apply_threads();
   return guarded(msg, msglen, [&] {
     Ladder L = make_ladder(m, opts->gpu_tile);
     if (i0 < 0 || i1 > L.M.ni || i0 >= i1) throw OracleError(EPSP_EINVAL, "bad outer-state range");
-    ladder_contract_sample(L, T, opts->omega_acoustic, J, i0, i1);
+    std::vector<cplx> Gm, Gp;
+    propagators(L, sigma_T, mu, T, Omega, Gm, Gp);
+    ladder_apply(L, Gm, Gp, T, opts->omega_acoustic, J, LJ, i0, i1);
+  });
+}
+
+int epsp_oracle_ladder_chunks(const epsp_model* m, const epsp_options* opts, int64_t* n_chunks, int64_t* i_lo,
+                              int64_t* i_hi, int64_t cap, int64_t* nshift, char* msg, int32_t msglen) {
+  return guarded(msg, msglen, [&] {
+    Ladder L = make_ladder(m, opts->gpu_tile);
+    *n_chunks = int64_t(L.chunks.size());
+    if (nshift) *nshift = L.nshift;
+    for (int64_t c = 0; c < std::min<int64_t>(cap, *n_chunks); ++c) {
+      i_lo[c] = L.chunks[size_t(c)].i0;
+      i_hi[c] = L.chunks[size_t(c)].i1;
+    }
+  });
+}
+
+int epsp_oracle_ladder_chunk_operands(const epsp_model* m, const epsp_options* opts, double T, const double* J,
+                                      int64_t chunk, double* Xp, double* Xm, double* Bt, char* msg, int32_t msglen) {
+  apply_threads();
+  return guarded(msg, msglen, [&] {
+    Ladder L = make_ladder(m, opts->gpu_tile);
+    if (chunk < 0 || chunk >= int64_t(L.chunks.size())) throw OracleError(EPSP_EINVAL, "bad chunk index");
+    const auto& ch = L.chunks[size_t(chunk)];
+    chunk_coupling(L, ch, T, opts->omega_acoustic, 0, L.M.ni, Bt);
+    chunk_shifted_vertex(L, ch, 0, J, Xp);
+    chunk_shifted_vertex(L, ch, 1, J, Xm);
   });
 }
 

@@ -83,14 +83,23 @@ int epsp_oracle_ladder_run(const epsp_model* m, const epsp_options* opts, const 
                            int32_t* niter, epsp_ladder_history* hist, double* J_out, char* msg,
                            int32_t msglen);
 
-/* Bounded samples of the two dominant CPU costs, for the benchmark's CPU baseline: the Fan-Migdal
- * sum of the outer states [i0, i1) only (imsigma [nω, ni], those columns accumulated), and the
- * shift-grid contraction C± += X B̃ of apply_ladder_kernel! for the output columns of the outer
- * states [i0, i1) (src/ladder.jl:254-291). */
+/* Bounded samples of the two dominant CPU costs, for the benchmark's CPU baseline and the parity
+ * tests at full size: the Fan-Migdal sum of the outer states [i0, i1) only (imsigma [nω, ni], those
+ * columns accumulated); one ladder application for the output states [i0, i1) only (LJ [nω, 4, 3, 2,
+ * i1 - i0], bitwise the full application's slice); the chunks of apply_ladder_kernel!
+ * (src/ladder.jl:180-202: count, outer-state ranges [i_lo, i_hi) of the first cap chunks, nshift);
+ * and one chunk's operands of C± += X± B̃ (src/ladder.jl:254-290): X± [16 nω, nk] and B̃ [nk, 6 ni],
+ * nk = nshift·3·(i_hi - i_lo), so that the product can be timed as a BLAS DGEMM, as the reference's
+ * mul! runs it. */
 int epsp_oracle_imsigma_sample(const epsp_model* m, const epsp_options* opts, const double* sigma_in, double mu,
                                double T, int64_t i0, int64_t i1, double* imsigma, char* msg, int32_t msglen);
-int epsp_oracle_ladder_contract_sample(const epsp_model* m, const epsp_options* opts, double T, const double* J,
-                                       int64_t i0, int64_t i1, char* msg, int32_t msglen);
+int epsp_oracle_ladder_apply_sample(const epsp_model* m, const epsp_options* opts, const double* sigma_T, double mu,
+                                    double T, double Omega, const double* J, int64_t i0, int64_t i1, double* LJ,
+                                    char* msg, int32_t msglen);
+int epsp_oracle_ladder_chunks(const epsp_model* m, const epsp_options* opts, int64_t* n_chunks, int64_t* i_lo,
+                              int64_t* i_hi, int64_t cap, int64_t* nshift, char* msg, int32_t msglen);
+int epsp_oracle_ladder_chunk_operands(const epsp_model* m, const epsp_options* opts, double T, const double* J,
+                                      int64_t chunk, double* Xp, double* Xm, double* Bt, char* msg, int32_t msglen);
 
 /* Threads used by the OpenMP loops (0 = the OpenMP default). */
 void epsp_oracle_set_threads(int32_t n);

@@ -79,8 +79,12 @@ def lib():
                                                  c_int32_p, P(epsp_ladder_history), c_double_p] + msg),
             "epsp_oracle_imsigma_sample": (C.c_int, [P(epsp_model), P(epsp_options), c_double_p, d, d, i64, i64,
                                                      c_double_p] + msg),
-            "epsp_oracle_ladder_contract_sample": (C.c_int, [P(epsp_model), P(epsp_options), d, c_double_p, i64, i64]
-                                                   + msg),
+            "epsp_oracle_ladder_apply_sample": (C.c_int, [P(epsp_model), P(epsp_options), c_double_p, d, d, d,
+                                                          c_double_p, i64, i64, c_double_p] + msg),
+            "epsp_oracle_ladder_chunks": (C.c_int, [P(epsp_model), P(epsp_options), P(i64), P(i64), P(i64), i64,
+                                                    P(i64)] + msg),
+            "epsp_oracle_ladder_chunk_operands": (C.c_int, [P(epsp_model), P(epsp_options), d, c_double_p, i64,
+                                                            c_double_p, c_double_p, c_double_p] + msg),
             "epsp_oracle_set_threads": (None, [i32]),
             "epsp_oracle_get_threads": (i32, []),
         }
@@ -289,11 +293,48 @@ def imsigma_sample(setup, sigma_in, mu, T, i0, i1, *, omega_acoustic, gpu_tile=N
     return out
 
 
-def ladder_contract_sample(setup, J, T, i0, i1, *, omega_acoustic, gpu_tile=None):
-    """The shift-grid contraction of one ladder application for the outer states [i0, i1)."""
+def ladder_apply_sample(setup, J, sigma_T, mu, T, Omega, i0, i1, *, omega_acoustic, gpu_tile=None):
+    """apply_ladder_kernel! for the output states [i0, i1) only: LJ [nω, 4, 3, 2, i1 - i0], bitwise the
+    slice of the full application (a bounded sample at sizes the full application is too slow for)."""
     M = ModelArrays(setup)
     J = as_complex_F(J, (M.nw, 4, 3, 2, M.ni))
+    sT = as_complex_F(sigma_T, (M.nw, M.ni))
+    LJ = np.zeros((M.nw, 4, 3, 2, int(i1) - int(i0)), dtype=np.complex128, order="F")
     opts = _options(gpu_tile, omega_acoustic)
     buf, n = _msgbuf()
-    _check(lib().epsp_oracle_ladder_contract_sample(C.byref(M.struct), C.byref(opts), float(T), cptr(J), int(i0),
-                                                    int(i1), buf, n), buf)
+    _check(lib().epsp_oracle_ladder_apply_sample(C.byref(M.struct), C.byref(opts), cptr(sT), float(mu), float(T),
+                                                 float(Omega), cptr(J), int(i0), int(i1), cptr(LJ), buf, n), buf)
+    return LJ
+
+
+def ladder_chunks(setup, *, omega_acoustic, gpu_tile=None):
+    """The chunks of apply_ladder_kernel! (whole stars within CHUNK_BYTES, src/ladder.jl:180-202):
+    ([(i_lo, i_hi), ...], nshift)."""
+    M = ModelArrays(setup)
+    opts = _options(gpu_tile, omega_acoustic)
+    buf, n = _msgbuf()
+    cnt, ns = C.c_int64(), C.c_int64()
+    cap = M.ni + 1
+    lo, hi = (C.c_int64 * cap)(), (C.c_int64 * cap)()
+    _check(lib().epsp_oracle_ladder_chunks(C.byref(M.struct), C.byref(opts), C.byref(cnt), lo, hi, cap, C.byref(ns),
+                                           buf, n), buf)
+    return [(int(lo[c]), int(hi[c])) for c in range(cnt.value)], int(ns.value)
+
+
+def ladder_chunk_operands(setup, J, T, chunk, *, omega_acoustic, gpu_tile=None):
+    """One chunk's operands of C± += X± B̃ (src/ladder.jl:254-290): X+ and X- [16 nω, nk] and B̃
+    [nk, 6 ni] (Fortran order, nk = nshift·3·(i_hi - i_lo)), so that the product can run as a BLAS
+    DGEMM, as the reference's mul! does."""
+    M = ModelArrays(setup)
+    J = as_complex_F(J, (M.nw, 4, 3, 2, M.ni))
+    chunks, ns = ladder_chunks(setup, omega_acoustic=omega_acoustic, gpu_tile=gpu_tile)
+    i_lo, i_hi = chunks[int(chunk)]
+    nk = ns * 3 * (i_hi - i_lo)
+    Xp = np.empty((16 * M.nw, nk), order="F")
+    Xm = np.empty((16 * M.nw, nk), order="F")
+    Bt = np.empty((nk, 6 * M.ni), order="F")
+    opts = _options(gpu_tile, omega_acoustic)
+    buf, n = _msgbuf()
+    _check(lib().epsp_oracle_ladder_chunk_operands(C.byref(M.struct), C.byref(opts), float(T), cptr(J), int(chunk),
+                                                   ptr(Xp), ptr(Xm), ptr(Bt), buf, n), buf)
+    return Xp, Xm, Bt

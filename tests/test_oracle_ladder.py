@@ -248,3 +248,36 @@ def test_ladder_argument_checks(oracle, ccase):
             oracle.loop_ladder(c["setup"], c["sigma"], c["mu"], c["Tlist"], [0.0], **args)
     with pytest.raises(ArgumentError):
         oracle.loop_ladder(c["setup"], c["sigma"], c["mu"], c["Tlist"], [], omega_acoustic=W_AC)
+
+
+@pytest.mark.parametrize("tile", [None, 7])
+def test_apply_sample_is_the_full_slice(oracle, ccase, tile):
+    # the output-state range of one application (the bounded sample the full-size GPU parity tests
+    # compare against) is bitwise the slice of the full application, with one chunk or several
+    s = ccase["setup"]
+    w = s["omegas"].nodes()
+    nw, ni = len(w), s["eps_i"].size
+    J = R.pseudorandom_complex(nw, 4, 3, 2, ni, seed=2.1)
+    J[0] = 0
+    J[-1] = 0
+    args = (s, J, ccase["sigma"][:, :, 1], ccase["mu"][1], ccase["Tlist"][1], 0.09)
+    full = oracle.apply_ladder_kernel(*args, omega_acoustic=W_AC, gpu_tile=tile)
+    for i0, i1 in ((0, 2), (3, ni), (ni - 1, ni)):
+        part = oracle.ladder_apply_sample(*args, i0, i1, omega_acoustic=W_AC, gpu_tile=tile)
+        assert np.array_equal(part, full[..., i0:i1]), (i0, i1)
+
+
+def test_chunk_operands_cover_the_contraction(oracle, ccase):
+    # the CPU baseline times one chunk's C± += X± B̃ as a DGEMM: the chunks partition the outer
+    # states in order, and the operands have the shapes of src/ladder.jl:283-290
+    s = ccase["setup"]
+    nw, ni = len(s["omegas"]), s["eps_i"].size
+    chunks, ns = oracle.ladder_chunks(s, omega_acoustic=W_AC, gpu_tile=7)
+    assert len(chunks) > 1 and chunks[0][0] == 0 and chunks[-1][1] == ni
+    assert all(a[1] == b[0] for a, b in zip(chunks, chunks[1:]))
+    J = R.pseudorandom_complex(nw, 4, 3, 2, ni, seed=0.4)
+    for c in (0, len(chunks) - 1):
+        Xp, Xm, Bt = oracle.ladder_chunk_operands(s, J, ccase["Tlist"][0], c, omega_acoustic=W_AC, gpu_tile=7)
+        nk = ns * 3 * (chunks[c][1] - chunks[c][0])
+        assert Xp.shape == Xm.shape == (16 * nw, nk) and Bt.shape == (nk, 6 * ni)
+        assert np.all(np.isfinite(Xp @ Bt)) and np.linalg.norm(Bt) > 0 and not np.array_equal(Xp, Xm)
