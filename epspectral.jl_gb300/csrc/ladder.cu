@@ -65,9 +65,12 @@ struct LadderPlan {
   // GEMM paths: rows (j, q, c0, ri) with j padded to nwp (a multiple of 32), K = (ν, b, i') with ν
   // padded to nmp (a multiple of 16)
   long nwp = 0, nmp = 0;
-  long Kx = 0, Kp = 0, Kp2 = 0;
-  DBuf<int32_t> d_mt_k;          // [nwp, nmp, 2] first node p0 of the three nodes a mode's two shift tables read
-  DBuf<float> d_mt_w;            // [nwp, nmp, 2][4] the weights of p0, p0 + 1, p0 + 2 (tent weights folded in), 0
+  long Kx = 0, Kp2 = 0;
+  // tensor-core paths: the contraction Z = Jr Bz (M = 16 nwp rows (c12, c0, ri, p), N = nm 3ni
+  // columns (ν, a, i), K = 3ni pairs (b, i') padded to Kzp), then D from Z by zgather_kernel
+  long Mz = 0, Nz = 0, Kz = 0, Kzp = 0;
+  DBuf<int32_t> d_zt_k;          // [nm, 2, nwp] first node p0 of the three nodes a mode's two shift tables read
+  DBuf<float> d_zt_w;            // [nm, 2, nwp][4] the weights of p0, p0 + 1, p0 + 2 (tent weights folded in), 0
   DBuf<float> d_nnu_f;
   DBuf<__nv_bfloat16> d_KKh, d_KKl, d_Yh, d_Yl;
   DBuf<float> d_part2;
@@ -76,13 +79,15 @@ struct LadderPlan {
   DBuf<double> d_Gt, d_Af, d_D;   // G̃ [Kx, 3ni]; A (FP64) [24nω, Kx]; D [24nω, 3ni]
   DBuf<int32_t> d_mnu;
   DBuf<double> d_rnu, d_nnu;
-  DBuf<__nv_bfloat16> d_Ah, d_Al, d_Gh, d_Gl;
-  DBuf<float> d_At, d_Gtf;  // GEMM_TF32: A and G̃ as TF32-rounded FP32, rows of Kp
-  DBuf<float> d_part;
+  DBuf<__nv_bfloat16> d_Jh, d_Jl, d_Bzh, d_Bzl;  // GEMM_BF16: Jr and Bz as BF16 hi/lo rows of Kzp
+  DBuf<float> d_Jt, d_Bzt;                        // GEMM_TF32: the same as TF32-rounded FP32
+  DBuf<float> d_Z, d_Dz;  // Z (split-K partials, zsplit_cap of them at most) [Mz, Nz]; D [24 nwp, 3ni]
+  int zsplit_cap = 1;
   DBuf<int> d_err;
   TcOperand opA{}, opG{}, opA64{}, opG128{}, opG256{}, opA32{}, opG256_32{};
   int bn = 128, splits = 1, bk = kTcBK;  // the contraction's tile shape, picked by the autotuner at setup
   bool persist = false;                  // ... and whether it runs as the persistent kernel
+  int gm = 1;                            // ... in launch order (1) or grouped tile order
   bool pair = false;                     // ... or as the CTA-pair kernel (cta_group::2)
   std::vector<TcTune> tune_all;
   float tune_ms_heuristic = 0.f;
@@ -587,194 +592,233 @@ __global__ void xgen_f64_kernel(const double2* __restrict__ J, const int32_t* __
   A[idx] = (j < nw && nu < nm) ? xgen_value(J, klo, wlo, whi, nw, ns, j, q, c0, ri, mnu[nu], rnu[nu], nnu[nu], b, ip) : 0.0;
 }
 
-// BF16 hi/lo A operand, row-major [24 nwp][Kp], FP32 arithmetic; row (q, c0, re/im) nwp + j. The
-// six row combinations q read four vertex components c12 (q 0, 1: 11; q 2, 3: 22; q 4: 21; q 5:
-// 12), so a block owns 32 nodes j (nwp is a multiple of 32) of one component (c12, c0) and makes
-// every row group that reads it: both q of the component and both re/im parts (4 or 2 row groups)
-// from one staged copy of the vertex and one evaluation of the shifted sums X+, X-. Per K-tile (64
-// columns = 4 pairs (b, i') x 16 modes) it stages the window of the vertex the shift tables of its
-// nodes can reach (nodes j0 - W .. j0 + 32 + W, W = nshift + 2, zero outside the grid) in shared
-// memory; each thread holds the mode-table entries it needs (two shift tables per mode and sign,
-// with the tent weights folded in) in registers. Tiles are transposed through shared memory so
-// that the BF16 rows are written 16 bytes at a time. With kTf32 the operand is one FP32 matrix At
-// of TF32-rounded values (the same 4 bytes per element) instead of the BF16 hi/lo pair.
-constexpr int kXgTiles = 8;
-constexpr int kXgPreMax = 8;  // prefetch slots per thread: windows of up to 4 x 512 values (nshift <= 222)
+// ---- the tensor-core contraction, interpolation after the product ----
+// The shift interpolation of the regrouped sums acts on the frequency axis only, with weights that
+// depend on (j, ν, sign) and not on the pair (b, i'), so it commutes with the contraction over the
+// pairs:
+//   Z_ν[(c12, c0, ri, p), (a, i)] = Σ_{b, i'} Jr[(c12, c0, ri, p), (b, i')] G̃[(ν, b, i'), (a, i)]
+//   D[(q, c0, ri, j), (a, i)] = Σ_ν Σ_s c_q(ν, s) Σ_t w_{ν,s,t}(j) Z_ν[(c12(q), c0, ri, p_{ν,s}(j) + t), (a, i)]
+// with Jr the vertex's re/im parts as rows. One product for all modes (N = nm 3ni columns (ν, a, i),
+// K = 3ni) replaces the per-mode A operand (K = 16 3ni, 24 rows per node instead of 16): 0.62 of
+// the tensor-core work, and the operand written and read back is Z instead of A (1.8 GB against
+// 2.9 GB at 1251 nodes and 495 outer states). The channel combinations c_q (q = 0..5 on the
+// components c12 = 11, 11, 22, 22, 21, 12) and the three taps of each mode and sign are applied by
+// zgather_kernel; D's layout is the one the Kramers-Kronig and channel kernels read.
 
-// Batched over blockIdx.z: slot z makes the rows z 24 nwp.. of A from the vertex J + jstride r and
-// the occupations nnu + 16 r of right-hand side r = rmap[z] (r = z without rmap).
-template <int kXgPre, bool kTf32>
-__global__ void __launch_bounds__(256) xgen_bf16_kernel(const float2* __restrict__ J_all, long jstride,
-                                                        const int* __restrict__ rmap, const int32_t* __restrict__ mt_k,
-                                                        const float* __restrict__ mt_w, const float* __restrict__ nnu_all,
-                                                        int nw, int nwp, int ns, int nmp, int ni, long Kx, long Kp,
-                                                        __nv_bfloat16* __restrict__ Ah, __nv_bfloat16* __restrict__ Al,
-                                                        float* __restrict__ At) {
-  extern __shared__ float xg_smem[];
-  const int rhs = rmap ? rmap[blockIdx.z] : int(blockIdx.z);
+// Jr rows z 16 nwp + ((ri 2 + c0) 4 + c12) nwp + p, K-major with row stride Kzp (columns k = b + 3i',
+// zero for p >= nω and k >= 3ni), from the vertex of right-hand side rmap[z] (z without rmap), FP32
+// complex [nω, 4, 3, 2, ni] jstride apart: TF32-rounded (kTf32) or split into BF16 hi/lo. A block
+// transposes a tile of 32 nodes x 32 pairs of one (c12, c0) through shared memory, reading node
+// runs and writing 128-byte row segments. Grid (Kzp / 32, nwp / 32, 8 slots).
+template <bool kTf32>
+__global__ void __launch_bounds__(256) jmat_kernel(const float2* __restrict__ J_all, long jstride, const int* __restrict__ rmap,
+                                                   int nw, int nwp, int ni, long Kzp, float* __restrict__ Jt,
+                                                   __nv_bfloat16* __restrict__ Jh, __nv_bfloat16* __restrict__ Jl) {
+  __shared__ float2 tile[32][33];
+  const int k0 = blockIdx.x * 32, p0 = blockIdx.y * 32;
+  const int comp = blockIdx.z % 8, z = blockIdx.z / 8;
+  const int c12 = comp % 4, c0 = comp / 4;
+  const int rhs = rmap ? rmap[z] : z;
   const float2* J = J_all + jstride * rhs;
-  const float* nnu = nnu_all + 16 * rhs;
-  const long row_base = long(blockIdx.z) * 24 * nwp;
-  const int W = ns + 2, win = 32 + 2 * W;
-  float2* s_jbuf = reinterpret_cast<float2*>(xg_smem);                               // [2][4][win] (re, im)
-  float (*tile)[64][33] = reinterpret_cast<float (*)[64][33]>(s_jbuf + 8 * win);    // [4][64][33]
-  const int nblk = nwp / 32;
-  const int j0 = (blockIdx.x % nblk) * 32, comp = blockIdx.x / nblk;
-  const int cc = comp % 4, c0 = comp / 4;
-  const int c12 = cc == 0 ? 0 : (cc == 1 ? 3 : (cc == 2 ? 1 : 2));
-  const int nq = cc < 2 ? 2 : 1;            // row combinations q reading this component
-  const int qbase = cc < 2 ? 2 * cc : cc + 2;  // 0, 2, 4, 5
-  const int tr = threadIdx.x % 32, tk = threadIdx.x / 32;
-  const int j = j0 + tr;
-  int ka[2][2];
-  float w[2][2][3], nB[2];
+  const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+  const long Kz = 3l * ni;
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int nu = tk + 8 * h;
-    nB[h] = nnu[nu];
-#pragma unroll
-    for (int sg = 0; sg < 2; ++sg) {
-      const long g = (long(j) * nmp + nu) * 2 + sg;  // [j][nu][s] with nmp == 16 per K-group
-      ka[h][sg] = mt_k[g] - (j0 - W);
-      const float4 wv = reinterpret_cast<const float4*>(mt_w)[g];
-      w[h][sg][0] = wv.x;
-      w[h][sg][1] = wv.y;
-      w[h][sg][2] = wv.z;
-    }
+  for (int r = 0; r < 4; ++r) {  // pair k0 + ty + 8 r, node p0 + tx
+    const long k = k0 + ty + 8 * r;
+    const int p = p0 + tx;
+    float2 v = make_float2(0.f, 0.f);
+    if (k < Kz && p < nw) v = J[jidx(nw, p, c12, int(k % 3), c0, k / 3)];
+    tile[ty + 8 * r][tx] = v;
   }
-  const long kt0 = long(blockIdx.y) * kXgTiles;
-  // The vertex window of the 4 pairs (b, i') of a K-tile (4 win <= 256 kXgPre values, chosen at
-  // launch) is loaded into registers one K-tile ahead and stored into the other half of a double
-  // buffer, so its global latency hides behind the current K-tile's arithmetic.
-  float2 pre[kXgPre];
-  auto load_window = [&](long k0) {
+  __syncthreads();
 #pragma unroll
-    for (int q = 0; q < kXgPre; ++q) {
-      const int e = threadIdx.x + 256 * q;
-      float2 v = make_float2(0.f, 0.f);
-      if (e < 4 * win && k0 < Kp) {
-        const int g = e / win, node = j0 - W + e % win;
-        const long pair = (k0 / 16) + g;  // (b, i') index = k / 16
-        if (node >= 0 && node < nw && pair < 3l * ni) {
-          const int b = int(pair % 3);
-          const long ip = pair / 3;
-          v = J[jidx(nw, node, c12, b, c0, ip)];
-        }
-      }
-      pre[q] = v;
-    }
-  };
-  auto store_window = [&](float2* dst) {
-#pragma unroll
-    for (int q = 0; q < kXgPre; ++q) {
-      const int e = threadIdx.x + 256 * q;
-      if (e < 4 * win) dst[e] = pre[q];
-    }
-  };
-  load_window(kt0 * 64);
-  store_window(s_jbuf);
-  for (int kt = 0; kt < kXgTiles; ++kt) {
-    const long k0 = (kt0 + kt) * 64;
-    if (k0 >= Kp) break;
-    float2* s_j = s_jbuf + (kt & 1) * 4 * win;
-    __syncthreads();  // s_j complete; the previous K-tile's rows are written out
-    if (kt + 1 < kXgTiles) load_window(k0 + 64);
-#pragma unroll
-    for (int p = 0; p < 8; ++p) {
-      const int h = p & 1, g = p >> 1;
-      const int kl = tk + 8 * p;  // 0..63: pair g, mode tk + 8 h
-      const long k = k0 + kl;
-      float2 xs[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-      if (j < nw && k < Kx) {
-        const float2* jw = s_j + g * win;
-#pragma unroll
-        for (int sg = 0; sg < 2; ++sg) {
-          const float2 u0 = jw[ka[h][sg]], u1 = jw[ka[h][sg] + 1], u2 = jw[ka[h][sg] + 2];
-          xs[sg].x = w[h][sg][0] * u0.x + w[h][sg][1] * u1.x + w[h][sg][2] * u2.x;
-          xs[sg].y = w[h][sg][0] * u0.y + w[h][sg][1] * u1.y + w[h][sg][2] * u2.y;
-        }
-      }
-      const float n = nB[h];
-      if (cc < 2) {
-        // q even: ½(X+ - X-); q odd: -(½ + n)(X+ + X-)
-        tile[0][kl][tr] = 0.5f * (xs[0].x - xs[1].x);
-        tile[1][kl][tr] = 0.5f * (xs[0].y - xs[1].y);
-        tile[2][kl][tr] = -(0.5f + n) * (xs[0].x + xs[1].x);
-        tile[3][kl][tr] = -(0.5f + n) * (xs[0].y + xs[1].y);
-      } else if (cc == 2) {
-        tile[0][kl][tr] = n * xs[0].x + (1.f + n) * xs[1].x;
-        tile[1][kl][tr] = n * xs[0].y + (1.f + n) * xs[1].y;
-      } else {
-        tile[0][kl][tr] = (1.f + n) * xs[0].x + n * xs[1].x;
-        tile[1][kl][tr] = (1.f + n) * xs[0].y + n * xs[1].y;
-      }
-    }
-    __syncthreads();
-    // write-out: a warp takes 4 rows x 8 column chunks of 8, i.e. whole 128-byte row segments (an
-    // 8 x 4 split of the warp avoids the 2-way bank conflicts of the transposed reads but writes
-    // 64-byte segments, and measured slower)
-    const int wr = threadIdx.x / 8, kc = (threadIdx.x % 8) * 8;
+  for (int r = 0; r < 8; ++r) {  // row (ri, node p0 + ty + 4 (r % 4)... ): 8 rows of 32 columns per pass
+    const int pl = ty + 8 * (r % 4), ri = r / 4;
+    const float2 v = tile[tx][pl];
+    const float x = ri ? v.y : v.x;
+    const long row = long(z) * 16 * nwp + long((ri * 2 + c0) * 4 + c12) * nwp + p0 + pl;
+    const long off = row * Kzp + k0 + tx;
     if constexpr (kTf32) {
-      // FP32 rows: 8 lanes cover 128 contiguous bytes per store (columns kq.. and 32 + kq..); the
-      // transposed reads are conflict-free in this order
-      const int kq = (threadIdx.x % 8) * 4;
-      for (int t4 = 0; t4 < 2 * nq; ++t4) {
-        const int q = qbase + t4 / 2, ri = t4 % 2;
-        const float4 lo = make_float4(round_tf32(tile[t4][kq][wr]), round_tf32(tile[t4][kq + 1][wr]),
-                                      round_tf32(tile[t4][kq + 2][wr]), round_tf32(tile[t4][kq + 3][wr]));
-        const float4 hi = make_float4(round_tf32(tile[t4][32 + kq][wr]), round_tf32(tile[t4][33 + kq][wr]),
-                                      round_tf32(tile[t4][34 + kq][wr]), round_tf32(tile[t4][35 + kq][wr]));
-        const long row = row_base + long(q + 6 * (c0 + 2 * ri)) * nwp + j0 + wr;
-        const long off = row * Kp + k0 + kq;
-        *reinterpret_cast<float4*>(At + off) = lo;
-        *reinterpret_cast<float4*>(At + off + 32) = hi;
-      }
-    } else
-    for (int t4 = 0; t4 < 2 * nq; ++t4) {
-      const int q = qbase + t4 / 2, ri = t4 % 2;
-      __align__(16) __nv_bfloat16 hh[8], ll[8];
-#pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        const float x = tile[t4][kc + t][wr];
-        hh[t] = __float2bfloat16_rn(x);
-        ll[t] = __float2bfloat16_rn(x - __bfloat162float(hh[t]));
-      }
-      const long row = row_base + long(q + 6 * (c0 + 2 * ri)) * nwp + j0 + wr;
-      const long off = row * Kp + k0 + kc;
-      *reinterpret_cast<uint4*>(Ah + off) = *reinterpret_cast<const uint4*>(hh);
-      *reinterpret_cast<uint4*>(Al + off) = *reinterpret_cast<const uint4*>(ll);
+      Jt[off] = round_tf32(x);
+    } else {
+      const __nv_bfloat16 h = __float2bfloat16_rn(x);
+      Jh[off] = h;
+      Jl[off] = __float2bfloat16_rn(x - __bfloat162float(h));
     }
-    // the next window goes to the other buffer (its readers finished at the barrier above); the
-    // barrier at the top of the next K-tile publishes it and retires this K-tile's tiles
-    if (kt + 1 < kXgTiles) store_window(s_jbuf + ((kt + 1) & 1) * 4 * win);
   }
 }
 
-static int xgen_pre(long ns) {
-  const long v = 4 * (32 + 2 * (ns + 2));
-  return v <= 512 ? 2 : (v <= 1024 ? 4 : 8);
+// The contraction's B operand: rows (ν, a, i) = ν 3ni + n, K-major with row stride Kzp, from G̃
+// [Kx, 3ni] column-major (rows k = ν + nmp (b + 3i')): TF32-rounded (Bt) or BF16 hi/lo (Bh, Bl).
+__global__ void bz_build_kernel(const double* __restrict__ Gt, long Kx, int nmp, int nm, long N, long Kzp,
+                                float* __restrict__ Bt, __nv_bfloat16* __restrict__ Bh, __nv_bfloat16* __restrict__ Bl) {
+  const long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= long(nm) * N * Kzp) return;
+  const long row = idx / Kzp, k = idx % Kzp;
+  const long nu = row / N, n = row % N;
+  const float x = k < N ? float(Gt[nu + nmp * k + Kx * n]) : 0.f;  // k < 3ni = N
+  if (Bt) {
+    Bt[idx] = round_tf32(x);
+  } else {
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    Bh[idx] = h;
+    Bl[idx] = __float2bfloat16_rn(x - __bfloat162float(h));
+  }
 }
 
-// xgen_bf16_kernel with the fewest prefetch slots that hold the window.
-template <bool kTf32, class... A>
-static void launch_xgen_t(long ns, dim3 grid, size_t smem, cudaStream_t s, A... args) {
-  switch (xgen_pre(ns)) {
-    case 2: xgen_bf16_kernel<2, kTf32><<<grid, 256, smem, s>>>(args...); break;
-    case 4: xgen_bf16_kernel<4, kTf32><<<grid, 256, smem, s>>>(args...); break;
-    default: xgen_bf16_kernel<8, kTf32><<<grid, 256, smem, s>>>(args...); break;
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// D from Z (the formula above), FP32, modes in ascending order, both signs and three taps each.
+// Z: [Mz, nm N] column-major (ld ldZ) as zsplits split-K partials zstride apart (summed in
+// ascending order as they are staged); rows of slot z at z 16 nwp. zt_k [nm][2][nwp] first tap
+// node p_{ν,s}(j), zt_w [nm][2][nwp] its three weights (tent split folded in); nnu_all 16 Bose
+// occupations per right-hand side (rmap[z], or z). D[z 24 nwp + (q + 6 (c0 + 2 ri)) nwp + j + ldD n],
+// rows j < nω. Grid (N / NC, 4 (c0, ri), slots), blockDim = nodes / U rounded up to warps: a block
+// owns NC columns n of one (c0, ri) and every node; per mode it stages the four components' Z
+// columns (asynchronous copies, double-buffered over ν) and each thread accumulates U nodes.
+template <int U, int NC>
+__global__ void zgather_kernel(const float* __restrict__ Z, long ldZ, int zsplits, long zstride,
+                               const int32_t* __restrict__ zt_k, const float4* __restrict__ zt_w,
+                               const float* __restrict__ nnu_all, const int* __restrict__ rmap, int nw, int nwp, int nm,
+                               long N, float* __restrict__ D, long ldD) {
+  extern __shared__ __align__(16) float zs[];  // [2][NC][4][nwp + 4]
+  const int stride = nwp + 4;
+  const long n0 = long(blockIdx.x) * NC;
+  const int c0 = blockIdx.y & 1, ri = blockIdx.y >> 1;
+  const long z = blockIdx.z;
+  const int rhs = rmap ? rmap[z] : int(z);
+  const float* nnu = nnu_all + 16 * rhs;
+  const float* zb = Z + z * 16 * nwp + long((ri * 2 + c0) * 4) * nwp;  // the 4 components, contiguous
+  const int nthr = blockDim.x;
+  for (int e = threadIdx.x; e < 2 * NC * 4 * 4; e += nthr) zs[(e / 4) * stride + nwp + e % 4] = 0.f;  // tap pads
+  const int nv = nwp / 4;  // float4 chunks per component column
+  auto stage = [&](int nu, int buf) {
+    for (int c = 0; c < NC; ++c) {
+      const long n = n0 + c;
+      if (n >= N) break;
+      float* dst = zs + long((buf * NC + c) * 4) * stride;
+      const float* src = zb + ldZ * (long(nu) * N + n);
+      if (zsplits == 1) {
+        for (int e = threadIdx.x; e < 4 * nv; e += nthr) {
+          const int comp = e / nv, p4 = e % nv;
+          cp_async16(dst + comp * stride + 4 * p4, src + long(comp) * nwp + 4 * p4);
+        }
+      } else {  // split-K partials: summed here in ascending order (synchronous loads)
+        for (int e = threadIdx.x; e < 4 * nwp; e += nthr) {
+          const int comp = e / nwp, p = e % nwp;
+          float acc = 0.f;
+          for (int sp = 0; sp < zsplits; ++sp) acc += src[long(comp) * nwp + p + zstride * sp];
+          dst[comp * stride + p] = acc;
+        }
+      }
+    }
+    cp_async_commit();
+  };
+  float acc[NC][U][6];
+#pragma unroll
+  for (int c = 0; c < NC; ++c)
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int q = 0; q < 6; ++q) acc[c][u][q] = 0.f;
+  stage(0, 0);
+  for (int nu = 0; nu < nm; ++nu) {
+    cp_async_wait_all();
+    __syncthreads();  // mode nu's columns are in buffer nu & 1; buffer (nu + 1) & 1 is free
+    if (nu + 1 < nm) stage(nu + 1, (nu + 1) & 1);
+    const float nb = nnu[nu];
+    const float hp = 0.5f + nb;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int j = threadIdx.x + nthr * u;
+      if (j >= nw) continue;
+      int pk[2];
+      float4 wv[2];
+#pragma unroll
+      for (int sg = 0; sg < 2; ++sg) {
+        const long e = (long(nu) * 2 + sg) * nwp + j;
+        pk[sg] = zt_k[e];
+        wv[sg] = zt_w[e];
+      }
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const float* zc = zs + long(((nu & 1) * NC + c) * 4) * stride;
+        float x[2][4];
+#pragma unroll
+        for (int sg = 0; sg < 2; ++sg)
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) {
+            const float* r = zc + cc * stride + pk[sg];
+            x[sg][cc] = wv[sg].x * r[0] + wv[sg].y * r[1] + wv[sg].z * r[2];
+          }
+        // components c12 = 0 (11), 1 (21), 2 (12), 3 (22)
+        acc[c][u][0] += 0.5f * (x[0][0] - x[1][0]);
+        acc[c][u][1] += -hp * (x[0][0] + x[1][0]);
+        acc[c][u][2] += 0.5f * (x[0][3] - x[1][3]);
+        acc[c][u][3] += -hp * (x[0][3] + x[1][3]);
+        acc[c][u][4] += nb * x[0][1] + (1.f + nb) * x[1][1];
+        acc[c][u][5] += (1.f + nb) * x[0][2] + nb * x[1][2];
+      }
+    }
   }
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const long n = n0 + c;
+    if (n >= N) break;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int j = threadIdx.x + nthr * u;
+      if (j >= nw) continue;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) D[z * 24 * nwp + long(q + 6 * (c0 + 2 * ri)) * nwp + j + ldD * n] = acc[c][u][q];
+    }
+  }
+}
+
+// Group size (M tiles) of the contraction's grouped tile order: 8 tiles of 128 rows of Jr.
+constexpr int kZGroupM = 8;
+
+// zgather_kernel's launch shape: U nodes per thread (4 up to 4096 nodes, else 8), NC columns per
+// block (2 while the double-buffered staging of two columns fits 110 KB, else 1).
+struct ZgatherShape {
+  int U = 4, NC = 2, threads = 0;
+  size_t smem = 0;
+};
+static ZgatherShape zgather_shape(long nw, long nwp) {
+  ZgatherShape g;
+  g.U = nw <= 4096 ? 4 : 8;
+  if (nw > 8192) fail(EPSP_EUNSUPPORTED, "the tensor-core ladder paths take at most 8192 frequency nodes");
+  g.threads = int((nw + g.U - 1) / g.U + 31) / 32 * 32;
+  const size_t per_col = size_t(2 * 4 * (nwp + 4)) * sizeof(float);
+  g.NC = per_col * 2 <= (size_t(110) << 10) ? 2 : 1;
+  g.smem = per_col * size_t(g.NC);
+  return g;
 }
 template <class... A>
-static void launch_xgen(bool tf32, long ns, dim3 grid, size_t smem, cudaStream_t s, A... args) {
-  if (tf32)
-    launch_xgen_t<true>(ns, grid, smem, s, args...);
+static void launch_zgather(const ZgatherShape& g, dim3 grid, cudaStream_t s, A... args) {
+  static size_t smem_set[4] = {0, 0, 0, 0};  // the largest dynamic shared memory allowed so far, per instantiation
+  const int v = (g.U == 4 ? 0 : 2) + (g.NC == 2 ? 0 : 1);
+  if (g.smem > smem_set[v]) {
+    switch (v) {
+      case 0: EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem))); break;
+      case 1: EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem))); break;
+      case 2: EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem))); break;
+      default: EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem))); break;
+    }
+    smem_set[v] = g.smem;
+  }
+  if (g.U == 4 && g.NC == 2)
+    zgather_kernel<4, 2><<<grid, g.threads, g.smem, s>>>(args...);
+  else if (g.U == 4)
+    zgather_kernel<4, 1><<<grid, g.threads, g.smem, s>>>(args...);
+  else if (g.NC == 2)
+    zgather_kernel<8, 2><<<grid, g.threads, g.smem, s>>>(args...);
   else
-    launch_xgen_t<false>(ns, grid, smem, s, args...);
-}
-
-static size_t xgen_smem_bytes(int ns) {
-  const int W = ns + 2, win = 32 + 2 * W;
-  return size_t(8 * win) * sizeof(float2) + size_t(4 * 64 * 33) * 4;
+    zgather_kernel<8, 1><<<grid, g.threads, g.smem, s>>>(args...);
 }
 
 // Y (rows q = 0, 2 of D) as the BF16 hi/lo B operand of the Kramers-Kronig GEMM: row (qq, c0, ri, n),
@@ -808,27 +852,6 @@ __global__ void y_split_kernel(const float* __restrict__ D, long ldD, int dsplit
     Yh[o] = h;
     Yl[o] = __float2bfloat16_rn(x[r8] - __bfloat162float(h));
   }
-}
-
-__global__ void split_rows_plain_kernel(const double* __restrict__ S, long rows, long cols, long ld, long Kp,
-                                        __nv_bfloat16* __restrict__ oh, __nv_bfloat16* __restrict__ ol) {
-  // out[r * Kp + c] = split(S[c + ld r]) (a column-major [cols, rows] matrix read row by row).
-  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= rows * Kp) return;
-  long r = idx / Kp, c = idx % Kp;
-  float x = c < cols ? float(S[c + ld * r]) : 0.f;
-  __nv_bfloat16 h = __float2bfloat16_rn(x);
-  oh[idx] = h;
-  ol[idx] = __float2bfloat16_rn(x - __bfloat162float(h));
-}
-
-// out[r * Kp + c] = S[c + ld r] rounded to TF32 (0 past cols): the TF32 form of split_rows_plain.
-__global__ void round_rows_tf32_kernel(const double* __restrict__ S, long rows, long cols, long ld, long Kp,
-                                       float* __restrict__ out) {
-  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= rows * Kp) return;
-  long r = idx / Kp, c = idx % Kp;
-  out[idx] = c < cols ? round_tf32(float(S[c + ld * r])) : 0.f;
 }
 
 // out[r * Kp + c] = split(S[r + ldr c]) for c < cols (a column-major matrix read by rows).
@@ -1420,8 +1443,8 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       // three weights per entry (the fourth weight slot is zero).
       {
         const long nwp = P->nwp;
-        std::vector<int32_t> hk(size_t(nwp * 16 * 2));
-        std::vector<float> hw(size_t(nwp * 16 * 2 * 4), 0.f);
+        std::vector<int32_t> hk(size_t(nwp * nm * 2));
+        std::vector<float> hw(size_t(nwp * nm * 2 * 4), 0.f);
         std::vector<int32_t> klo(size_t(nw * ns * 2));
         std::vector<double> wlo(klo.size()), whi(klo.size());
         P->d_klo.download(klo.data(), klo.size(), s);
@@ -1429,11 +1452,11 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
         P->d_whi.download(whi.data(), whi.size(), s);
         EPSP_CUDA(cudaStreamSynchronize(s));
         for (long j = 0; j < nwp; ++j)
-          for (long nu = 0; nu < 16; ++nu)
+          for (long nu = 0; nu < nm; ++nu)
             for (long sg = 0; sg < 2; ++sg) {
-              const size_t e = size_t((j * 16 + nu) * 2 + sg);
-              hk[e] = int32_t(j);
-              if (j >= nw || nu >= nm || P->wnu[size_t(nu)] < P->w_ac) continue;
+              const size_t e = size_t((nu * 2 + sg) * nwp + j);  // [ν][s][j]: consecutive nodes adjacent
+              hk[e] = int32_t(j);  // zero weights; the taps j.. j + 2 stay inside the staged rows and pads
+              if (j >= nw || P->wnu[size_t(nu)] < P->w_ac) continue;
               const long mm = P->m_nu[size_t(nu)];
               const double r = P->r_nu[size_t(nu)];
               const size_t t0 = size_t(j + nw * (mm + ns * sg));
@@ -1456,59 +1479,71 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
               hk[e] = int32_t(p0);
               for (int t = 0; t < 3; ++t) hw[4 * e + size_t(t)] = float(cw[t]);
             }
-        P->d_mt_k = to_device(ctx, hk);
-        P->d_mt_w = to_device(ctx, hw);
+        P->d_zt_k = to_device(ctx, hk);
+        P->d_zt_w = to_device(ctx, hw);
       }
-      P->Kp = (P->Kx + 63) / 64 * 64;
       P->Kp2 = (nw + 63) / 64 * 64;
       const bool tf = P->path == EPSP_PATH_GEMM_TF32;
+      // the contraction Z = Jr Bz: Jr [16 nwp][Kzp] (written per application), Bz [nm 3ni][Kzp] from G̃
+      P->Mz = 16 * P->nwp;
+      P->Nz = nm * N;
+      P->Kz = N;
+      P->Kzp = (P->Kz + 63) / 64 * 64;
+      const size_t nB = size_t(P->Nz * P->Kzp);
       if (tf) {
-        P->d_At.alloc(ctx, size_t(M * P->Kp));
-        P->d_Gtf.alloc(ctx, size_t(N * P->Kp));
-        round_rows_tf32_kernel<<<div_up(size_t(N * P->Kp), 256), 256, 0, s>>>(P->d_Gt.p, N, P->Kx, P->Kx, P->Kp,
-                                                                               P->d_Gtf.p);
+        P->d_Jt.alloc(ctx, size_t(P->Mz * P->Kzp));
+        P->d_Bzt.alloc(ctx, nB);
+        bz_build_kernel<<<div_up(nB, 256), 256, 0, s>>>(P->d_Gt.p, P->Kx, int(P->nmp), int(nm), N, P->Kzp, P->d_Bzt.p,
+                                                        nullptr, nullptr);
       } else {
-        P->d_Ah.alloc(ctx, size_t(M * P->Kp));
-        P->d_Al.alloc(ctx, size_t(M * P->Kp));
-        P->d_Gh.alloc(ctx, size_t(N * P->Kp));
-        P->d_Gl.alloc(ctx, size_t(N * P->Kp));
-        split_rows_plain_kernel<<<div_up(size_t(N * P->Kp), 256), 256, 0, s>>>(P->d_Gt.p, N, P->Kx, P->Kx, P->Kp,
-                                                                                P->d_Gh.p, P->d_Gl.p);
+        P->d_Jh.alloc(ctx, size_t(P->Mz * P->Kzp));
+        P->d_Jl.alloc(ctx, size_t(P->Mz * P->Kzp));
+        P->d_Bzh.alloc(ctx, nB);
+        P->d_Bzl.alloc(ctx, nB);
+        bz_build_kernel<<<div_up(nB, 256), 256, 0, s>>>(P->d_Gt.p, P->Kx, int(P->nmp), int(nm), N, P->Kzp, nullptr,
+                                                        P->d_Bzh.p, P->d_Bzl.p);
       }
       EPSP_LAUNCHED(ctx);
       plog.mark("mode tables, operand buffers");
-      // the contraction's tile shape: the autotuner times the candidates on these operands (A
-      // zeroed) and keeps the fastest; the partial buffer holds the largest split count tried
+      // the contraction's tile shape: the autotuner times the candidates on these operands (Jr
+      // zeroed), in launch order and in grouped order (Bz, nm 3ni rows, is too large to stay in L2
+      // across the M tiles), and keeps the fastest. Z holds two split-K partials while that costs
+      // at most 512 MB, else one.
+      const size_t zbytes = size_t(P->Mz) * size_t(P->Nz) * sizeof(float);
+      P->zsplit_cap = zbytes * 2 <= (size_t(512) << 20) ? 2 : 1;
+      const int Mi = int(P->Mz), Ni = int(P->Nz), Ki = int(P->Kz);
       int bn_h = 128, sp_h = 1;
-      tc_gemm_shape(ctx, int(M), int(N), int(P->Kx), 16, 2, &bn_h, &sp_h);
-      const int max_sp = 2 * std::max(tc_splits_for(ctx, int(M), int(N), int(P->Kx), 128),
-                                       tc_splits_for(ctx, int(M), int(N), int(P->Kx), 256));
-      P->d_part.alloc(ctx, size_t(max_sp) * size_t(M * N));
+      tc_gemm_shape(ctx, Mi, Ni, Ki, P->zsplit_cap, 2, &bn_h, &sp_h);
+      P->d_Z.alloc(ctx, size_t(P->zsplit_cap) * size_t(P->Mz * P->Nz));
+      P->d_Dz.alloc(ctx, size_t(M * N));
       P->d_err.alloc(ctx, 1);
       P->d_err.zero(s);
       if (tf) {  // one TF32 map per operand, K boxes of 32 (128 bytes); opA32 / opG256_32 alias them
-        P->d_At.zero(s);
-        P->opA64 = P->opA32 = one_part_tf32(P->d_At.p, M, P->Kx, P->Kp, kTcBM);
-        P->opG128 = one_part_tf32(P->d_Gtf.p, N, P->Kx, P->Kp, 128);
-        P->opG256 = P->opG256_32 = one_part_tf32(P->d_Gtf.p, N, P->Kx, P->Kp, 256);
+        P->d_Jt.zero(s);
+        P->opA64 = P->opA32 = one_part_tf32(P->d_Jt.p, P->Mz, P->Kz, P->Kzp, kTcBM);
+        P->opG128 = one_part_tf32(P->d_Bzt.p, P->Nz, P->Kz, P->Kzp, 128);
+        P->opG256 = P->opG256_32 = one_part_tf32(P->d_Bzt.p, P->Nz, P->Kz, P->Kzp, 256);
       } else {
-        P->d_Ah.zero(s);
-        P->d_Al.zero(s);
-        P->opA64 = two_part(P->d_Ah.p, P->d_Al.p, M, P->Kx, P->Kp, kTcBM);
-        P->opG128 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 128);
-        P->opG256 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 256);
-        P->opA32 = two_part(P->d_Ah.p, P->d_Al.p, M, P->Kx, P->Kp, kTcBM, 32);
-        P->opG256_32 = two_part(P->d_Gh.p, P->d_Gl.p, N, P->Kx, P->Kp, 256, 32);
+        P->d_Jh.zero(s);
+        P->d_Jl.zero(s);
+        P->opA64 = two_part(P->d_Jh.p, P->d_Jl.p, P->Mz, P->Kz, P->Kzp, kTcBM);
+        P->opG128 = two_part(P->d_Bzh.p, P->d_Bzl.p, P->Nz, P->Kz, P->Kzp, 128);
+        P->opG256 = two_part(P->d_Bzh.p, P->d_Bzl.p, P->Nz, P->Kz, P->Kzp, 256);
+        P->opA32 = two_part(P->d_Jh.p, P->d_Jl.p, P->Mz, P->Kz, P->Kzp, kTcBM, 32);
+        P->opG256_32 = two_part(P->d_Bzh.p, P->d_Bzl.p, P->Nz, P->Kz, P->Kzp, 256, 32);
       }
-      const TcTune best = tc_gemm_autotune(ctx, P->opA64, P->opG128, P->opG256, int(M), int(N), int(P->Kx), P->d_part.p,
-                                           M, M * N, max_sp, P->d_err.p, 3, &P->tune_all, &P->opA32, &P->opG256_32);
+      const TcTune best = tc_gemm_autotune(ctx, P->opA64, P->opG128, P->opG256, Mi, Ni, Ki, P->d_Z.p, P->Mz,
+                                           P->Mz * P->Nz, P->zsplit_cap, P->d_err.p, 3, &P->tune_all, &P->opA32,
+                                           &P->opG256_32, kZGroupM);
       for (const auto& c : P->tune_all)
-        if (c.bn == bn_h && c.splits == sp_h && c.bk == (tf ? 32 : kTcBK) && !c.persist) P->tune_ms_heuristic = c.ms;
+        if (c.bn == bn_h && c.splits == sp_h && c.bk == (tf ? 32 : kTcBK) && !c.persist && c.gm == 1)
+          P->tune_ms_heuristic = c.ms;
       P->bn = best.bn;
       P->splits = best.splits;
       P->bk = best.bk;
       P->persist = best.persist;
       P->pair = best.pair;
+      P->gm = best.gm;
       pick_contraction_operands(P);
       int terr = 0;
       P->d_err.download(&terr, 1, s);
@@ -1527,12 +1562,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       P->d_part2.alloc(ctx, size_t(P->splits2) * size_t(nw * 8 * N));
       P->opKK = two_part(P->d_KKh.p, P->d_KKl.p, nw, nw, P->Kp2, kTcBM);
       P->opY = two_part(P->d_Yh.p, P->d_Yl.p, 8 * N, nw, P->Kp2, P->bn2);
-      if (4 * (32 + 2 * (ns + 2)) > 256 * kXgPreMax)
-        fail(EPSP_EUNSUPPORTED, "the shift grid is too fine for the BF16 operand kernel (nshift = " + std::to_string(ns) +
-                                    " > 222); use EPSP_PATH_GEMM_FP64");
-      for (auto fn : {xgen_bf16_kernel<2, false>, xgen_bf16_kernel<4, false>, xgen_bf16_kernel<8, false>,
-                      xgen_bf16_kernel<2, true>, xgen_bf16_kernel<4, true>, xgen_bf16_kernel<8, true>})
-        EPSP_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(xgen_smem_bytes(int(ns)))));
+      zgather_shape(nw, P->nwp);  // the grid's size is checked here
     }
     EPSP_CUDA(cudaStreamSynchronize(s));
   } else {
@@ -1690,27 +1720,43 @@ static void apply_L(LadderPlan* P, const double2* J, double2* LJ, const double2*
   EPSP_LAUNCHED(ctx);
 }
 
-// The tensor-core path (GEMM_BF16), FP32 vertices: LJ = L(J), or X - L(J) with X.
+// Jr of nA vertices (rows z 16 nwp..) into the plan's or a batch's operand buffers.
+static void launch_jmat(LadderPlan* P, const float2* J, long jstride, const int* rmap, int nA, float* Jt,
+                        __nv_bfloat16* Jh, __nv_bfloat16* Jl) {
+  Ctx* ctx = P->ctx;
+  const dim3 grid(unsigned(P->Kzp / 32), unsigned(P->nwp / 32), unsigned(8 * nA));
+  if (P->path == EPSP_PATH_GEMM_TF32)
+    jmat_kernel<true><<<grid, 256, 0, ctx->stream>>>(J, jstride, rmap, int(P->nw), int(P->nwp), int(P->ni), P->Kzp, Jt,
+                                                     nullptr, nullptr);
+  else
+    jmat_kernel<false><<<grid, 256, 0, ctx->stream>>>(J, jstride, rmap, int(P->nw), int(P->nwp), int(P->ni), P->Kzp,
+                                                      nullptr, Jh, Jl);
+  EPSP_LAUNCHED(ctx);
+}
+
+// The tensor-core paths (GEMM_BF16, GEMM_TF32), FP32 vertices: LJ = L(J), or X - L(J) with X.
 static void apply_L(LadderPlan* P, const float2* J, float2* LJ, const float2* X = nullptr) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
-  const long nw = P->nw, ni = P->ni, ns = P->nshift;
+  const long nw = P->nw, ni = P->ni;
   if (!tc_path(P->path)) fail(EPSP_EINVAL, "internal: FP32 vertices on an FP64 path");
   set_mode_occupations(P, P->cur_T);
   const long nwp = P->nwp, M = 24 * nwp, N = 3 * ni;
-  long px = prof_begin(ctx, "xgen");
-  const unsigned ktiles = unsigned((P->Kp / 64 + kXgTiles - 1) / kXgTiles);
-  launch_xgen(P->path == EPSP_PATH_GEMM_TF32, ns, dim3(unsigned(nwp / 32 * 8), ktiles, 1), xgen_smem_bytes(int(ns)), s, J,
-              long(0), static_cast<const int*>(nullptr), static_cast<const int32_t*>(P->d_mt_k.p),
-              static_cast<const float*>(P->d_mt_w.p), static_cast<const float*>(P->d_nnu_f.p), int(nw), int(nwp),
-              int(ns), int(P->nmp), int(ni), P->Kx, P->Kp, P->d_Ah.p, P->d_Al.p, P->d_At.p);
-  EPSP_LAUNCHED(ctx);
+  long px = prof_begin(ctx, "jmat");
+  launch_jmat(P, J, 0, nullptr, 1, P->d_Jt.p, P->d_Jh.p, P->d_Jl.p);
   prof_end(ctx, px);
-  int sp = tc_gemm_launch_with(ctx, P->opA, P->opG, P->bn, P->splits, int(M), int(N), int(P->Kx), P->d_part.p, M, M * N,
-                               P->d_err.p, "tc_ladder", P->persist, P->pair);
-  // D stays as the contraction's split-K partials; y_split and finish add them as they read
+  const int sp = tc_gemm_launch_with(ctx, P->opA, P->opG, P->bn, P->splits, int(P->Mz), int(P->Nz), int(P->Kz), P->d_Z.p,
+                                     P->Mz, P->Mz * P->Nz, P->d_err.p, "tc_ladder", P->persist, P->pair, P->gm);
+  long pz = prof_begin(ctx, "zgather");
+  const ZgatherShape zg = zgather_shape(nw, nwp);
+  launch_zgather(zg, dim3(unsigned((N + zg.NC - 1) / zg.NC), 4, 1), s, static_cast<const float*>(P->d_Z.p), P->Mz, sp,
+                 P->Mz * P->Nz, static_cast<const int32_t*>(P->d_zt_k.p),
+                 reinterpret_cast<const float4*>(P->d_zt_w.p), static_cast<const float*>(P->d_nnu_f.p),
+                 static_cast<const int*>(nullptr), int(nw), int(nwp), int(P->nm), N, P->d_Dz.p, M);
+  EPSP_LAUNCHED(ctx);
+  prof_end(ctx, pz);
   long pl = prof_begin(ctx, "lsum");
-  y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), 1), 256, 0, s>>>(P->d_part.p, M, sp, M * N, int(nw), int(nwp),
+  y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), 1), 256, 0, s>>>(P->d_Dz.p, M, 1, 0, int(nw), int(nwp),
                                                                                   N, P->Kp2, P->d_Yh.p, P->d_Yl.p);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pl);
@@ -1718,8 +1764,8 @@ static void apply_L(LadderPlan* P, const float2* J, float2* LJ, const float2* X 
                            "tc_ladder_kk");
   pl = prof_begin(ctx, "lfinish");
   finish_gemm_kernel<float><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), 1), 256, 0, s>>>(
-      P->d_part.p, M, sp, M * N, P->d_part2.p, sp2, nw * 8 * N, P->d_Gmf.p, P->d_Gpf.p, nullptr, int(nw), int(nwp),
-      int(ni), LJ, X);
+      P->d_Dz.p, M, 1, 0, P->d_part2.p, sp2, nw * 8 * N, P->d_Gmf.p, P->d_Gpf.p, nullptr, int(nw), int(nwp), int(ni), LJ,
+      X);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pl);
 }
@@ -2137,10 +2183,10 @@ constexpr int kDotBlocksB = 256;
 // Buffers of a batch of right-hand sides (capacity cap), tensor maps over them.
 struct LadderBatch {
   long cap = 0;
-  int bk = 0;  // K block of the A maps
-  DBuf<__nv_bfloat16> Ah, Al, Yh, Yl;
-  DBuf<float> At;  // GEMM_TF32: the A operand as TF32-rounded FP32
-  DBuf<float> part, part2, nnu;
+  int bk = 0;  // K block of the Jr maps
+  DBuf<__nv_bfloat16> Jh, Jl, Yh, Yl;
+  DBuf<float> Jt;  // GEMM_TF32: Jr as TF32-rounded FP32
+  DBuf<float> Z, D, part2, nnu;
   DBuf<float2> Gm, Gp, J0, J, LJ, W;
   DBuf<double2> dpart, H, coef_a, coef_b;
   std::vector<DBuf<float2>> V;
@@ -2158,22 +2204,21 @@ static void batch_reserve(LadderPlan* P, LadderBatch& B, long R, int maxiter) {
   B.cap = R;
   const bool tf = P->path == EPSP_PATH_GEMM_TF32;
   if (tf) {
-    B.At.alloc(ctx, size_t(R * M * P->Kp));
+    B.Jt.alloc(ctx, size_t(R * P->Mz * P->Kzp));
   } else {
-    B.Ah.alloc(ctx, size_t(R * M * P->Kp));
-    B.Al.alloc(ctx, size_t(R * M * P->Kp));
+    B.Jh.alloc(ctx, size_t(R * P->Mz * P->Kzp));
+    B.Jl.alloc(ctx, size_t(R * P->Mz * P->Kzp));
   }
   B.Yh.alloc(ctx, size_t(R * 8 * N * P->Kp2));
   B.Yl.alloc(ctx, size_t(R * 8 * N * P->Kp2));
-  size_t p1 = 0, p2 = 0;
+  size_t p2 = 0;
   for (long a = 1; a <= R; ++a) {
     int bn, sp2;
-    const int sp1 = tc_splits_for(ctx, int(a * M), int(N), int(P->Kx), P->bn);
     tc_gemm_shape(ctx, int(nw), int(a * 8 * N), int(nw), 16, 2, &bn, &sp2);
-    p1 = std::max(p1, size_t(sp1) * size_t(a * M * N));
     p2 = std::max(p2, size_t(sp2) * size_t(a * nw * 8 * N));
   }
-  B.part.alloc(ctx, p1);
+  B.Z.alloc(ctx, size_t(R * P->Mz) * size_t(P->Nz));  // one split: the stacked product has tiles for every SM
+  B.D.alloc(ctx, size_t(R * M * N));
   B.part2.alloc(ctx, p2);
   B.nnu.alloc(ctx, size_t(16 * R));
   B.Gm.alloc(ctx, size_t(R * 4 * nw * ni));
@@ -2190,8 +2235,8 @@ static void batch_reserve(LadderPlan* P, LadderBatch& B, long R, int maxiter) {
   B.pp.alloc(ctx, size_t(R));
   B.rmap.alloc(ctx, size_t(R));
   B.Y.alloc(ctx, size_t(R * 3 * ni));
-  B.opA = tf ? one_part_tf32(B.At.p, R * M, P->Kx, P->Kp, kTcBM, P->bk)
-             : two_part(B.Ah.p, B.Al.p, R * M, P->Kx, P->Kp, kTcBM, P->bk);
+  B.opA = tf ? one_part_tf32(B.Jt.p, R * P->Mz, P->Kz, P->Kzp, kTcBM, P->bk)
+             : two_part(B.Jh.p, B.Jl.p, R * P->Mz, P->Kz, P->Kzp, kTcBM, P->bk);
   B.bk = P->bk;
   B.opY = two_part(B.Yh.p, B.Yl.p, R * 8 * N, nw, P->Kp2, P->bn2);
 }
@@ -2200,27 +2245,27 @@ static void batch_reserve(LadderPlan* P, LadderBatch& B, long R, int maxiter) {
 static void apply_L_batch(LadderPlan* P, LadderBatch& B, const float2* X, int nA, float2* LJ) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
-  const long nw = P->nw, ni = P->ni, ns = P->nshift, nwp = P->nwp, M = 24 * nwp, N = 3 * ni, n = nw * 24 * ni;
-  const long Mt = M * nA;
-  long px = prof_begin(ctx, "xgen");
-  const unsigned ktiles = unsigned((P->Kp / 64 + kXgTiles - 1) / kXgTiles);
-  launch_xgen(P->path == EPSP_PATH_GEMM_TF32, ns, dim3(unsigned(nwp / 32 * 8), ktiles, unsigned(nA)),
-              xgen_smem_bytes(int(ns)), s, X, n, static_cast<const int*>(B.rmap.p),
-              static_cast<const int32_t*>(P->d_mt_k.p), static_cast<const float*>(P->d_mt_w.p),
-              static_cast<const float*>(B.nnu.p), int(nw), int(nwp), int(ns), int(P->nmp), int(ni), P->Kx, P->Kp, B.Ah.p,
-              B.Al.p, B.At.p);
-  EPSP_LAUNCHED(ctx);
+  const long nw = P->nw, ni = P->ni, nwp = P->nwp, M = 24 * nwp, N = 3 * ni, n = nw * 24 * ni;
+  const long Mt = M * nA, Mzt = P->Mz * nA;
+  long px = prof_begin(ctx, "jmat");
+  launch_jmat(P, X, n, B.rmap.p, nA, B.Jt.p, B.Jh.p, B.Jl.p);
   prof_end(ctx, px);
-  int sp = tc_gemm_launch_with(ctx, B.opA, P->opG, P->bn, 0, int(Mt), int(N), int(P->Kx), B.part.p, Mt, Mt * N, P->d_err.p,
-                               "tc_ladder", P->persist, P->pair);
+  tc_gemm_launch_with(ctx, B.opA, P->opG, P->bn, 1, int(Mzt), int(P->Nz), int(P->Kz), B.Z.p, Mzt, Mzt * P->Nz,
+                      P->d_err.p, "tc_ladder", P->persist, P->pair, P->gm);
+  const ZgatherShape zg = zgather_shape(nw, nwp);
+  launch_zgather(zg, dim3(unsigned((N + zg.NC - 1) / zg.NC), 4, unsigned(nA)), s, static_cast<const float*>(B.Z.p), Mzt,
+                 1, long(0), static_cast<const int32_t*>(P->d_zt_k.p), reinterpret_cast<const float4*>(P->d_zt_w.p),
+                 static_cast<const float*>(B.nnu.p), static_cast<const int*>(B.rmap.p), int(nw), int(nwp), int(P->nm), N,
+                 B.D.p, Mt);
+  EPSP_LAUNCHED(ctx);
   y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), unsigned(nA)), 256, 0, s>>>(
-      B.part.p, Mt, sp, Mt * N, int(nw), int(nwp), N, P->Kp2, B.Yh.p, B.Yl.p);
+      B.D.p, Mt, 1, 0, int(nw), int(nwp), N, P->Kp2, B.Yh.p, B.Yl.p);
   EPSP_LAUNCHED(ctx);
   const long N2 = 8 * N * nA;
   int sp2 = tc_gemm_launch(ctx, P->opKK, B.opY, int(nw), int(N2), int(nw), B.part2.p, nw, nw * N2, 16, P->d_err.p,
                            "tc_ladder_kk");
   finish_gemm_kernel<float><<<dim3(div_up(size_t(nw), 256), unsigned(6 * ni), unsigned(nA)), 256, 0, s>>>(
-      B.part.p, Mt, sp, Mt * N, B.part2.p, sp2, nw * N2, B.Gm.p, B.Gp.p, B.rmap.p, int(nw), int(nwp), int(ni), LJ);
+      B.D.p, Mt, 1, 0, B.part2.p, sp2, nw * N2, B.Gm.p, B.Gp.p, B.rmap.p, int(nw), int(nwp), int(ni), LJ);
   EPSP_LAUNCHED(ctx);
 }
 
@@ -2585,7 +2630,7 @@ epsp_status epsp_ladder_set_gemm_config(epsp_ladder_plan* plan, int32_t bn, int3
     if (!ok)
       fail(EPSP_EINVAL, tf ? "TF32 tile shape must be bn 128 or 256 with bk 32"
                            : "tile shape must be bn 128 or 256 with bk 64, or bn 256 with bk 32");
-    const int max_sp = int(P->d_part.n / size_t(24 * P->nwp * 3 * P->ni));
+    const int max_sp = P->zsplit_cap;
     if (splits < 1 || splits > max_sp) fail(EPSP_EINVAL, "splits must be in [1, " + std::to_string(max_sp) + "]");
     P->bn = bn;
     P->splits = splits;
@@ -2641,7 +2686,8 @@ epsp_status epsp_ladder_gemm_config(const epsp_ladder_plan* plan, int32_t* bn, i
   if (bk) *bk = P->bk;
   double best = 0;
   for (const auto& c : P->tune_all)
-    if (c.bn == P->bn && c.splits == P->splits && c.bk == P->bk && c.persist == P->persist && c.pair == P->pair)
+    if (c.bn == P->bn && c.splits == P->splits && c.bk == P->bk && c.persist == P->persist && c.pair == P->pair &&
+        c.gm == P->gm)
       best = c.ms;
   if (ms_chosen) *ms_chosen = best;
   if (ms_heuristic) *ms_heuristic = P->tune_ms_heuristic;

@@ -92,7 +92,7 @@ void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* b
 
 template <int BN, int STAGES, int NS, int BK = kTcBK, bool TF32 = false>
 static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int kblocks, int per, int splits,
-                   float* out, long ld_out, long split_stride, int* d_err) {
+                   float* out, long ld_out, long split_stride, int* d_err, int gm = 1) {
   using L = TcSmem<BN, STAGES, NS, BK, TF32>;
   if (A.bk != BK || B.bk != BK) fail(EPSP_EINVAL, "operand tensor maps were built for another K block");
   if (A.tf32 != TF32 || B.tf32 != TF32) fail(EPSP_EINVAL, "operand tensor maps were built for another element type");
@@ -109,7 +109,7 @@ static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int 
   }
   dim3 grid((N + BN - 1) / BN, (M + kTcBM - 1) / kTcBM, splits);
   tc_gemm_split_kernel<BN, STAGES, NS, BK, TF32><<<grid, 128, L::kBytes, ctx->stream>>>(maps, M, N, kblocks, per, out,
-                                                                                        ld_out, split_stride, d_err);
+                                                                                        ld_out, split_stride, d_err, gm);
   EPSP_LAUNCHED(ctx);
 }
 
@@ -122,7 +122,7 @@ static CUtensorMap remap(const TcOperand& op, int p, int box_rows) {
 
 template <int BN, int STAGES, int NS, int BK, bool TF32 = false>
 static void launch_persist(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int kblocks, int per,
-                           int splits, float* out, long ld_out, long split_stride, int* d_err) {
+                           int splits, float* out, long ld_out, long split_stride, int* d_err, int gm = 1) {
   using L = TcPSmem<BN, STAGES, NS, BK, TF32>;
   if (A.bk != BK || B.bk != BK) fail(EPSP_EINVAL, "operand tensor maps were built for another K block");
   if (A.tf32 != TF32 || B.tf32 != TF32) fail(EPSP_EINVAL, "operand tensor maps were built for another element type");
@@ -141,14 +141,14 @@ static void launch_persist(Ctx* ctx, const TcOperand& A, const TcOperand& B, int
   const int nitems = nN * nM * splits;  // (N tile, M tile, split)
   const int grid = std::min(nitems, ctx->sm_count);
   kern<<<grid, 192, L::kBytes, ctx->stream>>>(maps, M, N, kblocks, per, nN, nM, nitems, out, ld_out, split_stride,
-                                              d_err);
+                                              d_err, gm);
   EPSP_LAUNCHED(ctx);
 }
 
 // The CTA-pair kernel: clusters of two CTAs, each pair one 256 x BN tile (B halves of BN / 2 rows).
 template <int BN, int STAGES, int NS, int BK, bool TF32>
 static void launch_pair(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int kblocks, int per,
-                        int splits, float* out, long ld_out, long split_stride, int* d_err) {
+                        int splits, float* out, long ld_out, long split_stride, int* d_err, int gm = 1) {
   using L = TcPairSmem<BN, STAGES, NS, BK, TF32>;
   if (A.bk != BK || B.bk != BK) fail(EPSP_EINVAL, "operand tensor maps were built for another K block");
   if (A.tf32 != TF32 || B.tf32 != TF32) fail(EPSP_EINVAL, "operand tensor maps were built for another element type");
@@ -175,7 +175,7 @@ static void launch_pair(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M,
   cfg.stream = ctx->stream;
   cfg.attrs = &cl;
   cfg.numAttrs = 1;
-  EPSP_CUDA(cudaLaunchKernelEx(&cfg, kern, maps, M, N, kblocks, per, out, ld_out, split_stride, d_err));
+  EPSP_CUDA(cudaLaunchKernelEx(&cfg, kern, maps, M, N, kblocks, per, out, ld_out, split_stride, d_err, gm));
   EPSP_LAUNCHED(ctx);
 }
 
@@ -215,7 +215,7 @@ int tc_splits_for(Ctx* ctx, int M, int N, int K, int bn) {
 
 int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn, int splits, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int* d_err, const char* prof_name, bool persist,
-                        bool pair) {
+                        bool pair, int gm) {
   if (bn != 128 && bn != 256) fail(EPSP_EINVAL, "tile width must be 128 or 256");
   if (pair && (persist || bn != 256)) fail(EPSP_EINVAL, "the CTA-pair kernel is one-tile, tile width 256");
   if (A.tf32 || B.tf32) {
@@ -228,15 +228,15 @@ int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn
     splits = (kblocks + per - 1) / per;
     long pi = prof_begin(ctx, prof_name);
     if (pair)
-      launch_pair<256, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+      launch_pair<256, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
     else if (persist && bn == 256)
-      launch_persist<256, 4, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+      launch_persist<256, 4, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
     else if (persist)
-      launch_persist<128, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+      launch_persist<128, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
     else if (bn == 256)
-      launch<256, 4, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+      launch<256, 4, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
     else
-      launch<128, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+      launch<128, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
     prof_end(ctx, pi);
     return splits;
   }
@@ -252,15 +252,15 @@ int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn
   if (pair && bk != 32) fail(EPSP_EINVAL, "the BF16x3 CTA-pair kernel takes K blocks of 32");
   long pi = prof_begin(ctx, prof_name);
   if (pair)
-    launch_pair<256, 6, 2, 32, false>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    launch_pair<256, 6, 2, 32, false>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
   else if (persist)
-    launch_persist<256, 4, 2, 32>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    launch_persist<256, 4, 2, 32>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
   else if (bk == 32)
-    launch<256, 4, 2, 32>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    launch<256, 4, 2, 32>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
   else if (bn == 256)
-    launch<256, 2, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    launch<256, 2, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
   else
-    launch<128, 3, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err);
+    launch<128, 3, 2>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
   prof_end(ctx, pi);
   return splits;
 }
@@ -274,8 +274,9 @@ std::map<std::array<long, 5>, std::vector<TcTune>> g_tune_cache;
 
 TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, const TcOperand& B256, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int max_splits, int* d_err, int reps,
-                        std::vector<TcTune>* all, const TcOperand* A32, const TcOperand* B256_32) {
-  const std::array<long, 5> key{ctx->device, M, N, K, max_splits + (A32 && B256_32 ? 1000 : 0) + (A.tf32 ? 2000 : 0)};
+                        std::vector<TcTune>* all, const TcOperand* A32, const TcOperand* B256_32, int gm) {
+  const std::array<long, 5> key{ctx->device, M, N, K,
+                                max_splits + (A32 && B256_32 ? 1000 : 0) + (A.tf32 ? 2000 : 0) + 10000l * gm};
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune_cache.find(key);
@@ -300,6 +301,11 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
         cand.push_back(TcTune{bn, sp, 32, 0.f});
         cand.push_back(TcTune{bn, sp, 32, 0.f, true});
         if (bn == 256) cand.push_back(TcTune{bn, sp, 32, 0.f, false, true});  // CTA pairs
+        if (gm > 1) {  // the same kernels in grouped tile order
+          cand.push_back(TcTune{bn, sp, 32, 0.f, false, false, gm});
+          cand.push_back(TcTune{bn, sp, 32, 0.f, true, false, gm});
+          if (bn == 256) cand.push_back(TcTune{bn, sp, 32, 0.f, false, true, gm});
+        }
         continue;
       }
       cand.push_back(TcTune{bn, sp, kTcBK, 0.f});
@@ -307,6 +313,11 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
         cand.push_back(TcTune{bn, sp, 32, 0.f});
         cand.push_back(TcTune{bn, sp, 32, 0.f, true});
         cand.push_back(TcTune{bn, sp, 32, 0.f, false, true});  // CTA pairs
+        if (gm > 1) {
+          cand.push_back(TcTune{bn, sp, 32, 0.f, false, false, gm});
+          cand.push_back(TcTune{bn, sp, 32, 0.f, true, false, gm});
+          cand.push_back(TcTune{bn, sp, 32, 0.f, false, true, gm});
+        }
       }
     }
   }
@@ -323,7 +334,7 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
   // one untimed launch first, so that no candidate pays the first launch's costs
   if (!cand.empty())
     tc_gemm_launch_with(ctx, opA(cand[0]), opB(cand[0]), cand[0].bn, cand[0].splits, M, N, K, out, ld_out, split_stride,
-                        d_err, "autotune", cand[0].persist, cand[0].pair);
+                        d_err, "autotune", cand[0].persist, cand[0].pair, cand[0].gm);
   for (auto& c : cand) {
     const TcOperand& A_ = opA(c);
     const TcOperand& B = opB(c);
@@ -331,7 +342,7 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
     float ms = 0.f;
     EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
     tc_gemm_launch_with(ctx, A_, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune", c.persist,
-                        c.pair);
+                        c.pair, c.gm);
     EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
     EPSP_CUDA(cudaEventSynchronize(e1));
     EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
@@ -342,7 +353,7 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
       for (int r = 0; r < reps; ++r) {
         EPSP_CUDA(cudaEventRecord(e0, ctx->stream));
         tc_gemm_launch_with(ctx, A_, B, c.bn, c.splits, M, N, K, out, ld_out, split_stride, d_err, "autotune",
-                            c.persist, c.pair);
+                            c.persist, c.pair, c.gm);
         EPSP_CUDA(cudaEventRecord(e1, ctx->stream));
         EPSP_CUDA(cudaEventSynchronize(e1));
         EPSP_CUDA(cudaEventElapsedTime(&ms, e0, e1));

@@ -78,6 +78,23 @@ __device__ __forceinline__ void cluster_sync_all() {
   asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
+// The (N tile, M tile) of tile index L (0 <= L < nN nM) in launch order. gm <= 1: N tiles fastest
+// (CTAs resident together share one A tile and sweep B). gm > 1: grouped order, the M tiles of a
+// group of gm run fastest and the group sweeps every N tile before the next group starts, so a
+// group's A tiles stay in L2 while B streams once per group -- for products whose B operand is too
+// large to stay in L2 across the M tiles.
+__device__ __forceinline__ void tile_of(int L, int nN, int nM, int gm, int& nt, int& mt) {
+  if (gm <= 1) {
+    nt = L % nN;
+    mt = L / nN;
+    return;
+  }
+  const int per = gm * nN, g = L / per, r = L % per;
+  const int rows = min(gm, nM - g * gm);
+  mt = g * gm + r % rows;
+  nt = r / rows;
+}
+
 // Shared-memory matrix descriptor of a K-major operand tile with 128-byte swizzle: rows of 128 B
 // (64 BF16), 8-row groups 1024 B apart (stride byte offset), descriptor version 1.
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
@@ -170,7 +187,7 @@ struct TcMaps {
 template <int BN, int STAGES, int NS, int BK = kTcBK, bool TF32 = false>
 __global__ void __launch_bounds__(128, 1)
     tc_gemm_split_kernel(const __grid_constant__ TcMaps maps, int M, int N, int kblocks, int kb_per_split,
-                         float* __restrict__ out, long ld_out, long split_stride, int* __restrict__ err) {
+                         float* __restrict__ out, long ld_out, long split_stride, int* __restrict__ err, int gm = 1) {
   using L = TcSmem<BN, STAGES, NS, BK, TF32>;
   static_assert(!TF32 || NS == 1, "TF32 operands have one part");
   extern __shared__ uint8_t smem_raw[];
@@ -180,9 +197,11 @@ __global__ void __launch_bounds__(128, 1)
   __shared__ int s_abort;
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES), done_bar = smem_u32(bars + 2 * STAGES);
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  // N tiles vary fastest over the launch order, so the CTAs resident together share A tiles
-  // (the large operand) through L2 and A streams from DRAM about once
-  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * kTcBM;
+  // N tiles vary fastest over the launch order (gm <= 1), so the CTAs resident together share A
+  // tiles (the large operand) through L2 and A streams from DRAM about once; gm > 1 groups M tiles
+  int nt, mt;
+  tile_of(int(blockIdx.y) * int(gridDim.x) + int(blockIdx.x), int(gridDim.x), int(gridDim.y), gm, nt, mt);
+  const int n0 = nt * BN, m0 = mt * kTcBM;
   const int kb0 = blockIdx.z * kb_per_split;
   const int nkb = max(0, min(kblocks, kb0 + kb_per_split) - kb0);
 
@@ -322,7 +341,7 @@ template <int BN, int STAGES, int NS, int BK, bool TF32 = false>
 __global__ void __launch_bounds__(192, 1)
     tc_gemm_persist_kernel(const __grid_constant__ TcMaps maps, int M, int N, int kblocks, int kb_per_split, int nN,
                            int nM, int nitems, float* __restrict__ out, long ld_out, long split_stride,
-                           int* __restrict__ err) {
+                           int* __restrict__ err, int gm = 1) {
   using L = TcPSmem<BN, STAGES, NS, BK, TF32>;
   static_assert(!TF32 || NS == 1, "TF32 operands have one part");
   static_assert(2 * BN <= 512, "two accumulators must fit TMEM");
@@ -336,8 +355,10 @@ __global__ void __launch_bounds__(192, 1)
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int first = int(blockIdx.x), stride = int(gridDim.x);  // this CTA's items
   auto coords = [&](int item, int& n0, int& m0, int& z, int& kb0, int& nkb) {
-    n0 = (item % nN) * BN;
-    m0 = ((item / nN) % nM) * kTcBM;
+    int nt, mt;
+    tile_of(item % (nN * nM), nN, nM, gm, nt, mt);
+    n0 = nt * BN;
+    m0 = mt * kTcBM;
     z = item / (nN * nM);
     kb0 = z * kb_per_split;
     nkb = max(0, min(kblocks, kb0 + kb_per_split) - kb0);
@@ -560,7 +581,7 @@ __host__ __device__ constexpr uint32_t idesc_pair(int n) {
 template <int BN, int STAGES, int NS, int BK, bool TF32>
 __global__ void __launch_bounds__(128, 1)
     tc_gemm_pair_kernel(const __grid_constant__ TcMaps maps, int M, int N, int kblocks, int kb_per_split,
-                        float* __restrict__ out, long ld_out, long split_stride, int* __restrict__ err) {
+                        float* __restrict__ out, long ld_out, long split_stride, int* __restrict__ err, int gm = 1) {
   using L = TcPairSmem<BN, STAGES, NS, BK, TF32>;
   static_assert(!TF32 || NS == 1, "TF32 operands have one part");
   static_assert((BN / 2) % 8 == 0 && BN <= 256, "B halves of whole 8-row swizzle groups");
@@ -572,8 +593,12 @@ __global__ void __launch_bounds__(128, 1)
   const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * STAGES, done_bar = full0 + 16 * STAGES;
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const uint32_t rank = cluster_ctarank();  // 0: the leader, which issues the MMAs
-  // clusters are consecutive blockIdx.x pairs; N tiles vary fastest, as in the one-tile kernel
-  const int n0 = int(blockIdx.x >> 1) * BN, m0 = int(blockIdx.y) * 2 * kTcBM + int(rank) * kTcBM;
+  // clusters are consecutive blockIdx.x pairs; the pair's tile in the one-tile kernel's order (both
+  // CTAs of a pair compute the same tile index)
+  int nt, mt;
+  tile_of(int(blockIdx.y) * int(gridDim.x >> 1) + int(blockIdx.x >> 1), int(gridDim.x >> 1), int(gridDim.y), gm, nt,
+          mt);
+  const int n0 = nt * BN, m0 = mt * 2 * kTcBM + int(rank) * kTcBM;
   const int kb0 = blockIdx.z * kb_per_split;
   const int nkb = max(0, min(kblocks, kb0 + kb_per_split) - kb0);
 
@@ -723,7 +748,7 @@ void tc_gemm_shape(Ctx* ctx, int M, int N, int K, int max_splits, int ns, int* b
 // used. pair: the CTA-pair kernel (bn 256; BF16 with K blocks of 32, or TF32), six stages.
 int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn, int splits, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int* d_err, const char* prof_name = "tc_gemm",
-                        bool persist = false, bool pair = false);
+                        bool persist = false, bool pair = false, int gm = 1);
 // The variant with K blocks of 32 (64-byte swizzle) and four pipeline stages, bn = 256; A and B
 // maps built with bk = 32.
 
@@ -736,6 +761,7 @@ struct TcTune {
   float ms = 0.f;
   bool persist = false;  // the persistent kernel (one CTA per SM, two accumulators)
   bool pair = false;     // the CTA-pair kernel (tcgen05 cta_group::2, 256-row tiles)
+  int gm = 1;            // tile order: N tiles fastest (1) or groups of gm M tiles
 };
 
 // The autotuner: times every candidate tile shape of one two-part BF16 or one-part TF32 product on
@@ -745,11 +771,12 @@ struct TcTune {
 // with the heuristic split count and twice it, capped at max_splits -- with CUDA events on ctx's
 // stream (a first launch, then unless it took 20 ms or more the best of `reps` launches timed one
 // by one), and returns the fastest; every candidate's time goes to *all when given. B128 / B256: B's maps
-// with boxes of 128 / 256 rows. Results are cached per device and shape for the process.
+// with boxes of 128 / 256 rows. gm > 1 adds the one-tile, persistent and pair candidates in grouped
+// tile order (groups of gm M tiles). Results are cached per device and shape for the process.
 TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, const TcOperand& B256, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int max_splits, int* d_err, int reps,
                         std::vector<TcTune>* all = nullptr, const TcOperand* A32 = nullptr,
-                        const TcOperand* B256_32 = nullptr);
+                        const TcOperand* B256_32 = nullptr, int gm = 1);
 
 // x = Σ_p x_p with x_p BF16, p < ns (round to nearest at every step).
 __device__ __forceinline__ void split_bf16_n(float x, int ns, __nv_bfloat16* out) {
