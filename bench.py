@@ -380,8 +380,9 @@ def run_ours(args, world, rank, local):
     out["ladder_gemm_autotune"] = lp.gemm_config()
     out["ladder_gmres_iters"] = int(l["niter"][0, 0])
     out["gpu_launches"] = int(launches)
-    # roofline of the dominant kernel: the ladder's tensor-core contraction
-    M, N, K = 24 * nw, 3 * ni, 15 * 3 * ni
+    # roofline of the dominant kernel: the ladder's tensor-core contraction Z = Jr Bz (rows: 16 per
+    # node; columns: 15 modes x 3ni; K: 3ni pairs), useful work without the node padding
+    M, N, K = 16 * nw, 15 * 3 * ni, 3 * ni
     if prof_n:
         avg_s = prof_ms / prof_n / 1e3
         flops = 2.0 * M * N * K
@@ -566,19 +567,22 @@ def batched_c3(s, ctx, ws) -> dict:
     dsig_T = [float(np.max(np.abs(r8["sigma"][:, :, k] - r64["sigma"][:, :, k]))) for k in range(8)]
     dmu_T = [float(abs(r8["mu"][k] - r64["mu"][k])) for k in range(8)]
     sub = [0, len(Om) - 1]
+    # σ: the mixed path against FP64 on the same Ω chain (the same warm starts, so the difference is
+    # the precision's, not the solver tolerance's), each on its own scGD0 Σ
+    oms = [Om[j] for j in sub]
     lp64 = api.LadderPlan(s, path="gemm_fp64", omega_acoustic=W_AC, ctx=ctx)
-    l64 = lp64.run(r64["sigma"], r64["mu"], Ts, [Om[j] for j in sub], rtol=L_RTOL, maxiter=L_MAXITER)
+    l64 = lp64.run(r64["sigma"], r64["mu"], Ts, oms, rtol=L_RTOL, maxiter=L_MAXITER)
     lp64.close()
-
-    def rel_pairs(sl):
-        return [[float(np.linalg.norm(sl[:, :, j, k] - l64["sigma_ladder"][:, :, n, k]) /
-                       np.linalg.norm(l64["sigma_ladder"][:, :, n, k])) for n, j in enumerate(sub)] for k in range(8)]
-    rel_b, rel_s = rel_pairs(lb["sigma_ladder"]), rel_pairs(ls["sigma_ladder"])
+    lp = api.LadderPlan(s, path=LADDER_PATH, omega_acoustic=W_AC, ctx=ctx)
+    lm = lp.run(r8["sigma"], r8["mu"], Ts, oms, rtol=L_RTOL, maxiter=L_MAXITER)
+    lp.close()
+    rel_m = [[float(np.linalg.norm(lm["sigma_ladder"][:, :, n, k] - l64["sigma_ladder"][:, :, n, k]) /
+                    np.linalg.norm(l64["sigma_ladder"][:, :, n, k])) for n in range(len(oms))] for k in range(8)]
     err = dict(scgd0_max_abs_dsigma_eV_per_T=dsig_T, scgd0_abs_dmu_eV_per_T=dmu_T,
-               ladder_pairs_checked=f"8 T x Omega in {{{Om[sub[0]]:g}, {Om[sub[1]]:g}}} eV",
-               ladder_rel_sigma_batched_per_T_Omega=rel_b, ladder_rel_sigma_sequential_per_T_Omega=rel_s,
-               max_abs_dsigma_eV=max(dsig_T), max_rel_sigma_batched=max(max(x) for x in rel_b),
-               max_rel_sigma_sequential=max(max(x) for x in rel_s))
+               ladder_pairs_checked=f"8 T x Omega in {{{oms[0]:g}, {oms[1]:g}}} eV, both paths on that Omega chain",
+               ladder_rel_sigma_per_T_Omega=rel_m, max_abs_dsigma_eV=max(dsig_T),
+               max_rel_sigma=max(max(x) for x in rel_m),
+               niter_equal=bool(np.array_equal(lm["niter"], l64["niter"])))
     return dict(workload="8 T (100-800 K) x 32 Omega (0-0.5 eV), same model", errors_vs_fp64=err,
                 scgd0_8T_batched_s=t_batched, scgd0_8T_iters=int(r8["iters_total"]),
                 scgd0_8T_one_by_one_s=t_single, scgd0_one_by_one_iters=it_single,

@@ -301,10 +301,11 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
         cand.push_back(TcTune{bn, sp, 32, 0.f});
         cand.push_back(TcTune{bn, sp, 32, 0.f, true});
         if (bn == 256) cand.push_back(TcTune{bn, sp, 32, 0.f, false, true});  // CTA pairs
-        if (gm > 1) {  // the same kernels in grouped tile order
-          cand.push_back(TcTune{bn, sp, 32, 0.f, false, false, gm});
-          cand.push_back(TcTune{bn, sp, 32, 0.f, true, false, gm});
-          if (bn == 256) cand.push_back(TcTune{bn, sp, 32, 0.f, false, true, gm});
+        for (int g : {gm, 4 * gm}) {  // the same kernels in grouped tile order, two group sizes
+          if (gm <= 1) break;
+          cand.push_back(TcTune{bn, sp, 32, 0.f, false, false, g});
+          cand.push_back(TcTune{bn, sp, 32, 0.f, true, false, g});
+          if (bn == 256) cand.push_back(TcTune{bn, sp, 32, 0.f, false, true, g});
         }
         continue;
       }
@@ -313,10 +314,11 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
         cand.push_back(TcTune{bn, sp, 32, 0.f});
         cand.push_back(TcTune{bn, sp, 32, 0.f, true});
         cand.push_back(TcTune{bn, sp, 32, 0.f, false, true});  // CTA pairs
-        if (gm > 1) {
-          cand.push_back(TcTune{bn, sp, 32, 0.f, false, false, gm});
-          cand.push_back(TcTune{bn, sp, 32, 0.f, true, false, gm});
-          cand.push_back(TcTune{bn, sp, 32, 0.f, false, true, gm});
+        for (int g : {gm, 4 * gm}) {
+          if (gm <= 1) break;
+          cand.push_back(TcTune{bn, sp, 32, 0.f, false, false, g});
+          cand.push_back(TcTune{bn, sp, 32, 0.f, true, false, g});
+          cand.push_back(TcTune{bn, sp, 32, 0.f, false, true, g});
         }
       }
     }

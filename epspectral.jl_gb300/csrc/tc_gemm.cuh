@@ -772,7 +772,8 @@ struct TcTune {
 // stream (a first launch, then unless it took 20 ms or more the best of `reps` launches timed one
 // by one), and returns the fastest; every candidate's time goes to *all when given. B128 / B256: B's maps
 // with boxes of 128 / 256 rows. gm > 1 adds the one-tile, persistent and pair candidates in grouped
-// tile order (groups of gm M tiles). Results are cached per device and shape for the process.
+// tile order (groups of gm and of 4 gm M tiles). Results are cached per device and shape for the
+// process.
 TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, const TcOperand& B256, int M, int N, int K,
                         float* out, long ld_out, long split_stride, int max_splits, int* d_err, int reps,
                         std::vector<TcTune>* all = nullptr, const TcOperand* A32 = nullptr,
