@@ -40,6 +40,14 @@ using cplx = std::complex<double>;
 // plan
 // ---------------------------------------------------------------------------------------------
 
+// The GMRES state on the device, FP64 (Krylov.gmres, restart = false): the rotated Hessenberg R
+// (packed columns), the rotations (c, s), the right-hand side z, and the status the host reads.
+struct GmresDev {
+  double nJ0, beta, atol, rnorm;  // ‖J0‖, ‖r0‖, atol = rtol ‖J0‖, the current residual
+  double hbis, inv_hbis;          // H[k + 1, k] and its inverse (0 for a breakdown)
+  int solved, breakdown, solved_x0, inner;
+};
+
 struct LadderChunk {
   long i0 = 0, i1 = 0;     // outer states [i0, i1)
   long f0 = 0, f1 = 0;     // positions [f0, f1) in star order
@@ -109,6 +117,12 @@ struct LadderPlan {
   std::vector<DBuf<double2>> w_V;
   DBuf<float2> w_J0f, w_Jf, w_LJf, w_Wf;
   std::vector<DBuf<float2>> w_Vf;
+  // the device Arnoldi step: the two Gram-Schmidt passes' projections, ‖w‖^2, the rotated
+  // Hessenberg (packed), the rotations, z, 1 / H[k + 1, k], the status, the Krylov vectors' pointers
+  DBuf<double2> g_h1, g_h2, g_hsq, g_R, g_sn, g_z, g_inv;
+  DBuf<double> g_cs;
+  DBuf<GmresDev> g_st;
+  DBuf<void*> g_vp;
   std::shared_ptr<void> w_batch;  // the LadderBatch of the batched solves, kept across runs
 };
 
@@ -1148,6 +1162,219 @@ __global__ void __launch_bounds__(256) axpy_norm_kernel(V* __restrict__ q, const
   if (threadIdx.x == 0) part[blockIdx.x] = make_double2(sr[0], 0.0);
 }
 
+// Complex FP64 scalar arithmetic of the device Givens step (the operations of std::complex<double>
+// on finite values: products without the C99 special cases, |z| as hypot, division by a real).
+struct cuda_cplx {
+  double x, y;
+  static __device__ __forceinline__ cuda_cplx of(double2 v) { return {v.x, v.y}; }
+  __device__ __forceinline__ double2 d2() const { return make_double2(x, y); }
+  __device__ __forceinline__ cuda_cplx conj() const { return {x, -y}; }
+  __device__ __forceinline__ double abs() const { return hypot(x, y); }
+  __device__ __forceinline__ cuda_cplx operator*(cuda_cplx b) const { return {x * b.x - y * b.y, x * b.y + y * b.x}; }
+  __device__ __forceinline__ cuda_cplx operator*(double s) const { return {x * s, y * s}; }
+  __device__ __forceinline__ cuda_cplx operator/(double s) const { return {x / s, y / s}; }
+  __device__ __forceinline__ cuda_cplx operator+(cuda_cplx b) const { return {x + b.x, y + b.y}; }
+  __device__ __forceinline__ cuda_cplx operator-(cuda_cplx b) const { return {x - b.x, y - b.y}; }
+};
+
+// ---- the Arnoldi step on the device: classical Gram-Schmidt with one reorthogonalisation (CGS2)
+// over the Krylov vectors (pointers vp[i]), m <= kMG vectors per pass, and the Givens update of
+// Krylov.gmres's Hessenberg least-squares problem in FP64 on one thread ----
+constexpr int kMG = 8;
+
+// part[t kDotBlocks + block] = block partial of conj(V_{i0 + t}) w, t < m, in the reduction order of
+// dot_partial_kernel (one pass over w for m vectors).
+template <class V>
+__global__ void __launch_bounds__(256) mdot_partial_kernel(V* const* __restrict__ vp, int i0, int m, const V* __restrict__ w,
+                                                           long n, double2* __restrict__ part) {
+  __shared__ double sr[256], si[256];
+  double ar[kMG], ai[kMG];
+  const V* vt[kMG];  // the m vectors' pointers, read once
+#pragma unroll
+  for (int t = 0; t < kMG; ++t) {
+    ar[t] = ai[t] = 0;
+    vt[t] = t < m ? vp[i0 + t] : w;
+  }
+  const long stride = long(gridDim.x) * 256;
+  if constexpr (std::is_same_v<V, double2>) {
+    for (long k = long(blockIdx.x) * 256 + threadIdx.x; k < n; k += stride) {
+      const double2 b = w[k];
+#pragma unroll
+      for (int t = 0; t < kMG; ++t)
+        if (t < m) {
+          const double2 a = vt[t][k];
+          ar[t] += a.x * b.x + a.y * b.y;  // conj(a) b
+          ai[t] += a.x * b.y - a.y * b.x;
+        }
+    }
+  } else {
+    for (long k0 = long(blockIdx.x) * 256 + threadIdx.x; k0 < n; k0 += stride * kRun) {
+      float2 b[kRun];
+#pragma unroll
+      for (int q = 0; q < kRun; ++q) {
+        const long k = k0 + stride * q;
+        b[q] = k < n ? w[k] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int t = 0; t < kMG; ++t)
+        if (t < m) {
+          const float2* v = vt[t];
+          float fr = 0.f, fi = 0.f;
+#pragma unroll
+          for (int q = 0; q < kRun; ++q) {
+            const long k = k0 + stride * q;
+            const float2 a = k < n ? v[k] : make_float2(0.f, 0.f);
+            fr += a.x * b[q].x + a.y * b[q].y;
+            fi += a.x * b[q].y - a.y * b[q].x;
+          }
+          ar[t] += fr;
+          ai[t] += fi;
+        }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < kMG; ++t) {
+    if (t >= m) break;  // m is the same for the whole block
+    sr[threadIdx.x] = ar[t];
+    si[threadIdx.x] = ai[t];
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+      if (threadIdx.x < st) {
+        sr[threadIdx.x] += sr[threadIdx.x + st];
+        si[threadIdx.x] += si[threadIdx.x + st];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[long(t) * gridDim.x + blockIdx.x] = make_double2(sr[0], si[0]);
+    __syncthreads();
+  }
+}
+
+// w -= Σ_{t < m} h[i0 + t] V_{i0 + t} (ascending t, in the arithmetic of axpy_dev_kernel); with part,
+// also the block partials of |w|^2 of the result.
+template <class V>
+__global__ void __launch_bounds__(256) maxpy_kernel(V* __restrict__ w, V* const* __restrict__ vp, int i0, int m,
+                                                    const double2* __restrict__ h, long n, double2* __restrict__ part) {
+  using R = typename VecOf<V>::R;
+  __shared__ double sr[256];
+  R hx[kMG], hy[kMG];
+  const V* vt[kMG];  // the m vectors' pointers, read once
+#pragma unroll
+  for (int t = 0; t < kMG; ++t) {
+    const double2 hd = t < m ? h[i0 + t] : make_double2(0, 0);
+    hx[t] = R(hd.x);
+    hy[t] = R(hd.y);
+    vt[t] = t < m ? vp[i0 + t] : w;
+  }
+  double ar = 0;
+  const long stride = long(gridDim.x) * 256;
+  for (long k0 = long(blockIdx.x) * 256 + threadIdx.x; k0 < n; k0 += stride * kRun) {
+    R fr = 0;
+#pragma unroll
+    for (int q = 0; q < kRun; ++q) {
+      const long k = k0 + stride * q;
+      if (k < n) {
+        V a = w[k];
+#pragma unroll
+        for (int t = 0; t < kMG; ++t)
+          if (t < m) {
+            const V x = vt[t][k];
+            a = VecOf<V>::make(a.x - (hx[t] * x.x - hy[t] * x.y), a.y - (hx[t] * x.y + hy[t] * x.x));
+          }
+        w[k] = a;
+        if constexpr (std::is_same_v<V, double2>)
+          ar += a.x * a.x + a.y * a.y;
+        else
+          fr += a.x * a.x + a.y * a.y;
+      }
+    }
+    if constexpr (!std::is_same_v<V, double2>) ar += fr;
+  }
+  if (!part) return;
+  sr[threadIdx.x] = ar;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sr[threadIdx.x] += sr[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = make_double2(sr[0], 0.0);
+}
+
+// One Givens step for Arnoldi column `inner` (1-based): h1 + h2 (the two Gram-Schmidt passes'
+// projections, inner entries; h2 NULL after one pass) and ‖w‖^2 (hsq) complete the column; the
+// previous rotations are applied, a new one annihilates H[k + 1, k], and z and the residual follow
+// (src/ladder.jl:340-353 through Krylov.gmres). At inner = 1 it also takes ‖J0‖^2 and ‖r0‖^2 and sets
+// atol and z[0]; a solve already solved at x0 stops there. inv_out receives 1 / H[k + 1, k] (0 for a
+// breakdown), the scale of the next Krylov vector.
+__global__ void gmres_givens_kernel(const double2* __restrict__ h1, const double2* __restrict__ h2,
+                                    const double2* __restrict__ hsq, const double2* __restrict__ nJ0sq,
+                                    const double2* __restrict__ beta_sq, double rtol, double btol, int inner,
+                                    double2* __restrict__ Rp, double* __restrict__ cs, double2* __restrict__ sn,
+                                    double2* __restrict__ zv, GmresDev* __restrict__ st, double2* __restrict__ inv_out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  using C = cuda_cplx;
+  if (inner == 1) {
+    st->nJ0 = sqrt(nJ0sq->x);
+    st->atol = rtol * st->nJ0;
+    st->beta = sqrt(beta_sq->x);
+    st->rnorm = st->beta;
+    st->solved = 0;
+    st->breakdown = 0;
+    st->solved_x0 = st->beta <= st->atol || st->beta == 0;
+    zv[0] = make_double2(st->beta, 0);
+    if (st->solved_x0) {
+      st->solved = 1;
+      st->inner = 0;
+      inv_out->x = inv_out->y = 0;
+      return;
+    }
+  }
+  const long nr = long(inner - 1) * inner / 2;  // packed start of column inner - 1
+  for (int i = 0; i < inner; ++i)
+    Rp[nr + i] = h2 ? make_double2(h1[i].x + h2[i].x, h1[i].y + h2[i].y) : h1[i];
+  const double Hbis = sqrt(hsq->x);
+  for (int i = 0; i < inner - 1; ++i) {
+    const C r0 = C::of(Rp[nr + i]), r1 = C::of(Rp[nr + i + 1]), sv = C::of(sn[i]);
+    const C Rt = r0 * cs[i] + sv * r1;  // c R[i] + s R[i + 1]
+    Rp[nr + i + 1] = (sv.conj() * r0 - r1 * cs[i]).d2();
+    Rp[nr + i] = Rt.d2();
+  }
+  const C a = C::of(Rp[nr + inner - 1]);
+  const double abs_a = a.abs();
+  double cc;
+  C ss, rho;
+  if (Hbis == 0) {
+    cc = 1;
+    ss = C{0, 0};
+    rho = a;
+  } else if (abs_a == 0) {
+    cc = 0;
+    ss = C{1, 0};
+    rho = C{Hbis, 0};
+  } else {
+    const double rr = hypot(abs_a, Hbis);
+    const C psi = a / abs_a;
+    cc = abs_a / rr;
+    ss = psi * (Hbis / rr);
+    rho = psi * rr;
+  }
+  cs[inner - 1] = cc;
+  sn[inner - 1] = ss.d2();
+  Rp[nr + inner - 1] = rho.d2();
+  const C zk = C::of(zv[inner - 1]);
+  const C zeta = ss.conj() * zk;
+  zv[inner - 1] = (zk * cc).d2();
+  zv[inner] = zeta.d2();
+  st->rnorm = zeta.abs();
+  st->solved = st->rnorm <= st->atol || st->rnorm + 1.0 <= 1.0;
+  st->breakdown = Hbis <= btol;
+  st->hbis = Hbis;
+  st->inv_hbis = Hbis > 0 ? 1.0 / Hbis : 0.0;
+  st->inner = inner;
+  inv_out->x = st->inv_hbis;
+  inv_out->y = 0;
+}
+
 // O[r] = X[r] - Y[r] resp. X[r] + Y[r].
 template <class V>
 __global__ void sub_kernel(const V* __restrict__ X, const V* __restrict__ Y, V* __restrict__ O, long n,
@@ -1872,11 +2099,26 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
   DBuf<double2>& Hdev = P->w_H;
   DBuf<double2>& Ybuf = P->w_Y;
   for (auto* b : {&J0, &J, &LJ, &W}) ensure(*b, ctx, size_t(n));
-  ensure(part, ctx, size_t(std::max<long>(kDotBlocks, ni)));
-  ensure(Hdev, ctx, size_t(maxiter + 5));  // Hessenberg column, wait flag, ‖J0‖², β², 1/β
+  ensure(part, ctx, size_t(std::max<long>(kMG * kDotBlocks, ni)));  // block partials of up to kMG dot products
+  ensure(Hdev, ctx, size_t(maxiter + 5));  // (unused), ‖J0‖², β², 1/β
   ensure(Ybuf, ctx, size_t(3 * ni * (maxiter + 2)));  // σ sums of J0, x0 and each Krylov vector
   std::vector<DBuf<V>>& Vk = Vb;
   const double btol = std::pow(std::numeric_limits<double>::epsilon(), 0.75);
+  {
+    const size_t m1 = size_t(maxiter + 1);
+    for (auto* b : {&P->g_h1, &P->g_h2, &P->g_z}) ensure(*b, ctx, m1);
+    for (auto* b : {&P->g_hsq, &P->g_inv}) ensure(*b, ctx, 1);
+    ensure(P->g_R, ctx, m1 * m1 / 2 + m1);
+    ensure(P->g_sn, ctx, m1);
+    ensure(P->g_cs, ctx, m1);
+    ensure(P->g_st, ctx, 1);
+    if (ensure(P->g_vp, ctx, m1)) {  // a new pointer table: the kept Krylov vectors' pointers again
+      std::vector<void*> ptrs(m1, nullptr);
+      for (size_t k = 0; k < std::min(Vk.size(), m1); ++k) ptrs[k] = Vk[k].p;
+      P->g_vp.upload(ptrs.data(), m1, s);
+      EPSP_CUDA(cudaStreamSynchronize(s));
+    }
+  }
   for (int64_t iT = 0; iT < nT; ++iT) {
     const double T = Tlist[iT];
     long pu = prof_begin(ctx, "ladder_io");
@@ -1915,9 +2157,12 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
       };
       if (solver == EPSP_SOLVER_GMRES) {
         // Krylov.gmres(A, b[, x0]; atol = rtol ‖J0‖, rtol = 0, itmax = maxiter), restart = false,
-        // MGS, Givens (src/ladder.jl:340-353). The host reads the device once per iteration: the
+        // Givens (src/ladder.jl:340-353), the Arnoldi step on the device: classical Gram-Schmidt with
+        // one reorthogonalisation (CGS2; one pass while the basis holds one vector, where it is the
+        // MGS step) in multi-vector passes, and the Givens update, the residual and the stopping test
+        // in FP64 by gmres_givens_kernel. The host reads a small status once per iteration: the
         // first operator application starts before ‖J0‖ and β are known (the first Krylov vector
-        // is scaled on the device), and they come back with the first Hessenberg column. σ of the
+        // is scaled on the device), and they come back with the first status. σ of the
         // solution is Σ y_i σ(v_i) (+ σ(x0)) from the per-vector sums, unless the vertex itself is
         // wanted (stored, or the next Ω's start), when x is formed and summed.
         const bool warm = iO > 0;
@@ -1938,45 +2183,65 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
         }
         rsqrt_coef_kernel<<<1, 32, 0, s>>>(Hdev.p + (warm ? hB2 : hN0), Hdev.p + hC);
         EPSP_LAUNCHED(ctx);
-        if (Vk.empty()) Vk.emplace_back();
-        if (Vk[0].n != size_t(n)) Vk[0].alloc(ctx, size_t(n));
-        scale_kernel<V><<<eb, 256, 0, s>>>(make_double2(0, 0), Hdev.p + hC, r0, Vk[0].p, n, nullptr);
+        // the Krylov vectors and their pointers on the device (allocated as the basis grows, kept)
+        auto vec = [&](int k) -> V* {
+          if (Vk.size() < size_t(k + 1)) Vk.resize(size_t(k + 1));
+          if (Vk[size_t(k)].n != size_t(n)) {
+            Vk[size_t(k)].alloc(ctx, size_t(n));
+            void* pv = Vk[size_t(k)].p;
+            EPSP_CUDA(cudaMemcpyAsync(P->g_vp.p + k, &pv, sizeof(void*), cudaMemcpyHostToDevice, s));
+            EPSP_CUDA(cudaStreamSynchronize(s));  // the pointer's host copy is a local
+          }
+          return Vk[size_t(k)].p;
+        };
+        scale_kernel<V><<<eb, 256, 0, s>>>(make_double2(0, 0), Hdev.p + hC, r0, vec(0), n, nullptr);
         EPSP_LAUNCHED(ctx);
         prof_end(ctx, plp);
         plp = -1;
-        double nJ0 = 0, atol = 0, beta = 0, rNorm = 0;
         std::vector<double> res;
         bool solved = false, breakdown = false, tired = false;
-        int inner = 0, nr = 0;
-        std::vector<cplx> R, sv, z;
-        std::vector<double> cv;
+        int inner = 0;
         std::vector<cplx> Yb(static_cast<size_t>(ny)), Yx0(static_cast<size_t>(ny), cplx(0, 0));
         std::vector<std::vector<cplx>> Yv;
         const bool tc = tc_path(P->path);
-        std::vector<double2> hcol(size_t(maxiter + 5));
+        V* const* vp = reinterpret_cast<V* const*>(P->g_vp.p);
+        GmresDev gs{};
+        int werr = 0;
         while (!(solved || tired || breakdown)) {
           ++inner;
           // a cold start's first Krylov vector is J0 times 1/β: its σ sums are J0's (slot 0) times
           // the same factor, formed on the host once β is read, instead of another pass
           const bool v_from_j0 = inner == 1 && !warm;
-          op(Vk[size_t(inner - 1)].p, W.p);  // q = A v_k
+          op(Vk[size_t(inner - 1)].p, W.p);  // w = A v_k
           if (!needJ && !v_from_j0) cond_launch(P, Vk[size_t(inner - 1)].p, Ybuf.p + (2 + (inner - 1)) * ny);
           long pbl = prof_begin(ctx, "lblas");
-          for (int i = 0; i < inner; ++i) {
-            dot_dev(P, Vk[size_t(i)].p, W.p, n, part, Hdev.p + i);
-            if (i + 1 < inner) {
-              axpy_dev_kernel<V><<<eb, 256, 0, s>>>(W.p, Vk[size_t(i)].p, Hdev.p + i, n, nullptr);
+          // CGS2: h1 = V^H w, w -= V h1; h2 = V^H w, w -= V h2 with ‖w‖^2; m <= kMG vectors per pass.
+          // With one Krylov vector the second pass is left out (one projection: the MGS step itself).
+          const int npass = inner >= 2 ? 2 : 1;
+          for (int pass = 0; pass < npass; ++pass) {
+            double2* hp = pass == 0 ? P->g_h1.p : P->g_h2.p;
+            for (int i0 = 0; i0 < inner; i0 += kMG) {
+              const int m = std::min(kMG, inner - i0);
+              mdot_partial_kernel<V><<<kDotBlocks, 256, 0, s>>>(vp, i0, m, W.p, n, part.p);
               EPSP_LAUNCHED(ctx);
-            } else {  // the last projection and the norm of what remains, in one pass
-              axpy_norm_kernel<V><<<kDotBlocks, 256, 0, s>>>(W.p, Vk[size_t(i)].p, Hdev.p + i, n, part.p);
+              dot_final_kernel<<<unsigned(m), 256, 0, s>>>(part.p, kDotBlocks, nullptr, hp + i0);
               EPSP_LAUNCHED(ctx);
-              dot_final_kernel<<<1, 256, 0, s>>>(part.p, kDotBlocks, nullptr, Hdev.p + inner);
+            }
+            for (int i0 = 0; i0 < inner; i0 += kMG) {
+              const int m = std::min(kMG, inner - i0);
+              const bool last = pass == npass - 1 && i0 + m >= inner;
+              maxpy_kernel<V><<<kDotBlocks, 256, 0, s>>>(W.p, vp, i0, m, hp, n, last ? part.p : nullptr);
               EPSP_LAUNCHED(ctx);
             }
           }
-          if (tc)  // the tensor-core wait flag rides along with the Hessenberg column
-            EPSP_CUDA(cudaMemcpyAsync(Hdev.p + maxiter + 1, P->d_err.p, sizeof(int), cudaMemcpyDeviceToDevice, s));
-          Hdev.download(hcol.data(), hcol.size(), s);
+          dot_final_kernel<<<1, 256, 0, s>>>(part.p, kDotBlocks, nullptr, P->g_hsq.p);
+          EPSP_LAUNCHED(ctx);
+          gmres_givens_kernel<<<1, 32, 0, s>>>(P->g_h1.p, npass == 2 ? P->g_h2.p : nullptr, P->g_hsq.p, Hdev.p + hN0,
+                                               Hdev.p + (warm ? hB2 : hN0), rtol, btol, inner, P->g_R.p, P->g_cs.p,
+                                               P->g_sn.p, P->g_z.p, P->g_st.p, P->g_inv.p);
+          EPSP_LAUNCHED(ctx);
+          P->g_st.download(&gs, 1, s);
+          if (tc) P->d_err.download(&werr, 1, s);
           if (inner == 1) {
             EPSP_CUDA(cudaMemcpyAsync(Yb.data(), Ybuf.p, size_t(ny) * sizeof(cplx), cudaMemcpyDeviceToHost, s));
             if (warm && !needJ)
@@ -1990,85 +2255,50 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
           }
           prof_end(ctx, pbl);
           EPSP_CUDA(cudaStreamSynchronize(s));
-          if (tc) {
-            int e = 0;
-            std::memcpy(&e, &hcol[size_t(maxiter + 1)], sizeof(int));
-            if (e) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
-          }
+          if (werr) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
           if (inner == 1) {
-            nJ0 = std::sqrt(hcol[hN0].x);
-            atol = rtol * nJ0;
-            beta = warm ? std::sqrt(hcol[hB2].x) : nJ0;
-            rNorm = beta;
-            res.push_back(beta);
-            if (beta <= atol || beta == 0) {  // solved at x0: the speculative first step is dropped
+            res.push_back(gs.beta);
+            if (gs.solved_x0) {  // solved at x0: the speculative first step is dropped
               solved = true;
               inner = 0;
               Yv.clear();
               break;
             }
-            z.push_back(beta);
           }
           if (v_from_j0 && !needJ) {  // the factor the device scaled J0 by (rsqrt_coef, in R precision)
-            const double c = 1.0 / std::sqrt(hcol[hN0].x);
-            const double cr = tc ? double(float(c)) : c;
+            const double c1 = 1.0 / gs.nJ0;
+            const double cr = tc ? double(float(c1)) : c1;
             for (long k = 0; k < ny; ++k) Yv[0][size_t(k)] = Yb[size_t(k)] * cr;
           }
-          for (int i = 0; i < inner; ++i) R.push_back(cplx(hcol[size_t(i)].x, hcol[size_t(i)].y));
-          const double Hbis = std::sqrt(hcol[size_t(inner)].x);
-          for (int i = 0; i < inner - 1; ++i) {
-            cplx Rt = cv[size_t(i)] * R[size_t(nr + i)] + sv[size_t(i)] * R[size_t(nr + i + 1)];
-            R[size_t(nr + i + 1)] = std::conj(sv[size_t(i)]) * R[size_t(nr + i)] - cv[size_t(i)] * R[size_t(nr + i + 1)];
-            R[size_t(nr + i)] = Rt;
-          }
-          cplx a = R[size_t(nr + inner - 1)];
-          double abs_a = std::abs(a), cc;
-          cplx ss, rho;
-          if (Hbis == 0) {
-            cc = 1;
-            ss = 0;
-            rho = a;
-          } else if (abs_a == 0) {
-            cc = 0;
-            ss = 1;
-            rho = Hbis;
-          } else {
-            double rr = std::hypot(abs_a, Hbis);
-            cplx psi = a / abs_a;
-            cc = abs_a / rr;
-            ss = psi * (Hbis / rr);
-            rho = psi * rr;
-          }
-          cv.push_back(cc);
-          sv.push_back(ss);
-          R[size_t(nr + inner - 1)] = rho;
-          cplx zeta = std::conj(ss) * z[size_t(inner - 1)];
-          z[size_t(inner - 1)] = cc * z[size_t(inner - 1)];
-          rNorm = std::abs(zeta);
-          res.push_back(rNorm);
-          nr += inner;
-          solved = rNorm <= atol || rNorm + 1.0 <= 1.0;
-          breakdown = Hbis <= btol;
+          res.push_back(gs.rnorm);
+          solved = gs.solved != 0;
+          breakdown = gs.breakdown != 0;
           tired = inner >= maxiter;
-          if (!(solved || tired || breakdown)) {
-            if (Vk.size() < size_t(inner + 1)) Vk.emplace_back();
-            if (Vk[size_t(inner)].n != size_t(n)) Vk[size_t(inner)].alloc(ctx, size_t(n));
-            scale_kernel<V><<<eb, 256, 0, s>>>(make_double2(1.0 / Hbis, 0), nullptr, W.p, Vk[size_t(inner)].p, n, nullptr);
+          if (!(solved || tired || breakdown)) {  // the next Krylov vector w / H[k + 1, k]
+            scale_kernel<V><<<eb, 256, 0, s>>>(make_double2(0, 0), P->g_inv.p, W.p, vec(inner), n, nullptr);
             EPSP_LAUNCHED(ctx);
-            z.push_back(zeta);
           }
         }
-        std::vector<cplx> y = z;
-        for (int i = inner - 1; i >= 0; --i) {
-          int pos = nr + i - inner;
-          for (int jj = inner - 1; jj >= i + 1; --jj) {
-            y[size_t(i)] -= R[size_t(pos)] * y[size_t(jj)];
-            pos -= jj;
+        // y = R \ z (the least-squares solution of Krylov.gmres, FP64, on the host)
+        std::vector<cplx> y(static_cast<size_t>(inner)), Rh(static_cast<size_t>(inner * (inner + 1) / 2));
+        if (inner > 0) {
+          EPSP_CUDA(cudaMemcpyAsync(Rh.data(), P->g_R.p, Rh.size() * sizeof(cplx), cudaMemcpyDeviceToHost, s));
+          EPSP_CUDA(cudaMemcpyAsync(y.data(), P->g_z.p, y.size() * sizeof(cplx), cudaMemcpyDeviceToHost, s));
+          EPSP_CUDA(cudaStreamSynchronize(s));
+        }
+        {
+          const int nr = inner * (inner + 1) / 2;
+          for (int i = inner - 1; i >= 0; --i) {
+            int pos = nr + i - inner;
+            for (int jj = inner - 1; jj >= i + 1; --jj) {
+              y[size_t(i)] -= Rh[size_t(pos)] * y[size_t(jj)];
+              pos -= jj;
+            }
+            if (std::abs(Rh[size_t(pos)]) <= btol)
+              y[size_t(i)] = 0;
+            else
+              y[size_t(i)] /= Rh[size_t(pos)];
           }
-          if (std::abs(R[size_t(pos)]) <= btol)
-            y[size_t(i)] = 0;
-          else
-            y[size_t(i)] /= R[size_t(pos)];
         }
         sigma_from_Y(P, Yb.data(), Om, T, sb + 9 * idx);
         if (needJ) {

@@ -803,10 +803,13 @@ static void check_model_common(const epsp_model* m) {
   for (int64_t k = 0; k < m->nk_i * m->nk_f; ++k)
     if (m->iq_kk[k] < 0 || m->iq_kk[k] >= m->nq) fail(EPSP_EINVAL, "iq_kk out of range");
   if (m->nmult < 0 || (m->nmult > 0 && (!m->mult_ptr || !m->mult_idx))) fail(EPSP_EINVAL, "bad multiplet lists");
+  std::vector<char> seen(size_t(m->ni), 0);
   for (int64_t g = 0; g < m->nmult; ++g) {
     if (m->mult_ptr[g + 1] < m->mult_ptr[g]) fail(EPSP_EINVAL, "multiplet pointers must not decrease");
-    for (int32_t p = m->mult_ptr[g]; p < m->mult_ptr[g + 1]; ++p)
+    for (int32_t p = m->mult_ptr[g]; p < m->mult_ptr[g + 1]; ++p) {
       if (m->mult_idx[p] < 0 || m->mult_idx[p] >= m->ni) fail(EPSP_EINVAL, "multiplet member out of range");
+      if (seen[size_t(m->mult_idx[p])]++) fail(EPSP_EINVAL, "a state belongs to two multiplets");
+    }
   }
 }
 
@@ -906,6 +909,26 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
     P->nmult = m->nmult;
     P->d_mptr = to_device(ctx, m->mult_ptr, size_t(m->nmult + 1));
     P->d_midx = to_device(ctx, m->mult_idx, size_t(m->mult_ptr[m->nmult]));
+  }
+  {  // state groups of the tensor-core epilogue: the multiplets, then every state in none
+    std::vector<int32_t> gptr{0}, gidx;
+    std::vector<char> in_mult(size_t(m->ni), 0);
+    for (int64_t g = 0; g < m->nmult; ++g) {
+      for (int64_t p = m->mult_ptr[g]; p < m->mult_ptr[g + 1]; ++p) {
+        gidx.push_back(int32_t(m->mult_idx[p]));
+        in_mult[size_t(m->mult_idx[p])] = 1;
+      }
+      gptr.push_back(int32_t(gidx.size()));
+    }
+    for (int64_t i = 0; i < m->ni; ++i)
+      if (!in_mult[size_t(i)]) {
+        gidx.push_back(int32_t(i));
+        gptr.push_back(int32_t(gidx.size()));
+      }
+    P->ngroups = long(gptr.size()) - 1;
+    if (P->ngroups > 65535) fail(EPSP_EUNSUPPORTED, "at most 65535 state groups (multiplets and single states)");
+    P->d_gptr = to_device(ctx, gptr);
+    P->d_gidx = to_device(ctx, gidx);
   }
   plog.mark("grid tables");
   kk_matrix_to_device(ctx, P->ws.nodes, P->d_KK);
@@ -1236,7 +1259,9 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
         clamp_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(S.p, Sin_b.p, slab, d_slots.p, d_tp.p);
       EPSP_LAUNCHED(ctx);
       if (P->path == EPSP_PATH_GEMM_BF16) {
-        tc_iterate(P, nA, d_slots.p, slots.data(), d_tp.p, nullptr, Snew.p);
+        // Σ_new, its multiplet average, max|ΔΣ|, Σ ← Σ_new and the spectral terms from the
+        // Kramers-Kronig product's epilogue (so no multiplet, spectral-prep or err/copy pass below)
+        tc_iterate(P, nA, d_slots.p, slots.data(), d_tp.p, nullptr, S.p, P->w_Pf.p, d_err, d_minA);
         EPSP_CUDA(cudaMemcpyAsync(d_tcerr, tc_err_ptr(P), sizeof(int), cudaMemcpyDeviceToDevice, s));
       } else {
         for (int a = 0; a < nA; ++a) {
@@ -1250,16 +1275,13 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
           prof_end(ctx, pk);
         }
       }
-      if (P->nmult > 0) {
+      if (P->nmult > 0 && !f32_spec) {
         multiplet_kernel<<<dim3(div_up(size_t(nw * P->nmult), 256), unsigned(nA)), 256, 0, s>>>(
             Snew.p, int(nw), slab, d_slots.p, P->d_mptr.p, P->d_midx.p, P->nmult);
         EPSP_LAUNCHED(ctx);
       }
       long psp = prof_begin(ctx, "spectral");
-      if (f32_spec) {
-        spectral_prep_f32_kernel<<<dim3(div_up(size_t(nw), 256), unsigned(ni), unsigned(nA)), 256, 0, s>>>(
-            Snew.p, int(nw), slab, d_slots.p, P->d_ws.p, P->d_eps_i.p, P->w_Pf.p, d_minA);
-        EPSP_LAUNCHED(ctx);
+      if (f32_spec) {  // the per-node terms came from the Kramers-Kronig epilogue
         spectral_ad_f32_kernel<<<dim3(unsigned(spec_nab), unsigned(spec_nch), unsigned(nA)), 256, 0, s>>>(
             P->w_Pf.p, int(nw), slab, P->d_jsp.p, P->d_dspf.p, P->d_tspf.p, P->d_Waf.p, P->d_w_if.p, int(nwa), int(ni),
             P->w_Dpart.p, P->w_Cpart.p);
@@ -1294,11 +1316,10 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
         EPSP_LAUNCHED(ctx);
         prof_end(ctx, pm);
       }
-      if (P->path == EPSP_PATH_GEMM_BF16)
-        err_copy_kernel<true><<<dim3(eb, unsigned(nA)), 256, 0, s>>>(Snew.p, S.p, slab, d_slots.p, d_err);
-      else
+      if (P->path != EPSP_PATH_GEMM_BF16) {  // (the tensor-core epilogue took err and the copy)
         err_copy_kernel<false><<<dim3(eb, unsigned(nA)), 256, 0, s>>>(Snew.p, S.p, slab, d_slots.p, d_err);
-      EPSP_LAUNCHED(ctx);
+        EPSP_LAUNCHED(ctx);
+      }
     };
     // iteration 1 replays a graph a previous run captured with the same key; otherwise it runs
     // eagerly (first launches set kernel attributes) and iteration 2 captures

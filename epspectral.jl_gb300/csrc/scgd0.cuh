@@ -30,6 +30,9 @@ struct Scgd0Plan {
   CellTableDev ct{};
   long nmult = 0;
   DBuf<int32_t> d_mptr, d_midx;
+  // every state in one group: the multiplets, then the states in none (CSR, members in order)
+  long ngroups = 0;
+  DBuf<int32_t> d_gptr, d_gidx;
   // DIRECT_FP64
   int64_t nf_chunk = 1;
   DBuf<double> d_g2t, d_wqt, d_eps_f, d_w_f;
@@ -77,11 +80,14 @@ void tc_kk_assemble(Scgd0Plan* P, double2* d_Snew);
 void tc_reserve(Scgd0Plan* P, long nT);
 // The temperatures tc_reserve's buffers hold now.
 long tc_capacity(Scgd0Plan* P);
-// Σ_new of nA active temperatures at once: slot a reads the clamped Σ_in + a nω ni and writes
-// Snew_all + slots_h[a] nω ni (temperature index); per-temperature T and μ from tp (device).
-// With d_Sin_b null, the slots' clamped Σ are already in the FP32 buffer tc_sigma_f32 returns.
+// One iteration of nA active temperatures at once, up to the spectral functions: slot a reads the
+// clamped Σ_in + a nω ni; per-temperature T and μ from tp (device). With d_Sin_b null, the slots'
+// clamped Σ are already in the FP32 buffer tc_sigma_f32 returns. The Kramers-Kronig product's
+// epilogue writes Σ_new (multiplet-averaged) into S_all + slots_h[a] nω ni (temperature index),
+// max |Σ_new - Σ| into d_errbits[temperature] (bit patterns, atomic maximum), the spectral
+// functions' per-node terms into d_P + a nω ni, and +inf into d_minA[temperature].
 void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, const TParams* d_tp,
-                const double2* d_Sin_b, double2* d_Snew_all);
+                const double2* d_Sin_b, double2* d_S_all, float4* d_P, unsigned long long* d_errbits, double* d_minA);
 // The FP32 form of the clamped Σ of every reserved temperature ({Re hi, Re lo, Im, 0}, slot-major).
 float4* tc_sigma_f32(Scgd0Plan* P);
 // Fails with EPSP_EDEVICE_TIMEOUT if a tensor-core GEMM's bounded wait ran out (synchronises).

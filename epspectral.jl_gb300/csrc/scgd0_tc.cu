@@ -257,18 +257,77 @@ __global__ void finalize_fm_batch_kernel(const float* __restrict__ part, int nw,
   }
 }
 
-// Σ_new of temperature slots[a] = Σ_s part[s][a slab + k] + i ImS[a][k] (the KK product's columns
-// are the slots' states in order).
-__global__ void finalize_kk_batch_kernel(const float* __restrict__ part, long slab, int splits, long stride,
-                                         const double* __restrict__ ImS, const int* __restrict__ slots,
-                                         double2* __restrict__ Snew_all) {
-  const long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= slab) return;
-  const int a = blockIdx.y;
-  const long src = slab * a + k;
-  float acc = 0.f;
-  for (int p = 0; p < splits; ++p) acc += part[src + stride * p];
-  Snew_all[slab * slots[a] + k] = make_double2(double(acc), ImS[src]);
+// The Kramers-Kronig product's epilogue and the rest of the iteration's tail, in one pass over its
+// split-K partials (src/scgd0.jl:287-301, 326-328): per state group of slot a -- a degenerate
+// multiplet, or a single state -- Σ_new(ω_j) = Σ_s part[s] + i ImΣ of every member (the partials in
+// ascending order), averaged over the members of a multiplet (their sum in member order divided by
+// the count); then per member: err = max |Σ_new - Σ| over the slot's temperature (FP64 differences,
+// FP32 magnitude, the maximum taken on the bit patterns as err_copy_kernel does), Σ ← Σ_new, and the
+// spectral functions' per-node terms P[i][j] = (ε_i - ω_j + ReΣ_j, ReΣ_{j+1} - ReΣ_j, ImΣ_j, ImΣ_{j+1})
+// of spectral_prep_f32_kernel (ImΣ_{j+1}, ReΣ_{j+1} = those of j at the last node). Bitwise the
+// results of the separate kernels. Groups: CSR (gptr, gidx), members in order. Grid (nω / 255,
+// groups, slots), 256 threads: thread t takes node j = 255 blockIdx.x + t; the last thread's node
+// is the next block's first, formed again to give node 254 its neighbour.
+__global__ void __launch_bounds__(256) kk_epilogue_kernel(const float* __restrict__ part, int splits, long stride,
+                                                          const double* __restrict__ ImS_b, int nw, long slab,
+                                                          const int* __restrict__ slots, const int32_t* __restrict__ gptr,
+                                                          const int32_t* __restrict__ gidx, const double* __restrict__ ws,
+                                                          const double* __restrict__ eps_i, double2* __restrict__ S_all,
+                                                          float4* __restrict__ Pall,
+                                                          unsigned long long* __restrict__ errbits_all,
+                                                          double* __restrict__ minA_all) {
+  __shared__ double2 sh[256];
+  __shared__ unsigned long long she[256];
+  const int a = blockIdx.z, t = slots[a];
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)  // the minimum of spectral_fin starts at +inf
+    minA_all[t] = INFINITY;
+  const int j = blockIdx.x * 255 + threadIdx.x;
+  const bool in = j < nw;
+  const int p0 = gptr[blockIdx.y], p1 = gptr[blockIdx.y + 1];
+  double sr = 0, si = 0;
+  if (in) {
+    for (int p = p0; p < p1; ++p) {
+      const long src = slab * a + j + long(nw) * gidx[p];
+      float acc = 0.f;
+      for (int q = 0; q < splits; ++q) acc += part[src + stride * q];
+      if (p1 - p0 == 1) {
+        sr = double(acc);
+        si = ImS_b[src];
+      } else {
+        sr += double(acc);
+        si += ImS_b[src];
+      }
+    }
+    if (p1 - p0 > 1) {
+      const double len = double(p1 - p0);
+      sr /= len;
+      si /= len;
+    }
+  }
+  sh[threadIdx.x] = make_double2(sr, si);
+  __syncthreads();
+  unsigned long long e = 0;
+  if (in && threadIdx.x < 255) {
+    const double2 lo = sh[threadIdx.x];
+    const double2 hi = j + 1 < nw ? sh[threadIdx.x + 1] : lo;
+    double2* S = S_all + slab * t;
+    for (int p = p0; p < p1; ++p) {
+      const int i = gidx[p];
+      const long k = j + long(nw) * i;
+      const double2 b = S[k];
+      const double d = double(hypotf(float(lo.x - b.x), float(lo.y - b.y)));
+      e = max(e, (unsigned long long)__double_as_longlong(d));
+      S[k] = lo;
+      Pall[slab * a + k] = make_float4(float(eps_i[i] - ws[j] + lo.x), float(hi.x - lo.x), float(lo.y), float(hi.y));
+    }
+  }
+  she[threadIdx.x] = e;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st) she[threadIdx.x] = max(she[threadIdx.x], she[threadIdx.x + st]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicMax(errbits_all + t, she[0]);
 }
 
 static long pad64(long x) { return (x + 63) / 64 * 64; }
@@ -429,7 +488,7 @@ long tc_capacity(Scgd0Plan* P) { return P->tc->ImS_b.p ? P->tc->capT : 0; }
 float4* tc_sigma_f32(Scgd0Plan* P) { return P->tc->Sf.p; }
 
 void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, const TParams* d_tp,
-                const double2* d_Sin_b, double2* d_Snew_all) {
+                const double2* d_Sin_b, double2* d_S_all, float4* d_P, unsigned long long* d_errbits, double* d_minA) {
   (void)slots_h;
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
@@ -469,9 +528,10 @@ void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, co
   const long N2 = long(nA) * ni;
   int sp2 = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(N2), int(nw), T->part.p, nw, nw * N2, 16, T->err.p,
                            "tc_kk", kKbCap);
-  pf = prof_begin(ctx, "finalize");
-  finalize_kk_batch_kernel<<<dim3(eb, unsigned(nA)), 256, 0, s>>>(T->part.p, slab, sp2, nw * N2, T->ImS_b.p, d_slots,
-                                                                   d_Snew_all);
+  pf = prof_begin(ctx, "kk_epilogue");
+  kk_epilogue_kernel<<<dim3(div_up(size_t(nw), 255), unsigned(P->ngroups), unsigned(nA)), 256, 0, s>>>(
+      T->part.p, sp2, nw * N2, T->ImS_b.p, int(nw), slab, d_slots, P->d_gptr.p, P->d_gidx.p, P->d_ws.p, P->d_eps_i.p,
+      d_S_all, d_P, d_errbits, d_minA);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pf);
 }
