@@ -451,6 +451,7 @@ def run_ours(args, world, rank, local):
         max_abs_dsigma_without_warm_start_eV=float(np.max(np.abs(r_cold["sigma"] - r64["sigma"]))),
         abs_dmu_eV=float(abs(r["mu"][0] - r64["mu"][0])),
         rel_sigma_ladder=float(np.linalg.norm(l["sigma_ladder"] - l64["sigma_ladder"]) / np.linalg.norm(l64["sigma_ladder"])))
+    out["gmres_tight"] = gmres_tight(s, ctx, T, r, r64)
     out["batched_c3"] = batched_c3(s, ctx, ws)
     flush_l2(local)
     out["cpu_baseline"] = cpu_baseline(s, T, r64, plain["fp64_scgd0_iters"], plain["fp64_ladder_gmres_iters"])
@@ -525,6 +526,29 @@ def run_e2e_cold(path: str, local: int):
     t = e2e_calls(s, ws, ctx, T, occ, mu0)
     print(json.dumps(dict(value=t, unit="s", note="fresh process: plan set-ups incl. the autotuner, first launches")),
           flush=True)
+
+
+def gmres_tight(s, ctx, T, r, r64, rtol=1e-10) -> dict:
+    """The ladder solve at Ω = 0.1 eV to a tight tolerance, so that GMRES runs several Arnoldi steps
+    (8 on this model at 1e-10): the timed path (TF32 contraction, FP32 vertices, the Arnoldi step
+    on the device) on its scGD0 Σ against the plain FP64 path on the FP64 Σ. Device seconds."""
+    from epspectral_gb300 import api
+    lp = api.LadderPlan(s, path=LADDER_PATH, omega_acoustic=W_AC, ctx=ctx)
+    lp.run(r["sigma"], r["mu"], [T], [OMEGA], rtol=rtol, maxiter=60)  # warm-up (Krylov vectors allocated)
+    ctx.timer_begin()
+    lt = lp.run(r["sigma"], r["mu"], [T], [OMEGA], rtol=rtol, maxiter=60)
+    t_tc = ctx.timer_end() / 1e3
+    lp.close()
+    lp64 = api.LadderPlan(s, path="gemm_fp64", omega_acoustic=W_AC, ctx=ctx)
+    ctx.timer_begin()
+    l64 = lp64.run(r64["sigma"], r64["mu"], [T], [OMEGA], rtol=rtol, maxiter=60)
+    t_64 = ctx.timer_end() / 1e3
+    lp64.close()
+    n_tc, n_64 = int(lt["niter"][0, 0]), int(l64["niter"][0, 0])
+    return dict(rtol=rtol, niter=n_tc, s=t_tc, s_per_iter=t_tc / max(1, n_tc), converged=bool(lt["converged"][0, 0]),
+                fp64_niter=n_64, fp64_s=t_64, fp64_s_per_iter=t_64 / max(1, n_64),
+                rel_sigma_vs_fp64=float(np.linalg.norm(lt["sigma_ladder"] - l64["sigma_ladder"]) /
+                                        np.linalg.norm(l64["sigma_ladder"])))
 
 
 def batched_c3(s, ctx, ws) -> dict:
