@@ -950,6 +950,15 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
     P->d_w_f = to_device(ctx, m->w_f, size_t(nf));
     P->d_f_to_i = to_device(ctx, m->f_to_i, size_t(nf));
     EPSP_CUDA(cudaStreamSynchronize(s));
+  } else if (P->path == EPSP_PATH_GEMM_BF16 && [&] {
+               std::vector<double> w;
+               return !dispersionless(m, w);
+             }()) {
+    // dispersive modes on the tensor-core path: the Fan-Migdal sum term by term in FP32, the rest of
+    // the iteration (Kramers-Kronig product and its epilogue, spectral functions, μ) as below
+    tc_setup_dispersive(P, m);
+    tc_setup(P);
+    EPSP_CUDA(cudaStreamSynchronize(s));
   } else if (P->path == EPSP_PATH_GEMM_FP64 || P->path == EPSP_PATH_GEMM_BF16) {
     std::vector<double> wnu;
     if (!dispersionless(m, wnu))
@@ -1095,6 +1104,10 @@ void scgd0_imsigma(Scgd0Plan* P, const double2* d_Sin, double mu, double T, doub
       EPSP_LAUNCHED(ctx);
       prof_end(ctx, pi);
     }
+    return;
+  }
+  if (P->disp) {
+    tc_imsigma_disp(P, d_Sin, mu, T, d_ImS);
     return;
   }
   occ_table_kernel<<<div_up(size_t(nw * nm), 256), 256, 0, s>>>(P->d_ws.p, int(nw), P->d_wnu.p, int(nm), mu, T, P->w_ac,

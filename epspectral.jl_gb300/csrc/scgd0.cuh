@@ -42,6 +42,17 @@ struct Scgd0Plan {
   long nc = 0;
   DBuf<double> d_wnu, d_epsc, d_G, d_Fa, d_Fe, d_Kt;
   DBuf<int32_t> d_colc;
+  // GEMM_BF16 with dispersive modes: the Fan-Migdal sum term by term in FP32 (fm_disp_f32_kernel):
+  // w_f g2 [ν f, i] (FP32), ωph, the pair table and its indices, ε_f, f_to_i, the nodes
+  // as float pairs with their neighbouring cells' inverse widths, the bucket table's origin and scale
+  bool disp = false;
+  long nk_i = 0, ntab = 0;
+  float x0f = 0.f, inv_hf = 0.f;
+  DBuf<float> d_gwf;
+  DBuf<double> d_wph;
+  DBuf<int32_t> d_iq, d_iksi, d_iksf, d_fti;
+  DBuf<double> d_epsf;
+  DBuf<float4> d_wtab;
   // cells of ω ± ω_ν for every (ω, ν): [2][nω·nm] lower node, weight and point (absorption, emission)
   DBuf<int32_t> d_cell_j;
   DBuf<double> d_cell_t, d_cell_x;
@@ -74,7 +85,12 @@ struct Scgd0Plan {
 
 // Tensor-core pieces of the GEMM_BF16 path, in scgd0_tc.cu.
 void tc_setup(Scgd0Plan* P);
+// The FP32 term-by-term Fan-Migdal sum's tables for a model with dispersive modes (before tc_setup).
+void tc_setup_dispersive(Scgd0Plan* P, const epsp_model* m);
 void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS);
+void tc_imsigma_disp(Scgd0Plan* P, const double2* d_Sin, double mu, double T, double* d_ImS);
+// The g2 upload of the term-by-term sums: g2 [nm, ni, nf] of any dtype to [nm nf, ni] FP64 (scgd0.cu).
+void upload_g2_permuted(Ctx* ctx, const epsp_model* m, DBuf<double>& g2t);
 void tc_kk_assemble(Scgd0Plan* P, double2* d_Snew);
 // Buffers and tensor maps for up to nT temperatures in one iteration.
 void tc_reserve(Scgd0Plan* P, long nT);

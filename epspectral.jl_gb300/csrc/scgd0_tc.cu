@@ -45,6 +45,14 @@ __global__ void split_df_kernel(const double* __restrict__ x, long n, float2* __
   if (k < n) out[k] = split_df(x[k]);
 }
 
+// gw[vf + nvf i] = w_f[f] g2t[vf + nvf i] rounded to FP32 (vf = ν + nm f).
+__global__ void gw_f32_kernel(const double* __restrict__ g2t, const double* __restrict__ w_f, int nm, long nvf, long ni,
+                              float* __restrict__ gw) {
+  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= nvf * ni) return;
+  gw[k] = float(w_f[(k % nvf) / nm] * g2t[k]);
+}
+
 __global__ void to_f32_kernel(const double* __restrict__ x, long n, float* __restrict__ out) {
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k < n) out[k] = float(x[k]);
@@ -163,6 +171,191 @@ __global__ void __launch_bounds__(256, 6) kbuild_bf16_kernel(int nw, long slab, 
 }
 
 static size_t kbuild_smem_bytes(long nm) { return size_t(kKbCols * nm * (kKbW + 1)) * sizeof(float); }
+
+// ---- dispersive phonons: the Fan-Migdal sum term by term in FP32 ----
+// The reference's element sum (src/scgd0_kernel.jl:27-39, 59-86) with ωq gathered per pair
+// (ωq[ν, f, i] = ωph[ν, iq_kk[iks_i[i], iks_f[f]]], src/scgd0.jl:270): for each (ω, i) and every
+// (ν, f) with ωq >= ω_acoustic, w_f g2 {Im[1/(x_a - ε_f - Σ_in(x_a))] (n + f(x_a - μ)) +
+// Im[1/(x_e - ε_f - Σ_in(x_e))] (n + 1 - f(x_e - μ))}, x_a,e = ω ± ωq. FP32 arithmetic with float
+// pairs where the value cancels: x = ω ± ωq, ε_f and Re Σ are float pairs and Re z = (x - ε) - Re Σ(x)
+// is formed exactly on them (re_z), as in kbuild_bf16_kernel; the cell of x (the O(1) bucket table of
+// _interp_linear_grid, flat outside the grid: a bucket, then one node entry that carries the inverse
+// widths of both its cells, so the weight needs no division) is found on the pair; the weight, Im Σ,
+// the reciprocal and the occupations are FP32, the Fermi factors from exp((ω - μ)/T) exp(±ωq/T)
+// (one exponential per thread and one per staged mode instead of two per term; evaluated directly
+// where a factor leaves FP32's range), and each thread sums its terms in FP32 runs of one tile
+// (256 pairs (ν, f)) added into FP64. The (ν, f) tile of the block's outer state -- w_f g2, ωq,
+// n(ωq), exp(±ωq/T), ε_f, the Σ column -- is staged in shared memory by the block; the node table
+// and the bucket table too, when they fit.
+// Grid (nω / 256, ni, slots), 256 threads, thread = node ω. Slot a reads Σ_in from Sf_all + a nω ni
+// and T, μ from tp[slots[a]]. Output: with ImS_b, ImΣ of the slot (ImS_b + a nω ni) and its BF16
+// split as the Kramers-Kronig product's B operand (rows a ni + i, columns ω, stride Kp2), as
+// finalize_fm_batch_kernel writes them; else ImΣ added into add_out [nω, ni] (slot 0).
+constexpr int kFdTile = 256;
+
+__device__ __forceinline__ float2 pair_add(float2 a, float2 b) {  // a + b as a float pair
+  float e;
+  const float s = two_sum(a.x, b.x, e);
+  e += a.y + b.y;
+  const float h = s + e;
+  return make_float2(h, e - (h - s));
+}
+__device__ __forceinline__ bool pair_le(float2 a, float2 b) {  // a <= b for float pairs (normalised)
+  return a.x < b.x || (a.x == b.x && a.y <= b.y);
+}
+__device__ __forceinline__ float occ_fermion_f(float e, float T) {  // occ_fermion, src/utils.jl:14-22
+  if (T > 1.4901161193847656e-08f) return 1.f / (__expf(e / T) + 1.f);
+  return e > 0.f ? 0.f : (e < 0.f ? 1.f : 0.5f);
+}
+__device__ __forceinline__ float occ_boson_f(float e, float T) {  // occ_boson, src/utils.jl:24-38
+  if (T > 1.4901161193847656e-08f) return e == 0.f ? -0.5f : 1.f / expm1f(e / T);
+  return e > 0.f ? 0.f : (e == 0.f ? -0.5f : -1.f);
+}
+
+template <bool kSmemTab>
+__global__ void __launch_bounds__(kFdTile) fm_disp_f32_kernel(
+    int nw, long slab, const float4* __restrict__ Sf_all, const float4* __restrict__ wtab_g,
+    const int32_t* __restrict__ jtab_g, float x0, float inv_h, long ntab, const float* __restrict__ gw,
+    const double* __restrict__ wph, const int32_t* __restrict__ iq_kk, const int32_t* __restrict__ iks_i,
+    const int32_t* __restrict__ iks_f, long nk_i, const double* __restrict__ eps_f, const int32_t* __restrict__ f_to_i,
+    int nm, long nvf, int ni, double w_ac, const int* __restrict__ slots, const TParams* __restrict__ tp,
+    double* __restrict__ ImS_b, __nv_bfloat16* __restrict__ Im0, __nv_bfloat16* __restrict__ Im1,
+    __nv_bfloat16* __restrict__ Im2, long Kp2, double* __restrict__ add_out) {
+  extern __shared__ __align__(16) unsigned char fd_tab[];  // kSmemTab: node table [nw] float4, then the buckets
+  // the staged (ν, f) pairs: {w_f g2, n(ωq), exp(ωq/T), exp(-ωq/T)}, {ε - ωq, ε + ωq} as float pairs,
+  // {ωq as a float pair, the Σ column's offset, 0}
+  __shared__ float4 s_a[kFdTile], s_e[kFdTile], s_q[kFdTile];
+  const float4* wtab = wtab_g;
+  const int32_t* jtab = jtab_g;
+  if constexpr (kSmemTab) {
+    float4* sw = reinterpret_cast<float4*>(fd_tab);
+    int32_t* sj = reinterpret_cast<int32_t*>(fd_tab + sizeof(float4) * size_t(nw));
+    for (int k = threadIdx.x; k < nw; k += kFdTile) sw[k] = wtab_g[k];
+    for (long k = threadIdx.x; k < ntab; k += kFdTile) sj[k] = jtab_g[k];
+    wtab = sw;
+    jtab = sj;
+  }
+  const int i = blockIdx.y, a = blockIdx.z;
+  const int iw = blockIdx.x * kFdTile + threadIdx.x;
+  const bool on = iw < nw;
+  const TParams q = tp[slots[a]];
+  const float T = float(q.T);
+  const bool warm = T > 1.4901161193847656e-08f;
+  const float invT = warm ? 1.f / T : 0.f;
+  const float2 mu = split_df(q.mu);
+  const float4* Sf = Sf_all + slab * a;
+  const float4 wn = wtab_g[on ? iw : 0];
+  const float2 w = make_float2(wn.x, wn.y);
+  // exp((ω - μ)/T) of the thread's node: f(ω ± ωq - μ) = 1 / (E exp(±ωq/T) + 1); a node whose E
+  // leaves FP32's range takes the exponential of each term directly
+  const float wm = (w.x - mu.x) + (w.y - mu.y);
+  const float E = warm ? __expf(wm * invT) : 0.f;
+  const bool Eok = warm && E > 0.f && E < INFINITY;
+  const int ntab_i = int(ntab), jmax = nw - 2;
+  const int ki = iks_i[i];
+  // one side of a term, x = ω + sg ωq (sg = ±1), with em = ε - sg ωq: Im 1/(x - ε - Σ(x)) times its
+  // occupation bracket
+  auto side = [&](const float4* col, float sgwq_hi, float sgwq_lo, float2 em, float nq, float eq, bool absorb) -> float {
+    const float xh = w.x + sgwq_hi;
+    const float v = fminf(fmaxf((xh - x0) * inv_h, -1.f), float(ntab_i)) - 0.5f;
+    // the bucket floor((x - x0) / h) in 32-bit integer arithmetic (1.5 2^23 added: the integer part
+    // lands in the mantissa; |v| < 2^22); an off-by-one bucket at a bucket edge still picks the
+    // cell whose value is continuous there
+    int b = __float_as_int(v + 12582912.f) - 0x4B400000;
+    b = min(max(b, 0), ntab_i - 1);
+    const int c = jtab[b];
+    const float4 wc = wtab[c];  // node c: (hi, lo, 1 / (w[c+1] - w[c]), 1 / (w[c] - w[c-1]))
+    const float dx = ((w.x - wc.x) + sgwq_hi) + ((w.y - wc.y) + sgwq_lo);
+    const bool below = dx < 0.f;
+    int j = below ? c - 1 : c;
+    float t = below ? fmaf(dx, wc.w, 1.f) : dx * wc.z;
+    if (j < 0 || j > jmax) {  // outside the grid the value is flat (the first or the last node)
+      t = j < 0 ? 0.f : 1.f;
+      j = j < 0 ? 0 : jmax;
+    }
+    const float4 lo = col[j], hi = col[j + 1];
+    // Re z = (x - ε) - Re Σ(x) = (ω - em) - Re Σ(x), exact on the float pairs
+    const float zr = re_z(w, em, lo, hi, t);
+    const float si = fmaf(t, hi.z - lo.z, lo.z);  // Im Σ(x)
+    const float g = __fdividef(si, fmaf(zr, zr, si * si));
+    float y = E * eq;
+    if (!Eok || y != y) {  // a factor out of range (stored as NaN), or T -> 0
+      const float xm = (xh - mu.x) + ((w.y + sgwq_lo) - mu.y);
+      y = warm ? __expf(xm * invT) : (xm > 0.f ? INFINITY : (xm < 0.f ? 0.f : 1.f));
+    }
+    const float f = __fdividef(1.f, y + 1.f);
+    return g * (absorb ? nq + f : nq + 1.f - f);
+  };
+  double acc = 0.0;
+  for (long t0 = 0; t0 < nvf; t0 += kFdTile) {
+    const long vf = t0 + threadIdx.x;
+    __syncthreads();  // the previous tile's readers are done (and, first, the tables are staged)
+    // below ω_acoustic (and past the end) no term: zero coupling, the first column as a stand-in and
+    // ε - ωq = -1e30, so that Re z^2 overflows and Im 1/z is exactly 0 whatever the column holds
+    float4 sa = make_float4(0.f, 0.f, 0.f, 0.f), se = make_float4(-1e30f, 0.f, -1e30f, 0.f), sq = sa;
+    if (vf < nvf) {
+      const int nu = int(vf % nm);
+      const long f = vf / nm;
+      const double wq = wph[nu + long(nm) * iq_kk[ki + nk_i * long(iks_f[f])]];
+      if (!(wq < w_ac)) {
+        const double e = eps_f[f];
+        const float wqf = float(wq);
+        const float2 ea = split_df(e - wq), ee = split_df(e + wq), wqp = split_df(wq);
+        float eq = warm ? __expf(wqf * invT) : 0.f, ieq = warm ? __expf(-wqf * invT) : 0.f;
+        if (!(eq < INFINITY) || !(ieq > 0.f)) eq = ieq = __int_as_float(0x7fc00000);  // out of range: NaN
+        sa = make_float4(gw[vf + nvf * i], occ_boson_f(wqf, T), eq, ieq);
+        se = make_float4(ea.x, ea.y, ee.x, ee.y);
+        sq = make_float4(wqp.x, wqp.y, __int_as_float(nw * f_to_i[f]), 0.f);
+      }
+    }
+    s_a[threadIdx.x] = sa;
+    s_e[threadIdx.x] = se;
+    s_q[threadIdx.x] = sq;
+    __syncthreads();
+    float run0 = 0.f, run1 = 0.f;
+    if (on) {
+      const int nt = int(min(long(kFdTile), nvf - t0));
+#pragma unroll 2
+      for (int k = 0; k < nt; ++k) {
+        const float4 A = s_a[k], Ee = s_e[k], Q = s_q[k];
+        const float4* col = Sf + __float_as_int(Q.z);
+        const float va = side(col, Q.x, Q.y, make_float2(Ee.x, Ee.y), A.y, A.z, true);
+        const float ve = side(col, -Q.x, -Q.y, make_float2(Ee.z, Ee.w), A.y, A.w, false);
+        const float v = A.x * (va + ve);
+        if (k & 1)
+          run1 += v;
+        else
+          run0 += v;
+      }
+    }
+    acc += double(run0) + double(run1);
+  }
+  if (!on) return;
+  const long k = iw + long(nw) * i;
+  if (ImS_b) {
+    ImS_b[slab * a + k] = acc;
+    __nv_bfloat16 p[3];
+    split_bf16_n(float(acc), 3, p);
+    const long o = (long(a) * ni + i) * Kp2 + iw;
+    Im0[o] = p[0];
+    Im1[o] = p[1];
+    Im2[o] = p[2];
+  } else {
+    add_out[k] += acc;
+  }
+}
+
+// The node table of fm_disp_f32_kernel: node j as (hi, lo, 1 / (w[j+1] - w[j]), 1 / (w[j] - w[j-1]))
+// (0 past the ends).
+__global__ void fd_node_table_kernel(const double* __restrict__ ws, int nw, float4* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nw) return;
+  const float2 p = split_df(ws[j]);
+  const float up = j + 1 < nw ? float(1.0 / (ws[j + 1] - ws[j])) : 0.f;
+  const float dn = j > 0 ? float(1.0 / (ws[j] - ws[j - 1])) : 0.f;
+  out[j] = make_float4(p.x, p.y, up, dn);
+}
+
 
 // out_p[r * ld + c] = part p of S(r, c) for c < cols, 0 for cols <= c < ld, with S(r, c) =
 // S[c + ldc r] (transposed = false: rows of the output are columns of the column-major S) or
@@ -353,6 +546,23 @@ void tc_setup(Scgd0Plan* P) {
   T->Kp = pad64(nk);
   T->Kp2 = pad64(nw);
   if (nw > (1l << 30) || ni > (1l << 30) || nk > (1l << 30)) fail(EPSP_EINVAL, "sizes beyond the 32-bit tile grid");
+  if (P->disp) {  // the Kramers-Kronig map's operands only: the Fan-Migdal sum is fm_disp_f32_kernel
+    for (int p = 0; p < kNs; ++p) {
+      T->KK[p].alloc(ctx, size_t(nw * T->Kp2));
+      T->Im[p].alloc(ctx, size_t(ni * T->Kp2));
+    }
+    T->err.alloc(ctx, 1);
+    T->err.zero(s);
+    split3_rows_kernel<<<div_up(size_t(nw * T->Kp2), 256), 256, 0, s>>>(P->d_KK.p, nw, nw, nw, T->Kp2, true, T->KK[0].p,
+                                                                        T->KK[1].p, T->KK[2].p);
+    EPSP_LAUNCHED(ctx);
+    tc_gemm_shape(ctx, int(nw), int(ni), int(nw), 16, kNs, &T->bn2, &T->splits2, kKbCap);
+    T->part.alloc(ctx, size_t(T->splits2) * size_t(nw * ni));
+    T->Sf.alloc(ctx, size_t(nw * ni));
+    T->opKK = operand(T->KK, nw, nw, T->Kp2, kTcBM);
+    T->opIm = operand(T->Im, ni, nw, T->Kp2, T->bn2);
+    return;
+  }
   if (kbuild_smem_bytes(P->nm) > size_t(227 * 1024))
     fail(EPSP_EUNSUPPORTED, "the BF16 scGD0 path takes at most 427 modes; use EPSP_PATH_GEMM_FP64");
   if (kbuild_smem_bytes(P->nm) > size_t(48 * 1024))
@@ -410,6 +620,93 @@ static void check_err(Scgd0Plan* P) {
   if (e) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
 }
 
+// fm_disp_f32_kernel over nA slots (Σ_in in T->Sf): into ImS_b and the Kramers-Kronig operand, or
+// added into add_out (one slot).
+static void launch_fm_disp(Scgd0Plan* P, int nA, const int* d_slots, const TParams* d_tp, double* ImS_b,
+                           double* add_out) {
+  Ctx* ctx = P->ctx;
+  auto* T = P->tc.get();
+  const long nw = P->nw, ni = P->ni;
+  // the grid nodes and the bucket table in shared memory when they fit 96 KB
+  const size_t tab = sizeof(float4) * size_t(nw) + sizeof(int32_t) * size_t(P->ntab);
+  const bool smem = tab <= (size_t(96) << 10);
+  const dim3 grid(div_up(size_t(nw), kFdTile), unsigned(ni), unsigned(nA));
+  static size_t smem_set = 0;
+  if (smem && tab > smem_set) {
+    EPSP_CUDA(cudaFuncSetAttribute(fm_disp_f32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(tab)));
+    smem_set = tab;
+  }
+  auto args = [&](auto kern, size_t bytes) {
+    kern<<<grid, kFdTile, bytes, ctx->stream>>>(
+        int(nw), nw * ni, T->Sf.p, P->d_wtab.p, P->d_jtab.p, P->x0f, P->inv_hf, P->ntab, P->d_gwf.p, P->d_wph.p,
+        P->d_iq.p, P->d_iksi.p, P->d_iksf.p, P->nk_i, P->d_epsf.p, P->d_fti.p, int(P->nm), P->nm * P->nf, int(ni),
+        P->w_ac, d_slots, d_tp, ImS_b, T->Im[0].p, T->Im[1].p, T->Im[2].p, T->Kp2, add_out);
+  };
+  if (smem)
+    args(fm_disp_f32_kernel<true>, tab);
+  else
+    args(fm_disp_f32_kernel<false>, size_t(0));
+  EPSP_LAUNCHED(ctx);
+}
+
+// One Fan-Migdal sum at (μ, T) for a model with dispersive modes, added into d_ImS.
+void tc_imsigma_disp(Scgd0Plan* P, const double2* d_Sin, double mu, double T, double* d_ImS) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  auto* T_ = P->tc.get();
+  const long nw = P->nw, ni = P->ni;
+  sigma_f32_kernel<<<div_up(size_t(nw * ni), 256), 256, 0, s>>>(d_Sin, nw * ni, T_->Sf.p);
+  EPSP_LAUNCHED(ctx);
+  TParams q{};
+  q.T = T;
+  q.mu = mu;
+  DBuf<TParams> d_q = to_device(ctx, &q, 1);
+  DBuf<int> d_slot0;
+  d_slot0.alloc(ctx, 1);
+  d_slot0.zero(s);
+  long pk = prof_begin(ctx, "fm_disp");
+  launch_fm_disp(P, 1, d_slot0.p, d_q.p, nullptr, d_ImS);
+  prof_end(ctx, pk);
+  EPSP_CUDA(cudaStreamSynchronize(s));  // the parameter buffers are locals
+}
+
+// The tables of fm_disp_f32_kernel (see Scgd0Plan): w_f g2 permuted to [ν f, i] and rounded to
+// FP32, ωph, iq_kk, iks_i, iks_f, f_to_i, ε_f and the grid nodes as float pairs, the bucket table's
+// origin and scale. ωq itself is gathered per term, never stored.
+void tc_setup_dispersive(Scgd0Plan* P, const epsp_model* m) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  P->disp = true;
+  const long nm = m->nm, ni = m->ni, nf = m->nf, nvf = nm * nf;
+  {
+    DBuf<double> g2t;
+    upload_g2_permuted(ctx, m, g2t);
+    auto d_wf = to_device(ctx, m->w_f, size_t(nf));
+    auto d_fti = to_device(ctx, m->f_to_i, size_t(nf));
+    P->d_gwf.alloc(ctx, size_t(nvf * ni));
+    gw_f32_kernel<<<div_up(size_t(nvf * ni), 256), 256, 0, s>>>(g2t.p, d_wf.p, int(nm), nvf, ni, P->d_gwf.p);
+    EPSP_LAUNCHED(ctx);
+    EPSP_CUDA(cudaStreamSynchronize(s));
+  }
+  P->d_wph = to_device(ctx, m->omega_ph, size_t(nm * m->nq));
+  P->d_iq = to_device(ctx, m->iq_kk, size_t(m->nk_i * m->nk_f));
+  P->d_iksi = to_device(ctx, m->iks_i, size_t(ni));
+  P->d_iksf = to_device(ctx, m->iks_f, size_t(nf));
+  P->d_fti = to_device(ctx, m->f_to_i, size_t(nf));
+  P->nk_i = m->nk_i;
+  P->d_epsf = to_device(ctx, m->eps_f, size_t(nf));
+  P->d_wtab.alloc(ctx, size_t(P->nw));
+  fd_node_table_kernel<<<div_up(size_t(P->nw), 256), 256, 0, s>>>(P->d_ws.p, int(P->nw), P->d_wtab.p);
+  EPSP_LAUNCHED(ctx);
+  P->x0f = float(P->ct.x0);
+  P->inv_hf = float(P->ct.inv_h);
+  P->ntab = long(P->d_jtab.n);
+  if (P->ntab >= (long(1) << 21))
+    fail(EPSP_EUNSUPPORTED, "the grid's cell-search table is too long for the FP32 dispersive path (2^21 buckets at "
+                            "most); use EPSP_PATH_DIRECT_FP64");
+  EPSP_CUDA(cudaStreamSynchronize(s));
+}
+
 void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
@@ -419,6 +716,7 @@ void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS) {
   const long nwm = nw * P->nm;
   sigma_f32_kernel<<<div_up(size_t(nw * ni), 256), 256, 0, s>>>(d_Sin, nw * ni, T->Sf.p);
   EPSP_LAUNCHED(ctx);
+
   to_f32_kernel<<<div_up(size_t(nwm), 256), 256, 0, s>>>(P->d_Fa.p, nwm, T->Ff.p);
   EPSP_LAUNCHED(ctx);
   to_f32_kernel<<<div_up(size_t(nwm), 256), 256, 0, s>>>(P->d_Fe.p, nwm, T->Ff.p + nwm);
@@ -459,22 +757,22 @@ void tc_reserve(Scgd0Plan* P, long nT) {
   nT = std::max(nT, T->capT);
   if (nT * nw > (1l << 30) || nT * ni > (1l << 30)) fail(EPSP_EINVAL, "too many temperatures for the 32-bit tile grid");
   for (int p = 0; p < kNs; ++p) {
-    T->Kt[p].alloc(ctx, size_t(nT * nw * T->Kp));
+    if (!P->disp) T->Kt[p].alloc(ctx, size_t(nT * nw * T->Kp));
     T->Im[p].alloc(ctx, size_t(nT * ni * T->Kp2));
     T->Im[p].zero(ctx->stream);  // the padding columns nω.. Kp2 of the KK operand stay zero
   }
   T->Sf.alloc(ctx, size_t(nT * slab));
-  T->Ff.alloc(ctx, size_t(nT * 2 * nwm));
+  if (!P->disp) T->Ff.alloc(ctx, size_t(nT * 2 * nwm));
   T->ImS_b.alloc(ctx, size_t(nT * slab));
   size_t part = 0;
   for (long a = 1; a <= nT; ++a) {
-    int bn, sp1, sp2;
-    tc_gemm_shape(ctx, int(a * nw), int(ni), int(nk), 16, kNs, &bn, &sp1, kKbCap);
+    int bn, sp1 = 1, sp2;
+    if (!P->disp) tc_gemm_shape(ctx, int(a * nw), int(ni), int(nk), 16, kNs, &bn, &sp1, kKbCap);
     tc_gemm_shape(ctx, int(nw), int(a * ni), int(nw), 16, kNs, &bn, &sp2, kKbCap);
     part = std::max(part, size_t(std::max(sp1, sp2)) * size_t(a * slab));
   }
   T->part.alloc(ctx, part);
-  T->opK = operand(T->Kt, nT * nw, nk, T->Kp, kTcBM);
+  if (!P->disp) T->opK = operand(T->Kt, nT * nw, nk, T->Kp, kTcBM);
   T->opIm = operand(T->Im, nT * ni, nw, T->Kp2, T->bn2);
   T->capT = nT;
 }
@@ -486,6 +784,9 @@ int* tc_err_ptr(Scgd0Plan* P) { return P->tc->err.p; }
 long tc_capacity(Scgd0Plan* P) { return P->tc->ImS_b.p ? P->tc->capT : 0; }
 
 float4* tc_sigma_f32(Scgd0Plan* P) { return P->tc->Sf.p; }
+
+static void tc_kk_tail(Scgd0Plan* P, int nA, const int* d_slots, double2* d_S_all, float4* d_P,
+                       unsigned long long* d_errbits, double* d_minA);
 
 void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, const TParams* d_tp,
                 const double2* d_Sin_b, double2* d_S_all, float4* d_P, unsigned long long* d_errbits, double* d_minA) {
@@ -500,6 +801,14 @@ void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, co
   if (d_Sin_b) {
     sigma_f32_batch_kernel<<<div_up(size_t(slab * nA), 256), 256, 0, s>>>(d_Sin_b, slab, nA, T->Sf.p);
     EPSP_LAUNCHED(ctx);
+  }
+  if (P->disp) {  // dispersive modes: ImΣ of every slot term by term, then the same Kramers-Kronig tail
+    prof_end(ctx, pp);
+    long pk = prof_begin(ctx, "fm_disp");
+    launch_fm_disp(P, nA, d_slots, d_tp, T->ImS_b.p, nullptr);
+    prof_end(ctx, pk);
+    tc_kk_tail(P, nA, d_slots, d_S_all, d_P, d_errbits, d_minA);
+    return;
   }
   // small blocks: the FP64 exponentials of the table spread over every SM
   occ_table_f32_kernel<<<dim3(div_up(size_t(nwm), 64), unsigned(nA)), 64, 0, s>>>(
@@ -525,10 +834,20 @@ void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, co
                                                                    T->Im[0].p, T->Im[1].p, T->Im[2].p, T->Kp2);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pf);
+  tc_kk_tail(P, nA, d_slots, d_S_all, d_P, d_errbits, d_minA);
+}
+
+// ReΣ = KK ImΣ for every slot (the split ImΣ rows already in T->Im) and the fused epilogue.
+static void tc_kk_tail(Scgd0Plan* P, int nA, const int* d_slots, double2* d_S_all, float4* d_P,
+                       unsigned long long* d_errbits, double* d_minA) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  auto* T = P->tc.get();
+  const long nw = P->nw, ni = P->ni, slab = nw * ni;
   const long N2 = long(nA) * ni;
   int sp2 = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(N2), int(nw), T->part.p, nw, nw * N2, 16, T->err.p,
                            "tc_kk", kKbCap);
-  pf = prof_begin(ctx, "kk_epilogue");
+  long pf = prof_begin(ctx, "kk_epilogue");
   kk_epilogue_kernel<<<dim3(div_up(size_t(nw), 255), unsigned(P->ngroups), unsigned(nA)), 256, 0, s>>>(
       T->part.p, sp2, nw * N2, T->ImS_b.p, int(nw), slab, d_slots, P->d_gptr.p, P->d_gidx.p, P->d_ws.p, P->d_eps_i.p,
       d_S_all, d_P, d_errbits, d_minA);

@@ -206,6 +206,19 @@ def cubic_t2g_setup(N: int = 16, t: float = 0.26, tp: float = 0.08, nmodes: int 
                 dispersionless=True, wph=wph)
 
 
+def with_dispersion(setup: dict, N: int, amplitude: float) -> dict:
+    """The cubic t2g model of cubic_t2g_setup (N^3 q points) with dispersive modes:
+    ω_ν(q) = ω_ν (1 + amplitude (cos 2π q1/N + cos 2π q2/N + cos 2π q3/N) / 3), q = (q1, q2, q3)."""
+    q = np.arange(N ** 3)
+    q3 = np.stack([q % N, (q // N) % N, q // (N * N)])
+    shape = np.cos(2 * np.pi * q3 / N).sum(axis=0) / 3.0
+    wph = np.asarray(setup["wph"], dtype=np.float64)
+    out = dict(setup)
+    out["omega_ph"] = np.asfortranarray(wph[:, None] * (1.0 + amplitude * shape[None, :]))
+    out["dispersionless"] = False
+    return out
+
+
 def c2_output_grid() -> FrequencyGrid:
     """The graded ωs of the 3-band benchmark configuration: 2 meV on ±0.5 eV, 10 meV on ±3 eV,
     40 meV on ±8 eV (1251 nodes)."""

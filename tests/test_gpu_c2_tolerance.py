@@ -113,3 +113,20 @@ def test_fp64_ladder_application_matches_oracle_on_samples_at_full_size(c2, orac
         ref = oracle.ladder_apply_sample(s, J, S, mu, T, 0.1, i0, i1, omega_acoustic=W_AC)
         assert np.linalg.norm(ref) > 0
         assert np.linalg.norm(got[..., i0:i1] - ref) <= 1e-10 * np.linalg.norm(ref), (path, i0, i1)
+
+
+def test_dispersive_fan_migdal_on_samples_at_full_size(c2, oracle):
+    # the benchmark model with dispersive modes (±20 % over the zone): the tensor-core plan's FP32
+    # term-by-term Fan-Migdal sum against the oracle's FP64 sum on bounded samples, |ΔImΣ| <= 1e-5 eV
+    from epspectral_gb300 import api, synthetic
+    s = synthetic.with_dispersion(c2["setup"], 16, 0.2)
+    T, ctx = c2["T"], c2["ctx"]
+    Sin = c2["r64"]["sigma"][:, :, 0]
+    mu = c2["r64"]["mu"][0]
+    plan = api.Scgd0Plan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
+    got = plan.imsigma(Sin, mu, T)
+    plan.close()
+    for i0, i1 in IMSIGMA_SAMPLE:
+        ref = oracle.imsigma_sample(s, Sin, mu, T, i0, i1, omega_acoustic=W_AC)[:, i0:i1]
+        assert np.linalg.norm(ref) > 0
+        assert np.max(np.abs(got[:, i0:i1] - ref)) <= 1e-5, (i0, i1)

@@ -54,6 +54,45 @@ def test_fan_migdal_sum_matches_oracle(api, oracle):
         assert rel(got, ref) <= 1e-13
 
 
+def test_dispersive_fan_migdal_fp32_matches_oracle(api, oracle):
+    # the same per-pair-ωq case on the tensor-core plan, whose Fan-Migdal sum for dispersive modes
+    # runs term by term in FP32 (float pairs where the value cancels): within 1e-5 relative of the
+    # oracle's FP64 sum, the Inf coupling below ω_acoustic never read
+    from test_oracle_scgd0 import per_pair_setup
+    nm, ni, nf = 3, 13, 17
+    g = FrequencyGrid.from_nodes(np.concatenate([np.arange(-1.0, -0.5999, 0.02), np.arange(-0.5, 0.5001, 0.1),
+                                                 np.arange(0.6, 1.0001, 0.02)]))
+    nw = len(g)
+    Sin = 0.1 * R.pseudorandom(nw, ni, seed=7) + 1j * (-0.05 - 0.05 * np.abs(R.pseudorandom(nw, ni, seed=8)))
+    g2 = np.abs(R.pseudorandom(nm, ni, nf, seed=9))
+    wq = 0.05 + 0.2 * np.abs(R.pseudorandom(nm, ni, nf, seed=10))
+    wq[1, 2, :] = 0.0
+    g2[1, 2, :] = np.inf
+    s = per_pair_setup(g, g2, wq, 0.8 * R.pseudorandom(nf, seed=11),
+                       np.array([(5 * (f + 1)) % ni for f in range(nf)], dtype=np.int32), np.full(nf, 1.0 / nf))
+    ref = oracle.imsigma(s, Sin, 0.07, 0.03, np.full((nw, ni), 0.5), omega_acoustic=1e-3)
+    plan = api.Scgd0Plan(s, path="gemm_bf16", omega_acoustic=1e-3)
+    got = plan.imsigma(Sin, 0.07, 0.03, np.full((nw, ni), 0.5))
+    assert np.all(np.isfinite(got))
+    assert rel(got, ref) <= 1e-5
+
+
+def test_dispersive_loop_matches_oracle(api, oracle):
+    # the small 3-band model with dispersive modes (±20 % over the zone): the tensor-core loop
+    # (FP32 Fan-Migdal terms, BF16x3 Kramers-Kronig map) within |ΔΣ| <= 1e-5 eV, |Δμ| <= 1e-5 eV of the
+    # oracle over three iterations with the μ update
+    ws = graded_frequency_grid([(-0.3, 0.3, 0.01), (-1.5, 1.5, 0.05)])
+    s = synthetic.with_dispersion(synthetic.cubic_t2g_setup(N=4, ws=ws, g2_dtype=np.float32, seed=5), 4, 0.2)
+    o = occ(0.0, Tlist=(300 * synthetic.KELVIN, 600 * synthetic.KELVIN))
+    kw = dict(eta_init=0.05, eta_min=[0.0, 0.03], tol=0.0, maxiter=3, mu_start=[-0.5, -0.5], omega_acoustic=W_AC)
+    ref = oracle.loop_scgd0(s, o, **kw)
+    got = api.loop_scgd0(s, o, path="gemm_bf16", **kw)
+    assert np.max(np.abs(got["sigma"] - ref["sigma"])) <= 1e-5
+    assert np.max(np.abs(got["mu"] - ref["mu"])) <= 1e-5
+    direct = api.loop_scgd0(s, o, path="direct_fp64", **kw)
+    assert rel(direct["sigma"], ref["sigma"]) <= 1e-10
+
+
 @pytest.fixture(scope="module")
 def holstein_gpu():
     ws = FrequencyGrid.from_nodes(np.arange(-200, 201) * 0.02)
@@ -118,11 +157,13 @@ def test_errors_come_back_as_status(api, holstein_gpu, cubic_small):
     with pytest.raises(ArgumentError):
         api.loop_scgd0(s, occ(0.0), eta_init=0.05, tol=1e-6, maxiter=2, mu_start=[0.0],
                        sigma_init=np.zeros((401, 33, 2), complex), omega_acoustic=W_AC)
-    # dispersive modes are refused by the recast paths, accepted by the direct one
+    # dispersive modes are refused by the FP64 recast path, accepted by the direct one and by the
+    # tensor-core path (its FP32 term-by-term sum)
     disp = dict(s, omega_ph=np.asfortranarray(0.2 + 0.01 * np.arange(64.0)[None, :]))
     with pytest.raises(api.EpspError, match="dispersionless"):
-        api.Scgd0Plan(disp, path="gemm_bf16", omega_acoustic=W_AC)
+        api.Scgd0Plan(disp, path="gemm_fp64", omega_acoustic=W_AC)
     api.Scgd0Plan(disp, path="direct_fp64", omega_acoustic=W_AC).close()
+    api.Scgd0Plan(disp, path="gemm_bf16", omega_acoustic=W_AC).close()
     # a device allocation failure is reported, and the context stays usable
     ctx = api.Context(0)
     ctx.fail_next_alloc(1)
