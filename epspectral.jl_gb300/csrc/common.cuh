@@ -72,6 +72,10 @@ struct Ctx {
   size_t prof_used = 0;
   // Host-side test hook: the next allocation of at least `fail_alloc_bytes` fails (0 = off).
   size_t fail_alloc_bytes = 0;
+  // Test hook of the one-CTA tensor-core GEMM: the producer skips K block `stall_kb` of every tile
+  // (-1 = off) and the pipeline waits give up after `stall_wait_limit` tries (0 = the default).
+  int stall_kb = -1;
+  unsigned stall_wait_limit = 0;
   cudaEvent_t timer[2] = {nullptr, nullptr};
   // host time spent in device allocations (for the set-up phase log)
   double alloc_ms = 0;

@@ -183,4 +183,19 @@ epsp_status epsp_test_fail_alloc(epsp_ctx* c, uint64_t bytes) {
   return EPSP_OK;
 }
 
+/* Test hook (not in the reference): the one-CTA tensor-core GEMM kernel's producer skips K block
+ * `skip_kblock` of every tile (-1 switches it off), and that kernel's pipeline waits give up after
+ * `wait_limit` tries (0 restores the default), so a call returns EPSP_EDEVICE_TIMEOUT from a wait
+ * that runs out on the device rather than from a fault. */
+epsp_status epsp_test_gemm_stall(epsp_ctx* c, int32_t skip_kblock, uint32_t wait_limit) {
+  if (!c) return EPSP_EINVAL;
+  if (skip_kblock < -1 || (wait_limit != 0 && wait_limit < 64)) {
+    c->c.last_error = "epsp_test_gemm_stall: skip_kblock must be -1 or a K block, wait_limit 0 or at least 64";
+    return EPSP_EINVAL;
+  }
+  c->c.stall_kb = skip_kblock;
+  c->c.stall_wait_limit = wait_limit;
+  return EPSP_OK;
+}
+
 }  // extern "C"

@@ -79,6 +79,7 @@ struct LadderPlan {
   long Mz = 0, Nz = 0, Kz = 0, Kzp = 0;
   DBuf<int32_t> d_zt_k;          // [nm, 2, nwp] first node p0 of the three nodes a mode's two shift tables read
   DBuf<float> d_zt_w;            // [nm, 2, nwp][4] the weights of p0, p0 + 1, p0 + 2 (tent weights folded in), 0
+  DBuf<int32_t> d_zwin;          // [node ranges, nm][2] zgather_kernel's staging windows (float4 chunks)
   DBuf<float> d_nnu_f;
   DBuf<__nv_bfloat16> d_KKh, d_KKl, d_Yh, d_Yl;
   DBuf<float> d_part2;
@@ -686,44 +687,52 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
+// zgather_kernel: nodes per thread, and the largest block (two blocks resident per SM, the
+// accumulators in registers).
+constexpr int kZgU = 4, kZgMaxThreads = 320;
+
 // D from Z (the formula above), FP32, modes in ascending order, both signs and three taps each.
 // Z: [Mz, nm N] column-major (ld ldZ) as zsplits split-K partials zstride apart (summed in
 // ascending order as they are staged); rows of slot z at z 16 nwp. zt_k [nm][2][nwp] first tap
 // node p_{ν,s}(j), zt_w [nm][2][nwp] its three weights (tent split folded in); nnu_all 16 Bose
 // occupations per right-hand side (rmap[z], or z). D[z 24 nwp + (q + 6 (c0 + 2 ri)) nwp + j + ldD n],
-// rows j < nω. Grid (N / NC, 4 (c0, ri), slots), blockDim = nodes / U rounded up to warps: a block
-// owns NC columns n of one (c0, ri) and every node; per mode it stages the four components' Z
-// columns (asynchronous copies, double-buffered over ν) and each thread accumulates U nodes.
-template <int U, int NC>
-__global__ void zgather_kernel(const float* __restrict__ Z, long ldZ, int zsplits, long zstride,
-                               const int32_t* __restrict__ zt_k, const float4* __restrict__ zt_w,
-                               const float* __restrict__ nnu_all, const int* __restrict__ rmap, int nw, int nwp, int nm,
-                               long N, float* __restrict__ D, long ldD) {
+// rows j < nω. Grid (N / NC, 4 (c0, ri) x node ranges, slots), blockDim a multiple of 32 up to
+// kZgMaxThreads: a block owns NC columns n of one (c0, ri) and the kZgU blockDim nodes of its range;
+// per mode it stages the window zwin[range][ν] (float4 chunks [lo, hi) of each of the four
+// components' Z columns: every row the range's taps read) by asynchronous copies, double-buffered
+// over ν, and each thread accumulates kZgU nodes.
+template <int NC>
+__global__ void __launch_bounds__(kZgMaxThreads, 2)
+    zgather_kernel(const float* __restrict__ Z, long ldZ, int zsplits, long zstride, const int32_t* __restrict__ zt_k,
+                   const float4* __restrict__ zt_w, const int2* __restrict__ zwin, const float* __restrict__ nnu_all,
+                   const int* __restrict__ rmap, int nw, int nwp, int nm, long N, float* __restrict__ D, long ldD) {
+  constexpr int U = kZgU;
   extern __shared__ __align__(16) float zs[];  // [2][NC][4][nwp + 4]
   const int stride = nwp + 4;
   const long n0 = long(blockIdx.x) * NC;
-  const int c0 = blockIdx.y & 1, ri = blockIdx.y >> 1;
+  const int c0 = blockIdx.y & 1, ri = (blockIdx.y >> 1) & 1, rg = int(blockIdx.y >> 2);
   const long z = blockIdx.z;
   const int rhs = rmap ? rmap[z] : int(z);
   const float* nnu = nnu_all + 16 * rhs;
   const float* zb = Z + z * 16 * nwp + long((ri * 2 + c0) * 4) * nwp;  // the 4 components, contiguous
   const int nthr = blockDim.x;
+  const int jb = rg * U * nthr;  // the range's first node
   for (int e = threadIdx.x; e < 2 * NC * 4 * 4; e += nthr) zs[(e / 4) * stride + nwp + e % 4] = 0.f;  // tap pads
-  const int nv = nwp / 4;  // float4 chunks per component column
-  auto stage = [&](int nu, int buf) {
+  auto stage = [&](int nu, int buf, int2 win) {
+    const int nc = win.y - win.x;  // float4 chunks per component
     for (int c = 0; c < NC; ++c) {
       const long n = n0 + c;
       if (n >= N) break;
       float* dst = zs + long((buf * NC + c) * 4) * stride;
       const float* src = zb + ldZ * (long(nu) * N + n);
       if (zsplits == 1) {
-        for (int e = threadIdx.x; e < 4 * nv; e += nthr) {
-          const int comp = e / nv, p4 = e % nv;
+        for (int e = threadIdx.x; e < 4 * nc; e += nthr) {
+          const int comp = e / nc, p4 = win.x + e % nc;
           cp_async16(dst + comp * stride + 4 * p4, src + long(comp) * nwp + 4 * p4);
         }
       } else {  // split-K partials: summed here in ascending order (synchronous loads)
-        for (int e = threadIdx.x; e < 4 * nwp; e += nthr) {
-          const int comp = e / nwp, p = e % nwp;
+        for (int e = threadIdx.x; e < 16 * nc; e += nthr) {
+          const int comp = e / (4 * nc), p = 4 * win.x + e % (4 * nc);
           float acc = 0.f;
           for (int sp = 0; sp < zsplits; ++sp) acc += src[long(comp) * nwp + p + zstride * sp];
           dst[comp * stride + p] = acc;
@@ -739,16 +748,18 @@ __global__ void zgather_kernel(const float* __restrict__ Z, long ldZ, int zsplit
     for (int u = 0; u < U; ++u)
 #pragma unroll
       for (int q = 0; q < 6; ++q) acc[c][u][q] = 0.f;
-  stage(0, 0);
+  const int2* win_rg = zwin + long(rg) * nm;
+  stage(0, 0, win_rg[0]);
   for (int nu = 0; nu < nm; ++nu) {
-    cp_async_wait_all();
-    __syncthreads();  // mode nu's columns are in buffer nu & 1; buffer (nu + 1) & 1 is free
-    if (nu + 1 < nm) stage(nu + 1, (nu + 1) & 1);
     const float nb = nnu[nu];
     const float hp = 0.5f + nb;
+    const int2 win_next = win_rg[nu + 1 < nm ? nu + 1 : nu];  // loaded before the wait
+    cp_async_wait_all();
+    __syncthreads();  // mode nu's columns are in buffer nu & 1; buffer (nu + 1) & 1 is free
+    if (nu + 1 < nm) stage(nu + 1, (nu + 1) & 1, win_next);
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const int j = threadIdx.x + nthr * u;
+      const int j = jb + threadIdx.x + nthr * u;
       if (j >= nw) continue;
       int pk[2];
       float4 wv[2];
@@ -785,7 +796,7 @@ __global__ void zgather_kernel(const float* __restrict__ Z, long ldZ, int zsplit
     if (n >= N) break;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const int j = threadIdx.x + nthr * u;
+      const int j = jb + threadIdx.x + nthr * u;
       if (j >= nw) continue;
 #pragma unroll
       for (int q = 0; q < 6; ++q) D[z * 24 * nwp + long(q + 6 * (c0 + 2 * ri)) * nwp + j + ldD * n] = acc[c][u][q];
@@ -796,43 +807,63 @@ __global__ void zgather_kernel(const float* __restrict__ Z, long ldZ, int zsplit
 // Group size (M tiles) of the contraction's grouped tile order: 8 tiles of 128 rows of Jr.
 constexpr int kZGroupM = 8;
 
-// zgather_kernel's launch shape: U nodes per thread (4 up to 4096 nodes, else 8), NC columns per
+// zgather_kernel's launch shape: nranges node ranges of kZgU threads nodes each, NC columns per
 // block (2 while the double-buffered staging of two columns fits 110 KB, else 1).
 struct ZgatherShape {
-  int U = 4, NC = 2, threads = 0;
+  int NC = 2, threads = 0, nranges = 1;
   size_t smem = 0;
 };
 static ZgatherShape zgather_shape(long nw, long nwp) {
   ZgatherShape g;
-  g.U = nw <= 4096 ? 4 : 8;
-  if (nw > 8192) fail(EPSP_EUNSUPPORTED, "the tensor-core ladder paths take at most 8192 frequency nodes");
-  g.threads = int((nw + g.U - 1) / g.U + 31) / 32 * 32;
+  const long nthr = (nw + kZgU - 1) / kZgU;  // threads for all nodes in one block
+  g.nranges = int((nthr + kZgMaxThreads - 1) / kZgMaxThreads);
+  g.threads = int(((nthr + g.nranges - 1) / g.nranges + 31) / 32 * 32);
   const size_t per_col = size_t(2 * 4 * (nwp + 4)) * sizeof(float);
   g.NC = per_col * 2 <= (size_t(110) << 10) ? 2 : 1;
   g.smem = per_col * size_t(g.NC);
+  if (g.smem > (size_t(227) << 10))
+    fail(EPSP_EUNSUPPORTED, "the tensor-core ladder paths take at most 7000 frequency nodes");
   return g;
+}
+// The staging windows of zgather_kernel: for each node range and mode, the float4 chunks [lo, hi)
+// of a component column that hold every tap p0 .. p0 + 2 of the range's nodes (both signs),
+// from the first-tap table hk [nm][2][nwp]; taps at or past nwp read the zeroed pads.
+static std::vector<int32_t> zgather_windows(const ZgatherShape& g, const std::vector<int32_t>& hk, long nw, long nwp,
+                                            long nm) {
+  std::vector<int32_t> win(size_t(2 * g.nranges * nm));
+  const long span = long(kZgU) * g.threads;
+  for (long r = 0; r < g.nranges; ++r)
+    for (long nu = 0; nu < nm; ++nu) {
+      long lo = nwp, hi = 0;
+      for (long j = r * span; j < std::min(nw, (r + 1) * span); ++j)
+        for (long sg = 0; sg < 2; ++sg) {
+          const long p0 = hk[size_t((nu * 2 + sg) * nwp + j)];
+          if (p0 < 0 || p0 + 2 >= nwp + 4) fail(EPSP_EINVAL, "a shift-table tap outside the staged rows");
+          lo = std::min(lo, p0);
+          hi = std::max(hi, p0 + 3);
+        }
+      if (hi <= lo) lo = hi = 0;  // an empty range stages nothing
+      win[size_t(2 * (r * nm + nu))] = int32_t(lo / 4);
+      win[size_t(2 * (r * nm + nu) + 1)] = int32_t(std::min((hi + 3) / 4, nwp / 4));
+    }
+  return win;
 }
 template <class... A>
 static void launch_zgather(const ZgatherShape& g, dim3 grid, cudaStream_t s, A... args) {
-  static size_t smem_set[4] = {0, 0, 0, 0};  // the largest dynamic shared memory allowed so far, per instantiation
-  const int v = (g.U == 4 ? 0 : 2) + (g.NC == 2 ? 0 : 1);
+  static size_t smem_set[2] = {0, 0};  // the largest dynamic shared memory allowed so far, per instantiation
+  const int v = g.NC == 2 ? 0 : 1;
   if (g.smem > smem_set[v]) {
-    switch (v) {
-      case 0: EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem))); break;
-      case 1: EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem))); break;
-      case 2: EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem))); break;
-      default: EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem))); break;
-    }
+    if (v == 0)
+      EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)));
+    else
+      EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)));
     smem_set[v] = g.smem;
   }
-  if (g.U == 4 && g.NC == 2)
-    zgather_kernel<4, 2><<<grid, g.threads, g.smem, s>>>(args...);
-  else if (g.U == 4)
-    zgather_kernel<4, 1><<<grid, g.threads, g.smem, s>>>(args...);
-  else if (g.NC == 2)
-    zgather_kernel<8, 2><<<grid, g.threads, g.smem, s>>>(args...);
+  grid.y *= unsigned(g.nranges);
+  if (g.NC == 2)
+    zgather_kernel<2><<<grid, g.threads, g.smem, s>>>(args...);
   else
-    zgather_kernel<8, 1><<<grid, g.threads, g.smem, s>>>(args...);
+    zgather_kernel<1><<<grid, g.threads, g.smem, s>>>(args...);
 }
 
 // Y (rows q = 0, 2 of D) as the BF16 hi/lo B operand of the Kramers-Kronig GEMM: row (qq, c0, ri, n),
@@ -1708,6 +1739,7 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
             }
         P->d_zt_k = to_device(ctx, hk);
         P->d_zt_w = to_device(ctx, hw);
+        P->d_zwin = to_device(ctx, zgather_windows(zgather_shape(nw, nwp), hk, nw, nwp, nm));
       }
       P->Kp2 = (nw + 63) / 64 * 64;
       const bool tf = P->path == EPSP_PATH_GEMM_TF32;
@@ -1775,7 +1807,10 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       int terr = 0;
       P->d_err.download(&terr, 1, s);
       EPSP_CUDA(cudaStreamSynchronize(s));
-      if (terr) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out while tuning (bounded device wait)");
+      if (terr) {
+        P->d_err.zero(s);
+        fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out while tuning (bounded device wait)");
+      }
       plog.mark("tile shape (autotuner or cache)");
       // the Kramers-Kronig image on the tensor cores: A = KK [nω][nω'], B = Y [8N][nω']
       P->d_KKh.alloc(ctx, size_t(nw * P->Kp2));
@@ -1789,7 +1824,6 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       P->d_part2.alloc(ctx, size_t(P->splits2) * size_t(nw * 8 * N));
       P->opKK = two_part(P->d_KKh.p, P->d_KKl.p, nw, nw, P->Kp2, kTcBM);
       P->opY = two_part(P->d_Yh.p, P->d_Yl.p, 8 * N, nw, P->Kp2, P->bn2);
-      zgather_shape(nw, P->nwp);  // the grid's size is checked here
     }
     EPSP_CUDA(cudaStreamSynchronize(s));
   } else {
@@ -1978,7 +2012,8 @@ static void apply_L(LadderPlan* P, const float2* J, float2* LJ, const float2* X 
   const ZgatherShape zg = zgather_shape(nw, nwp);
   launch_zgather(zg, dim3(unsigned((N + zg.NC - 1) / zg.NC), 4, 1), s, static_cast<const float*>(P->d_Z.p), P->Mz, sp,
                  P->Mz * P->Nz, static_cast<const int32_t*>(P->d_zt_k.p),
-                 reinterpret_cast<const float4*>(P->d_zt_w.p), static_cast<const float*>(P->d_nnu_f.p),
+                 reinterpret_cast<const float4*>(P->d_zt_w.p), reinterpret_cast<const int2*>(P->d_zwin.p),
+                 static_cast<const float*>(P->d_nnu_f.p),
                  static_cast<const int*>(nullptr), int(nw), int(nwp), int(P->nm), N, P->d_Dz.p, M);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pz);
@@ -2002,7 +2037,10 @@ static void check_tc_err(LadderPlan* P) {
   int e = 0;
   P->d_err.download(&e, 1, P->ctx->stream);
   EPSP_CUDA(cudaStreamSynchronize(P->ctx->stream));
-  if (e) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+  if (e) {
+    P->d_err.zero(P->ctx->stream);  // cleared, so that the plan's next call starts clean
+    fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+  }
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -2255,7 +2293,10 @@ static void ladder_run_t(LadderPlan* P, const double* sigma, const double* mu, c
           }
           prof_end(ctx, pbl);
           EPSP_CUDA(cudaStreamSynchronize(s));
-          if (werr) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+          if (werr) {
+            P->d_err.zero(s);
+            fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+          }
           if (inner == 1) {
             res.push_back(gs.beta);
             if (gs.solved_x0) {  // solved at x0: the speculative first step is dropped
@@ -2485,7 +2526,7 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const float2* X, int nA
   const ZgatherShape zg = zgather_shape(nw, nwp);
   launch_zgather(zg, dim3(unsigned((N + zg.NC - 1) / zg.NC), 4, unsigned(nA)), s, static_cast<const float*>(B.Z.p), Mzt,
                  1, long(0), static_cast<const int32_t*>(P->d_zt_k.p), reinterpret_cast<const float4*>(P->d_zt_w.p),
-                 static_cast<const float*>(B.nnu.p), static_cast<const int*>(B.rmap.p), int(nw), int(nwp), int(P->nm), N,
+                 reinterpret_cast<const int2*>(P->d_zwin.p), static_cast<const float*>(B.nnu.p), static_cast<const int*>(B.rmap.p), int(nw), int(nwp), int(P->nm), N,
                  B.D.p, Mt);
   EPSP_LAUNCHED(ctx);
   y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), unsigned(nA)), 256, 0, s>>>(

@@ -1373,7 +1373,10 @@ void scgd0_run(Scgd0Plan* P, const epsp_occ* occ, const double* eta_min, double 
     if (P->path == EPSP_PATH_GEMM_BF16) {
       int tcerr = 0;
       std::memcpy(&tcerr, &h_pack[size_t(4 * nT)], sizeof(int));
-      if (tcerr) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+      if (tcerr) {
+        EPSP_CUDA(cudaMemsetAsync(tc_err_ptr(P), 0, sizeof(int), s));  // the plan's next run starts clean
+        fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+      }
     }
     const auto* h_err = reinterpret_cast<const unsigned long long*>(h_pack);
     const double* h_mu = h_pack + nT;

@@ -617,7 +617,10 @@ static void check_err(Scgd0Plan* P) {
   int e = 0;
   P->tc->err.download(&e, 1, P->ctx->stream);
   EPSP_CUDA(cudaStreamSynchronize(P->ctx->stream));
-  if (e) fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+  if (e) {
+    P->tc->err.zero(P->ctx->stream);  // cleared, so that the plan's next call starts clean
+    fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out (bounded device wait)");
+  }
 }
 
 // fm_disp_f32_kernel over nA slots (Σ_in in T->Sf): into ImS_b and the Kramers-Kronig operand, or

@@ -108,8 +108,9 @@ static void launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int 
     maps.b[p] = B.m[p < NS ? p : 0];
   }
   dim3 grid((N + BN - 1) / BN, (M + kTcBM - 1) / kTcBM, splits);
-  tc_gemm_split_kernel<BN, STAGES, NS, BK, TF32><<<grid, 128, L::kBytes, ctx->stream>>>(maps, M, N, kblocks, per, out,
-                                                                                        ld_out, split_stride, d_err, gm);
+  tc_gemm_split_kernel<BN, STAGES, NS, BK, TF32><<<grid, 128, L::kBytes, ctx->stream>>>(
+      maps, M, N, kblocks, per, out, ld_out, split_stride, d_err, gm, ctx->stall_kb,
+      ctx->stall_wait_limit ? ctx->stall_wait_limit : kWaitLimit);
   EPSP_LAUNCHED(ctx);
 }
 

@@ -16,7 +16,10 @@
 //                    and tcgen05.commit to release a stage and, at the end, to signal the epilogue;
 //   warps 0-3      : epilogue, tcgen05.ld of TMEM lanes 32w..32w+31 into registers, masked stores.
 // Every mbarrier wait is bounded; on timeout the kernel records the error in *err and winds down
-// (waits, again bounded, for its own copies and MMAs, frees TMEM and returns).
+// (waits, again bounded, for its own copies and MMAs, frees TMEM and returns). The one-CTA kernel
+// takes its pipeline waits' limit as an argument, and a K block its producer skips (a test hook:
+// the wait for that block's copies then runs out; the wind-down waits keep the full limit, and the
+// epilogue's wait for the MMAs ends when the MMA thread, which always commits, gives up).
 // Two more kernels below share that pipeline: the persistent one (a CTA per SM over all tiles,
 // two TMEM accumulators) and the CTA-pair one (tcgen05 cta_group::2: a 256-row tile over two CTAs,
 // each holding half of B). Every TMA load reads this GPU's own memory into the issuing CTA's
@@ -53,9 +56,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait for the phase of parity `parity` to complete; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (unsigned it = 0; it < kWaitLimit; ++it) {
+// Bounded wait for the phase of parity `parity` to complete; false after `limit` tries.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned limit = kWaitLimit) {
+  for (unsigned it = 0; it < limit; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if (it > 64) __nanosleep(64);
   }
@@ -187,7 +190,8 @@ struct TcMaps {
 template <int BN, int STAGES, int NS, int BK = kTcBK, bool TF32 = false>
 __global__ void __launch_bounds__(128, 1)
     tc_gemm_split_kernel(const __grid_constant__ TcMaps maps, int M, int N, int kblocks, int kb_per_split,
-                         float* __restrict__ out, long ld_out, long split_stride, int* __restrict__ err, int gm = 1) {
+                         float* __restrict__ out, long ld_out, long split_stride, int* __restrict__ err, int gm = 1,
+                         int skip_kb = -1, unsigned wait_limit = kWaitLimit) {
   using L = TcSmem<BN, STAGES, NS, BK, TF32>;
   static_assert(!TF32 || NS == 1, "TF32 operands have one part");
   extern __shared__ uint8_t smem_raw[];
@@ -223,9 +227,10 @@ __global__ void __launch_bounds__(128, 1)
     // producer
     int issued = 0;
     for (int kb = 0; kb < nkb; ++kb) {
+      if (kb == skip_kb) continue;  // test hook: this K block's copies are never issued
       const int s = kb % STAGES;
       const uint32_t ph = (kb / STAGES) & 1;
-      if (kb >= STAGES && !mbar_wait(empty0 + 8 * s, ph ^ 1)) {
+      if (kb >= STAGES && !mbar_wait(empty0 + 8 * s, ph ^ 1, wait_limit)) {
         atomicExch(&s_abort, 1);
         break;
       }
@@ -243,7 +248,9 @@ __global__ void __launch_bounds__(128, 1)
     }
     if (*(volatile int*)&s_abort) {
       // wind down: wait (bounded) for the copies this thread issued into stages not yet consumed
-      for (int kb = max(0, issued - STAGES); kb < issued; ++kb) mbar_wait(full0 + 8 * (kb % STAGES), (kb / STAGES) & 1);
+      // (a skipped K block's stage is never reused: the wait for its release runs out first)
+      for (int kb = max(0, issued - STAGES); kb < issued; ++kb)
+        if (kb != skip_kb) mbar_wait(full0 + 8 * (kb % STAGES), (kb / STAGES) & 1);
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
@@ -251,7 +258,7 @@ __global__ void __launch_bounds__(128, 1)
     for (int kb = 0; kb < nkb; ++kb) {
       const int s = kb % STAGES;
       const uint32_t ph = (kb / STAGES) & 1;
-      if (!mbar_wait(full0 + 8 * s, ph)) {
+      if (!mbar_wait(full0 + 8 * s, ph, wait_limit)) {
         atomicExch(&s_abort, 1);
         break;
       }

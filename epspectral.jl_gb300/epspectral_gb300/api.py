@@ -60,6 +60,7 @@ def lib():
         "epsp_profile_kernel": (C.c_int, [vp, C.c_char_p]),
         "epsp_profile_read": (C.c_int, [vp, P(d), P(i64)]),
         "epsp_test_fail_alloc": (C.c_int, [vp, C.c_uint64]),
+        "epsp_test_gemm_stall": (C.c_int, [vp, C.c_int32, C.c_uint32]),
         "epsp_timer_begin": (C.c_int, [vp]),
         "epsp_timer_end": (C.c_int, [vp, P(d)]),
         "epsp_scgd0_setup": (C.c_int, [vp, P(epsp_model), P(epsp_options), P(vp)]),
@@ -147,6 +148,11 @@ class Context:
     def fail_next_alloc(self, nbytes: int):
         """Test hook: the next device allocation of at least nbytes fails with ENOMEM."""
         self.check(lib().epsp_test_fail_alloc(self.handle, int(nbytes)))
+
+    def stall_gemm(self, skip_kblock: int = -1, wait_limit: int = 0):
+        """Test hook: the one-CTA tensor-core GEMM skips K block skip_kblock of every tile and gives
+        up its pipeline waits after wait_limit tries (EDEVICE_TIMEOUT); stall_gemm() switches it off."""
+        self.check(lib().epsp_test_gemm_stall(self.handle, int(skip_kblock), int(wait_limit)))
 
     def close(self):
         if self.handle:

@@ -18,6 +18,8 @@ from __future__ import annotations
 
 import itertools
 import math
+import os
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -109,8 +111,8 @@ def cubic_t2g_setup(N: int = 16, t: float = 0.26, tp: float = 0.08, nmodes: int 
     inner state's IBZ representative has the same sorted band energies, assigned bitwise, and the
     rotation R_f is the signed permutation g with k_f = g k_rep (R_f v_rep = v_f). Multiplets chain
     levels at one k closer than `degen_cutoff` (src/scgd0.jl:144-160). With g2_chunk, g2 is drawn
-    g2_chunk inner states at a time (another seeded stream; for sizes whose FP64 draw would not fit
-    in memory at once).
+    g2_chunk inner states at a time, chunk c from the stream seeded by (seed, 1, c), the chunks on
+    host threads (for sizes whose FP64 draw would not fit in memory at once).
     """
     rng = np.random.default_rng(seed)
     half = N // 2
@@ -172,11 +174,16 @@ def cubic_t2g_setup(N: int = 16, t: float = 0.26, tp: float = 0.08, nmodes: int 
     if g2_chunk:
         dt = np.uint16 if g2_dtype == "bf16" else np.dtype(g2_dtype)
         g2 = np.empty((nmodes, ni, nf), dtype=dt, order="F")
-        for f0 in range(0, nf, g2_chunk):
-            f1 = min(nf, f0 + g2_chunk)
-            x = rng.standard_normal(size=(nmodes, ni, f1 - f0), dtype=np.float32)
+
+        def draw(c):  # chunk c from its own stream, seeded by (seed, c): the same in any thread order
+            f0, f1 = c * g2_chunk, min(nf, (c + 1) * g2_chunk)
+            x = np.random.default_rng([seed, 1, c]).standard_normal(size=(nmodes, ni, f1 - f0), dtype=np.float32)
             x = np.float32(g2_scale) * np.exp(np.float32(g2_logmean) + np.float32(g2_logsigma) * x)
             g2[:, :, f0:f1] = float32_to_bf16_bits(x) if g2_dtype == "bf16" else x.astype(dt)
+
+        nchunk = (nf + g2_chunk - 1) // g2_chunk
+        with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as pool:
+            list(pool.map(draw, range(nchunk)))
     else:
         g2 = (g2_scale * np.exp(rng.normal(g2_logmean, g2_logsigma, size=(nmodes, ni, nf)))).astype(np.float32)
         g2 = np.asfortranarray(g2)

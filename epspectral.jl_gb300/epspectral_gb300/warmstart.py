@@ -291,24 +291,27 @@ def sample_runs(n: int, seed: int, *, T_range=(100.0, 800.0), filling_range=(0.5
 
 
 def generate_pairs(setup: dict, runs, *, path="gemm_bf16", eta_init=0.01, tol=1e-6, maxiter=50,
-                   omega_acoustic=1e-4, spin_degeneracy=2.0, ctx: api.Context | None = None):
+                   omega_acoustic=1e-4, spin_degeneracy=2.0, gpu_tile=None, ctx: api.Context | None = None):
     """(features, targets) of each run, from the method itself: the G0D0 iteration and the plain
-    iteration to tol. Runs sharing a scale share one plan (g2 scaled on the host: FP32 or FP64 g2).
-    Returns (X list, Y list, records), X and Y float32 [ni, ...] per run."""
-    if setup["g2"].dtype not in (np.float32, np.float64):
-        raise ArgumentError("generate_pairs scales g2 on the host: pass FP32 or FP64 g2")
+    iteration to tol. Runs sharing a scale share one plan (g2 scaled on the host: FP32 or FP64 g2;
+    g2 of another type, e.g. BF16 bit patterns, only for runs of scale 1). Returns (X list, Y list,
+    records), X and Y float32 [ni, ...] per run."""
+    g2 = setup["g2"]
+    if g2.dtype not in (np.float32, np.float64) and any(run["scale"] != 1.0 for run in runs):
+        raise ArgumentError("generate_pairs scales g2 on the host: pass FP32 or FP64 g2, or runs of scale 1")
     from .synthetic import KELVIN, bare_mu
     ctx = ctx or api.default_context()
     Xs, Ys, recs = [], [], []
     plan, plan_scale = None, None
-    g2 = setup["g2"]
     for run in runs:
         if plan is None or run["scale"] != plan_scale:
             if plan is not None:
                 plan.close()
             s = dict(setup)
-            s["g2"] = np.asfortranarray(g2 * np.asarray(run["scale"], dtype=g2.dtype))
-            plan, plan_scale = api.Scgd0Plan(s, path=path, omega_acoustic=omega_acoustic, ctx=ctx), run["scale"]
+            if run["scale"] != 1.0:
+                s["g2"] = np.asfortranarray(g2 * np.asarray(run["scale"], dtype=g2.dtype))
+            plan = api.Scgd0Plan(s, path=path, omega_acoustic=omega_acoustic, gpu_tile=gpu_tile, ctx=ctx)
+            plan_scale = run["scale"]
         T = run["T_K"] * KELVIN
         occ = dict(Tlist=[T], nlist=[0.0], nelec=run["filling"], spin_degeneracy=spin_degeneracy, type="metal")
         mu0 = bare_mu(setup, T, run["filling"], spin_degeneracy)

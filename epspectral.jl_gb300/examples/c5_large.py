@@ -80,7 +80,9 @@ def main():
     out["ladder_gmres_iters"] = [int(x) for x in l["niter"].ravel()]
     out["ladder_converged"] = bool(l["converged"].all())
     ni = int(s["eps_i"].size)
-    M, N, K = 24 * len(ws), 3 * ni, 15 * 3 * ni
+    # the contraction Z = Jr Bz: rows 16 nω (4 components x (c0, re/im) x nodes), columns 15 modes x 3ni,
+    # depth 3ni (rows padded to 32 nodes are not counted)
+    M, N, K = 16 * len(ws), 15 * 3 * ni, 3 * ni
     if n:
         out["tc_ladder_ms_per_launch"] = ms / n
         out["tc_ladder_useful_tflops"] = 2.0 * M * N * K / (ms / n / 1e3) / 1e12

@@ -166,16 +166,23 @@ int64_t epsp_kernel_launches(const epsp_ctx* ctx);
 
 /* Library utilities with no counterpart in the reference (benchmarks and tests):
  *  - epsp_profile_kernel brackets every launch of the kernel family `name` ("tc_ladder",
- *    "tc_fm", "kbuild", "xgen", "mu", ...) with CUDA events on the context's stream until the next
- *    call (NULL or "" switches it off); epsp_profile_read returns their summed milliseconds and count;
+ *    "tc_fm", "kbuild", "jmat", "zgather", "mu", ...) with CUDA events on the context's stream
+ *    until the next call (NULL or "" switches it off); epsp_profile_read returns their summed
+ *    milliseconds and count;
  *  - epsp_timer_begin / epsp_timer_end time the context's stream between two calls;
  *  - epsp_test_fail_alloc makes the next device allocation of at least `bytes` bytes fail with
- *    EPSP_ENOMEM (0 switches it off), to test the error path without exhausting a device. */
+ *    EPSP_ENOMEM (0 switches it off), to test the error path without exhausting a device;
+ *  - epsp_test_gemm_stall makes the one-CTA tensor-core GEMM kernel's producer skip K block
+ *    `skip_kblock` of every tile (-1 switches it off) and that kernel's pipeline waits give up after
+ *    `wait_limit` tries (0: the default, about 2^26), so that a call returns EPSP_EDEVICE_TIMEOUT
+ *    from a bounded device wait (the kernel frees its tensor memory and returns; the context and
+ *    the plan stay usable). */
 epsp_status epsp_profile_kernel(epsp_ctx* ctx, const char* name);
 epsp_status epsp_profile_read(epsp_ctx* ctx, double* total_ms, int64_t* count);
 epsp_status epsp_timer_begin(epsp_ctx* ctx);
 epsp_status epsp_timer_end(epsp_ctx* ctx, double* ms);
 epsp_status epsp_test_fail_alloc(epsp_ctx* ctx, uint64_t bytes);
+epsp_status epsp_test_gemm_stall(epsp_ctx* ctx, int32_t skip_kblock, uint32_t wait_limit);
 
 /* ---- scGD0 ---- */
 

@@ -271,6 +271,40 @@ def test_every_contraction_tile_shape_matches_the_oracle(api, oracle, cc, unit):
     plan.close()
 
 
+def test_bounded_wait_runs_out_and_the_plan_stays_usable(api, cc):
+    # the one-CTA tensor-core kernel's producer skips K block 0 of every tile (a test hook): the MMA
+    # thread's wait for that stage gives up after 4096 tries, the kernel records it, waits for its
+    # own copies and products, frees its tensor memory and returns; the call reports EDEVICE_TIMEOUT,
+    # and the same plan on the same context then applies the operator bitwise as before
+    import time
+    from epspectral_gb300 import abi
+    c = cc
+    s = c["setup"]
+    nw, ni = len(s["omegas"]), s["eps_i"].size
+    J = R.pseudorandom_complex(nw, 4, 3, 2, ni, seed=0.41)
+    J[0] = 0
+    J[-1] = 0
+    args = (J, c["sigma"][:, :, 0], c["mu"][0], c["Tlist"][0], 0.07)
+    plan = api.LadderPlan(s, path="gemm_tf32", omega_acoustic=W_AC)
+    plan.set_gemm_config(128, 1, 32)  # the one-CTA kernel
+    want = plan.apply(*args)
+    plan.ctx.stall_gemm(0, 4096)
+    try:
+        t0 = time.perf_counter()
+        with pytest.raises(api.EpspError) as err:
+            plan.apply(*args)
+        assert err.value.status == abi.EPSP_EDEVICE_TIMEOUT
+        assert time.perf_counter() - t0 < 60
+    finally:
+        plan.ctx.stall_gemm()  # the context is shared with the other tests
+    assert np.array_equal(plan.apply(*args), want)
+    with pytest.raises(ArgumentError):
+        plan.ctx.stall_gemm(-2, 0)
+    with pytest.raises(ArgumentError):
+        plan.ctx.stall_gemm(0, 8)
+    plan.close()
+
+
 def test_scgd0_sigma_stays_on_the_device_for_the_ladder(api, cc):
     # epsp_scgd0_run with sigma_out = NULL keeps Σ in the plan (epsp_scgd0_sigma_device); the ladder
     # reads it there (cudaMemcpyDefault): the same σ, bitwise, as from the downloaded Σ
