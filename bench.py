@@ -299,7 +299,8 @@ def train_warm_start(s, ctx):
     plan.close()
     info = dict(train_runs=WARM_TRAIN_RUNS, heldout_runs=WARM_HELDOUT_RUNS, epochs=WARM_EPOCHS,
                 network=f"MLP {'-'.join(map(str, ws.dims))}, SiLU, BF16 weights / FP32 accumulate, Adam",
-                pair_generation_s=t_gen, train_s=t_fit, final_loss=float(hist[-1]), first_loss=float(hist[0]),
+                pair_generation_s=t_gen, train_s=t_fit, train_device_s=ws.train_device_s,
+                final_loss=float(hist[-1]), first_loss=float(hist[0]),
                 heldout_plain_iters_mean=float(np.mean(plain)), heldout_warm_iters_mean=float(np.mean(warm)),
                 heldout_fallbacks=fallbacks, heldout_max_abs_dsigma_vs_plain_eV=float(np.max(dsig)))
     return ws, info
@@ -683,6 +684,7 @@ def large_c5(ctx) -> dict:
     t_fit = time.perf_counter() - t0
     del X, Y
     out["warm_start"] = dict(train_runs=16, epochs=20, rows=16 * ni, pair_generation_s=t_gen, train_s=t_fit,
+                             train_device_s=ws.train_device_s,
                              first_loss=float(hist[0]), final_loss=float(hist[-1]),
                              train_runs_plain_iters_mean=float(np.mean([r["niter"] for r in recs])))
     t0 = time.perf_counter()

@@ -29,6 +29,7 @@
 #include <chrono>
 #include <type_traits>
 #include <complex>
+#include <cstring>
 #include <limits>
 #include <memory>
 
@@ -54,6 +55,13 @@ struct LadderChunk {
   long k_off = 0;          // row offset of the chunk in B̃
 };
 
+// zgather_kernel's launch shape: U nodes per thread, nranges node ranges of U threads nodes each,
+// NC columns per block, staged rows of wstride floats (the widest window + 4 zeros); smem bytes.
+struct ZgatherShape {
+  int U = 2, NC = 4, threads = 0, nranges = 1, wstride = 0;
+  size_t smem = 0;
+};
+
 struct LadderPlan {
   Ctx* ctx = nullptr;
   int path = EPSP_PATH_DIRECT_FP64;
@@ -77,9 +85,10 @@ struct LadderPlan {
   // tensor-core paths: the contraction Z = Jr Bz (M = 16 nwp rows (c12, c0, ri, p), N = nm 3ni
   // columns (ν, a, i), K = 3ni pairs (b, i') padded to Kzp), then D from Z by zgather_kernel
   long Mz = 0, Nz = 0, Kz = 0, Kzp = 0;
-  DBuf<int32_t> d_zt_k;          // [nm, 2, nwp] first node p0 of the three nodes a mode's two shift tables read
-  DBuf<float> d_zt_w;            // [nm, 2, nwp][4] the weights of p0, p0 + 1, p0 + 2 (tent weights folded in), 0
+  DBuf<float> d_ztab;            // [nm, 2, nwp][4] the weights of p0, p0 + 1, p0 + 2 (tent weights folded in), p0
+                                 // (integer bits): the three nodes a mode's two shift tables read
   DBuf<int32_t> d_zwin;          // [node ranges, nm][2] zgather_kernel's staging windows (float4 chunks)
+  ZgatherShape zg;               // zgather_kernel's launch shape
   DBuf<float> d_nnu_f;
   DBuf<__nv_bfloat16> d_KKh, d_KKl, d_Yh, d_Yl;
   DBuf<float> d_part2;
@@ -687,28 +696,26 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// zgather_kernel: nodes per thread, and the largest block (two blocks resident per SM, the
-// accumulators in registers).
-constexpr int kZgU = 4, kZgMaxThreads = 320;
+// zgather_kernel: the largest block (two blocks resident per SM, the accumulators in registers).
+constexpr int kZgMaxThreads = 320;
 
 // D from Z (the formula above), FP32, modes in ascending order, both signs and three taps each.
 // Z: [Mz, nm N] column-major (ld ldZ) as zsplits split-K partials zstride apart (summed in
-// ascending order as they are staged); rows of slot z at z 16 nwp. zt_k [nm][2][nwp] first tap
-// node p_{ν,s}(j), zt_w [nm][2][nwp] its three weights (tent split folded in); nnu_all 16 Bose
-// occupations per right-hand side (rmap[z], or z). D[z 24 nwp + (q + 6 (c0 + 2 ri)) nwp + j + ldD n],
-// rows j < nω. Grid (N / NC, 4 (c0, ri) x node ranges, slots), blockDim a multiple of 32 up to
-// kZgMaxThreads: a block owns NC columns n of one (c0, ri) and the kZgU blockDim nodes of its range;
-// per mode it stages the window zwin[range][ν] (float4 chunks [lo, hi) of each of the four
-// components' Z columns: every row the range's taps read) by asynchronous copies, double-buffered
-// over ν, and each thread accumulates kZgU nodes.
-template <int NC>
+// ascending order as they are staged); rows of slot z at z 16 nwp. ztab [nm][2][nwp]: per node,
+// mode and sign the three tap weights (tent split folded in) and, in .w as integer bits, the first
+// tap node p0 (the taps are p0, p0 + 1, p0 + 2); nnu_all 16 Bose occupations per right-hand side
+// (rmap[z], or z). D[z 24 nwp + (q + 6 (c0 + 2 ri)) nwp + j + ldD n], rows j < nω.
+// Grid (N / NC, 4 (c0, ri) x node ranges, slots), blockDim a multiple of 32 up to kZgMaxThreads: a
+// block owns NC columns n of one (c0, ri) and the U blockDim nodes of its range; per mode it stages
+// the window zwin[range][ν] (float4 chunks [lo, hi) of each of the four components' Z columns:
+// every row the range's taps read) into rows of wstride floats by asynchronous copies,
+// double-buffered over ν, and each thread accumulates U nodes x NC columns.
+template <int U, int NC>
 __global__ void __launch_bounds__(kZgMaxThreads, 2)
-    zgather_kernel(const float* __restrict__ Z, long ldZ, int zsplits, long zstride, const int32_t* __restrict__ zt_k,
-                   const float4* __restrict__ zt_w, const int2* __restrict__ zwin, const float* __restrict__ nnu_all,
+    zgather_kernel(const float* __restrict__ Z, long ldZ, int zsplits, long zstride, const float4* __restrict__ ztab,
+                   const int2* __restrict__ zwin, int wstride, const float* __restrict__ nnu_all,
                    const int* __restrict__ rmap, int nw, int nwp, int nm, long N, float* __restrict__ D, long ldD) {
-  constexpr int U = kZgU;
-  extern __shared__ __align__(16) float zs[];  // [2][NC][4][nwp + 4]
-  const int stride = nwp + 4;
+  extern __shared__ __align__(16) float zs[];  // [2][NC][4][wstride]
   const long n0 = long(blockIdx.x) * NC;
   const int c0 = blockIdx.y & 1, ri = (blockIdx.y >> 1) & 1, rg = int(blockIdx.y >> 2);
   const long z = blockIdx.z;
@@ -717,25 +724,26 @@ __global__ void __launch_bounds__(kZgMaxThreads, 2)
   const float* zb = Z + z * 16 * nwp + long((ri * 2 + c0) * 4) * nwp;  // the 4 components, contiguous
   const int nthr = blockDim.x;
   const int jb = rg * U * nthr;  // the range's first node
-  for (int e = threadIdx.x; e < 2 * NC * 4 * 4; e += nthr) zs[(e / 4) * stride + nwp + e % 4] = 0.f;  // tap pads
   auto stage = [&](int nu, int buf, int2 win) {
     const int nc = win.y - win.x;  // float4 chunks per component
     for (int c = 0; c < NC; ++c) {
       const long n = n0 + c;
       if (n >= N) break;
-      float* dst = zs + long((buf * NC + c) * 4) * stride;
-      const float* src = zb + ldZ * (long(nu) * N + n);
+      float* dst = zs + long((buf * NC + c) * 4) * wstride;
+      // zeros after each staged row: a tap past the grid's last padded node (weight zero) reads them
+      if (threadIdx.x < 16) dst[(threadIdx.x / 4) * wstride + 4 * nc + threadIdx.x % 4] = 0.f;
+      const float* src = zb + ldZ * (long(nu) * N + n) + 4 * win.x;
       if (zsplits == 1) {
         for (int e = threadIdx.x; e < 4 * nc; e += nthr) {
-          const int comp = e / nc, p4 = win.x + e % nc;
-          cp_async16(dst + comp * stride + 4 * p4, src + long(comp) * nwp + 4 * p4);
+          const int comp = e / nc, p4 = e % nc;
+          cp_async16(dst + comp * wstride + 4 * p4, src + long(comp) * nwp + 4 * p4);
         }
       } else {  // split-K partials: summed here in ascending order (synchronous loads)
         for (int e = threadIdx.x; e < 16 * nc; e += nthr) {
-          const int comp = e / (4 * nc), p = 4 * win.x + e % (4 * nc);
+          const int comp = e / (4 * nc), p = e % (4 * nc);
           float acc = 0.f;
           for (int sp = 0; sp < zsplits; ++sp) acc += src[long(comp) * nwp + p + zstride * sp];
-          dst[comp * stride + p] = acc;
+          dst[comp * wstride + p] = acc;
         }
       }
     }
@@ -749,7 +757,8 @@ __global__ void __launch_bounds__(kZgMaxThreads, 2)
 #pragma unroll
       for (int q = 0; q < 6; ++q) acc[c][u][q] = 0.f;
   const int2* win_rg = zwin + long(rg) * nm;
-  stage(0, 0, win_rg[0]);
+  int2 win = win_rg[0];
+  stage(0, 0, win);
   for (int nu = 0; nu < nm; ++nu) {
     const float nb = nnu[nu];
     const float hp = 0.5f + nb;
@@ -757,28 +766,28 @@ __global__ void __launch_bounds__(kZgMaxThreads, 2)
     cp_async_wait_all();
     __syncthreads();  // mode nu's columns are in buffer nu & 1; buffer (nu + 1) & 1 is free
     if (nu + 1 < nm) stage(nu + 1, (nu + 1) & 1, win_next);
+    const int base = 4 * win.x;  // the staged rows start at node base
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int j = jb + threadIdx.x + nthr * u;
       if (j >= nw) continue;
+      float4 t[2];
       int pk[2];
-      float4 wv[2];
 #pragma unroll
       for (int sg = 0; sg < 2; ++sg) {
-        const long e = (long(nu) * 2 + sg) * nwp + j;
-        pk[sg] = zt_k[e];
-        wv[sg] = zt_w[e];
+        t[sg] = ztab[(long(nu) * 2 + sg) * nwp + j];
+        pk[sg] = __float_as_int(t[sg].w) - base;
       }
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
-        const float* zc = zs + long(((nu & 1) * NC + c) * 4) * stride;
+        const float* zc = zs + long(((nu & 1) * NC + c) * 4) * wstride;
         float x[2][4];
 #pragma unroll
         for (int sg = 0; sg < 2; ++sg)
 #pragma unroll
           for (int cc = 0; cc < 4; ++cc) {
-            const float* r = zc + cc * stride + pk[sg];
-            x[sg][cc] = wv[sg].x * r[0] + wv[sg].y * r[1] + wv[sg].z * r[2];
+            const float* r = zc + cc * wstride + pk[sg];
+            x[sg][cc] = t[sg].x * r[0] + t[sg].y * r[1] + t[sg].z * r[2];
           }
         // components c12 = 0 (11), 1 (21), 2 (12), 3 (22)
         acc[c][u][0] += 0.5f * (x[0][0] - x[1][0]);
@@ -789,6 +798,7 @@ __global__ void __launch_bounds__(kZgMaxThreads, 2)
         acc[c][u][5] += (1.f + nb) * x[0][2] + nb * x[1][2];
       }
     }
+    win = win_next;
   }
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
@@ -807,31 +817,23 @@ __global__ void __launch_bounds__(kZgMaxThreads, 2)
 // Group size (M tiles) of the contraction's grouped tile order: 8 tiles of 128 rows of Jr.
 constexpr int kZGroupM = 8;
 
-// zgather_kernel's launch shape: nranges node ranges of kZgU threads nodes each, NC columns per
-// block (2 while the double-buffered staging of two columns fits 110 KB, else 1).
-struct ZgatherShape {
-  int NC = 2, threads = 0, nranges = 1;
-  size_t smem = 0;
-};
-static ZgatherShape zgather_shape(long nw, long nwp) {
+// Threads and ranges for nω nodes (the windows, and with them NC and the staging, follow).
+static ZgatherShape zgather_ranges(long nw, int U) {
   ZgatherShape g;
-  const long nthr = (nw + kZgU - 1) / kZgU;  // threads for all nodes in one block
+  g.U = U;
+  const long nthr = (nw + U - 1) / U;  // threads for all nodes in one block
   g.nranges = int((nthr + kZgMaxThreads - 1) / kZgMaxThreads);
   g.threads = int(((nthr + g.nranges - 1) / g.nranges + 31) / 32 * 32);
-  const size_t per_col = size_t(2 * 4 * (nwp + 4)) * sizeof(float);
-  g.NC = per_col * 2 <= (size_t(110) << 10) ? 2 : 1;
-  g.smem = per_col * size_t(g.NC);
-  if (g.smem > (size_t(227) << 10))
-    fail(EPSP_EUNSUPPORTED, "the tensor-core ladder paths take at most 7000 frequency nodes");
   return g;
 }
 // The staging windows of zgather_kernel: for each node range and mode, the float4 chunks [lo, hi)
 // of a component column that hold every tap p0 .. p0 + 2 of the range's nodes (both signs),
-// from the first-tap table hk [nm][2][nwp]; taps at or past nwp read the zeroed pads.
-static std::vector<int32_t> zgather_windows(const ZgatherShape& g, const std::vector<int32_t>& hk, long nw, long nwp,
-                                            long nm) {
+// from the first-tap table hk [nm][2][nwp]; taps past the last chunk read the zeros staged after
+// it. Sets g.wstride, g.NC (4 while two double-buffered blocks fit an SM, else 2, else 1) and g.smem.
+static std::vector<int32_t> zgather_windows(ZgatherShape& g, const std::vector<int32_t>& hk, long nw, long nwp, long nm) {
   std::vector<int32_t> win(size_t(2 * g.nranges * nm));
-  const long span = long(kZgU) * g.threads;
+  const long span = long(g.U) * g.threads;
+  long maxnc = 1;
   for (long r = 0; r < g.nranges; ++r)
     for (long nu = 0; nu < nm; ++nu) {
       long lo = nwp, hi = 0;
@@ -843,27 +845,42 @@ static std::vector<int32_t> zgather_windows(const ZgatherShape& g, const std::ve
           hi = std::max(hi, p0 + 3);
         }
       if (hi <= lo) lo = hi = 0;  // an empty range stages nothing
-      win[size_t(2 * (r * nm + nu))] = int32_t(lo / 4);
-      win[size_t(2 * (r * nm + nu) + 1)] = int32_t(std::min((hi + 3) / 4, nwp / 4));
+      const long lo4 = lo / 4, hi4 = std::min((hi + 3) / 4, nwp / 4);
+      win[size_t(2 * (r * nm + nu))] = int32_t(lo4);
+      win[size_t(2 * (r * nm + nu) + 1)] = int32_t(std::max(lo4, hi4));
+      maxnc = std::max(maxnc, hi4 - lo4);
     }
+  g.wstride = int(4 * maxnc + 4);
+  const size_t per_col = size_t(2 * 4 * g.wstride) * sizeof(float);  // two buffers, four components
+  g.NC = per_col * 4 <= (size_t(110) << 10) ? 4 : per_col * 2 <= (size_t(110) << 10) ? 2 : 1;
+  g.smem = per_col * size_t(g.NC);
+  if (g.smem > (size_t(227) << 10))
+    fail(EPSP_EUNSUPPORTED, "the ladder's interpolation windows do not fit shared memory (grid too fine for its modes)");
   return win;
 }
-template <class... A>
-static void launch_zgather(const ZgatherShape& g, dim3 grid, cudaStream_t s, A... args) {
-  static size_t smem_set[2] = {0, 0};  // the largest dynamic shared memory allowed so far, per instantiation
-  const int v = g.NC == 2 ? 0 : 1;
-  if (g.smem > smem_set[v]) {
-    if (v == 0)
-      EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)));
-    else
-      EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)));
-    smem_set[v] = g.smem;
+template <int U, int NC>
+static void launch_zgather_t(const ZgatherShape& g, dim3 grid, cudaStream_t s, const float* Z, long ldZ, int zsplits,
+                             long zstride, const float4* ztab, const int2* zwin, const float* nnu, const int* rmap, int nw,
+                             int nwp, int nm, long N, float* D, long ldD) {
+  static size_t smem_set = 0;  // the largest dynamic shared memory allowed so far
+  if (g.smem > smem_set) {
+    EPSP_CUDA(cudaFuncSetAttribute(zgather_kernel<U, NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(g.smem)));
+    smem_set = g.smem;
   }
-  grid.y *= unsigned(g.nranges);
-  if (g.NC == 2)
-    zgather_kernel<2><<<grid, g.threads, g.smem, s>>>(args...);
+  zgather_kernel<U, NC><<<grid, g.threads, g.smem, s>>>(Z, ldZ, zsplits, zstride, ztab, zwin, g.wstride, nnu, rmap, nw,
+                                                        nwp, nm, N, D, ldD);
+}
+// Grid (N / NC, 4 x node ranges, slots).
+static void launch_zgather(const ZgatherShape& g, long N, unsigned slots, cudaStream_t s, const float* Z, long ldZ,
+                           int zsplits, long zstride, const float4* ztab, const int2* zwin, const float* nnu,
+                           const int* rmap, int nw, int nwp, int nm, float* D, long ldD) {
+  const dim3 grid(unsigned((N + g.NC - 1) / g.NC), 4u * unsigned(g.nranges), slots);
+  if (g.NC == 4)
+    launch_zgather_t<2, 4>(g, grid, s, Z, ldZ, zsplits, zstride, ztab, zwin, nnu, rmap, nw, nwp, nm, N, D, ldD);
+  else if (g.NC == 2)
+    launch_zgather_t<2, 2>(g, grid, s, Z, ldZ, zsplits, zstride, ztab, zwin, nnu, rmap, nw, nwp, nm, N, D, ldD);
   else
-    zgather_kernel<1><<<grid, g.threads, g.smem, s>>>(args...);
+    launch_zgather_t<2, 1>(g, grid, s, Z, ldZ, zsplits, zstride, ztab, zwin, nnu, rmap, nw, nwp, nm, N, D, ldD);
 }
 
 // Y (rows q = 0, 2 of D) as the BF16 hi/lo B operand of the Kramers-Kronig GEMM: row (qq, c0, ri, n),
@@ -1697,8 +1714,8 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       // mode tables: for node j, mode ν and sign s, the two shift tables (m_ν, m_ν + 1) with the
       // tent weights (1 - r_ν, r_ν) folded into their interpolation weights (FP32). The two tables'
       // lower nodes differ by at most one (the grid's spacing is a multiple of its unit, the shift
-      // step), so their four taps lie on three consecutive nodes p0, p0 + 1, p0 + 2: one node and
-      // three weights per entry (the fourth weight slot is zero).
+      // step), so their four taps lie on three consecutive nodes p0, p0 + 1, p0 + 2: three weights
+      // and the node (as integer bits in the fourth slot) per entry.
       {
         const long nwp = P->nwp;
         std::vector<int32_t> hk(size_t(nwp * nm * 2));
@@ -1737,9 +1754,10 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
               hk[e] = int32_t(p0);
               for (int t = 0; t < 3; ++t) hw[4 * e + size_t(t)] = float(cw[t]);
             }
-        P->d_zt_k = to_device(ctx, hk);
-        P->d_zt_w = to_device(ctx, hw);
-        P->d_zwin = to_device(ctx, zgather_windows(zgather_shape(nw, nwp), hk, nw, nwp, nm));
+        for (size_t e = 0; e < hk.size(); ++e) std::memcpy(&hw[4 * e + 3], &hk[e], sizeof(int32_t));
+        P->d_ztab = to_device(ctx, hw);
+        P->zg = zgather_ranges(nw, 2);
+        P->d_zwin = to_device(ctx, zgather_windows(P->zg, hk, nw, nwp, nm));
       }
       P->Kp2 = (nw + 63) / 64 * 64;
       const bool tf = P->path == EPSP_PATH_GEMM_TF32;
@@ -2009,12 +2027,9 @@ static void apply_L(LadderPlan* P, const float2* J, float2* LJ, const float2* X 
   const int sp = tc_gemm_launch_with(ctx, P->opA, P->opG, P->bn, P->splits, int(P->Mz), int(P->Nz), int(P->Kz), P->d_Z.p,
                                      P->Mz, P->Mz * P->Nz, P->d_err.p, "tc_ladder", P->persist, P->pair, P->gm);
   long pz = prof_begin(ctx, "zgather");
-  const ZgatherShape zg = zgather_shape(nw, nwp);
-  launch_zgather(zg, dim3(unsigned((N + zg.NC - 1) / zg.NC), 4, 1), s, static_cast<const float*>(P->d_Z.p), P->Mz, sp,
-                 P->Mz * P->Nz, static_cast<const int32_t*>(P->d_zt_k.p),
-                 reinterpret_cast<const float4*>(P->d_zt_w.p), reinterpret_cast<const int2*>(P->d_zwin.p),
-                 static_cast<const float*>(P->d_nnu_f.p),
-                 static_cast<const int*>(nullptr), int(nw), int(nwp), int(P->nm), N, P->d_Dz.p, M);
+  launch_zgather(P->zg, N, 1, s, P->d_Z.p, P->Mz, sp, P->Mz * P->Nz, reinterpret_cast<const float4*>(P->d_ztab.p),
+                 reinterpret_cast<const int2*>(P->d_zwin.p), P->d_nnu_f.p, nullptr, int(nw), int(nwp), int(P->nm),
+                 P->d_Dz.p, M);
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pz);
   long pl = prof_begin(ctx, "lsum");
@@ -2523,11 +2538,8 @@ static void apply_L_batch(LadderPlan* P, LadderBatch& B, const float2* X, int nA
   prof_end(ctx, px);
   tc_gemm_launch_with(ctx, B.opA, P->opG, P->bn, 1, int(Mzt), int(P->Nz), int(P->Kz), B.Z.p, Mzt, Mzt * P->Nz,
                       P->d_err.p, "tc_ladder", P->persist, P->pair, P->gm);
-  const ZgatherShape zg = zgather_shape(nw, nwp);
-  launch_zgather(zg, dim3(unsigned((N + zg.NC - 1) / zg.NC), 4, unsigned(nA)), s, static_cast<const float*>(B.Z.p), Mzt,
-                 1, long(0), static_cast<const int32_t*>(P->d_zt_k.p), reinterpret_cast<const float4*>(P->d_zt_w.p),
-                 reinterpret_cast<const int2*>(P->d_zwin.p), static_cast<const float*>(B.nnu.p), static_cast<const int*>(B.rmap.p), int(nw), int(nwp), int(P->nm), N,
-                 B.D.p, Mt);
+  launch_zgather(P->zg, N, unsigned(nA), s, B.Z.p, Mzt, 1, long(0), reinterpret_cast<const float4*>(P->d_ztab.p),
+                 reinterpret_cast<const int2*>(P->d_zwin.p), B.nnu.p, B.rmap.p, int(nw), int(nwp), int(P->nm), B.D.p, Mt);
   EPSP_LAUNCHED(ctx);
   y_split_kernel<<<dim3(div_up(size_t(P->Kp2), 256), unsigned(N), unsigned(nA)), 256, 0, s>>>(
       B.D.p, Mt, 1, 0, int(nw), int(nwp), N, P->Kp2, B.Yh.p, B.Yl.p);
@@ -2925,8 +2937,7 @@ epsp_status epsp_ladder_set_gemm_persistent(epsp_ladder_plan* plan, int32_t on) 
     if (!tc_path(P->path)) fail(EPSP_EUNSUPPORTED, "tile shapes apply to tensor-core plans (GEMM_BF16, GEMM_TF32)");
     if (on && P->path == EPSP_PATH_GEMM_BF16 && !(P->bn == 256 && P->bk == 32))
       fail(EPSP_EINVAL, "the persistent BF16x3 kernel takes bn 256 with bk 32");
-    P->persist = on != 0;
-    if (P->persist) P->pair = false;
+    P->persist = on != 0;  // with pair: the persistent CTA-pair kernel
   });
 }
 
@@ -2942,9 +2953,8 @@ epsp_status epsp_ladder_set_gemm_pair(epsp_ladder_plan* plan, int32_t on) {
   return lguard(P->ctx, [&] {
     if (!tc_path(P->path)) fail(EPSP_EUNSUPPORTED, "tile shapes apply to tensor-core plans (GEMM_BF16, GEMM_TF32)");
     if (on && (P->bn != 256 || P->bk != 32))
-      fail(EPSP_EINVAL, "the CTA-pair kernel takes bn 256 with bk 32");
-    P->pair = on != 0;
-    if (P->pair) P->persist = false;
+      fail(EPSP_EINVAL, "the CTA-pair kernels take bn 256 with bk 32");
+    P->pair = on != 0;  // with persistent: the persistent CTA-pair kernel
   });
 }
 

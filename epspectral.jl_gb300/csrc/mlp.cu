@@ -3,11 +3,13 @@
 //
 // Network: L fully connected layers d_0 -> d_1 -> ... -> d_L, SiLU between layers, linear output.
 // Weights W_l [d_{l+1}][d_l] (row-major) are kept in FP32 (the optimiser's master copy) and used in
-// BF16 by the forward and backward products (BF16 weights, FP32 accumulation); biases FP32. The
-// loss is the mean squared error over the batch and the outputs; the optimiser is Adam. The products
-// are register-tiled SIMT GEMMs over arbitrary strides (the network is ~1e6 parameters: a training
-// epoch over the warm-start set is tens of milliseconds), every reduction in fixed order, so a
-// training run is bitwise reproducible.
+// BF16 by the products (BF16 weights, FP32 accumulation); biases FP32. The loss is the mean squared
+// error over the batch and the outputs; the optimiser is Adam. Every product of the training, of
+// the gradient and of the prediction runs on the tensor cores (tc_gemm_launch: tcgen05, TMA, TMEM)
+// with the FP32 activations and gradients split into three BF16 parts (six products, ~2^-24
+// relative, as FP32; the BF16 weights' second and third parts are zero), every reduction in fixed
+// order, so a training run is bitwise reproducible. The scGD0 hook's inference (forward_tc) splits
+// the activations into two parts.
 #include "common.cuh"
 #include "tc_gemm.cuh"
 #include "warmstart.cuh"
@@ -19,63 +21,6 @@
 
 namespace epsp {
 
-// C[m, n] = Σ_k A(m, k) B(k, n), with A(m, k) = A[m sam + k sak], B(k, n) = B[k sbk + n sbn],
-// C[m scm + n scn]; 64x64 tiles, 256 threads with 4x4 outputs each, k in order. With gridDim.z > 1
-// slice z sums k in [z kc, (z + 1) kc) and writes C + z M N (row-major partials, summed in order by
-// partial_sum_kernel).
-template <class TA, class TB>
-__global__ void __launch_bounds__(256) mlp_gemm_kernel(int M, int N, int K, int kc, const TA* __restrict__ A, long sam,
-                                                       long sak, const TB* __restrict__ B, long sbk, long sbn,
-                                                       float* __restrict__ C, long scm, long scn) {
-  __shared__ float As[16][64 + 1];
-  __shared__ float Bs[16][64 + 1];
-  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  const int m0 = blockIdx.x * 64, n0 = blockIdx.y * 64;
-  const int kb = blockIdx.z * kc, ke = min(K, kb + kc);
-  if (gridDim.z > 1) C += long(blockIdx.z) * M * N;
-  float acc[4][4] = {};
-  for (int k0 = kb; k0 < ke; k0 += 16) {
-    // consecutive threads walk the operand's unit-stride index (k when that stride is 1)
-    for (int r = threadIdx.x; r < 1024; r += 256) {
-      int kk = r / 64, mm = r % 64;
-      if (sak == 1) kk = r % 16, mm = r / 16;
-      const int gm = m0 + mm, gk = k0 + kk;
-      As[kk][mm] = (gm < M && gk < ke) ? float(A[long(gm) * sam + long(gk) * sak]) : 0.f;
-      kk = r / 64, mm = r % 64;
-      if (sbk == 1) kk = r % 16, mm = r / 16;
-      const int gn = n0 + mm, gk2 = k0 + kk;
-      Bs[kk][mm] = (gn < N && gk2 < ke) ? float(B[long(gk2) * sbk + long(gn) * sbn]) : 0.f;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < 16; ++kk) {
-      float a[4], b[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        a[u] = As[kk][tx + 16 * u];
-        b[u] = Bs[kk][ty + 16 * u];
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], b[v], acc[u][v]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int u = 0; u < 4; ++u)
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const int gm = m0 + tx + 16 * u, gn = n0 + ty + 16 * v;
-      if (gm < M && gn < N) {
-        if (gridDim.z > 1)
-          C[long(gm) * N + gn] = acc[u][v];
-        else
-          C[long(gm) * scm + long(gn) * scn] = acc[u][v];
-      }
-    }
-}
-
 // C[m scm + n scn] = Σ_z P[z][m][n], z ascending.
 __global__ void partial_sum_kernel(const float* __restrict__ P, int M, int N, int nz, float* __restrict__ C, long scm,
                                    long scn) {
@@ -86,47 +31,68 @@ __global__ void partial_sum_kernel(const float* __restrict__ P, int M, int N, in
   C[(k / N) * scm + (k % N) * scn] = acc;
 }
 
-// Slices of K for a product of few output tiles, so that the grid covers the GPU twice.
-static int gemm_splits(const Ctx* ctx, int M, int N, int K) {
-  const int tiles = int(div_up(size_t(M), 64) * div_up(size_t(N), 64));
-  const int want = std::max(1, 2 * ctx->sm_count / tiles);
-  return std::max(1, std::min(want, K / 128));
-}
-
-template <class TA, class TB>
-static void mlp_gemm(Ctx* ctx, float* work, int M, int N, int K, const TA* A, long sam, long sak, const TB* B, long sbk,
-                     long sbn, float* C, long scm, long scn) {
-  const int sp = gemm_splits(ctx, M, N, K);
-  const int kc = int(div_up(div_up(size_t(K), size_t(sp)), 16) * 16);
-  const int nz = int(div_up(size_t(K), size_t(kc)));
-  dim3 grid(div_up(size_t(M), 64), div_up(size_t(N), 64), unsigned(nz));
-  mlp_gemm_kernel<TA, TB><<<grid, 256, 0, ctx->stream>>>(M, N, K, kc, A, sam, sak, B, sbk, sbn, nz > 1 ? work : C, scm,
-                                                         scn);
-  EPSP_LAUNCHED(ctx);
-  if (nz > 1) {
-    partial_sum_kernel<<<div_up(size_t(M) * N, 256), 256, 0, ctx->stream>>>(work, M, N, nz, C, scm, scn);
-    EPSP_LAUNCHED(ctx);
-  }
-}
-
 __device__ __forceinline__ float sigmoidf_(float x) { return 1.f / (1.f + expf(-x)); }
 
-// Z += b (row-major [n][d]); X = SiLU(Z) if act, else X = Z.
-__global__ void bias_act_kernel(float* __restrict__ Z, const float* __restrict__ b, long n, int d, bool act,
-                                float* __restrict__ X) {
-  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= n * d) return;
-  float z = Z[k] + b[k % d];
-  Z[k] = z;
-  X[k] = act ? z * sigmoidf_(z) : z;
-}
-
-// dZ = dX * SiLU'(Z).
-__global__ void act_back_kernel(const float* __restrict__ dX, const float* __restrict__ Z, long n, float* __restrict__ dZ) {
-  long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  float z = Z[k], s = sigmoidf_(z);
-  dZ[k] = dX[k] * (s * (1.f + z * (1.f - s)));
+// One pass over a [rows][cols] matrix in 32 x 32 tiles. The value v(m, j) is, by MODE:
+//   kEmitCopy    src[m ld_src + j];
+//   kEmitBiasAct z = Σ_s part[s pstride + j + cols m] + bias[j] (a product's split-K slabs, summed in
+//                order), written to Zout[m cols + j] when given, then v = SiLU(z) if act, else z;
+//   kEmitActBack Σ_s part[s pstride + j + cols m] times SiLU'(Zin[m cols + j]).
+// v goes to out32[m cols + j] (FP32) and, as three BF16 parts, to rp[p rpart + m ldr + j] (rows)
+// and tp[p tpart + j ldt + m] (transposed, through shared memory; columns m in [rows, ldt) get
+// zeros, so that the padded K of a product over the rows adds nothing). Grid (cols / 32, M / 32)
+// with M = ldt when tp is given, else rows; 32 x 8 threads.
+enum { kEmitCopy = 0, kEmitBiasAct = 1, kEmitActBack = 2 };
+template <int MODE>
+__global__ void __launch_bounds__(256)
+    emit_kernel(int rows, int cols, const float* __restrict__ src, long ld_src, const float* __restrict__ part, int splits,
+                long pstride, const float* __restrict__ bias, bool act, const float* __restrict__ Zin,
+                float* __restrict__ Zout, float* __restrict__ out32, __nv_bfloat16* __restrict__ rp, long ldr, long rpart,
+                __nv_bfloat16* __restrict__ tp, long ldt, long tpart) {
+  __shared__ float tile[32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int j0 = blockIdx.x * 32, m0 = blockIdx.y * 32;
+  const int j = j0 + tx;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int ml = ty + 8 * r, m = m0 + ml;
+    float v = 0.f;
+    if (m < rows && j < cols) {
+      if constexpr (MODE == kEmitCopy) {
+        v = src[long(m) * ld_src + j];
+      } else {
+        float acc = 0.f;
+        for (int sp = 0; sp < splits; ++sp) acc += part[long(sp) * pstride + j + long(cols) * m];
+        if constexpr (MODE == kEmitBiasAct) {
+          const float z = acc + bias[j];
+          if (Zout) Zout[long(m) * cols + j] = z;
+          v = act ? z * sigmoidf_(z) : z;
+        } else {
+          const float z = Zin[long(m) * cols + j], sg = sigmoidf_(z);
+          v = acc * (sg * (1.f + z * (1.f - sg)));
+        }
+      }
+      if (out32) out32[long(m) * cols + j] = v;
+      if (rp) {
+        __nv_bfloat16 q[3];
+        split_bf16_n(v, 3, q);
+#pragma unroll
+        for (int p = 0; p < 3; ++p) rp[p * rpart + long(m) * ldr + j] = q[p];
+      }
+    }
+    tile[ml][tx] = v;
+  }
+  if (!tp) return;
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int jl = ty + 8 * r, jj = j0 + jl, m = m0 + tx;
+    if (jj >= cols || m >= ldt) continue;
+    __nv_bfloat16 q[3];
+    split_bf16_n(tile[tx][jl], 3, q);  // zero for m >= rows
+#pragma unroll
+    for (int p = 0; p < 3; ++p) tp[p * tpart + long(jj) * ldt + m] = q[p];
+  }
 }
 
 // db[j] = Σ_m dZ[m][j] in ascending m.
@@ -174,11 +140,24 @@ __global__ void sum_kernel(const float* __restrict__ x, long n, double* __restri
 
 __global__ void step_kernel(int* t) { *t += 1; }
 
+// BF16 copies of the weight element k = o d_in + i of W [d_out][d_in]: wbf[k], the tensor-core
+// products' rows wp[o ldp + i] and the transposed rows wt[i ldt + o].
+__device__ __forceinline__ void store_wbf(long k, float w, int din, __nv_bfloat16* __restrict__ wbf,
+                                          __nv_bfloat16* __restrict__ wp, long ldp, __nv_bfloat16* __restrict__ wt,
+                                          long ldt) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(w);
+  wbf[k] = h;
+  const long o = k / din, i = k % din;
+  wp[o * ldp + i] = h;
+  wt[i * ldt + o] = h;
+}
+
 // Adam step t (read from the device, so a captured epoch replays with the right bias corrections)
-// on one parameter block; writes the BF16 copy of the weights the products use.
+// on one parameter block; for a weight block (wbf given) writes the BF16 copies the products use.
 __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m1, float* __restrict__ m2,
                             long n, float lr, float b1, float b2, float eps, const int* __restrict__ t,
-                            __nv_bfloat16* __restrict__ wbf) {
+                            __nv_bfloat16* __restrict__ wbf, int din, __nv_bfloat16* __restrict__ wp, long ldp,
+                            __nv_bfloat16* __restrict__ wt, long ldt) {
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const float c1 = 1.f - powf(b1, float(*t)), c2 = 1.f - powf(b2, float(*t));
@@ -189,12 +168,13 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, 
   m2[k] = v;
   const float wn = w[k] - lr * (a / c1) / (sqrtf(v / c2) + eps);
   w[k] = wn;
-  if (wbf) wbf[k] = __float2bfloat16_rn(wn);
+  if (wbf) store_wbf(k, wn, din, wbf, wp, ldp, wt, ldt);
 }
 
-__global__ void to_bf16_kernel(const float* __restrict__ w, long n, __nv_bfloat16* __restrict__ o) {
+__global__ void to_bf16_kernel(const float* __restrict__ w, long n, int din, __nv_bfloat16* __restrict__ wbf,
+                               __nv_bfloat16* __restrict__ wp, long ldp, __nv_bfloat16* __restrict__ wt, long ldt) {
   long k = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k < n) o[k] = __float2bfloat16_rn(w[k]);
+  if (k < n) store_wbf(k, w[k], din, wbf, wp, ldp, wt, ldt);
 }
 
 // Gathers the rows idx[0..n) of X [N][d] into out [n][d].
@@ -212,7 +192,8 @@ struct Mlp {
   std::vector<DBuf<float>> W, b, gW, gb, mW, vW, mb, vb;
   std::vector<DBuf<__nv_bfloat16>> Wbf;
   std::vector<DBuf<float>> Z, X;  // per layer, sized for the largest batch
-  DBuf<float> dA, dB, loss_rows, Yb, work;
+  DBuf<float> dA, dB, loss_rows, Yb;
+  DBuf<int> d_err;                // the tensor-core products' bounded-wait flag
   DBuf<double> loss_sum;
   DBuf<int> d_step;  // Adam's step counter
   long cap = 0;      // rows the activation buffers hold
@@ -222,6 +203,7 @@ struct Mlp {
   float y_scale = 1.f;
   bool scaled = false;
   long wgen = 0;  // bumped whenever the weights change (set_params, train)
+  double train_ms = 0;  // device milliseconds of the last training's epochs
   // Tensor-core inference: weights as the B operand [d_{l+1}][d_l padded to 8] (hi = the BF16
   // weights, lo = 0), activations as the A operand (BF16 hi/lo of the FP32 values) [cap][d_l
   // padded], split-K partials; rebuilt when wgen or the row capacity changes.
@@ -232,6 +214,21 @@ struct Mlp {
     std::vector<TcOperand> opA, opB;
     DBuf<float> part;
   } inf;
+  // Tensor-core training and prediction (three BF16 parts per operand, FP32 accumulation). Layer l
+  // (d_l -> d_{l+1}), batches of up to cap rows, rows padded to ldT = cap rounded up to 8:
+  //   forward   Z_l^T = W_l X_l^T     A = W_l  [d_{l+1}][dp_l]  B = Xs_l  [cap][dp_l]      K = d_l
+  //   gradient  gW_l^T = X_l^T dZ_l   A = XT_l [d_l][ldT]       B = dZT_l [d_{l+1}][ldT]   K = rows
+  //   backward  dX_l^T = W_l^T dZ_l^T A = WT_l [d_l][dp_{l+1}]  B = dZs_l [cap][dp_{l+1}]  K = d_{l+1}
+  // (dp_l = d_l padded to 8: 16-byte rows); the activation and gradient buffers hold their three
+  // parts one after the other.
+  struct Train {
+    long cap = 0, ldT = 0;
+    std::vector<int> dp;
+    std::vector<DBuf<__nv_bfloat16>> Wp, WT, Xs, XT, dZs, dZT;
+    DBuf<__nv_bfloat16> zero;  // the weights' second and third parts
+    std::vector<TcOperand> opW, opWT, opXs, opXT, opdZs, opdZT;
+    DBuf<float> part;
+  } tr;
 };
 
 // X[i][j] = (feature j of state i - x_mean[j]) / x_std[j]: Re Σ(ω_j), Im Σ(ω_j), T, μ, scale, ε_i - μ.
@@ -269,24 +266,182 @@ __global__ void correct_kernel(double2* __restrict__ S, int nw, const float* __r
   S[long(i) * nw + j] = v;
 }
 
+// A three-part operand over `parts` (three consecutive [rows][ld] BF16 blocks, or one block and
+// the shared zero block twice when zero is given), boxes of box_rows rows.
+static TcOperand three_part(const __nv_bfloat16* parts, const __nv_bfloat16* zero, long rows, long cols, long ld,
+                            int box_rows) {
+  TcOperand op;
+  op.ns = 3;
+  for (int p = 0; p < 3; ++p) {
+    const __nv_bfloat16* base = p == 0 ? parts : zero ? zero : parts + long(p) * rows * ld;
+    op.m[p] = make_tmap_bf16(base, rows, cols, ld, box_rows);
+    op.base[p] = base;
+  }
+  op.rows = rows;
+  op.cols = cols;
+  op.ld = ld;
+  return op;
+}
+
+// The BF16 weight rows of the products and their operands (fixed sizes; built once per network).
+static void train_weights_init(Mlp* P) {
+  Mlp::Train& T = P->tr;
+  const int L = P->L;
+  T.dp.resize(size_t(L + 1));
+  for (int l = 0; l <= L; ++l) T.dp[size_t(l)] = (P->dims[size_t(l)] + 7) / 8 * 8;
+  T.Wp.resize(size_t(L));
+  T.WT.resize(size_t(L));
+  size_t zmax = 0;
+  for (int l = 0; l < L; ++l) {
+    const long din = P->dims[size_t(l)], dout = P->dims[size_t(l + 1)];
+    T.Wp[size_t(l)].alloc(P->ctx, size_t(dout * T.dp[size_t(l)]));
+    T.WT[size_t(l)].alloc(P->ctx, size_t(din * T.dp[size_t(l + 1)]));
+    T.Wp[size_t(l)].zero(P->ctx->stream);  // the padding columns stay zero
+    T.WT[size_t(l)].zero(P->ctx->stream);
+    zmax = std::max(zmax, std::max(size_t(dout * T.dp[size_t(l)]), size_t(din * T.dp[size_t(l + 1)])));
+  }
+  T.zero.alloc(P->ctx, zmax);
+  T.zero.zero(P->ctx->stream);
+  T.opW.resize(size_t(L));
+  T.opWT.resize(size_t(L));
+  for (int l = 0; l < L; ++l) {
+    const long din = P->dims[size_t(l)], dout = P->dims[size_t(l + 1)];
+    T.opW[size_t(l)] = three_part(T.Wp[size_t(l)].p, T.zero.p, dout, din, T.dp[size_t(l)], kTcBM);
+    T.opWT[size_t(l)] = three_part(T.WT[size_t(l)].p, T.zero.p, din, dout, T.dp[size_t(l + 1)], kTcBM);
+  }
+}
+
 static void ensure_cap(Mlp* P, long n) {
   if (n <= P->cap) return;
   Ctx* ctx = P->ctx;
+  const int L = P->L;
   int dmax = 0;
   for (int d : P->dims) dmax = std::max(dmax, d);
-  P->Z.resize(size_t(P->L));
-  P->X.resize(size_t(P->L + 1));
-  for (int l = 0; l <= P->L; ++l) P->X[size_t(l)].alloc(ctx, size_t(n) * size_t(P->dims[size_t(l)]));
-  for (int l = 0; l < P->L; ++l) P->Z[size_t(l)].alloc(ctx, size_t(n) * size_t(P->dims[size_t(l + 1)]));
+  P->Z.resize(size_t(L));
+  P->X.resize(size_t(L + 1));
+  for (int l = 0; l <= L; ++l) P->X[size_t(l)].alloc(ctx, size_t(n) * size_t(P->dims[size_t(l)]));
+  for (int l = 0; l < L; ++l) P->Z[size_t(l)].alloc(ctx, size_t(n) * size_t(P->dims[size_t(l + 1)]));
   P->dA.alloc(ctx, size_t(n) * size_t(dmax));
   P->dB.alloc(ctx, size_t(n) * size_t(dmax));
   P->loss_rows.alloc(ctx, size_t(n));
   P->Yb.alloc(ctx, size_t(n) * size_t(P->dims.back()));
-  // split-K partials: a product is split only when its tiles cover the GPU less than twice, and
-  // slices x M x N <= (2 SMs / tiles) x tiles x 64 x 64
-  const size_t wmax = size_t(2) * size_t(ctx->sm_count) * 64 * 64;
-  P->work.alloc(ctx, wmax);
+  // the tensor-core operands of the activations and gradients, and the products' split-K slabs:
+  // a product of t tiles takes at most ceil(SMs / t) splits, so splits x M x N stays below
+  // (SMs + t) tiles of 128 x 128
+  Mlp::Train& T = P->tr;
+  T.cap = n;
+  T.ldT = (n + 7) / 8 * 8;
+  for (auto* v : {&T.Xs, &T.XT, &T.dZs, &T.dZT}) v->resize(size_t(L));
+  for (auto* v : {&T.opXs, &T.opXT, &T.opdZs, &T.opdZT}) v->resize(size_t(L));
+  const long sm = ctx->sm_count;
+  auto tiles = [](long M, long N) { return ((M + 127) / 128) * ((N + 127) / 128); };
+  long part = 0;
+  for (int l = 0; l < L; ++l) {
+    const long din = P->dims[size_t(l)], dout = P->dims[size_t(l + 1)];
+    const long dpi = T.dp[size_t(l)], dpo = T.dp[size_t(l + 1)];
+    T.Xs[size_t(l)].alloc(ctx, size_t(3 * n * dpi));
+    T.XT[size_t(l)].alloc(ctx, size_t(3 * din * T.ldT));
+    T.dZs[size_t(l)].alloc(ctx, size_t(3 * n * dpo));
+    T.dZT[size_t(l)].alloc(ctx, size_t(3 * dout * T.ldT));
+    T.opXs[size_t(l)] = three_part(T.Xs[size_t(l)].p, nullptr, n, din, dpi, 128);
+    T.opXT[size_t(l)] = three_part(T.XT[size_t(l)].p, nullptr, din, T.ldT, T.ldT, kTcBM);
+    T.opdZs[size_t(l)] = three_part(T.dZs[size_t(l)].p, nullptr, n, dout, dpo, 128);
+    T.opdZT[size_t(l)] = three_part(T.dZT[size_t(l)].p, nullptr, dout, T.ldT, T.ldT, 128);
+    for (const long t : {tiles(dout, n), tiles(din, dout), tiles(din, n)}) part = std::max(part, (sm + t) * 128 * 128);
+  }
+  T.part.alloc(ctx, size_t(part));
   P->cap = n;
+}
+
+// One three-part product into the split-K slabs T.part (out[s][m + ld_out n]); returns the splits.
+static int mlp_product(Mlp* P, const TcOperand& A, const TcOperand& B, int M, int N, int K, long ld_out) {
+  int bn = 0, sp = 0;
+  tc_gemm_shape(P->ctx, M, N, K, 16, 3, &bn, &sp);
+  if (bn != 128) fail(EPSP_EINVAL, "three-part products run with tiles of 128 columns");
+  if (size_t(sp) * size_t(M) * size_t(N) > P->tr.part.n) fail(EPSP_EINVAL, "split-K slabs exceed their buffer");
+  return tc_gemm_launch(P->ctx, A, B, M, N, K, P->tr.part.p, ld_out, long(M) * N, 16, P->d_err.p, "mlp");
+}
+
+static dim3 emit_grid(long cols, long rows) { return dim3(unsigned((cols + 31) / 32), unsigned((rows + 31) / 32)); }
+
+// Forward over the n rows in P->X[0] on the tensor cores; output in P->X[L]. With `train` the
+// transposed activations (the gradient products' operands) and the pre-activations Z are kept.
+static void forward_train(Mlp* P, long n, bool train) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  Mlp::Train& T = P->tr;
+  const dim3 blk(32, 8);
+  const int d0 = P->dims[0];
+  emit_kernel<kEmitCopy><<<emit_grid(d0, train ? T.ldT : n), blk, 0, s>>>(
+      int(n), d0, P->X[0].p, d0, nullptr, 0, 0, nullptr, false, nullptr, nullptr, nullptr, T.Xs[0].p, T.dp[0],
+      long(T.cap) * T.dp[0], train ? T.XT[0].p : nullptr, T.ldT, long(d0) * T.ldT);
+  EPSP_LAUNCHED(ctx);
+  for (int l = 0; l < P->L; ++l) {
+    const int din = P->dims[size_t(l)], dout = P->dims[size_t(l + 1)];
+    const bool last = l + 1 == P->L;
+    const int sp = mlp_product(P, T.opW[size_t(l)], T.opXs[size_t(l)], dout, int(n), din, dout);
+    const bool tpose = train && !last;
+    emit_kernel<kEmitBiasAct><<<emit_grid(dout, tpose ? T.ldT : n), blk, 0, s>>>(
+        int(n), dout, nullptr, 0, T.part.p, sp, long(dout) * n, P->b[size_t(l)].p, !last, nullptr,
+        (train && !last) ? P->Z[size_t(l)].p : nullptr, last ? P->X[size_t(P->L)].p : nullptr,
+        last ? nullptr : T.Xs[size_t(l + 1)].p, last ? 0 : T.dp[size_t(l + 1)], last ? 0 : long(T.cap) * T.dp[size_t(l + 1)],
+        tpose ? T.XT[size_t(l + 1)].p : nullptr, T.ldT, long(dout) * T.ldT);
+    EPSP_LAUNCHED(ctx);
+  }
+}
+
+// Gradients of the mean squared error of the batch in P->X[0], P->Yb (n rows, normalised by
+// n_total rows) into gW, gb; the batch's sum of squared errors goes to P->loss_sum[slot]. Needs the
+// forward with `train`.
+static void backward(Mlp* P, long n, long n_total, int slot) {
+  Ctx* ctx = P->ctx;
+  cudaStream_t s = ctx->stream;
+  Mlp::Train& T = P->tr;
+  const dim3 blk(32, 8);
+  const int L = P->L, dl = P->dims.back();
+  mse_kernel<<<unsigned(n), 256, 0, s>>>(P->X[size_t(L)].p, P->Yb.p, dl, 2.f / (float(n_total) * float(dl)), P->dA.p,
+                                         P->loss_rows.p);
+  EPSP_LAUNCHED(ctx);
+  sum_kernel<<<1, 256, 0, s>>>(P->loss_rows.p, n, P->loss_sum.p, slot);
+  EPSP_LAUNCHED(ctx);
+  // dZ of the last layer (linear output) as the products' operands
+  emit_kernel<kEmitCopy><<<emit_grid(dl, T.ldT), blk, 0, s>>>(
+      int(n), dl, P->dA.p, dl, nullptr, 0, 0, nullptr, false, nullptr, nullptr, nullptr, T.dZs[size_t(L - 1)].p,
+      T.dp[size_t(L)], long(T.cap) * T.dp[size_t(L)], T.dZT[size_t(L - 1)].p, T.ldT, long(dl) * T.ldT);
+  EPSP_LAUNCHED(ctx);
+  float* dZ = P->dA.p;  // FP32 dZ of layer l, [n][d_{l+1}]
+  float* other = P->dB.p;
+  for (int l = L - 1; l >= 0; --l) {
+    const int din = P->dims[size_t(l)], dout = P->dims[size_t(l + 1)];
+    // gW[o][i] = Σ_m dZ[m][o] X[m][i]: the product's slab element (i, o) at i + din o
+    const int sg = mlp_product(P, T.opXT[size_t(l)], T.opdZT[size_t(l)], din, dout, int(n), din);
+    partial_sum_kernel<<<div_up(size_t(dout) * size_t(din), 256), 256, 0, s>>>(T.part.p, dout, din, sg,
+                                                                               P->gW[size_t(l)].p, din, 1);
+    EPSP_LAUNCHED(ctx);
+    bias_grad_kernel<<<div_up(size_t(dout), 128), 128, 0, s>>>(dZ, n, dout, P->gb[size_t(l)].p);
+    EPSP_LAUNCHED(ctx);
+    if (l > 0) {
+      // dX[m][i] = Σ_o dZ[m][o] W[o][i] (slab element (i, m) at i + din m), through SiLU of layer l - 1
+      const int sx = mlp_product(P, T.opWT[size_t(l)], T.opdZs[size_t(l)], din, int(n), dout, din);
+      emit_kernel<kEmitActBack><<<emit_grid(din, T.ldT), blk, 0, s>>>(
+          int(n), din, nullptr, 0, T.part.p, sx, long(din) * n, nullptr, false, P->Z[size_t(l - 1)].p, nullptr, other,
+          T.dZs[size_t(l - 1)].p, T.dp[size_t(l)], long(T.cap) * T.dp[size_t(l)], T.dZT[size_t(l - 1)].p, T.ldT,
+          long(din) * T.ldT);
+      EPSP_LAUNCHED(ctx);
+      std::swap(dZ, other);
+    }
+  }
+}
+
+// Reports (and clears) a bounded wait that ran out in the network's tensor-core products.
+static void check_mlp_err(Mlp* P) {
+  int e = 0;
+  P->d_err.download(&e, 1, P->ctx->stream);
+  EPSP_CUDA(cudaStreamSynchronize(P->ctx->stream));
+  if (e) {
+    P->d_err.zero(P->ctx->stream);
+    fail(EPSP_EDEVICE_TIMEOUT, "a tensor-core GEMM wait ran out in the warm-start network (bounded device wait)");
+  }
 }
 
 // ---- tensor-core inference (the scGD0 hook on the tensor-core path) ----
@@ -416,50 +571,6 @@ static void forward_tc(Mlp* P, long n, int* d_err) {
   }
 }
 
-// Forward over the rows in P->X[0] (n rows); output in P->X[L].
-static void forward(Mlp* P, long n) {
-  Ctx* ctx = P->ctx;
-  for (int l = 0; l < P->L; ++l) {
-    const int din = P->dims[size_t(l)], dout = P->dims[size_t(l + 1)];
-    mlp_gemm<float, __nv_bfloat16>(ctx, P->work.p, int(n), dout, din, P->X[size_t(l)].p, din, 1, P->Wbf[size_t(l)].p, 1,
-                                   din, P->Z[size_t(l)].p, dout, 1);
-    bias_act_kernel<<<div_up(size_t(n * dout), 256), 256, 0, ctx->stream>>>(P->Z[size_t(l)].p, P->b[size_t(l)].p, n, dout,
-                                                                          l + 1 < P->L, P->X[size_t(l + 1)].p);
-    EPSP_LAUNCHED(ctx);
-  }
-}
-
-// Gradients of the mean squared error of the batch in P->X[0], P->Yb (n rows, normalised by
-// n_total rows) into gW, gb; the batch's sum of squared errors goes to P->loss_sum[slot].
-static void backward(Mlp* P, long n, long n_total, int slot) {
-  Ctx* ctx = P->ctx;
-  cudaStream_t s = ctx->stream;
-  const int dl = P->dims.back();
-  mse_kernel<<<unsigned(n), 256, 0, s>>>(P->X[size_t(P->L)].p, P->Yb.p, dl, 2.f / (float(n_total) * float(dl)), P->dA.p,
-                                         P->loss_rows.p);
-  EPSP_LAUNCHED(ctx);
-  sum_kernel<<<1, 256, 0, s>>>(P->loss_rows.p, n, P->loss_sum.p, slot);
-  EPSP_LAUNCHED(ctx);
-  float* dZ = P->dA.p;  // gradient w.r.t. the last pre-activation (linear output)
-  float* other = P->dB.p;
-  for (int l = P->L - 1; l >= 0; --l) {
-    const int din = P->dims[size_t(l)], dout = P->dims[size_t(l + 1)];
-    // gW[o][i] = Σ_m dZ[m][o] X[m][i]
-    mlp_gemm<float, float>(ctx, P->work.p, dout, din, int(n), dZ, 1, dout, P->X[size_t(l)].p, din, 1, P->gW[size_t(l)].p,
-                           din, 1);
-    bias_grad_kernel<<<div_up(size_t(dout), 128), 128, 0, s>>>(dZ, n, dout, P->gb[size_t(l)].p);
-    EPSP_LAUNCHED(ctx);
-    if (l > 0) {
-      // dX[m][i] = Σ_o dZ[m][o] W[o][i], then through SiLU of layer l-1
-      mlp_gemm<float, __nv_bfloat16>(ctx, P->work.p, int(n), din, dout, dZ, dout, 1, P->Wbf[size_t(l)].p, din, 1, other,
-                                     din, 1);
-      act_back_kernel<<<div_up(size_t(n * din), 256), 256, 0, s>>>(other, P->Z[size_t(l - 1)].p, n * din, other);
-      EPSP_LAUNCHED(ctx);
-      std::swap(dZ, other);
-    }
-  }
-}
-
 static void adam(Mlp* P, float lr) {
   Ctx* ctx = P->ctx;
   cudaStream_t s = ctx->stream;
@@ -468,12 +579,14 @@ static void adam(Mlp* P, float lr) {
   EPSP_LAUNCHED(ctx);
   for (int l = 0; l < P->L; ++l) {
     const long nw = long(P->dims[size_t(l)]) * P->dims[size_t(l + 1)], nb = P->dims[size_t(l + 1)];
-    adam_kernel<<<div_up(size_t(nw), 256), 256, 0, s>>>(P->W[size_t(l)].p, P->gW[size_t(l)].p, P->mW[size_t(l)].p,
-                                                        P->vW[size_t(l)].p, nw, lr, b1, b2, eps, P->d_step.p,
-                                                        P->Wbf[size_t(l)].p);
+    adam_kernel<<<div_up(size_t(nw), 256), 256, 0, s>>>(
+        P->W[size_t(l)].p, P->gW[size_t(l)].p, P->mW[size_t(l)].p, P->vW[size_t(l)].p, nw, lr, b1, b2, eps, P->d_step.p,
+        P->Wbf[size_t(l)].p, P->dims[size_t(l)], P->tr.Wp[size_t(l)].p, P->tr.dp[size_t(l)], P->tr.WT[size_t(l)].p,
+        P->tr.dp[size_t(l + 1)]);
     EPSP_LAUNCHED(ctx);
     adam_kernel<<<div_up(size_t(nb), 256), 256, 0, s>>>(P->b[size_t(l)].p, P->gb[size_t(l)].p, P->mb[size_t(l)].p,
-                                                        P->vb[size_t(l)].p, nb, lr, b1, b2, eps, P->d_step.p, nullptr);
+                                                        P->vb[size_t(l)].p, nb, lr, b1, b2, eps, P->d_step.p, nullptr, 1,
+                                                        nullptr, 0, nullptr, 0);
     EPSP_LAUNCHED(ctx);
   }
 }
@@ -507,10 +620,12 @@ void warmstart_correct(epsp_warmstart* w, Ctx* ctx, double2* S_T, long nw, long 
   features_kernel<<<dim3(div_up(size_t(2 * nw + 4), 256), unsigned(ni)), 256, 0, s>>>(
       S_T, int(nw), int(ni), d_eps_i, T, mu, scale, P.x_mean.p, P.x_std.p, P.X[0].p);
   EPSP_LAUNCHED(ctx);
-  if (tc_err)
+  if (tc_err) {
     forward_tc(&P, ni, tc_err);
-  else
-    forward(&P, ni);
+  } else {
+    forward_train(&P, ni, false);
+    check_mlp_err(&P);
+  }
   correct_kernel<<<dim3(div_up(size_t(nw), 256), unsigned(ni)), 256, 0, s>>>(S_T, int(nw), P.X[size_t(P.L)].p, P.y_scale,
                                                                             P.y_mean.p);
   EPSP_LAUNCHED(ctx);
@@ -568,6 +683,9 @@ epsp_status epsp_warmstart_create(epsp_ctx* ctx, int32_t nlayers, const int32_t*
     P.loss_sum.alloc(P.ctx, 1);
     P.d_step.alloc(P.ctx, 1);
     P.d_step.zero(P.ctx->stream);
+    P.d_err.alloc(P.ctx, 1);
+    P.d_err.zero(P.ctx->stream);
+    train_weights_init(&P);
     EPSP_CUDA(cudaStreamSynchronize(P.ctx->stream));
     *out = guard.release();
   });
@@ -580,6 +698,10 @@ void epsp_warmstart_destroy(epsp_warmstart* w) {
 }
 
 int64_t epsp_warmstart_nparams(const epsp_warmstart* w) { return w ? nparams(&w->m) : 0; }
+
+/* Device milliseconds of the epochs of the last epsp_warmstart_train (CUDA events around each
+ * epoch's graph replay; the uploads and the capture are not included). */
+double epsp_warmstart_train_ms(const epsp_warmstart* w) { return w ? w->m.train_ms : 0.0; }
 
 /* Parameters as one flat FP32 vector: for each layer, W [d_{l+1}][d_l] then b [d_{l+1}]. Setting
  * them resets the optimiser state. */
@@ -595,7 +717,9 @@ epsp_status epsp_warmstart_set_params(epsp_warmstart* w, const float* params) {
       off += nw;
       P.b[size_t(l)].upload(params + off, size_t(nb), s);
       off += nb;
-      to_bf16_kernel<<<div_up(size_t(nw), 256), 256, 0, s>>>(P.W[size_t(l)].p, nw, P.Wbf[size_t(l)].p);
+      to_bf16_kernel<<<div_up(size_t(nw), 256), 256, 0, s>>>(P.W[size_t(l)].p, nw, P.dims[size_t(l)], P.Wbf[size_t(l)].p,
+                                                             P.tr.Wp[size_t(l)].p, P.tr.dp[size_t(l)],
+                                                             P.tr.WT[size_t(l)].p, P.tr.dp[size_t(l + 1)]);
       EPSP_LAUNCHED(P.ctx);
       P.mW[size_t(l)].zero(s);
       P.vW[size_t(l)].zero(s);
@@ -662,10 +786,10 @@ epsp_status epsp_warmstart_predict(epsp_warmstart* w, const float* X, int64_t n,
     for (long r0 = 0; r0 < n; r0 += chunk) {
       const long nb = std::min(chunk, n - r0);
       P.X[0].upload(X + r0 * P.dims[0], size_t(nb * P.dims[0]), s);
-      forward(&P, nb);
+      forward_train(&P, nb, false);
       P.X[size_t(P.L)].download(Y + r0 * P.dims.back(), size_t(nb * P.dims.back()), s);
     }
-    EPSP_CUDA(cudaStreamSynchronize(s));
+    check_mlp_err(&P);
   });
 }
 
@@ -679,7 +803,7 @@ epsp_status epsp_warmstart_grad(epsp_warmstart* w, const float* X, const float* 
     ensure_cap(&P, n);
     P.X[0].upload(X, size_t(n * P.dims[0]), s);
     P.Yb.upload(Y, size_t(n * P.dims.back()), s);
-    forward(&P, n);
+    forward_train(&P, n, true);
     backward(&P, n, n, 0);
     long off = 0;
     for (int l = 0; l < P.L; ++l) {
@@ -691,7 +815,7 @@ epsp_status epsp_warmstart_grad(epsp_warmstart* w, const float* X, const float* 
     }
     double ls = 0;
     P.loss_sum.download(&ls, 1, s);
-    EPSP_CUDA(cudaStreamSynchronize(s));
+    check_mlp_err(&P);
     if (loss) *loss = ls / (double(n) * P.dims.back());
   });
 }
@@ -734,7 +858,7 @@ epsp_status epsp_warmstart_train(epsp_warmstart* w, const float* X, const float*
         EPSP_LAUNCHED(P.ctx);
         gather_rows_kernel<<<div_up(size_t(nb * dl), 256), 256, 0, s>>>(P.dataY.p, d_perm.p + r0, nb, dl, P.Yb.p);
         EPSP_LAUNCHED(P.ctx);
-        forward(&P, nb);
+        forward_train(&P, nb, true);
         backward(&P, nb, nb, int(bi));
         adam(&P, lr);
       }
@@ -749,6 +873,19 @@ epsp_status epsp_warmstart_train(epsp_warmstart* w, const float* X, const float*
         if (*g) cudaGraphDestroy(*g);
       }
     } gguard{&graph, &exec};
+    // one gradient pass on the first minibatch outside the capture (no parameter update), so that
+    // every kernel's launch attributes are set before the capture
+    {
+      const long nb = std::min<long>(batch, n);
+      d_perm.upload(perm ? perm : ident.data(), size_t(n), s);
+      gather_rows_kernel<<<div_up(size_t(nb * d0), 256), 256, 0, s>>>(P.dataX.p, d_perm.p, nb, d0, P.X[0].p);
+      EPSP_LAUNCHED(P.ctx);
+      gather_rows_kernel<<<div_up(size_t(nb * dl), 256), 256, 0, s>>>(P.dataY.p, d_perm.p, nb, dl, P.Yb.p);
+      EPSP_LAUNCHED(P.ctx);
+      forward_train(&P, nb, true);
+      backward(&P, nb, nb, 0);
+      check_mlp_err(&P);
+    }
     const int64_t l0 = P.ctx->launches;
     EPSP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     try {
@@ -761,12 +898,27 @@ epsp_status epsp_warmstart_train(epsp_warmstart* w, const float* X, const float*
     EPSP_CUDA(cudaGraphInstantiate(&exec, graph, 0));
     const int64_t per_epoch = P.ctx->launches - l0;
     P.ctx->launches = l0;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    struct EventGuard {
+      cudaEvent_t* e;
+      ~EventGuard() {
+        for (int k = 0; k < 2; ++k)
+          if (e[k]) cudaEventDestroy(e[k]);
+      }
+    } eguard{ev};
+    for (auto& e : ev) EPSP_CUDA(cudaEventCreate(&e));
+    P.train_ms = 0;
     for (int e = 0; e < epochs; ++e) {
       d_perm.upload(perm ? perm + long(e) * n : ident.data(), size_t(n), s);
+      EPSP_CUDA(cudaEventRecord(ev[0], s));
       EPSP_CUDA(cudaGraphLaunch(exec, s));
+      EPSP_CUDA(cudaEventRecord(ev[1], s));
       P.ctx->launches += per_epoch;
       P.loss_sum.download(bl.data(), size_t(nbat), s);
-      EPSP_CUDA(cudaStreamSynchronize(s));
+      check_mlp_err(&P);
+      float ms = 0;
+      EPSP_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+      P.train_ms += double(ms);
       double tot = 0;
       for (double v : bl) tot += v;
       if (loss_history) loss_history[e] = tot / (double(n) * dl);

@@ -20,6 +20,16 @@ constexpr int kNs = 3;
 // K-blocks of 64 summed by one FP32 accumulator at most: the Fan-Migdal sums are long and of one
 // sign, and their FP32 rounding must stay well below the iteration's tol (1e-6 eV)
 constexpr int kKbCap = 16;
+// The Kramers-Kronig product's bound: its terms cancel (principal value), so the FP32 rounding of
+// a long accumulation is large against the result (at 4101 nodes and 800 K, 16 K blocks per
+// accumulator left |ΔReΣ| ~1e-5 eV against FP64, 4 K blocks ~3x less).
+constexpr int kKbCapKK = 4;
+// Split limit of a product of depth K: enough splits that no FP32 accumulator sums more than cap
+// K blocks (the Fan-Migdal product of a 32^3 model has ~680), and at least 16.
+static int max_splits_for(long K, int cap = kKbCap) {
+  const long kb = (K + kTcBK - 1) / kTcBK;
+  return int(std::max<long>(16, (kb + cap - 1) / cap));
+}
 
 struct Scgd0Plan::Tc {
   long Kp = 0, Kp2 = 0;
@@ -556,7 +566,7 @@ void tc_setup(Scgd0Plan* P) {
     split3_rows_kernel<<<div_up(size_t(nw * T->Kp2), 256), 256, 0, s>>>(P->d_KK.p, nw, nw, nw, T->Kp2, true, T->KK[0].p,
                                                                         T->KK[1].p, T->KK[2].p);
     EPSP_LAUNCHED(ctx);
-    tc_gemm_shape(ctx, int(nw), int(ni), int(nw), 16, kNs, &T->bn2, &T->splits2, kKbCap);
+    tc_gemm_shape(ctx, int(nw), int(ni), int(nw), max_splits_for(nw, kKbCapKK), kNs, &T->bn2, &T->splits2, kKbCapKK);
     T->part.alloc(ctx, size_t(T->splits2) * size_t(nw * ni));
     T->Sf.alloc(ctx, size_t(nw * ni));
     T->opKK = operand(T->KK, nw, nw, T->Kp2, kTcBM);
@@ -592,8 +602,8 @@ void tc_setup(Scgd0Plan* P) {
   split3_rows_kernel<<<div_up(size_t(nw * T->Kp2), 256), 256, 0, s>>>(P->d_KK.p, nw, nw, nw, T->Kp2, true, T->KK[0].p,
                                                                       T->KK[1].p, T->KK[2].p);
   EPSP_LAUNCHED(ctx);
-  tc_gemm_shape(ctx, int(nw), int(ni), int(nk), 16, kNs, &T->bn1, &T->splits1, kKbCap);
-  tc_gemm_shape(ctx, int(nw), int(ni), int(nw), 16, kNs, &T->bn2, &T->splits2, kKbCap);
+  tc_gemm_shape(ctx, int(nw), int(ni), int(nk), max_splits_for(nk), kNs, &T->bn1, &T->splits1, kKbCap);
+  tc_gemm_shape(ctx, int(nw), int(ni), int(nw), max_splits_for(nw, kKbCapKK), kNs, &T->bn2, &T->splits2, kKbCapKK);
   T->part.alloc(ctx, size_t(std::max(T->splits1, T->splits2)) * size_t(nw * ni));
   const long nwm = nw * P->nm;
   T->xf.alloc(ctx, size_t(2 * nwm));
@@ -731,8 +741,8 @@ void tc_imsigma(Scgd0Plan* P, const double2* d_Sin, double* d_ImS) {
   EPSP_LAUNCHED(ctx);
   prof_end(ctx, pk);
   const long slab = nw * ni;
-  int sp = tc_gemm_launch(ctx, T->opK, T->opG, int(nw), int(ni), int(nk), T->part.p, nw, slab, 16, T->err.p, "tc_fm",
-                          kKbCap);
+  int sp = tc_gemm_launch(ctx, T->opK, T->opG, int(nw), int(ni), int(nk), T->part.p, nw, slab, max_splits_for(nk),
+                          T->err.p, "tc_fm", kKbCap);
   finalize_add_kernel<<<div_up(size_t(slab), 256), 256, 0, s>>>(T->part.p, slab, sp, slab, d_ImS);
   EPSP_LAUNCHED(ctx);
   check_err(P);
@@ -746,8 +756,8 @@ void tc_kk_assemble(Scgd0Plan* P, double2* d_Snew) {
   split3_rows_kernel<<<div_up(size_t(ni * T->Kp2), 256), 256, 0, s>>>(P->d_ImS.p, nw, ni, nw, T->Kp2, false, T->Im[0].p,
                                                                       T->Im[1].p, T->Im[2].p);
   EPSP_LAUNCHED(ctx);
-  int sp = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(ni), int(nw), T->part.p, nw, slab, 16, T->err.p, "tc_kk",
-                          kKbCap);
+  int sp = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(ni), int(nw), T->part.p, nw, slab,
+                          max_splits_for(nw, kKbCapKK), T->err.p, "tc_kk", kKbCapKK);
   finalize_assemble_kernel<<<div_up(size_t(slab), 256), 256, 0, s>>>(T->part.p, slab, sp, slab, P->d_ImS.p, d_Snew);
   EPSP_LAUNCHED(ctx);
 }
@@ -770,8 +780,8 @@ void tc_reserve(Scgd0Plan* P, long nT) {
   size_t part = 0;
   for (long a = 1; a <= nT; ++a) {
     int bn, sp1 = 1, sp2;
-    if (!P->disp) tc_gemm_shape(ctx, int(a * nw), int(ni), int(nk), 16, kNs, &bn, &sp1, kKbCap);
-    tc_gemm_shape(ctx, int(nw), int(a * ni), int(nw), 16, kNs, &bn, &sp2, kKbCap);
+    if (!P->disp) tc_gemm_shape(ctx, int(a * nw), int(ni), int(nk), max_splits_for(nk), kNs, &bn, &sp1, kKbCap);
+    tc_gemm_shape(ctx, int(nw), int(a * ni), int(nw), max_splits_for(nw, kKbCapKK), kNs, &bn, &sp2, kKbCapKK);
     part = std::max(part, size_t(std::max(sp1, sp2)) * size_t(a * slab));
   }
   T->part.alloc(ctx, part);
@@ -828,8 +838,8 @@ void tc_iterate(Scgd0Plan* P, int nA, const int* d_slots, const int* slots_h, co
   prof_end(ctx, pk);
   // ImΣ of every slot: the stacked K_t rows times G
   const long M = long(nA) * nw;
-  int sp = tc_gemm_launch(ctx, T->opK, T->opG, int(M), int(ni), int(nk), T->part.p, M, M * ni, 16, T->err.p, "tc_fm",
-                          kKbCap);
+  int sp = tc_gemm_launch(ctx, T->opK, T->opG, int(M), int(ni), int(nk), T->part.p, M, M * ni, max_splits_for(nk),
+                          T->err.p, "tc_fm", kKbCap);
   // ImΣ of every slot, and its BF16 split as the B operand of ReΣ = KK ImΣ (columns: the slots'
   // states in order)
   long pf = prof_begin(ctx, "finalize");
@@ -848,8 +858,8 @@ static void tc_kk_tail(Scgd0Plan* P, int nA, const int* d_slots, double2* d_S_al
   auto* T = P->tc.get();
   const long nw = P->nw, ni = P->ni, slab = nw * ni;
   const long N2 = long(nA) * ni;
-  int sp2 = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(N2), int(nw), T->part.p, nw, nw * N2, 16, T->err.p,
-                           "tc_kk", kKbCap);
+  int sp2 = tc_gemm_launch(ctx, T->opKK, T->opIm, int(nw), int(N2), int(nw), T->part.p, nw, nw * N2,
+                           max_splits_for(nw, kKbCapKK), T->err.p, "tc_kk", kKbCapKK);
   long pf = prof_begin(ctx, "kk_epilogue");
   kk_epilogue_kernel<<<dim3(div_up(size_t(nw), 255), unsigned(P->ngroups), unsigned(nA)), 256, 0, s>>>(
       T->part.p, sp2, nw * N2, T->ImS_b.p, int(nw), slab, d_slots, P->d_gptr.p, P->d_gidx.p, P->d_ws.p, P->d_eps_i.p,

@@ -180,6 +180,45 @@ static void launch_pair(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M,
   EPSP_LAUNCHED(ctx);
 }
 
+// The persistent CTA-pair kernel: one cluster of two CTAs per SM pair over all items.
+template <int BN, int STAGES, int NS, int BK, bool TF32>
+static void launch_pair_persist(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int kblocks, int per,
+                                int splits, float* out, long ld_out, long split_stride, int* d_err, int gm = 1) {
+  using L = TcPairPSmem<BN, STAGES, NS, BK, TF32>;
+  if (A.bk != BK || B.bk != BK) fail(EPSP_EINVAL, "operand tensor maps were built for another K block");
+  if (A.tf32 != TF32 || B.tf32 != TF32) fail(EPSP_EINVAL, "operand tensor maps were built for another element type");
+  auto* kern = tc_gemm_pair_persist_kernel<BN, STAGES, NS, BK, TF32>;
+  static bool configured = false;  // one process, one attribute setting per instantiation
+  if (!configured) {
+    EPSP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, L::kBytes));
+    configured = true;
+  }
+  TcMaps maps;
+  for (int p = 0; p < 3; ++p) {
+    maps.a[p] = A.m[p < NS ? p : 0];
+    maps.b[p] = p < NS ? remap(B, p, BN / 2) : maps.b[0];  // B halves of BN / 2 rows, each part encoded once
+  }
+  const int nN = (N + BN - 1) / BN, nM2 = (M + 2 * kTcBM - 1) / (2 * kTcBM);
+  const long items = long(nN) * nM2 * splits;
+  if (items > (1l << 30)) fail(EPSP_EINVAL, "too many tiles for the persistent kernel");
+  const int npairs = int(std::min<long>(std::max(1, ctx->sm_count / 2), items));
+  cudaLaunchAttribute cl;
+  cl.id = cudaLaunchAttributeClusterDimension;
+  cl.val.clusterDim.x = 2;
+  cl.val.clusterDim.y = 1;
+  cl.val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(2 * npairs), 1, 1);
+  cfg.blockDim = dim3(192);
+  cfg.dynamicSmemBytes = L::kBytes;
+  cfg.stream = ctx->stream;
+  cfg.attrs = &cl;
+  cfg.numAttrs = 1;
+  EPSP_CUDA(cudaLaunchKernelEx(&cfg, kern, maps, M, N, kblocks, per, nN, nM2, int(items), out, ld_out, split_stride,
+                               d_err, gm));
+  EPSP_LAUNCHED(ctx);
+}
+
 int tc_gemm_launch(Ctx* ctx, const TcOperand& A, const TcOperand& B, int M, int N, int K, float* out, long ld_out,
                    long split_stride, int max_splits, int* d_err, const char* prof_name, int kb_cap) {
   if (A.tf32 || B.tf32) fail(EPSP_EINVAL, "TF32 operands take tc_gemm_launch_with");
@@ -218,7 +257,7 @@ int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn
                         float* out, long ld_out, long split_stride, int* d_err, const char* prof_name, bool persist,
                         bool pair, int gm) {
   if (bn != 128 && bn != 256) fail(EPSP_EINVAL, "tile width must be 128 or 256");
-  if (pair && (persist || bn != 256)) fail(EPSP_EINVAL, "the CTA-pair kernel is one-tile, tile width 256");
+  if (pair && bn != 256) fail(EPSP_EINVAL, "the CTA-pair kernels take tile width 256");
   if (A.tf32 || B.tf32) {
     if (!(A.tf32 && B.tf32 && A.ns == 1 && B.ns == 1 && A.bk == 32 && B.bk == 32))
       fail(EPSP_EINVAL, "TF32 operands are one-part maps with K boxes of 32 on both sides");
@@ -228,7 +267,10 @@ int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn
     const int per = (kblocks + splits - 1) / splits;
     splits = (kblocks + per - 1) / per;
     long pi = prof_begin(ctx, prof_name);
-    if (pair)
+    if (pair && persist)
+      launch_pair_persist<256, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err,
+                                               gm);
+    else if (pair)
       launch_pair<256, 6, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
     else if (persist && bn == 256)
       launch_persist<256, 4, 1, 32, true>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
@@ -252,7 +294,10 @@ int tc_gemm_launch_with(Ctx* ctx, const TcOperand& A, const TcOperand& B, int bn
   if (persist && !(bk == 32 && bn == 256)) fail(EPSP_EINVAL, "the persistent kernel takes tile width 256 with K blocks of 32");
   if (pair && bk != 32) fail(EPSP_EINVAL, "the BF16x3 CTA-pair kernel takes K blocks of 32");
   long pi = prof_begin(ctx, prof_name);
-  if (pair)
+  if (pair && persist)
+    launch_pair_persist<256, 6, 2, 32, false>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err,
+                                              gm);
+  else if (pair)
     launch_pair<256, 6, 2, 32, false>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
   else if (persist)
     launch_persist<256, 4, 2, 32>(ctx, A, B, M, N, kblocks, per, splits, out, ld_out, split_stride, d_err, gm);
@@ -302,11 +347,13 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
         cand.push_back(TcTune{bn, sp, 32, 0.f});
         cand.push_back(TcTune{bn, sp, 32, 0.f, true});
         if (bn == 256) cand.push_back(TcTune{bn, sp, 32, 0.f, false, true});  // CTA pairs
+        if (bn == 256) cand.push_back(TcTune{bn, sp, 32, 0.f, true, true});   // persistent CTA pairs
         for (int g : {gm, 4 * gm}) {  // the same kernels in grouped tile order, two group sizes
           if (gm <= 1) break;
           cand.push_back(TcTune{bn, sp, 32, 0.f, false, false, g});
           cand.push_back(TcTune{bn, sp, 32, 0.f, true, false, g});
           if (bn == 256) cand.push_back(TcTune{bn, sp, 32, 0.f, false, true, g});
+          if (bn == 256) cand.push_back(TcTune{bn, sp, 32, 0.f, true, true, g});
         }
         continue;
       }
@@ -315,11 +362,13 @@ TcTune tc_gemm_autotune(Ctx* ctx, const TcOperand& A, const TcOperand& B128, con
         cand.push_back(TcTune{bn, sp, 32, 0.f});
         cand.push_back(TcTune{bn, sp, 32, 0.f, true});
         cand.push_back(TcTune{bn, sp, 32, 0.f, false, true});  // CTA pairs
+        cand.push_back(TcTune{bn, sp, 32, 0.f, true, true});   // persistent CTA pairs
         for (int g : {gm, 4 * gm}) {
           if (gm <= 1) break;
           cand.push_back(TcTune{bn, sp, 32, 0.f, false, false, g});
           cand.push_back(TcTune{bn, sp, 32, 0.f, true, false, g});
           cand.push_back(TcTune{bn, sp, 32, 0.f, false, true, g});
+          cand.push_back(TcTune{bn, sp, 32, 0.f, true, true, g});
         }
       }
     }

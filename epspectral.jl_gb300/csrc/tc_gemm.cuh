@@ -716,6 +716,218 @@ __global__ void __launch_bounds__(128, 1)
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
 }
 
+// ---- persistent CTA-pair variant ----
+// The CTA-pair kernel run persistently: cluster p of two CTAs takes the items (pair of M tiles,
+// N tile, split) i = p, p + npairs, ... in the one-tile kernel's order, with two TMEM accumulators
+// of BN columns per CTA (allocated by both CTAs together), so that both CTAs' epilogues drain item
+// t while the leader's products run item t + 1. Barriers: full (the leader's: both CTAs' copies
+// of a stage, as in the one-tile pair kernel), empty and accumulator-full (each CTA's, from the
+// leader's commits to both), accumulator-empty (the leader's: eight arrivals, the four epilogue
+// warps of each CTA, the peer's through their cluster addresses), done. 192 threads: warp 0 the
+// producer, warp 1 the leader's MMA issuer, warps 2-5 the epilogue (TMEM lanes 32 (warp % 4)..).
+template <int BN, int STAGES, int NS, int BK, bool TF32>
+struct TcPairPSmem {
+  static constexpr int kES = TF32 ? 4 : 2;
+  static constexpr int kRB = BK * kES;
+  static constexpr int kA = kTcBM * kRB;        // this CTA's 128 A rows
+  static constexpr int kBh = (BN / 2) * kRB;    // this CTA's half of the B tile
+  static constexpr int kStage = NS * kA + NS * kBh;
+  static constexpr int kBars = 2 * STAGES + 5;  // full, empty, accumulator full x2, empty x2, done
+  static constexpr int kBytes = STAGES * kStage + 8 * kBars + 16 + 1024;
+};
+
+// Arrival on an mbarrier of another CTA of the cluster (addr from mapa).
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(addr) : "memory");
+}
+
+template <int BN, int STAGES, int NS, int BK, bool TF32>
+__global__ void __launch_bounds__(192, 1)
+    tc_gemm_pair_persist_kernel(const __grid_constant__ TcMaps maps, int M, int N, int kblocks, int kb_per_split,
+                                int nN, int nM2, int nitems, float* __restrict__ out, long ld_out, long split_stride,
+                                int* __restrict__ err, int gm = 1) {
+  using L = TcPairPSmem<BN, STAGES, NS, BK, TF32>;
+  static_assert(!TF32 || NS == 1, "TF32 operands have one part");
+  static_assert((BN / 2) % 8 == 0 && 2 * BN <= 512, "B halves of whole 8-row swizzle groups; two accumulators");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * L::kStage);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + L::kBars);
+  __shared__ int s_abort;
+  const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * STAGES, accf0 = full0 + 16 * STAGES,
+                 acce0 = accf0 + 16, done_bar = accf0 + 32;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const uint32_t rank = cluster_ctarank();  // 0: the leader, which issues the MMAs
+  const int pair = int(blockIdx.x >> 1), npairs = int(gridDim.x >> 1);
+  auto coords = [&](int item, int& n0, int& m0, int& z, int& kb0, int& nkb) {
+    int nt, mt;
+    tile_of(item % (nN * nM2), nN, nM2, gm, nt, mt);
+    n0 = nt * BN;
+    m0 = mt * 2 * kTcBM + int(rank) * kTcBM;
+    z = item / (nN * nM2);
+    kb0 = z * kb_per_split;
+    nkb = max(0, min(kblocks, kb0 + kb_per_split) - kb0);
+  };
+  auto aborted = [&] { return *(volatile int*)&s_abort != 0; };
+
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int s = 0; s < 2 * STAGES; ++s) mbar_init(smem_u32(bars + s), 1);
+    mbar_init(accf0, 1);
+    mbar_init(accf0 + 8, 1);
+    mbar_init(acce0, 8);
+    mbar_init(acce0 + 8, 8);
+    mbar_init(done_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(2 * BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  cluster_sync_all();  // both CTAs' barriers initialised and TMEM allocated
+
+  if (warp == 0 && lane == 0) {
+    // producer: this CTA's A rows and B half of every item, completing on the leader's full barrier
+    int g = 0;
+    bool stop = false;
+    for (int item = pair; item < nitems && !stop; item += npairs) {
+      int n0, m0, z, kb0, nkb;
+      coords(item, n0, m0, z, kb0, nkb);
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = g % STAGES;
+        const uint32_t ph = (g / STAGES) & 1;
+        if (g >= STAGES && !mbar_wait(empty0 + 8 * s, ph ^ 1)) {
+          atomicExch(&s_abort, 1);
+          stop = true;
+          break;
+        }
+        if (aborted()) {
+          stop = true;
+          break;
+        }
+        uint8_t* st = smem + s * L::kStage;
+        const uint32_t fb = mapa_shared(full0 + 8 * s, 0);
+        if (rank == 0) mbar_expect_tx(full0 + 8 * s, 2 * L::kStage);
+        const int kc = (kb0 + kb) * BK;
+#pragma unroll
+        for (int p = 0; p < NS; ++p) {
+          tma_load_2d_pair(smem_u32(st + p * L::kA), &maps.a[p], kc, m0, fb);
+          tma_load_2d_pair(smem_u32(st + NS * L::kA + p * L::kBh), &maps.b[p], kc, n0 + int(rank) * (BN / 2), fb);
+        }
+        ++g;
+      }
+    }
+    // the leader's last releases of this CTA's stages have landed (bounded)
+    for (int k = max(0, g - STAGES); k < g; ++k)
+      if (!mbar_wait(empty0 + 8 * (k % STAGES), (k / STAGES) & 1)) {
+        atomicExch(&s_abort, 1);
+        break;
+      }
+  } else if (warp == 1 && lane == 0 && rank == 0) {
+    // MMA issuer (leader only): M = 256 over both CTAs' operands, accumulators alternating per item
+    constexpr uint32_t idesc = idesc_pair<TF32>(BN);
+    int g = 0, t = 0;
+    bool stop = false;
+    for (int item = pair; item < nitems && !stop; item += npairs, ++t) {
+      int n0, m0, z, kb0, nkb;
+      coords(item, n0, m0, z, kb0, nkb);
+      const int b = t & 1;
+      const uint32_t acc = tmem + uint32_t(b * BN);
+      if (t >= 2 && !mbar_wait(acce0 + 8 * b, ((t >> 1) & 1) ^ 1)) {  // both CTAs' epilogues drained it
+        atomicExch(&s_abort, 1);
+        break;
+      }
+      tc_fence_after();
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = g % STAGES;
+        const uint32_t ph = (g / STAGES) & 1;
+        if (!mbar_wait(full0 + 8 * s, ph)) {
+          atomicExch(&s_abort, 1);
+          stop = true;
+          break;
+        }
+        if (aborted()) {
+          stop = true;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(smem + s * L::kStage);
+        const uint32_t b0 = a0 + NS * L::kA;
+#pragma unroll
+        for (int ks = 0; ks < L::kRB / 32; ++ks) {
+          const uint32_t off = ks * 32;
+          umma_pair<TF32>(acc, sw_desc<L::kRB>(a0 + off), sw_desc<L::kRB>(b0 + off), idesc, (kb | ks) != 0);
+          if constexpr (NS >= 2) {
+            umma_pair<TF32>(acc, sw_desc<L::kRB>(a0 + off), sw_desc<L::kRB>(b0 + L::kBh + off), idesc, 1);
+            umma_pair<TF32>(acc, sw_desc<L::kRB>(a0 + L::kA + off), sw_desc<L::kRB>(b0 + off), idesc, 1);
+          }
+        }
+        umma_commit_pair(empty0 + 8 * s);  // the stage is free in both CTAs
+        ++g;
+      }
+      umma_commit_pair(accf0 + 8 * b);  // both CTAs: the item's products are done
+    }
+    umma_commit_pair(done_bar);  // both CTAs: every MMA issued above has completed
+  } else if (warp >= 2) {
+    // epilogue: this CTA's 128 rows of each item from its own TMEM
+    const int q = warp % 4;
+    int t = 0;
+    for (int item = pair; item < nitems; item += npairs, ++t) {
+      if (aborted()) break;
+      int n0, m0, z, kb0, nkb;
+      coords(item, n0, m0, z, kb0, nkb);
+      const int b = t & 1;
+      if (!mbar_wait(accf0 + 8 * b, (t >> 1) & 1)) {
+        atomicExch(&s_abort, 1);
+        break;
+      }
+      tc_fence_after();
+      if (aborted()) break;
+      const int row = m0 + q * 32 + lane;
+      float* o = out + long(z) * split_stride;
+#pragma unroll 1
+      for (int c = 0; c < BN; c += 32) {
+        float v[32];
+        tmem_ld32(tmem + (uint32_t(q * 32) << 16) + uint32_t(b * BN + c), v);
+        if (nkb == 0) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] = 0.f;
+        }
+        if (row < M) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int n = n0 + c + j;
+            if (n < N) o[row + ld_out * long(n)] = v[j];
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) {
+        if (rank == 0)
+          mbar_arrive(acce0 + 8 * b);
+        else
+          mbar_arrive_cluster(mapa_shared(acce0 + 8 * b, 0));
+      }
+    }
+  }
+  __syncwarp();
+  // every MMA issued has completed before TMEM is freed (bounded)
+  if (!mbar_wait(done_bar, 0)) atomicExch(&s_abort, 1);
+  tc_fence_after();
+  __syncthreads();
+  if (aborted() && threadIdx.x == 0) atomicExch(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  cluster_sync_all();  // neither CTA frees TMEM or leaves while its peer still runs
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
+}
+
 // ---- host side ----
 
 // A 2-D BF16 tensor map over a row-major [rows][ld] array (K contiguous, rows of `cols` valid

@@ -86,6 +86,7 @@ def lib():
         "epsp_warmstart_create": (C.c_int, [vp, i32, P(i32), P(vp)]),
         "epsp_warmstart_destroy": (None, [vp]),
         "epsp_warmstart_nparams": (i64, [vp]),
+        "epsp_warmstart_train_ms": (C.c_double, [vp]),
         "epsp_warmstart_set_params": (C.c_int, [vp, P(C.c_float)]),
         "epsp_warmstart_get_params": (C.c_int, [vp, P(C.c_float)]),
         "epsp_warmstart_predict": (C.c_int, [vp, P(C.c_float), i64, P(C.c_float)]),
@@ -312,7 +313,8 @@ class LadderPlan:
     def set_gemm_config(self, bn: int, splits: int, bk: int = 64, persistent: bool = False, pair: bool = False):
         """Overrides the autotuner's tile shape of the contraction (GEMM_BF16 / GEMM_TF32 plans);
         persistent: one CTA per SM over all tiles (BF16: bn 256, bk 32 only; TF32: bk 32, either bn);
-        pair: CTA pairs computing 256-row tiles (tcgen05 cta_group::2; bn 256, bk 32)."""
+        pair: CTA pairs computing 256-row tiles (tcgen05 cta_group::2; bn 256, bk 32); both: the
+        persistent CTA-pair kernel."""
         self.ctx.check(lib().epsp_ladder_set_gemm_config(self.handle, int(bn), int(splits), int(bk)))
         self.ctx.check(lib().epsp_ladder_set_gemm_persistent(self.handle, 1 if persistent else 0))
         self.ctx.check(lib().epsp_ladder_set_gemm_pair(self.handle, 1 if pair else 0))

@@ -58,6 +58,7 @@ class Network:
         d = (C.c_int32 * len(self.dims))(*self.dims)
         self.ctx.check(api.lib().epsp_warmstart_create(self.ctx.handle, len(self.dims) - 1, d, C.byref(self.handle)))
         self.nparams = int(api.lib().epsp_warmstart_nparams(self.handle))
+        self.last_train_device_s = 0.0
         self.set_params(init_params(self.dims, seed))
 
     def set_params(self, p):
@@ -115,6 +116,7 @@ class Network:
         self.ctx.check(api.lib().epsp_warmstart_train(self.handle, X.ctypes.data_as(_fp), Y.ctypes.data_as(_fp), n,
                                                       int(epochs), int(batch), float(lr), pp,
                                                       hist.ctypes.data_as(C.POINTER(C.c_double))))
+        self.last_train_device_s = api.lib().epsp_warmstart_train_ms(self.handle) / 1e3
         return hist
 
     def close(self):
@@ -170,6 +172,7 @@ class WarmStart:
         self.x_mean = self.x_std = self.y_mean = None
         self.y_scale = 1.0
         self.loss_history = np.zeros(0)
+        self.train_device_s = 0.0
 
     def fit(self, X, Y, *, epochs: int = 120, batch: int = 256, lr: float = 1e-3, lr_stages: int = 4,
             lr_decay: float = 0.5, seed: int = 0) -> np.ndarray:
@@ -189,8 +192,10 @@ class WarmStart:
         self._set_scaling()
         hist = []
         lr_k = lr
+        self.train_device_s = 0.0  # the epochs on the device, without the standardisation and uploads
         for k, n_ep in enumerate(_stages(epochs, lr_stages)):
             hist.append(self.net.train(Xn, Yn, epochs=n_ep, batch=batch, lr=lr_k, seed=seed + k))
+            self.train_device_s += self.net.last_train_device_s
             lr_k *= lr_decay
         self.loss_history = np.concatenate(hist)
         return self.loss_history

@@ -287,9 +287,10 @@ epsp_status epsp_ladder_set_gemm_config(epsp_ladder_plan* plan, int32_t bn, int3
  * shape). Same results bitwise. */
 epsp_status epsp_ladder_gemm_persistent(const epsp_ladder_plan* plan, int32_t* on);
 epsp_status epsp_ladder_set_gemm_persistent(epsp_ladder_plan* plan, int32_t on);
-/* Whether the contraction runs as the CTA-pair kernel (tcgen05 cta_group::2: two CTAs of a cluster
- * compute a 256-row tile, each holding its 128 A rows and half of the B tile; bn 256 with bk 32):
- * read, and set (on = 0 or 1; on turns the persistent kernel off). Same results bitwise. */
+/* Whether the contraction runs on CTA pairs (tcgen05 cta_group::2: two CTAs of a cluster compute a
+ * 256-row tile, each holding its 128 A rows and half of the B tile; bn 256 with bk 32): read, and
+ * set (on = 0 or 1). With the persistent setting also on, the persistent CTA-pair kernel (one
+ * cluster per two SMs over all tiles, two TMEM accumulators per CTA). Same results bitwise. */
 epsp_status epsp_ladder_gemm_pair(const epsp_ladder_plan* plan, int32_t* on);
 epsp_status epsp_ladder_set_gemm_pair(epsp_ladder_plan* plan, int32_t on);
 
@@ -311,6 +312,9 @@ epsp_status epsp_ladder_apply(epsp_ladder_plan* plan, const double* sigma_T, dou
 epsp_status epsp_warmstart_create(epsp_ctx* ctx, int32_t nlayers, const int32_t* dims, epsp_warmstart** net);
 void epsp_warmstart_destroy(epsp_warmstart* net);
 int64_t epsp_warmstart_nparams(const epsp_warmstart* net);
+/* Device milliseconds of the epochs of the last epsp_warmstart_train (CUDA events around each
+ * epoch's graph replay; data uploads and graph capture not included). */
+double epsp_warmstart_train_ms(const epsp_warmstart* net);
 /* Setting the parameters resets the optimiser state. */
 epsp_status epsp_warmstart_set_params(epsp_warmstart* net, const float* params);
 epsp_status epsp_warmstart_get_params(epsp_warmstart* net, float* params);

@@ -241,6 +241,10 @@ def test_every_contraction_tile_shape_matches_the_oracle(api, oracle, cc, unit):
                 plan.set_gemm_config(bn, sp, bk, pair=True)
                 assert plan.gemm_config()["pair"]
                 assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, "pair")
+                # persistent CTA pairs (one cluster per two SMs over all tiles): bitwise the same
+                plan.set_gemm_config(bn, sp, bk, persistent=True, pair=True)
+                assert plan.gemm_config()["pair"] and plan.gemm_config()["persistent"]
+                assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, "pair persistent")
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(128, 1, 32)
     with pytest.raises(ArgumentError):
@@ -262,6 +266,9 @@ def test_every_contraction_tile_shape_matches_the_oracle(api, oracle, cc, unit):
                 plan.set_gemm_config(bn, sp, bk, pair=True)
                 assert plan.gemm_config()["pair"]
                 assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, "pair")
+                plan.set_gemm_config(bn, sp, bk, persistent=True, pair=True)
+                assert plan.gemm_config()["pair"] and plan.gemm_config()["persistent"]
+                assert np.array_equal(plan.apply(J, sig, c["mu"][0], T, 0.07), got), (bn, bk, sp, "pair persistent")
     with pytest.raises(ArgumentError):
         plan.set_gemm_config(256, 1, 64)
     with pytest.raises(ArgumentError):
