@@ -53,10 +53,10 @@ LADDER_PATH = "gemm_tf32"
 FP64_SCGD0_ITERS = 12
 FP64_LADDER_APPLIES = 2
 # DRAM bytes (read + write) and tensor-pipe activity of one ladder-contraction launch of this
-# workload (Z = Jr Bz, the TF32 persistent kernel in grouped tile order), from one Nsight Compute
+# workload (Z = Jr Bz, the TF32 persistent CTA-pair kernel), from one Nsight Compute
 # capture of the same kernel on a GB300 (profiles/tc_ladder_zgemm_c2.md)
-TC_LADDER_TRAFFIC_BYTES = 0.848e9 + 1.784e9
-TC_LADDER_TENSOR_PIPE_ACTIVE = 0.625
+TC_LADDER_TRAFFIC_BYTES = 1.643e9 + 1.786e9
+TC_LADDER_TENSOR_PIPE_ACTIVE = 0.633
 # learned warm start: training and held-out runs, epochs
 WARM_TRAIN_RUNS, WARM_HELDOUT_RUNS, WARM_EPOCHS = 256, 32, 40
 
