@@ -56,7 +56,7 @@ struct LadderChunk {
 };
 
 // zgather_kernel's launch shape: U nodes per thread, nranges node ranges of U threads nodes each,
-// NC columns per block, staged rows of wstride floats (the widest window + 4 zeros); smem bytes.
+// NC columns per block, staged rows of wstride float4s (the widest window + 4 zeros); smem bytes.
 struct ZgatherShape {
   int U = 2, NC = 4, threads = 0, nranges = 1, wstride = 0;
   size_t smem = 0;
@@ -82,7 +82,7 @@ struct LadderPlan {
   // padded to nmp (a multiple of 16)
   long nwp = 0, nmp = 0;
   long Kx = 0, Kp2 = 0;
-  // tensor-core paths: the contraction Z = Jr Bz (M = 16 nwp rows (c12, c0, ri, p), N = nm 3ni
+  // tensor-core paths: the contraction Z = Jr Bz (M = 16 nwp rows (ri, c0, p, c12), N = nm 3ni
   // columns (ν, a, i), K = 3ni pairs (b, i') padded to Kzp), then D from Z by zgather_kernel
   long Mz = 0, Nz = 0, Kz = 0, Kzp = 0;
   DBuf<float> d_ztab;            // [nm, 2, nwp][4] the weights of p0, p0 + 1, p0 + 2 (tent weights folded in), p0
@@ -629,7 +629,8 @@ __global__ void xgen_f64_kernel(const double2* __restrict__ J, const int32_t* __
 // components c12 = 11, 11, 22, 22, 21, 12) and the three taps of each mode and sign are applied by
 // zgather_kernel; D's layout is the one the Kramers-Kronig and channel kernels read.
 
-// Jr rows z 16 nwp + ((ri 2 + c0) 4 + c12) nwp + p, K-major with row stride Kzp (columns k = b + 3i',
+// Jr rows z 16 nwp + (ri 2 + c0) 4 nwp + 4 p + c12 (a node's four components adjacent, so that Z
+// holds them as one float4), K-major with row stride Kzp (columns k = b + 3i',
 // zero for p >= nω and k >= 3ni), from the vertex of right-hand side rmap[z] (z without rmap), FP32
 // complex [nω, 4, 3, 2, ni] jstride apart: TF32-rounded (kTf32) or split into BF16 hi/lo. A block
 // transposes a tile of 32 nodes x 32 pairs of one (c12, c0) through shared memory, reading node
@@ -660,7 +661,7 @@ __global__ void __launch_bounds__(256) jmat_kernel(const float2* __restrict__ J_
     const int pl = ty + 8 * (r % 4), ri = r / 4;
     const float2 v = tile[tx][pl];
     const float x = ri ? v.y : v.x;
-    const long row = long(z) * 16 * nwp + long((ri * 2 + c0) * 4 + c12) * nwp + p0 + pl;
+    const long row = long(z) * 16 * nwp + long(ri * 2 + c0) * 4 * nwp + long(p0 + pl) * 4 + c12;
     const long off = row * Kzp + k0 + tx;
     if constexpr (kTf32) {
       Jt[off] = round_tf32(x);
@@ -701,49 +702,46 @@ constexpr int kZgMaxThreads = 320;
 
 // D from Z (the formula above), FP32, modes in ascending order, both signs and three taps each.
 // Z: [Mz, nm N] column-major (ld ldZ) as zsplits split-K partials zstride apart (summed in
-// ascending order as they are staged); rows of slot z at z 16 nwp. ztab [nm][2][nwp]: per node,
-// mode and sign the three tap weights (tent split folded in) and, in .w as integer bits, the first
-// tap node p0 (the taps are p0, p0 + 1, p0 + 2); nnu_all 16 Bose occupations per right-hand side
-// (rmap[z], or z). D[z 24 nwp + (q + 6 (c0 + 2 ri)) nwp + j + ldD n], rows j < nω.
+// ascending order as they are staged); rows of slot z at z 16 nwp, then (ri 2 + c0) 4 nwp + 4 p +
+// c12: a node's four components are one float4. ztab [nm][2][nwp]: per node, mode and sign the
+// three tap weights (tent split folded in) and, in .w as integer bits, the first tap node p0 (the
+// taps are p0, p0 + 1, p0 + 2); nnu_all 16 Bose occupations per right-hand side (rmap[z], or z).
+// D[z 24 nwp + (q + 6 (c0 + 2 ri)) nwp + j + ldD n], rows j < nω.
 // Grid (N / NC, 4 (c0, ri) x node ranges, slots), blockDim a multiple of 32 up to kZgMaxThreads: a
 // block owns NC columns n of one (c0, ri) and the U blockDim nodes of its range; per mode it stages
-// the window zwin[range][ν] (float4 chunks [lo, hi) of each of the four components' Z columns:
-// every row the range's taps read) into rows of wstride floats by asynchronous copies,
-// double-buffered over ν, and each thread accumulates U nodes x NC columns.
+// the window zwin[range][ν] (nodes [lo, hi): every node the range's taps read, as float4s) into
+// rows of wstride float4s by asynchronous copies, double-buffered over ν, and each thread
+// accumulates U nodes x NC columns, one shared-memory load per tap for the four components.
 template <int U, int NC>
 __global__ void __launch_bounds__(kZgMaxThreads, 2)
     zgather_kernel(const float* __restrict__ Z, long ldZ, int zsplits, long zstride, const float4* __restrict__ ztab,
                    const int2* __restrict__ zwin, int wstride, const float* __restrict__ nnu_all,
                    const int* __restrict__ rmap, int nw, int nwp, int nm, long N, float* __restrict__ D, long ldD) {
-  extern __shared__ __align__(16) float zs[];  // [2][NC][4][wstride]
+  extern __shared__ __align__(16) float4 zs4[];  // [2][NC][wstride]
   const long n0 = long(blockIdx.x) * NC;
   const int c0 = blockIdx.y & 1, ri = (blockIdx.y >> 1) & 1, rg = int(blockIdx.y >> 2);
   const long z = blockIdx.z;
   const int rhs = rmap ? rmap[z] : int(z);
   const float* nnu = nnu_all + 16 * rhs;
-  const float* zb = Z + z * 16 * nwp + long((ri * 2 + c0) * 4) * nwp;  // the 4 components, contiguous
+  const float* zb = Z + z * 16 * nwp + long(ri * 2 + c0) * 4 * nwp;  // the nodes' float4s, contiguous
   const int nthr = blockDim.x;
   const int jb = rg * U * nthr;  // the range's first node
   auto stage = [&](int nu, int buf, int2 win) {
-    const int nc = win.y - win.x;  // float4 chunks per component
+    const int nn = win.y - win.x;  // nodes staged
     for (int c = 0; c < NC; ++c) {
       const long n = n0 + c;
       if (n >= N) break;
-      float* dst = zs + long((buf * NC + c) * 4) * wstride;
-      // zeros after each staged row: a tap past the grid's last padded node (weight zero) reads them
-      if (threadIdx.x < 16) dst[(threadIdx.x / 4) * wstride + 4 * nc + threadIdx.x % 4] = 0.f;
-      const float* src = zb + ldZ * (long(nu) * N + n) + 4 * win.x;
+      float4* dst = zs4 + long(buf * NC + c) * wstride;
+      // zeros after the staged nodes: a tap past the grid's last padded node (weight zero) reads them
+      if (threadIdx.x < 4) dst[nn + threadIdx.x] = make_float4(0.f, 0.f, 0.f, 0.f);
+      const float* src = zb + ldZ * (long(nu) * N + n) + 4l * win.x;
       if (zsplits == 1) {
-        for (int e = threadIdx.x; e < 4 * nc; e += nthr) {
-          const int comp = e / nc, p4 = e % nc;
-          cp_async16(dst + comp * wstride + 4 * p4, src + long(comp) * nwp + 4 * p4);
-        }
+        for (int e = threadIdx.x; e < nn; e += nthr) cp_async16(dst + e, src + 4l * e);
       } else {  // split-K partials: summed here in ascending order (synchronous loads)
-        for (int e = threadIdx.x; e < 16 * nc; e += nthr) {
-          const int comp = e / (4 * nc), p = e % (4 * nc);
+        for (int e = threadIdx.x; e < 4 * nn; e += nthr) {
           float acc = 0.f;
-          for (int sp = 0; sp < zsplits; ++sp) acc += src[long(comp) * nwp + p + zstride * sp];
-          dst[comp * wstride + p] = acc;
+          for (int sp = 0; sp < zsplits; ++sp) acc += src[e + zstride * sp];
+          reinterpret_cast<float*>(dst)[e] = acc;
         }
       }
     }
@@ -766,7 +764,6 @@ __global__ void __launch_bounds__(kZgMaxThreads, 2)
     cp_async_wait_all();
     __syncthreads();  // mode nu's columns are in buffer nu & 1; buffer (nu + 1) & 1 is free
     if (nu + 1 < nm) stage(nu + 1, (nu + 1) & 1, win_next);
-    const int base = 4 * win.x;  // the staged rows start at node base
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int j = jb + threadIdx.x + nthr * u;
@@ -776,26 +773,28 @@ __global__ void __launch_bounds__(kZgMaxThreads, 2)
 #pragma unroll
       for (int sg = 0; sg < 2; ++sg) {
         t[sg] = ztab[(long(nu) * 2 + sg) * nwp + j];
-        pk[sg] = __float_as_int(t[sg].w) - base;
+        pk[sg] = __float_as_int(t[sg].w) - win.x;
       }
+      // per sign s: the factors of components c12 = 0 (11, .x), 1 (21, .y), 2 (12, .z), 3 (22, .w)
+      // in the six rows q (sign + : 1/2, -(1/2 + n), n, 1 + n; sign - : -1/2, -(1/2 + n), 1 + n, n)
 #pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        const float* zc = zs + long(((nu & 1) * NC + c) * 4) * wstride;
-        float x[2][4];
+      for (int sg = 0; sg < 2; ++sg) {
+        const float half = sg ? -0.5f : 0.5f, fy = sg ? 1.f + nb : nb, fz = sg ? nb : 1.f + nb;
 #pragma unroll
-        for (int sg = 0; sg < 2; ++sg)
-#pragma unroll
-          for (int cc = 0; cc < 4; ++cc) {
-            const float* r = zc + cc * wstride + pk[sg];
-            x[sg][cc] = t[sg].x * r[0] + t[sg].y * r[1] + t[sg].z * r[2];
-          }
-        // components c12 = 0 (11), 1 (21), 2 (12), 3 (22)
-        acc[c][u][0] += 0.5f * (x[0][0] - x[1][0]);
-        acc[c][u][1] += -hp * (x[0][0] + x[1][0]);
-        acc[c][u][2] += 0.5f * (x[0][3] - x[1][3]);
-        acc[c][u][3] += -hp * (x[0][3] + x[1][3]);
-        acc[c][u][4] += nb * x[0][1] + (1.f + nb) * x[1][1];
-        acc[c][u][5] += (1.f + nb) * x[0][2] + nb * x[1][2];
+        for (int c = 0; c < NC; ++c) {
+          const float4* zc = zs4 + long((nu & 1) * NC + c) * wstride + pk[sg];
+          const float4 r0 = zc[0], r1 = zc[1], r2 = zc[2];
+          const float xx = t[sg].x * r0.x + t[sg].y * r1.x + t[sg].z * r2.x;
+          const float xy = t[sg].x * r0.y + t[sg].y * r1.y + t[sg].z * r2.y;
+          const float xz = t[sg].x * r0.z + t[sg].y * r1.z + t[sg].z * r2.z;
+          const float xw = t[sg].x * r0.w + t[sg].y * r1.w + t[sg].z * r2.w;
+          acc[c][u][0] += half * xx;
+          acc[c][u][1] += -hp * xx;
+          acc[c][u][2] += half * xw;
+          acc[c][u][3] += -hp * xw;
+          acc[c][u][4] += fy * xy;
+          acc[c][u][5] += fz * xz;
+        }
       }
     }
     win = win_next;
@@ -826,14 +825,15 @@ static ZgatherShape zgather_ranges(long nw, int U) {
   g.threads = int(((nthr + g.nranges - 1) / g.nranges + 31) / 32 * 32);
   return g;
 }
-// The staging windows of zgather_kernel: for each node range and mode, the float4 chunks [lo, hi)
-// of a component column that hold every tap p0 .. p0 + 2 of the range's nodes (both signs),
-// from the first-tap table hk [nm][2][nwp]; taps past the last chunk read the zeros staged after
-// it. Sets g.wstride, g.NC (4 while two double-buffered blocks fit an SM, else 2, else 1) and g.smem.
+// The staging windows of zgather_kernel: for each node range and mode, the nodes [lo, hi) that
+// hold every tap p0 .. p0 + 2 of the range's nodes (both signs), from the first-tap table hk
+// [nm][2][nwp]; taps past nwp read the zeros staged after the window. Sets g.wstride (the widest
+// window + 4, float4s), g.NC (4 while two double-buffered blocks fit an SM, else 2, else 1) and
+// g.smem.
 static std::vector<int32_t> zgather_windows(ZgatherShape& g, const std::vector<int32_t>& hk, long nw, long nwp, long nm) {
   std::vector<int32_t> win(size_t(2 * g.nranges * nm));
   const long span = long(g.U) * g.threads;
-  long maxnc = 1;
+  long maxn = 1;
   for (long r = 0; r < g.nranges; ++r)
     for (long nu = 0; nu < nm; ++nu) {
       long lo = nwp, hi = 0;
@@ -845,13 +845,13 @@ static std::vector<int32_t> zgather_windows(ZgatherShape& g, const std::vector<i
           hi = std::max(hi, p0 + 3);
         }
       if (hi <= lo) lo = hi = 0;  // an empty range stages nothing
-      const long lo4 = lo / 4, hi4 = std::min((hi + 3) / 4, nwp / 4);
-      win[size_t(2 * (r * nm + nu))] = int32_t(lo4);
-      win[size_t(2 * (r * nm + nu) + 1)] = int32_t(std::max(lo4, hi4));
-      maxnc = std::max(maxnc, hi4 - lo4);
+      hi = std::min(hi, nwp);
+      win[size_t(2 * (r * nm + nu))] = int32_t(lo);
+      win[size_t(2 * (r * nm + nu) + 1)] = int32_t(std::max(lo, hi));
+      maxn = std::max(maxn, hi - lo);
     }
-  g.wstride = int(4 * maxnc + 4);
-  const size_t per_col = size_t(2 * 4 * g.wstride) * sizeof(float);  // two buffers, four components
+  g.wstride = int(maxn + 4);
+  const size_t per_col = size_t(2 * g.wstride) * sizeof(float4);  // two buffers
   g.NC = per_col * 4 <= (size_t(110) << 10) ? 4 : per_col * 2 <= (size_t(110) << 10) ? 2 : 1;
   g.smem = per_col * size_t(g.NC);
   if (g.smem > (size_t(227) << 10))
