@@ -54,7 +54,7 @@ FP64_SCGD0_ITERS = 12
 FP64_LADDER_APPLIES = 2
 # DRAM bytes (read + write) and tensor-pipe activity of one ladder-contraction launch of this
 # workload (Z = Jr Bz, the TF32 persistent CTA-pair kernel), from one Nsight Compute
-# capture of the same kernel on a GB300 (profiles/tc_ladder_zgemm_c2.md)
+# capture of the same kernel on a GB300 (summarised with the other captures under profiles/)
 TC_LADDER_TRAFFIC_BYTES = 1.643e9 + 1.786e9
 TC_LADDER_TENSOR_PIPE_ACTIVE = 0.633
 # learned warm start: training and held-out runs, epochs
@@ -394,14 +394,14 @@ def run_ours(args, world, rank, local):
                                achieved=achieved, peak=burst, unit="TFLOP/s", frac=achieved / burst,
                                traffic=TC_LADDER_TRAFFIC_BYTES,
                                traffic_source="ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
-                                              "(profiles/tc_ladder_zgemm_c2.md)",
+                                              "(the contraction's capture under profiles/)",
                                peak_source=f"{src} bf16 burst (cuBLAS, MEASURED_PEAKS.json)", launches=prof_n,
                                avg_ms=1e3 * avg_s, flops_per_launch=flops,
                                tf32_peak=tf32, frac_of_tf32_peak=(achieved / tf32) if tf32 else None,
                                tf32_peak_source="cuBLAS TF32 GEMM 8192^3 through torch, best of 10, this run",
                                tensor_pipe_active_ncu=TC_LADDER_TENSOR_PIPE_ACTIVE,
                                tensor_pipe_source="ncu sm__pipe_tensor_cycles_active of one launch "
-                                                  "(profiles/tc_ladder_zgemm_c2.md)")
+                                                  "(the contraction's capture under profiles/)")
     out["clocks"] = clk.summary()
     # end to end through the public API from host arrays
     e2e = e2e_calls(s, ws, ctx, T, occ, mu0)

@@ -86,7 +86,7 @@ def test_device_sigma_refuses_to_outlive_its_run():
 
 
 def test_julia_shim_and_integration_name_only_declared_entry_points():
-    """The Julia ccall shim and INTEGRATION.md call nothing the header does not declare."""
+    """The Julia ccall shim and the integration guide call nothing the header does not declare."""
     decl = set(declared())
     jl = open(os.path.join(PKG, "julia", "EPSpectralGB300.jl")).read()
     used = set(re.findall(r":(epsp_[a-z0-9_]+)", jl))
