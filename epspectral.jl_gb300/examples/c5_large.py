@@ -7,6 +7,7 @@ run, the FP64 recast path at one temperature for the error, and the ladder at a 
 Ω; the contraction in TF32, or --ladder-path gemm_bf16). Prints one JSON line.
 
     python epspectral.jl_gb300/examples/c5_large.py [--gpu-tile 8192] [--omegas 2] [--no-fp64] [--ladder-path P]
+        [--fp64-ladder]
 """
 import argparse
 import json
@@ -29,6 +30,8 @@ def main():
     ap.add_argument("--omegas", type=int, default=2)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--ladder-path", default="gemm_tf32", choices=("gemm_tf32", "gemm_bf16"))
+    ap.add_argument("--fp64-ladder", action="store_true",
+                    help="also the FP64 recast ladder at the first Omega on the FP64 Sigma (minutes), for the error")
     a = ap.parse_args()
     out = {}
     t0 = time.perf_counter()
@@ -88,6 +91,20 @@ def main():
         out["tc_ladder_useful_tflops"] = 2.0 * M * N * K / (ms / n / 1e3) / 1e12
     out["sigma_ladder_xx"] = float(l["sigma_ladder"][0, 0, 0, 0])
     lp.close()
+    if a.fp64_ladder and not a.no_fp64:
+        # the plain FP64 path end to end at the first Ω: FP64 Σ and μ (300 K), the recast ladder in FP64
+        t0 = time.perf_counter()
+        lp64 = api.LadderPlan(s, path="gemm_fp64", omega_acoustic=1e-4, gpu_tile=a.gpu_tile, ctx=ctx)
+        out["fp64_ladder_setup_s"] = time.perf_counter() - t0
+        ctx.timer_begin()
+        l64 = lp64.run(r64["sigma"], r64["mu"], [T3], Om[:1], rtol=1e-2, maxiter=30)
+        out["fp64_ladder_s"] = ctx.timer_end() / 1e3
+        out["fp64_ladder_gmres_iters"] = int(l64["niter"][0, 0])
+        lp64.close()
+        a_, b_ = l["sigma_ladder"][:, :, 0, 0], l64["sigma_ladder"][:, :, 0, 0]
+        out["rel_sigma_ladder_vs_fp64"] = float(np.linalg.norm(a_ - b_) / np.linalg.norm(b_))
+        a_, b_ = l["sigma_bubble"][:, :, 0, 0], l64["sigma_bubble"][:, :, 0, 0]
+        out["rel_sigma_bubble_vs_fp64"] = float(np.linalg.norm(a_ - b_) / np.linalg.norm(b_))
     print(json.dumps(out), flush=True)
 
 
