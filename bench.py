@@ -405,7 +405,8 @@ def run_ours(args, world, rank, local):
     out["clocks"] = clk.summary()
     # end to end through the public API from host arrays
     e2e = e2e_calls(s, ws, ctx, T, occ, mu0)
-    out["e2e"] = dict(value=e2e, unit="s", h2d_bytes_per_step=2 * setup_bytes(s) + 16 * nw * ni,
+    # both set-ups' arrays, g2 once (the context keeps it for the second), Σ to the ladder
+    out["e2e"] = dict(value=e2e, unit="s", h2d_bytes_per_step=2 * setup_bytes(s) - s["g2"].nbytes + 16 * nw * ni,
                       d2h_bytes_per_step=16 * nw * ni + 8 * 9 * 2)
     out["e2e_cold"] = e2e_cold(ws)
     # plain FP64 GPU paths, timed once
@@ -504,15 +505,21 @@ def measure_tf32_peak(device: int):
 
 def e2e_calls(s, ws, ctx, T, occ, mu0):
     """The end-to-end sequence through the public API from host arrays: the scGD0 plan's set-up (g2
-    upload), scGD0 from the warm start, Σ back to the host, the ladder's set-up and σ(Ω). Seconds."""
+    upload), scGD0 from the warm start, Σ back to the host, the ladder's set-up and σ(Ω). The context
+    keeps the g2 the first set-up streams (epsp_ctx_keep_g2, switched on afresh here, so the first
+    set-up does stream it) for the ladder's set-up of the same array. Seconds."""
     from epspectral_gb300 import api
+    ctx.keep_g2(False)
     t0 = time.perf_counter()
+    ctx.keep_g2(True)
     sp_e = api.Scgd0Plan(s, path="gemm_bf16", omega_acoustic=W_AC, ctx=ctx)
     r_e = sp_e.run(occ, eta_init=ETA_INIT, tol=TOL, maxiter=MAXITER, mu_start=[mu0], warm=ws)
     sp_e.close()
     api.loop_ladder(s, r_e["sigma"], r_e["mu"], [T], [OMEGA], rtol=L_RTOL, maxiter=L_MAXITER, omega_acoustic=W_AC,
                     path=LADDER_PATH, ctx=ctx)
-    return time.perf_counter() - t0
+    t = time.perf_counter() - t0
+    ctx.keep_g2(False)
+    return t
 
 
 def e2e_cold(ws) -> dict:

@@ -60,6 +60,29 @@ struct HostPinned {
   }
 };
 
+// The device copy of a streamed g2 that a context keeps on request (epsp_ctx_keep_g2): the host
+// array it came from (null while incomplete), its size, element type and member order.
+struct G2Kept {
+  bool on = false;
+  const void* host = nullptr;
+  size_t bytes = 0;
+  int dtype = -1;
+  std::vector<int32_t> order;
+  void* dev = nullptr;
+  size_t dev_bytes = 0;
+  void release() {
+    if (dev) cudaFree(dev);
+    dev = nullptr;
+    dev_bytes = 0;
+    host = nullptr;
+    order.clear();
+  }
+  G2Kept() = default;
+  G2Kept(const G2Kept&) = delete;
+  G2Kept& operator=(const G2Kept&) = delete;
+  ~G2Kept() { release(); }
+};
+
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -82,6 +105,8 @@ struct Ctx {
   long alloc_calls = 0;
   // the g2 stream's double-buffered staging, kept for the next plan of this context
   HostPinned g2_stage[2];
+  // the streamed g2 itself, when the caller asks the context to keep it
+  G2Kept g2_kept;
 };
 
 // Set-up phase log (verbosity >= 2): host milliseconds of each phase since the previous mark (the

@@ -183,6 +183,18 @@ epsp_status epsp_test_fail_alloc(epsp_ctx* c, uint64_t bytes) {
   return EPSP_OK;
 }
 
+/* Not in the reference: with on, the context keeps on the device the last g2 a plan set-up streamed
+ * (in that set-up's member order), and a later set-up whose model points at the same g2 array
+ * (address, size, element type) in the same order reads that copy instead of streaming g2 again
+ * (an scGD0 plan and a ladder plan of one model). The caller must not change the array in between.
+ * on = 0 switches it off and frees the copy. */
+epsp_status epsp_ctx_keep_g2(epsp_ctx* c, int32_t on) {
+  if (!c) return EPSP_EINVAL;
+  if (!on) c->c.g2_kept.release();
+  c->c.g2_kept.on = on != 0;
+  return EPSP_OK;
+}
+
 /* Test hook (not in the reference): the one-CTA tensor-core GEMM kernel's producer skips K block
  * `skip_kblock` of every tile (-1 switches it off), and that kernel's pipeline waits give up after
  * `wait_limit` tries (0 restores the default), so a call returns EPSP_EDEVICE_TIMEOUT from a wait

@@ -41,6 +41,34 @@ void stream_g2_by_columns(Ctx* ctx, const epsp_model* m, const std::vector<int32
   const long nchunk = long(cb.size()) - 1;
   const size_t bytes = size_t(std::max<long>(maxm, 1)) * slab;
   cudaStream_t s = ctx->stream;
+  // the copy the context keeps (epsp_ctx_keep_g2): the same array, size, type and member order are
+  // read there, chunk by chunk, without a host gather or a copy
+  G2Kept& K = ctx->g2_kept;
+  const size_t total = order.size() * slab;
+  if (K.on && K.host == m->g2 && K.bytes == total && K.dtype == m->g2_dtype && K.order == order) {
+    for (long k = 0; k < nchunk; ++k) {
+      const long c0 = cb[size_t(k)], c1 = cb[size_t(k + 1)], p0 = cptr[size_t(c0)];
+      fn(static_cast<uint8_t*>(K.dev) + size_t(p0) * slab, c0, c1, p0);
+    }
+    EPSP_CUDA(cudaStreamSynchronize(s));
+    return;
+  }
+  // otherwise the chunks are streamed, into the kept copy's slots when the context keeps g2 (each
+  // chunk its own slot: no double buffer on the device), else through two device buffers
+  bool keep = K.on;
+  if (keep) {
+    K.host = nullptr;
+    if (K.dev_bytes < total) {
+      K.release();
+      if (cudaMalloc(&K.dev, total) != cudaSuccess) {  // no room for a copy: stream as usual
+        (void)cudaGetLastError();
+        K.dev = nullptr;
+        keep = false;
+      } else {
+        K.dev_bytes = total;
+      }
+    }
+  }
   HostPinned* host = ctx->g2_stage;  // kept by the context for the next plan
   DBuf<uint8_t> dev[2];
   Events ev;
@@ -49,7 +77,7 @@ void stream_g2_by_columns(Ctx* ctx, const epsp_model* m, const std::vector<int32
   const int nb = nchunk > 1 ? 2 : 1;
   for (int b = 0; b < nb; ++b) {
     host[b].ensure(bytes);
-    dev[b].alloc(ctx, bytes);
+    if (!keep) dev[b].alloc(ctx, bytes);
   }
   // the star-order gather of a chunk into the staging buffer, over up to 16 host threads
   const int nthreads = int(std::clamp<unsigned>(std::thread::hardware_concurrency(), 1u, 16u));
@@ -81,15 +109,22 @@ void stream_g2_by_columns(Ctx* ctx, const epsp_model* m, const std::vector<int32
     if (k >= nb) EPSP_CUDA(cudaEventSynchronize(copied[b]));
     gather(static_cast<uint8_t*>(host[b].p), p0, p1);
     // the device buffer's previous chunk must be consumed before it is overwritten
-    if (k >= nb) EPSP_CUDA(cudaStreamWaitEvent(ev.copy, consumed[b], 0));
-    EPSP_CUDA(cudaMemcpyAsync(dev[b].p, host[b].p, size_t(p1 - p0) * slab, cudaMemcpyHostToDevice, ev.copy));
+    if (k >= nb && !keep) EPSP_CUDA(cudaStreamWaitEvent(ev.copy, consumed[b], 0));
+    uint8_t* d = keep ? static_cast<uint8_t*>(K.dev) + size_t(p0) * slab : dev[b].p;
+    EPSP_CUDA(cudaMemcpyAsync(d, host[b].p, size_t(p1 - p0) * slab, cudaMemcpyHostToDevice, ev.copy));
     EPSP_CUDA(cudaEventRecord(copied[b], ev.copy));
     EPSP_CUDA(cudaStreamWaitEvent(s, copied[b], 0));
-    fn(dev[b].p, c0, c1, p0);
+    fn(d, c0, c1, p0);
     EPSP_CUDA(cudaEventRecord(consumed[b], s));
   }
   EPSP_CUDA(cudaStreamSynchronize(s));
   EPSP_CUDA(cudaStreamSynchronize(ev.copy));
+  if (keep) {  // complete: a later set-up of the same array and order reads it
+    K.host = m->g2;
+    K.bytes = total;
+    K.dtype = m->g2_dtype;
+    K.order = order;
+  }
 }
 
 }  // namespace epsp

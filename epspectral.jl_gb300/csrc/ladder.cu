@@ -544,16 +544,19 @@ __global__ void coupling_rot_chunk_kernel(const T* __restrict__ g2c, const doubl
                                           const int32_t* __restrict__ star_ptr, long c0, long c1, long p0,
                                           const double* __restrict__ wnu, double w_ac, int nm, int nmp, int ni, long Kx,
                                           double* __restrict__ Gt) {
-  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  // thread (ν, i) of stars ip = c0 + blockIdx.y, + gridDim.y, ...: each star's members in order (a
+  // star's nine outputs are its own, so the stars run side by side; R of a member is the same for
+  // the block)
+  const long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= long(nm) * ni) return;
-  int nu = int(idx % nm), i = int(idx / nm);
-  bool skip = wnu[nu] < w_ac;
-  for (long ip = c0; ip < c1; ++ip) {
+  const int nu = int(idx % nm), i = int(idx / nm);
+  const bool skip = wnu[nu] < w_ac;
+  for (long ip = c0 + blockIdx.y; ip < c1; ip += gridDim.y) {
     double acc[3][3] = {};
     if (!skip)
       for (int p = star_ptr[ip]; p < star_ptr[ip + 1]; ++p) {
-        long f = by_star[p];
-        double g = w_f[f] * load_g2(g2c, nu + long(nm) * (i + long(ni) * (p - p0)));
+        const long f = by_star[p];
+        const double g = w_f[f] * load_g2(g2c, nu + long(nm) * (i + long(ni) * (p - p0)));
         for (int b = 0; b < 3; ++b)
           for (int a = 0; a < 3; ++a) acc[a][b] += R[a + 3 * (b + 3 * f)] * g;
       }
@@ -1690,15 +1693,15 @@ LadderPlan* ladder_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts
       const unsigned grid = div_up(size_t(nm * ni), 128);
       stream_g2_by_columns(ctx, m, by_star, sp, chunk_f, [&](const void* g2c, long c0, long c1, long p0) {
         if (m->g2_dtype == EPSP_F64)
-          coupling_rot_chunk_kernel<double><<<grid, 128, 0, s>>>(static_cast<const double*>(g2c), P->d_R.p, P->d_wf.p,
+          coupling_rot_chunk_kernel<double><<<dim3(grid, unsigned(std::min<long>(c1 - c0, 65535))), 128, 0, s>>>(static_cast<const double*>(g2c), P->d_R.p, P->d_wf.p,
                                                                 P->d_by_star.p, P->d_star_ptr.p, c0, c1, p0, d_wnu.p,
                                                                 P->w_ac, int(nm), int(P->nmp), int(ni), P->Kx, P->d_Gt.p);
         else if (m->g2_dtype == EPSP_F32)
-          coupling_rot_chunk_kernel<float><<<grid, 128, 0, s>>>(static_cast<const float*>(g2c), P->d_R.p, P->d_wf.p,
+          coupling_rot_chunk_kernel<float><<<dim3(grid, unsigned(std::min<long>(c1 - c0, 65535))), 128, 0, s>>>(static_cast<const float*>(g2c), P->d_R.p, P->d_wf.p,
                                                                P->d_by_star.p, P->d_star_ptr.p, c0, c1, p0, d_wnu.p,
                                                                P->w_ac, int(nm), int(P->nmp), int(ni), P->Kx, P->d_Gt.p);
         else
-          coupling_rot_chunk_kernel<uint16_t><<<grid, 128, 0, s>>>(static_cast<const uint16_t*>(g2c), P->d_R.p, P->d_wf.p,
+          coupling_rot_chunk_kernel<uint16_t><<<dim3(grid, unsigned(std::min<long>(c1 - c0, 65535))), 128, 0, s>>>(static_cast<const uint16_t*>(g2c), P->d_R.p, P->d_wf.p,
                                                                   P->d_by_star.p, P->d_star_ptr.p, c0, c1, p0, d_wnu.p,
                                                                   P->w_ac, int(nm), int(P->nmp), int(ni), P->Kx,
                                                                   P->d_Gt.p);

@@ -219,20 +219,22 @@ __global__ void kbuild_f64_kernel(const double* __restrict__ ws, int nw, CellTab
 // G[(ν, c), i] = Σ_{f in c} w_f g2[ν, i, f] over the inner states of column set c in star order,
 // for the column sets [c0, c1) of one streamed chunk: g2c [nm, ni, p - p0] holds their members p.
 // Rows of modes below ω_acoustic are 0 (they are skipped before g2 is read in the reference).
+// Thread (ν, i) of column sets c0 + blockIdx.y, c0 + blockIdx.y + gridDim.y, ...: each set's sum is
+// its own, so the sets run side by side.
 template <class T>
 __global__ void coupling_sum_chunk_kernel(const T* __restrict__ g2c, int nm, int ni, const int32_t* __restrict__ cptr,
                                           long c0, long c1, long p0, const int32_t* __restrict__ members, long nc,
                                           const double* __restrict__ w_f, const double* __restrict__ wnu, double w_ac,
                                           double* __restrict__ G) {
-  long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  const long idx = long(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= long(nm) * ni) return;
-  int nu = int(idx % nm), i = int(idx / nm);
-  bool skip = wnu[nu] < w_ac;
-  for (long c = c0; c < c1; ++c) {
+  const int nu = int(idx % nm), i = int(idx / nm);
+  const bool skip = wnu[nu] < w_ac;
+  for (long c = c0 + blockIdx.y; c < c1; c += gridDim.y) {
     double s = 0.0;
     if (!skip)
       for (int p = cptr[c]; p < cptr[c + 1]; ++p) {
-        long f = members[p];
+        const long f = members[p];
         s += w_f[f] * load_g2(g2c, nu + long(nm) * (i + long(ni) * (p - p0)));
       }
     G[(nu + nm * c) + long(nm) * nc * i] = s;
@@ -1018,13 +1020,13 @@ Scgd0Plan* scgd0_setup(Ctx* ctx, const epsp_model* m, const epsp_options* opts) 
     const unsigned grid = div_up(size_t(nm * ni), 128);
     stream_g2_by_columns(ctx, m, members, cptr, chunk_f, [&](const void* g2c, long c0, long c1, long p0) {
       if (m->g2_dtype == EPSP_F64)
-        coupling_sum_chunk_kernel<double><<<grid, 128, 0, s>>>(static_cast<const double*>(g2c), int(nm), int(ni), d_cptr.p, c0,
+        coupling_sum_chunk_kernel<double><<<dim3(grid, unsigned(std::min<long>(c1 - c0, 65535))), 128, 0, s>>>(static_cast<const double*>(g2c), int(nm), int(ni), d_cptr.p, c0,
                                                               c1, p0, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac, P->d_G.p);
       else if (m->g2_dtype == EPSP_F32)
-        coupling_sum_chunk_kernel<float><<<grid, 128, 0, s>>>(static_cast<const float*>(g2c), int(nm), int(ni), d_cptr.p, c0,
+        coupling_sum_chunk_kernel<float><<<dim3(grid, unsigned(std::min<long>(c1 - c0, 65535))), 128, 0, s>>>(static_cast<const float*>(g2c), int(nm), int(ni), d_cptr.p, c0,
                                                              c1, p0, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac, P->d_G.p);
       else
-        coupling_sum_chunk_kernel<uint16_t><<<grid, 128, 0, s>>>(static_cast<const uint16_t*>(g2c), int(nm), int(ni), d_cptr.p,
+        coupling_sum_chunk_kernel<uint16_t><<<dim3(grid, unsigned(std::min<long>(c1 - c0, 65535))), 128, 0, s>>>(static_cast<const uint16_t*>(g2c), int(nm), int(ni), d_cptr.p,
                                                                 c0, c1, p0, d_mem.p, P->nc, d_wf.p, P->d_wnu.p, P->w_ac,
                                                                 P->d_G.p);
       EPSP_LAUNCHED(ctx);

@@ -61,6 +61,7 @@ def lib():
         "epsp_profile_read": (C.c_int, [vp, P(d), P(i64)]),
         "epsp_test_fail_alloc": (C.c_int, [vp, C.c_uint64]),
         "epsp_test_gemm_stall": (C.c_int, [vp, C.c_int32, C.c_uint32]),
+        "epsp_ctx_keep_g2": (C.c_int, [vp, C.c_int32]),
         "epsp_timer_begin": (C.c_int, [vp]),
         "epsp_timer_end": (C.c_int, [vp, P(d)]),
         "epsp_scgd0_setup": (C.c_int, [vp, P(epsp_model), P(epsp_options), P(vp)]),
@@ -149,6 +150,12 @@ class Context:
     def fail_next_alloc(self, nbytes: int):
         """Test hook: the next device allocation of at least nbytes fails with ENOMEM."""
         self.check(lib().epsp_test_fail_alloc(self.handle, int(nbytes)))
+
+    def keep_g2(self, on: bool):
+        """Keep the last g2 a plan set-up streamed on the device, for a later set-up of the same array
+        (an scGD0 plan and a ladder plan of one model); the array must not change in between. False
+        frees the copy."""
+        self.check(lib().epsp_ctx_keep_g2(self.handle, 1 if on else 0))
 
     def stall_gemm(self, skip_kblock: int = -1, wait_limit: int = 0):
         """Test hook: the one-CTA tensor-core GEMM skips K block skip_kblock of every tile and gives

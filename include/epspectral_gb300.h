@@ -170,6 +170,11 @@ int64_t epsp_kernel_launches(const epsp_ctx* ctx);
  *    until the next call (NULL or "" switches it off); epsp_profile_read returns their summed
  *    milliseconds and count;
  *  - epsp_timer_begin / epsp_timer_end time the context's stream between two calls;
+ *  - epsp_ctx_keep_g2 (on = 1) makes the context keep on the device the last g2 a plan set-up
+ *    streamed, in that set-up's member order; a later set-up whose model points at the same g2 array
+ *    (address, size, element type) in the same order reads it instead of streaming g2 again (an
+ *    scGD0 plan and a ladder plan of one model). The caller must not change the array in between;
+ *    on = 0 (the default) switches it off and frees the copy;
  *  - epsp_test_fail_alloc makes the next device allocation of at least `bytes` bytes fail with
  *    EPSP_ENOMEM (0 switches it off), to test the error path without exhausting a device;
  *  - epsp_test_gemm_stall makes the one-CTA tensor-core GEMM kernel's producer skip K block
@@ -181,6 +186,7 @@ epsp_status epsp_profile_kernel(epsp_ctx* ctx, const char* name);
 epsp_status epsp_profile_read(epsp_ctx* ctx, double* total_ms, int64_t* count);
 epsp_status epsp_timer_begin(epsp_ctx* ctx);
 epsp_status epsp_timer_end(epsp_ctx* ctx, double* ms);
+epsp_status epsp_ctx_keep_g2(epsp_ctx* ctx, int32_t on);
 epsp_status epsp_test_fail_alloc(epsp_ctx* ctx, uint64_t bytes);
 epsp_status epsp_test_gemm_stall(epsp_ctx* ctx, int32_t skip_kblock, uint32_t wait_limit);
 

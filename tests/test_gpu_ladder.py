@@ -312,6 +312,38 @@ def test_bounded_wait_runs_out_and_the_plan_stays_usable(api, cc):
     plan.close()
 
 
+def test_kept_g2_serves_the_next_set_up(api, cc):
+    # epsp_ctx_keep_g2: the scGD0 plan's set-up streams g2 and the context keeps it; the ladder
+    # plan's set-up of the same array reads the kept copy. Shown by the contract itself: g2 changed
+    # in place between the two set-ups is not seen (the result is bitwise that of the old g2), and
+    # with the copy freed a new set-up streams the changed array.
+    c = cc
+    s = dict(c["setup"])
+    g2 = np.array(s["g2"], copy=True, order="F")
+    s["g2"] = g2
+    nw, ni = len(s["omegas"]), s["eps_i"].size
+    J = R.pseudorandom_complex(nw, 4, 3, 2, ni, seed=0.53)
+    J[0] = 0
+    J[-1] = 0
+    args = (J, c["sigma"][:, :, 0], c["mu"][0], c["Tlist"][0], 0.07)
+    ref = api.LadderPlan(s, path="gemm_tf32", omega_acoustic=W_AC)
+    want = ref.apply(*args)
+    ctx = ref.ctx
+    ref.close()
+    ctx.keep_g2(True)
+    try:
+        api.Scgd0Plan(s, path="gemm_bf16", omega_acoustic=W_AC).close()  # streams g2, the context keeps it
+        g2 *= 2  # in place: the same array, size and type
+        lp = api.LadderPlan(s, path="gemm_tf32", omega_acoustic=W_AC)
+        assert np.array_equal(lp.apply(*args), want)
+        lp.close()
+    finally:
+        ctx.keep_g2(False)
+    lp = api.LadderPlan(s, path="gemm_tf32", omega_acoustic=W_AC)
+    assert not np.allclose(lp.apply(*args), want)
+    lp.close()
+
+
 def test_scgd0_sigma_stays_on_the_device_for_the_ladder(api, cc):
     # epsp_scgd0_run with sigma_out = NULL keeps Σ in the plan (epsp_scgd0_sigma_device); the ladder
     # reads it there (cudaMemcpyDefault): the same σ, bitwise, as from the downloaded Σ
