@@ -2,7 +2,10 @@
 #include "g2stream.cuh"
 
 #include <algorithm>
+#include <condition_variable>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <thread>
 
 namespace epsp {
@@ -10,6 +13,58 @@ namespace epsp {
 size_t g2_elem_bytes(int dtype) { return dtype == EPSP_F64 ? 8 : (dtype == EPSP_F32 ? 4 : 2); }
 
 namespace {
+// Host threads for the star-order gather, started once per stream: the caller hands each chunk's
+// member range to them (a generation count under a mutex), takes the first share itself and waits
+// for the rest; the destructor stops and joins them.
+struct GatherCrew {
+  std::vector<std::thread> th;
+  std::mutex mu;
+  std::condition_variable go, done;
+  long gen = 0;
+  int pending = 0;
+  bool stop = false;
+  std::function<void(int)> work;  // work(t): thread t's share of the current chunk
+  explicit GatherCrew(int n) {
+    for (int t = 1; t < n; ++t)
+      th.emplace_back([this, t] {
+        long seen = 0;
+        for (;;) {
+          std::function<void(int)> w;
+          {
+            std::unique_lock<std::mutex> lk(mu);
+            go.wait(lk, [&] { return stop || gen != seen; });
+            if (stop) return;
+            seen = gen;
+            w = work;
+          }
+          w(t);
+          std::lock_guard<std::mutex> lk(mu);
+          if (--pending == 0) done.notify_one();
+        }
+      });
+  }
+  void run(const std::function<void(int)>& f) {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      work = f;
+      pending = int(th.size());
+      ++gen;
+    }
+    go.notify_all();
+    f(0);
+    std::unique_lock<std::mutex> lk(mu);
+    done.wait(lk, [&] { return pending == 0; });
+  }
+  ~GatherCrew() {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      stop = true;
+    }
+    go.notify_all();
+    for (auto& x : th) x.join();
+  }
+};
+
 struct Events {
   cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaStream_t copy = nullptr;
@@ -79,25 +134,26 @@ void stream_g2_by_columns(Ctx* ctx, const epsp_model* m, const std::vector<int32
     host[b].ensure(bytes);
     if (!keep) dev[b].alloc(ctx, bytes);
   }
-  // the star-order gather of a chunk into the staging buffer, over up to 16 host threads
+  // the star-order gather of a chunk into the staging buffer, over up to 16 host threads started
+  // once for the stream (chunks of less than 8 MB are gathered by the caller alone)
   const int nthreads = int(std::clamp<unsigned>(std::thread::hardware_concurrency(), 1u, 16u));
+  const bool crew_on = nthreads > 1 && size_t(std::max<long>(maxm, 1)) * slab >= (size_t(8) << 20);
+  std::unique_ptr<GatherCrew> crew(crew_on ? new GatherCrew(nthreads) : nullptr);
   auto gather = [&](uint8_t* dst, long p0, long p1) {
     const auto* src = static_cast<const uint8_t*>(m->g2);
     auto part = [&](long a, long b) {
       for (long p = a; p < b; ++p) std::memcpy(dst + size_t(p - p0) * slab, src + size_t(order[size_t(p)]) * slab, slab);
     };
     const long n = p1 - p0;
-    if (nthreads == 1 || size_t(n) * slab < (size_t(8) << 20)) {
+    if (!crew || size_t(n) * slab < (size_t(8) << 20)) {
       part(p0, p1);
       return;
     }
     const long per = (n + nthreads - 1) / nthreads;
-    std::vector<std::thread> th;
-    for (int t = 0; t < nthreads; ++t) {
+    crew->run([&](int t) {
       const long a = p0 + t * per, b = std::min(p1, a + per);
-      if (a < b) th.emplace_back(part, a, b);
-    }
-    for (auto& x : th) x.join();
+      if (a < b) part(a, b);
+    });
   };
   cudaEvent_t* copied = ev.e;
   cudaEvent_t* consumed = ev.e + 2;
