@@ -227,7 +227,7 @@ epsp_status epsp_scgd0_imsigma(epsp_scgd0_plan* plan, const double* sigma_in, do
  * live in a fixed static device array of 4.5 MiB (65536 nodes x 8 bytes + 2^20 table entries x 4
  * bytes; larger grids are rejected with EPSP_EINVAL), which every device that loads the library
  * keeps until the process exits. The first call on a device looks up that array's address (set-up
- * once per device), so make the first call before any stream capture. The kernel runs on the
+ * once per device). The kernel runs on the
  * context's own stream, which is not ordered after the caller's streams: the caller's device inputs
  * must be complete before the call (synchronise the stream that wrote them). The call is
  * synchronous: it returns after the kernel has finished, so imsigma is ready on return. Calls share
