@@ -99,6 +99,8 @@ struct Ctx {
   // (-1 = off) and the pipeline waits give up after `stall_wait_limit` tries (0 = the default).
   int stall_kb = -1;
   unsigned stall_wait_limit = 0;
+  // Test hook of the g2 stream: gather on the host and copy even where the GPU reads g2 in place.
+  bool g2_host_gather = false;
   cudaEvent_t timer[2] = {nullptr, nullptr};
   // host time spent in device allocations (for the set-up phase log)
   double alloc_ms = 0;

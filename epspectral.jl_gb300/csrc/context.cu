@@ -210,4 +210,42 @@ epsp_status epsp_test_gemm_stall(epsp_ctx* c, int32_t skip_kblock, uint32_t wait
   return EPSP_OK;
 }
 
+/* Page-locks host memory [ptr, ptr + bytes) and maps it for the device (cudaHostRegister, portable
+ * and mapped), so that plan set-ups read a g2 there in place; epsp_host_unregister undoes it. */
+epsp_status epsp_host_register(epsp_ctx* c, void* ptr, uint64_t bytes) {
+  if (!c) return EPSP_EINVAL;
+  if (!ptr || bytes == 0) {
+    c->c.last_error = "epsp_host_register: ptr must be non-NULL and bytes positive";
+    return EPSP_EINVAL;
+  }
+  cudaSetDevice(c->c.device);
+  const cudaError_t e = cudaHostRegister(ptr, size_t(bytes), cudaHostRegisterPortable | cudaHostRegisterMapped);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    c->c.last_error = std::string("cudaHostRegister: ") + cudaGetErrorString(e);
+    return e == cudaErrorHostMemoryAlreadyRegistered ? EPSP_EINVAL : EPSP_ECUDA;
+  }
+  return EPSP_OK;
+}
+
+epsp_status epsp_host_unregister(epsp_ctx* c, void* ptr) {
+  if (!c || !ptr) return EPSP_EINVAL;
+  cudaSetDevice(c->c.device);
+  const cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    c->c.last_error = std::string("cudaHostUnregister: ") + cudaGetErrorString(e);
+    return e == cudaErrorHostMemoryNotRegistered ? EPSP_EINVAL : EPSP_ECUDA;
+  }
+  return EPSP_OK;
+}
+
+/* Test hook: on = 1 makes the g2 stream gather on the host and copy even for a g2 the GPU reads in
+ * place (registered page-locked memory); on = 0 (the default) gathers such a g2 on the device. */
+epsp_status epsp_test_g2_host_gather(epsp_ctx* c, int32_t on) {
+  if (!c) return EPSP_EINVAL;
+  c->c.g2_host_gather = on != 0;
+  return EPSP_OK;
+}
+
 }  // extern "C"

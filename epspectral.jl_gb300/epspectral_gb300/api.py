@@ -61,6 +61,9 @@ def lib():
         "epsp_profile_read": (C.c_int, [vp, P(d), P(i64)]),
         "epsp_test_fail_alloc": (C.c_int, [vp, C.c_uint64]),
         "epsp_test_gemm_stall": (C.c_int, [vp, C.c_int32, C.c_uint32]),
+        "epsp_test_g2_host_gather": (C.c_int, [vp, C.c_int32]),
+        "epsp_host_register": (C.c_int, [vp, vp, C.c_uint64]),
+        "epsp_host_unregister": (C.c_int, [vp, vp]),
         "epsp_ctx_keep_g2": (C.c_int, [vp, C.c_int32]),
         "epsp_timer_begin": (C.c_int, [vp]),
         "epsp_timer_end": (C.c_int, [vp, P(d)]),
@@ -161,6 +164,19 @@ class Context:
         """Test hook: the one-CTA tensor-core GEMM skips K block skip_kblock of every tile and gives
         up its pipeline waits after wait_limit tries (EDEVICE_TIMEOUT); stall_gemm() switches it off."""
         self.check(lib().epsp_test_gemm_stall(self.handle, int(skip_kblock), int(wait_limit)))
+
+    def host_register(self, a: np.ndarray):
+        """Page-lock the memory of array `a` (epsp_host_register): set-ups then read a g2 there in
+        place. Call host_unregister(a) before `a` is freed."""
+        self.check(lib().epsp_host_register(self.handle, C.c_void_p(a.ctypes.data), int(a.nbytes)))
+
+    def host_unregister(self, a: np.ndarray):
+        self.check(lib().epsp_host_unregister(self.handle, C.c_void_p(a.ctypes.data)))
+
+    def g2_host_gather(self, on: bool = True):
+        """Test hook: the set-ups' g2 stream gathers on the host and copies even for a registered g2;
+        g2_host_gather(False) restores the device gather."""
+        self.check(lib().epsp_test_g2_host_gather(self.handle, 1 if on else 0))
 
     def close(self):
         if self.handle:

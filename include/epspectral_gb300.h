@@ -181,14 +181,30 @@ int64_t epsp_kernel_launches(const epsp_ctx* ctx);
  *    `skip_kblock` of every tile (-1 switches it off) and that kernel's pipeline waits give up after
  *    `wait_limit` tries (0: the default, about 2^26), so that a call returns EPSP_EDEVICE_TIMEOUT
  *    from a bounded device wait (the kernel frees its tensor memory and returns; the context and
- *    the plan stay usable). */
+ *    the plan stay usable);
+ *  - epsp_test_g2_host_gather(ctx, 1) makes the set-ups' g2 stream gather g2 on the host into
+ *    page-locked staging and copy it even when g2 is registered page-locked memory (0, the
+ *    default, gathers such a g2 on the device). */
 epsp_status epsp_profile_kernel(epsp_ctx* ctx, const char* name);
 epsp_status epsp_profile_read(epsp_ctx* ctx, double* total_ms, int64_t* count);
 epsp_status epsp_timer_begin(epsp_ctx* ctx);
 epsp_status epsp_timer_end(epsp_ctx* ctx, double* ms);
 epsp_status epsp_ctx_keep_g2(epsp_ctx* ctx, int32_t on);
+
+/* Page-locks the host memory [ptr, ptr + bytes) and maps it for the device (cudaHostRegister);
+ * epsp_host_unregister(ctx, ptr) undoes it and must be called before the memory is freed. A plan
+ * set-up whose g2 of at most 1 GiB lies in registered (or cudaHostAlloc'd) memory gathers it in
+ * star order with a kernel that reads it in place, with no host-side gather or staging copy; a
+ * larger g2, or one in pageable memory, is gathered on the host over up to 16 threads into
+ * page-locked staging and copied (on a GB300 node the in-place reads of an 8.6 GB g2 ran several
+ * times slower than that). Registering pins every page (0.7-2 ms for 365 MB there).
+ * EPSP_EINVAL if the range is already (or, for unregister, not) registered. No counterpart in the
+ * reference (CUDA.jl's pinning of host arrays plays the same role there). */
+epsp_status epsp_host_register(epsp_ctx* ctx, void* ptr, uint64_t bytes);
+epsp_status epsp_host_unregister(epsp_ctx* ctx, void* ptr);
 epsp_status epsp_test_fail_alloc(epsp_ctx* ctx, uint64_t bytes);
 epsp_status epsp_test_gemm_stall(epsp_ctx* ctx, int32_t skip_kblock, uint32_t wait_limit);
+epsp_status epsp_test_g2_host_gather(epsp_ctx* ctx, int32_t on);
 
 /* ---- scGD0 ---- */
 

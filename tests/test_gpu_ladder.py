@@ -189,6 +189,58 @@ def test_streamed_g2_gives_the_resident_ladder(api, cc):
         assert np.array_equal(got["sigma_ladder"], one["sigma_ladder"]), path
 
 
+def test_device_gather_gives_the_host_gather(api, cc):
+    # A g2 in registered page-locked memory is gathered in star order by a kernel that reads it in
+    # place; the test hook makes the set-ups gather it on the host and copy instead. The coupling
+    # sums (scGD0) and G̃ (ladder) built either way are the same bits: FP64, FP32 and BF16 storage,
+    # one chunk and chunks of 5 inner states, and a g2 whose address is one element past an aligned
+    # one (the kernel then copies in element-sized words).
+    from epspectral_gb300 import synthetic
+    c = cc
+    nw, ni = len(c["setup"]["omegas"]), c["setup"]["eps_i"].size
+    J = R.pseudorandom_complex(nw, 4, 3, 2, ni, seed=0.61)
+    J[0] = 0
+    J[-1] = 0
+    sig, mu, T = c["sigma"][:, :, 0], c["mu"][0], c["Tlist"][0]
+
+    def shifted(a):
+        buf = np.empty(a.size + 1, dtype=a.dtype)
+        v = buf[1:].reshape(a.shape, order="F")
+        v[...] = a
+        return v
+
+    def both_ways(s, tile):
+        got = []
+        for host in (False, True):
+            ctx.g2_host_gather(host)
+            sp = api.Scgd0Plan(s, path="gemm_fp64", gpu_tile=tile, omega_acoustic=W_AC, ctx=ctx)
+            im = sp.imsigma(sig, mu, T)
+            sp.close()
+            lp = api.LadderPlan(s, path="gemm_tf32", gpu_tile=tile, omega_acoustic=W_AC, ctx=ctx)
+            got.append((im, lp.apply(J, sig, mu, T, 0.07)))
+            lp.close()
+        return got
+
+    g64 = np.array(c["setup"]["g2"], dtype=np.float64, order="F")
+    g32 = g64.astype(np.float32, order="F")
+    gbf = synthetic.float32_to_bf16_bits(g32)
+    ctx = api.Context(0)
+    try:
+        for g2 in (g64, g32, gbf, shifted(g32), shifted(gbf)):
+            s = dict(c["setup"], g2=g2)
+            ctx.host_register(g2)
+            try:
+                for tile in (None, 5):
+                    (im_d, ap_d), (im_h, ap_h) = both_ways(s, tile)
+                    assert np.array_equal(im_d, im_h), (g2.dtype, tile)
+                    assert np.array_equal(ap_d, ap_h), (g2.dtype, tile)
+            finally:
+                ctx.host_unregister(g2)
+    finally:
+        ctx.g2_host_gather(False)
+        ctx.close()
+
+
 @pytest.mark.parametrize("unit", [0.001, 0.0005])
 def test_apply_on_fine_shift_grids(api, oracle, unit):
     # Fine grids make the shift window wide (nshift = 81 and 161 here, vertex windows of 4 x 198
