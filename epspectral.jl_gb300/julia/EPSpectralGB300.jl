@@ -6,6 +6,8 @@
 # library, and turns its status codes into the reference's errors (ArgumentError for EINVAL and
 # ENOROOT_MU) and its convergence flags into the reference's warnings. Arrays are passed by pointer
 # in their Julia (column-major) layout; index arrays are converted to 0-based Int32 once per call.
+# A g2 of at most 1 GiB that the caller has pinned (`CUDA.pin(setup.g2)`, or `epsp_host_register`)
+# is read in place by the plan set-ups' gather kernel; an unpinned one is gathered on the host.
 # Not executed in this repository (no Julia toolchain here). To wire it, include this file from
 # EPSpectral.jl and add a method of `_loop_scgd0` / `_loop_ladder` for `backend::GB300Backend` that
 # calls `loop_scgd0` / `loop_ladder` below.
