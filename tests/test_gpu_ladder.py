@@ -93,6 +93,33 @@ def test_loop_matches_oracle(api, oracle, cc):
     assert rel(fgot["sigma_ladder"], fref["sigma_ladder"]) <= 1e-10
 
 
+def test_density_vertex_ward_identity_long_gmres(api, oracle, hc):
+    # The Ward-identity case of the oracle tests (test/test_ladder_holstein.jl:28-45: no symmetry,
+    # the density vertex V = 1 in the x slot, q = 0) on the FP64 paths. GMRES at rtol 1e-8 takes
+    # 28-49 iterations here, so the device Arnoldi (multi-vector CGS2 passes, FP64 Givens) runs long
+    # solves: iteration counts within one of the oracle's, the bare response to 1e-10, the dressed
+    # one (which nearly cancels: 4e-4 to 1.6e-2 of the bare) to 1e-7 of the bare.
+    c = hc
+    s = dict(c["setup"])
+    v = np.zeros_like(s["v"])
+    v[0, :] = 1.0
+    s["v"] = v
+    Omegas = [0.1, 0.3]
+    kw = dict(solver="gmres", rtol=1e-8, maxiter=200, omega_acoustic=W_AC)
+    ref = oracle.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], Omegas, **kw)
+    assert ref["niter"].min() >= 10
+    nb = np.linalg.norm(ref["sigma_bubble"])
+    for path in ("direct_fp64", "gemm_fp64"):
+        got = api.loop_ladder(s, c["sigma"], c["mu"], c["Tlist"], Omegas, path=path, **kw)
+        assert got["converged"].all(), path
+        dn = np.abs(got["niter"].astype(np.int64) - ref["niter"].astype(np.int64)).max()
+        assert dn <= 1, (path, got["niter"], ref["niter"])
+        assert rel(got["sigma_bubble"], ref["sigma_bubble"]) <= 1e-10, path
+        assert np.linalg.norm(got["sigma_ladder"] - ref["sigma_ladder"]) <= 1e-7 * nb, path
+        ratio = got["sigma_ladder"][0, 0] / got["sigma_bubble"][0, 0]
+        assert np.max(np.abs(ratio)) <= 0.05, (path, ratio)
+
+
 def test_holstein_current_correction_vanishes(api, hsym):
     # test/test_ladder_holstein.jl:5-26 on the GPU paths; the tensor-core path keeps its vertices in
     # FP32, so there the correction vanishes to FP32 rounding (a surviving correction is ~1e-2)
