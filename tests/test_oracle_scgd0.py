@@ -302,6 +302,49 @@ def test_holstein_run_record(oracle, holstein):
     assert abs(r["mu"][0] - rec["mu"]) <= 0.1 * abs(rec["mu"])
 
 
+def test_spectral_grid_graded_against_fine_uniform(oracle, holstein):
+    # test/test_scgd0_spectral_grid.jl:3-62: one iteration (μ and min_i ∫A_i read from that
+    # iteration's Σ, so runs on different spectral grids share Σ and differ only by the quadrature)
+    # of the Holstein chain at nlist = -0.3 on a graded spectral grid (0.005 around μ ≈ -0.91, 0.02
+    # outside), a uniform one of 8001 nodes and a uniform one of the graded grid's node count. The
+    # fine grid's min ∫A matches the trapezoid rule on 40001 nodes to 1e-6; the graded grid is
+    # within 1e-4 of it in ∫A and 1e-5 in μ and ten times closer than the uniform grid of the same
+    # size in both. The reference records its measured errors (:54-55): 7e-6 in ∫A and 2e-6 in μ on
+    # the graded grid, 5e-4 and 4e-5 on the uniform one; the oracle's (7.3e-6, 2.1e-6, 4.9e-4,
+    # 3.6e-5) round to the same digits.
+    h = holstein
+    graded = graded_frequency_grid([(-1.4, -0.4, 0.005), (-4.0, 4.0, 0.02)])
+    wg = graded.nodes()
+    fine = FrequencyGrid.from_nodes(np.linspace(wg[0], wg[-1], 8001))
+    same_count = FrequencyGrid.from_nodes(np.linspace(wg[0], wg[-1], len(wg)))
+    assert len(wg) < len(fine.nodes()) / 10
+    n_target = 1.0 - 0.3
+    mu0 = synthetic.bare_mu(h["setup"], 0.1, n_target)
+    kw = dict(eta_init=0.05, tol=1e-6, maxiter=1, mu_start=[mu0], omega_acoustic=OMEGA_AC)
+    run = {name: oracle.loop_scgd0(dict(h["setup"], omegas_spectral=g), occ(-0.3), **kw)
+           for name, g in (("graded", graded), ("fine", fine), ("same_count", same_count))}
+    assert np.array_equal(run["graded"]["sigma"], run["fine"]["sigma"])
+    w = h["ws"].nodes()
+    wa = np.linspace(wg[0], wg[-1], 40001)
+    Wa = R.trapezoid(wa)
+    eps_i = h["setup"]["eps_i"]
+    S = run["fine"]["sigma"][:, :, 0]
+    minA_ref = min(float(np.sum(-np.imag(1.0 / (wa - eps_i[i] - R.interp_flat(w, S[:, i], wa))) / math.pi * Wa))
+                   for i in range(len(eps_i)))
+    minA = {k: r["history"]["min_spectral_weight"][0, 0] for k, r in run.items()}
+    mu = {k: r["mu"][0] for k, r in run.items()}
+    assert abs(minA["fine"] - minA_ref) <= 1e-6 * minA_ref
+    err = {k: abs(minA[k] - minA_ref) / minA_ref for k in ("graded", "same_count")}
+    assert err["graded"] < 1e-4
+    assert abs(mu["graded"] - mu["fine"]) < 1e-5
+    assert err["same_count"] > 10 * err["graded"]
+    assert abs(mu["same_count"] - mu["fine"]) > 10 * abs(mu["graded"] - mu["fine"])
+    recorded = ((err["graded"], 7e-6), (abs(mu["graded"] - mu["fine"]), 2e-6), (err["same_count"], 5e-4),
+                (abs(mu["same_count"] - mu["fine"]), 4e-5))
+    for got, rec in recorded:  # to the recorded digit
+        assert abs(got - rec) <= 0.5 * 10 ** math.floor(math.log10(rec)), (got, rec)
+
+
 def test_loop_maxiter_no_root_and_multiplets(oracle, holstein):
     # test/test_scgd0_loop.jl:1-38
     s = holstein["setup"]
