@@ -639,10 +639,9 @@ void propagators(const Ladder& L, const double* sigma_T, double mu, double T, do
   }
 }
 
-// attach_greens_to_bare_vertex!, src/ladder_kernel.jl:70-73, 97-99.
-void attach_bare(const Ladder& L, const std::vector<cplx>& Gm, const std::vector<cplx>& Gp, double* J0) {
-  const int64_t nw = L.M.nw, ni = L.M.ni;
-  const double* v = L.M.m->v;
+// attach_greens_to_bare_vertex!, src/ladder_kernel.jl:70-73, 97-99: J0 = Gm V Gp with
+// V^{c1 c2, c0} = δ_{c1 c2} δ_{c1 c0} v_i. Gm, Gp [nω, 4, ni]; v [3, ni].
+void attach_bare_core(int64_t nw, int64_t ni, const cplx* Gm, const cplx* Gp, const double* v, double* J0) {
   for (int64_t i = 0; i < ni; ++i)
     for (int c0 = 0; c0 < 2; ++c0)
       for (int cart = 0; cart < 3; ++cart)
@@ -658,11 +657,14 @@ void attach_bare(const Ladder& L, const std::vector<cplx>& Gm, const std::vector
         }
 }
 
+void attach_bare(const Ladder& L, const std::vector<cplx>& Gm, const std::vector<cplx>& Gp, double* J0) {
+  attach_bare_core(L.M.nw, L.M.ni, Gm.data(), Gp.data(), L.M.m->v, J0);
+}
+
 // attach_greens_to_vertex!, src/ladder_kernel.jl:61-67, 87-89: J = Gm X Gp per (ω, cart, c0, i),
-// for the outer states [ia, ia + n) (all by default); X and J hold those n states only.
-void attach(const Ladder& L, const std::vector<cplx>& Gm, const std::vector<cplx>& Gp,
-            const std::vector<cplx>& X, double* J, double scale, int64_t ia = 0, int64_t n = -1) {
-  const int64_t nw = L.M.nw, ni = n < 0 ? L.M.ni : n;
+// for the outer states [ia, ia + ni) of Gm, Gp [nω, 4, *]; X and J hold those ni states only.
+void attach_core(int64_t nw, int64_t ni, const cplx* Gm, const cplx* Gp, const cplx* X, double* J, double scale,
+                 int64_t ia) {
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < ni; ++i)
     for (int c0 = 0; c0 < 2; ++c0)
@@ -680,6 +682,12 @@ void attach(const Ladder& L, const std::vector<cplx>& Gm, const std::vector<cplx
             J[2 * k + 1] = scale * z.imag();
           }
         }
+}
+
+// all outer states by default, or [ia, ia + n)
+void attach(const Ladder& L, const std::vector<cplx>& Gm, const std::vector<cplx>& Gp,
+            const std::vector<cplx>& X, double* J, double scale, int64_t ia = 0, int64_t n = -1) {
+  attach_core(L.M.nw, n < 0 ? L.M.ni : n, Gm.data(), Gp.data(), X.data(), J, scale, ia);
 }
 
 // conductivity_from_vertex, src/ladder_kernel.jl:116-122.
@@ -1197,6 +1205,18 @@ void epsp_oracle_bin_coupling(const epsp_model* mp, double w_ac, double T, doubl
 void epsp_oracle_conductivity(const double* J, const double* v, const double* w_i, const double* Ww, int64_t nw,
                               int64_t ni, double Omega, double T, double* sigma) {
   conductivity(J, v, w_i, Ww, nw, ni, Omega, T, sigma);
+}
+
+// Gm, Gp [nω, 4, ni], X and J [nω, 4, 3, 2, ni]: complex, interleaved.
+void epsp_oracle_attach_greens(int64_t nw, int64_t ni, const double* Gm, const double* Gp, const double* X,
+                               double* J) {
+  attach_core(nw, ni, reinterpret_cast<const cplx*>(Gm), reinterpret_cast<const cplx*>(Gp),
+              reinterpret_cast<const cplx*>(X), J, 1.0, 0);
+}
+
+void epsp_oracle_attach_bare(int64_t nw, int64_t ni, const double* Gm, const double* Gp, const double* v,
+                             double* J0) {
+  attach_bare_core(nw, ni, reinterpret_cast<const cplx*>(Gm), reinterpret_cast<const cplx*>(Gp), v, J0);
 }
 
 int epsp_oracle_ladder_apply(const epsp_model* m, const epsp_options* opts, const double* sigma_T, double mu,

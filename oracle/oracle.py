@@ -36,9 +36,9 @@ class OracleError(RuntimeError):
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with its Makefile (g++, OpenMP)."""
-    if force or not os.path.exists(LIB_PATH):
-        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    """Compile the oracle with its Makefile (g++, OpenMP); make rebuilds it when a source is newer
+    than the library (force: always)."""
+    subprocess.run(["make", "-s", "-C", _HERE] + (["-B"] if force else []), check=True)
     return LIB_PATH
 
 
@@ -72,6 +72,8 @@ def lib():
             "epsp_oracle_bin_coupling": (None, [P(epsp_model), d, d, c_double_p]),
             "epsp_oracle_conductivity": (None, [c_double_p, c_double_p, c_double_p, c_double_p, i64, i64, d, d,
                                                 c_double_p]),
+            "epsp_oracle_attach_greens": (None, [i64, i64, c_double_p, c_double_p, c_double_p, c_double_p]),
+            "epsp_oracle_attach_bare": (None, [i64, i64, c_double_p, c_double_p, c_double_p, c_double_p]),
             "epsp_oracle_ladder_apply": (C.c_int, [P(epsp_model), P(epsp_options), c_double_p, d, d, d, c_double_p,
                                                    c_double_p] + msg),
             "epsp_oracle_ladder_run": (C.c_int, [P(epsp_model), P(epsp_options), c_double_p, c_double_p, c_double_p,
@@ -245,6 +247,27 @@ def conductivity(J, v, w_i, Ww, Omega, T):
     s = np.zeros((3, 3), order="F")
     lib().epsp_oracle_conductivity(cptr(J), ptr(v), ptr(w_i), ptr(Ww), nw, ni, float(Omega), float(T), ptr(s))
     return s
+
+
+def attach_greens(Gm, Gp, X):
+    """attach_greens_to_vertex! (src/ladder_kernel.jl:61-67): J = Gm X Gp per (ω, cart, c0, i);
+    Gm, Gp [nω, 4, ni], X [nω, 4, 3, 2, ni]."""
+    nw, ni = Gm.shape[0], Gm.shape[2]
+    Gm, Gp = as_complex_F(Gm, (nw, 4, ni)), as_complex_F(Gp, (nw, 4, ni))
+    X = as_complex_F(X, (nw, 4, 3, 2, ni))
+    J = np.zeros_like(X)
+    lib().epsp_oracle_attach_greens(nw, ni, cptr(Gm), cptr(Gp), cptr(X), cptr(J))
+    return J
+
+
+def attach_bare(Gm, Gp, v):
+    """attach_greens_to_bare_vertex! (src/ladder_kernel.jl:70-73): J0 for the velocities v [3, ni]."""
+    nw, ni = Gm.shape[0], Gm.shape[2]
+    Gm, Gp = as_complex_F(Gm, (nw, 4, ni)), as_complex_F(Gp, (nw, 4, ni))
+    v = np.asfortranarray(v, dtype=np.float64)
+    J0 = np.zeros((nw, 4, 3, 2, ni), dtype=np.complex128, order="F")
+    lib().epsp_oracle_attach_bare(nw, ni, cptr(Gm), cptr(Gp), ptr(v), cptr(J0))
+    return J0
 
 
 def apply_ladder_kernel(setup, J, sigma_T, mu, T, Omega, *, omega_acoustic, gpu_tile=None):

@@ -74,6 +74,34 @@ def test_trapezoid_weights(oracle):
     assert abs(np.sum(W * ws) - (ws[-1] ** 2 - ws[0] ** 2) / 2) < 1e-14
 
 
+def test_attach_greens_against_2x2_matrices(oracle):
+    # test/test_ladder_bubble.jl:71-98: the pair index (c1, c2) is column-major, so a four-vector
+    # reshaped to 2x2 is the contour matrix and J = Gm X Gp per (ω, cart, c0, i); the bare vertex is
+    # the attachment of V^{c1 c2, c0} = δ_{c1 c2} δ_{c1 c0} v_i.
+    nw, ni = 5, 3
+    Gm = R.pseudorandom_complex(nw, 4, ni, seed=1.1)
+    Gp = R.pseudorandom_complex(nw, 4, ni, seed=2.3)
+    X = R.pseudorandom_complex(nw, 4, 3, 2, ni, seed=3.7)
+    J = oracle.attach_greens(Gm, Gp, X)
+    m2 = lambda a: a.reshape(2, 2, order="F")
+    J_ref = np.zeros((nw, 4, 3, 2, ni), dtype=complex)
+    for i in range(ni):
+        for c0 in range(2):
+            for a in range(3):
+                for w in range(nw):
+                    J_ref[w, :, a, c0, i] = (m2(Gm[w, :, i]) @ m2(X[w, :, a, c0, i]) @ m2(Gp[w, :, i])).reshape(
+                        4, order="F")
+    assert np.linalg.norm(J - J_ref) <= 1e-14 * np.linalg.norm(J_ref)
+    v = R.pseudorandom(3, ni, seed=4.1)
+    V = np.zeros((nw, 4, 3, 2, ni), dtype=complex)
+    for c0 in range(2):
+        V[:, c0 + 2 * c0, :, c0, :] = v[None, :, :]
+    J_V = oracle.attach_greens(Gm, Gp, V)
+    J0 = oracle.attach_bare(Gm, Gp, v)
+    assert np.linalg.norm(J0 - J_V) <= 1e-14 * np.linalg.norm(J0)
+    assert np.linalg.norm(J0) > 0
+
+
 @pytest.mark.parametrize("case_name", ["hcase", "ccase"])
 def test_bubble_identity(oracle, request, case_name):
     # test/test_ladder_bubble.jl:101-122: the bare-vertex contour bubble equals the spectral bubble.
