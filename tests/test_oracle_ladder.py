@@ -203,6 +203,26 @@ def test_apply_ladder_against_naive_loop(oracle, request, case_name, Omega, refi
             assert np.linalg.norm(LJ - ref) <= 1e-12 * np.linalg.norm(ref)
 
 
+def test_apply_unchanged_on_a_finer_shift_table(oracle, ccase):
+    # test/test_ladder_kernel.jl:200-208: the same hat-basis shifts on a table twice as fine; one
+    # application on a vertex that vanishes at the end nodes is unchanged to 1e-12 (a non-zero end
+    # value is spread over one table step beyond the end, so it makes the result depend on the step).
+    c = ccase
+    s = c["setup"]
+    g = s["omegas"]
+    s_half = dict(s, omegas=FrequencyGrid(g.origin, g.unit / 2, np.asarray(g.offsets) * 2))
+    assert np.array_equal(s_half["omegas"].nodes(), g.nodes())
+    nw, ni = len(g), s["eps_i"].size
+    J = R.pseudorandom_complex(nw, 4, 3, 2, ni, seed=0.9)
+    J[0] = 0
+    J[-1] = 0
+    args = (c["sigma"][:, :, 0], c["mu"][0], c["Tlist"][0], 0.123)
+    LJ = oracle.apply_ladder_kernel(s, J, *args, omega_acoustic=W_AC)
+    LJ_half = oracle.apply_ladder_kernel(s_half, J, *args, omega_acoustic=W_AC)
+    assert oracle.nshift(s_half) > oracle.nshift(s)
+    assert np.linalg.norm(LJ_half - LJ) <= 1e-12 * np.linalg.norm(LJ)
+
+
 def test_holstein_current_vertex_correction_vanishes(oracle, hcase):
     # test/test_ladder_holstein.jl:5-26: Σ_f J_f = 0 for J_{-k} = -J_k, so L(J0) = 0 and
     # σ_ladder = σ_bubble; without the sign of the time-reversed partners it does not cancel.

@@ -34,6 +34,11 @@ def test_frequency_grid_structure():
             FrequencyGrid(o, u, [0, 1])
     g = FrequencyGrid.from_nodes(np.concatenate([np.arange(0, 0.5001, 0.05), np.arange(0.52, 0.8001, 0.02)]))
     assert g.unit == pytest.approx(0.01) and g.dw_min == pytest.approx(0.02)
+    # test/test_ladder_kernel.jl:181-186: a 45 meV coarse step with 20 meV cells and a 10 meV
+    # transition at 11.83 eV: the commensurate step is 5 meV, half the minimum step
+    g = FrequencyGrid.from_nodes(11.83 + np.concatenate([np.arange(-1.2, -0.2499, 0.045), np.arange(-0.24, 0.2401, 0.02),
+                                                         np.arange(0.25, 1.2001, 0.045)]))
+    assert g.unit == pytest.approx(5e-3, rel=1e-12) and g.dw_min == pytest.approx(1e-2, rel=1e-12)
     with pytest.raises(ArgumentError, match="not commensurate"):
         FrequencyGrid.from_nodes([0.0, 1.0, 1.0 + math.sqrt(2) / 100])
     for bad in ([0.0, 0.5, 0.5, 1.0], [0.0, 1.0, 0.5], [0.0, 1e-12, 0.5]):
