@@ -129,19 +129,24 @@ constexpr size_t kDeviceGatherMaxBytes = size_t(1) << 30;
 // The address at which kernels read the caller's g2 of `bytes` bytes, or nullptr when it goes
 // through the host gather. Device or managed memory is read in place; page-locked host memory
 // registered with CUDA (epsp_host_register, cudaHostRegister, cudaHostAlloc) through its device
-// alias, up to kDeviceGatherMaxBytes. Pageable memory is not read in place even where the GPU
-// could (cudaDevAttrPageableMemoryAccess on NVLink-C2C nodes): on a GB300 node, set-ups of a
-// 365 MB g2 that the host had worked on meanwhile slowed several times over that way, as when the
-// driver moves the pages the GPU reads.
+// alias, up to kDeviceGatherMaxBytes, when its first and last bytes lie in one contiguous device
+// mapping of the same kind (a g2 registered only in part goes through the host gather). Pageable
+// memory is not read in place even where the GPU could (cudaDevAttrPageableMemoryAccess on
+// NVLink-C2C nodes): on a GB300 node, set-ups of a 365 MB g2 that the host had worked on meanwhile
+// slowed several times over that way, as when the driver moves the pages the GPU reads.
 const void* device_view(Ctx* ctx, const void* h, size_t bytes) {
-  if (ctx->g2_host_gather) return nullptr;
-  cudaPointerAttributes a{};
-  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+  if (ctx->g2_host_gather || bytes == 0) return nullptr;
+  cudaPointerAttributes a{}, z{};
+  const void* last = static_cast<const uint8_t*>(h) + (bytes - 1);
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess || cudaPointerGetAttributes(&z, last) != cudaSuccess) {
     (void)cudaGetLastError();
     return nullptr;
   }
-  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return h;
-  if (a.type == cudaMemoryTypeHost && a.devicePointer && bytes <= kDeviceGatherMaxBytes) return a.devicePointer;
+  if (a.type != z.type || !a.devicePointer ||
+      static_cast<const uint8_t*>(z.devicePointer) != static_cast<const uint8_t*>(a.devicePointer) + (bytes - 1))
+    return nullptr;
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return a.devicePointer;
+  if (a.type == cudaMemoryTypeHost && bytes <= kDeviceGatherMaxBytes) return a.devicePointer;
   return nullptr;
 }
 
