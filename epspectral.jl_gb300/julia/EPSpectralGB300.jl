@@ -18,12 +18,16 @@ const LIB = get(ENV, "EPSPECTRAL_GB300_LIB", joinpath(@__DIR__, "..", "epspectra
 const EPSP_OK, EPSP_EINVAL, EPSP_ENOMEM, EPSP_ENOROOT_MU = 0, 1, 2, 3
 const PATHS = (direct_fp64 = Int32(0), gemm_fp64 = Int32(1), gemm_bf16 = Int32(2), gemm_tf32 = Int32(3))
 
-"""The backend value `run_scgd0(...; backend = GB300Backend())` selects."""
+"""The backend value `run_scgd0(...; backend = GB300Backend())` selects. With `keep_g2`, the
+library keeps on the device the g2 the scGD0 set-up streams, and a ladder set-up of the same array
+reads it there (a driver running `_loop_scgd0` and `_loop_ladder` on one setup; `run_scgd0_ladder`
+extracts a new g2). The copy is freed after the next ladder set-up (epsp_ctx_keep_g2)."""
 Base.@kwdef struct GB300Backend
     device::Int = 0
     path::Symbol = :gemm_bf16
     ladder_path::Union{Nothing, Symbol} = nothing  # the ladder's path when it differs (e.g. :gemm_tf32, ladder only)
     batch_rhs::Union{Nothing, Int} = nothing   # solve up to this many (T, Ω) pairs together (GMRES, :gemm_bf16)
+    keep_g2::Bool = false
 end
 
 struct Grid
@@ -68,11 +72,49 @@ function check(ctx, status)
     error("libepspectral_gb300: status $status: $msg")
 end
 
+# One library context per device for the process (its stream, its page-locked staging and the g2
+# it keeps live across calls), created on first use and destroyed at exit. The library's calls on
+# one context are not concurrent: LOCK serialises the loops.
+const CONTEXTS = Dict{Int, Ptr{Cvoid}}()
+const LOCK = ReentrantLock()
+
+function __init__()
+    atexit() do
+        for ctx in values(CONTEXTS)
+            ccall((:epsp_destroy, LIB), Cvoid, (Ptr{Cvoid},), ctx)
+        end
+        empty!(CONTEXTS)
+    end
+end
+
 function context(backend::GB300Backend)
-    ref = Ref{Ptr{Cvoid}}(C_NULL)
-    st = ccall((:epsp_create, LIB), Cint, (Ref{Ptr{Cvoid}}, Int32), ref, backend.device)
-    st == EPSP_OK || error("epsp_create failed with status $st")
-    ref[]
+    get!(CONTEXTS, backend.device) do
+        ref = Ref{Ptr{Cvoid}}(C_NULL)
+        st = ccall((:epsp_create, LIB), Cint, (Ref{Ptr{Cvoid}}, Int32), ref, backend.device)
+        st == EPSP_OK || error("epsp_create failed with status $st")
+        ref[]
+    end
+end
+
+"""
+    host_register(backend, A) / host_unregister(backend, A)
+
+Page-lock the memory of the dense array `A` for the library (epsp_host_register): plan set-ups
+then read a g2 of at most 1 GiB there in place. `CUDA.pin(A)` does the same. Unregister before
+`A` is freed.
+"""
+function host_register(backend::GB300Backend, A::Array)
+    lock(LOCK) do
+        ctx = context(backend)
+        check(ctx, ccall((:epsp_host_register, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, UInt64), ctx, pointer(A),
+            sizeof(A)))
+    end
+end
+function host_unregister(backend::GB300Backend, A::Array)
+    lock(LOCK) do
+        ctx = context(backend)
+        check(ctx, ccall((:epsp_host_unregister, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), ctx, pointer(A)))
+    end
 end
 
 dtype_tag(::Type{Float64}) = Int32(0)
@@ -82,9 +124,12 @@ dtype_tag(::Type{Float32}) = Int32(1)
 function model_arrays(setup, R, v)
     (; g2, ωph, iq_kk, iks_i, iks_f, ε_i, w_i, ε_f, w_f, f_to_i, W, nstates_base, multiplets, ωs, ωs_spectral) = setup
     zb(x) = Int32.(Array(x) .- 1)   # 1-based Julia indices -> 0-based Int32
+    # g2 is passed as the caller's own array when it is dense, so that its address is the same in
+    # both set-ups of a run (the kept copy) and a pinned g2 is the memory the library reads
+    g2 = g2 isa Array ? g2 : Array(g2)
     mult_ptr = Int32[0; cumsum(length.(multiplets))]
     mult_idx = isempty(multiplets) ? Int32[0] : Int32.(reduce(vcat, multiplets) .- 1)
-    (; g2 = Array(g2), ωph = Array(ωph), iq_kk = zb(iq_kk), iks_i = zb(iks_i), iks_f = zb(iks_f),
+    (; g2, ωph = Array(ωph), iq_kk = zb(iq_kk), iks_i = zb(iks_i), iks_f = zb(iks_f),
        ε_i = Array(ε_i), w_i = Array(w_i), ε_f = Array(ε_f), w_f = Array(w_f), f_to_i = zb(f_to_i),
        W, nstates_base, mult_ptr, mult_idx, offsets = collect(Int64, ωs.offsets), ωs,
        offsets_sp = collect(Int64, ωs_spectral.offsets), ωs_spectral,
@@ -112,8 +157,8 @@ same arguments and the same return value `(; Σ, μ, converged, history)`.
 """
 function loop_scgd0(setup, occ; η_min, η_init, maxiter, tol, backend::GB300Backend, gpu_tile, Σ_init, fix_μ,
         ω_acoustic, verbosity)
-    ctx = context(backend)
-    try
+    lock(LOCK) do
+        ctx = context(backend)
         a = model_arrays(setup, nothing, nothing)
         nω, ni, nT = length(setup.ωs), size(setup.g2, 2), length(occ.Tlist)
         Tlist, nlist = collect(Float64, occ.Tlist), collect(Float64, occ.nlist)
@@ -128,6 +173,7 @@ function loop_scgd0(setup, occ; η_min, η_init, maxiter, tol, backend::GB300Bac
             m = Ref(model_struct(a))
             opts = Ref(Options(getfield(PATHS, backend.path), verbosity, gpu_tile === nothing ? 0 : gpu_tile, ω_acoustic))
             plan = Ref{Ptr{Cvoid}}(C_NULL)
+            backend.keep_g2 && check(ctx, ccall((:epsp_ctx_keep_g2, LIB), Cint, (Ptr{Cvoid}, Int32), ctx, 1))
             check(ctx, ccall((:epsp_scgd0_setup, LIB), Cint, (Ptr{Cvoid}, Ref{Model}, Ref{Options}, Ref{Ptr{Cvoid}}),
                 ctx, m, opts, plan))
             try
@@ -148,8 +194,6 @@ function loop_scgd0(setup, occ; η_min, η_init, maxiter, tol, backend::GB300Bac
                 ccall((:epsp_scgd0_plan_destroy, LIB), Cvoid, (Ptr{Cvoid},), plan[])
             end
         end
-    finally
-        ccall((:epsp_destroy, LIB), Cvoid, (Ptr{Cvoid},), ctx)
     end
 end
 
@@ -162,8 +206,8 @@ the output of `_setup_ladder`, whose rotations `R` and velocities `v` are passed
 """
 function loop_ladder(ladder, Σ, μ, Tlist, Ωs; solver, rtol, maxiter, store_vertex, backend::GB300Backend,
         gpu_tile, ω_acoustic, verbosity)
-    ctx = context(backend)
-    try
+    lock(LOCK) do
+        ctx = context(backend)
         a = model_arrays(ladder, Array(ladder.R), Array(ladder.v))
         nω, ni = length(ladder.ωs), size(ladder.g2, 2)
         nT, nΩ = length(Tlist), length(Ωs)
@@ -177,8 +221,12 @@ function loop_ladder(ladder, Σ, μ, Tlist, Ωs; solver, rtol, maxiter, store_ve
             lpath = backend.ladder_path === nothing ? backend.path : backend.ladder_path
             opts = Ref(Options(getfield(PATHS, lpath), verbosity, gpu_tile === nothing ? 0 : gpu_tile, ω_acoustic))
             plan = Ref{Ptr{Cvoid}}(C_NULL)
-            check(ctx, ccall((:epsp_ladder_setup, LIB), Cint, (Ptr{Cvoid}, Ref{Model}, Ref{Options}, Ref{Ptr{Cvoid}}),
-                ctx, m, opts, plan))
+            try
+                check(ctx, ccall((:epsp_ladder_setup, LIB), Cint,
+                    (Ptr{Cvoid}, Ref{Model}, Ref{Options}, Ref{Ptr{Cvoid}}), ctx, m, opts, plan))
+            finally  # the ladder's set-up was the kept g2's last reader
+                backend.keep_g2 && ccall((:epsp_ctx_keep_g2, LIB), Cint, (Ptr{Cvoid}, Int32), ctx, 0)
+            end
             try
                 Jp = J === nothing ? Ptr{ComplexF64}(C_NULL) : pointer(J)
                 if backend.batch_rhs !== nothing && solver === :gmres
@@ -203,8 +251,6 @@ function loop_ladder(ladder, Σ, μ, Tlist, Ωs; solver, rtol, maxiter, store_ve
         all(converged) || @warn "ladder not converged (rtol = $rtol, maxiter = $maxiter)"
         history = fill((; norms = Float64[], σ_iter = Matrix{Float64}[]), nΩ, nT)
         return (; σ_bubble = σb, σ_ladder = σl, converged, niter = Int.(niter), history, J)
-    finally
-        ccall((:epsp_destroy, LIB), Cvoid, (Ptr{Cvoid},), ctx)
     end
 end
 
