@@ -60,6 +60,20 @@ def test_plan_queries_and_tile_setters_refuse_null_plans(library):
     assert library.epsp_ladder_set_gemm_config(None, i32(256), i32(1), i32(32)) == EINVAL
 
 
+def test_context_utilities_refuse_null_contexts(library):
+    """The host-registration, kept-g2 and test-hook entry points check the context first (no GPU)."""
+    EINVAL = 1
+    vp, i32, u32, u64 = C.c_void_p, C.c_int32, C.c_uint32, C.c_uint64
+    buf = C.create_string_buffer(64)
+    library.epsp_host_register.argtypes = [vp, vp, u64]
+    library.epsp_host_unregister.argtypes = [vp, vp]
+    assert library.epsp_host_register(None, C.cast(buf, vp), u64(64)) == EINVAL
+    assert library.epsp_host_unregister(None, C.cast(buf, vp)) == EINVAL
+    assert library.epsp_ctx_keep_g2(None, i32(1)) == EINVAL
+    assert library.epsp_test_g2_host_gather(None, i32(1)) == EINVAL
+    assert library.epsp_test_gemm_stall(None, i32(0), u32(64)) == EINVAL
+
+
 def test_header_declares_the_tensor_core_paths():
     text = open(HEADER).read()
     for name, value in (("EPSP_PATH_GEMM_BF16", 2), ("EPSP_PATH_GEMM_TF32", 3)):
